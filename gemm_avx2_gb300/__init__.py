@@ -1,0 +1,244 @@
+"""GB300 (sm_103a) drop-in for the sgemm_/dgemm_ path of wjc404/GEMM_AVX2.
+
+The product is native code in this directory:
+
+* ``DGEMM.so`` / ``SGEMM.so`` export exactly ``dgemm_`` / ``sgemm_`` with the
+  reference's Fortran-style ABI (reference ``src/gemm_driver.c:118``).
+* ``libgemm_gb300.so`` holds every CUDA kernel and the ``gb300_*`` C ABI
+  declared in ``include/gemm_gb300.h`` (device pointers, streams, split forms).
+
+This module is a thin ctypes mirror of that ABI so that tests and the
+benchmark call the library exactly as a C or Fortran caller would:
+
+* ``dgemm`` / ``sgemm`` mirror the reference interface argument for argument
+  (host arrays, column-major, ``lda``/``ldb``/``ldc``) and go through the
+  drop-in ``DGEMM.so``/``SGEMM.so``.
+* ``gemm_device`` and friends take device pointers (integers, e.g. from
+  ``torch.Tensor.data_ptr()``) and a stream handle.
+
+There is no CPU fallback: if the native library is missing, loading fails
+with an error.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import c_char, c_double, c_float, c_int, c_size_t, c_uint, c_void_p
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+
+OK = 0
+ERR_ARG = 1
+ERR_CUDA = 2
+ERR_TIMEOUT = 3
+ERR_NOMEM = 4
+ERR_UNSUPPORTED = 5
+ERR_WORKSPACE = 6
+
+_core = None
+_drop = {}
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+def build() -> None:
+    """Compile the native library in place (nvcc, sm_103a)."""
+    from . import native_build
+
+    native_build.build()
+
+
+def _load(name: str) -> ctypes.CDLL:
+    path = os.path.join(PKG, name)
+    if not os.path.exists(path):
+        raise NativeLibraryMissing(
+            "%s not built: run gemm_avx2_gb300.build() (or __graft_entry__.build())" % path)
+    return ctypes.CDLL(path, mode=ctypes.RTLD_GLOBAL)
+
+
+def core() -> ctypes.CDLL:
+    """libgemm_gb300.so with argument types declared."""
+    global _core
+    if _core is None:
+        L = _load("libgemm_gb300.so")
+        g = [c_char, c_char, c_int, c_int, c_int]
+        L.gb300_dgemm.argtypes = g + [c_double, c_void_p, c_int, c_void_p, c_int, c_double,
+                                      c_void_p, c_int, c_void_p]
+        L.gb300_sgemm.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int, c_float,
+                                      c_void_p, c_int, c_void_p]
+        L.gb300_host_dgemm.argtypes = g + [c_double, c_void_p, c_int, c_void_p, c_int, c_double,
+                                           c_void_p, c_int]
+        L.gb300_host_sgemm.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int, c_float,
+                                           c_void_p, c_int]
+        L.gb300_sgemm_bf16x.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int, c_float,
+                                            c_void_p, c_int, c_int, c_void_p]
+        L.gb300_sgemm_bf16x_ws.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int,
+                                               c_float, c_void_p, c_int, c_int, c_void_p,
+                                               c_size_t, c_void_p]
+        L.gb300_dgemm_ozaki.argtypes = g + [c_double, c_void_p, c_int, c_void_p, c_int,
+                                            c_double, c_void_p, c_int, c_int, c_void_p]
+        L.gb300_dgemm_ozaki_ws.argtypes = g + [c_double, c_void_p, c_int, c_void_p, c_int,
+                                               c_double, c_void_p, c_int, c_int, c_void_p,
+                                               c_size_t, c_void_p]
+        L.gb300_sgemm_bf16x_prepare.argtypes = g + [c_void_p, c_int, c_void_p, c_int, c_int,
+                                                    c_void_p, c_size_t, c_void_p]
+        L.gb300_sgemm_bf16x_run.argtypes = [c_int, c_int, c_int, c_float, c_float, c_void_p,
+                                            c_int, c_int, c_void_p, c_size_t, c_void_p]
+        L.gb300_dgemm_ozaki_prepare.argtypes = g + [c_void_p, c_int, c_void_p, c_int, c_int,
+                                                    c_void_p, c_size_t, c_void_p]
+        L.gb300_dgemm_ozaki_run.argtypes = [c_int, c_int, c_int, c_double, c_double, c_void_p,
+                                            c_int, c_int, c_void_p, c_size_t, c_void_p]
+        L.gb300_host_sgemm_bf16x.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int,
+                                                 c_float, c_void_p, c_int, c_int]
+        L.gb300_host_dgemm_ozaki.argtypes = g + [c_double, c_void_p, c_int, c_void_p, c_int,
+                                                 c_double, c_void_p, c_int, c_int]
+        L.gb300_split_workspace_bytes.argtypes = [c_int, c_int, c_int, c_int, c_int]
+        L.gb300_split_workspace_bytes.restype = c_size_t
+        L.gb300_device_error.argtypes = [c_int]
+        L.gb300_device_error.restype = c_uint
+        L.gb300_version.restype = ctypes.c_char_p
+        _core = L
+    return _core
+
+
+def dropin(precision: str) -> ctypes.CDLL:
+    """The drop-in library: 'd' -> DGEMM.so, 's' -> SGEMM.so."""
+    if precision not in _drop:
+        core()  # resolve libgemm_gb300.so first (RTLD_GLOBAL)
+        _drop[precision] = _load("DGEMM.so" if precision == "d" else "SGEMM.so")
+    return _drop[precision]
+
+
+def _b(c) -> bytes:
+    return c.encode() if isinstance(c, str) else bytes(c)
+
+
+def _ptr(x):
+    """Address of a numpy array, torch tensor or raw integer pointer."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return c_void_p(x)
+    if hasattr(x, "data_ptr"):
+        return c_void_p(x.data_ptr())
+    return c_void_p(x.ctypes.data)
+
+
+# ---------------------------------------------------------------------------
+# Reference interface mirror (host arrays, drop-in libraries)
+# ---------------------------------------------------------------------------
+def dgemm(transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc) -> None:
+    """dgemm_ of DGEMM.so: C = alpha*op(A)*op(B) + beta*C on host column-major arrays.
+
+    Same argument meaning as the reference (``src/gemm_driver.c:118``); returns
+    nothing; invalid arguments leave ``c`` untouched.
+    """
+    L = dropin("d")
+    i = lambda v: ctypes.byref(c_int(int(v)))
+    L.dgemm_(ctypes.c_char_p(_b(transa)), ctypes.c_char_p(_b(transb)), i(m), i(n), i(k),
+             ctypes.byref(c_double(alpha)), _ptr(a), i(lda), _ptr(b), i(ldb),
+             ctypes.byref(c_double(beta)), _ptr(c), i(ldc))
+
+
+def sgemm(transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc) -> None:
+    """sgemm_ of SGEMM.so (FP32), same contract as :func:`dgemm`."""
+    L = dropin("s")
+    i = lambda v: ctypes.byref(c_int(int(v)))
+    L.sgemm_(ctypes.c_char_p(_b(transa)), ctypes.c_char_p(_b(transb)), i(m), i(n), i(k),
+             ctypes.byref(c_float(alpha)), _ptr(a), i(lda), _ptr(b), i(ldb),
+             ctypes.byref(c_float(beta)), _ptr(c), i(ldc))
+
+
+def host_gemm(precision, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc) -> int:
+    """Host-pointer path with a status code (gb300_host_dgemm / gb300_host_sgemm)."""
+    L = core()
+    f = L.gb300_host_dgemm if precision == "d" else L.gb300_host_sgemm
+    return f(_b(transa), _b(transb), m, n, k, alpha, _ptr(a), lda, _ptr(b), ldb, beta, _ptr(c),
+             ldc)
+
+
+# ---------------------------------------------------------------------------
+# Device-pointer entry points
+# ---------------------------------------------------------------------------
+def gemm_device(precision, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                stream=0) -> int:
+    """gb300_dgemm / gb300_sgemm on device buffers; stream-ordered, returns a status."""
+    L = core()
+    f = L.gb300_dgemm if precision == "d" else L.gb300_sgemm
+    return f(_b(transa), _b(transb), m, n, k, alpha, _ptr(A), lda, _ptr(B), ldb, beta, _ptr(C),
+             ldc, c_void_p(stream))
+
+
+def sgemm_bf16x(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, products=3,
+                stream=0, workspace=None, workspace_bytes=0) -> int:
+    """Split-precision SGEMM (3xBF16 / 6xBF16) on the tensor cores."""
+    L = core()
+    if workspace is None:
+        return L.gb300_sgemm_bf16x(_b(transa), _b(transb), m, n, k, alpha, _ptr(A), lda,
+                                   _ptr(B), ldb, beta, _ptr(C), ldc, products, c_void_p(stream))
+    return L.gb300_sgemm_bf16x_ws(_b(transa), _b(transb), m, n, k, alpha, _ptr(A), lda, _ptr(B),
+                                  ldb, beta, _ptr(C), ldc, products, _ptr(workspace),
+                                  workspace_bytes, c_void_p(stream))
+
+
+def dgemm_ozaki(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices=0,
+                stream=0, workspace=None, workspace_bytes=0) -> int:
+    """Ozaki-scheme DGEMM (int8-range slices, exact products) on the tensor cores."""
+    L = core()
+    if workspace is None:
+        return L.gb300_dgemm_ozaki(_b(transa), _b(transb), m, n, k, alpha, _ptr(A), lda,
+                                   _ptr(B), ldb, beta, _ptr(C), ldc, slices, c_void_p(stream))
+    return L.gb300_dgemm_ozaki_ws(_b(transa), _b(transb), m, n, k, alpha, _ptr(A), lda, _ptr(B),
+                                  ldb, beta, _ptr(C), ldc, slices, _ptr(workspace),
+                                  workspace_bytes, c_void_p(stream))
+
+
+def split_prepare(form, transa, transb, m, n, k, A, lda, B, ldb, param, workspace,
+                  workspace_bytes, stream=0) -> int:
+    """Phase 1 of a split form ('bf16x' or 'ozaki'): split op(A), op(B) into the workspace."""
+    L = core()
+    f = L.gb300_sgemm_bf16x_prepare if form == "bf16x" else L.gb300_dgemm_ozaki_prepare
+    return f(_b(transa), _b(transb), m, n, k, _ptr(A), lda, _ptr(B), ldb, param, _ptr(workspace),
+             workspace_bytes, c_void_p(stream))
+
+
+def split_run(form, m, n, k, alpha, beta, C, ldc, param, workspace, workspace_bytes,
+              stream=0) -> int:
+    """Phase 2 of a split form: the tensor-core GEMM from a prepared workspace."""
+    L = core()
+    f = L.gb300_sgemm_bf16x_run if form == "bf16x" else L.gb300_dgemm_ozaki_run
+    return f(m, n, k, alpha, beta, _ptr(C), ldc, param, _ptr(workspace), workspace_bytes,
+             c_void_p(stream))
+
+
+def host_split_gemm(form, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
+                    param) -> int:
+    """Host-pointer split forms (synchronous, staged through HBM)."""
+    L = core()
+    f = L.gb300_host_sgemm_bf16x if form == "bf16x" else L.gb300_host_dgemm_ozaki
+    return f(_b(transa), _b(transb), m, n, k, alpha, _ptr(a), lda, _ptr(b), ldb, beta, _ptr(c),
+             ldc, param)
+
+
+def split_workspace_bytes(kind: int, m: int, n: int, k: int, param: int) -> int:
+    return core().gb300_split_workspace_bytes(kind, m, n, k, param)
+
+
+def device_error(clear: bool = False) -> int:
+    return core().gb300_device_error(1 if clear else 0)
+
+
+def version() -> str:
+    return core().gb300_version().decode()
+
+
+# Symbols every library must export (checked by the CPU tests).
+CORE_SYMBOLS = [
+    "gb300_host_dgemm", "gb300_host_sgemm", "gb300_dgemm", "gb300_sgemm", "gb300_sgemm_bf16x",
+    "gb300_sgemm_bf16x_ws", "gb300_dgemm_ozaki", "gb300_dgemm_ozaki_ws",
+    "gb300_split_workspace_bytes", "gb300_device_error", "gb300_version",
+    "gb300_sgemm_bf16x_prepare", "gb300_sgemm_bf16x_run", "gb300_dgemm_ozaki_prepare",
+    "gb300_dgemm_ozaki_run", "gb300_host_sgemm_bf16x", "gb300_host_dgemm_ozaki",
+]

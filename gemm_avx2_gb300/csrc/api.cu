@@ -1,0 +1,356 @@
+// api.cu -- the C ABI of libgemm_gb300.so: device-pointer entry points,
+// host-pointer (drop-in) staging, tensor-map encoding, device error words and
+// the cached split-form workspace.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+#include <utility>
+
+#include "plain_gemm.h"
+#include "split_gemm.h"
+
+#define GB300_API extern "C" __attribute__((visibility("default")))
+
+namespace gb300 {
+
+// ---------------------------------------------------------------- tensor maps
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn get_encode() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+bool encode_2d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t rows, int64_t cols,
+               int64_t ld, int box_rows, int box_cols, bool swizzle128) {
+  EncodeTiledFn fn = get_encode();
+  if (!fn || rows <= 0 || cols <= 0) return false;
+  CUtensorMapDataType dt = elem_bytes == 8   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                           : elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                             : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  cuuint64_t dims[2] = {(cuuint64_t)rows, (cuuint64_t)cols};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * (int64_t)elem_bytes)};
+  cuuint32_t box[2] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, dt, 2, const_cast<void *>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// ---------------------------------------------------------------- per-device state
+struct DeviceState {
+  unsigned *err = nullptr;  // device error word
+  // cached workspaces of the split forms, one per stream (grow-only): calls on
+  // one stream are ordered, calls on different streams never share scratch
+  std::unordered_map<cudaStream_t, std::pair<void *, size_t>> ws;
+  // staging buffers of the host-pointer (drop-in) path
+  void *stage[3] = {nullptr, nullptr, nullptr};
+  size_t stage_bytes[3] = {0, 0, 0};
+  cudaStream_t stage_stream = nullptr;
+  std::mutex mu;  // guards ws and staging (one host-pointer call at a time per device)
+};
+static constexpr int kMaxDevices = 64;
+static DeviceState g_dev[kMaxDevices];
+static std::mutex g_init_mu;
+
+static DeviceState *dev_state() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) return nullptr;
+  DeviceState &s = g_dev[d];
+  if (!s.err) {
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (!s.err) {
+      unsigned *p = nullptr;
+      if (cudaMalloc(&p, sizeof(unsigned)) != cudaSuccess) return nullptr;
+      if (cudaMemset(p, 0, sizeof(unsigned)) != cudaSuccess) return nullptr;
+      s.err = p;
+    }
+  }
+  return &s;
+}
+
+unsigned *device_error_word() {
+  DeviceState *s = dev_state();
+  return s ? s->err : nullptr;
+}
+
+static bool grow(void **p, size_t *have, size_t need) {
+  if (*have >= need) return true;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  size_t sz = need + need / 8 + 256;
+  if (cudaMalloc(p, sz) != cudaSuccess) {
+    *p = nullptr;
+    return false;
+  }
+  *have = sz;
+  return true;
+}
+
+// Library-owned workspace for the split forms on `st` (caller holds s->mu).
+void *cached_workspace(DeviceState *s, cudaStream_t st, size_t need) {
+  auto &e = s->ws[st];
+  if (e.second < need) {
+    // the stream may still be using the old buffer
+    if (e.first && cudaStreamSynchronize(st) != cudaSuccess) return nullptr;
+  }
+  if (!grow(&e.first, &e.second, need)) return nullptr;
+  return e.first;
+}
+
+// ---------------------------------------------------------------- host-pointer staging
+// form: 0 = plain kernel; 1 = BF16xP split (FP32, param = products);
+//       2 = Ozaki (FP64, param = slices).
+template <typename T>
+static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a, int lda,
+                     const T *b, int ldb, T beta, T *c, int ldc, int form = 0, int param = 0) {
+  const bool an = notrans(ta), bn = notrans(tb);
+  const int arows = an ? m : k, acols = an ? k : m;
+  const int brows = bn ? k : n, bcols = bn ? n : k;
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  if (alpha == T(0) && beta == T(1)) return GB300_OK;
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (!s->stage_stream &&
+      cudaStreamCreateWithFlags(&s->stage_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  cudaStream_t st = s->stage_stream;
+  const bool need_ab = alpha != T(0) && k > 0;
+  // Device copies use leading dimensions rounded up to 16 bytes so that the
+  // TMA path applies whatever the host ld was.
+  const int epl = 16 / (int)sizeof(T);
+  auto up = [&](int r) { return ((r > 1 ? r : 1) + epl - 1) / epl * epl; };
+  const int dla = up(arows), dlb = up(brows), dlc = up(m);
+  const size_t bytesA = need_ab ? (size_t)dla * acols * sizeof(T) : 0;
+  const size_t bytesB = need_ab ? (size_t)dlb * bcols * sizeof(T) : 0;
+  const size_t bytesC = (size_t)dlc * n * sizeof(T);
+  if (!grow(&s->stage[0], &s->stage_bytes[0], bytesA + 16) ||
+      !grow(&s->stage[1], &s->stage_bytes[1], bytesB + 16) ||
+      !grow(&s->stage[2], &s->stage_bytes[2], bytesC + 16))
+    return GB300_ERR_NOMEM;
+  T *dA = static_cast<T *>(s->stage[0]), *dB = static_cast<T *>(s->stage[1]);
+  T *dC = static_cast<T *>(s->stage[2]);
+  cudaError_t e = cudaSuccess;
+  if (need_ab) {
+    e = cudaMemcpy2DAsync(dA, dla * sizeof(T), a, (size_t)lda * sizeof(T), arows * sizeof(T),
+                          acols, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(dB, dlb * sizeof(T), b, (size_t)ldb * sizeof(T), brows * sizeof(T),
+                            bcols, cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dC, dlc * sizeof(T), c, (size_t)ldc * sizeof(T), m * sizeof(T), n,
+                          cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return GB300_ERR_CUDA;
+  int rc;
+  const int dlda = need_ab ? dla : up(arows), dldb = need_ab ? dlb : up(brows);
+  if (form != 0 && need_ab) {
+    const size_t wneed = split_workspace_bytes(form == 1 ? 0 : 1, m, n, k, param);
+    void *ws = wneed ? cached_workspace(s, st, wneed) : nullptr;
+    if (!ws) return GB300_ERR_NOMEM;
+    if constexpr (sizeof(T) == 8)
+      rc = ozaki_dgemm(ta, tb, m, n, k, alpha, dA, dlda, dB, dldb, beta, dC, dlc, param, ws,
+                       wneed, st, s->err);
+    else
+      rc = split_sgemm(ta, tb, m, n, k, alpha, dA, dlda, dB, dldb, beta, dC, dlc, param, ws,
+                       wneed, st, s->err);
+  } else if constexpr (sizeof(T) == 8) {
+    rc = plain_dgemm(ta, tb, m, n, k, alpha, need_ab ? dA : nullptr, dlda,
+                     need_ab ? dB : nullptr, dldb, beta, dC, dlc, st, s->err);
+  } else {
+    rc = plain_sgemm(ta, tb, m, n, k, alpha, need_ab ? dA : nullptr, dlda,
+                     need_ab ? dB : nullptr, dldb, beta, dC, dlc, st, s->err);
+  }
+  if (rc != GB300_OK) {
+    cudaStreamSynchronize(st);
+    return rc;
+  }
+  e = cudaMemcpy2DAsync(c, (size_t)ldc * sizeof(T), dC, dlc * sizeof(T), m * sizeof(T), n,
+                        cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return GB300_ERR_CUDA;
+  unsigned word = 0;
+  cudaMemcpy(&word, s->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  return word ? GB300_ERR_TIMEOUT : GB300_OK;
+}
+
+}  // namespace gb300
+
+using namespace gb300;
+
+// ---------------------------------------------------------------- exported C ABI
+GB300_API int gb300_host_dgemm(char ta, char tb, int m, int n, int k, double alpha,
+                               const double *a, int lda, const double *b, int ldb, double beta,
+                               double *c, int ldc) {
+  return host_gemm<double>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc);
+}
+GB300_API int gb300_host_sgemm(char ta, char tb, int m, int n, int k, float alpha,
+                               const float *a, int lda, const float *b, int ldb, float beta,
+                               float *c, int ldc) {
+  return host_gemm<float>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc);
+}
+
+GB300_API int gb300_host_sgemm_bf16x(char ta, char tb, int m, int n, int k, float alpha,
+                                     const float *a, int lda, const float *b, int ldb, float beta,
+                                     float *c, int ldc, int products) {
+  if (products != 3 && products != 6) return GB300_ERR_ARG;
+  return host_gemm<float>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, 1, products);
+}
+GB300_API int gb300_host_dgemm_ozaki(char ta, char tb, int m, int n, int k, double alpha,
+                                     const double *a, int lda, const double *b, int ldb,
+                                     double beta, double *c, int ldc, int slices) {
+  if (slices != 0 && (slices < 2 || slices > kOzakiMaxSlices)) return GB300_ERR_ARG;
+  return host_gemm<double>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, 2,
+                           slices > 0 ? slices : ozaki_default_slices(m, n, k));
+}
+
+GB300_API int gb300_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A,
+                          int lda, const double *B, int ldb, double beta, double *C, int ldc,
+                          void *stream) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  unsigned *err = device_error_word();
+  if (!err) return GB300_ERR_CUDA;
+  return plain_dgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                     static_cast<cudaStream_t>(stream), err);
+}
+GB300_API int gb300_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A,
+                          int lda, const float *B, int ldb, float beta, float *C, int ldc,
+                          void *stream) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  unsigned *err = device_error_word();
+  if (!err) return GB300_ERR_CUDA;
+  return plain_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                     static_cast<cudaStream_t>(stream), err);
+}
+
+GB300_API size_t gb300_split_workspace_bytes(int kind, int m, int n, int k, int param) {
+  return split_workspace_bytes(kind, m, n, k, param);
+}
+
+GB300_API int gb300_sgemm_bf16x_ws(char ta, char tb, int m, int n, int k, float alpha,
+                                   const float *A, int lda, const float *B, int ldb, float beta,
+                                   float *C, int ldc, int products, void *ws, size_t ws_bytes,
+                                   void *stream) {
+  if (products != 3 && products != 6) return GB300_ERR_ARG;
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  unsigned *err = device_error_word();
+  if (!err) return GB300_ERR_CUDA;
+  return split_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, products, ws, ws_bytes,
+                     static_cast<cudaStream_t>(stream), err);
+}
+GB300_API int gb300_sgemm_bf16x(char ta, char tb, int m, int n, int k, float alpha,
+                                const float *A, int lda, const float *B, int ldb, float beta,
+                                float *C, int ldc, int products, void *stream) {
+  if (products != 3 && products != 6) return GB300_ERR_ARG;
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  const size_t need = split_workspace_bytes(0, m, n, k, products);
+  std::lock_guard<std::mutex> lk(s->mu);
+  void *ws = need ? cached_workspace(s, static_cast<cudaStream_t>(stream), need) : nullptr;
+  if (need && !ws) return GB300_ERR_NOMEM;
+  return split_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, products, ws, need,
+                     static_cast<cudaStream_t>(stream), s->err);
+}
+
+GB300_API int gb300_dgemm_ozaki_ws(char ta, char tb, int m, int n, int k, double alpha,
+                                   const double *A, int lda, const double *B, int ldb,
+                                   double beta, double *C, int ldc, int slices, void *ws,
+                                   size_t ws_bytes, void *stream) {
+  if (slices != 0 && (slices < 2 || slices > kOzakiMaxSlices)) return GB300_ERR_ARG;
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  unsigned *err = device_error_word();
+  if (!err) return GB300_ERR_CUDA;
+  return ozaki_dgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, ws, ws_bytes,
+                     static_cast<cudaStream_t>(stream), err);
+}
+GB300_API int gb300_dgemm_ozaki(char ta, char tb, int m, int n, int k, double alpha,
+                                const double *A, int lda, const double *B, int ldb, double beta,
+                                double *C, int ldc, int slices, void *stream) {
+  if (slices != 0 && (slices < 2 || slices > kOzakiMaxSlices)) return GB300_ERR_ARG;
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  const size_t need = split_workspace_bytes(1, m, n, k, slices);
+  std::lock_guard<std::mutex> lk(s->mu);
+  void *ws = need ? cached_workspace(s, static_cast<cudaStream_t>(stream), need) : nullptr;
+  if (need && !ws) return GB300_ERR_NOMEM;
+  return ozaki_dgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, ws, need,
+                     static_cast<cudaStream_t>(stream), s->err);
+}
+
+GB300_API int gb300_sgemm_bf16x_prepare(char ta, char tb, int m, int n, int k, const float *A,
+                                        int lda, const float *B, int ldb, int products, void *ws,
+                                        size_t ws_bytes, void *stream) {
+  return split_sgemm_prepare(ta, tb, m, n, k, A, lda, B, ldb, products, ws, ws_bytes,
+                             static_cast<cudaStream_t>(stream));
+}
+GB300_API int gb300_sgemm_bf16x_run(int m, int n, int k, float alpha, float beta, float *C,
+                                    int ldc, int products, const void *ws, size_t ws_bytes,
+                                    void *stream) {
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || (products != 3 && products != 6))
+    return GB300_ERR_ARG;
+  if (m == 0 || n == 0) return GB300_OK;
+  unsigned *err = device_error_word();
+  if (!err) return GB300_ERR_CUDA;
+  return split_sgemm_run(m, n, k, alpha, beta, C, ldc, products, ws, ws_bytes,
+                         static_cast<cudaStream_t>(stream), err);
+}
+GB300_API int gb300_dgemm_ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A,
+                                        int lda, const double *B, int ldb, int slices, void *ws,
+                                        size_t ws_bytes, void *stream) {
+  return ozaki_prepare(ta, tb, m, n, k, A, lda, B, ldb, slices, ws, ws_bytes,
+                       static_cast<cudaStream_t>(stream));
+}
+GB300_API int gb300_dgemm_ozaki_run(int m, int n, int k, double alpha, double beta, double *C,
+                                    int ldc, int slices, const void *ws, size_t ws_bytes,
+                                    void *stream) {
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) ||
+      (slices != 0 && (slices < 2 || slices > kOzakiMaxSlices)))
+    return GB300_ERR_ARG;
+  if (m == 0 || n == 0) return GB300_OK;
+  unsigned *err = device_error_word();
+  if (!err) return GB300_ERR_CUDA;
+  return ozaki_run(m, n, k, alpha, beta, C, ldc, slices, ws, ws_bytes,
+                   static_cast<cudaStream_t>(stream), err);
+}
+
+GB300_API unsigned gb300_device_error(int clear) {
+  unsigned *err = device_error_word();
+  if (!err) return 0xFFFFFFFFu;
+  unsigned w = 0;
+  if (cudaMemcpy(&w, err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return 0xFFFFFFFFu;
+  if (clear) cudaMemset(err, 0, sizeof(unsigned));
+  return w;
+}
+
+GB300_API const char *gb300_version(void) { return "gemm_gb300 0.1 (sm_103a)"; }

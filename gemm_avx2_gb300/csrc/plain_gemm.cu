@@ -1,0 +1,469 @@
+// plain_gemm.cu -- the drop-in ("plain") forms of the reference's sgemm_/dgemm_:
+//   C = alpha*op(A)*op(B) + beta*C, column-major, any m/n/k/ld, op = N or T.
+//
+// Reference path replaced (wjc404/GEMM_AVX2):
+//   driver blocking loop        src/gemm_driver.c:118-197  -> tile grid + grouped raster
+//   A/B panel packing           src/gemm_copy.c:1-143      -> TMA boxes into shared memory
+//                                                             (transposes = box orientation)
+//   FMA3 register micro-kernel  src/kernel/gemm_kernel.S   -> register-blocked FFMA (FP32) /
+//                                                             DMMA m16n8k8 (FP64) consumers
+//   ragged-edge kernels         src/edge_kernel/*          -> TMA out-of-bounds zero fill +
+//                                                             predicated epilogue stores
+//   C_MULT_BETA + alpha-in-B    src/gemm_driver.c:106-116, src/gemm_copy.c:65
+//                                                          -> fused alpha/beta epilogue
+//   OpenMP N split + spin barrier src/gemm_driver.c:23-33,138 -> CTA grid; mbarrier pipeline
+//
+// Kernel shape (both precisions): 128x128 CTA tile, a 4-stage shared-memory ring
+// filled by one producer warp (TMA 2-D boxes, or cp.async element copies when a
+// leading dimension / base address breaks TMA's 16-byte rules), 8 consumer warps.
+//   FP32: each consumer thread owns an 8x8 register tile (FFMA pipe).
+//   FP64: each consumer warp owns a 64x32 tile of m16n8k8 DMMA fragments (the
+//         FP64 tensor path; measured on GB300 at 8x the DFMA rate).
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+#include "plain_gemm.h"
+
+namespace gb300 {
+
+constexpr int kBM = 128, kBN = 128, kStages = 4;
+constexpr int kConsumerWarps = 8;
+constexpr int kThreads = (kConsumerWarps + 1) * 32;  // + 1 producer warp
+
+template <typename T>
+struct PlainTraits;
+template <>
+struct PlainTraits<float> {
+  static constexpr int BK = 32;  // 128-byte rows for the K-major swizzled layout
+};
+template <>
+struct PlainTraits<double> {
+  static constexpr int BK = 16;
+};
+
+template <typename T>
+__host__ __device__ constexpr int tile_bytes() {
+  return kBM * PlainTraits<T>::BK * (int)sizeof(T);
+}
+template <typename T>
+__host__ __device__ constexpr int plain_smem_bytes() {
+  return kStages * 2 * tile_bytes<T>() + 1024 /*alignment slack*/ + 256 /*barriers*/;
+}
+
+constexpr int kGroupM = 16;
+
+// Offset (in elements) of logical (mn, k) inside one stage tile.
+//   MN-major tile: [BK][128] (mn contiguous), no swizzle.
+//   K-major tile : [128][BK] rows of 128 bytes, 128-byte swizzle: the 16-byte
+//                  chunk c of row r lives at chunk c ^ (r & 7).
+template <typename T, bool KMAJ>
+__device__ __forceinline__ int tile_off(int mn, int k) {
+  constexpr int BK = PlainTraits<T>::BK;
+  constexpr int EPC = 16 / (int)sizeof(T);  // elements per 16-byte chunk
+  if (KMAJ) {
+    const int chunk = (k / EPC) ^ (mn & 7);
+    return mn * BK + chunk * EPC + (k % EPC);
+  } else {
+    return k * kBM + mn;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// producer: fill one stage
+// ---------------------------------------------------------------------------
+struct OperandDesc {
+  const void *ptr;  // base of the stored matrix (column-major, ld)
+  int ld;
+  int rows, cols;   // stored shape
+};
+
+// cp.async fallback: every lane copies a strided share of the tile's elements.
+// Out-of-range elements are zero-filled (src-size 0), mirroring TMA's OOB fill.
+template <typename T, bool KMAJ>
+__device__ __forceinline__ void fallback_fill(T *tile, const OperandDesc &op, int mn0, int k0,
+                                              int lane) {
+  constexpr int BK = PlainTraits<T>::BK;
+  const T *base = static_cast<const T *>(op.ptr);
+  // stored (row, col): MN-major operand stores mn along rows; K-major stores k along rows.
+  for (int e = lane; e < kBM * BK; e += 32) {
+    int mn, k;
+    if (KMAJ) { mn = e / BK; k = e % BK; } else { k = e / kBM; mn = e % kBM; }
+    const int r = KMAJ ? (k0 + k) : (mn0 + mn);
+    const int c = KMAJ ? (mn0 + mn) : (k0 + k);
+    const bool ok = (r < op.rows) && (c < op.cols);
+    const T *src = ok ? base + (int64_t)c * op.ld + r : base;
+    if (sizeof(T) == 4)
+      cp_async_4(tile + tile_off<T, KMAJ>(mn, k), src, ok);
+    else
+      cp_async_8(tile + tile_off<T, KMAJ>(mn, k), src, ok);
+  }
+}
+
+template <typename T, bool AK, bool BK_>
+__device__ __forceinline__ void producer_loop(const CUtensorMap *tmA, const CUtensorMap *tmB,
+                                              const OperandDesc &opA, const OperandDesc &opB,
+                                              bool use_tma, T *sA, T *sB, uint64_t *full,
+                                              uint64_t *empty, int m0, int n0, int ktiles,
+                                              unsigned *err, volatile int *abort_flag) {
+  constexpr int BK = PlainTraits<T>::BK;
+  const int lane = threadIdx.x & 31;
+  for (int kt = 0; kt < ktiles; ++kt) {
+    const int s = kt % kStages;
+    if (kt >= kStages) {
+      if (!mbar_wait(&empty[s], ((kt / kStages) - 1) & 1, err, kErrTimeoutEmpty, abort_flag)) return;
+    }
+    T *ta = sA + s * (kBM * BK);
+    T *tb = sB + s * (kBN * BK);
+    const int k0 = kt * BK;
+    if (use_tma) {
+      if (lane == 0) {
+        mbar_arrive_expect_tx(&full[s], 2 * tile_bytes<T>());
+        // A: MN-major -> box (m, k) at (m0, k0); K-major -> box (k, m) at (k0, m0)
+        if (AK) tma_load_2d(ta, tmA, k0, m0, &full[s]);
+        else    tma_load_2d(ta, tmA, m0, k0, &full[s]);
+        if (BK_) tma_load_2d(tb, tmB, k0, n0, &full[s]);
+        else     tma_load_2d(tb, tmB, n0, k0, &full[s]);
+      }
+    } else {
+      fallback_fill<T, AK>(ta, opA, m0, k0, lane);
+      fallback_fill<T, BK_>(tb, opB, n0, k0, lane);
+      cp_async_mbar_arrive(&full[s]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 consumer: 8x8 register tile per thread (FFMA)
+// ---------------------------------------------------------------------------
+template <bool KMAJ>
+__device__ __forceinline__ int f32_row(int t, int i) {
+  // K-major tiles interleave rows (t + 16 i) so that a warp's eight distinct t
+  // hit eight different swizzle chunks; MN-major tiles use two 4-wide runs.
+  return KMAJ ? (t + 16 * i) : ((i < 4) ? (4 * t + i) : (64 + 4 * t + (i - 4)));
+}
+
+template <bool KMAJ>
+__device__ __forceinline__ void f32_load_frag(const float *tile, int t, int kq, float (&f)[8][4]) {
+  if (KMAJ) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = t + 16 * i;
+      const float4 v = *reinterpret_cast<const float4 *>(tile + r * 32 + ((kq ^ (r & 7)) << 2));
+      f[i][0] = v.x; f[i][1] = v.y; f[i][2] = v.z; f[i][3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float *row = tile + (4 * kq + q) * kBM;
+      const float4 v0 = *reinterpret_cast<const float4 *>(row + 4 * t);
+      const float4 v1 = *reinterpret_cast<const float4 *>(row + 64 + 4 * t);
+      f[0][q] = v0.x; f[1][q] = v0.y; f[2][q] = v0.z; f[3][q] = v0.w;
+      f[4][q] = v1.x; f[5][q] = v1.y; f[6][q] = v1.z; f[7][q] = v1.w;
+    }
+  }
+}
+
+template <bool AK, bool BK_>
+__global__ void __launch_bounds__(kThreads, 1)
+sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   OperandDesc opA, OperandDesc opB, int use_tma, int m, int n, int k, float alpha,
+                   float beta, float *__restrict__ C, int ldc, int tiles_m, int tiles_n,
+                   unsigned *err) {
+  constexpr int BK = PlainTraits<float>::BK;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                              ~uintptr_t(1023));
+  float *sA = reinterpret_cast<float *>(smem);
+  float *sB = sA + kStages * kBM * BK;
+  uint64_t *full = reinterpret_cast<uint64_t *>(sB + kStages * kBN * BK);
+  uint64_t *empty = full + kStages;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kStages);
+
+  int tmi, tni;
+  tile_coords(blockIdx.x, tiles_m, tiles_n, kGroupM, tmi, tni);
+  const int m0 = tmi * kBM, n0 = tni * kBN;
+  const int ktiles = (k + BK - 1) / BK;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], use_tma ? 1 : 32);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    *abort_flag = 0;
+    fence_barrier_init();
+    if (use_tma) { tma_prefetch_desc(&tmA); tma_prefetch_desc(&tmB); }
+  }
+  __syncthreads();
+
+  if (warp == kConsumerWarps) {
+    producer_loop<float, AK, BK_>(&tmA, &tmB, opA, opB, use_tma != 0, sA, sB, full, empty, m0, n0,
+                                  ktiles, err, abort_flag);
+    return;
+  }
+
+  // consumer thread coordinates
+  const int wm = warp & 1, wn = warp >> 1;
+  const int tm = wm * 8 + (lane & 7);
+  const int tn = wn * 4 + (lane >> 3);
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+
+  bool ok = true;
+  for (int kt = 0; kt < ktiles; ++kt) {
+    const int s = kt % kStages;
+    if (!mbar_wait(&full[s], (kt / kStages) & 1, err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
+    const float *ta = sA + s * (kBM * BK);
+    const float *tb = sB + s * (kBN * BK);
+#pragma unroll 2
+    for (int kq = 0; kq < BK / 4; ++kq) {
+      float a[8][4], b[8][4];
+      f32_load_frag<AK>(ta, tm, kq, a);
+      f32_load_frag<BK_>(tb, tn, kq, b);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i][q], b[j][q], acc[i][j]);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+  if (!ok) return;
+
+  // fused alpha/beta epilogue (beta*C first, as src/gemm_driver.c:133 does; beta == 0
+  // still multiplies, so NaN/Inf already in C propagate like the reference).
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int col = n0 + f32_row<BK_>(tn, j);
+    if (col >= n) continue;
+    float *cc = C + (int64_t)col * ldc;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int row = m0 + f32_row<AK>(tm, i);
+      if (row < m) {
+        const float c0 = cc[row];
+        const float cb = (beta == 1.0f) ? c0 : c0 * beta;
+        cc[row] = cb + alpha * acc[i][j];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 consumer: m16n8k8 DMMA fragments, warp tile 64 (m) x 32 (n)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void dmma_16x8x8(double (&c)[4], const double (&a)[4],
+                                            const double (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+d"(c[0]), "+d"(c[1]), "+d"(c[2]), "+d"(c[3])
+      : "d"(a[0]), "d"(a[1]), "d"(a[2]), "d"(a[3]), "d"(b[0]), "d"(b[1]));
+}
+
+template <bool AK, bool BK_>
+__global__ void __launch_bounds__(kThreads, 1)
+dgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   OperandDesc opA, OperandDesc opB, int use_tma, int m, int n, int k,
+                   double alpha, double beta, double *__restrict__ C, int ldc, int tiles_m,
+                   int tiles_n, unsigned *err) {
+  constexpr int BK = PlainTraits<double>::BK;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                              ~uintptr_t(1023));
+  double *sA = reinterpret_cast<double *>(smem);
+  double *sB = sA + kStages * kBM * BK;
+  uint64_t *full = reinterpret_cast<uint64_t *>(sB + kStages * kBN * BK);
+  uint64_t *empty = full + kStages;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kStages);
+
+  int tmi, tni;
+  tile_coords(blockIdx.x, tiles_m, tiles_n, kGroupM, tmi, tni);
+  const int m0 = tmi * kBM, n0 = tni * kBN;
+  const int ktiles = (k + BK - 1) / BK;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], use_tma ? 1 : 32);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    *abort_flag = 0;
+    fence_barrier_init();
+    if (use_tma) { tma_prefetch_desc(&tmA); tma_prefetch_desc(&tmB); }
+  }
+  __syncthreads();
+
+  if (warp == kConsumerWarps) {
+    producer_loop<double, AK, BK_>(&tmA, &tmB, opA, opB, use_tma != 0, sA, sB, full, empty, m0,
+                                   n0, ktiles, err, abort_flag);
+    return;
+  }
+
+  const int wm = warp & 1, wn = warp >> 1;  // 2 x 4 warps, warp tile 64 x 32
+  const int g = lane >> 2, t = lane & 3;
+  double acc[4][4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.0;
+
+  bool ok = true;
+  for (int kt = 0; kt < ktiles; ++kt) {
+    const int s = kt % kStages;
+    if (!mbar_wait(&full[s], (kt / kStages) & 1, err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
+    const double *ta = sA + s * (kBM * BK);
+    const double *tb = sB + s * (kBN * BK);
+#pragma unroll
+    for (int k8 = 0; k8 < BK; k8 += 8) {
+      double a[4][4], b[4][2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int mb = wm * 64 + i * 16;
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+          a[i][r] = ta[tile_off<double, AK>(mb + g + 8 * (r & 1), k8 + t + 4 * (r >> 1))];
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int nb = wn * 32 + j * 8;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) b[j][r] = tb[tile_off<double, BK_>(nb + g, k8 + t + 4 * r)];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dmma_16x8x8(acc[i][j], a[i], b[j]);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+  if (!ok) return;
+
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+#pragma unroll
+    for (int cj = 0; cj < 2; ++cj) {
+      const int col = n0 + wn * 32 + j * 8 + 2 * t + cj;
+      if (col >= n) continue;
+      double *cc = C + (int64_t)col * ldc;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int ri = 0; ri < 2; ++ri) {
+          const int row = m0 + wm * 64 + i * 16 + g + 8 * ri;
+          if (row < m) {
+            const double c0 = cc[row];
+            const double cb = (beta == 1.0) ? c0 : c0 * beta;
+            cc[row] = cb + alpha * acc[i][j][2 * ri + cj];
+          }
+        }
+      }
+    }
+  }
+}
+
+// C *= beta over the m x n window (alpha == 0, or k == 0 with the +0 of an empty sum).
+template <typename T>
+__global__ void scale_c_kernel(int m, int n, T beta, T add, T *__restrict__ C, int ldc) {
+  const int64_t total = (int64_t)m * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int col = (int)(e / m), row = (int)(e % m);
+    T *p = C + (int64_t)col * ldc + row;
+    *p = (beta == T(1) ? *p : *p * beta) + add;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <typename T>
+static void make_desc(OperandDesc &d, const T *p, int ld, int rows, int cols) {
+  d.ptr = p; d.ld = ld; d.rows = rows; d.cols = cols;
+}
+
+template <typename T, bool AK, bool BK_>
+static int launch_one(const CUtensorMap &tA, const CUtensorMap &tB, const OperandDesc &oA,
+                      const OperandDesc &oB, bool tma, int m, int n, int k, T alpha, T beta, T *C,
+                      int ldc, cudaStream_t st, unsigned *err) {
+  const int tiles_m = (m + kBM - 1) / kBM, tiles_n = (n + kBN - 1) / kBN;
+  const int smem = plain_smem_bytes<T>();
+  void (*kern)(const CUtensorMap, const CUtensorMap, OperandDesc, OperandDesc, int, int, int, int,
+               T, T, T *, int, int, int, unsigned *);
+  if constexpr (sizeof(T) == 4)
+    kern = sgemm_plain_kernel<AK, BK_>;
+  else
+    kern = dgemm_plain_kernel<AK, BK_>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return GB300_ERR_CUDA;
+  const int64_t ntiles = (int64_t)tiles_m * tiles_n;
+  if (ntiles > 0x7fffffff) return GB300_ERR_ARG;
+  kern<<<(unsigned)ntiles, kThreads, smem, st>>>(tA, tB, oA, oB, tma ? 1 : 0, m, n, k, alpha, beta,
+                                                  C, ldc, tiles_m, tiles_n, err);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+template <typename T>
+static int plain_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *A, int lda,
+                      const T *B, int ldb, T beta, T *C, int ldc, cudaStream_t st, unsigned *err) {
+  const bool an = notrans(ta), bn = notrans(tb);
+  const int arows = an ? m : k, brows = bn ? k : n;
+  if (m < 0 || n < 0 || k < 0 || lda < (arows > 1 ? arows : 1) ||
+      ldb < (brows > 1 ? brows : 1) || ldc < (m > 1 ? m : 1))
+    return GB300_ERR_ARG;
+  if (m == 0 || n == 0) return GB300_OK;
+  if (alpha == T(0) || k == 0) {
+    if (alpha == T(0) && beta == T(1)) return GB300_OK;
+    // alpha == 0: beta scaling only (src/gemm_driver.c:133-134); k == 0: the
+    // reference still adds an empty (zero) sum.
+    const T add = (alpha == T(0)) ? T(-0.0) : T(0);  // -0.0 leaves beta*C untouched
+    const int64_t total = (int64_t)m * n;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    scale_c_kernel<T><<<blocks, 256, 0, st>>>(m, n, beta, add, C, ldc);
+    return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  }
+  // Operand A: N -> stored m x k (MN-major tile), T -> stored k x m (K-major tile).
+  OperandDesc oA, oB;
+  make_desc(oA, A, lda, an ? m : k, an ? k : m);
+  make_desc(oB, B, ldb, bn ? k : n, bn ? n : k);
+  constexpr int BK = PlainTraits<T>::BK;
+  CUtensorMap tA{}, tB{};
+  bool tma = tma_ok(A, lda, sizeof(T)) && tma_ok(B, ldb, sizeof(T));
+  if (tma) {
+    // K-major operands use the 128-byte swizzle (box inner = BK elements = 128 B).
+    tma = encode_2d(&tA, A, sizeof(T), oA.rows, oA.cols, lda, an ? kBM : BK, an ? BK : kBM,
+                    /*swizzle128=*/!an) &&
+          encode_2d(&tB, B, sizeof(T), oB.rows, oB.cols, ldb, bn ? BK : kBN, bn ? kBN : BK,
+                    /*swizzle128=*/bn);
+  }
+  const bool AK = !an, BKm = bn;
+  if (!AK && !BKm) return launch_one<T, false, false>(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, st, err);
+  if (!AK && BKm)  return launch_one<T, false, true >(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, st, err);
+  if (AK && !BKm)  return launch_one<T, true,  false>(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, st, err);
+  return launch_one<T, true, true>(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, st, err);
+}
+
+int plain_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+                const double *B, int ldb, double beta, double *C, int ldc, cudaStream_t st,
+                unsigned *err) {
+  return plain_gemm<double>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err);
+}
+int plain_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
+                const float *B, int ldb, float beta, float *C, int ldc, cudaStream_t st,
+                unsigned *err) {
+  return plain_gemm<float>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err);
+}
+
+}  // namespace gb300

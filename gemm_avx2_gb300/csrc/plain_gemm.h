@@ -1,0 +1,49 @@
+// plain_gemm.h -- internal host-side declarations shared by the library's
+// translation units (not part of the public ABI; see include/gemm_gb300.h).
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/gemm_gb300.h"
+
+namespace gb300 {
+
+// 'N'/'n' = no transpose; any other character = transpose (src/gemm_driver.c:17-18).
+inline bool notrans(char t) { return t == 'N' || t == 'n'; }
+
+// Argument checks of every entry point (host only, no CUDA call):
+// GB300_ERR_ARG for negative sizes or leading dimensions below the stored rows
+// (at least 1); -1 for a valid call with nothing to compute (m or n == 0);
+// GB300_OK otherwise.
+inline int check_args(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc) {
+  const int arows = notrans(ta) ? m : k, brows = notrans(tb) ? k : n;
+  if (m < 0 || n < 0 || k < 0 || lda < (arows > 1 ? arows : 1) ||
+      ldb < (brows > 1 ? brows : 1) || ldc < (m > 1 ? m : 1))
+    return GB300_ERR_ARG;
+  return (m == 0 || n == 0) ? -1 : GB300_OK;
+}
+
+// TMA requires a 16-byte aligned base and a leading dimension whose byte
+// stride is a multiple of 16.
+inline bool tma_ok(const void *p, int ld, size_t elem) {
+  return (reinterpret_cast<uintptr_t>(p) % 16 == 0) && ((size_t)ld * elem) % 16 == 0;
+}
+
+// Encode a 2-D tiled tensor map over a column-major matrix of rows x cols
+// (rows contiguous, leading dimension ld elements).  box = (box_rows, box_cols).
+// elem_bytes 2 -> BF16, 4 -> FP32, 8 -> FP64.  Returns false if the driver
+// rejects it (the caller then falls back to non-TMA loads).
+bool encode_2d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t rows, int64_t cols,
+               int64_t ld, int box_rows, int box_cols, bool swizzle128);
+
+int plain_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+                const double *B, int ldb, double beta, double *C, int ldc, cudaStream_t st,
+                unsigned *err);
+int plain_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
+                const float *B, int ldb, float beta, float *C, int ldc, cudaStream_t st,
+                unsigned *err);
+
+}  // namespace gb300

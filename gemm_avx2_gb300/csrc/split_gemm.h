@@ -1,0 +1,41 @@
+// split_gemm.h -- internal declarations of the tensor-core split forms.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace gb300 {
+
+// Geometry shared by the split kernels and the workspace sizing.
+constexpr int kSplitBK = 64;       // K elements per pipeline stage (128 B of BF16)
+constexpr int kSplitBM = 128;      // tile rows (TMEM lanes)
+constexpr int kBf16xBN = 256;      // tile columns of the BF16xP SGEMM
+constexpr int kOzakiBN = 128;      // tile columns of the Ozaki DGEMM
+constexpr int kOzakiMaxSlices = 12;
+
+size_t split_workspace_bytes(int kind, int m, int n, int k, int param);
+
+int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
+                const float *B, int ldb, float beta, float *C, int ldc, int products, void *ws,
+                size_t ws_bytes, cudaStream_t st, unsigned *err);
+
+int ozaki_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+                const double *B, int ldb, double beta, double *C, int ldc, int slices, void *ws,
+                size_t ws_bytes, cudaStream_t st, unsigned *err);
+
+// Two-phase forms: prepare writes the split operands into the workspace,
+// run computes C from a prepared workspace (same m, n, k, products/slices).
+int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, int lda,
+                        const float *B, int ldb, int products, void *ws, size_t ws_bytes,
+                        cudaStream_t st);
+int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int ldc, int products,
+                    const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err);
+int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
+                  int ldb, int slices, void *ws, size_t ws_bytes, cudaStream_t st);
+int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int slices,
+              const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err);
+
+// Default slice count for a shape class (autotune cache, falls back to 8).
+int ozaki_default_slices(int m, int n, int k);
+
+}  // namespace gb300

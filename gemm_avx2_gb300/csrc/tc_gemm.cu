@@ -1,0 +1,810 @@
+// tc_gemm.cu -- tensor-core (tcgen05, sm_103a) split-precision forms of the
+// reference's sgemm_/dgemm_ (wjc404/GEMM_AVX2 src/gemm_driver.c:118; same
+// operand semantics, no reference kernel counterpart).
+//
+//  * BF16xP SGEMM: op(A), op(B) are split into BF16 terms by a split kernel that
+//    also absorbs the transposes and writes K-major operands (the role of the
+//    reference's packing, src/gemm_copy.c).  The P cross products are laid
+//    side by side along K, so one BF16 GEMM with FP32 accumulation in TMEM over
+//    K' = P * K computes their sum.
+//  * Ozaki DGEMM: rows of op(A) / columns of op(B) are scaled by powers of two
+//    and cut into S slices of signed 7-bit integers (|d| <= 127, int8 range).
+//    tcgen05 on sm_103a has no kind::i8, so the integer slices ride the BF16
+//    pipe: each slice value is exact in BF16, each product (< 2^14) exact in
+//    FP32, and every accumulation chunk is capped at 256 K-steps so partial sums
+//    stay below 2^22 -- integer-valued FP32 is then exact.  The epilogue warps
+//    drain each chunk from TMEM into 32-bit integer sums (exact), and fold each
+//    slice group t = i + j into an FP64 result held in TMEM with weight 2^-7t.
+//
+// Both GEMMs are persistent, warp-specialised kernels: warp 0 issues TMA loads
+// into a shared-memory ring, warp 1 allocates TMEM and issues tcgen05.mma from
+// one thread, the remaining warps run the epilogue from TMEM.  Two TMEM
+// accumulators let the epilogue of one tile/chunk overlap the next one's MMAs.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+#include "plain_gemm.h"
+#include "split_gemm.h"
+
+namespace gb300 {
+
+static inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+constexpr int kSplitGroupM = 16;
+
+// ===========================================================================
+// split kernels: read op(X) (R x K view of a column-major matrix) in 32 x 64
+// tiles through shared memory so that both the read and the K-major write
+// are coalesced whatever the transpose.
+// ===========================================================================
+template <typename T>
+__device__ __forceinline__ void load_tile_32x64(const T *__restrict__ X, int ld, int R, int K,
+                                                bool kcontig, int r0, int k0, T (*tile)[65]) {
+  const int tid = threadIdx.x;  // 256 threads
+  if (kcontig) {  // element (r, k) at X[k + r*ld]: read along k
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+      const int r = p * 4 + (tid >> 6), k = tid & 63;
+      const int gr = r0 + r, gk = k0 + k;
+      tile[r][k] = (gr < R && gk < K) ? X[(int64_t)gr * ld + gk] : T(0);
+    }
+  } else {  // element (r, k) at X[r + k*ld]: read along r
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+      const int r = tid & 31, k = p * 8 + (tid >> 5);
+      const int gr = r0 + r, gk = k0 + k;
+      tile[r][k] = (gr < R && gk < K) ? X[gr + (int64_t)gk * ld] : T(0);
+    }
+  }
+}
+
+// term[] of x: t0 = bf16(x), t1 = bf16(x - t0), t2 = bf16(x - t0 - t1); every
+// residual is exact in FP32.
+__device__ __forceinline__ void bf16_terms(float x, int nterms, __nv_bfloat16 (&t)[3]) {
+  float r = x;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (i < nterms) {
+      t[i] = __float2bfloat16_rn(r);
+      r = r - __bfloat162float(t[i]);
+    } else {
+      t[i] = __float2bfloat16_rn(0.f);
+    }
+  }
+}
+
+// Segment s of the concatenated operand holds term seg_term[s] of x.
+struct SegMap {
+  int nseg;
+  int term[6];
+};
+
+// out: Rp x (nseg * Kp) row-major BF16 (row stride ldo = nseg*Kp elements).
+__global__ void __launch_bounds__(256) split_bf16_kernel(const float *__restrict__ X, int ld, int R,
+                                                         int K, int kcontig, int Kp, SegMap seg,
+                                                         int nterms, __nv_bfloat16 *__restrict__ out,
+                                                         int64_t ldo) {
+  __shared__ float tile[32][65];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 64;
+  load_tile_32x64<float>(X, ld, R, K, kcontig != 0, r0, k0, tile);
+  __syncthreads();
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int r = p * 8 + (tid >> 5), kk = (tid & 31) * 2;
+    __nv_bfloat16 t0[3], t1[3];
+    bf16_terms(tile[r][kk], nterms, t0);
+    bf16_terms(tile[r][kk + 1], nterms, t1);
+    __nv_bfloat16 *row = out + (int64_t)(r0 + r) * ldo + k0 + kk;
+    for (int s = 0; s < seg.nseg; ++s) {
+      const int ti = seg.term[s];
+      __nv_bfloat162 v;
+      v.x = t0[ti];
+      v.y = t1[ti];
+      *reinterpret_cast<__nv_bfloat162 *>(row + (int64_t)s * Kp) = v;
+    }
+  }
+}
+
+// Ozaki step 1: per-row max |x| of op(X) as the bit pattern of a non-negative
+// double (monotone as an unsigned integer; NaN/Inf compare above finite values).
+__global__ void __launch_bounds__(256) row_absmax_kernel(const double *__restrict__ X, int ld,
+                                                         int R, int K, int kcontig,
+                                                         unsigned long long *__restrict__ amax) {
+  if (kcontig) {
+    // one warp per (row, 2048-wide k range)
+    const int warp = (blockIdx.x * 8) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int r = warp;
+    if (r >= R) return;
+    const int k0 = blockIdx.y * 2048, k1 = min(K, k0 + 2048);
+    unsigned long long m = 0;
+    const double *row = X + (int64_t)r * ld;
+    for (int kk = k0 + lane; kk < k1; kk += 32) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(row[kk]));
+      m = b > m ? b : m;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+      m = x > m ? x : m;
+    }
+    if (lane == 0 && m) atomicMax(&amax[r], m);
+  } else {
+    // one thread per row, a 256-wide k range per grid row
+    const int r = blockIdx.x * 256 + threadIdx.x;
+    if (r >= R) return;
+    const int k0 = blockIdx.y * 256, k1 = min(K, k0 + 256);
+    unsigned long long m = 0;
+    for (int kk = k0; kk < k1; ++kk) {
+      const unsigned long long b =
+          (unsigned long long)__double_as_longlong(fabs(X[r + (int64_t)kk * ld]));
+      m = b > m ? b : m;
+    }
+    if (m) atomicMax(&amax[r], m);
+  }
+}
+
+// Scale exponent of a row: 2^-E * max|x| < 1.  Non-finite rows return a marker.
+constexpr int kNonFiniteExp = 0x40000000;
+__device__ __forceinline__ int row_exponent(unsigned long long amax_bits) {
+  const double m = __longlong_as_double((long long)amax_bits);
+  if (!(m <= 1.7976931348623157e308)) return kNonFiniteExp;  // Inf or NaN
+  if (m == 0.0) return 0;
+  int e;
+  frexp(m, &e);  // m = f * 2^e, f in [0.5, 1)
+  return e;
+}
+
+// Ozaki step 2: slices.  x = op(X)(r,k) * 2^-E_r in (-1,1); for s = 1..S:
+// y = x * 128, d_s = trunc(y) (|d_s| <= 127), x = y - d_s (exact).
+// out: S blocks of Rp rows x Kp (row-major BF16), slice s at rows (s-1)*Rp.
+__global__ void __launch_bounds__(256) ozaki_slice_kernel(
+    const double *__restrict__ X, int ld, int R, int K, int kcontig, int Rp, int Kp, int S,
+    const unsigned long long *__restrict__ amax, __nv_bfloat16 *__restrict__ out) {
+  __shared__ double tile[32][65];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 64;
+  load_tile_32x64<double>(X, ld, R, K, kcontig != 0, r0, k0, tile);
+  __syncthreads();
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int r = p * 8 + (tid >> 5), kk = (tid & 31) * 2;
+    const int gr = r0 + r;
+    const int e = (gr < R) ? row_exponent(amax[gr]) : 0;
+    double x0 = tile[r][kk], x1 = tile[r][kk + 1];
+    const bool bad = (e == kNonFiniteExp);
+    if (!bad) { x0 = ldexp(x0, -e); x1 = ldexp(x1, -e); }
+    __nv_bfloat16 *base = out + (int64_t)gr * Kp + k0 + kk;
+    for (int s = 0; s < S; ++s) {
+      __nv_bfloat162 v;
+      if (bad) {
+        v.x = __float2bfloat16_rn(__int_as_float(0x7fc00000));
+        v.y = v.x;
+      } else {
+        const double y0 = x0 * 128.0, y1 = x1 * 128.0;
+        const double d0 = trunc(y0), d1 = trunc(y1);
+        x0 = y0 - d0; x1 = y1 - d1;
+        v.x = __float2bfloat16_rn((float)d0);
+        v.y = __float2bfloat16_rn((float)d1);
+      }
+      *reinterpret_cast<__nv_bfloat162 *>(base + (int64_t)s * Rp * Kp) = v;
+    }
+  }
+}
+
+// ===========================================================================
+// BF16xP GEMM: C = alpha * A'B'^T + beta * C, persistent, 128 x 256 tiles.
+// ===========================================================================
+struct Bf16xParams {
+  int m, n, tiles_m, tiles_n, kblocks;
+  float alpha, beta;
+  float *C;
+  int ldc;
+  unsigned *err;
+};
+
+constexpr int kBxStages = 4;
+constexpr int kBxThreads = 6 * 32;  // producer, MMA, 4 epilogue warps
+constexpr int kBxABytes = kSplitBM * 128;
+constexpr int kBxBBytes = kBf16xBN * 128;
+constexpr int kBxStage = kBxABytes + kBxBBytes;
+constexpr int kBxSmem = kBxStages * kBxStage + 1024 + 256;
+
+__global__ void __launch_bounds__(kBxThreads, 1)
+bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  Bf16xParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                              ~uintptr_t(1023));
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + kBxStages * kBxStage);
+  uint64_t *empty = full + kBxStages;
+  uint64_t *accf = empty + kBxStages;
+  uint64_t *acce = accf + 2;
+  uint64_t *done = acce + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kBxStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&accf[b], 1); mbar_init(&acce[b], 4); }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+    tma_prefetch_desc(&tmA);
+    tma_prefetch_desc(&tmB);
+  }
+  if (warp == 1) { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int ntiles = p.tiles_m * p.tiles_n;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t L = 0;
+      for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x) {
+        int tm, tn;
+        tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
+        for (int kb = 0; kb < p.kblocks; ++kb, ++L) {
+          const int s = L % kBxStages;
+          const uint32_t r = L / kBxStages;
+          if (!mbar_wait(&empty[s], (r & 1) ^ 1, p.err, kErrTimeoutEmpty, abort_flag)) break;
+          uint8_t *sa = smem + s * kBxStage;
+          mbar_arrive_expect_tx(&full[s], kBxStage);
+          tma_load_2d(sa, &tmA, kb * kSplitBK, tm * kSplitBM, &full[s]);
+          tma_load_2d(sa + kBxABytes, &tmB, kb * kSplitBK, tn * kBf16xBN, &full[s]);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16_f32(kSplitBM, kBf16xBN);
+      uint32_t L = 0, it = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++it) {
+        const int b = it & 1;
+        const uint32_t u = it >> 1;
+        if (!mbar_wait(&acce[b], (u & 1) ^ 1, p.err, kErrTimeoutMma, abort_flag)) break;
+        tc_fence_after();
+        const uint32_t dt = tmem + b * kBf16xBN;
+        for (int kb = 0; kb < p.kblocks; ++kb, ++L) {
+          const int s = L % kBxStages;
+          const uint32_t r = L / kBxStages;
+          if (!mbar_wait(&full[s], r & 1, p.err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sa = smem_u32(smem + s * kBxStage), sb = sa + kBxABytes;
+#pragma unroll
+          for (int kk = 0; kk < kSplitBK / 16; ++kk)
+            umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32), idesc,
+                      (kb > 0 || kk > 0) ? 1u : 0u);
+          umma_commit(&empty[s]);
+        }
+        if (ok) umma_commit(&accf[b]);
+      }
+      // every issued MMA has completed before TMEM is released
+      umma_commit(done);
+      mbar_wait(done, 0, p.err, kErrTimeoutMma, nullptr);
+    }
+  } else {
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int row_in_tile = q * 32 + lane;
+    uint32_t it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      int tm, tn;
+      tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
+      const int b = it & 1;
+      const uint32_t u = it >> 1;
+      if (!mbar_wait(&accf[b], u & 1, p.err, kErrTimeoutAcc, abort_flag)) break;
+      tc_fence_after();
+      const int row = tm * kSplitBM + row_in_tile;
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + b * kBf16xBN;
+#pragma unroll 1
+      for (int c = 0; c < kBf16xBN / 32; ++c) {
+        uint32_t v[32];
+        tmem_ld32(tbase + c * 32, v);
+        tmem_ld_wait();
+        if (row < p.m) {
+          const int col0 = tn * kBf16xBN + c * 32;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int col = col0 + j;
+            if (col < p.n) {
+              float *cp = p.C + (int64_t)col * p.ldc + row;
+              const float c0 = *cp;
+              const float cb = (p.beta == 1.0f) ? c0 : c0 * p.beta;
+              *cp = cb + p.alpha * __uint_as_float(v[j]);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[b]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+// ===========================================================================
+// Ozaki GEMM: persistent, 128 x 128 tiles, exact integer slice products.
+// TMEM: [0,128) and [128,256) chunk accumulators (FP32), [256,384) and
+// [384,512) the low and high words of the tile's FP64 result.
+// ===========================================================================
+struct OzakiParams {
+  int m, n, tiles_m, tiles_n;
+  int S, KB;   // slices, K blocks of 64 per slice pair
+  int Mp, Np;  // rows per slice block of A and B
+  double alpha, beta;
+  double *C;
+  int ldc;
+  const unsigned long long *amaxA, *amaxB;
+  unsigned *err;
+};
+
+constexpr int kOzStages = 6;
+constexpr int kOzEpiWarps = 8;
+constexpr int kOzThreads = (2 + kOzEpiWarps) * 32;
+constexpr int kOzABytes = kSplitBM * 128;
+constexpr int kOzBBytes = kOzakiBN * 128;
+constexpr int kOzStage = kOzABytes + kOzBBytes;
+constexpr int kOzSmem = kOzStages * kOzStage + 1024 + 256;
+constexpr int kOzChunkStages = 4;       // 4 x 64 = 256 K-steps per exact chunk
+constexpr int kOzRunChunks = 512;       // int32 sums folded at least every 512 chunks
+
+// pairs of slice group t: sa in [lo, hi], sb = t - sa
+__device__ __forceinline__ void group_pairs(int t, int S, int &lo, int &np) {
+  lo = max(1, t - S);
+  const int hi = min(S, t - 1);
+  np = hi - lo + 1;
+}
+
+__global__ void __launch_bounds__(kOzThreads, 1)
+ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  OzakiParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                              ~uintptr_t(1023));
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + kOzStages * kOzStage);
+  uint64_t *empty = full + kOzStages;
+  uint64_t *accf = empty + kOzStages;
+  uint64_t *acce = accf + 2;
+  uint64_t *done = acce + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kOzStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&accf[b], 1); mbar_init(&acce[b], kOzEpiWarps); }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+    tma_prefetch_desc(&tmA);
+    tma_prefetch_desc(&tmB);
+  }
+  if (warp == 1) { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int ntiles = p.tiles_m * p.tiles_n;
+  const int S = p.S, KB = p.KB;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t L = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        int tm, tn;
+        tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
+        for (int t = S + 1; t >= 2 && ok; --t) {
+          int lo, np;
+          group_pairs(t, S, lo, np);
+          const int G = np * KB;
+          for (int idx = 0; idx < G; ++idx, ++L) {
+            const int kb = idx / np, sa = lo + idx % np, sb = t - sa;
+            const int s = L % kOzStages;
+            const uint32_t r = L / kOzStages;
+            if (!mbar_wait(&empty[s], (r & 1) ^ 1, p.err, kErrTimeoutEmpty, abort_flag)) {
+              ok = false;
+              break;
+            }
+            uint8_t *sa_ptr = smem + s * kOzStage;
+            mbar_arrive_expect_tx(&full[s], kOzStage);
+            tma_load_2d(sa_ptr, &tmA, kb * kSplitBK, (sa - 1) * p.Mp + tm * kSplitBM, &full[s]);
+            tma_load_2d(sa_ptr + kOzABytes, &tmB, kb * kSplitBK, (sb - 1) * p.Np + tn * kOzakiBN,
+                        &full[s]);
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16_f32(kSplitBM, kOzakiBN);
+      uint32_t L = 0, chunk = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        for (int t = S + 1; t >= 2 && ok; --t) {
+          int lo, np;
+          group_pairs(t, S, lo, np);
+          const int G = np * KB;
+          for (int c0 = 0; c0 < G && ok; c0 += kOzChunkStages, ++chunk) {
+            const int b = chunk & 1;
+            const uint32_t u = chunk >> 1;
+            if (!mbar_wait(&acce[b], (u & 1) ^ 1, p.err, kErrTimeoutMma, abort_flag)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t dt = tmem + b * kOzakiBN;
+            const int c1 = min(G, c0 + kOzChunkStages);
+            for (int idx = c0; idx < c1; ++idx, ++L) {
+              const int s = L % kOzStages;
+              const uint32_t r = L / kOzStages;
+              if (!mbar_wait(&full[s], r & 1, p.err, kErrTimeoutFull, abort_flag)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+              const uint32_t sa = smem_u32(smem + s * kOzStage), sb = sa + kOzABytes;
+#pragma unroll
+              for (int kk = 0; kk < kSplitBK / 16; ++kk)
+                umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32), idesc,
+                          (idx > c0 || kk > 0) ? 1u : 0u);
+              umma_commit(&empty[s]);
+            }
+            if (ok) umma_commit(&accf[b]);
+          }
+        }
+      }
+      umma_commit(done);
+      mbar_wait(done, 0, p.err, kErrTimeoutMma, nullptr);
+    }
+  } else {
+    // 8 epilogue warps: lane quarter q = warp % 4, column half h
+    const int q = warp & 3;
+    const int h = (warp - 2) >> 2;
+    const int row_in_tile = q * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+    uint32_t chunk = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      int tm, tn;
+      tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
+      bool res_init = false;
+      for (int t = S + 1; t >= 2 && ok; --t) {
+        int lo, np;
+        group_pairs(t, S, lo, np);
+        const int G = np * KB;
+        const int nch = (G + kOzChunkStages - 1) / kOzChunkStages;
+        const double wt = ldexp(1.0, -7 * t);
+        int run[64];
+#pragma unroll
+        for (int j = 0; j < 64; ++j) run[j] = 0;
+        int since_fold = 0;
+        for (int c = 0; c < nch; ++c, ++chunk) {
+          const int b = chunk & 1;
+          const uint32_t u = chunk >> 1;
+          if (!mbar_wait(&accf[b], u & 1, p.err, kErrTimeoutAcc, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            uint32_t v[32];
+            tmem_ld32(lane_base + b * kOzakiBN + h * 64 + hh * 32, v);
+            tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              // |v| < 2^22 and integer-valued: exact conversion by the 1.5*2^23 shift
+              run[hh * 32 + j] += __float_as_int(__uint_as_float(v[j]) + 12582912.0f) - 0x4B400000;
+            }
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acce[b]);
+          const bool last = (c == nch - 1);
+          if (++since_fold == kOzRunChunks || last) {
+            // fold the exact group sum into the FP64 result: res += run * 2^-7t
+#pragma unroll
+            for (int g4 = 0; g4 < 4; ++g4) {
+              const uint32_t col = h * 64 + g4 * 16;
+              uint32_t lo_w[16], hi_w[16];
+              if (res_init) {
+                tmem_ld16(lane_base + 256 + col, lo_w);
+                tmem_ld16(lane_base + 384 + col, hi_w);
+                tmem_ld_wait();
+              }
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const double prev =
+                    res_init ? __hiloint2double((int)hi_w[j], (int)lo_w[j]) : 0.0;
+                const double nv = fma((double)run[g4 * 16 + j], wt, prev);
+                lo_w[j] = (uint32_t)__double2loint(nv);
+                hi_w[j] = (uint32_t)__double2hiint(nv);
+                run[g4 * 16 + j] = 0;
+              }
+              tmem_st16(lane_base + 256 + col, lo_w);
+              tmem_st16(lane_base + 384 + col, hi_w);
+            }
+            tmem_st_wait();
+            res_init = true;
+            since_fold = 0;
+          }
+        }
+      }
+      if (!ok) break;
+      // final epilogue: C = alpha * 2^(E_i + F_j) * res + beta * C
+      const int row = tm * kSplitBM + row_in_tile;
+      const int ea = (row < p.m) ? row_exponent(p.amaxA[row]) : 0;
+#pragma unroll
+      for (int g4 = 0; g4 < 4; ++g4) {
+        const int colt = h * 64 + g4 * 16;
+        uint32_t lo_w[16], hi_w[16];
+        tmem_ld16(lane_base + 256 + colt, lo_w);
+        tmem_ld16(lane_base + 384 + colt, hi_w);
+        tmem_ld_wait();
+        if (row < p.m) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = tn * kOzakiBN + colt + j;
+            if (col < p.n) {
+              const int eb = row_exponent(p.amaxB[col]);
+              double v = __hiloint2double((int)hi_w[j], (int)lo_w[j]);
+              v = (ea == kNonFiniteExp || eb == kNonFiniteExp) ? __longlong_as_double(0x7ff8000000000000LL)
+                                                               : ldexp(v, ea + eb);
+              double *cp = p.C + (int64_t)col * p.ldc + row;
+              const double c0 = *cp;
+              const double cb = (p.beta == 1.0) ? c0 : c0 * p.beta;
+              *cp = cb + p.alpha * v;
+            }
+          }
+        }
+      }
+      // the next tile's first fold overwrites the result columns: make the
+      // reads above complete first
+      tc_fence_before();
+      __syncwarp();
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+// ===========================================================================
+// host side
+// ===========================================================================
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int d = 0;
+    cudaGetDevice(&d);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d);
+    if (n <= 0) n = 148;
+  }
+  return n;
+}
+
+static SegMap seg_map(int products, bool is_a) {
+  SegMap s{};
+  if (products == 3) {
+    // products (lo*hi), (hi*lo), (hi*hi): small terms accumulate first
+    const int a[3] = {1, 0, 0}, b[3] = {0, 1, 0};
+    s.nseg = 3;
+    for (int i = 0; i < 3; ++i) s.term[i] = is_a ? a[i] : b[i];
+  } else {
+    // all (i, j) with i + j <= 2 over terms (hi, mid, lo), smallest order first
+    const int a[6] = {2, 1, 0, 1, 0, 0}, b[6] = {0, 1, 2, 0, 1, 0};
+    s.nseg = 6;
+    for (int i = 0; i < 6; ++i) s.term[i] = is_a ? a[i] : b[i];
+  }
+  return s;
+}
+
+size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  const int64_t Kp = round_up(k, kSplitBK);
+  if (kind == 0) {
+    if (param != 3 && param != 6) return 0;
+    const int64_t Mp = round_up(m, kSplitBM), Np = round_up(n, kBf16xBN);
+    return (size_t)((Mp + Np) * param * Kp * 2 + 1024);
+  }
+  int S = param > 0 ? param : ozaki_default_slices(m, n, k);
+  if (S < 2 || S > kOzakiMaxSlices) return 0;
+  const int64_t Mp = round_up(m, kSplitBM), Np = round_up(n, kOzakiBN);
+  return (size_t)((Mp + Np) * S * Kp * 2 + (Mp + Np) * 8 + 2048);
+}
+
+int ozaki_default_slices(int, int, int) { return 8; }
+
+// ----------------------------------------------------------------- BF16xP
+struct Bf16xLayout {
+  int64_t Kp, Kld, Mp, Np;
+  __nv_bfloat16 *Ap, *Bp;
+};
+static Bf16xLayout bf16x_layout(int m, int n, int k, int products, void *ws) {
+  Bf16xLayout L;
+  L.Kp = round_up(k, kSplitBK);
+  L.Kld = L.Kp * products;
+  L.Mp = round_up(m, kSplitBM);
+  L.Np = round_up(n, kBf16xBN);
+  L.Ap = reinterpret_cast<__nv_bfloat16 *>((reinterpret_cast<uintptr_t>(ws) + 1023) &
+                                           ~uintptr_t(1023));
+  L.Bp = L.Ap + L.Mp * L.Kld;
+  return L;
+}
+
+int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, int lda,
+                        const float *B, int ldb, int products, void *ws, size_t ws_bytes,
+                        cudaStream_t st) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
+  if (ck == GB300_ERR_ARG || (products != 3 && products != 6)) return GB300_ERR_ARG;
+  if (ck < 0 || k == 0) return GB300_OK;
+  const size_t need = split_workspace_bytes(0, m, n, k, products);
+  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
+  const Bf16xLayout L = bf16x_layout(m, n, k, products, ws);
+  if (L.Kld > 0x7fffffff || L.Mp > 0x7fffffff || L.Np > 0x7fffffff) return GB300_ERR_ARG;
+  const bool an = notrans(ta), bn = notrans(tb);
+  const int nterms = products == 3 ? 2 : 3;
+  split_bf16_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Mp / 32)), 256, 0, st>>>(
+      A, lda, m, k, an ? 0 : 1, (int)L.Kp, seg_map(products, true), nterms, L.Ap, L.Kld);
+  split_bf16_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Np / 32)), 256, 0, st>>>(
+      B, ldb, n, k, bn ? 1 : 0, (int)L.Kp, seg_map(products, false), nterms, L.Bp, L.Kld);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int ldc, int products,
+                    const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err) {
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || (products != 3 && products != 6))
+    return GB300_ERR_ARG;
+  if (m == 0 || n == 0) return GB300_OK;
+  if (alpha == 0.0f || k == 0)
+    return plain_sgemm('N', 'N', m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc,
+                       st, err);
+  const size_t need = split_workspace_bytes(0, m, n, k, products);
+  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
+  const Bf16xLayout L = bf16x_layout(m, n, k, products, const_cast<void *>(ws));
+  CUtensorMap tA{}, tB{};
+  if (!encode_2d(&tA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
+      !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, kBf16xBN, true))
+    return GB300_ERR_CUDA;
+  Bf16xParams p;
+  p.m = m; p.n = n;
+  p.tiles_m = (int)(L.Mp / kSplitBM);
+  p.tiles_n = (int)(L.Np / kBf16xBN);
+  p.kblocks = (int)(L.Kld / kSplitBK);
+  p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.err = err;
+  if (cudaFuncSetAttribute(bf16x_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kBxSmem) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  const int ntiles = p.tiles_m * p.tiles_n;
+  const int grid = ntiles < sm_count() ? ntiles : sm_count();
+  bf16x_gemm_kernel<<<grid, kBxThreads, kBxSmem, st>>>(tA, tB, p);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
+                const float *B, int ldb, float beta, float *C, int ldc, int products, void *ws,
+                size_t ws_bytes, cudaStream_t st, unsigned *err) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck == GB300_ERR_ARG || (products != 3 && products != 6)) return GB300_ERR_ARG;
+  if (ck < 0) return GB300_OK;
+  if (alpha == 0.0f || k == 0)  // no products to form: the plain path's beta handling
+    return plain_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err);
+  int rc = split_sgemm_prepare(ta, tb, m, n, k, A, lda, B, ldb, products, ws, ws_bytes, st);
+  if (rc != GB300_OK) return rc;
+  return split_sgemm_run(m, n, k, alpha, beta, C, ldc, products, ws, ws_bytes, st, err);
+}
+
+// ----------------------------------------------------------------- Ozaki
+struct OzakiLayout {
+  int64_t Kp, Mp, Np;
+  __nv_bfloat16 *As, *Bs;
+  unsigned long long *amaxA, *amaxB;
+};
+static OzakiLayout ozaki_layout(int m, int n, int k, int S, void *ws) {
+  OzakiLayout L;
+  L.Kp = round_up(k, kSplitBK);
+  L.Mp = round_up(m, kSplitBM);
+  L.Np = round_up(n, kOzakiBN);
+  uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(ws) + 1023) &
+                                              ~uintptr_t(1023));
+  L.As = reinterpret_cast<__nv_bfloat16 *>(base);
+  L.Bs = L.As + S * L.Mp * L.Kp;
+  L.amaxA = reinterpret_cast<unsigned long long *>(L.Bs + S * L.Np * L.Kp);
+  L.amaxB = L.amaxA + L.Mp;
+  return L;
+}
+
+int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
+                  int ldb, int slices, void *ws, size_t ws_bytes, cudaStream_t st) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
+  const int S = slices > 0 ? slices : ozaki_default_slices(m, n, k);
+  if (ck == GB300_ERR_ARG || S < 2 || S > kOzakiMaxSlices) return GB300_ERR_ARG;
+  if (ck < 0 || k == 0) return GB300_OK;
+  const size_t need = split_workspace_bytes(1, m, n, k, S);
+  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
+  const OzakiLayout L = ozaki_layout(m, n, k, S, ws);
+  if (S * L.Mp > 0x7fffffff || S * L.Np > 0x7fffffff || L.Kp > 0x7fffffff) return GB300_ERR_ARG;
+  const bool an = notrans(ta), bn = notrans(tb);
+  if (cudaMemsetAsync(L.amaxA, 0, (size_t)(L.Mp + L.Np) * 8, st) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  // per-row / per-column max |.|: A rows are k-contiguous when transposed, B
+  // columns when not.
+  auto absmax = [&](const double *X, int ld, int R, bool kc, unsigned long long *am) {
+    if (kc)
+      row_absmax_kernel<<<dim3((unsigned)((R + 7) / 8), (unsigned)((k + 2047) / 2048)), 256, 0,
+                           st>>>(X, ld, R, k, 1, am);
+    else
+      row_absmax_kernel<<<dim3((unsigned)((R + 255) / 256), (unsigned)((k + 255) / 256)), 256, 0,
+                           st>>>(X, ld, R, k, 0, am);
+  };
+  absmax(A, lda, m, !an, L.amaxA);
+  absmax(B, ldb, n, bn, L.amaxB);
+  ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Mp / 32)), 256, 0, st>>>(
+      A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, S, L.amaxA, L.As);
+  ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Np / 32)), 256, 0, st>>>(
+      B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, S, L.amaxB, L.Bs);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int slices,
+              const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err) {
+  const int S = slices > 0 ? slices : ozaki_default_slices(m, n, k);
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || S < 2 || S > kOzakiMaxSlices)
+    return GB300_ERR_ARG;
+  if (m == 0 || n == 0) return GB300_OK;
+  if (alpha == 0.0 || k == 0)
+    return plain_dgemm('N', 'N', m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc,
+                       st, err);
+  const size_t need = split_workspace_bytes(1, m, n, k, S);
+  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
+  const OzakiLayout L = ozaki_layout(m, n, k, S, const_cast<void *>(ws));
+  CUtensorMap tA{}, tB{};
+  if (!encode_2d(&tA, L.As, 2, L.Kp, S * L.Mp, L.Kp, kSplitBK, kSplitBM, true) ||
+      !encode_2d(&tB, L.Bs, 2, L.Kp, S * L.Np, L.Kp, kSplitBK, kOzakiBN, true))
+    return GB300_ERR_CUDA;
+  OzakiParams p;
+  p.m = m; p.n = n;
+  p.tiles_m = (int)(L.Mp / kSplitBM);
+  p.tiles_n = (int)(L.Np / kOzakiBN);
+  p.S = S; p.KB = (int)(L.Kp / kSplitBK);
+  p.Mp = (int)L.Mp; p.Np = (int)L.Np;
+  p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc;
+  p.amaxA = L.amaxA; p.amaxB = L.amaxB; p.err = err;
+  if (cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kOzSmem) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  const int ntiles = p.tiles_m * p.tiles_n;
+  const int grid = ntiles < sm_count() ? ntiles : sm_count();
+  ozaki_gemm_kernel<<<grid, kOzThreads, kOzSmem, st>>>(tA, tB, p);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int ozaki_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+                const double *B, int ldb, double beta, double *C, int ldc, int slices, void *ws,
+                size_t ws_bytes, cudaStream_t st, unsigned *err) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  const int S = slices > 0 ? slices : ozaki_default_slices(m, n, k);
+  if (ck == GB300_ERR_ARG || S < 2 || S > kOzakiMaxSlices) return GB300_ERR_ARG;
+  if (ck < 0) return GB300_OK;
+  if (alpha == 0.0 || k == 0)
+    return plain_dgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err);
+  int rc = ozaki_prepare(ta, tb, m, n, k, A, lda, B, ldb, S, ws, ws_bytes, st);
+  if (rc != GB300_OK) return rc;
+  return ozaki_run(m, n, k, alpha, beta, C, ldc, S, ws, ws_bytes, st, err);
+}
+
+}  // namespace gb300

@@ -1,0 +1,159 @@
+/*
+ * gemm_gb300.h -- C ABI of the GB300 (sm_103a) GEMM library.
+ *
+ * Two layers:
+ *
+ *  1. The drop-in BLAS symbols.  DGEMM.so exports exactly `dgemm_`, SGEMM.so
+ *     exactly `sgemm_`, with the reference's Fortran-style signature and
+ *     semantics (wjc404/GEMM_AVX2 src/gemm_driver.c:118, README.md:10).  They
+ *     take HOST pointers, stage the operands through HBM, run the plain
+ *     FP64/FP32 kernels and return when C has been written back.
+ *
+ *  2. Device-pointer entry points in libgemm_gb300.so (prefix gb300_).  All
+ *     matrices are column-major device buffers; every call is stream-ordered
+ *     and asynchronous (the stream is a cudaStream_t passed as void*, NULL =
+ *     legacy default stream).  They return a gb300_status.  Operand
+ *     semantics are the reference's (see `dgemm_` below).
+ *
+ * Semantics shared by every entry point (src/gemm_driver.c:17-18,118-197):
+ *   - op(X) = X when trans is 'N' or 'n'; ANY other character means transpose.
+ *   - C = beta*C first (when beta != 1; beta == 0 still multiplies, so NaN/Inf
+ *     already in C propagate), then C += alpha*op(A)*op(B) when alpha != 0.
+ *     alpha == 0 therefore never reads A or B.
+ *   - m, n or k == 0 is valid.  Only the m x n window of C is written.
+ *   - Invalid arguments (negative sizes, lda/ldb/ldc smaller than the stored
+ *     rows, at least 1): the drop-in symbols return without touching C (the
+ *     reference has no argument checks; this is the safe reading of its
+ *     undefined behaviour); the gb300_ calls return GB300_ERR_ARG.
+ */
+#ifndef GEMM_GB300_H
+#define GEMM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GB300_OK = 0,
+  GB300_ERR_ARG = 1,         /* invalid size / leading dimension / option   */
+  GB300_ERR_CUDA = 2,        /* a CUDA runtime call failed                    */
+  GB300_ERR_TIMEOUT = 3,     /* a kernel's bounded wait expired (device error word set) */
+  GB300_ERR_NOMEM = 4,       /* device workspace could not be allocated       */
+  GB300_ERR_UNSUPPORTED = 5, /* option outside what this build implements     */
+  GB300_ERR_WORKSPACE = 6    /* caller-provided workspace too small           */
+} gb300_status;
+
+/* ------------------------------------------------------------------------
+ * 1. Drop-in symbols (DGEMM.so / SGEMM.so).
+ *    Replace: src/gemm_driver.c:118 (GEMM_DRIVER = dgemm_ / sgemm_, :8-14).
+ *    Synchronous; host pointers; 32-bit int sizes (LP64, no ILP64).
+ * ---------------------------------------------------------------------- */
+void dgemm_(const char *transa, const char *transb, const int *m, const int *n, const int *k,
+            const double *alpha, const double *a, const int *lda, const double *b,
+            const int *ldb, const double *beta, double *c, const int *ldc);
+void sgemm_(const char *transa, const char *transb, const int *m, const int *n, const int *k,
+            const float *alpha, const float *a, const int *lda, const float *b, const int *ldb,
+            const float *beta, float *c, const int *ldc);
+
+/* Host-pointer forms of the drop-in symbols with a status return
+ * (libgemm_gb300.so).  dgemm_/sgemm_ call these and drop the status.
+ * Replace: src/gemm_driver.c:118. */
+int gb300_host_dgemm(char transa, char transb, int m, int n, int k, double alpha, const double *a,
+                     int lda, const double *b, int ldb, double beta, double *c, int ldc);
+int gb300_host_sgemm(char transa, char transb, int m, int n, int k, float alpha, const float *a,
+                     int lda, const float *b, int ldb, float beta, float *c, int ldc);
+
+/* ------------------------------------------------------------------------
+ * 2. Device-pointer entry points (libgemm_gb300.so).
+ * ---------------------------------------------------------------------- */
+
+/* Plain native-precision forms: the same computation as dgemm_/sgemm_
+ * (src/gemm_driver.c:118-197) on device buffers.  FP64 runs on the FP64
+ * tensor path (DMMA), FP32 on the FFMA pipe. */
+int gb300_dgemm(char transa, char transb, int m, int n, int k, double alpha, const double *A,
+                int lda, const double *B, int ldb, double beta, double *C, int ldc,
+                void *stream);
+int gb300_sgemm(char transa, char transb, int m, int n, int k, float alpha, const float *A,
+                int lda, const float *B, int ldb, float beta, float *C, int ldc, void *stream);
+
+/* Split-precision SGEMM on the BF16 tensor cores (tcgen05, FP32 accumulation
+ * in TMEM).  No reference counterpart: a tensor-core form of sgemm_
+ * (src/gemm_driver.c:118) with the same operand semantics.
+ *   products = 3: A = Ah + Al, B = Bh + Bl (BF16 hi + BF16 lo of the residual),
+ *                 C += Ah*Bh + Ah*Bl + Al*Bh                  ("3xBF16")
+ *   products = 6: three BF16 terms per operand, all cross products whose
+ *                 order sum is <= 2                              ("6xBF16")
+ * Uses a device workspace of gb300_split_workspace_bytes() bytes, allocated
+ * and cached by the library (the _ws variant takes the caller's instead). */
+int gb300_sgemm_bf16x(char transa, char transb, int m, int n, int k, float alpha, const float *A,
+                      int lda, const float *B, int ldb, float beta, float *C, int ldc,
+                      int products, void *stream);
+int gb300_sgemm_bf16x_ws(char transa, char transb, int m, int n, int k, float alpha,
+                         const float *A, int lda, const float *B, int ldb, float beta, float *C,
+                         int ldc, int products, void *workspace, size_t workspace_bytes,
+                         void *stream);
+
+/* Ozaki-scheme DGEMM on the tensor cores.  No reference counterpart: a
+ * tensor-core form of dgemm_ (src/gemm_driver.c:118).  Rows of op(A) and
+ * columns of op(B) are scaled by powers of two and cut into `slices`
+ * signed 7-bit integer slices (int8 range, |v| <= 127); the slice products
+ * with i + j <= slices + 1 are accumulated exactly (integer-valued FP32 in
+ * TMEM over bounded K chunks, flushed into 32-bit integers) and recombined
+ * in FP64 with the fused alpha/beta epilogue.  slices in [2, 12]; 0 picks the
+ * autotuned default for the shape class. */
+int gb300_dgemm_ozaki(char transa, char transb, int m, int n, int k, double alpha,
+                      const double *A, int lda, const double *B, int ldb, double beta, double *C,
+                      int ldc, int slices, void *stream);
+int gb300_dgemm_ozaki_ws(char transa, char transb, int m, int n, int k, double alpha,
+                         const double *A, int lda, const double *B, int ldb, double beta,
+                         double *C, int ldc, int slices, void *workspace, size_t workspace_bytes,
+                         void *stream);
+
+/* Two-phase forms of the split GEMMs (no reference counterpart; the split of
+ * the reference's pack-then-compute structure, src/gemm_driver.c:157-188):
+ * _prepare writes the split/sliced operands of op(A), op(B) into the
+ * workspace; _run computes C = alpha*op(A)op(B) + beta*C from a workspace
+ * prepared for the same m, n, k and products/slices.  One prepared operand
+ * set can serve several _run calls (e.g. different alpha/beta/C). */
+int gb300_sgemm_bf16x_prepare(char transa, char transb, int m, int n, int k, const float *A,
+                              int lda, const float *B, int ldb, int products, void *workspace,
+                              size_t workspace_bytes, void *stream);
+int gb300_sgemm_bf16x_run(int m, int n, int k, float alpha, float beta, float *C, int ldc,
+                          int products, const void *workspace, size_t workspace_bytes,
+                          void *stream);
+int gb300_dgemm_ozaki_prepare(char transa, char transb, int m, int n, int k, const double *A,
+                              int lda, const double *B, int ldb, int slices, void *workspace,
+                              size_t workspace_bytes, void *stream);
+int gb300_dgemm_ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc,
+                          int slices, const void *workspace, size_t workspace_bytes,
+                          void *stream);
+
+/* Host-pointer (synchronous, staged through HBM) forms of the split GEMMs,
+ * with the drop-in's argument conventions (src/gemm_driver.c:118). */
+int gb300_host_sgemm_bf16x(char transa, char transb, int m, int n, int k, float alpha,
+                           const float *a, int lda, const float *b, int ldb, float beta, float *c,
+                           int ldc, int products);
+int gb300_host_dgemm_ozaki(char transa, char transb, int m, int n, int k, double alpha,
+                           const double *a, int lda, const double *b, int ldb, double beta,
+                           double *c, int ldc, int slices);
+
+/* Workspace needed by the split forms for one call of the given shape.
+ * kind = 0: sgemm_bf16x with `param` = products; kind = 1: dgemm_ozaki with
+ * `param` = slices. */
+size_t gb300_split_workspace_bytes(int kind, int m, int n, int k, int param);
+
+/* After a stream synchronisation: the first error code any kernel of this
+ * library recorded on the current device since the last clear (0 = none).
+ * Bounded waits that expired record codes 0x10-0x14.  clear != 0 resets it. */
+unsigned gb300_device_error(int clear);
+
+/* Library version string. */
+const char *gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GEMM_GB300_H */

@@ -1,0 +1,99 @@
+"""numpy restatements of the split-precision decompositions -- TEST INFRASTRUCTURE.
+
+These have no counterpart in the reference (the split forms are tensor-core
+forms of its sgemm_/dgemm_, src/gemm_driver.c:118); they restate the published
+methods so that the GPU split kernels can be checked bit for bit:
+
+* bf16_terms: x = t0 + t1 + t2 + r with t_i = RNE-to-BF16 of the running
+  residual (Henry, Tang & Heinecke, "Leveraging the bfloat16 AI datatype for
+  higher-precision computations", ARITH 2019).
+* ozaki_slices: row scaling by 2^-E (E from frexp of the row max) and
+  truncated 7-bit integer digits, x*2^-E = sum_s d_s 2^-7s + r, |d_s| <= 127
+  (error-free splitting of Ozaki, Ogita, Oishi & Rump 2012, with the integer
+  slices of Mukunoki, Ozaki, Ogita & Imamura, ISC 2020).
+* ozaki_gemm_model: the exact-integer product/recombination model of the GPU
+  kernel (slice products grouped by t = i + j, weight 2^-7t, FP64 folding from
+  the largest t down).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def bf16_round(x: np.ndarray) -> np.ndarray:
+    """Round float32 to the nearest bfloat16 (ties to even), returned as float32."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    b = x.view(np.uint32).astype(np.uint64)
+    lsb = (b >> 16) & 1
+    r = ((b + 0x7FFF + lsb) & 0xFFFF0000).astype(np.uint32)
+    out = r.view(np.float32).copy()
+    nan = np.isnan(x)
+    out[nan] = x[nan]
+    return out
+
+
+def bf16_terms(x: np.ndarray, nterms: int):
+    """[t0, t1, t2] (float32 arrays holding BF16 values); unused terms are 0."""
+    r = np.asarray(x, dtype=np.float32)
+    terms = []
+    for i in range(3):
+        if i < nterms:
+            t = bf16_round(r)
+            r = (r - t).astype(np.float32)
+        else:
+            t = np.zeros_like(r)
+        terms.append(t)
+    return terms
+
+
+# segment -> term index, for the A and B operands (smallest products first)
+SEGMENTS = {
+    3: ([1, 0, 0], [0, 1, 0]),
+    6: ([2, 1, 0, 1, 0, 0], [0, 1, 2, 0, 1, 0]),
+}
+
+
+def bf16x_operand(X: np.ndarray, products: int, is_a: bool) -> np.ndarray:
+    """The concatenated K-major operand (R x P*K, float32 holding BF16) of an
+    R x K op(X) view."""
+    nterms = 2 if products == 3 else 3
+    terms = bf16_terms(np.asarray(X, np.float32), nterms)
+    seg = SEGMENTS[products][0 if is_a else 1]
+    return np.concatenate([terms[t] for t in seg], axis=1)
+
+
+def row_exponents(X: np.ndarray) -> np.ndarray:
+    """E_r with max_k |X[r,k]| * 2^-E_r < 1 (frexp exponent of the row max; 0 for zero rows)."""
+    m = np.abs(np.asarray(X, np.float64)).max(axis=1) if X.shape[1] else np.zeros(X.shape[0])
+    e = np.frexp(m)[1].astype(np.int64)
+    e[m == 0] = 0
+    return e
+
+
+def ozaki_slices(X: np.ndarray, S: int):
+    """(slices, E): slices[s] is an R x K float64 array of integers in [-127, 127]."""
+    X = np.asarray(X, np.float64)
+    E = row_exponents(X)
+    x = np.ldexp(X, -E[:, None])
+    out = []
+    for _ in range(S):
+        y = x * 128.0
+        d = np.trunc(y)
+        x = y - d
+        out.append(d)
+    return out, E
+
+
+def ozaki_gemm_model(A_op: np.ndarray, B_op: np.ndarray, S: int) -> np.ndarray:
+    """op(A) @ op(B) as computed by the Ozaki kernel: exact integer group sums,
+    weight 2^-7t, FP64 folding from t = S+1 down to 2, then 2^(E_i + F_j)."""
+    As, E = ozaki_slices(A_op, S)
+    Bs, F = ozaki_slices(B_op.T, S)
+    res = np.zeros((A_op.shape[0], B_op.shape[1]))
+    for t in range(S + 1, 1, -1):
+        P = np.zeros_like(res, dtype=object) if False else np.zeros(res.shape, dtype=np.int64)
+        for sa in range(max(1, t - S), min(S, t - 1) + 1):
+            sb = t - sa
+            P += (As[sa - 1].astype(np.int64) @ Bs[sb - 1].astype(np.int64).T)
+        res = P.astype(np.float64) * 2.0 ** (-7 * t) + res
+    return np.ldexp(res, (E[:, None] + F[None, :]).astype(np.int64))

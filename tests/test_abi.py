@@ -1,0 +1,93 @@
+"""CPU tests of the C-ABI boundary: the libraries load, export exactly what
+include/*.h declares (the drop-in libraries exactly one symbol each, like the
+reference's DGEMM.so/SGEMM.so), and report argument errors without a GPU."""
+import os
+import re
+import subprocess
+
+import pytest
+
+import gemm_avx2_gb300 as g
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def exported(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True,
+                         check=True).stdout
+    return {l.split()[-1] for l in out.splitlines() if re.match(r"^[0-9a-f]+ [TW] ", l)}
+
+
+def header_functions():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b((?:gb300_|[ds]gemm_)\w*)\s*\(", src))
+    return names
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    if not os.path.exists(os.path.join(g.PKG, "libgemm_gb300.so")):
+        g.build()
+
+
+def test_dropin_exports_exactly_one_symbol():
+    assert exported(os.path.join(g.PKG, "DGEMM.so")) == {"dgemm_"}
+    assert exported(os.path.join(g.PKG, "SGEMM.so")) == {"sgemm_"}
+
+
+def test_core_exports_every_declared_function():
+    decl = header_functions()
+    assert {"dgemm_", "sgemm_", "gb300_dgemm", "gb300_sgemm"} <= decl
+    core = exported(os.path.join(g.PKG, "libgemm_gb300.so"))
+    dropin = exported(os.path.join(g.PKG, "DGEMM.so")) | exported(os.path.join(g.PKG, "SGEMM.so"))
+    missing = {n for n in decl if n not in core and n not in dropin}
+    assert not missing, missing
+    # nothing but the declared ABI is exported from the core library
+    extra = {n for n in core if n.startswith("gb300_")} - decl
+    assert not extra, extra
+    assert set(g.CORE_SYMBOLS) <= core
+
+
+def test_libraries_load_and_version():
+    assert "sm_103a" in g.version()
+    g.dropin("d")
+    g.dropin("s")
+
+
+def test_argument_errors_need_no_gpu():
+    # invalid sizes / leading dimensions are rejected before any CUDA call
+    assert g.gemm_device("d", "N", "N", -1, 4, 4, 1.0, 0, 4, 0, 4, 0.0, 0, 4) == g.ERR_ARG
+    assert g.gemm_device("s", "N", "N", 8, 4, 4, 1.0, 0, 7, 0, 4, 0.0, 0, 8) == g.ERR_ARG
+    assert g.gemm_device("s", "T", "N", 8, 4, 4, 1.0, 0, 3, 0, 4, 0.0, 0, 8) == g.ERR_ARG
+    assert g.gemm_device("d", "N", "T", 8, 4, 4, 1.0, 0, 8, 0, 3, 0.0, 0, 8) == g.ERR_ARG
+    assert g.gemm_device("d", "N", "N", 8, 4, 4, 1.0, 0, 8, 0, 4, 0.0, 0, 7) == g.ERR_ARG
+    assert g.sgemm_bf16x("N", "N", 8, 8, 8, 1.0, 0, 8, 0, 8, 0.0, 0, 8, products=4) == g.ERR_ARG
+    assert g.dgemm_ozaki("N", "N", 8, 8, 8, 1.0, 0, 8, 0, 8, 0.0, 0, 8, slices=1) == g.ERR_ARG
+    assert g.dgemm_ozaki("N", "N", 8, 8, 8, 1.0, 0, 8, 0, 8, 0.0, 0, 8, slices=13) == g.ERR_ARG
+    # empty problems are valid no-ops
+    assert g.gemm_device("d", "N", "N", 0, 4, 4, 1.0, 0, 1, 0, 4, 0.0, 0, 1) == g.OK
+
+
+def test_workspace_sizes():
+    assert g.split_workspace_bytes(0, 0, 8, 8, 3) == 0
+    w3 = g.split_workspace_bytes(0, 8192, 8192, 8192, 3)
+    w6 = g.split_workspace_bytes(0, 8192, 8192, 8192, 6)
+    assert w3 >= (8192 + 8192) * 3 * 8192 * 2 and w6 >= 2 * w3 - 4096
+    assert g.split_workspace_bytes(0, 10, 10, 10, 5) == 0
+    wo = g.split_workspace_bytes(1, 1000, 1000, 1000, 8)
+    assert wo >= 8 * (1024 + 1024) * 1024 * 2
+
+
+def test_dropin_invalid_args_leave_c_untouched():
+    import numpy as np
+    c = np.arange(12, dtype=np.float64).reshape(3, 4, order="F").copy(order="F")
+    before = c.copy()
+    a = np.ones((3, 3), order="F")
+    g.dgemm("N", "N", 3, 4, 3, 1.0, a, 2, a, 3, 0.0, c, 3)  # lda < m
+    assert np.array_equal(c, before)
+    g.dgemm("N", "N", 3, -4, 3, 1.0, a, 3, a, 3, 0.0, c, 3)
+    assert np.array_equal(c, before)

@@ -1,0 +1,177 @@
+"""GPU tests of the tensor-core split forms (tcgen05): bit-exact split/slice
+kernels against the numpy restatement, and accuracy against the Dot2 oracle."""
+import numpy as np
+import pytest
+
+import gemm_avx2_gb300 as g
+from gpu_util import from_dev, sync, to_dev, torch_cuda
+from oracle import split as osp
+from util import op
+
+pytestmark = pytest.mark.gpu
+
+
+def ru(x, a):
+    return (x + a - 1) // a * a
+
+
+def ws_tensor(nbytes):
+    torch = torch_cuda()
+    return torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+
+
+def aligned_view(ws, nbytes_needed_from):
+    base = ws.data_ptr()
+    off = (-base) % 1024
+    return off
+
+
+def rel_errs(x, truth):
+    d = np.abs(np.asarray(x, np.float64) - truth)
+    fro = np.linalg.norm(d) / np.linalg.norm(truth)
+    mx = np.max(d / np.maximum(np.abs(truth), 1e-300))
+    return mx, fro
+
+
+@pytest.mark.parametrize("products", [3, 6])
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+def test_bf16x_split_bitexact_and_result(orc, products, ta, tb):
+    m, n, k = 200, 300, 100
+    ar, ac = (m, k) if ta == "N" else (k, m)
+    br, bc = (k, n) if tb == "N" else (n, k)
+    A = orc.uniform((ar + 1, ac), np.float32, 11, 0)
+    B = orc.uniform((br + 3, bc), np.float32, 11, 1)
+    C = orc.uniform((m, n), np.float32, 11, 2)
+    need = g.split_workspace_bytes(0, m, n, k, products)
+    ws = ws_tensor(need)
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
+    rc = g.sgemm_bf16x(ta, tb, m, n, k, 1.0, dA.data_ptr(), ar + 1, dB.data_ptr(), br + 3, 0.5,
+                       dC.data_ptr(), m, products=products, workspace=ws.data_ptr(),
+                       workspace_bytes=need)
+    assert rc == g.OK
+    sync()
+    # workspace: A' (Mp x P*Kp) then B' (Np x P*Kp), BF16, from the first 1024-aligned byte
+    Kp = ru(k, 64)
+    Mp, Np = ru(m, 128), ru(n, 256)
+    off = aligned_view(ws, need)
+    raw = ws.cpu().numpy()[off:]
+    kld = products * Kp
+    bf = raw[:2 * (Mp + Np) * kld].view(np.uint16).astype(np.uint32) << 16
+    vals = bf.view(np.float32)
+    Ap = vals[:Mp * kld].reshape(Mp, kld)
+    Bp = vals[Mp * kld:(Mp + Np) * kld].reshape(Np, kld)
+    Aop = np.zeros((Mp, Kp), np.float32)
+    Aop[:m, :k] = op(A, ta, m, k)
+    Bop = np.zeros((Np, Kp), np.float32)
+    Bop[:n, :k] = op(B, tb, k, n).T
+    assert np.array_equal(Ap.view(np.uint32), osp.bf16x_operand(Aop, products, True).view(np.uint32))
+    assert np.array_equal(Bp.view(np.uint32), osp.bf16x_operand(Bop, products, False).view(np.uint32))
+    # result vs Dot2 truth
+    got = from_dev(dC, m)
+    truth = orc.dot2gemm(ta, tb, m, n, k, 1.0, A, ar + 1, B, br + 3, 0.5, C, m)
+    mx, fro = rel_errs(got, truth)
+    assert fro < (2e-5 if products == 3 else 2e-7), (mx, fro)
+    assert g.device_error() == 0
+
+
+@pytest.mark.parametrize("products", [3, 6])
+def test_bf16x_multi_tile_ragged(orc, products):
+    m, n, k = 300, 520, 333
+    A = orc.uniform((k, m), np.float32, 12, 0)   # transa = T
+    B = orc.uniform((k, n), np.float32, 12, 1)   # transb = N
+    C = orc.uniform((m + 5, n), np.float32, 12, 2)
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
+    assert g.sgemm_bf16x("T", "N", m, n, k, -1.0, dA.data_ptr(), k, dB.data_ptr(), k, 1.0,
+                         dC.data_ptr(), m + 5, products=products) == g.OK
+    sync()
+    got = from_dev(dC, m + 5)
+    truth = orc.dot2gemm("T", "N", m, n, k, -1.0, A, k, B, k, 1.0, C, m + 5)
+    mx, fro = rel_errs(got[:m], truth)
+    assert fro < (2e-5 if products == 3 else 2e-7), (mx, fro)
+    assert np.array_equal(got[m:], C[m:])
+
+
+@pytest.mark.parametrize("S", [4, 8])
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+def test_ozaki_slices_bitexact_and_result(orc, S, ta, tb):
+    m, n, k = 150, 140, 200
+    ar, ac = (m, k) if ta == "N" else (k, m)
+    br, bc = (k, n) if tb == "N" else (n, k)
+    A = orc.spread((ar + 2, ac), 21, 0, 1.0)
+    B = orc.spread((br, bc), 21, 1, 1.0)
+    C = orc.uniform((m, n), np.float64, 21, 2)
+    need = g.split_workspace_bytes(1, m, n, k, S)
+    ws = ws_tensor(need)
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
+    rc = g.dgemm_ozaki(ta, tb, m, n, k, 1.0, dA.data_ptr(), ar + 2, dB.data_ptr(), br, 0.0,
+                       dC.data_ptr(), m, slices=S, workspace=ws.data_ptr(), workspace_bytes=need)
+    assert rc == g.OK
+    sync()
+    Kp, Mp, Np = ru(k, 64), ru(m, 128), ru(n, 128)
+    off = aligned_view(ws, need)
+    raw = ws.cpu().numpy()[off:]
+    bf = raw[:2 * S * (Mp + Np) * Kp].view(np.uint16).astype(np.uint32) << 16
+    vals = bf.view(np.float32).astype(np.float64)
+    As = vals[:S * Mp * Kp].reshape(S, Mp, Kp)
+    Bs = vals[S * Mp * Kp:].reshape(S, Np, Kp)
+    Aop = op(A, ta, m, k)
+    Bop = op(B, tb, k, n)
+    sa, E = osp.ozaki_slices(Aop, S)
+    sb, F = osp.ozaki_slices(Bop.T, S)
+    for s in range(S):
+        assert np.array_equal(As[s, :m, :k], sa[s])
+        assert np.array_equal(Bs[s, :n, :k], sb[s])
+        assert not As[s, m:, :].any() and not As[s, :, k:].any()
+    got = from_dev(dC, m)
+    model = osp.ozaki_gemm_model(Aop, Bop, S)
+    # the kernel's integer sums are exact, so it matches the model up to the
+    # FP64 rounding of the final alpha/beta update
+    assert np.allclose(got, model, rtol=4e-16, atol=0), np.abs(got - model).max()
+    truth = orc.dot2gemm(ta, tb, m, n, k, 1.0, A, ar + 2, B, br, 0.0, C, m)
+    mx, fro = rel_errs(got, truth)
+    assert fro < (2.0 ** (-7 * S + 12)), (mx, fro)
+    assert g.device_error() == 0
+
+
+def test_ozaki_vs_plain_accuracy(orc):
+    """At S = 8 the Ozaki form is as accurate as the plain FP64 kernel (uniform data)."""
+    m = n = 384
+    k = 2048
+    A = orc.uniform((m, k), np.float64, 31, 0)
+    B = orc.uniform((n, k), np.float64, 31, 1)
+    C = orc.uniform((m, n), np.float64, 31, 2)
+    dA, dB = to_dev(A), to_dev(B)
+    dC1, dC2 = to_dev(C), to_dev(C)
+    assert g.dgemm_ozaki("N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 1.0,
+                         dC1.data_ptr(), m, slices=8) == g.OK
+    assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 1.0,
+                         dC2.data_ptr(), m) == g.OK
+    sync()
+    truth = orc.dot2gemm("N", "T", m, n, k, 1.0, A, m, B, n, 1.0, C, m)
+    e_oz = rel_errs(from_dev(dC1, m), truth)
+    e_pl = rel_errs(from_dev(dC2, m), truth)
+    assert e_oz[1] <= 4 * e_pl[1] + 1e-16, (e_oz, e_pl)
+
+
+def test_ozaki_edge_semantics(orc):
+    m, n, k = 70, 50, 30
+    A = orc.uniform((m, k), np.float64, 41, 0)
+    B = orc.uniform((k, n), np.float64, 41, 1)
+    C = np.ones((m, n), order="F")
+    C[2, 3] = np.nan
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
+    # alpha == 0 -> beta scaling only
+    assert g.dgemm_ozaki("N", "N", m, n, k, 0.0, dA.data_ptr(), m, dB.data_ptr(), k, 2.0,
+                         dC.data_ptr(), m, slices=6) == g.OK
+    sync()
+    got = from_dev(dC, m)
+    assert np.isnan(got[2, 3]) and np.all(got[~np.isnan(got)] == 2.0)
+    # a NaN in A's row 5 poisons C's row 5
+    A2 = A.copy(order="F")
+    A2[5, 7] = np.nan
+    dA2, dC = to_dev(A2), to_dev(np.zeros((m, n), order="F"))
+    assert g.dgemm_ozaki("N", "N", m, n, k, 1.0, dA2.data_ptr(), m, dB.data_ptr(), k, 0.0,
+                         dC.data_ptr(), m, slices=6) == g.OK
+    sync()
+    got = from_dev(dC, m)
+    assert np.isnan(got[5]).all() and np.isfinite(np.delete(got, 5, axis=0)).all()
