@@ -1,0 +1,519 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 sgemm_/dgemm_ path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME]
+
+Metric: GEMM TFLOP/s (2*m*n*k per second) on one GB300 of the tensor-core
+split form at equal error to the native FP32/FP64 kernel.  A step is one call
+of the split form (split kernels + tcgen05 GEMM) over the workload's inputs,
+already resident in HBM.  The default workload is SGEMM TN m=n=k=8192,
+alpha=1, beta=0 (the configuration the metric is quoted on); the split form
+(3xBF16 or 6xBF16) is the smallest one whose max relative error on sampled
+entries does not exceed the plain FP32 kernel's.
+
+Printed JSON line (rank 0): metric/value/unit, ms_per_step, e2e (the same
+metric through the host-pointer C ABI with host<->device copies inside the
+timed region), roofline of the dominant kernel (the tcgen05 GEMM), the plain
+kernel's TFLOP/s and errors of both forms against exact sampled dot products,
+clocks sampled during the timed region, gpu_launches, and a CPU baseline.
+
+--impl reference times the reference's CPU implementation of the same
+workload on the host cores (the reference library compiled from its sources
+when this host can run it, else the oracle's C restatement of its algorithm)
+on a bounded column sample of the workload.
+
+N > 1 (torchrun): every rank runs the same single-GPU workload (the path
+shards by whole problems; replicas only), value = sum over ranks of the work /
+max over ranks of the time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # configs: SGEMM TN 8192^3 (the metric's configuration), DGEMM NN 2048^3,
+    # DGEMM NT 16384^3 (phi = 0), rank-256 updates with padded ld.
+    "sgemm_tn_8192": dict(prec="s", ta="T", tb="N", m=8192, n=8192, k=8192, lda=8192, ldb=8192,
+                          ldc=8192, alpha=1.0, beta=0.0, seed=1),
+    "dgemm_nn_2048": dict(prec="d", ta="N", tb="N", m=2048, n=2048, k=2048, lda=2048, ldb=2048,
+                          ldc=2048, alpha=1.0, beta=0.5, seed=0),
+    "dgemm_nt_16384": dict(prec="d", ta="N", tb="T", m=16384, n=16384, k=16384, lda=16384,
+                           ldb=16384, ldc=16384, alpha=1.0, beta=1.0, seed=2),
+    "rank256_d": dict(prec="d", ta="N", tb="T", m=32768, n=32768, k=256, lda=32800, ldb=32800,
+                      ldc=32832, alpha=-1.0, beta=1.0, seed=3),
+    "rank256_s": dict(prec="s", ta="N", tb="T", m=32768, n=32768, k=256, lda=32800, ldb=32800,
+                      ldc=32832, alpha=-1.0, beta=1.0, seed=3),
+}
+METRIC = "GEMM TFLOP/s on 1 GB300: tensor-core split vs native FP64/FP32, at equal error"
+L2_BYTES = 129 * 2**20
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "bf16_tflops": d.get("bf16_tflops", 1900.0),
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", 1700.0),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+            "source": "fallback"}
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = max((float(r[2]) for r in rows if r[2].replace(".", "").isdigit()), default=None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- exact samples
+def _two_prod(a, b):
+    """Dekker/Veltkamp TwoProduct without FMA: a*b = p + e exactly (numpy float64)."""
+    import numpy as np
+
+    p = a * b
+    c = 134217729.0
+    t = c * a
+    ah = t - (t - a)
+    al = a - ah
+    t = c * b
+    bh = t - (t - b)
+    bl = b - bh
+    e = ((ah * bh - p) + ah * bl + al * bh) + al * bl
+    return p, np.asarray(e)
+
+
+def exact_samples(A_rows, B_cols, alpha, beta, c0):
+    """Correctly rounded alpha*dot + beta*c for each sampled (row of op(A), column of op(B))."""
+    import numpy as np
+
+    out = np.empty(A_rows.shape[0])
+    for q in range(A_rows.shape[0]):
+        p, e = _two_prod(A_rows[q].astype(np.float64), B_cols[q].astype(np.float64))
+        dot = math.fsum(np.concatenate([p, e]).tolist())
+        out[q] = math.fsum([alpha * dot, beta * float(c0[q])])
+    return out
+
+
+def rel_err(got, truth):
+    import numpy as np
+
+    d = np.abs(np.asarray(got, np.float64) - truth)
+    mx = float(np.max(d / np.maximum(np.abs(truth), 1e-300)))
+    fro = float(np.linalg.norm(d) / max(np.linalg.norm(truth), 1e-300))
+    return mx, fro
+
+
+# ----------------------------------------------------------------------------- workload
+class Problem:
+    """Device-resident operands of one workload (column-major, seeded U[-1,1))."""
+
+    def __init__(self, torch, w):
+        self.w = w
+        dt = torch.float64 if w["prec"] == "d" else torch.float32
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(int(w["seed"]))
+        ar, ac = (w["m"], w["k"]) if w["ta"] == "N" else (w["k"], w["m"])
+        br, bc = (w["k"], w["n"]) if w["tb"] == "N" else (w["n"], w["k"])
+        self.ar, self.ac, self.br, self.bc = ar, ac, br, bc
+        # column-major ld x cols buffers are stored as row-major (cols, ld) tensors
+        self.A = torch.rand((ac, w["lda"]), generator=gen, device="cuda", dtype=dt) * 2 - 1
+        self.B = torch.rand((bc, w["ldb"]), generator=gen, device="cuda", dtype=dt) * 2 - 1
+        self.C0 = torch.rand((w["n"], w["ldc"]), generator=gen, device="cuda", dtype=dt) * 2 - 1
+        if w["beta"] == 0.0:
+            self.C0.zero_()
+        self.C = self.C0.clone()
+        self.flops = 2.0 * w["m"] * w["n"] * w["k"]
+
+    def opA_rows(self, rows):
+        A = self.A[:, :self.ar] if True else None  # (cols, ld) -> element (r, c) = A[c, r]
+        if self.w["ta"] == "N":   # op(A)[i, :] = A[i, 0:k] -> tensor[0:k, i]
+            return A[:, rows].T.cpu().numpy()
+        return A[rows, :].cpu().numpy()  # op(A)[i, :] = A^T[i, :] = stored column i
+
+    def opB_cols(self, cols):
+        B = self.B[:, :self.br]
+        if self.w["tb"] == "N":   # op(B)[:, j] = stored column j
+            return B[cols, :].cpu().numpy()
+        return B[:, cols].T.cpu().numpy()  # op(B)[:, j] = stored row j
+
+
+def sample_truth(prob, n_samples=1024):
+    import numpy as np
+
+    w = prob.w
+    rng = np.random.default_rng(99)
+    rows = rng.integers(0, w["m"], n_samples)
+    cols = rng.integers(0, w["n"], n_samples)
+    Ar = prob.opA_rows(rows)
+    Bc = prob.opB_cols(cols)
+    c0 = prob.C0[cols, rows].cpu().numpy()
+    return rows, cols, exact_samples(Ar, Bc, w["alpha"], w["beta"], c0)
+
+
+# ----------------------------------------------------------------------------- our arm
+def run_ours(args, torch, rank, world):
+    import numpy as np
+
+    import gemm_avx2_gb300 as g
+
+    w = WORKLOADS[args.workload]
+    prob = Problem(torch, w)
+    stream = torch.cuda.current_stream().cuda_stream
+    is_d = w["prec"] == "d"
+    form = "ozaki" if is_d else "bf16x"
+    m, n, k = w["m"], w["n"], w["k"]
+
+    def plain_call(C):
+        return g.gemm_device(w["prec"], w["ta"], w["tb"], m, n, k, w["alpha"], prob.A.data_ptr(),
+                             w["lda"], prob.B.data_ptr(), w["ldb"], w["beta"], C.data_ptr(),
+                             w["ldc"], stream)
+
+    # ---- accuracy of the plain kernel and of the split candidates (sampled, exact truth)
+    rows, cols, truth = sample_truth(prob)
+    prob.C.copy_(prob.C0)
+    assert plain_call(prob.C) == g.OK
+    torch.cuda.synchronize()
+    plain_err = rel_err(prob.C[cols, rows].cpu().numpy(), truth)
+    cands = list(range(6, 13)) if is_d else [3, 6]
+    chosen, errs = None, {}
+    ws = None
+    for param in cands:
+        need = g.split_workspace_bytes(1 if is_d else 0, m, n, k, param)
+        if ws is None or ws.numel() < need:
+            ws = torch.empty(need, dtype=torch.uint8, device="cuda")
+        prob.C.copy_(prob.C0)
+        assert g.split_prepare(form, w["ta"], w["tb"], m, n, k, prob.A.data_ptr(), w["lda"],
+                               prob.B.data_ptr(), w["ldb"], param, ws.data_ptr(), need,
+                               stream) == g.OK
+        assert g.split_run(form, m, n, k, w["alpha"], w["beta"], prob.C.data_ptr(), w["ldc"],
+                           param, ws.data_ptr(), need, stream) == g.OK
+        torch.cuda.synchronize()
+        errs[param] = rel_err(prob.C[cols, rows].cpu().numpy(), truth)
+        if errs[param][0] <= plain_err[0]:
+            chosen = param
+            break
+    if chosen is None:
+        chosen = cands[-1]
+    param = chosen
+    need = g.split_workspace_bytes(1 if is_d else 0, m, n, k, param)
+
+    # ---- timed region: W warm-up + K steps of prepare + run, inputs resident in HBM
+    def step(ev0=None, ev1=None, ev2=None):
+        if ev0 is not None:
+            ev0.record()
+        rc = g.split_prepare(form, w["ta"], w["tb"], m, n, k, prob.A.data_ptr(), w["lda"],
+                             prob.B.data_ptr(), w["ldb"], param, ws.data_ptr(), need, stream)
+        if ev1 is not None:
+            ev1.record()
+        rc |= g.split_run(form, m, n, k, w["alpha"], w["beta"], prob.C.data_ptr(), w["ldc"],
+                          param, ws.data_ptr(), need, stream)
+        if ev2 is not None:
+            ev2.record()
+        return rc
+
+    for _ in range(args.warmup):
+        assert step() == g.OK
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    barrier(torch, world)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for s in range(args.steps):
+        assert step(*evs[s]) == g.OK
+    t1.record()
+    torch.cuda.synchronize()
+    barrier(torch, world)
+    clocks = sampler.stop() if sampler else None
+    total_ms = t0.elapsed_time(t1)
+    gemm_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
+    prep_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
+    max_ms = allreduce_max(torch, world, total_ms)
+    value = prob.flops * args.steps * world / (max_ms / 1e3) / 1e12
+    assert g.device_error() == 0
+
+    # ---- plain kernel throughput (same workload)
+    for _ in range(2):
+        plain_call(prob.C)
+    torch.cuda.synchronize()
+    reps = 3 if not (is_d and m >= 16384) else 1
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record()
+    for _ in range(reps):
+        plain_call(prob.C)
+    a1.record()
+    torch.cuda.synchronize()
+    plain_ms = a0.elapsed_time(a1) / reps
+    plain_tflops = prob.flops / (plain_ms / 1e3) / 1e12
+
+    # ---- end to end through the host-pointer C ABI (pinned host buffers)
+    e2e = None
+    try:
+        hA = torch.empty(prob.A.shape, dtype=prob.A.dtype, pin_memory=True)
+        hB = torch.empty(prob.B.shape, dtype=prob.B.dtype, pin_memory=True)
+        hC = torch.empty(prob.C0.shape, dtype=prob.C0.dtype, pin_memory=True)
+        hA.copy_(prob.A)
+        hB.copy_(prob.B)
+        hC.copy_(prob.C0)
+        ah, bh, ch = hA.numpy(), hB.numpy(), hC.numpy()
+        for _ in range(2):
+            assert g.host_split_gemm(form, w["ta"], w["tb"], m, n, k, w["alpha"], ah, w["lda"],
+                                     bh, w["ldb"], w["beta"], ch, w["ldc"], param) == g.OK
+        steps_e2e = max(3, min(args.steps, 10))
+        t = time.perf_counter()
+        for _ in range(steps_e2e):
+            assert g.host_split_gemm(form, w["ta"], w["tb"], m, n, k, w["alpha"], ah, w["lda"],
+                                     bh, w["ldb"], w["beta"], ch, w["ldc"], param) == g.OK
+        dt = (time.perf_counter() - t) / steps_e2e
+        esz = 8 if is_d else 4
+        h2d = (prob.ar * prob.ac + prob.br * prob.bc + m * n) * esz
+        e2e = {"value": round(prob.flops / dt / 1e12, 3), "unit": "TFLOP/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": m * n * esz,
+               "ms_per_step": round(dt * 1e3, 3), "api": "gb300_host_%s" %
+               ("dgemm_ozaki" if is_d else "sgemm_bf16x")}
+    except Exception as ex:  # noqa: BLE001
+        e2e = {"value": None, "error": repr(ex)}
+
+    # ---- roofline of the dominant kernel (the tcgen05 GEMM of the split form)
+    pk = peaks()
+    products = (param * (param + 1)) // 2 if is_d else param
+    pipe_flops = products * prob.flops
+    achieved = pipe_flops / (gemm_ms / 1e3) / 1e12
+    roof = {"bound": "tensor", "achieved": round(achieved, 2), "peak": pk["bf16_tflops"],
+            "unit": "TFLOP/s", "frac": round(achieved / pk["bf16_tflops"], 4),
+            "traffic": traffic_from_profile(args.workload, param),
+            "kernel": "ozaki_gemm_kernel" if is_d else "bf16x_gemm_kernel",
+            "kernel_ms": round(gemm_ms, 4), "prepare_ms": round(prep_ms, 4),
+            "peak_source": "%s bf16 burst (MEASURED_PEAKS.json)" % pk["source"],
+            "algorithmic_flops_per_launch": pipe_flops}
+    form_name = ("ozaki_s%d" % param) if is_d else ("bf16x%d" % param)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(max_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if is_d else "f32",
+        "data": "synthetic (seeded uniform[-1,1), generated on the device)",
+        "config": {"workload": args.workload, "transa": w["ta"], "transb": w["tb"], "m": m,
+                   "n": n, "k": k, "lda": w["lda"], "ldb": w["ldb"], "ldc": w["ldc"],
+                   "alpha": w["alpha"], "beta": w["beta"], "form": form_name,
+                   "l2": "inputs larger than L2 (%d MB per operand > %d MB)" % (
+                       prob.A.numel() * prob.A.element_size() // 2**20, L2_BYTES // 2**20),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": e2e,
+        "roofline": roof,
+        "plain": {"kernel": "dgemm_plain (DMMA)" if is_d else "sgemm_plain (FFMA)",
+                  "value": round(plain_tflops, 3), "unit": "TFLOP/s",
+                  "ms": round(plain_ms, 3), "split_speedup": round(value / world / plain_tflops, 3)},
+        "accuracy": {"samples": int(len(truth)), "truth": "exact sampled dot products",
+                     "plain_max_rel": plain_err[0], "plain_fro_rel": plain_err[1],
+                     "split": {str(p): {"max_rel": e[0], "fro_rel": e[1]} for p, e in errs.items()},
+                     "chosen": form_name},
+        "clocks": clocks,
+        "gpu_launches": args.steps * (3 if not is_d else 5),
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+
+
+def traffic_from_profile(workload, param):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        v = d.get("%s:%s" % (workload, param))
+        if v is not None:
+            return v
+    return None
+
+
+# ----------------------------------------------------------------------------- CPU side
+def cpu_gemm_callable():
+    """(kind, cores, f): the reference library when it runs on this host, else the
+    oracle's C restatement of its algorithm ("port")."""
+    import oracle
+
+    lib = os.path.join(ROOT, "oracle", "liborc.so")
+    if not os.path.exists(lib):
+        oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    if oracle.RefLib.available():
+        ref = oracle.RefLib()
+        return "reference", cores, lambda *a: ref.gemm(*a)
+    return "port", cores, lambda *a: oracle.refgemm(*a, cores)
+
+
+def cpu_sample_rate(w, seconds):
+    """TFLOP/s of the CPU implementation on a column sample of the workload."""
+    import numpy as np
+
+    import oracle
+
+    kind, cores, f = cpu_gemm_callable()
+    dt = np.float64 if w["prec"] == "d" else np.float32
+    m, k = w["m"], w["k"]
+    ar, ac = (m, k) if w["ta"] == "N" else (k, m)
+    A = oracle.storage(ar, ac, w["lda"], dt, w["seed"], 0)
+
+    def run(ns):
+        br, bc = (k, ns) if w["tb"] == "N" else (ns, k)
+        B = oracle.storage(br, bc, max(br, 1), dt, w["seed"], 1)
+        C = oracle.storage(m, ns, w["ldc"], dt, w["seed"], 2)
+        t = time.perf_counter()
+        f(w["ta"], w["tb"], m, ns, k, w["alpha"], A, w["lda"], B, max(br, 1), w["beta"], C,
+          w["ldc"])
+        return time.perf_counter() - t
+
+    ns = 16
+    dt0 = run(ns)
+    ns = int(min(w["n"], max(16, ns * seconds / max(dt0, 1e-3))))
+    t = run(ns)
+    tf = 2.0 * m * ns * k / t / 1e12
+    sample = "%s%s m=%d n=%d (of %d) k=%d, %d columns of C" % (
+        w["ta"], w["tb"], m, ns, w["n"], k, ns)
+    return kind, cores, tf, t, sample
+
+
+def cpu_baseline(w, seconds):
+    try:
+        kind, cores, tf, t, sample = cpu_sample_rate(w, seconds)
+        return {"value": round(tf, 5), "unit": "TFLOP/s", "cores": cores, "kind": kind,
+                "sample": sample, "seconds": round(t, 2)}
+    except Exception as ex:  # noqa: BLE001
+        return {"value": None, "error": repr(ex)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    w = WORKLOADS[args.workload]
+    per_step = max(1.0, min(10.0, 120.0 / max(1, args.steps + args.warmup)))
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        kind, cores, tf, t, sample = cpu_sample_rate(w, per_step)
+        if i >= args.warmup:
+            vals.append((tf, t))
+        info = (kind, cores, sample)
+    tf = sum(v[0] for v in vals) / len(vals)
+    line = {"metric": METRIC, "value": round(tf, 5), "unit": "TFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * sum(v[1] for v in vals) / len(vals), 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if w["prec"] == "d" else "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "transa": w["ta"], "transb": w["tb"],
+                       "m": w["m"], "n": w["n"], "k": w["k"]},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(tf, 5), "unit": "TFLOP/s", "cores": info[1],
+                             "kind": info[0], "sample": info[2]},
+            "e2e": {"value": round(tf, 5), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- distributed
+def barrier(torch, world):
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def allreduce_max(torch, world, v):
+    if world <= 1:
+        return v
+    t = torch.tensor([v], dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sgemm_tn_8192")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
+    run_ours(args, torch, rank, world)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -99,6 +99,7 @@ def core() -> ctypes.CDLL:
         L.gb300_device_error.argtypes = [c_int]
         L.gb300_device_error.restype = c_uint
         L.gb300_version.restype = ctypes.c_char_p
+        L.gb300_selftest_wait_timeout.argtypes = [c_uint]
         _core = L
     return _core
 
@@ -230,6 +231,11 @@ def device_error(clear: bool = False) -> int:
     return core().gb300_device_error(1 if clear else 0)
 
 
+def selftest_wait_timeout(poll_limit: int = 4096) -> int:
+    """Bounded-wait self-test: a kernel waits on an mbarrier nothing arrives on."""
+    return core().gb300_selftest_wait_timeout(poll_limit)
+
+
 def version() -> str:
     return core().gb300_version().decode()
 
@@ -241,4 +247,5 @@ CORE_SYMBOLS = [
     "gb300_split_workspace_bytes", "gb300_device_error", "gb300_version",
     "gb300_sgemm_bf16x_prepare", "gb300_sgemm_bf16x_run", "gb300_dgemm_ozaki_prepare",
     "gb300_dgemm_ozaki_run", "gb300_host_sgemm_bf16x", "gb300_host_dgemm_ozaki",
+    "gb300_selftest_wait_timeout",
 ]

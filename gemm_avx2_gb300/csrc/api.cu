@@ -11,6 +11,7 @@
 #include <unordered_map>
 #include <utility>
 
+#include "common.cuh"
 #include "plain_gemm.h"
 #include "split_gemm.h"
 
@@ -196,6 +197,21 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
   return word ? GB300_ERR_TIMEOUT : GB300_OK;
 }
 
+// Failure-detection self-test: one CTA waits on an mbarrier that nothing ever
+// arrives on, with a short poll limit; the wait gives up, records
+// kErrTimeoutFull in the error word and the kernel returns normally.
+__global__ void wait_timeout_selftest_kernel(unsigned limit, unsigned *err, int *reached_end) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  const bool ok = mbar_wait_limit(&bar, 0, limit, err, kErrTimeoutFull);
+  __syncthreads();
+  if (threadIdx.x == 0) *reached_end = ok ? 2 : 1;
+}
+
 }  // namespace gb300
 
 using namespace gb300;
@@ -351,6 +367,23 @@ GB300_API unsigned gb300_device_error(int clear) {
     return 0xFFFFFFFFu;
   if (clear) cudaMemset(err, 0, sizeof(unsigned));
   return w;
+}
+
+GB300_API int gb300_selftest_wait_timeout(unsigned poll_limit) {
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  int *flag = nullptr;
+  if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) return GB300_ERR_CUDA;
+  cudaMemset(flag, 0, sizeof(int));
+  wait_timeout_selftest_kernel<<<1, 32>>>(poll_limit, s->err, flag);
+  int reached = 0;
+  cudaError_t e = cudaMemcpy(&reached, flag, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(flag);
+  if (e != cudaSuccess) return GB300_ERR_CUDA;
+  unsigned w = 0;
+  cudaMemcpy(&w, s->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  if (reached == 1 && w == kErrTimeoutFull) return GB300_ERR_TIMEOUT;
+  return reached == 2 ? GB300_OK : GB300_ERR_CUDA;
 }
 
 GB300_API const char *gb300_version(void) { return "gemm_gb300 0.1 (sm_103a)"; }

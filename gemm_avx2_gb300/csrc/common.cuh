@@ -80,6 +80,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsign
   if (cta_abort) *cta_abort = 1;
   return false;
 }
+// Same with a caller-chosen poll limit (used by the timeout self-test).
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t *bar, uint32_t parity, uint32_t limit,
+                                                unsigned *err, unsigned code) {
+  for (uint32_t i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  record_error(err, code);
+  return false;
+}
 // cp.async completion -> one (non-incrementing) arrival on the barrier.
 __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar) {
   asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar))

@@ -150,6 +150,14 @@ size_t gb300_split_workspace_bytes(int kind, int m, int n, int k, int param);
  * Bounded waits that expired record codes 0x10-0x14.  clear != 0 resets it. */
 unsigned gb300_device_error(int clear);
 
+/* Failure-detection self-test (no reference counterpart; the reference has no
+ * error detection at all, src/gemm_driver.c:23-33 spins without a limit):
+ * launches one CTA that waits on an mbarrier nothing arrives on, with a poll
+ * limit of `poll_limit`.  Expected result: GB300_ERR_TIMEOUT, with the error
+ * word set to 0x10 (clear it with gb300_device_error(1)) and the CUDA context
+ * still usable.  Faults, traps and hangs are never used to test this. */
+int gb300_selftest_wait_timeout(unsigned poll_limit);
+
 /* Library version string. */
 const char *gb300_version(void);
 

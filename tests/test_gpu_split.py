@@ -70,7 +70,7 @@ def test_bf16x_split_bitexact_and_result(orc, products, ta, tb):
     got = from_dev(dC, m)
     truth = orc.dot2gemm(ta, tb, m, n, k, 1.0, A, ar + 1, B, br + 3, 0.5, C, m)
     mx, fro = rel_errs(got, truth)
-    assert fro < (2e-5 if products == 3 else 2e-7), (mx, fro)
+    assert fro < (2e-5 if products == 3 else 1e-6), (mx, fro)
     assert g.device_error() == 0
 
 
@@ -80,14 +80,22 @@ def test_bf16x_multi_tile_ragged(orc, products):
     A = orc.uniform((k, m), np.float32, 12, 0)   # transa = T
     B = orc.uniform((k, n), np.float32, 12, 1)   # transb = N
     C = orc.uniform((m + 5, n), np.float32, 12, 2)
-    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
+    dA, dB, dC, dP = to_dev(A), to_dev(B), to_dev(C), to_dev(C)
     assert g.sgemm_bf16x("T", "N", m, n, k, -1.0, dA.data_ptr(), k, dB.data_ptr(), k, 1.0,
                          dC.data_ptr(), m + 5, products=products) == g.OK
+    assert g.gemm_device("s", "T", "N", m, n, k, -1.0, dA.data_ptr(), k, dB.data_ptr(), k, 1.0,
+                         dP.data_ptr(), m + 5) == g.OK
     sync()
     got = from_dev(dC, m + 5)
     truth = orc.dot2gemm("T", "N", m, n, k, -1.0, A, k, B, k, 1.0, C, m + 5)
     mx, fro = rel_errs(got[:m], truth)
-    assert fro < (2e-5 if products == 3 else 2e-7), (mx, fro)
+    pmx, pfro = rel_errs(from_dev(dP, m + 5)[:m], truth)
+    # 3xBF16 carries ~17 significant bits per operand; 6xBF16 all 24, so its
+    # error is of the plain FP32 kernel's order
+    if products == 3:
+        assert fro < 2e-5, (mx, fro)
+    else:
+        assert fro < 1e-6 and fro < 4 * pfro, (mx, fro, pfro)
     assert np.array_equal(got[m:], C[m:])
 
 
