@@ -34,6 +34,7 @@ ERR_TIMEOUT = 3
 ERR_NOMEM = 4
 ERR_UNSUPPORTED = 5
 ERR_WORKSPACE = 6
+ERR_NOALLOC_LIMIT = 7
 
 _core = None
 _drop = {}
@@ -100,6 +101,8 @@ def core() -> ctypes.CDLL:
         L.gb300_device_error.restype = c_uint
         L.gb300_version.restype = ctypes.c_char_p
         L.gb300_selftest_wait_timeout.argtypes = [c_uint]
+        L.gb300_sgemm_bf16x_noalloc.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int,
+                                                    c_float, c_void_p, c_int, c_int, c_void_p]
         _core = L
     return _core
 
@@ -196,6 +199,16 @@ def dgemm_ozaki(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, sl
                                   workspace_bytes, c_void_p(stream))
 
 
+def sgemm_bf16x_noalloc(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                        products=3, stream=0) -> int:
+    """BF16xP split SGEMM whose scratch is the library's fixed 32 MiB device array
+    (no allocation; for callers that may not call cudaMalloc)."""
+    L = core()
+    return L.gb300_sgemm_bf16x_noalloc(_b(transa), _b(transb), m, n, k, alpha, _ptr(A), lda,
+                                       _ptr(B), ldb, beta, _ptr(C), ldc, products,
+                                       c_void_p(stream))
+
+
 def split_prepare(form, transa, transb, m, n, k, A, lda, B, ldb, param, workspace,
                   workspace_bytes, stream=0) -> int:
     """Phase 1 of a split form ('bf16x' or 'ozaki'): split op(A), op(B) into the workspace."""
@@ -247,5 +260,5 @@ CORE_SYMBOLS = [
     "gb300_split_workspace_bytes", "gb300_device_error", "gb300_version",
     "gb300_sgemm_bf16x_prepare", "gb300_sgemm_bf16x_run", "gb300_dgemm_ozaki_prepare",
     "gb300_dgemm_ozaki_run", "gb300_host_sgemm_bf16x", "gb300_host_dgemm_ozaki",
-    "gb300_selftest_wait_timeout",
+    "gb300_selftest_wait_timeout", "gb300_sgemm_bf16x_noalloc",
 ]

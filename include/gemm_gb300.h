@@ -43,7 +43,8 @@ typedef enum {
   GB300_ERR_TIMEOUT = 3,     /* a kernel's bounded wait expired (device error word set) */
   GB300_ERR_NOMEM = 4,       /* device workspace could not be allocated       */
   GB300_ERR_UNSUPPORTED = 5, /* option outside what this build implements     */
-  GB300_ERR_WORKSPACE = 6    /* caller-provided workspace too small           */
+  GB300_ERR_WORKSPACE = 6,   /* caller-provided workspace too small           */
+  GB300_ERR_NOALLOC_LIMIT = 7 /* problem needs more scratch than gb300_sgemm_bf16x_noalloc's fixed array */
 } gb300_status;
 
 /* ------------------------------------------------------------------------
@@ -111,6 +112,28 @@ int gb300_dgemm_ozaki_ws(char transa, char transb, int m, int n, int k, double a
                          const double *A, int lda, const double *B, int ldb, double beta,
                          double *C, int ldc, int slices, void *workspace, size_t workspace_bytes,
                          void *stream);
+
+/* BF16xP split SGEMM that allocates nothing.  No counterpart in the reference.
+ * For callers that may not call cudaMalloc/cudaFree: code running under a
+ * framework that owns all device memory (a pool or a fixed budget that must
+ * not be bypassed) and code on a latency-critical path.  Same arguments and
+ * result as gb300_sgemm_bf16x (products 3 or 6), but the scratch is a fixed
+ * 32 MiB array that is part of the library's device image (each GPU that loads
+ * the library holds it until exit); the call allocates and frees nothing.
+ *   - Problems whose scratch (gb300_split_workspace_bytes(0, m, n, k,
+ *     products)) exceeds 32 MiB are rejected with GB300_ERR_NOALLOC_LIMIT
+ *     (3xBF16: up to about m = n = k = 1400; 6xBF16: about 1000).
+ *   - The first call on a device looks up the array's device address (set-up,
+ *     once per device); make that first call before any stream capture.
+ *   - Every call uses the same array: calls whose execution overlaps on the
+ *     GPU (different streams, or different host threads) race on it; order
+ *     them on one stream.  Each call writes all the scratch it reads, so no
+ *     state carries over from the previous call.
+ *   - Kernel time-outs are recorded in a separate error word of this entry
+ *     point, not the one gb300_device_error reads. */
+int gb300_sgemm_bf16x_noalloc(char transa, char transb, int m, int n, int k, float alpha,
+                              const float *A, int lda, const float *B, int ldb, float beta,
+                              float *C, int ldc, int products, void *stream);
 
 /* Two-phase forms of the split GEMMs (no reference counterpart; the split of
  * the reference's pack-then-compute structure, src/gemm_driver.c:157-188):
