@@ -101,6 +101,7 @@ def core() -> ctypes.CDLL:
         L.gb300_device_error.restype = c_uint
         L.gb300_version.restype = ctypes.c_char_p
         L.gb300_selftest_wait_timeout.argtypes = [c_uint]
+        L.gb300_tune_param.argtypes = [c_int, c_int]
         L.gb300_sgemm_bf16x_noalloc.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int,
                                                     c_float, c_void_p, c_int, c_int, c_void_p]
         _core = L
@@ -249,6 +250,14 @@ def selftest_wait_timeout(poll_limit: int = 4096) -> int:
     return core().gb300_selftest_wait_timeout(poll_limit)
 
 
+TUNE_BF16X_CHUNK = 1
+
+
+def tune_param(param: int, value: int) -> int:
+    """Set a process-wide tuning knob (see include/gemm_gb300.h)."""
+    return core().gb300_tune_param(param, value)
+
+
 def version() -> str:
     return core().gb300_version().decode()
 
@@ -260,5 +269,5 @@ CORE_SYMBOLS = [
     "gb300_split_workspace_bytes", "gb300_device_error", "gb300_version",
     "gb300_sgemm_bf16x_prepare", "gb300_sgemm_bf16x_run", "gb300_dgemm_ozaki_prepare",
     "gb300_dgemm_ozaki_run", "gb300_host_sgemm_bf16x", "gb300_host_dgemm_ozaki",
-    "gb300_selftest_wait_timeout", "gb300_sgemm_bf16x_noalloc",
+    "gb300_selftest_wait_timeout", "gb300_sgemm_bf16x_noalloc", "gb300_tune_param",
 ]

@@ -386,4 +386,14 @@ GB300_API int gb300_selftest_wait_timeout(unsigned poll_limit) {
   return reached == 2 ? GB300_OK : GB300_ERR_CUDA;
 }
 
+GB300_API int gb300_tune_param(int param, int value) {
+  switch (param) {
+    case GB300_TUNE_BF16X_CHUNK:
+      set_bf16x_chunk_kblocks(value);
+      return GB300_OK;
+    default:
+      return GB300_ERR_ARG;
+  }
+}
+
 GB300_API const char *gb300_version(void) { return "gemm_gb300 0.1 (sm_103a)"; }

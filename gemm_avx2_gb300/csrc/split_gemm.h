@@ -35,6 +35,10 @@ int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int ld
 int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int slices,
               const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err);
 
+// Accumulation chunk of the BF16xP GEMM in 64-wide K blocks (0 = default, 4).
+int bf16x_chunk_kblocks();
+void set_bf16x_chunk_kblocks(int c);
+
 // Default slice count for a shape class (autotune cache, falls back to 8).
 int ozaki_default_slices(int m, int n, int k);
 

@@ -197,9 +197,22 @@ __global__ void __launch_bounds__(256) ozaki_slice_kernel(
 
 // ===========================================================================
 // BF16xP GEMM: C = alpha * A'B'^T + beta * C, persistent, 128 x 256 tiles.
+//
+// The tensor core's FP32 accumulation over a long K' is less accurate than a
+// round-to-nearest FFMA chain (measured: both 3x and 6x forms ~9e-6 relative
+// at K' = 3*8192 and 6*8192).  So TMEM accumulates bounded chunks only; the 8
+// epilogue warps add every chunk into FP32 running sums in registers (round to
+// nearest) while the MMA warp fills the other TMEM buffer with the next chunk.
+// Chunks never cross a segment (one cross product), and their length follows
+// the segment's magnitude: order-2 products (~2^-16 of the result) need no
+// chunking, order-1 products (~2^-8) chunks of 16 blocks, the hi*hi segment
+// chunks of `chunk0` blocks.  Small segments come first in K', so each tile
+// starts with a long chunk that hides the previous tile's C store.
 // ===========================================================================
 struct Bf16xParams {
   int m, n, tiles_m, tiles_n, kblocks;
+  int seg_kblocks, nseg;
+  int chunk_len[6];  // per segment: 64-wide K blocks per chunk (0 = whole segment)
   float alpha, beta;
   float *C;
   int ldc;
@@ -207,11 +220,14 @@ struct Bf16xParams {
 };
 
 constexpr int kBxStages = 4;
-constexpr int kBxThreads = 6 * 32;  // producer, MMA, 4 epilogue warps
+constexpr int kBxEpiWarps = 8;                      // 2 per TMEM lane quarter
+constexpr int kBxThreads = (2 + kBxEpiWarps) * 32;  // producer, MMA, epilogue
 constexpr int kBxABytes = kSplitBM * 128;
 constexpr int kBxBBytes = kBf16xBN * 128;
 constexpr int kBxStage = kBxABytes + kBxBBytes;
 constexpr int kBxSmem = kBxStages * kBxStage + 1024 + 256;
+constexpr int kBxColsPerWarp = kBf16xBN / 2;        // columns each epilogue warp owns
+constexpr int kBxDefaultChunk = 4;                  // 4 x 64 = 256 K' per chunk
 
 __global__ void __launch_bounds__(kBxThreads, 1)
 bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -230,7 +246,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kBxStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    for (int b = 0; b < 2; ++b) { mbar_init(&accf[b], 1); mbar_init(&acce[b], 4); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&accf[b], 1); mbar_init(&acce[b], kBxEpiWarps); }
     mbar_init(done, 1);
     *abort_flag = 0;
     fence_barrier_init();
@@ -243,6 +259,11 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const int ntiles = p.tiles_m * p.tiles_n;
+  int nchunks = 0;
+  for (int sg = 0; sg < p.nseg; ++sg) {
+    const int cl = p.chunk_len[sg] > 0 ? p.chunk_len[sg] : p.seg_kblocks;
+    nchunks += (p.seg_kblocks + cl - 1) / cl;
+  }
 
   if (warp == 0) {
     if (lane == 0) {
@@ -264,67 +285,92 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16_f32(kSplitBM, kBf16xBN);
-      uint32_t L = 0, it = 0;
+      uint32_t L = 0, chunk = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++it) {
-        const int b = it & 1;
-        const uint32_t u = it >> 1;
-        if (!mbar_wait(&acce[b], (u & 1) ^ 1, p.err, kErrTimeoutMma, abort_flag)) break;
-        tc_fence_after();
-        const uint32_t dt = tmem + b * kBf16xBN;
-        for (int kb = 0; kb < p.kblocks; ++kb, ++L) {
-          const int s = L % kBxStages;
-          const uint32_t r = L / kBxStages;
-          if (!mbar_wait(&full[s], r & 1, p.err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        int sg = 0, c0 = 0;
+        for (int c = 0; c < nchunks && ok; ++c, ++chunk) {
+          // chunk c covers K blocks [c0, c1) of segment sg
+          const int cl = p.chunk_len[sg] > 0 ? p.chunk_len[sg] : p.seg_kblocks;
+          const int seg_end = (sg + 1) * p.seg_kblocks;
+          const int c1 = min(seg_end, c0 + cl);
+          const int b = chunk & 1;
+          const uint32_t u = chunk >> 1;
+          if (!mbar_wait(&acce[b], (u & 1) ^ 1, p.err, kErrTimeoutMma, abort_flag)) {
+            ok = false;
+            break;
+          }
           tc_fence_after();
-          const uint32_t sa = smem_u32(smem + s * kBxStage), sb = sa + kBxABytes;
+          const uint32_t dt = tmem + b * kBf16xBN;
+          for (int kb = c0; kb < c1; ++kb, ++L) {
+            const int s = L % kBxStages;
+            const uint32_t r = L / kBxStages;
+            if (!mbar_wait(&full[s], r & 1, p.err, kErrTimeoutFull, abort_flag)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + s * kBxStage), sb = sa + kBxABytes;
 #pragma unroll
-          for (int kk = 0; kk < kSplitBK / 16; ++kk)
-            umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32), idesc,
-                      (kb > 0 || kk > 0) ? 1u : 0u);
-          umma_commit(&empty[s]);
+            for (int kk = 0; kk < kSplitBK / 16; ++kk)
+              umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32), idesc,
+                        (kb > c0 || kk > 0) ? 1u : 0u);
+            umma_commit(&empty[s]);
+          }
+          if (ok) umma_commit(&accf[b]);
+          c0 = c1;
+          if (c0 == seg_end) ++sg;
         }
-        if (ok) umma_commit(&accf[b]);
       }
       // every issued MMA has completed before TMEM is released
       umma_commit(done);
       mbar_wait(done, 0, p.err, kErrTimeoutMma, nullptr);
     }
   } else {
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int q = warp & 3;             // TMEM lane quarter this warp may access
+    const int h = (warp - 2) >> 2;      // column half of the tile
     const int row_in_tile = q * 32 + lane;
-    uint32_t it = 0;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + h * kBxColsPerWarp;
+    uint32_t chunk = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
       int tm, tn;
       tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
-      const int b = it & 1;
-      const uint32_t u = it >> 1;
-      if (!mbar_wait(&accf[b], u & 1, p.err, kErrTimeoutAcc, abort_flag)) break;
-      tc_fence_after();
-      const int row = tm * kSplitBM + row_in_tile;
-      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + b * kBf16xBN;
-#pragma unroll 1
-      for (int c = 0; c < kBf16xBN / 32; ++c) {
-        uint32_t v[32];
-        tmem_ld32(tbase + c * 32, v);
-        tmem_ld_wait();
-        if (row < p.m) {
-          const int col0 = tn * kBf16xBN + c * 32;
+      float run[kBxColsPerWarp];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int col = col0 + j;
-            if (col < p.n) {
-              float *cp = p.C + (int64_t)col * p.ldc + row;
-              const float c0 = *cp;
-              const float cb = (p.beta == 1.0f) ? c0 : c0 * p.beta;
-              *cp = cb + p.alpha * __uint_as_float(v[j]);
-            }
+      for (int j = 0; j < kBxColsPerWarp; ++j) run[j] = 0.f;
+      for (int c = 0; c < nchunks; ++c, ++chunk) {
+        const int b = chunk & 1;
+        const uint32_t u = chunk >> 1;
+        if (!mbar_wait(&accf[b], u & 1, p.err, kErrTimeoutAcc, abort_flag)) { ok = false; break; }
+        tc_fence_after();
+#pragma unroll
+        for (int g = 0; g < kBxColsPerWarp / 32; ++g) {
+          uint32_t v[32];
+          tmem_ld32(lane_base + b * kBf16xBN + g * 32, v);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 32; ++j) run[g * 32 + j] += __uint_as_float(v[j]);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[b]);
+      }
+      if (!ok) break;
+      const int row = tm * kSplitBM + row_in_tile;
+      if (row < p.m) {
+        const int col0 = tn * kBf16xBN + h * kBxColsPerWarp;
+#pragma unroll
+        for (int j = 0; j < kBxColsPerWarp; ++j) {
+          const int col = col0 + j;
+          if (col < p.n) {
+            float *cp = p.C + (int64_t)col * p.ldc + row;
+            const float c0 = *cp;
+            const float cb = (p.beta == 1.0f) ? c0 : c0 * p.beta;
+            *cp = cb + p.alpha * run[j];
           }
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acce[b]);
     }
   }
   tc_fence_before();
@@ -629,6 +675,11 @@ size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
 
 int ozaki_default_slices(int, int, int) { return 8; }
 
+// K blocks per TMEM accumulation chunk of the BF16xP GEMM (0 = default).
+static int g_bf16x_chunk = 0;
+int bf16x_chunk_kblocks() { return g_bf16x_chunk; }
+void set_bf16x_chunk_kblocks(int c) { g_bf16x_chunk = c < 0 ? 0 : c; }
+
 // ----------------------------------------------------------------- BF16xP
 struct Bf16xLayout {
   int64_t Kp, Kld, Mp, Np;
@@ -685,6 +736,17 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
   p.tiles_m = (int)(L.Mp / kSplitBM);
   p.tiles_n = (int)(L.Np / kBf16xBN);
   p.kblocks = (int)(L.Kld / kSplitBK);
+  p.seg_kblocks = (int)(L.Kp / kSplitBK);
+  p.nseg = products;
+  {
+    // order (i + j) of each segment's cross product, see seg_map()
+    static const int order3[3] = {1, 1, 0}, order6[6] = {2, 2, 2, 1, 1, 0};
+    const int c0 = bf16x_chunk_kblocks() > 0 ? bf16x_chunk_kblocks() : kBxDefaultChunk;
+    for (int sg = 0; sg < 6; ++sg) {
+      const int ord = sg < products ? (products == 3 ? order3[sg] : order6[sg]) : 2;
+      p.chunk_len[sg] = ord == 0 ? c0 : (ord == 1 ? 4 * c0 : 0);
+    }
+  }
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.err = err;
   if (cudaFuncSetAttribute(bf16x_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kBxSmem) != cudaSuccess)

@@ -181,6 +181,15 @@ unsigned gb300_device_error(int clear);
  * still usable.  Faults, traps and hangs are never used to test this. */
 int gb300_selftest_wait_timeout(unsigned poll_limit);
 
+/* Process-wide tuning knobs (the role of the reference's compile-time tune
+ * headers, dgemm_tune.h / sgemm_tune.h via src/gemm_set_parameters.h:1-61).
+ *   GB300_TUNE_BF16X_CHUNK: K extent (in 64-wide blocks) of one TMEM
+ *   accumulation chunk of the BF16xP SGEMM's hi*hi product; products of
+ *   order 1 use 4x that, order-2 products are not chunked.  0 restores the
+ *   default (4). */
+enum { GB300_TUNE_BF16X_CHUNK = 1 };
+int gb300_tune_param(int param, int value);
+
 /* Library version string. */
 const char *gb300_version(void);
 
