@@ -46,6 +46,11 @@ WORKLOADS = {
     # DGEMM NT 16384^3 (phi = 0), rank-256 updates with padded ld.
     "sgemm_tn_8192": dict(prec="s", ta="T", tb="N", m=8192, n=8192, k=8192, lda=8192, ldb=8192,
                           ldc=8192, alpha=1.0, beta=0.0, seed=1),
+    # a smaller case of the same kernels for ncu captures (split operands still > L2)
+    "sgemm_tn_4096": dict(prec="s", ta="T", tb="N", m=4096, n=4096, k=4096, lda=4096, ldb=4096,
+                          ldc=4096, alpha=1.0, beta=0.0, seed=1),
+    "dgemm_nt_4096": dict(prec="d", ta="N", tb="T", m=4096, n=4096, k=4096, lda=4096, ldb=4096,
+                          ldc=4096, alpha=1.0, beta=1.0, seed=2),
     "dgemm_nn_2048": dict(prec="d", ta="N", tb="N", m=2048, n=2048, k=2048, lda=2048, ldb=2048,
                           ldc=2048, alpha=1.0, beta=0.5, seed=0),
     "dgemm_nt_16384": dict(prec="d", ta="N", tb="T", m=16384, n=16384, k=16384, lda=16384,
@@ -171,8 +176,18 @@ class Problem:
         br, bc = (w["k"], w["n"]) if w["tb"] == "N" else (w["n"], w["k"])
         self.ar, self.ac, self.br, self.bc = ar, ac, br, bc
         # column-major ld x cols buffers are stored as row-major (cols, ld) tensors
-        self.A = torch.rand((ac, w["lda"]), generator=gen, device="cuda", dtype=dt) * 2 - 1
-        self.B = torch.rand((bc, w["ldb"]), generator=gen, device="cuda", dtype=dt) * 2 - 1
+        phi = float(w.get("phi", 0.0))
+        if phi > 0.0:
+            # exponent-spread inputs a = (u - 0.5) * exp(phi * g), u ~ U[0,1), g ~ N(0,1)
+            def spread(shape):
+                u = torch.rand(shape, generator=gen, device="cuda", dtype=torch.float64)
+                gn = torch.randn(shape, generator=gen, device="cuda", dtype=torch.float64)
+                return ((u - 0.5) * torch.exp(phi * gn)).to(dt)
+            self.A = spread((ac, w["lda"]))
+            self.B = spread((bc, w["ldb"]))
+        else:
+            self.A = torch.rand((ac, w["lda"]), generator=gen, device="cuda", dtype=dt) * 2 - 1
+            self.B = torch.rand((bc, w["ldb"]), generator=gen, device="cuda", dtype=dt) * 2 - 1
         self.C0 = torch.rand((w["n"], w["ldc"]), generator=gen, device="cuda", dtype=dt) * 2 - 1
         if w["beta"] == 0.0:
             self.C0.zero_()
@@ -211,7 +226,9 @@ def run_ours(args, torch, rank, world):
 
     import gemm_avx2_gb300 as g
 
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.phi is not None:
+        w["phi"] = args.phi
     prob = Problem(torch, w)
     stream = torch.cuda.current_stream().cuda_stream
     is_d = w["prec"] == "d"
@@ -310,7 +327,11 @@ def run_ours(args, torch, rank, world):
 
     # ---- end to end through the host-pointer C ABI (pinned host buffers)
     e2e = None
+    if args.no_e2e:
+        e2e = {"value": None, "skipped": "--no-e2e"}
     try:
+        if args.no_e2e:
+            raise StopIteration
         hA = torch.empty(prob.A.shape, dtype=prob.A.dtype, pin_memory=True)
         hB = torch.empty(prob.B.shape, dtype=prob.B.dtype, pin_memory=True)
         hC = torch.empty(prob.C0.shape, dtype=prob.C0.dtype, pin_memory=True)
@@ -333,6 +354,8 @@ def run_ours(args, torch, rank, world):
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": m * n * esz,
                "ms_per_step": round(dt * 1e3, 3), "api": "gb300_host_%s" %
                ("dgemm_ozaki" if is_d else "sgemm_bf16x")}
+    except StopIteration:
+        pass
     except Exception as ex:  # noqa: BLE001
         e2e = {"value": None, "error": repr(ex)}
 
@@ -359,6 +382,8 @@ def run_ours(args, torch, rank, world):
         "config": {"workload": args.workload, "transa": w["ta"], "transb": w["tb"], "m": m,
                    "n": n, "k": k, "lda": w["lda"], "ldb": w["ldb"], "ldc": w["ldc"],
                    "alpha": w["alpha"], "beta": w["beta"], "form": form_name,
+                   "phi": float(w.get("phi", 0.0)),
+                   "exponent_spread": exponent_spread(prob),
                    "l2": "inputs larger than L2 (%d MB per operand > %d MB)" % (
                        prob.A.numel() * prob.A.element_size() // 2**20, L2_BYTES // 2**20),
                    "parallelism": "replicas" if world > 1 else "single"},
@@ -375,8 +400,22 @@ def run_ours(args, torch, rank, world):
         "gpu_launches": args.steps * (3 if not is_d else 5),
     }
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+        line["cpu_baseline"] = (cpu_baseline(w, args.cpu_seconds) if not args.no_cpu
+                                else {"value": None, "skipped": "--no-cpu"})
         print(json.dumps(line), flush=True)
+
+
+def exponent_spread(prob):
+    """max - min of the binary exponent over the nonzero entries of op(A) and op(B)."""
+    import torch
+
+    out = {}
+    for name, X, rows in (("A", prob.A, prob.ar), ("B", prob.B, prob.br)):
+        x = X[:, :rows].abs()
+        x = x[x > 0]
+        e = torch.frexp(x.to(torch.float64))[1]
+        out[name] = int(e.max().item() - e.min().item()) if e.numel() else 0
+    return out
 
 
 def traffic_from_profile(workload, param):
@@ -429,6 +468,7 @@ def cpu_sample_rate(w, seconds):
         return time.perf_counter() - t
 
     ns = 16
+    run(ns)          # warm-up (thread team start, page faults)
     dt0 = run(ns)
     ns = int(min(w["n"], max(16, ns * seconds / max(dt0, 1e-3))))
     t = run(ns)
@@ -497,6 +537,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sgemm_tn_8192")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--phi", type=float, default=None,
+                    help="exponent spread of A and B: (u-0.5)*exp(phi*g) (DGEMM NT 16384 sweep)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-pointer leg (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

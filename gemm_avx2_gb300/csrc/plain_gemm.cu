@@ -166,8 +166,14 @@ __device__ __forceinline__ void f32_load_frag(const float *tile, int t, int kq, 
   }
 }
 
+// The FP32 kernel has no dedicated producer warp: 8 warps (256 threads, up to
+// 255 registers each) all compute, and thread 0 also refills the ring with TMA
+// kStages-1 tiles ahead.  With a ninth warp the register budget drops to 168
+// and the K-major variants spill into the inner loop.
+constexpr int kThreadsS = kConsumerWarps * 32;
+
 template <bool AK, bool BK_>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreadsS, 1)
 sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    OperandDesc opA, OperandDesc opB, int use_tma, int m, int n, int k, float alpha,
                    float beta, float *__restrict__ C, int ldc, int tiles_m, int tiles_n,
@@ -187,25 +193,56 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
   const int m0 = tmi * kBM, n0 = tni * kBN;
   const int ktiles = (k + BK - 1) / BK;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool tma = use_tma != 0;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&full[s], use_tma ? 1 : 32);
+      mbar_init(&full[s], tma ? 1 : kThreadsS);
       mbar_init(&empty[s], kConsumerWarps);
     }
     *abort_flag = 0;
     fence_barrier_init();
-    if (use_tma) { tma_prefetch_desc(&tmA); tma_prefetch_desc(&tmB); }
+    if (tma) { tma_prefetch_desc(&tmA); tma_prefetch_desc(&tmB); }
   }
   __syncthreads();
 
-  if (warp == kConsumerWarps) {
-    producer_loop<float, AK, BK_>(&tmA, &tmB, opA, opB, use_tma != 0, sA, sB, full, empty, m0, n0,
-                                  ktiles, err, abort_flag);
-    return;
-  }
+  // Fill k-tile kt into its stage.  TMA: thread 0 only.  Fallback: every thread
+  // copies a strided share of the elements with cp.async and arrives once.
+  auto fill = [&](int kt) {
+    const int s = kt % kStages;
+    float *ta = sA + s * (kBM * BK);
+    float *tb = sB + s * (kBN * BK);
+    const int k0 = kt * BK;
+    if (tma) {
+      if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&full[s], 2 * tile_bytes<float>());
+        if (AK) tma_load_2d(ta, &tmA, k0, m0, &full[s]);
+        else    tma_load_2d(ta, &tmA, m0, k0, &full[s]);
+        if (BK_) tma_load_2d(tb, &tmB, k0, n0, &full[s]);
+        else     tma_load_2d(tb, &tmB, n0, k0, &full[s]);
+      }
+    } else {
+      const float *baseA = static_cast<const float *>(opA.ptr);
+      const float *baseB = static_cast<const float *>(opB.ptr);
+      for (int e = threadIdx.x; e < kBM * BK; e += kThreadsS) {
+        int mn, kk;
+        if (AK) { mn = e / BK; kk = e % BK; } else { kk = e / kBM; mn = e % kBM; }
+        const int r = AK ? (k0 + kk) : (m0 + mn), c = AK ? (m0 + mn) : (k0 + kk);
+        const bool ok = r < opA.rows && c < opA.cols;
+        cp_async_4(ta + tile_off<float, AK>(mn, kk), ok ? baseA + (int64_t)c * opA.ld + r : baseA, ok);
+      }
+      for (int e = threadIdx.x; e < kBN * BK; e += kThreadsS) {
+        int mn, kk;
+        if (BK_) { mn = e / BK; kk = e % BK; } else { kk = e / kBN; mn = e % kBN; }
+        const int r = BK_ ? (k0 + kk) : (n0 + mn), c = BK_ ? (n0 + mn) : (k0 + kk);
+        const bool ok = r < opB.rows && c < opB.cols;
+        cp_async_4(tb + tile_off<float, BK_>(mn, kk), ok ? baseB + (int64_t)c * opB.ld + r : baseB, ok);
+      }
+      cp_async_mbar_arrive(&full[s]);
+    }
+  };
 
-  // consumer thread coordinates
+  // thread coordinates of the 8x8 register tile
   const int wm = warp & 1, wn = warp >> 1;
   const int tm = wm * 8 + (lane & 7);
   const int tn = wn * 4 + (lane >> 3);
@@ -215,8 +252,19 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
 
+  for (int kt = 0; kt < kStages - 1 && kt < ktiles; ++kt) fill(kt);
+
   bool ok = true;
   for (int kt = 0; kt < ktiles; ++kt) {
+    // refill the stage consumed in iteration kt-1 with k-tile kt + kStages - 1
+    const int nk = kt + kStages - 1;
+    if (nk < ktiles) {
+      if (kt >= 1 && (!tma || threadIdx.x == 0)) {
+        if (!mbar_wait(&empty[nk % kStages], ((nk / kStages) - 1) & 1, err, kErrTimeoutEmpty,
+                       abort_flag)) { ok = false; break; }
+      }
+      fill(nk);
+    }
     const int s = kt % kStages;
     if (!mbar_wait(&full[s], (kt / kStages) & 1, err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
     const float *ta = sA + s * (kBM * BK);
@@ -409,7 +457,7 @@ static int launch_one(const CUtensorMap &tA, const CUtensorMap &tB, const Operan
   if (e != cudaSuccess) return GB300_ERR_CUDA;
   const int64_t ntiles = (int64_t)tiles_m * tiles_n;
   if (ntiles > 0x7fffffff) return GB300_ERR_ARG;
-  kern<<<(unsigned)ntiles, kThreads, smem, st>>>(tA, tB, oA, oB, tma ? 1 : 0, m, n, k, alpha, beta,
+  kern<<<(unsigned)ntiles, sizeof(T) == 4 ? kThreadsS : kThreads, smem, st>>>(tA, tB, oA, oB, tma ? 1 : 0, m, n, k, alpha, beta,
                                                   C, ldc, tiles_m, tiles_n, err);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }

@@ -11,8 +11,8 @@
 //    and cut into S slices of signed 7-bit integers (|d| <= 127, int8 range).
 //    tcgen05 on sm_103a has no kind::i8, so the integer slices ride the BF16
 //    pipe: each slice value is exact in BF16, each product (< 2^14) exact in
-//    FP32, and every accumulation chunk is capped at 256 K-steps so partial sums
-//    stay below 2^22 -- integer-valued FP32 is then exact.  The epilogue warps
+//    FP32, and every accumulation chunk is capped at 1024 K-steps so partial sums
+//    stay below 1024*127^2 < 2^24 -- integer-valued FP32 is then exact.  The epilogue warps
 //    drain each chunk from TMEM into 32-bit integer sums (exact), and fold each
 //    slice group t = i + j into an FP64 result held in TMEM with weight 2^-7t.
 //
@@ -404,8 +404,12 @@ constexpr int kOzABytes = kSplitBM * 128;
 constexpr int kOzBBytes = kOzakiBN * 128;
 constexpr int kOzStage = kOzABytes + kOzBBytes;
 constexpr int kOzSmem = kOzStages * kOzStage + 1024 + 256;
-constexpr int kOzChunkStages = 4;       // 4 x 64 = 256 K-steps per exact chunk
-constexpr int kOzRunChunks = 512;       // int32 sums folded at least every 512 chunks
+// 16 x 64 = 1024 K-steps per exact chunk: |partial sum| <= 1024 * 127^2 =
+// 16,516,096 < 2^24, so every partial sum is an exactly representable FP32 integer.
+constexpr int kOzChunkStages = 16;
+// int32 running sums are folded into FP64 at least every 128 chunks:
+// 128 * 16,516,096 < 2^31.
+constexpr int kOzRunChunks = 128;
 
 // pairs of slice group t: sa in [lo, hi], sb = t - sa
 __device__ __forceinline__ void group_pairs(int t, int S, int &lo, int &np) {
@@ -550,8 +554,8 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             tmem_ld_wait();
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-              // |v| < 2^22 and integer-valued: exact conversion by the 1.5*2^23 shift
-              run[hh * 32 + j] += __float_as_int(__uint_as_float(v[j]) + 12582912.0f) - 0x4B400000;
+              // integer-valued with |v| < 2^24: round-to-nearest conversion is exact
+              run[hh * 32 + j] += __float2int_rn(__uint_as_float(v[j]));
             }
           }
           tc_fence_before();

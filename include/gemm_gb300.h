@@ -102,7 +102,8 @@ int gb300_sgemm_bf16x_ws(char transa, char transb, int m, int n, int k, float al
  * columns of op(B) are scaled by powers of two and cut into `slices`
  * signed 7-bit integer slices (int8 range, |v| <= 127); the slice products
  * with i + j <= slices + 1 are accumulated exactly (integer-valued FP32 in
- * TMEM over bounded K chunks, flushed into 32-bit integers) and recombined
+ * TMEM over K chunks of 1024, whose sums stay below 2^24, flushed into 32-bit
+ * integers) and recombined
  * in FP64 with the fused alpha/beta epilogue.  slices in [2, 12]; 0 picks the
  * autotuned default for the shape class. */
 int gb300_dgemm_ozaki(char transa, char transb, int m, int n, int k, double alpha,

@@ -183,3 +183,26 @@ def test_ozaki_edge_semantics(orc):
     sync()
     got = from_dev(dC, m)
     assert np.isnan(got[5]).all() and np.isfinite(np.delete(got, 5, axis=0)).all()
+
+
+def test_ozaki_exact_at_chunk_bound(orc):
+    """Worst case for the exact chunks: every slice digit is 127, so a 1024-step
+    chunk sums to 1024*127^2 (just below 2^24) and the int32 running sums grow
+    the most.  The kernel must reproduce the integer model bit for bit."""
+    S = 4
+    m, n, k = 130, 140, 3000
+    v = 1.0 - 2.0 ** (-7 * S - 3)  # all S digits 127 after scaling by 2^0
+    A = np.full((m, k), v, order="F")
+    B = np.full((k, n), -v, order="F")
+    A[1, 5] = -v
+    C = np.zeros((m, n), order="F")
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
+    assert g.dgemm_ozaki("N", "N", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), k, 0.0,
+                         dC.data_ptr(), m, slices=S) == g.OK
+    sync()
+    got = from_dev(dC, m)
+    sa, _ = osp.ozaki_slices(A, S)
+    assert (sa[0] == 127).sum() > 0.99 * m * k
+    model = osp.ozaki_gemm_model(A, B, S)
+    assert np.array_equal(got, model), np.abs(got - model).max()
+    assert g.device_error() == 0
