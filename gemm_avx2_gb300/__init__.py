@@ -102,6 +102,13 @@ def core() -> ctypes.CDLL:
         L.gb300_version.restype = ctypes.c_char_p
         L.gb300_selftest_wait_timeout.argtypes = [c_uint]
         L.gb300_tune_param.argtypes = [c_int, c_int]
+        L.gb300_grouped_workspace_bytes.argtypes = [c_int]
+        L.gb300_grouped_workspace_bytes.restype = c_size_t
+        L.gb300_gemm_grouped.argtypes = [c_void_p, c_int, c_void_p]
+        L.gb300_gemm_grouped_ws.argtypes = [c_void_p, c_int, c_void_p, c_size_t, c_void_p]
+        L.gb300_grouped_graph_create.argtypes = [c_void_p, c_int, c_int, ctypes.POINTER(c_void_p)]
+        L.gb300_grouped_graph_launch.argtypes = [c_void_p, c_void_p]
+        L.gb300_grouped_graph_destroy.argtypes = [c_void_p]
         L.gb300_sgemm_bf16x_noalloc.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int,
                                                     c_float, c_void_p, c_int, c_int, c_void_p]
         _core = L
@@ -253,6 +260,67 @@ def selftest_wait_timeout(poll_limit: int = 4096) -> int:
 TUNE_BF16X_CHUNK = 1
 
 
+class GemmProblem(ctypes.Structure):
+    """gb300_gemm_problem of include/gemm_gb300.h (one problem of a grouped call)."""
+
+    _fields_ = [("transa", c_char), ("transb", c_char), ("precision", c_char),
+                ("m", c_int), ("n", c_int), ("k", c_int),
+                ("alpha", c_double), ("beta", c_double),
+                ("A", c_void_p), ("lda", c_int), ("B", c_void_p), ("ldb", c_int),
+                ("C", c_void_p), ("ldc", c_int)]
+
+
+def problem_array(problems):
+    """A ctypes array of GemmProblem from dicts with keys precision, transa,
+    transb, m, n, k, alpha, beta, A, lda, B, ldb, C, ldc (A/B/C device pointers)."""
+    arr = (GemmProblem * len(problems))()
+    for i, p in enumerate(problems):
+        arr[i] = GemmProblem(_b(p["transa"]), _b(p["transb"]), _b(p["precision"]), p["m"],
+                             p["n"], p["k"], p["alpha"], p["beta"], p["A"], p["lda"], p["B"],
+                             p["ldb"], p["C"], p["ldc"])
+    return arr
+
+
+def gemm_grouped(problems, stream=0, workspace=None, workspace_bytes=0) -> int:
+    """All problems' plain forms in one persistent launch (device-side tile scheduler)."""
+    arr = problem_array(problems)
+    L = core()
+    if workspace is None:
+        return L.gb300_gemm_grouped(ctypes.cast(arr, c_void_p), len(problems), c_void_p(stream))
+    return L.gb300_gemm_grouped_ws(ctypes.cast(arr, c_void_p), len(problems), _ptr(workspace),
+                                   workspace_bytes, c_void_p(stream))
+
+
+def grouped_workspace_bytes(count: int) -> int:
+    return core().gb300_grouped_workspace_bytes(count)
+
+
+class GroupedGraph:
+    """A fixed grouped batch captured into a CUDA graph (form 0 plain, 1 split)."""
+
+    def __init__(self, problems, form=0):
+        self.handle = c_void_p()
+        arr = problem_array(problems)
+        rc = core().gb300_grouped_graph_create(ctypes.cast(arr, c_void_p), len(problems), form,
+                                               ctypes.byref(self.handle))
+        if rc != OK:
+            raise RuntimeError("gb300_grouped_graph_create failed: status %d" % rc)
+
+    def launch(self, stream=0) -> int:
+        return core().gb300_grouped_graph_launch(self.handle, c_void_p(stream))
+
+    def destroy(self) -> None:
+        if self.handle:
+            core().gb300_grouped_graph_destroy(self.handle)
+            self.handle = c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:  # noqa: BLE001
+            pass
+
+
 def tune_param(param: int, value: int) -> int:
     """Set a process-wide tuning knob (see include/gemm_gb300.h)."""
     return core().gb300_tune_param(param, value)
@@ -270,4 +338,6 @@ CORE_SYMBOLS = [
     "gb300_sgemm_bf16x_prepare", "gb300_sgemm_bf16x_run", "gb300_dgemm_ozaki_prepare",
     "gb300_dgemm_ozaki_run", "gb300_host_sgemm_bf16x", "gb300_host_dgemm_ozaki",
     "gb300_selftest_wait_timeout", "gb300_sgemm_bf16x_noalloc", "gb300_tune_param",
+    "gb300_grouped_workspace_bytes", "gb300_gemm_grouped", "gb300_gemm_grouped_ws",
+    "gb300_grouped_graph_create", "gb300_grouped_graph_launch", "gb300_grouped_graph_destroy",
 ]

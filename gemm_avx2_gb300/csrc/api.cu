@@ -359,6 +359,147 @@ GB300_API int gb300_dgemm_ozaki_run(int m, int n, int k, double alpha, double be
                    static_cast<cudaStream_t>(stream), err);
 }
 
+// ---------------------------------------------------------------- grouped
+GB300_API size_t gb300_grouped_workspace_bytes(int count) { return grouped_workspace_bytes(count); }
+
+GB300_API int gb300_gemm_grouped_ws(const gb300_gemm_problem *problems, int count, void *ws,
+                                    size_t ws_bytes, void *stream) {
+  for (int i = 0; i < count; ++i) {
+    const gb300_gemm_problem &q = problems[i];
+    if ((q.precision != 'd' && q.precision != 's') ||
+        check_args(q.transa, q.transb, q.m, q.n, q.k, q.lda, q.ldb, q.ldc) == GB300_ERR_ARG)
+      return GB300_ERR_ARG;
+  }
+  if (count <= 0) return count < 0 ? GB300_ERR_ARG : GB300_OK;
+  unsigned *err = device_error_word();
+  if (!err) return GB300_ERR_CUDA;
+  return grouped_plain(problems, count, ws, ws_bytes, static_cast<cudaStream_t>(stream), err);
+}
+
+GB300_API int gb300_gemm_grouped(const gb300_gemm_problem *problems, int count, void *stream) {
+  for (int i = 0; i < count; ++i) {
+    const gb300_gemm_problem &q = problems[i];
+    if ((q.precision != 'd' && q.precision != 's') ||
+        check_args(q.transa, q.transb, q.m, q.n, q.k, q.lda, q.ldb, q.ldc) == GB300_ERR_ARG)
+      return GB300_ERR_ARG;
+  }
+  if (count <= 0) return count < 0 ? GB300_ERR_ARG : GB300_OK;
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  const size_t need = grouped_workspace_bytes(count);
+  std::lock_guard<std::mutex> lk(s->mu);
+  // the grouped metadata gets its own cache slot (key: stream pointer + 1)
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  void *ws = cached_workspace(s, reinterpret_cast<cudaStream_t>(reinterpret_cast<uintptr_t>(st) + 1),
+                              need);
+  if (!ws) return GB300_ERR_NOMEM;
+  return grouped_plain(problems, count, ws, need, st, s->err);
+}
+
+struct gb300_grouped_graph_s {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  void *meta = nullptr;  // grouped metadata blob (form 0)
+  void *ws = nullptr;    // split-form workspace (form 1)
+  int device = 0;
+};
+
+GB300_API int gb300_grouped_graph_destroy(gb300_grouped_graph g) {
+  if (!g) return GB300_ERR_ARG;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->meta) cudaFree(g->meta);
+  if (g->ws) cudaFree(g->ws);
+  delete g;
+  return GB300_OK;
+}
+
+GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int count, int form,
+                                         gb300_grouped_graph *out) {
+  if (!out || count < 0 || (count > 0 && !problems) || (form != 0 && form != 1))
+    return GB300_ERR_ARG;
+  *out = nullptr;
+  for (int i = 0; i < count; ++i) {
+    const gb300_gemm_problem &q = problems[i];
+    if ((q.precision != 'd' && q.precision != 's') ||
+        check_args(q.transa, q.transb, q.m, q.n, q.k, q.lda, q.ldb, q.ldc) == GB300_ERR_ARG)
+      return GB300_ERR_ARG;
+  }
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  gb300_grouped_graph g = new (std::nothrow) gb300_grouped_graph_s();
+  if (!g) return GB300_ERR_NOMEM;
+  cudaGetDevice(&g->device);
+  cudaStream_t cs = nullptr;
+  int rc = GB300_OK;
+  std::vector<uint8_t> blob;
+  int used = 0, tiles = 0;
+  size_t wneed = 0;
+  if (form == 0) {
+    rc = grouped_build(problems, count, nullptr, blob, used, tiles);
+    if (rc == GB300_OK && used > 0) {
+      if (cudaMalloc(&g->meta, blob.size()) != cudaSuccess) rc = GB300_ERR_NOMEM;
+      else if (cudaMemcpy(g->meta, blob.data(), blob.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = GB300_ERR_CUDA;
+    }
+  } else {
+    for (int i = 0; i < count; ++i) {
+      const gb300_gemm_problem &q = problems[i];
+      const size_t w = q.precision == 'd' ? split_workspace_bytes(1, q.m, q.n, q.k, 0)
+                                          : split_workspace_bytes(0, q.m, q.n, q.k, 6);
+      if (w > wneed) wneed = w;
+    }
+    if (wneed && cudaMalloc(&g->ws, wneed) != cudaSuccess) rc = GB300_ERR_NOMEM;
+  }
+  if (rc == GB300_OK && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+    rc = GB300_ERR_CUDA;
+  if (rc == GB300_OK && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    rc = GB300_ERR_CUDA;
+  if (rc == GB300_OK) {
+    int rc2 = GB300_OK;
+    if (form == 0) {
+      if (used > 0) {
+        if (cudaMemsetAsync(g->meta, 0, sizeof(int), cs) != cudaSuccess) rc2 = GB300_ERR_CUDA;
+        else rc2 = grouped_launch_blob(g->meta, used, tiles, cs, s->err);
+      }
+    } else {
+      // one split-form call per problem, in order; they share the workspace
+      for (int i = 0; i < count && rc2 == GB300_OK; ++i) {
+        const gb300_gemm_problem &q = problems[i];
+        if (q.precision == 'd')
+          rc2 = ozaki_dgemm(q.transa, q.transb, q.m, q.n, q.k, q.alpha,
+                            static_cast<const double *>(q.A), q.lda,
+                            static_cast<const double *>(q.B), q.ldb, q.beta,
+                            static_cast<double *>(q.C), q.ldc, 0, g->ws, wneed, cs, s->err);
+        else
+          rc2 = split_sgemm(q.transa, q.transb, q.m, q.n, q.k, (float)q.alpha,
+                            static_cast<const float *>(q.A), q.lda,
+                            static_cast<const float *>(q.B), q.ldb, (float)q.beta,
+                            static_cast<float *>(q.C), q.ldc, 6, g->ws, wneed, cs, s->err);
+      }
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    g->graph = graph;
+    if (rc2 != GB300_OK) rc = rc2;
+    else if (e != cudaSuccess || !graph) rc = GB300_ERR_CUDA;
+    else if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) rc = GB300_ERR_CUDA;
+  }
+  if (cs) cudaStreamDestroy(cs);
+  if (rc != GB300_OK) {
+    gb300_grouped_graph_destroy(g);
+    return rc;
+  }
+  *out = g;
+  return GB300_OK;
+}
+
+GB300_API int gb300_grouped_graph_launch(gb300_grouped_graph g, void *stream) {
+  if (!g || !g->exec) return GB300_ERR_ARG;
+  return cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)) == cudaSuccess ? GB300_OK
+                                                                                    : GB300_ERR_CUDA;
+}
+
 GB300_API unsigned gb300_device_error(int clear) {
   unsigned *err = device_error_word();
   if (!err) return 0xFFFFFFFFu;

@@ -6,6 +6,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 #include "../../include/gemm_gb300.h"
 
@@ -45,5 +46,15 @@ int plain_dgemm(char ta, char tb, int m, int n, int k, double alpha, const doubl
 int plain_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
                 const float *B, int ldb, float beta, float *C, int ldc, cudaStream_t st,
                 unsigned *err);
+
+// Grouped plain GEMMs (grouped.cu).
+size_t grouped_workspace_bytes(int count);
+size_t grouped_blob_bytes(int count_used);
+int grouped_build(const gb300_gemm_problem *P, int count, void *dev_base,
+                  std::vector<uint8_t> &blob, int &count_used, int &total_tiles);
+int grouped_launch_blob(void *dev_blob, int count_used, int total_tiles, cudaStream_t st,
+                        unsigned *err);
+int grouped_plain(const gb300_gemm_problem *P, int count, void *ws, size_t ws_bytes,
+                  cudaStream_t st, unsigned *err);
 
 }  // namespace gb300

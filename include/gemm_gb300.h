@@ -164,6 +164,51 @@ int gb300_host_dgemm_ozaki(char transa, char transb, int m, int n, int k, double
                            const double *a, int lda, const double *b, int ldb, double beta,
                            double *c, int ldc, int slices);
 
+/* ------------------------------------------------------------------------
+ * Grouped GEMMs (no reference counterpart: the reference computes one problem
+ * per call, src/gemm_driver.c:118).  Many independent problems of any sizes,
+ * FP64 ('d') or FP32 ('s'), any transposes and leading dimensions, each with
+ * the semantics of dgemm_/sgemm_ above, on device buffers.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  char transa, transb;
+  char precision; /* 'd': A, B, C are double; 's': float */
+  int m, n, k;
+  double alpha, beta; /* rounded to float for 's' problems */
+  const void *A;
+  int lda;
+  const void *B;
+  int ldb;
+  void *C;
+  int ldc;
+} gb300_gemm_problem;
+
+/* Plain (native precision) forms of all problems in ONE persistent launch:
+ * the 128x128 tiles of all problems are ordered longest-work-first and CTAs
+ * take them from a device-side atomic counter.  Problems must not overlap
+ * in C.  Returns GB300_ERR_ARG (and launches nothing) if any problem is
+ * invalid.  The _ws form takes a caller workspace of
+ * gb300_grouped_workspace_bytes(count) bytes (metadata: tensor maps, tile
+ * table); the other uses a library-owned one. */
+size_t gb300_grouped_workspace_bytes(int count);
+int gb300_gemm_grouped(const gb300_gemm_problem *problems, int count, void *stream);
+int gb300_gemm_grouped_ws(const gb300_gemm_problem *problems, int count, void *workspace,
+                          size_t workspace_bytes, void *stream);
+
+/* A fixed batch captured once into a CUDA graph and replayed.  The problem
+ * table, tensor maps and all workspace are built at creation (which may
+ * allocate and synchronise); each launch replays the graph on `stream` with
+ * no host-side work: the operand pointers are fixed, their contents may
+ * change between launches.
+ *   form 0: plain forms, one persistent launch (as gb300_gemm_grouped);
+ *   form 1: split forms, one call per problem (FP32: 6xBF16, FP64: Ozaki with
+ *           the default slice count), captured in order. */
+typedef struct gb300_grouped_graph_s *gb300_grouped_graph;
+int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int count, int form,
+                               gb300_grouped_graph *out);
+int gb300_grouped_graph_launch(gb300_grouped_graph graph, void *stream);
+int gb300_grouped_graph_destroy(gb300_grouped_graph graph);
+
 /* Workspace needed by the split forms for one call of the given shape.
  * kind = 0: sgemm_bf16x with `param` = products; kind = 1: dgemm_ozaki with
  * `param` = slices. */

@@ -91,3 +91,18 @@ def test_dropin_invalid_args_leave_c_untouched():
     assert np.array_equal(c, before)
     g.dgemm("N", "N", 3, -4, 3, 1.0, a, 3, a, 3, 0.0, c, 3)
     assert np.array_equal(c, before)
+
+
+def test_grouped_problem_struct_layout_and_args():
+    import ctypes
+    P = g.GemmProblem
+    # LP64 layout of gb300_gemm_problem (x86-64 and aarch64 alike)
+    assert ctypes.sizeof(P) == 80
+    assert (P.m.offset, P.alpha.offset, P.A.offset, P.lda.offset, P.B.offset, P.C.offset,
+            P.ldc.offset) == (4, 16, 32, 40, 48, 64, 72)
+    bad = dict(precision="d", transa="N", transb="N", m=4, n=4, k=4, alpha=1.0, beta=0.0,
+               A=0, lda=3, B=0, ldb=4, C=0, ldc=4)
+    assert g.gemm_grouped([bad]) == g.ERR_ARG          # lda < m, checked before any CUDA call
+    bad2 = dict(bad, lda=4, precision="z")
+    assert g.gemm_grouped([bad2]) == g.ERR_ARG
+    assert g.gemm_grouped([]) == g.OK

@@ -1,0 +1,118 @@
+"""Grouped GEMMs on the GPU through the C ABI: one persistent launch over a
+mixed batch (FP64/FP32, N/T, ragged and tiny sizes, odd and aligned leading
+dimensions, alpha == 0, k == 0), CUDA-graph replay, and the split-form graph.
+Each result is checked like a single call: against the bit-exact oracle
+restatement of the reference, with the summation-order bound."""
+import numpy as np
+import pytest
+
+import gemm_avx2_gb300 as g
+from gpu_util import from_dev, sync, to_dev
+from util import U32, U64, check_close, gemm_bound
+
+pytestmark = pytest.mark.gpu
+
+
+def make_batch(orc, count, seed, max_dim=300):
+    rng = np.random.default_rng(seed)
+    probs, host, dev = [], [], []
+    for i in range(count):
+        prec = "d" if rng.random() < 0.6 else "s"
+        dt = np.float64 if prec == "d" else np.float32
+        m, n, k = (int(x) for x in np.round(np.exp(rng.uniform(0, np.log(max_dim), 3))))
+        if i == 3:
+            k = 0
+        ta, tb = ("N", "T")[rng.integers(2)], ("N", "T")[rng.integers(2)]
+        alpha = 0.0 if i == 5 else float(rng.uniform(0.5, 2))
+        beta = float(rng.choice([0.0, 1.0, 0.5]))
+        ar, ac = (m, k) if ta == "N" else (k, m)
+        br, bc = (k, n) if tb == "N" else (n, k)
+        pad = int(rng.integers(0, 3)) if i % 2 else 0   # odd pads -> cp.async path
+        lda, ldb, ldc = max(ar, 1) + pad, max(br, 1) + pad, max(m, 1) + pad
+        A = orc.storage(ar, ac, lda, dt, seed * 1000 + i, 0)
+        B = orc.storage(br, bc, ldb, dt, seed * 1000 + i, 1)
+        C = orc.storage(m, n, ldc, dt, seed * 1000 + i, 2)
+        dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
+        probs.append(dict(precision=prec, transa=ta, transb=tb, m=m, n=n, k=k, alpha=alpha,
+                          beta=beta, A=dA.data_ptr(), lda=lda, B=dB.data_ptr(), ldb=ldb,
+                          C=dC.data_ptr(), ldc=ldc))
+        host.append((A, B, C))
+        dev.append((dA, dB, dC))
+    return probs, host, dev
+
+
+def check_batch(orc, probs, host, dev, C_inputs=None):
+    for p, (A, B, C), (dA, dB, dC) in zip(probs, host, dev):
+        C0 = C if C_inputs is None else C_inputs
+        want = C0.copy(order="F")
+        orc.refgemm(p["transa"], p["transb"], p["m"], p["n"], p["k"], p["alpha"], A, p["lda"], B,
+                    p["ldb"], p["beta"], want, p["ldc"], 2)
+        got = from_dev(dC, C0.shape[0])
+        m, n = p["m"], p["n"]
+        u = U64 if p["precision"] == "d" else U32
+        check_close(got[:m, :n], want[:m, :n],
+                    gemm_bound(A, B, C0, p["transa"], p["transb"], m, n, p["k"], p["alpha"],
+                               p["beta"], u))
+        assert np.array_equal(got[m:], C0[m:])
+
+
+def test_grouped_one_launch_matches_oracle(orc):
+    probs, host, dev = make_batch(orc, 48, 1)
+    assert g.gemm_grouped(probs) == g.OK
+    sync()
+    check_batch(orc, probs, host, dev)
+    assert g.device_error() == 0
+
+
+def test_grouped_caller_workspace(orc):
+    probs, host, dev = make_batch(orc, 9, 2, max_dim=200)
+    import torch
+    nb = g.grouped_workspace_bytes(len(probs))
+    ws = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    assert g.gemm_grouped(probs, workspace=ws.data_ptr(), workspace_bytes=nb - 4096) == \
+        g.ERR_WORKSPACE
+    assert g.gemm_grouped(probs, workspace=ws.data_ptr(), workspace_bytes=nb) == g.OK
+    sync()
+    check_batch(orc, probs, host, dev)
+
+
+def test_grouped_graph_replay(orc):
+    """Capture once, replay twice; the second replay sees new A contents."""
+    probs, host, dev = make_batch(orc, 24, 3)
+    C_init = [h[2].copy(order="F") for h in host]
+    graph = g.GroupedGraph(probs, form=0)
+    assert graph.launch() == g.OK
+    sync()
+    check_batch(orc, probs, host, dev)
+    # new operands in the same buffers; reset C; replay
+    host2 = []
+    for i, (p, (A, B, C), (dA, dB, dC)) in enumerate(zip(probs, host, dev)):
+        A2 = (A * -0.5).astype(A.dtype, order="F")
+        dA.copy_(to_dev(A2))
+        dC.copy_(to_dev(C_init[i]))
+        host2.append((A2, B, C_init[i]))
+    assert graph.launch() == g.OK
+    sync()
+    check_batch(orc, probs, host2, dev)
+    graph.destroy()
+    assert g.device_error() == 0
+
+
+def test_grouped_split_graph(orc):
+    """Split forms (6xBF16 for FP32, Ozaki for FP64) captured per problem."""
+    probs, host, dev = make_batch(orc, 12, 4, max_dim=260)
+    C_init = [h[2].copy(order="F") for h in host]
+    graph = g.GroupedGraph(probs, form=1)
+    assert graph.launch() == g.OK
+    sync()
+    for p, (A, B, C), (dA, dB, dC), C0 in zip(probs, host, dev, C_init):
+        m, n = p["m"], p["n"]
+        if m == 0 or n == 0:
+            continue
+        truth = orc.dot2gemm(p["transa"], p["transb"], m, n, p["k"], p["alpha"], A, p["lda"], B,
+                             p["ldb"], p["beta"], C0, p["ldc"])
+        got = from_dev(dC, C0.shape[0])[:m, :n].astype(np.float64)
+        d = np.linalg.norm(got - truth) / max(np.linalg.norm(truth), 1e-300)
+        assert d < (1e-13 if p["precision"] == "d" else 1e-6), (p, d)
+    graph.destroy()
+    assert g.device_error() == 0
