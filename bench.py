@@ -418,6 +418,143 @@ def exponent_spread(prob):
     return out
 
 
+# ----------------------------------------------------------------------------- grouped workload
+FP64_PEAK_TFLOPS = 1.05   # DFMA / DMMA m16n8k8, measured on GB300 by microbenchmark
+FP32_PEAK_TFLOPS = 73.0   # FFMA, measured on GB300 by microbenchmark
+
+
+def run_grouped(args, torch, rank, world):
+    """1024 independent GEMMs: m, n, k = round(exp(U[ln 16, ln 2048])), transa/transb
+    N or T with p = 0.5, 60% FP64 / 40% FP32, alpha ~ U[0.5, 2], beta in {0, 1},
+    entries U[-1,1), ld = rows of the stored matrix (seed 4).  A step replays a
+    captured CUDA graph: the split forms (one call per problem) for the headline,
+    the plain forms (one persistent launch) for the comparison."""
+    import numpy as np
+
+    import gemm_avx2_gb300 as g
+
+    rng = np.random.default_rng(4)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(4)
+    count = 1024
+    probs, bufs, flops = [], [], 0.0
+    fl_d = fl_s = 0.0
+    for i in range(count):
+        m, n, k = (int(round(math.exp(x))) for x in rng.uniform(math.log(16), math.log(2048), 3))
+        ta = "N" if rng.random() < 0.5 else "T"
+        tb = "N" if rng.random() < 0.5 else "T"
+        prec = "d" if rng.random() < 0.6 else "s"
+        alpha = float(rng.uniform(0.5, 2.0))
+        beta = float(rng.choice([0.0, 1.0]))
+        dt = torch.float64 if prec == "d" else torch.float32
+        ar, ac = (m, k) if ta == "N" else (k, m)
+        br, bc = (k, n) if tb == "N" else (n, k)
+        A = torch.rand((ac, ar), generator=gen, device="cuda", dtype=dt) * 2 - 1
+        B = torch.rand((bc, br), generator=gen, device="cuda", dtype=dt) * 2 - 1
+        C0 = torch.rand((n, m), generator=gen, device="cuda", dtype=dt) * 2 - 1
+        C = C0.clone()
+        bufs.append((A, B, C0, C))
+        probs.append(dict(precision=prec, transa=ta, transb=tb, m=m, n=n, k=k, alpha=alpha,
+                          beta=beta, A=A.data_ptr(), lda=ar, B=B.data_ptr(), ldb=br,
+                          C=C.data_ptr(), ldc=m))
+        f = 2.0 * m * n * k
+        flops += f
+        if prec == "d":
+            fl_d += f
+        else:
+            fl_s += f
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def reset():
+        for (A, B, C0, C) in bufs:
+            C.copy_(C0)
+
+    def timed(graph, steps, warmup):
+        for _ in range(warmup):
+            reset()
+            assert graph.launch(stream) == g.OK
+        torch.cuda.synchronize()
+        total = 0.0
+        for _ in range(steps):
+            reset()   # restore C outside the timed launch
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            assert graph.launch(stream) == g.OK
+            e1.record()
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        return total / steps
+
+    gp = g.GroupedGraph(probs, form=0)
+    gs = g.GroupedGraph(probs, form=1)
+    # accuracy of both forms on sampled entries of 48 problems (exact sampled dots)
+    def sampled_errors(graph):
+        reset()
+        assert graph.launch(stream) == g.OK
+        torch.cuda.synchronize()
+        worst = [0.0, 0.0]
+        for i in range(0, count, count // 48):
+            p = probs[i]
+            A, B, C0, C = bufs[i]
+            r = rng.integers(0, p["m"], 8)
+            c = rng.integers(0, p["n"], 8)
+            Ah = A.cpu().numpy()
+            Bh = B.cpu().numpy()
+            Arows = Ah[:, r].T if p["transa"] == "N" else Ah[r, :]
+            Bcols = Bh[c, :] if p["transb"] == "N" else Bh[:, c].T
+            truth = exact_samples(Arows, Bcols, p["alpha"], p["beta"], C0[c, r].cpu().numpy())
+            e = rel_err(C[c, r].cpu().numpy(), truth)
+            tag = 0 if p["precision"] == "d" else 1
+            worst[tag] = max(worst[tag], e[0])
+        return {"fp64_max_rel": worst[0], "fp32_max_rel": worst[1]}
+
+    err_plain = sampled_errors(gp)
+    err_split = sampled_errors(gs)
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    barrier(torch, world)
+    ms_split = timed(gs, args.steps, args.warmup)
+    ms_plain = timed(gp, max(3, args.steps // 2), args.warmup)
+    barrier(torch, world)
+    clocks = sampler.stop() if sampler else None
+    max_ms = allreduce_max(torch, world, ms_split)
+    value = flops * world / (max_ms / 1e3) / 1e12
+    plain_tflops = flops / (ms_plain / 1e3) / 1e12
+    # roofline of the plain persistent kernel: FP64 tiles on the FP64 pipe, FP32 on FFMA
+    t_lb = fl_d / (FP64_PEAK_TFLOPS * 1e12) + fl_s / (FP32_PEAK_TFLOPS * 1e12)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(max_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded uniform[-1,1), generated on the device)",
+        "config": {"workload": "grouped_1024", "problems": count, "fp64_share_of_flops":
+                   round(fl_d / flops, 4), "total_gflop": round(flops / 1e9, 3),
+                   "form": "split (FP32: bf16x6, FP64: ozaki_s8), CUDA graph",
+                   "l2": "%d MB of operands > %d MB" % (
+                       sum(sum(t.numel() * t.element_size() for t in b[:3]) for b in bufs) // 2**20,
+                       L2_BYTES // 2**20)},
+        "plain": {"kernel": "grouped_plain_kernel (one persistent launch, CUDA graph)",
+                  "value": round(plain_tflops, 3), "unit": "TFLOP/s", "ms": round(ms_plain, 3),
+                  "split_speedup": round(value / world / plain_tflops, 3)},
+        "roofline": {"bound": "fp64+fp32 pipes (plain grouped kernel)",
+                     "achieved": round(plain_tflops, 3), "peak": round(flops / t_lb / 1e12, 3),
+                     "unit": "TFLOP/s", "frac": round(t_lb / (ms_plain / 1e3), 4),
+                     "traffic": None,
+                     "peak_source": "FP64 1.05 and FP32 73 TFLOP/s measured by microbenchmark"},
+        "accuracy": {"plain": err_plain, "split": err_split, "samples": "8 entries x 48 problems"},
+        "clocks": clocks,
+        "gpu_launches": args.steps * sum(5 if p["precision"] == "d" else 3 for p in probs),
+        "e2e": {"value": None, "skipped": "device-pointer grouped API"},
+    }
+    gp.destroy()
+    gs.destroy()
+    if rank == 0:
+        line["cpu_baseline"] = {"value": None, "skipped": "grouped workload"}
+        print(json.dumps(line), flush=True)
+
+
 def traffic_from_profile(workload, param):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
@@ -490,6 +627,10 @@ def cpu_baseline(w, seconds):
 def run_reference(args, rank, world):
     if rank != 0:
         return
+    if args.workload == "grouped_1024":
+        print(json.dumps({"impl": "reference", "metric": METRIC,
+                          "unavailable": "the reference has no grouped interface"}))
+        return
     w = WORKLOADS[args.workload]
     per_step = max(1.0, min(10.0, 120.0 / max(1, args.steps + args.warmup)))
     vals = []
@@ -535,7 +676,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sgemm_tn_8192")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["grouped_1024"],
+                    default="sgemm_tn_8192")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--phi", type=float, default=None,
                     help="exponent spread of A and B: (u-0.5)*exp(phi*g) (DGEMM NT 16384 sweep)")
@@ -556,7 +698,10 @@ def main():
     if world > 1:
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
-    run_ours(args, torch, rank, world)
+    if args.workload == "grouped_1024":
+        run_grouped(args, torch, rank, world)
+    else:
+        run_ours(args, torch, rank, world)
     if world > 1:
         torch.distributed.destroy_process_group()
 

@@ -10,6 +10,8 @@
 #include <mutex>
 #include <unordered_map>
 #include <utility>
+#include <algorithm>
+#include <vector>
 
 #include "common.cuh"
 #include "plain_gemm.h"
@@ -396,11 +398,16 @@ GB300_API int gb300_gemm_grouped(const gb300_gemm_problem *problems, int count, 
   return grouped_plain(problems, count, ws, need, st, s->err);
 }
 
+// Split-form batches are captured as kGraphBranches parallel branches (forked
+// from and joined into the capture stream), problems assigned longest-work-
+// first to the least-loaded branch; each branch has its own workspace.
+constexpr int kGraphBranches = 16;
+
 struct gb300_grouped_graph_s {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  void *meta = nullptr;  // grouped metadata blob (form 0)
-  void *ws = nullptr;    // split-form workspace (form 1)
+  void *meta = nullptr;                   // grouped metadata blob (form 0)
+  void *ws[kGraphBranches] = {nullptr};   // split-form workspaces (form 1), one per branch
   int device = 0;
 };
 
@@ -409,7 +416,8 @@ GB300_API int gb300_grouped_graph_destroy(gb300_grouped_graph g) {
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   if (g->meta) cudaFree(g->meta);
-  if (g->ws) cudaFree(g->ws);
+  for (int b = 0; b < kGraphBranches; ++b)
+    if (g->ws[b]) cudaFree(g->ws[b]);
   delete g;
   return GB300_OK;
 }
@@ -434,7 +442,10 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
   int rc = GB300_OK;
   std::vector<uint8_t> blob;
   int used = 0, tiles = 0;
-  size_t wneed = 0;
+  std::vector<int> branch_of(count > 0 ? count : 1, 0);
+  size_t wneed_b[kGraphBranches] = {0};
+  cudaStream_t bs[kGraphBranches] = {nullptr};
+  cudaEvent_t fork = nullptr, join[kGraphBranches] = {nullptr};
   if (form == 0) {
     rc = grouped_build(problems, count, nullptr, blob, used, tiles);
     if (rc == GB300_OK && used > 0) {
@@ -443,13 +454,29 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
         rc = GB300_ERR_CUDA;
     }
   } else {
-    for (int i = 0; i < count; ++i) {
+    // longest work first onto the least-loaded branch (FP64 problems run
+    // S(S+1)/2 slice products, FP32 ones 6)
+    std::vector<int> order(count);
+    for (int i = 0; i < count; ++i) order[i] = i;
+    auto work = [&](int i) {
+      const gb300_gemm_problem &q = problems[i];
+      return (double)q.m * q.n * q.k * (q.precision == 'd' ? 36.0 : 6.0) + 1e6;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work(a) > work(b); });
+    double load[kGraphBranches] = {0};
+    for (int i : order) {
+      int b = 0;
+      for (int j = 1; j < kGraphBranches; ++j)
+        if (load[j] < load[b]) b = j;
+      load[b] += work(i);
+      branch_of[i] = b;
       const gb300_gemm_problem &q = problems[i];
       const size_t w = q.precision == 'd' ? split_workspace_bytes(1, q.m, q.n, q.k, 0)
                                           : split_workspace_bytes(0, q.m, q.n, q.k, 6);
-      if (w > wneed) wneed = w;
+      if (w > wneed_b[b]) wneed_b[b] = w;
     }
-    if (wneed && cudaMalloc(&g->ws, wneed) != cudaSuccess) rc = GB300_ERR_NOMEM;
+    for (int b = 0; b < kGraphBranches && rc == GB300_OK; ++b)
+      if (wneed_b[b] && cudaMalloc(&g->ws[b], wneed_b[b]) != cudaSuccess) rc = GB300_ERR_NOMEM;
   }
   if (rc == GB300_OK && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
     rc = GB300_ERR_CUDA;
@@ -463,20 +490,35 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
         else rc2 = grouped_launch_blob(g->meta, used, tiles, cs, s->err);
       }
     } else {
-      // one split-form call per problem, in order; they share the workspace
+      // fork kGraphBranches branches off the capture stream; each branch runs
+      // its problems' split-form calls in order on its own workspace; join.
+      bool forked = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess &&
+                    cudaEventRecord(fork, cs) == cudaSuccess;
+      for (int b = 0; b < kGraphBranches && forked; ++b)
+        forked = cudaStreamCreateWithFlags(&bs[b], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming) == cudaSuccess &&
+                 cudaStreamWaitEvent(bs[b], fork, 0) == cudaSuccess;
+      if (!forked) rc2 = GB300_ERR_CUDA;
       for (int i = 0; i < count && rc2 == GB300_OK; ++i) {
         const gb300_gemm_problem &q = problems[i];
+        const int b = branch_of[i];
         if (q.precision == 'd')
           rc2 = ozaki_dgemm(q.transa, q.transb, q.m, q.n, q.k, q.alpha,
                             static_cast<const double *>(q.A), q.lda,
                             static_cast<const double *>(q.B), q.ldb, q.beta,
-                            static_cast<double *>(q.C), q.ldc, 0, g->ws, wneed, cs, s->err);
+                            static_cast<double *>(q.C), q.ldc, 0, g->ws[b], wneed_b[b], bs[b],
+                            s->err);
         else
           rc2 = split_sgemm(q.transa, q.transb, q.m, q.n, q.k, (float)q.alpha,
                             static_cast<const float *>(q.A), q.lda,
                             static_cast<const float *>(q.B), q.ldb, (float)q.beta,
-                            static_cast<float *>(q.C), q.ldc, 6, g->ws, wneed, cs, s->err);
+                            static_cast<float *>(q.C), q.ldc, 6, g->ws[b], wneed_b[b], bs[b],
+                            s->err);
       }
+      for (int b = 0; b < kGraphBranches && forked; ++b)
+        if (cudaEventRecord(join[b], bs[b]) != cudaSuccess ||
+            cudaStreamWaitEvent(cs, join[b], 0) != cudaSuccess)
+          rc2 = GB300_ERR_CUDA;
     }
     cudaGraph_t graph = nullptr;
     const cudaError_t e = cudaStreamEndCapture(cs, &graph);
@@ -486,6 +528,11 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
     else if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) rc = GB300_ERR_CUDA;
   }
   if (cs) cudaStreamDestroy(cs);
+  for (int b = 0; b < kGraphBranches; ++b) {
+    if (bs[b]) cudaStreamDestroy(bs[b]);
+    if (join[b]) cudaEventDestroy(join[b]);
+  }
+  if (fork) cudaEventDestroy(fork);
   if (rc != GB300_OK) {
     gb300_grouped_graph_destroy(g);
     return rc;

@@ -178,12 +178,17 @@ __device__ void g_tile(const GroupedProblemDev &p, const CUtensorMap *tmA, const
       const int col = n0 + f32_row<BK_>(tn, j);
       if (col >= p.n) continue;
       float *cc = C + (int64_t)col * p.ldc;
+      float cv[8];  // the column's 8 loads first, then the stores
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int row = m0 + f32_row<AK>(tm, i);
+        cv[i] = (row < p.m) ? cc[row] : 0.f;
+      }
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int row = m0 + f32_row<AK>(tm, i);
         if (row < p.m) {
-          const float c0 = cc[row];
-          float v = (beta == 1.0f) ? c0 : c0 * beta;
+          float v = (beta == 1.0f) ? cv[i] : cv[i] * beta;
           if (alpha != 0.0f) v = v + alpha * acc[i][j];
           cc[row] = v;
         }

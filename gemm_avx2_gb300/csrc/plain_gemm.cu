@@ -157,12 +157,17 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
     const int col = n0 + f32_row<BK_>(tn, j);
     if (col >= n) continue;
     float *cc = C + (int64_t)col * ldc;
+    float cv[8];  // the column's 8 loads first, then the stores
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int row = m0 + f32_row<AK>(tm, i);
+      cv[i] = (row < m) ? cc[row] : 0.f;
+    }
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int row = m0 + f32_row<AK>(tm, i);
       if (row < m) {
-        const float c0 = cc[row];
-        const float cb = (beta == 1.0f) ? c0 : c0 * beta;
+        const float cb = (beta == 1.0f) ? cv[i] : cv[i] * beta;
         cc[row] = cb + alpha * acc[i][j];
       }
     }

@@ -360,14 +360,23 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       const int row = tm * kSplitBM + row_in_tile;
       if (row < p.m) {
         const int col0 = tn * kBf16xBN + h * kBxColsPerWarp;
+        // C in batches of 16 columns: all loads of a batch are issued before its
+        // stores, so the batch pays one memory latency instead of sixteen
 #pragma unroll
-        for (int j = 0; j < kBxColsPerWarp; ++j) {
-          const int col = col0 + j;
-          if (col < p.n) {
-            float *cp = p.C + (int64_t)col * p.ldc + row;
-            const float c0 = *cp;
-            const float cb = (p.beta == 1.0f) ? c0 : c0 * p.beta;
-            *cp = cb + p.alpha * run[j];
+        for (int jb = 0; jb < kBxColsPerWarp; jb += 16) {
+          float cv[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = col0 + jb + j;
+            cv[j] = (col < p.n) ? p.C[(int64_t)col * p.ldc + row] : 0.f;
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = col0 + jb + j;
+            if (col < p.n) {
+              const float cb = (p.beta == 1.0f) ? cv[j] : cv[j] * p.beta;
+              p.C[(int64_t)col * p.ldc + row] = cb + p.alpha * run[jb + j];
+            }
           }
         }
       }
@@ -603,6 +612,12 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         tmem_ld16(lane_base + 384 + colt, hi_w);
         tmem_ld_wait();
         if (row < p.m) {
+          double cv[16];  // loads of the 16 columns first, then the stores
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = tn * kOzakiBN + colt + j;
+            cv[j] = (col < p.n) ? p.C[(int64_t)col * p.ldc + row] : 0.0;
+          }
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int col = tn * kOzakiBN + colt + j;
@@ -611,10 +626,8 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               double v = __hiloint2double((int)hi_w[j], (int)lo_w[j]);
               v = (ea == kNonFiniteExp || eb == kNonFiniteExp) ? __longlong_as_double(0x7ff8000000000000LL)
                                                                : ldexp(v, ea + eb);
-              double *cp = p.C + (int64_t)col * p.ldc + row;
-              const double c0 = *cp;
-              const double cb = (p.beta == 1.0) ? c0 : c0 * p.beta;
-              *cp = cb + p.alpha * v;
+              const double cb = (p.beta == 1.0) ? cv[j] : cv[j] * p.beta;
+              p.C[(int64_t)col * p.ldc + row] = cb + p.alpha * v;
             }
           }
         }

@@ -202,7 +202,9 @@ int gb300_gemm_grouped_ws(const gb300_gemm_problem *problems, int count, void *w
  * change between launches.
  *   form 0: plain forms, one persistent launch (as gb300_gemm_grouped);
  *   form 1: split forms, one call per problem (FP32: 6xBF16, FP64: Ozaki with
- *           the default slice count), captured in order. */
+ *           the default slice count), captured as 16 parallel branches
+ *           (longest work first onto the least-loaded branch), each branch
+ *           with its own workspace. */
 typedef struct gb300_grouped_graph_s *gb300_grouped_graph;
 int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int count, int form,
                                gb300_grouped_graph *out);
