@@ -102,6 +102,13 @@ def core() -> ctypes.CDLL:
         L.gb300_version.restype = ctypes.c_char_p
         L.gb300_selftest_wait_timeout.argtypes = [c_uint]
         L.gb300_tune_param.argtypes = [c_int, c_int]
+        L.gb300_autotune.argtypes = [c_int, c_char, c_char, c_int, c_int, c_int, c_void_p, c_int,
+                                     c_void_p, c_int, c_void_p, ctypes.POINTER(c_int)]
+        L.gb300_tune_lookup.argtypes = [c_int, c_int, c_int, c_int, ctypes.POINTER(c_int),
+                                        ctypes.POINTER(c_int)]
+        L.gb300_tune_cache_save.argtypes = [ctypes.c_char_p]
+        L.gb300_tune_cache_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(c_int)]
+        L.gb300_tune_cache_clear.restype = None
         L.gb300_grouped_workspace_bytes.argtypes = [c_int]
         L.gb300_grouped_workspace_bytes.restype = c_size_t
         L.gb300_gemm_grouped.argtypes = [c_void_p, c_int, c_void_p]
@@ -258,6 +265,38 @@ def selftest_wait_timeout(poll_limit: int = 4096) -> int:
 
 
 TUNE_BF16X_CHUNK = 1
+TUNE_BF16X = 0     # autotuner kinds
+TUNE_OZAKI = 1
+
+
+def autotune(kind, transa, transb, m, n, k, A, lda, B, ldb, stream=0):
+    """Tune the split form for this shape class on these device operands.
+    Returns (status, chosen products or slices)."""
+    out = c_int(0)
+    rc = core().gb300_autotune(kind, _b(transa), _b(transb), m, n, k, _ptr(A), lda, _ptr(B),
+                               ldb, c_void_p(stream), ctypes.byref(out))
+    return rc, out.value
+
+
+def tune_lookup(kind, m, n, k):
+    """(status, param, chunk) that products/slices = 0 resolve to for this shape."""
+    p, c = c_int(0), c_int(0)
+    rc = core().gb300_tune_lookup(kind, m, n, k, ctypes.byref(p), ctypes.byref(c))
+    return rc, p.value, c.value
+
+
+def tune_cache_save(path=None) -> int:
+    return core().gb300_tune_cache_save(path.encode() if path else None)
+
+
+def tune_cache_load(path=None):
+    n = c_int(0)
+    rc = core().gb300_tune_cache_load(path.encode() if path else None, ctypes.byref(n))
+    return rc, n.value
+
+
+def tune_cache_clear() -> None:
+    core().gb300_tune_cache_clear()
 
 
 class GemmProblem(ctypes.Structure):
@@ -339,5 +378,7 @@ CORE_SYMBOLS = [
     "gb300_dgemm_ozaki_run", "gb300_host_sgemm_bf16x", "gb300_host_dgemm_ozaki",
     "gb300_selftest_wait_timeout", "gb300_sgemm_bf16x_noalloc", "gb300_tune_param",
     "gb300_grouped_workspace_bytes", "gb300_gemm_grouped", "gb300_gemm_grouped_ws",
+    "gb300_autotune", "gb300_tune_lookup", "gb300_tune_cache_save", "gb300_tune_cache_load",
+    "gb300_tune_cache_clear",
     "gb300_grouped_graph_create", "gb300_grouped_graph_launch", "gb300_grouped_graph_destroy",
 ]

@@ -233,7 +233,7 @@ GB300_API int gb300_host_sgemm(char ta, char tb, int m, int n, int k, float alph
 GB300_API int gb300_host_sgemm_bf16x(char ta, char tb, int m, int n, int k, float alpha,
                                      const float *a, int lda, const float *b, int ldb, float beta,
                                      float *c, int ldc, int products) {
-  if (products != 3 && products != 6) return GB300_ERR_ARG;
+  if (products != 0 && products != 3 && products != 6) return GB300_ERR_ARG;
   return host_gemm<float>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, 1, products);
 }
 GB300_API int gb300_host_dgemm_ozaki(char ta, char tb, int m, int n, int k, double alpha,
@@ -273,7 +273,7 @@ GB300_API int gb300_sgemm_bf16x_ws(char ta, char tb, int m, int n, int k, float 
                                    const float *A, int lda, const float *B, int ldb, float beta,
                                    float *C, int ldc, int products, void *ws, size_t ws_bytes,
                                    void *stream) {
-  if (products != 3 && products != 6) return GB300_ERR_ARG;
+  if (products != 0 && products != 3 && products != 6) return GB300_ERR_ARG;
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
   if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
   unsigned *err = device_error_word();
@@ -284,7 +284,7 @@ GB300_API int gb300_sgemm_bf16x_ws(char ta, char tb, int m, int n, int k, float 
 GB300_API int gb300_sgemm_bf16x(char ta, char tb, int m, int n, int k, float alpha,
                                 const float *A, int lda, const float *B, int ldb, float beta,
                                 float *C, int ldc, int products, void *stream) {
-  if (products != 3 && products != 6) return GB300_ERR_ARG;
+  if (products != 0 && products != 3 && products != 6) return GB300_ERR_ARG;
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
   if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
   DeviceState *s = dev_state();
@@ -334,7 +334,8 @@ GB300_API int gb300_sgemm_bf16x_prepare(char ta, char tb, int m, int n, int k, c
 GB300_API int gb300_sgemm_bf16x_run(int m, int n, int k, float alpha, float beta, float *C,
                                     int ldc, int products, const void *ws, size_t ws_bytes,
                                     void *stream) {
-  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || (products != 3 && products != 6))
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) ||
+      (products != 0 && products != 3 && products != 6))
     return GB300_ERR_ARG;
   if (m == 0 || n == 0) return GB300_OK;
   unsigned *err = device_error_word();
@@ -573,6 +574,31 @@ GB300_API int gb300_selftest_wait_timeout(unsigned poll_limit) {
   if (reached == 1 && w == kErrTimeoutFull) return GB300_ERR_TIMEOUT;
   return reached == 2 ? GB300_OK : GB300_ERR_CUDA;
 }
+
+GB300_API int gb300_autotune(int kind, char ta, char tb, int m, int n, int k, const void *A,
+                             int lda, const void *B, int ldb, void *stream, int *chosen) {
+  if (kind != 0 && kind != 1) return GB300_ERR_ARG;
+  if (check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1) != GB300_OK || k == 0)
+    return GB300_ERR_ARG;
+  unsigned *err = device_error_word();
+  if (!err) return GB300_ERR_CUDA;
+  return autotune(kind, ta, tb, m, n, k, A, lda, B, ldb, static_cast<cudaStream_t>(stream), err,
+                  chosen);
+}
+GB300_API int gb300_tune_lookup(int kind, int m, int n, int k, int *param, int *chunk) {
+  if (kind != 0 && kind != 1) return GB300_ERR_ARG;
+  int p = 0, c = 0;
+  if (kind == 0) bf16x_resolve(m, n, k, &p, &c);
+  else p = ozaki_default_slices(m, n, k);
+  if (param) *param = p;
+  if (chunk) *chunk = c;
+  return tune_lookup(kind, m, n, k, nullptr, nullptr) ? GB300_OK : GB300_ERR_UNSUPPORTED;
+}
+GB300_API int gb300_tune_cache_save(const char *path) { return tune_cache_save(path); }
+GB300_API int gb300_tune_cache_load(const char *path, int *loaded) {
+  return tune_cache_load(path, loaded);
+}
+GB300_API void gb300_tune_cache_clear(void) { tune_cache_clear(); }
 
 GB300_API int gb300_tune_param(int param, int value) {
   switch (param) {

@@ -1,0 +1,337 @@
+// autotune.cu -- measured choice of the split forms' parameters, cached per
+// shape class.  It replaces the reference's compile-time tune headers
+// (wjc404/GEMM_AVX2 dgemm_tune.h, sgemm_tune.h, clamped and expanded in
+// src/gemm_set_parameters.h:1-61), which fix block sizes once per build for one
+// CPU model, by a run-time search on the GPU the library runs on:
+//
+//   BF16xP SGEMM: products P in {3, 6} x hi*hi chunk length in {2, 4, 8};
+//   Ozaki DGEMM : slice count S in [4, 12].
+//
+// A candidate qualifies when its max and Frobenius relative errors against a
+// near-exact FP64 reference do not exceed those of the plain kernel on the
+// same operands ("equal error"); the fastest qualifying candidate wins (for
+// Ozaki: the smallest S, which is also the fastest).  The reference is the
+// Ozaki form with S = 12 -- 84 bits per operand, whose truncation lies far
+// below FP64 rounding -- run on FP64 copies of the operands for FP32 problems,
+// where every product is then exact.
+//
+// Shape class: form and floor(log2) of m, n, k (the GEMM kernels read K-major
+// workspace whatever the transposes, and the precision choice depends on the
+// data, not the layout).  The cache is
+// a JSON file (gb300_tune_cache_save / _load; path argument or the
+// GB300_TUNE_CACHE environment variable); a missing or unreadable file leaves
+// the built-in defaults (P = 6, chunk 4, S = 8).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "plain_gemm.h"
+#include "split_gemm.h"
+
+namespace gb300 {
+
+struct TuneEntry {
+  int param = 0;       // products (BF16xP) or slices (Ozaki)
+  int chunk = 0;       // BF16xP hi*hi chunk length (0 for Ozaki)
+  double ms = 0;       // measured time of the chosen candidate
+  double err_max = 0, err_fro = 0;              // chosen candidate vs reference
+  double plain_max = 0, plain_fro = 0;          // plain kernel vs reference
+};
+
+static std::map<std::string, TuneEntry> g_tune;
+static std::mutex g_tune_mu;
+
+static int ilog2(int x) {
+  int l = 0;
+  while (x > 1) { x >>= 1; ++l; }
+  return l;
+}
+
+static std::string tune_key(int kind, int m, int n, int k) {
+  char buf[96];
+  snprintf(buf, sizeof buf, "%s:%d:%d:%d", kind == 0 ? "bf16x" : "ozaki", ilog2(m), ilog2(n),
+           ilog2(k));
+  return buf;
+}
+
+bool tune_lookup(int kind, int m, int n, int k, int *param, int *chunk) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(tune_key(kind, m, n, k));
+  if (it == g_tune.end()) return false;
+  if (param) *param = it->second.param;
+  if (chunk) *chunk = it->second.chunk;
+  return true;
+}
+
+// ---------------------------------------------------------------- device helpers
+// dst (FP64, column-major, ld = rows) = src (FP32, column-major, ld) over rows x cols
+__global__ void widen_kernel(const float *__restrict__ src, int ld, int rows, int cols,
+                             double *__restrict__ dst) {
+  const int64_t total = (int64_t)rows * cols;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e / rows), r = (int)(e % rows);
+    dst[e] = (double)src[(int64_t)c * ld + r];
+  }
+}
+
+// stats[0] += sum (t - r)^2, stats[1] += sum r^2, stats[2] = max |t - r| / |r|
+// (as the bit pattern of a non-negative double), over an m x n window.
+template <typename T>
+__global__ void err_stats_kernel(const T *__restrict__ t, int ldt, const double *__restrict__ r,
+                                 int ldr, int m, int n, double *stats) {
+  double s_d = 0, s_r = 0, mx = 0;
+  const int64_t total = (int64_t)m * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e / m), i = (int)(e % m);
+    const double tv = (double)t[(int64_t)c * ldt + i], rv = r[(int64_t)c * ldr + i];
+    const double d = tv - rv;
+    s_d += d * d;
+    s_r += rv * rv;
+    const double rel = rv != 0.0 ? fabs(d) / fabs(rv) : (d != 0.0 ? 1e300 : 0.0);
+    mx = rel > mx ? rel : mx;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s_d += __shfl_xor_sync(0xffffffffu, s_d, o);
+    s_r += __shfl_xor_sync(0xffffffffu, s_r, o);
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&stats[0], s_d);
+    atomicAdd(&stats[1], s_r);
+    atomicMax(reinterpret_cast<unsigned long long *>(&stats[2]),
+              (unsigned long long)__double_as_longlong(mx));
+  }
+}
+
+// ---------------------------------------------------------------- tuning run
+namespace {
+struct DevBuf {
+  void *p = nullptr;
+  ~DevBuf() { if (p) cudaFree(p); }
+  bool alloc(size_t n) { return cudaMalloc(&p, n > 0 ? n : 1) == cudaSuccess; }
+};
+
+struct Stats {
+  double max_rel, fro;
+};
+
+int measure(const void *t, bool t_double, int m, int n, const double *ref, double *dstats,
+            cudaStream_t st, Stats *out) {
+  if (cudaMemsetAsync(dstats, 0, 3 * sizeof(double), st) != cudaSuccess) return GB300_ERR_CUDA;
+  const int64_t total = (int64_t)m * n;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 2048) blocks = 2048;
+  if (t_double)
+    err_stats_kernel<double><<<blocks, 256, 0, st>>>(static_cast<const double *>(t), m, ref, m,
+                                                      m, n, dstats);
+  else
+    err_stats_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float *>(t), m, ref, m, m,
+                                                     n, dstats);
+  double h[3];
+  if (cudaMemcpyAsync(h, dstats, sizeof h, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  out->fro = h[1] > 0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
+  out->max_rel = h[2];
+  return GB300_OK;
+}
+}  // namespace
+
+int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int lda,
+             const void *B, int ldb, cudaStream_t st, unsigned *err, int *chosen) {
+  if (kind != 0 && kind != 1) return GB300_ERR_ARG;
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
+  if (ck != GB300_OK || k == 0) return ck == GB300_ERR_ARG ? ck : GB300_ERR_ARG;
+  const bool an = notrans(ta), bn = notrans(tb);
+  const int ar = an ? m : k, ac = an ? k : m, br = bn ? k : n, bc = bn ? n : k;
+  const size_t mn = (size_t)m * n;
+  DevBuf cref, ctest, a64, b64, ws, dstats;
+  const size_t ws_ref = split_workspace_bytes(1, m, n, k, 12);
+  size_t ws_need = ws_ref;
+  if (kind == 0) {
+    const size_t w6 = split_workspace_bytes(0, m, n, k, 6);
+    if (w6 > ws_need) ws_need = w6;
+  }
+  if (!cref.alloc(mn * 8) || !ctest.alloc(mn * (kind == 0 ? 4 : 8)) || !ws.alloc(ws_need) ||
+      !dstats.alloc(3 * sizeof(double)))
+    return GB300_ERR_NOMEM;
+  const double *Ad = static_cast<const double *>(A), *Bd = static_cast<const double *>(B);
+  int Alda = lda, Bldb = ldb;
+  if (kind == 0) {  // exact FP64 copies of the FP32 operands for the reference
+    if (!a64.alloc((size_t)ar * ac * 8) || !b64.alloc((size_t)br * bc * 8)) return GB300_ERR_NOMEM;
+    widen_kernel<<<1024, 256, 0, st>>>(static_cast<const float *>(A), lda, ar, ac,
+                                       static_cast<double *>(a64.p));
+    widen_kernel<<<1024, 256, 0, st>>>(static_cast<const float *>(B), ldb, br, bc,
+                                       static_cast<double *>(b64.p));
+    Ad = static_cast<const double *>(a64.p);
+    Bd = static_cast<const double *>(b64.p);
+    Alda = ar;
+    Bldb = br;
+  }
+  double *Cr = static_cast<double *>(cref.p);
+  double *stats = static_cast<double *>(dstats.p);
+  int rc = cudaMemsetAsync(Cr, 0, mn * 8, st) == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  if (rc == GB300_OK)
+    rc = ozaki_dgemm(ta, tb, m, n, k, 1.0, Ad, Alda, Bd, Bldb, 0.0, Cr, m, 12, ws.p, ws_ref, st,
+                     err);
+  if (rc != GB300_OK) return rc;
+
+  // run one candidate into ctest (C = 0 first: beta = 0 still multiplies C)
+  auto run = [&](int form, int param, int chunk) -> int {
+    if (cudaMemsetAsync(ctest.p, 0, mn * (kind == 0 ? 4 : 8), st) != cudaSuccess)
+      return GB300_ERR_CUDA;
+    if (kind == 0) {
+      float *Ct = static_cast<float *>(ctest.p);
+      if (form == 0)
+        return plain_sgemm(ta, tb, m, n, k, 1.0f, static_cast<const float *>(A), lda,
+                           static_cast<const float *>(B), ldb, 0.0f, Ct, m, st, err);
+      return split_sgemm(ta, tb, m, n, k, 1.0f, static_cast<const float *>(A), lda,
+                         static_cast<const float *>(B), ldb, 0.0f, Ct, m, param, ws.p, ws_need,
+                         st, err, chunk);
+    }
+    double *Ct = static_cast<double *>(ctest.p);
+    if (form == 0)
+      return plain_dgemm(ta, tb, m, n, k, 1.0, static_cast<const double *>(A), lda,
+                         static_cast<const double *>(B), ldb, 0.0, Ct, m, st, err);
+    return ozaki_dgemm(ta, tb, m, n, k, 1.0, static_cast<const double *>(A), lda,
+                       static_cast<const double *>(B), ldb, 0.0, Ct, m, param, ws.p, ws_need, st,
+                       err);
+  };
+  auto timed = [&](int param, int chunk, double *ms) -> int {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int r = run(1, param, chunk);  // warm-up (and the result measured for accuracy)
+    cudaEventRecord(e0, st);
+    for (int i = 0; i < 2 && r == GB300_OK; ++i) r = run(1, param, chunk);
+    cudaEventRecord(e1, st);
+    float t = 0;
+    if (r == GB300_OK && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / 2;
+    return r;
+  };
+
+  Stats plain{};
+  if ((rc = run(0, 0, 0)) != GB300_OK) return rc;
+  if ((rc = measure(ctest.p, kind == 1, m, n, Cr, stats, st, &plain)) != GB300_OK) return rc;
+
+  TuneEntry best;
+  bool found = false;
+  if (kind == 0) {
+    const int Ps[2] = {3, 6}, chunks[3] = {2, 4, 8};
+    for (int P : Ps)
+      for (int c : chunks) {
+        double ms = 0;
+        Stats e{};
+        if ((rc = timed(P, c, &ms)) != GB300_OK) return rc;
+        if ((rc = measure(ctest.p, false, m, n, Cr, stats, st, &e)) != GB300_OK) return rc;
+        const bool ok = e.max_rel <= plain.max_rel && e.fro <= plain.fro;
+        if (ok && (!found || ms < best.ms)) {
+          found = true;
+          best.param = P; best.chunk = c; best.ms = ms;
+          best.err_max = e.max_rel; best.err_fro = e.fro;
+        }
+      }
+    if (!found) { best.param = 6; best.chunk = 2; }  // most accurate candidate
+  } else {
+    for (int S = 4; S <= 12; ++S) {
+      double ms = 0;
+      Stats e{};
+      if ((rc = timed(S, 0, &ms)) != GB300_OK) return rc;
+      if ((rc = measure(ctest.p, true, m, n, Cr, stats, st, &e)) != GB300_OK) return rc;
+      if (e.max_rel <= plain.max_rel && e.fro <= plain.fro) {
+        found = true;
+        best.param = S; best.ms = ms; best.err_max = e.max_rel; best.err_fro = e.fro;
+        break;
+      }
+    }
+    if (!found) best.param = 12;
+  }
+  best.plain_max = plain.max_rel;
+  best.plain_fro = plain.fro;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[tune_key(kind, m, n, k)] = best;
+  }
+  if (chosen) *chosen = best.param;
+  return GB300_OK;
+}
+
+// ---------------------------------------------------------------- cache file
+static std::string cache_path(const char *path) {
+  if (path && *path) return path;
+  const char *env = getenv("GB300_TUNE_CACHE");
+  if (env && *env) return env;
+  const char *home = getenv("HOME");
+  return std::string(home ? home : ".") + "/.gemm_gb300_tune.json";
+}
+
+int tune_cache_save(const char *path) {
+  const std::string p = cache_path(path);
+  FILE *f = fopen(p.c_str(), "w");
+  if (!f) return GB300_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  fprintf(f, "{\"version\": 1, \"entries\": [\n");
+  size_t i = 0;
+  for (const auto &kv : g_tune) {
+    const TuneEntry &e = kv.second;
+    fprintf(f,
+            "  {\"key\": \"%s\", \"param\": %d, \"chunk\": %d, \"ms\": %.6g, \"err_max\": %.6g, "
+            "\"err_fro\": %.6g, \"plain_max\": %.6g, \"plain_fro\": %.6g}%s\n",
+            kv.first.c_str(), e.param, e.chunk, e.ms, e.err_max, e.err_fro, e.plain_max,
+            e.plain_fro, ++i < g_tune.size() ? "," : "");
+  }
+  fprintf(f, "]}\n");
+  return fclose(f) == 0 ? GB300_OK : GB300_ERR_ARG;
+}
+
+// Reads entries written by tune_cache_save.  Lines that do not parse, keys of
+// unknown forms and out-of-range values are skipped; an unreadable file
+// returns GB300_ERR_ARG and leaves the cache as it was.
+int tune_cache_load(const char *path, int *loaded) {
+  const std::string p = cache_path(path);
+  FILE *f = fopen(p.c_str(), "r");
+  if (loaded) *loaded = 0;
+  if (!f) return GB300_ERR_ARG;
+  char line[512];
+  std::map<std::string, TuneEntry> add;
+  while (fgets(line, sizeof line, f)) {
+    char key[96];
+    TuneEntry e;
+    if (sscanf(line,
+               " {\"key\": \"%95[^\"]\", \"param\": %d, \"chunk\": %d, \"ms\": %lf, \"err_max\": "
+               "%lf, \"err_fro\": %lf, \"plain_max\": %lf, \"plain_fro\": %lf",
+               key, &e.param, &e.chunk, &e.ms, &e.err_max, &e.err_fro, &e.plain_max,
+               &e.plain_fro) != 8)
+      continue;
+    const bool bx = strncmp(key, "bf16x:", 6) == 0, oz = strncmp(key, "ozaki:", 6) == 0;
+    if (bx && (e.param == 3 || e.param == 6) && e.chunk >= 0 && e.chunk <= 64)
+      add[key] = e;
+    else if (oz && e.param >= 2 && e.param <= kOzakiMaxSlices)
+      add[key] = e;
+  }
+  fclose(f);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (auto &kv : add) g_tune[kv.first] = kv.second;
+  if (loaded) *loaded = (int)add.size();
+  return GB300_OK;
+}
+
+void tune_cache_clear() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+}
+
+}  // namespace gb300

@@ -15,9 +15,11 @@ constexpr int kOzakiMaxSlices = 12;
 
 size_t split_workspace_bytes(int kind, int m, int n, int k, int param);
 
+// products 0 = the autotuned choice for the shape class (default 6); chunk0 =
+// hi*hi chunk length in 64-wide K blocks (0 = tuned / knob / default).
 int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
                 const float *B, int ldb, float beta, float *C, int ldc, int products, void *ws,
-                size_t ws_bytes, cudaStream_t st, unsigned *err);
+                size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0 = 0);
 
 int ozaki_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                 const double *B, int ldb, double beta, double *C, int ldc, int slices, void *ws,
@@ -29,7 +31,8 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
                         const float *B, int ldb, int products, void *ws, size_t ws_bytes,
                         cudaStream_t st);
 int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int ldc, int products,
-                    const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err);
+                    const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err,
+                    int chunk0 = 0);
 int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
                   int ldb, int slices, void *ws, size_t ws_bytes, cudaStream_t st);
 int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int slices,
@@ -41,5 +44,15 @@ void set_bf16x_chunk_kblocks(int c);
 
 // Default slice count for a shape class (autotune cache, falls back to 8).
 int ozaki_default_slices(int m, int n, int k);
+// Products / chunk of the BF16xP form for a shape class (cache, else 6 / 0).
+void bf16x_resolve(int m, int n, int k, int *products, int *chunk);
+
+// Autotuner (autotune.cu): kind 0 = BF16xP SGEMM, 1 = Ozaki DGEMM.
+bool tune_lookup(int kind, int m, int n, int k, int *param, int *chunk);
+int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int lda,
+             const void *B, int ldb, cudaStream_t st, unsigned *err, int *chosen);
+int tune_cache_save(const char *path);
+int tune_cache_load(const char *path, int *loaded);
+void tune_cache_clear();
 
 }  // namespace gb300

@@ -680,6 +680,10 @@ size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
   const int64_t Kp = round_up(k, kSplitBK);
   if (kind == 0) {
+    if (param == 0) {
+      int c = 0;
+      bf16x_resolve(m, n, k, &param, &c);
+    }
     if (param != 3 && param != 6) return 0;
     const int64_t Mp = round_up(m, kSplitBM), Np = round_up(n, kBf16xBN);
     return (size_t)((Mp + Np) * param * Kp * 2 + 1024);
@@ -690,7 +694,17 @@ size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
   return (size_t)((Mp + Np) * S * Kp * 2 + (Mp + Np) * 8 + 2048);
 }
 
-int ozaki_default_slices(int, int, int) { return 8; }
+int ozaki_default_slices(int m, int n, int k) {
+  int S = 0;
+  return tune_lookup(1, m, n, k, &S, nullptr) ? S : 8;
+}
+
+void bf16x_resolve(int m, int n, int k, int *products, int *chunk) {
+  int P = 0, c = 0;
+  if (!tune_lookup(0, m, n, k, &P, &c)) { P = 6; c = 0; }
+  *products = P;
+  *chunk = c;
+}
 
 // K blocks per TMEM accumulation chunk of the BF16xP GEMM (0 = default).
 static int g_bf16x_chunk = 0;
@@ -717,6 +731,10 @@ static Bf16xLayout bf16x_layout(int m, int n, int k, int products, void *ws) {
 int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, int lda,
                         const float *B, int ldb, int products, void *ws, size_t ws_bytes,
                         cudaStream_t st) {
+  if (products == 0) {
+    int c = 0;
+    bf16x_resolve(m, n, k, &products, &c);
+  }
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
   if (ck == GB300_ERR_ARG || (products != 3 && products != 6)) return GB300_ERR_ARG;
   if (ck < 0 || k == 0) return GB300_OK;
@@ -734,7 +752,12 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
 }
 
 int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int ldc, int products,
-                    const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err) {
+                    const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0) {
+  if (products == 0) {
+    int c = 0;
+    bf16x_resolve(m, n, k, &products, &c);
+    if (chunk0 == 0) chunk0 = c;
+  }
   if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || (products != 3 && products != 6))
     return GB300_ERR_ARG;
   if (m == 0 || n == 0) return GB300_OK;
@@ -758,7 +781,9 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
   {
     // order (i + j) of each segment's cross product, see seg_map()
     static const int order3[3] = {1, 1, 0}, order6[6] = {2, 2, 2, 1, 1, 0};
-    const int c0 = bf16x_chunk_kblocks() > 0 ? bf16x_chunk_kblocks() : kBxDefaultChunk;
+    const int c0 = chunk0 > 0                  ? chunk0
+                   : bf16x_chunk_kblocks() > 0 ? bf16x_chunk_kblocks()
+                                               : kBxDefaultChunk;
     for (int sg = 0; sg < 6; ++sg) {
       const int ord = sg < products ? (products == 3 ? order3[sg] : order6[sg]) : 2;
       p.chunk_len[sg] = ord == 0 ? c0 : (ord == 1 ? 4 * c0 : 0);
@@ -776,7 +801,12 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
 
 int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
                 const float *B, int ldb, float beta, float *C, int ldc, int products, void *ws,
-                size_t ws_bytes, cudaStream_t st, unsigned *err) {
+                size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0) {
+  if (products == 0) {
+    int c = 0;
+    bf16x_resolve(m, n, k, &products, &c);
+    if (chunk0 == 0) chunk0 = c;
+  }
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
   if (ck == GB300_ERR_ARG || (products != 3 && products != 6)) return GB300_ERR_ARG;
   if (ck < 0) return GB300_OK;
@@ -784,7 +814,7 @@ int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float 
     return plain_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err);
   int rc = split_sgemm_prepare(ta, tb, m, n, k, A, lda, B, ldb, products, ws, ws_bytes, st);
   if (rc != GB300_OK) return rc;
-  return split_sgemm_run(m, n, k, alpha, beta, C, ldc, products, ws, ws_bytes, st, err);
+  return split_sgemm_run(m, n, k, alpha, beta, C, ldc, products, ws, ws_bytes, st, err, chunk0);
 }
 
 // ----------------------------------------------------------------- Ozaki

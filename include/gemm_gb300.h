@@ -87,6 +87,8 @@ int gb300_sgemm(char transa, char transb, int m, int n, int k, float alpha, cons
  *                 C += Ah*Bh + Ah*Bl + Al*Bh                  ("3xBF16")
  *   products = 6: three BF16 terms per operand, all cross products whose
  *                 order sum is <= 2                              ("6xBF16")
+ *   products = 0: the autotuned choice for the shape class (gb300_autotune),
+ *                 else 6
  * Uses a device workspace of gb300_split_workspace_bytes() bytes, allocated
  * and cached by the library (the _ws variant takes the caller's instead). */
 int gb300_sgemm_bf16x(char transa, char transb, int m, int n, int k, float alpha, const float *A,
@@ -228,6 +230,29 @@ unsigned gb300_device_error(int clear);
  * word set to 0x10 (clear it with gb300_device_error(1)) and the CUDA context
  * still usable.  Faults, traps and hangs are never used to test this. */
 int gb300_selftest_wait_timeout(unsigned poll_limit);
+
+/* Autotuner (replaces the reference's compile-time tune headers dgemm_tune.h /
+ * sgemm_tune.h, src/gemm_set_parameters.h:1-61).  kind 0 = BF16xP SGEMM
+ * (chooses products 3/6 and the hi*hi chunk length), kind 1 = Ozaki DGEMM
+ * (chooses the slice count 4..12).  gb300_autotune runs the candidates on the
+ * given device operands (FP32 for kind 0, FP64 for kind 1) and keeps the fastest
+ * whose max and Frobenius relative errors against a near-exact FP64 reference
+ * (the Ozaki form with 12 slices) do not exceed the plain kernel's; the result
+ * is cached for the shape class (floor(log2) of m, n, k) and used whenever a
+ * split entry point gets products = 0 / slices = 0.  It allocates temporary
+ * device memory and synchronises `stream`.
+ * gb300_tune_lookup: the parameters products/slices = 0 resolve to for a
+ * shape (GB300_OK if a tuned entry exists, GB300_ERR_UNSUPPORTED if the
+ * defaults apply: 6 products, chunk 4, 8 slices).
+ * Cache file: gb300_tune_cache_save/_load (path NULL: $GB300_TUNE_CACHE, else
+ * $HOME/.gemm_gb300_tune.json); loading skips malformed or out-of-range
+ * entries and returns GB300_ERR_ARG for an unreadable file, keeping the cache. */
+int gb300_autotune(int kind, char transa, char transb, int m, int n, int k, const void *A,
+                   int lda, const void *B, int ldb, void *stream, int *chosen);
+int gb300_tune_lookup(int kind, int m, int n, int k, int *param, int *chunk);
+int gb300_tune_cache_save(const char *path);
+int gb300_tune_cache_load(const char *path, int *loaded);
+void gb300_tune_cache_clear(void);
 
 /* Process-wide tuning knobs (the role of the reference's compile-time tune
  * headers, dgemm_tune.h / sgemm_tune.h via src/gemm_set_parameters.h:1-61).

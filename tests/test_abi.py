@@ -106,3 +106,32 @@ def test_grouped_problem_struct_layout_and_args():
     bad2 = dict(bad, lda=4, precision="z")
     assert g.gemm_grouped([bad2]) == g.ERR_ARG
     assert g.gemm_grouped([]) == g.OK
+
+
+def test_tune_cache_roundtrip_and_corruption(tmp_path):
+    g.tune_cache_clear()
+    # defaults without a tuned entry
+    assert g.tune_lookup(g.TUNE_OZAKI, 1000, 1000, 1000) == (g.ERR_UNSUPPORTED, 8, 0)
+    assert g.tune_lookup(g.TUNE_BF16X, 1000, 1000, 1000) == (g.ERR_UNSUPPORTED, 6, 0)
+    # a hand-written cache file with good, malformed and out-of-range lines
+    f = tmp_path / "tune.json"
+    f.write_text('{"version": 1, "entries": [\n'
+                 '  {"key": "ozaki:9:9:9", "param": 10, "chunk": 0, "ms": 1, "err_max": 1e-14, '
+                 '"err_fro": 1e-16, "plain_max": 2e-14, "plain_fro": 1e-15},\n'
+                 '  {"key": "bf16x:9:9:9", "param": 3, "chunk": 8, "ms": 1, "err_max": 1e-5, '
+                 '"err_fro": 1e-7, "plain_max": 2e-5, "plain_fro": 1e-6},\n'
+                 '  {"key": "ozaki:8:8:8", "param": 99, "chunk": 0, "ms": 1, "err_max": 0, '
+                 '"err_fro": 0, "plain_max": 0, "plain_fro": 0},\n'
+                 '  garbage line\n]}\n')
+    assert g.tune_cache_load(str(f)) == (g.OK, 2)
+    assert g.tune_lookup(g.TUNE_OZAKI, 1000, 600, 700) == (g.OK, 10, 0)      # log2 buckets 9
+    assert g.tune_lookup(g.TUNE_BF16X, 512, 1023, 600) == (g.OK, 3, 8)
+    assert g.tune_lookup(g.TUNE_OZAKI, 300, 300, 300)[0] == g.ERR_UNSUPPORTED  # rejected entry
+    assert g.split_workspace_bytes(0, 512, 512, 512, 0) == g.split_workspace_bytes(0, 512, 512, 512, 3)
+    out = tmp_path / "saved.json"
+    assert g.tune_cache_save(str(out)) == g.OK
+    g.tune_cache_clear()
+    assert g.tune_cache_load(str(out)) == (g.OK, 2)
+    assert g.tune_cache_load(str(tmp_path / "missing.json"))[0] == g.ERR_ARG
+    assert g.tune_lookup(g.TUNE_OZAKI, 1000, 600, 700) == (g.OK, 10, 0)        # cache kept
+    g.tune_cache_clear()
