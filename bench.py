@@ -353,7 +353,10 @@ def run_ours(args, torch, rank, world):
         e2e = {"value": round(prob.flops / dt / 1e12, 3), "unit": "TFLOP/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": m * n * esz,
                "ms_per_step": round(dt * 1e3, 3), "api": "gb300_host_%s" %
-               ("dgemm_ozaki" if is_d else "sgemm_bf16x")}
+               ("dgemm_ozaki" if is_d else "sgemm_bf16x"),
+               "transfer": "pinned host buffers; the split/slice kernels read A and B and the "
+                           "GEMM epilogue reads and writes C in host memory over the coherent "
+                           "CPU-GPU link (bytes above cross it once per step)"}
     except StopIteration:
         pass
     except Exception as ex:  # noqa: BLE001

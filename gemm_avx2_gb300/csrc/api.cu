@@ -122,6 +122,28 @@ void *cached_workspace(DeviceState *s, cudaStream_t st, size_t need) {
 }
 
 // ---------------------------------------------------------------- host-pointer staging
+// True when kernels may dereference these host pointers directly: the device
+// reads pageable memory through the host's page tables (coherent CPU-GPU
+// systems such as Grace + GB300), or every pointer is page-locked / registered.
+static bool host_direct_ok(const void *a, const void *b, const void *c) {
+  int dev = 0, pageable = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) ==
+          cudaSuccess &&
+      pageable == 1)
+    return true;
+  for (const void *p : {a, b, c}) {
+    if (!p) continue;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (at.type != cudaMemoryTypeHost) return false;
+  }
+  return true;
+}
+
 // form: 0 = plain kernel; 1 = BF16xP split (FP32, param = products);
 //       2 = Ozaki (FP64, param = slices).
 template <typename T>
@@ -141,6 +163,27 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
     return GB300_ERR_CUDA;
   cudaStream_t st = s->stage_stream;
   const bool need_ab = alpha != T(0) && k > 0;
+  if (form != 0 && host_direct_ok(a, b, c)) {
+    // Split forms read A and B once (split / slice kernels, plain loads) and
+    // read and write each C element once (GEMM epilogue): they run directly on
+    // the caller's host memory over the coherent CPU-GPU link, no staging.
+    const size_t wneed = need_ab ? split_workspace_bytes(form == 1 ? 0 : 1, m, n, k, param) : 0;
+    void *ws = wneed ? cached_workspace(s, st, wneed) : nullptr;
+    if (wneed && !ws) return GB300_ERR_NOMEM;
+    int rc;
+    if constexpr (sizeof(T) == 8)
+      rc = ozaki_dgemm(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, param, ws, wneed, st,
+                       s->err);
+    else
+      rc = split_sgemm(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, param, ws, wneed, st,
+                       s->err);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (rc != GB300_OK) return rc;
+    if (e != cudaSuccess) return GB300_ERR_CUDA;
+    unsigned word = 0;
+    cudaMemcpy(&word, s->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    return word ? GB300_ERR_TIMEOUT : GB300_OK;
+  }
   // Device copies use leading dimensions rounded up to 16 bytes so that the
   // TMA path applies whatever the host ld was.
   const int epl = 16 / (int)sizeof(T);

@@ -206,3 +206,24 @@ def test_ozaki_exact_at_chunk_bound(orc):
     model = osp.ozaki_gemm_model(A, B, S)
     assert np.array_equal(got, model), np.abs(got - model).max()
     assert g.device_error() == 0
+
+
+@pytest.mark.parametrize("form", ["bf16x", "ozaki"])
+def test_host_pointer_split_forms(orc, form):
+    """gb300_host_sgemm_bf16x / gb300_host_dgemm_ozaki on pageable host arrays with
+    padded leading dimensions: results within the split forms' bounds and the
+    ldc padding rows untouched (the kernels access host memory directly on
+    coherent CPU-GPU systems, or stage it otherwise)."""
+    dt = np.float32 if form == "bf16x" else np.float64
+    m, n, k = 333, 290, 517
+    A = orc.uniform((k + 3, m), dt, 71, 0)        # transa = T, lda = k + 3
+    B = orc.uniform((n + 1, k), dt, 71, 1)        # transb = T, ldb = n + 1
+    C = orc.uniform((m + 2, n), dt, 71, 2)
+    C0 = C.copy(order="F")
+    param = 6 if form == "bf16x" else 8
+    assert g.host_split_gemm(form, "T", "T", m, n, k, 0.75, A, k + 3, B, n + 1, -1.25, C, m + 2,
+                             param) == g.OK
+    truth = orc.dot2gemm("T", "T", m, n, k, 0.75, A, k + 3, B, n + 1, -1.25, C0, m + 2)
+    d = np.linalg.norm(C[:m].astype(np.float64) - truth) / np.linalg.norm(truth)
+    assert d < (1e-6 if form == "bf16x" else 1e-15), d
+    assert np.array_equal(C[m:], C0[m:])
