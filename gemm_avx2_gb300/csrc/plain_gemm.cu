@@ -110,11 +110,14 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
   const int wm = warp & 1, wn = warp >> 1;
   const int tm = wm * 8 + (lane & 7);
   const int tn = wn * 4 + (lane >> 3);
-  float acc[8][8];
+  // accumulators as column pairs: with MN-major B one packed FMA
+  // (fma.rn.f32x2) updates two outputs per issue slot, with the same
+  // round-to-nearest FMA per element
+  float2 acc[8][4];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
 
   for (int kt = 0; kt < kStages - 1 && kt < ktiles; ++kt) fill(kt);
 
@@ -138,12 +141,32 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
       float a[8][4], b[8][4];
       f32_load_frag<AK>(ta, tm, kq, a);
       f32_load_frag<BK_>(tb, tn, kq, b);
+      if constexpr (!BK_) {
+        // MN-major B: (b[2jp], b[2jp+1]) are neighbours of one float4 load
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
+        for (int q = 0; q < 4; ++q) {
+          float2 bp[4];
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
+          for (int jp = 0; jp < 4; ++jp) bp[jp] = make_float2(b[2 * jp][q], b[2 * jp + 1][q]);
 #pragma unroll
-          for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i][q], b[j][q], acc[i][j]);
+          for (int i = 0; i < 8; ++i) {
+            const float2 ab = make_float2(a[i][q], a[i][q]);
+#pragma unroll
+            for (int jp = 0; jp < 4; ++jp) acc[i][jp] = __ffma2_rn(ab, bp[jp], acc[i][jp]);
+          }
+        }
+      } else {
+        // K-major B: pairs would need register moves; scalar FFMA on the halves
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int jp = 0; jp < 4; ++jp) {
+              acc[i][jp].x = fmaf(a[i][q], b[2 * jp][q], acc[i][jp].x);
+              acc[i][jp].y = fmaf(a[i][q], b[2 * jp + 1][q], acc[i][jp].y);
+            }
+      }
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
@@ -168,7 +191,7 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
       const int row = m0 + f32_row<AK>(tm, i);
       if (row < m) {
         const float cb = (beta == 1.0f) ? cv[i] : cv[i] * beta;
-        cc[row] = cb + alpha * acc[i][j];
+        cc[row] = cb + alpha * ((j & 1) ? acc[i][j >> 1].y : acc[i][j >> 1].x);
       }
     }
   }

@@ -158,12 +158,27 @@ __device__ __forceinline__ int row_exponent(unsigned long long amax_bits) {
   return e;
 }
 
+// Ozaki step 1b: the per-row exponents, once (the slice kernel and the GEMM
+// epilogue read them instead of recomputing frexp per element).
+__global__ void row_exponent_kernel(const unsigned long long *__restrict__ amax, int R,
+                                    int *__restrict__ ex) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < R) ex[r] = row_exponent(amax[r]);
+}
+
+// 2^e as a double when it is a normal number, built from the exponent bits
+// (one multiply then scales exactly); ldexp outside that range.
+__device__ __forceinline__ double scale_pow2(double v, int e) {
+  if (e >= -1022 && e <= 1023) return v * __longlong_as_double((long long)(e + 1023) << 52);
+  return ldexp(v, e);
+}
+
 // Ozaki step 2: slices.  x = op(X)(r,k) * 2^-E_r in (-1,1); for s = 1..S:
 // y = x * 128, d_s = trunc(y) (|d_s| <= 127), x = y - d_s (exact).
 // out: S blocks of Rp rows x Kp (row-major BF16), slice s at rows (s-1)*Rp.
 __global__ void __launch_bounds__(256) ozaki_slice_kernel(
     const double *__restrict__ X, int ld, int R, int K, int kcontig, int Rp, int Kp, int S,
-    const unsigned long long *__restrict__ amax, __nv_bfloat16 *__restrict__ out) {
+    const int *__restrict__ ex, __nv_bfloat16 *__restrict__ out) {
   __shared__ double tile[32][65];
   const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 64;
   load_tile_32x64<double>(X, ld, R, K, kcontig != 0, r0, k0, tile);
@@ -173,7 +188,7 @@ __global__ void __launch_bounds__(256) ozaki_slice_kernel(
   for (int p = 0; p < 4; ++p) {
     const int r = p * 8 + (tid >> 5), kk = (tid & 31) * 2;
     const int gr = r0 + r;
-    const int e = (gr < R) ? row_exponent(amax[gr]) : 0;
+    const int e = (gr < R) ? ex[gr] : 0;
     double x0 = tile[r][kk], x1 = tile[r][kk + 1];
     const bool bad = (e == kNonFiniteExp);
     if (!bad) { x0 = ldexp(x0, -e); x1 = ldexp(x1, -e); }
@@ -402,7 +417,7 @@ struct OzakiParams {
   double alpha, beta;
   double *C;
   int ldc;
-  const unsigned long long *amaxA, *amaxB;
+  const int *expA, *expB;  // per-row / per-column scale exponents
   unsigned *err;
 };
 
@@ -603,7 +618,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       if (!ok) break;
       // final epilogue: C = alpha * 2^(E_i + F_j) * res + beta * C
       const int row = tm * kSplitBM + row_in_tile;
-      const int ea = (row < p.m) ? row_exponent(p.amaxA[row]) : 0;
+      const int ea = (row < p.m) ? p.expA[row] : 0;
 #pragma unroll
       for (int g4 = 0; g4 < 4; ++g4) {
         const int colt = h * 64 + g4 * 16;
@@ -622,10 +637,10 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           for (int j = 0; j < 16; ++j) {
             const int col = tn * kOzakiBN + colt + j;
             if (col < p.n) {
-              const int eb = row_exponent(p.amaxB[col]);
+              const int eb = p.expB[col];
               double v = __hiloint2double((int)hi_w[j], (int)lo_w[j]);
               v = (ea == kNonFiniteExp || eb == kNonFiniteExp) ? __longlong_as_double(0x7ff8000000000000LL)
-                                                               : ldexp(v, ea + eb);
+                                                               : scale_pow2(v, ea + eb);
               const double cb = (p.beta == 1.0) ? cv[j] : cv[j] * p.beta;
               p.C[(int64_t)col * p.ldc + row] = cb + p.alpha * v;
             }
@@ -691,7 +706,7 @@ size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
   int S = param > 0 ? param : ozaki_default_slices(m, n, k);
   if (S < 2 || S > kOzakiMaxSlices) return 0;
   const int64_t Mp = round_up(m, kSplitBM), Np = round_up(n, kOzakiBN);
-  return (size_t)((Mp + Np) * S * Kp * 2 + (Mp + Np) * 8 + 2048);
+  return (size_t)((Mp + Np) * S * Kp * 2 + (Mp + Np) * 12 + 2048);
 }
 
 int ozaki_default_slices(int m, int n, int k) {
@@ -822,6 +837,7 @@ struct OzakiLayout {
   int64_t Kp, Mp, Np;
   __nv_bfloat16 *As, *Bs;
   unsigned long long *amaxA, *amaxB;
+  int *expA, *expB;
 };
 static OzakiLayout ozaki_layout(int m, int n, int k, int S, void *ws) {
   OzakiLayout L;
@@ -834,6 +850,8 @@ static OzakiLayout ozaki_layout(int m, int n, int k, int S, void *ws) {
   L.Bs = L.As + S * L.Mp * L.Kp;
   L.amaxA = reinterpret_cast<unsigned long long *>(L.Bs + S * L.Np * L.Kp);
   L.amaxB = L.amaxA + L.Mp;
+  L.expA = reinterpret_cast<int *>(L.amaxB + L.Np);
+  L.expB = L.expA + L.Mp;
   return L;
 }
 
@@ -862,10 +880,12 @@ int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int ld
   };
   absmax(A, lda, m, !an, L.amaxA);
   absmax(B, ldb, n, bn, L.amaxB);
+  row_exponent_kernel<<<(unsigned)((L.Mp + L.Np + 255) / 256), 256, 0, st>>>(
+      L.amaxA, (int)(L.Mp + L.Np), L.expA);  // amaxB and expB follow amaxA and expA
   ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Mp / 32)), 256, 0, st>>>(
-      A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, S, L.amaxA, L.As);
+      A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, S, L.expA, L.As);
   ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Np / 32)), 256, 0, st>>>(
-      B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, S, L.amaxB, L.Bs);
+      B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, S, L.expB, L.Bs);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
@@ -892,7 +912,7 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
   p.S = S; p.KB = (int)(L.Kp / kSplitBK);
   p.Mp = (int)L.Mp; p.Np = (int)L.Np;
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc;
-  p.amaxA = L.amaxA; p.amaxB = L.amaxB; p.err = err;
+  p.expA = L.expA; p.expB = L.expB; p.err = err;
   if (cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kOzSmem) != cudaSuccess)
     return GB300_ERR_CUDA;
