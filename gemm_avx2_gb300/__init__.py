@@ -109,6 +109,10 @@ def core() -> ctypes.CDLL:
         L.gb300_tune_cache_save.argtypes = [ctypes.c_char_p]
         L.gb300_tune_cache_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(c_int)]
         L.gb300_tune_cache_clear.restype = None
+        for nm, F in (("gb300_dtrsm", c_double), ("gb300_strsm", c_float),
+                      ("gb300_dtrmm", c_double), ("gb300_strmm", c_float)):
+            getattr(L, nm).argtypes = [c_char, c_char, c_char, c_char, c_int, c_int, F, c_void_p,
+                                       c_int, c_void_p, c_int, c_int, c_void_p]
         L.gb300_grouped_workspace_bytes.argtypes = [c_int]
         L.gb300_grouped_workspace_bytes.restype = c_size_t
         L.gb300_gemm_grouped.argtypes = [c_void_p, c_int, c_void_p]
@@ -251,6 +255,22 @@ def host_split_gemm(form, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, 
              ldc, param)
 
 
+def trsm(precision, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, form=0,
+         stream=0) -> int:
+    """Triangular solve on device buffers (BLAS TRSM semantics); X overwrites B."""
+    f = core().gb300_dtrsm if precision == "d" else core().gb300_strsm
+    return f(_b(side), _b(uplo), _b(transa), _b(diag), m, n, alpha, _ptr(A), lda, _ptr(B), ldb,
+             form, c_void_p(stream))
+
+
+def trmm(precision, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, form=0,
+         stream=0) -> int:
+    """Triangular multiply on device buffers (BLAS TRMM semantics), in place on B."""
+    f = core().gb300_dtrmm if precision == "d" else core().gb300_strmm
+    return f(_b(side), _b(uplo), _b(transa), _b(diag), m, n, alpha, _ptr(A), lda, _ptr(B), ldb,
+             form, c_void_p(stream))
+
+
 def split_workspace_bytes(kind: int, m: int, n: int, k: int, param: int) -> int:
     return core().gb300_split_workspace_bytes(kind, m, n, k, param)
 
@@ -379,6 +399,6 @@ CORE_SYMBOLS = [
     "gb300_selftest_wait_timeout", "gb300_sgemm_bf16x_noalloc", "gb300_tune_param",
     "gb300_grouped_workspace_bytes", "gb300_gemm_grouped", "gb300_gemm_grouped_ws",
     "gb300_autotune", "gb300_tune_lookup", "gb300_tune_cache_save", "gb300_tune_cache_load",
-    "gb300_tune_cache_clear",
+    "gb300_tune_cache_clear", "gb300_dtrsm", "gb300_strsm", "gb300_dtrmm", "gb300_strmm",
     "gb300_grouped_graph_create", "gb300_grouped_graph_launch", "gb300_grouped_graph_destroy",
 ]

@@ -591,6 +591,47 @@ GB300_API int gb300_grouped_graph_launch(gb300_grouped_graph g, void *stream) {
                                                                                     : GB300_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------- TRSM / TRMM
+template <typename T>
+static int tr_api(int solve, char side, char uplo, char ta, char diag, int m, int n, T alpha,
+                  const T *A, int lda, T *B, int ldb, int form, void *stream) {
+  const int ck = tr_check(side, uplo, ta, diag, m, n, lda, ldb);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  if (form != 0 && form != 1) return GB300_ERR_ARG;
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t need = tr_workspace_bytes(sizeof(T) == 8, form, m, n);
+  std::lock_guard<std::mutex> lk(s->mu);
+  void *ws = need ? cached_workspace(s, st, need) : nullptr;
+  if (need && !ws) return GB300_ERR_NOMEM;
+  if constexpr (sizeof(T) == 8)
+    return trsm_d(solve, side, uplo, ta, diag, m, n, alpha, A, lda, B, ldb, form, ws, need, st,
+                  s->err);
+  else
+    return trsm_s(solve, side, uplo, ta, diag, m, n, alpha, A, lda, B, ldb, form, ws, need, st,
+                  s->err);
+}
+
+GB300_API int gb300_dtrsm(char side, char uplo, char transa, char diag, int m, int n,
+                          double alpha, const double *A, int lda, double *B, int ldb, int form,
+                          void *stream) {
+  return tr_api<double>(1, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, form, stream);
+}
+GB300_API int gb300_strsm(char side, char uplo, char transa, char diag, int m, int n, float alpha,
+                          const float *A, int lda, float *B, int ldb, int form, void *stream) {
+  return tr_api<float>(1, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, form, stream);
+}
+GB300_API int gb300_dtrmm(char side, char uplo, char transa, char diag, int m, int n,
+                          double alpha, const double *A, int lda, double *B, int ldb, int form,
+                          void *stream) {
+  return tr_api<double>(0, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, form, stream);
+}
+GB300_API int gb300_strmm(char side, char uplo, char transa, char diag, int m, int n, float alpha,
+                          const float *A, int lda, float *B, int ldb, int form, void *stream) {
+  return tr_api<float>(0, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, form, stream);
+}
+
 GB300_API unsigned gb300_device_error(int clear) {
   unsigned *err = device_error_word();
   if (!err) return 0xFFFFFFFFu;

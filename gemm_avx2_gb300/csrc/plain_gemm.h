@@ -57,4 +57,15 @@ int grouped_launch_blob(void *dev_blob, int count_used, int total_tiles, cudaStr
 int grouped_plain(const gb300_gemm_problem *P, int count, void *ws, size_t ws_bytes,
                   cudaStream_t st, unsigned *err);
 
+// Blocked TRSM / TRMM (trsm.cu): solve = 1 TRSM, 0 TRMM; form 0 plain GEMM
+// updates, 1 split-form updates (workspace of tr_workspace_bytes bytes).
+size_t tr_workspace_bytes(int is_double, int form, int m, int n);
+int tr_check(char side, char uplo, char transa, char diag, int m, int n, int lda, int ldb);
+int trsm_d(int solve, char side, char uplo, char ta, char diag, int m, int n, double alpha,
+           const double *A, int lda, double *B, int ldb, int form, void *ws, size_t wsb,
+           cudaStream_t st, unsigned *err);
+int trsm_s(int solve, char side, char uplo, char ta, char diag, int m, int n, float alpha,
+           const float *A, int lda, float *B, int ldb, int form, void *ws, size_t wsb,
+           cudaStream_t st, unsigned *err);
+
 }  // namespace gb300

@@ -1,0 +1,332 @@
+// trsm.cu -- blocked triangular solve (TRSM) and triangular multiply (TRMM)
+// built on this library's GEMM, the BLAS-3 routines that spend most of their
+// time in GEMM updates.  The reference ships TRSM/TRMM only as OpenBLAS-style
+// packed-panel kernels (OpenBLAS-like_implementation/TRSM_KERNEL_*_simplified.c,
+// trmm_kernel_4x8_simplified.c), outside its built library; this file gives them
+// the BLAS interface and semantics:
+//
+//   TRSM: side 'L': op(A) X = alpha B,  side 'R': X op(A) = alpha B   (X -> B)
+//   TRMM: side 'L': B = alpha op(A) B,  side 'R': B = alpha B op(A)
+//
+// A is triangular (uplo 'U'/'L', diag 'U' unit / 'N'), op(A) = A or A^T.  Both
+// reduce to passes over 64-wide blocks of the "effective" triangle of op(A)
+// (lower when uplo == 'L' xor op transposes): one small kernel per diagonal
+// block (the triangle in shared memory, one thread per right-hand side) and
+// one GEMM per block for the off-diagonal part -- the plain kernel (form 0) or
+// the tensor-core split form (form 1: Ozaki for FP64, 6xBF16 for FP32).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+#include "plain_gemm.h"
+#include "split_gemm.h"
+
+namespace gb300 {
+
+constexpr int kTrNb = 64;     // diagonal block size
+constexpr int kTrCols = 128;  // right-hand sides per CTA of the diagonal kernels
+
+// op(A)(r, c) of the diagonal block starting at (d0, d0).
+template <typename T>
+__device__ __forceinline__ T opA_at(const T *A, int lda, bool trans, int d0, int r, int c) {
+  return trans ? A[(int64_t)(d0 + r) * lda + d0 + c] : A[(int64_t)(d0 + c) * lda + d0 + r];
+}
+
+// Load the nb x nb diagonal block of op(A) into shared memory as T[r][c] (only
+// the effective triangle is read; the rest is set to zero).
+template <typename T>
+__device__ void load_triangle(const T *A, int lda, bool trans, bool lower, bool unit, int d0,
+                              int nb, T *Ts) {
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int r = e / nb, c = e % nb;
+    const bool in = lower ? (c <= r) : (c >= r);
+    T v = T(0);
+    if (r == c && unit) v = T(1);
+    else if (in) v = opA_at(A, lda, trans, d0, r, c);
+    Ts[r * kTrNb + c] = v;
+  }
+}
+
+// Left side: the rows [d0, d0+nb) of B, all columns; one thread per column.
+//   solve = true : X = T^-1 Bblk (forward if lower, backward if upper)
+//   solve = false: X = T Bblk
+template <typename T>
+__global__ void __launch_bounds__(kTrCols) diag_left_kernel(const T *__restrict__ A, int lda,
+                                                            int trans, int lower, int unit,
+                                                            int d0, int nb, T *B, int ldb, int n,
+                                                            int solve) {
+  extern __shared__ uint8_t sm[];
+  T *Ts = reinterpret_cast<T *>(sm);                 // [kTrNb][kTrNb]
+  T *Xs = Ts + kTrNb * kTrNb;                        // [kTrNb][kTrCols]
+  load_triangle<T>(A, lda, trans != 0, lower != 0, unit != 0, d0, nb, Ts);
+  const int j = blockIdx.x * kTrCols + threadIdx.x;
+  const bool live = j < n;
+  T *col = B + (int64_t)j * ldb + d0;
+  for (int r = 0; r < nb; ++r) Xs[r * kTrCols + threadIdx.x] = live ? col[r] : T(0);
+  __syncthreads();
+  T *x = Xs + threadIdx.x;
+  if (solve) {
+    if (lower) {
+      for (int r = 0; r < nb; ++r) {
+        T s = x[r * kTrCols];
+        for (int c = 0; c < r; ++c) s -= Ts[r * kTrNb + c] * x[c * kTrCols];
+        x[r * kTrCols] = unit ? s : s / Ts[r * kTrNb + r];
+      }
+    } else {
+      for (int r = nb - 1; r >= 0; --r) {
+        T s = x[r * kTrCols];
+        for (int c = r + 1; c < nb; ++c) s -= Ts[r * kTrNb + c] * x[c * kTrCols];
+        x[r * kTrCols] = unit ? s : s / Ts[r * kTrNb + r];
+      }
+    }
+  } else {
+    // X = T Bblk in place: lower -> bottom row first, upper -> top row first
+    if (lower) {
+      for (int r = nb - 1; r >= 0; --r) {
+        T s = T(0);
+        for (int c = 0; c <= r; ++c) s += Ts[r * kTrNb + c] * x[c * kTrCols];
+        x[r * kTrCols] = s;
+      }
+    } else {
+      for (int r = 0; r < nb; ++r) {
+        T s = T(0);
+        for (int c = r; c < nb; ++c) s += Ts[r * kTrNb + c] * x[c * kTrCols];
+        x[r * kTrCols] = s;
+      }
+    }
+  }
+  __syncthreads();
+  if (live)
+    for (int r = 0; r < nb; ++r) col[r] = Xs[r * kTrCols + threadIdx.x];
+}
+
+// Right side: the columns [d0, d0+nb) of B, all rows; one thread per row.
+//   solve = true : X = Bblk T^-1 (forward over columns if upper, backward if lower)
+//   solve = false: X = Bblk T
+template <typename T>
+__global__ void __launch_bounds__(kTrCols) diag_right_kernel(const T *__restrict__ A, int lda,
+                                                             int trans, int lower, int unit,
+                                                             int d0, int nb, T *B, int ldb, int m,
+                                                             int solve) {
+  extern __shared__ uint8_t sm[];
+  T *Ts = reinterpret_cast<T *>(sm);
+  T *Xs = Ts + kTrNb * kTrNb;                        // [kTrNb][kTrCols]: column c, row slot
+  load_triangle<T>(A, lda, trans != 0, lower != 0, unit != 0, d0, nb, Ts);
+  const int i = blockIdx.x * kTrCols + threadIdx.x;
+  const bool live = i < m;
+  for (int c = 0; c < nb; ++c)
+    Xs[c * kTrCols + threadIdx.x] = live ? B[(int64_t)(d0 + c) * ldb + i] : T(0);
+  __syncthreads();
+  T *x = Xs + threadIdx.x;
+  if (solve) {
+    if (!lower) {
+      for (int c = 0; c < nb; ++c) {
+        T s = x[c * kTrCols];
+        for (int r = 0; r < c; ++r) s -= x[r * kTrCols] * Ts[r * kTrNb + c];
+        x[c * kTrCols] = unit ? s : s / Ts[c * kTrNb + c];
+      }
+    } else {
+      for (int c = nb - 1; c >= 0; --c) {
+        T s = x[c * kTrCols];
+        for (int r = c + 1; r < nb; ++r) s -= x[r * kTrCols] * Ts[r * kTrNb + c];
+        x[c * kTrCols] = unit ? s : s / Ts[c * kTrNb + c];
+      }
+    }
+  } else {
+    // X = Bblk T in place: upper -> last column first, lower -> first column first
+    if (!lower) {
+      for (int c = nb - 1; c >= 0; --c) {
+        T s = T(0);
+        for (int r = 0; r <= c; ++r) s += x[r * kTrCols] * Ts[r * kTrNb + c];
+        x[c * kTrCols] = s;
+      }
+    } else {
+      for (int c = 0; c < nb; ++c) {
+        T s = T(0);
+        for (int r = c; r < nb; ++r) s += x[r * kTrCols] * Ts[r * kTrNb + c];
+        x[c * kTrCols] = s;
+      }
+    }
+  }
+  __syncthreads();
+  if (live)
+    for (int c = 0; c < nb; ++c) B[(int64_t)(d0 + c) * ldb + i] = Xs[c * kTrCols + threadIdx.x];
+}
+
+// B(m x n window) *= s, or = 0 exactly when s == 0 (BLAS: alpha = 0 sets B to zero).
+template <typename T>
+__global__ void scale_b_kernel(int m, int n, T s, T *B, int ldb) {
+  const int64_t total = (int64_t)m * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    T *p = B + (e / m) * (int64_t)ldb + (e % m);
+    *p = (s == T(0)) ? T(0) : *p * s;
+  }
+}
+
+// ---------------------------------------------------------------- host driver
+static int in_set(char c, const char *set) {
+  for (; *set; ++set)
+    if (c == *set) return 1;
+  return 0;
+}
+
+// Off-diagonal update: C(mm x nn) -= op1(X) op2(Y) (solve) or += (multiply)
+// through the library's GEMM.
+template <typename T>
+static int tr_gemm(int form, char t1, char t2, int mm, int nn, int kk, const T *X, int ldx,
+                   const T *Y, int ldy, T *C, int ldc, void *ws, size_t ws_bytes, cudaStream_t st,
+                   unsigned *err, bool add = false) {
+  if (mm <= 0 || nn <= 0 || kk <= 0) return GB300_OK;
+  const T a = add ? T(1) : T(-1);
+  if constexpr (sizeof(T) == 8) {
+    if (form == 1)
+      return ozaki_dgemm(t1, t2, mm, nn, kk, a, X, ldx, Y, ldy, 1.0, C, ldc, 0, ws, ws_bytes, st,
+                         err);
+    return plain_dgemm(t1, t2, mm, nn, kk, a, X, ldx, Y, ldy, 1.0, C, ldc, st, err);
+  } else {
+    if (form == 1)
+      return split_sgemm(t1, t2, mm, nn, kk, a, X, ldx, Y, ldy, 1.0f, C, ldc, 6, ws, ws_bytes, st,
+                         err);
+    return plain_sgemm(t1, t2, mm, nn, kk, a, X, ldx, Y, ldy, 1.0f, C, ldc, st, err);
+  }
+}
+
+size_t tr_workspace_bytes(int is_double, int form, int m, int n) {
+  if (form != 1 || m <= 0 || n <= 0) return 0;
+  // The off-diagonal updates are at most (m x n x 64) for TRSM and
+  // (64 x n x m) / (m x 64 x n) for TRMM (left / right): size for the largest.
+  const int shapes[4][3] = {{m, n, kTrNb}, {kTrNb, n, m}, {m, kTrNb, n}, {m, n, kTrNb}};
+  size_t need = 0;
+  for (const auto &sh : shapes) {
+    const size_t w = is_double ? split_workspace_bytes(1, sh[0], sh[1], sh[2], 0)
+                               : split_workspace_bytes(0, sh[0], sh[1], sh[2], 6);
+    if (w > need) need = w;
+  }
+  return need;
+}
+
+int tr_check(char side, char uplo, char transa, char diag, int m, int n, int lda, int ldb) {
+  if (!in_set(side, "LlRr") || !in_set(uplo, "UuLl") || !in_set(transa, "NnTtCc") ||
+      !in_set(diag, "UuNn"))
+    return GB300_ERR_ARG;
+  const int na = (side == 'L' || side == 'l') ? m : n;
+  if (m < 0 || n < 0 || lda < (na > 1 ? na : 1) || ldb < (m > 1 ? m : 1)) return GB300_ERR_ARG;
+  return (m == 0 || n == 0) ? -1 : GB300_OK;
+}
+
+// solve = 1: TRSM, 0: TRMM.
+template <typename T>
+int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, int n, T alpha,
+              const T *A, int lda, T *B, int ldb, int form, void *ws, size_t ws_bytes,
+              cudaStream_t st, unsigned *err) {
+  const int ck = tr_check(side, uplo, transa, diag, m, n, lda, ldb);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  if (form != 0 && form != 1) return GB300_ERR_ARG;
+  if (form == 1 && (!ws || ws_bytes < tr_workspace_bytes(sizeof(T) == 8, form, m, n)))
+    return GB300_ERR_WORKSPACE;
+  const bool left = side == 'L' || side == 'l';
+  const bool trans = !(transa == 'N' || transa == 'n');
+  const bool lower = (uplo == 'L' || uplo == 'l') != trans;  // effective triangle of op(A)
+  const bool unit = diag == 'U' || diag == 'u';
+  const char tA = trans ? 'T' : 'N';
+  auto scale = [&](T s) {
+    const int64_t total = (int64_t)m * n;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    scale_b_kernel<T><<<blocks, 256, 0, st>>>(m, n, s, B, ldb);
+  };
+  if (alpha == T(0)) {
+    scale(T(0));
+    return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  }
+  // op(A)(r0.., c0..) as a GEMM operand: pointer and transpose flag
+  auto opA = [&](int r0, int c0) -> const T * {
+    return trans ? A + (int64_t)r0 * lda + c0 : A + (int64_t)c0 * lda + r0;
+  };
+  const int smem = (kTrNb * kTrNb + kTrNb * kTrCols) * (int)sizeof(T);
+  if (cudaFuncSetAttribute(diag_left_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           smem) != cudaSuccess ||
+      cudaFuncSetAttribute(diag_right_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           smem) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  const int na = left ? m : n;
+  const int nblk = (na + kTrNb - 1) / kTrNb;
+  // TRSM scales first (X = op(A)^-1 (alpha B)); TRMM scales last.
+  if (solve && alpha != T(1)) scale(alpha);
+  // Block order: a solve walks the triangle from its first row (lower-left /
+  // upper-right as seen by the side); a multiply in place walks the other way
+  // so that every block still reads unmodified rows / columns of B.
+  const bool forward = left ? (solve ? lower : !lower) : (solve ? !lower : lower);
+  int rc = GB300_OK;
+  for (int q = 0; q < nblk && rc == GB300_OK; ++q) {
+    const int ib = forward ? q : nblk - 1 - q;
+    const int d0 = ib * kTrNb, nb = (na - d0) < kTrNb ? (na - d0) : kTrNb;
+    const int lo = d0 + nb;  // first index after the block
+    if (solve) {
+      if (left) {
+        diag_left_kernel<T><<<(n + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
+            A, lda, trans, lower, unit, d0, nb, B, ldb, n, 1);
+        // the rows still to solve: below the block (lower) or above it (upper)
+        if (lower)
+          rc = tr_gemm<T>(form, tA, 'N', m - lo, n, nb, opA(lo, d0), lda, B + d0, ldb, B + lo,
+                          ldb, ws, ws_bytes, st, err);
+        else
+          rc = tr_gemm<T>(form, tA, 'N', d0, n, nb, opA(0, d0), lda, B + d0, ldb, B, ldb, ws,
+                          ws_bytes, st, err);
+      } else {
+        diag_right_kernel<T><<<(m + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
+            A, lda, trans, lower, unit, d0, nb, B, ldb, m, 1);
+        // the columns still to solve: right of the block (upper) or left of it (lower)
+        if (!lower)
+          rc = tr_gemm<T>(form, 'N', tA, m, n - lo, nb, B + (int64_t)d0 * ldb, ldb, opA(d0, lo),
+                          lda, B + (int64_t)lo * ldb, ldb, ws, ws_bytes, st, err);
+        else
+          rc = tr_gemm<T>(form, 'N', tA, m, d0, nb, B + (int64_t)d0 * ldb, ldb, opA(d0, 0), lda,
+                          B, ldb, ws, ws_bytes, st, err);
+      }
+    } else {
+      // multiply: block rows/cols of the result = diagonal part + off-diagonal part,
+      // the off-diagonal part reading rows/columns of B not yet overwritten
+      if (left) {
+        diag_left_kernel<T><<<(n + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
+            A, lda, trans, lower, unit, d0, nb, B, ldb, n, 0);
+        if (lower)  // B_i += op(A)(i, <i) B_<i ; rows above are still the input
+          rc = tr_gemm<T>(form, tA, 'N', nb, n, d0, opA(d0, 0), lda, B, ldb, B + d0, ldb, ws,
+                          ws_bytes, st, err, true);
+        else        // B_i += op(A)(i, >i) B_>i
+          rc = tr_gemm<T>(form, tA, 'N', nb, n, m - lo, opA(d0, lo), lda, B + lo, ldb, B + d0,
+                          ldb, ws, ws_bytes, st, err, true);
+      } else {
+        diag_right_kernel<T><<<(m + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
+            A, lda, trans, lower, unit, d0, nb, B, ldb, m, 0);
+        if (!lower)  // B_j += B_<j op(A)(<j, j)
+          rc = tr_gemm<T>(form, 'N', tA, m, nb, d0, B, ldb, opA(0, d0), lda,
+                          B + (int64_t)d0 * ldb, ldb, ws, ws_bytes, st, err, true);
+        else         // B_j += B_>j op(A)(>j, j)
+          rc = tr_gemm<T>(form, 'N', tA, m, nb, n - lo, B + (int64_t)lo * ldb, ldb, opA(lo, d0),
+                          lda, B + (int64_t)d0 * ldb, ldb, ws, ws_bytes, st, err, true);
+      }
+    }
+    if (rc == GB300_OK && cudaGetLastError() != cudaSuccess) rc = GB300_ERR_CUDA;
+  }
+  if (rc == GB300_OK && !solve && alpha != T(1)) scale(alpha);
+  if (rc == GB300_OK && cudaGetLastError() != cudaSuccess) rc = GB300_ERR_CUDA;
+  return rc;
+}
+
+int trsm_d(int solve, char side, char uplo, char ta, char diag, int m, int n, double alpha,
+           const double *A, int lda, double *B, int ldb, int form, void *ws, size_t wsb,
+           cudaStream_t st, unsigned *err) {
+  return tr_driver<double>(solve, side, uplo, ta, diag, m, n, alpha, A, lda, B, ldb, form, ws,
+                           wsb, st, err);
+}
+int trsm_s(int solve, char side, char uplo, char ta, char diag, int m, int n, float alpha,
+           const float *A, int lda, float *B, int ldb, int form, void *ws, size_t wsb,
+           cudaStream_t st, unsigned *err) {
+  return tr_driver<float>(solve, side, uplo, ta, diag, m, n, alpha, A, lda, B, ldb, form, ws, wsb,
+                          st, err);
+}
+
+}  // namespace gb300

@@ -213,6 +213,30 @@ int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int count, in
 int gb300_grouped_graph_launch(gb300_grouped_graph graph, void *stream);
 int gb300_grouped_graph_destroy(gb300_grouped_graph graph);
 
+/* ------------------------------------------------------------------------
+ * Triangular solve / multiply on top of the GEMM (BLAS semantics; the
+ * reference has these only as OpenBLAS-style packed-panel kernels,
+ * OpenBLAS-like_implementation/TRSM_KERNEL_*_simplified.c and
+ * trmm_kernel_4x8_simplified.c, outside its built library).
+ *   TRSM: side 'L': op(A) X = alpha B;  'R': X op(A) = alpha B;  X overwrites B
+ *   TRMM: side 'L': B = alpha op(A) B;  'R': B = alpha B op(A)
+ * A is m x m ('L') or n x n ('R'), triangle uplo 'U'/'L', diag 'U' (unit) or
+ * 'N'; op(A) = A for transa 'N', A^T for 'T'/'C'.  alpha == 0 sets B to zero.
+ * form 0: off-diagonal updates with the plain GEMM; form 1: with the split
+ * forms (Ozaki for FP64, 6xBF16 for FP32; library-owned workspace).  The
+ * diagonal 64x64 blocks are solved / multiplied by a small CUDA kernel.
+ * Device pointers, stream-ordered; GB300_ERR_ARG for invalid characters,
+ * sizes or leading dimensions.
+ * ---------------------------------------------------------------------- */
+int gb300_dtrsm(char side, char uplo, char transa, char diag, int m, int n, double alpha,
+                const double *A, int lda, double *B, int ldb, int form, void *stream);
+int gb300_strsm(char side, char uplo, char transa, char diag, int m, int n, float alpha,
+                const float *A, int lda, float *B, int ldb, int form, void *stream);
+int gb300_dtrmm(char side, char uplo, char transa, char diag, int m, int n, double alpha,
+                const double *A, int lda, double *B, int ldb, int form, void *stream);
+int gb300_strmm(char side, char uplo, char transa, char diag, int m, int n, float alpha,
+                const float *A, int lda, float *B, int ldb, int form, void *stream);
+
 /* Workspace needed by the split forms for one call of the given shape.
  * kind = 0: sgemm_bf16x with `param` = products; kind = 1: dgemm_ozaki with
  * `param` = slices. */

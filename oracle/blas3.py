@@ -1,0 +1,51 @@
+"""numpy restatements of the BLAS TRSM / TRMM definitions -- TEST INFRASTRUCTURE.
+
+The reference has TRSM/TRMM only as OpenBLAS-style packed-panel kernels outside
+its built library (OpenBLAS-like_implementation/TRSM_KERNEL_*_simplified.c,
+trmm_kernel_4x8_simplified.c), so there is nothing of it to run: these follow
+the BLAS definitions directly, in FP64 (parity unpinned for these two routines).
+
+  trsm: side 'L': solve op(A) X = alpha B;  'R': X op(A) = alpha B
+  trmm: side 'L': alpha op(A) B;            'R': alpha B op(A)
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def op_triangle(A: np.ndarray, na: int, uplo: str, transa: str, diag: str) -> np.ndarray:
+    """op(A) as a dense FP64 na x na matrix holding only the referenced triangle."""
+    T = np.array(A[:na, :na], dtype=np.float64)
+    T = np.tril(T) if uplo in "Ll" else np.triu(T)
+    if diag in "Uu":
+        np.fill_diagonal(T, 1.0)
+    return T if transa in "Nn" else T.T
+
+
+def trsm(side, uplo, transa, diag, m, n, alpha, A, B):
+    na = m if side in "Ll" else n
+    T = op_triangle(A, na, uplo, transa, diag)
+    Bm = np.array(B[:m, :n], dtype=np.float64)
+    if alpha == 0:
+        return np.zeros((m, n))
+    if side in "Ll":
+        return np.linalg.solve(T, alpha * Bm)
+    return np.linalg.solve(T.T, alpha * Bm.T).T
+
+
+def trmm(side, uplo, transa, diag, m, n, alpha, A, B):
+    na = m if side in "Ll" else n
+    T = op_triangle(A, na, uplo, transa, diag)
+    Bm = np.array(B[:m, :n], dtype=np.float64)
+    if alpha == 0:
+        return np.zeros((m, n))
+    return alpha * (T @ Bm) if side in "Ll" else alpha * (Bm @ T)
+
+
+def well_conditioned_triangle(rng, na, lda, dtype):
+    """A na x na (ld = lda) matrix whose both triangles are well conditioned:
+    diagonal in [1, 2), off-diagonal entries U[-1,1)/na."""
+    A = (rng.uniform(-1, 1, (lda, na)) / max(na, 1)).astype(dtype)
+    for i in range(na):
+        A[i, i] = dtype(1.0 + rng.uniform())
+    return np.asfortranarray(A)
