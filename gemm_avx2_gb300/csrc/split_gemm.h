@@ -10,7 +10,7 @@ namespace gb300 {
 constexpr int kSplitBK = 64;       // K elements per pipeline stage (128 B of BF16)
 constexpr int kSplitBM = 128;      // tile rows (TMEM lanes)
 constexpr int kBf16xBN = 256;      // tile columns of the BF16xP SGEMM
-constexpr int kOzakiBN = 128;      // tile columns of the Ozaki DGEMM
+constexpr int kOzakiBN = 256;      // tile columns of the Ozaki DGEMM
 constexpr int kOzakiMaxSlices = 12;
 
 size_t split_workspace_bytes(int kind, int m, int n, int k, int param);

@@ -406,9 +406,12 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 }
 
 // ===========================================================================
-// Ozaki GEMM: persistent, 128 x 128 tiles, exact integer slice products.
-// TMEM: [0,128) and [128,256) chunk accumulators (FP32), [256,384) and
-// [384,512) the low and high words of the tile's FP64 result.
+// Ozaki GEMM: persistent, 128 x 256 tiles, exact integer slice products.
+// TMEM: [0,256) and [256,512) chunk accumulators (FP32).  The tile's FP64
+// result accumulates in a global scratch (Mp x Np, column-major) that only
+// this tile's threads touch: each slice group is folded into it once, so its
+// traffic is small next to the operand stream, and TMEM holds two full-width
+// accumulators (128-column tiles reach only ~55% of the tensor pipe here).
 // ===========================================================================
 struct OzakiParams {
   int m, n, tiles_m, tiles_n;
@@ -418,16 +421,18 @@ struct OzakiParams {
   double *C;
   int ldc;
   const int *expA, *expB;  // per-row / per-column scale exponents
+  double *res;             // Mp x Np FP64 result scratch (ld = Mp)
   unsigned *err;
 };
 
-constexpr int kOzStages = 6;
+constexpr int kOzStages = 4;
 constexpr int kOzEpiWarps = 8;
 constexpr int kOzThreads = (2 + kOzEpiWarps) * 32;
 constexpr int kOzABytes = kSplitBM * 128;
 constexpr int kOzBBytes = kOzakiBN * 128;
 constexpr int kOzStage = kOzABytes + kOzBBytes;
 constexpr int kOzSmem = kOzStages * kOzStage + 1024 + 256;
+constexpr int kOzCols = kOzakiBN / 2;  // output columns per epilogue warp
 // 16 x 64 = 1024 K-steps per exact chunk: |partial sum| <= 1024 * 127^2 =
 // 16,516,096 < 2^24, so every partial sum is an exactly representable FP32 integer.
 constexpr int kOzChunkStages = 16;
@@ -545,16 +550,19 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       mbar_wait(done, 0, p.err, kErrTimeoutMma, nullptr);
     }
   } else {
-    // 8 epilogue warps: lane quarter q = warp % 4, column half h
+    // 8 epilogue warps: lane quarter q = warp % 4, column half h (128 columns each)
     const int q = warp & 3;
     const int h = (warp - 2) >> 2;
     const int row_in_tile = q * 32 + lane;
-    const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+    const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + h * kOzCols;
     uint32_t chunk = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
       int tm, tn;
       tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
+      const int row = tm * kSplitBM + row_in_tile;          // < Mp
+      const int col0 = tn * kOzakiBN + h * kOzCols;          // first of this warp's columns
+      double *res = p.res + (int64_t)col0 * p.Mp + row;      // res[j * Mp] is column col0 + j
       bool res_init = false;
       for (int t = S + 1; t >= 2 && ok; --t) {
         int lo, np;
@@ -562,9 +570,9 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const int G = np * KB;
         const int nch = (G + kOzChunkStages - 1) / kOzChunkStages;
         const double wt = ldexp(1.0, -7 * t);
-        int run[64];
+        int run[kOzCols];
 #pragma unroll
-        for (int j = 0; j < 64; ++j) run[j] = 0;
+        for (int j = 0; j < kOzCols; ++j) run[j] = 0;
         int since_fold = 0;
         for (int c = 0; c < nch; ++c, ++chunk) {
           const int b = chunk & 1;
@@ -572,15 +580,14 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           if (!mbar_wait(&accf[b], u & 1, p.err, kErrTimeoutAcc, abort_flag)) { ok = false; break; }
           tc_fence_after();
 #pragma unroll
-          for (int hh = 0; hh < 2; ++hh) {
-            uint32_t v[32];
-            tmem_ld32(lane_base + b * kOzakiBN + h * 64 + hh * 32, v);
+          for (int g = 0; g < kOzCols / 16; ++g) {
+            uint32_t v[16];
+            tmem_ld16(lane_base + b * kOzakiBN + g * 16, v);
             tmem_ld_wait();
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
+            for (int j = 0; j < 16; ++j)
               // integer-valued with |v| < 2^24: round-to-nearest conversion is exact
-              run[hh * 32 + j] += __float2int_rn(__uint_as_float(v[j]));
-            }
+              run[g * 16 + j] += __float2int_rn(__uint_as_float(v[j]));
           }
           tc_fence_before();
           __syncwarp();
@@ -589,27 +596,16 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           if (++since_fold == kOzRunChunks || last) {
             // fold the exact group sum into the FP64 result: res += run * 2^-7t
 #pragma unroll
-            for (int g4 = 0; g4 < 4; ++g4) {
-              const uint32_t col = h * 64 + g4 * 16;
-              uint32_t lo_w[16], hi_w[16];
-              if (res_init) {
-                tmem_ld16(lane_base + 256 + col, lo_w);
-                tmem_ld16(lane_base + 384 + col, hi_w);
-                tmem_ld_wait();
-              }
+            for (int g = 0; g < kOzCols; g += 8) {
+              double prev[8];
 #pragma unroll
-              for (int j = 0; j < 16; ++j) {
-                const double prev =
-                    res_init ? __hiloint2double((int)hi_w[j], (int)lo_w[j]) : 0.0;
-                const double nv = fma((double)run[g4 * 16 + j], wt, prev);
-                lo_w[j] = (uint32_t)__double2loint(nv);
-                hi_w[j] = (uint32_t)__double2hiint(nv);
-                run[g4 * 16 + j] = 0;
+              for (int j = 0; j < 8; ++j) prev[j] = res_init ? res[(int64_t)(g + j) * p.Mp] : 0.0;
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                res[(int64_t)(g + j) * p.Mp] = fma((double)run[g + j], wt, prev[j]);
+                run[g + j] = 0;
               }
-              tmem_st16(lane_base + 256 + col, lo_w);
-              tmem_st16(lane_base + 384 + col, hi_w);
             }
-            tmem_st_wait();
             res_init = true;
             since_fold = 0;
           }
@@ -617,40 +613,31 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       }
       if (!ok) break;
       // final epilogue: C = alpha * 2^(E_i + F_j) * res + beta * C
-      const int row = tm * kSplitBM + row_in_tile;
-      const int ea = (row < p.m) ? p.expA[row] : 0;
+      if (row < p.m) {
+        const int ea = p.expA[row];
+#pragma unroll 1
+        for (int g = 0; g < kOzCols; g += 8) {
+          double rv[8], cv[8];
 #pragma unroll
-      for (int g4 = 0; g4 < 4; ++g4) {
-        const int colt = h * 64 + g4 * 16;
-        uint32_t lo_w[16], hi_w[16];
-        tmem_ld16(lane_base + 256 + colt, lo_w);
-        tmem_ld16(lane_base + 384 + colt, hi_w);
-        tmem_ld_wait();
-        if (row < p.m) {
-          double cv[16];  // loads of the 16 columns first, then the stores
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int col = tn * kOzakiBN + colt + j;
+          for (int j = 0; j < 8; ++j) {
+            const int col = col0 + g + j;
+            rv[j] = res[(int64_t)(g + j) * p.Mp];
             cv[j] = (col < p.n) ? p.C[(int64_t)col * p.ldc + row] : 0.0;
           }
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int col = tn * kOzakiBN + colt + j;
+          for (int j = 0; j < 8; ++j) {
+            const int col = col0 + g + j;
             if (col < p.n) {
               const int eb = p.expB[col];
-              double v = __hiloint2double((int)hi_w[j], (int)lo_w[j]);
-              v = (ea == kNonFiniteExp || eb == kNonFiniteExp) ? __longlong_as_double(0x7ff8000000000000LL)
-                                                               : scale_pow2(v, ea + eb);
+              const double v = (ea == kNonFiniteExp || eb == kNonFiniteExp)
+                                   ? __longlong_as_double(0x7ff8000000000000LL)
+                                   : scale_pow2(rv[j], ea + eb);
               const double cb = (p.beta == 1.0) ? cv[j] : cv[j] * p.beta;
               p.C[(int64_t)col * p.ldc + row] = cb + p.alpha * v;
             }
           }
         }
       }
-      // the next tile's first fold overwrites the result columns: make the
-      // reads above complete first
-      tc_fence_before();
-      __syncwarp();
     }
   }
   tc_fence_before();
@@ -706,7 +693,7 @@ size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
   int S = param > 0 ? param : ozaki_default_slices(m, n, k);
   if (S < 2 || S > kOzakiMaxSlices) return 0;
   const int64_t Mp = round_up(m, kSplitBM), Np = round_up(n, kOzakiBN);
-  return (size_t)((Mp + Np) * S * Kp * 2 + (Mp + Np) * 12 + 2048);
+  return (size_t)((Mp + Np) * S * Kp * 2 + (Mp + Np) * 12 + Mp * Np * 8 + 4096);
 }
 
 int ozaki_default_slices(int m, int n, int k) {
@@ -838,6 +825,7 @@ struct OzakiLayout {
   __nv_bfloat16 *As, *Bs;
   unsigned long long *amaxA, *amaxB;
   int *expA, *expB;
+  double *res;
 };
 static OzakiLayout ozaki_layout(int m, int n, int k, int S, void *ws) {
   OzakiLayout L;
@@ -852,6 +840,8 @@ static OzakiLayout ozaki_layout(int m, int n, int k, int S, void *ws) {
   L.amaxB = L.amaxA + L.Mp;
   L.expA = reinterpret_cast<int *>(L.amaxB + L.Np);
   L.expB = L.expA + L.Mp;
+  L.res = reinterpret_cast<double *>(
+      (reinterpret_cast<uintptr_t>(L.expB + L.Np) + 255) & ~uintptr_t(255));
   return L;
 }
 
@@ -912,7 +902,7 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
   p.S = S; p.KB = (int)(L.Kp / kSplitBK);
   p.Mp = (int)L.Mp; p.Np = (int)L.Np;
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc;
-  p.expA = L.expA; p.expB = L.expB; p.err = err;
+  p.expA = L.expA; p.expB = L.expB; p.res = L.res; p.err = err;
   if (cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kOzSmem) != cudaSuccess)
     return GB300_ERR_CUDA;

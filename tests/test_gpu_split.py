@@ -115,7 +115,7 @@ def test_ozaki_slices_bitexact_and_result(orc, S, ta, tb):
                        dC.data_ptr(), m, slices=S, workspace=ws.data_ptr(), workspace_bytes=need)
     assert rc == g.OK
     sync()
-    Kp, Mp, Np = ru(k, 64), ru(m, 128), ru(n, 128)
+    Kp, Mp, Np = ru(k, 64), ru(m, 128), ru(n, 256)
     off = aligned_view(ws, need)
     raw = ws.cpu().numpy()[off:]
     bf = raw[:2 * S * (Mp + Np) * Kp].view(np.uint16).astype(np.uint32) << 16
