@@ -33,6 +33,9 @@
 namespace gb300 {
 
 static inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+// grid.y of the split / slice kernels: the 32-row blocks of Rp, capped at the
+// grid limit (the kernels stride over the rest).
+static inline unsigned row_blocks(int64_t Rp) { return (unsigned)(Rp / 32 < 65535 ? Rp / 32 : 65535); }
 constexpr int kSplitGroupM = 16;
 
 // ===========================================================================
@@ -82,46 +85,61 @@ struct SegMap {
   int term[6];
 };
 
-// out: Rp x (nseg * Kp) row-major BF16 (row stride ldo = nseg*Kp elements).
+// out: Rp x (nseg * Kp) row-major BF16 (row stride ldo = nseg*Kp elements);
+// grid.y strides over the Rp / 32 row blocks.  Each thread writes 8
+// consecutive k of one row (16 bytes) per segment.
 __global__ void __launch_bounds__(256) split_bf16_kernel(const float *__restrict__ X, int ld, int R,
-                                                         int K, int kcontig, int Kp, SegMap seg,
-                                                         int nterms, __nv_bfloat16 *__restrict__ out,
+                                                         int K, int kcontig, int Rp, int Kp,
+                                                         SegMap seg, int nterms,
+                                                         __nv_bfloat16 *__restrict__ out,
                                                          int64_t ldo) {
   __shared__ float tile[32][65];
-  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 64;
-  load_tile_32x64<float>(X, ld, R, K, kcontig != 0, r0, k0, tile);
-  __syncthreads();
-  const int tid = threadIdx.x;
+  const int k0 = blockIdx.x * 64;
+  const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
+  for (int r0 = blockIdx.y * 32; r0 < Rp; r0 += gridDim.y * 32) {
+    load_tile_32x64<float>(X, ld, R, K, kcontig != 0, r0, k0, tile);
+    __syncthreads();
+    unsigned w[3][4];  // term t of the 8 values, packed in pairs
 #pragma unroll
-  for (int p = 0; p < 4; ++p) {
-    const int r = p * 8 + (tid >> 5), kk = (tid & 31) * 2;
-    __nv_bfloat16 t0[3], t1[3];
-    bf16_terms(tile[r][kk], nterms, t0);
-    bf16_terms(tile[r][kk + 1], nterms, t1);
-    __nv_bfloat16 *row = out + (int64_t)(r0 + r) * ldo + k0 + kk;
-    for (int s = 0; s < seg.nseg; ++s) {
-      const int ti = seg.term[s];
-      __nv_bfloat162 v;
-      v.x = t0[ti];
-      v.y = t1[ti];
-      *reinterpret_cast<__nv_bfloat162 *>(row + (int64_t)s * Kp) = v;
+    for (int j = 0; j < 8; j += 2) {
+      __nv_bfloat16 t0[3], t1[3];
+      bf16_terms(tile[r][kq + j], nterms, t0);
+      bf16_terms(tile[r][kq + j + 1], nterms, t1);
+#pragma unroll
+      for (int t = 0; t < 3; ++t)
+        w[t][j / 2] = (unsigned)__bfloat16_as_ushort(t0[t]) |
+                      ((unsigned)__bfloat16_as_ushort(t1[t]) << 16);
     }
+    __nv_bfloat16 *row = out + (int64_t)(r0 + r) * ldo + k0 + kq;
+    for (int sg = 0; sg < seg.nseg; ++sg) {
+      const int ti = seg.term[sg];
+      const uint4 v = ti == 0   ? make_uint4(w[0][0], w[0][1], w[0][2], w[0][3])
+                      : ti == 1 ? make_uint4(w[1][0], w[1][1], w[1][2], w[1][3])
+                                : make_uint4(w[2][0], w[2][1], w[2][2], w[2][3]);
+      *reinterpret_cast<uint4 *>(row + (int64_t)sg * Kp) = v;
+    }
+    __syncthreads();  // the tile is refilled for the next row block
   }
 }
 
 // Ozaki step 1: per-row max |x| of op(X) as the bit pattern of a non-negative
 // double (monotone as an unsigned integer; NaN/Inf compare above finite values).
+// Short k ranges per grid row and unrolled loads keep enough reads in flight.
+// The k range of one warp (k-contiguous rows) or one thread (row-contiguous
+// columns) starts at these and doubles until the grid's y extent fits.
+constexpr int kAmaxSpanK = 1024;
+constexpr int kAmaxSpanR = 64;
 __global__ void __launch_bounds__(256) row_absmax_kernel(const double *__restrict__ X, int ld,
-                                                         int R, int K, int kcontig,
+                                                         int R, int K, int kcontig, int span,
                                                          unsigned long long *__restrict__ amax) {
   if (kcontig) {
-    // one warp per (row, 2048-wide k range)
-    const int warp = (blockIdx.x * 8) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    const int r = warp;
+    // one warp per (row, k range)
+    const int r = (blockIdx.x * 8) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (r >= R) return;
-    const int k0 = blockIdx.y * 2048, k1 = min(K, k0 + 2048);
+    const int k0 = blockIdx.y * span, k1 = min(K, k0 + span);
     unsigned long long m = 0;
     const double *row = X + (int64_t)r * ld;
+#pragma unroll 8
     for (int kk = k0 + lane; kk < k1; kk += 32) {
       const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(row[kk]));
       m = b > m ? b : m;
@@ -133,11 +151,12 @@ __global__ void __launch_bounds__(256) row_absmax_kernel(const double *__restric
     }
     if (lane == 0 && m) atomicMax(&amax[r], m);
   } else {
-    // one thread per row, a 256-wide k range per grid row
+    // one thread per row, one k range per grid row
     const int r = blockIdx.x * 256 + threadIdx.x;
     if (r >= R) return;
-    const int k0 = blockIdx.y * 256, k1 = min(K, k0 + 256);
+    const int k0 = blockIdx.y * span, k1 = min(K, k0 + span);
     unsigned long long m = 0;
+#pragma unroll 8
     for (int kk = k0; kk < k1; ++kk) {
       const unsigned long long b =
           (unsigned long long)__double_as_longlong(fabs(X[r + (int64_t)kk * ld]));
@@ -173,40 +192,69 @@ __device__ __forceinline__ double scale_pow2(double v, int e) {
   return ldexp(v, e);
 }
 
-// Ozaki step 2: slices.  x = op(X)(r,k) * 2^-E_r in (-1,1); for s = 1..S:
-// y = x * 128, d_s = trunc(y) (|d_s| <= 127), x = y - d_s (exact).
-// out: S blocks of Rp rows x Kp (row-major BF16), slice s at rows (s-1)*Rp.
+// The S digits of 8 consecutive values of one row (row exponent e), packed as
+// BF16 and written to dst[(s-1) * step].
+__device__ __forceinline__ void slice_digits(const double *x, int e, int S, uint4 *dst,
+                                             int64_t step) {
+  unsigned long long mag[8];
+  int sh[8];          // E - b: digit s sits at bits [sh - 7s, sh - 7s + 7) of M
+  unsigned neg = 0;   // sign bits
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x[j]);
+    const int be = (int)((u >> 52) & 0x7ff);
+    mag[j] = (u & 0xfffffffffffffull) | (be ? (1ull << 52) : 0ull);
+    sh[j] = e - ((be ? be : 1) - 1075);
+    neg |= (unsigned)(u >> 63) << j;
+  }
+  for (int s = 1; s <= S; ++s) {
+    unsigned w[4];
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+      unsigned h[2];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int t = sh[j + q] - 7 * s;
+        const unsigned long long v =
+            t >= 64 ? 0ull : (t >= 0 ? mag[j + q] >> t : (t > -7 ? mag[j + q] << -t : 0ull));
+        const int d = (int)(v & 127);
+        const float f = (float)(((neg >> (j + q)) & 1) ? -d : d);
+        h[q] = __float_as_uint(f) >> 16;  // |d| < 2^7: the BF16 of f is its top half
+      }
+      w[j / 2] = h[0] | (h[1] << 16);
+    }
+    dst[(s - 1) * step] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+// Ozaki step 2: slices.  y = op(X)(r,k) * 2^-E_r lies in (-1,1); its truncated
+// base-128 digits d_1..d_S (|d_s| <= 127, sign of y) are what the recurrence
+// y <- 128 y, d = trunc(y), y <- y - d produces, each step exact.  They are read
+// here straight from the bits: |x| = M * 2^b with M the 53-bit significand, so
+// d_s = floor(M * 2^(b - E + 7s)) mod 128, a shift and a mask (the GPU's FP64
+// rate would make the recurrence itself the bottleneck of this pass).
+// out: S blocks of Rp rows x Kp (row-major BF16), slice s at rows (s-1)*Rp;
+// each thread writes 8 consecutive k of one row (16 bytes) per slice.
 __global__ void __launch_bounds__(256) ozaki_slice_kernel(
     const double *__restrict__ X, int ld, int R, int K, int kcontig, int Rp, int Kp, int S,
     const int *__restrict__ ex, __nv_bfloat16 *__restrict__ out) {
   __shared__ double tile[32][65];
-  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 64;
-  load_tile_32x64<double>(X, ld, R, K, kcontig != 0, r0, k0, tile);
-  __syncthreads();
-  const int tid = threadIdx.x;
-#pragma unroll
-  for (int p = 0; p < 4; ++p) {
-    const int r = p * 8 + (tid >> 5), kk = (tid & 31) * 2;
+  const int k0 = blockIdx.x * 64;
+  const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
+  const int64_t step = (int64_t)Rp * Kp / 8;  // one slice block, in uint4
+  for (int r0 = blockIdx.y * 32; r0 < Rp; r0 += gridDim.y * 32) {
+    load_tile_32x64<double>(X, ld, R, K, kcontig != 0, r0, k0, tile);
+    __syncthreads();
     const int gr = r0 + r;
     const int e = (gr < R) ? ex[gr] : 0;
-    double x0 = tile[r][kk], x1 = tile[r][kk + 1];
-    const bool bad = (e == kNonFiniteExp);
-    if (!bad) { x0 = ldexp(x0, -e); x1 = ldexp(x1, -e); }
-    __nv_bfloat16 *base = out + (int64_t)gr * Kp + k0 + kk;
-    for (int s = 0; s < S; ++s) {
-      __nv_bfloat162 v;
-      if (bad) {
-        v.x = __float2bfloat16_rn(__int_as_float(0x7fc00000));
-        v.y = v.x;
-      } else {
-        const double y0 = x0 * 128.0, y1 = x1 * 128.0;
-        const double d0 = trunc(y0), d1 = trunc(y1);
-        x0 = y0 - d0; x1 = y1 - d1;
-        v.x = __float2bfloat16_rn((float)d0);
-        v.y = __float2bfloat16_rn((float)d1);
-      }
-      *reinterpret_cast<__nv_bfloat162 *>(base + (int64_t)s * Rp * Kp) = v;
+    uint4 *dst = reinterpret_cast<uint4 *>(out + (int64_t)gr * Kp + k0 + kq);
+    if (e == kNonFiniteExp) {
+      const uint4 nan4 = make_uint4(0x7fc07fc0u, 0x7fc07fc0u, 0x7fc07fc0u, 0x7fc07fc0u);
+      for (int s = 0; s < S; ++s) dst[s * step] = nan4;
+    } else {
+      slice_digits(tile[r] + kq, e, S, dst, step);
     }
+    __syncthreads();  // the tile is refilled for the next row block
   }
 }
 
@@ -746,10 +794,10 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
   if (L.Kld > 0x7fffffff || L.Mp > 0x7fffffff || L.Np > 0x7fffffff) return GB300_ERR_ARG;
   const bool an = notrans(ta), bn = notrans(tb);
   const int nterms = products == 3 ? 2 : 3;
-  split_bf16_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Mp / 32)), 256, 0, st>>>(
-      A, lda, m, k, an ? 0 : 1, (int)L.Kp, seg_map(products, true), nterms, L.Ap, L.Kld);
-  split_bf16_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Np / 32)), 256, 0, st>>>(
-      B, ldb, n, k, bn ? 1 : 0, (int)L.Kp, seg_map(products, false), nterms, L.Bp, L.Kld);
+  split_bf16_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Mp)), 256, 0, st>>>(
+      A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, seg_map(products, true), nterms, L.Ap, L.Kld);
+  split_bf16_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Np)), 256, 0, st>>>(
+      B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, seg_map(products, false), nterms, L.Bp, L.Kld);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
@@ -861,20 +909,23 @@ int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int ld
   // per-row / per-column max |.|: A rows are k-contiguous when transposed, B
   // columns when not.
   auto absmax = [&](const double *X, int ld, int R, bool kc, unsigned long long *am) {
+    int64_t span = kc ? kAmaxSpanK : kAmaxSpanR;
+    while ((k + span - 1) / span > 65535) span *= 2;
+    const unsigned gy = (unsigned)((k + span - 1) / span);
     if (kc)
-      row_absmax_kernel<<<dim3((unsigned)((R + 7) / 8), (unsigned)((k + 2047) / 2048)), 256, 0,
-                           st>>>(X, ld, R, k, 1, am);
+      row_absmax_kernel<<<dim3((unsigned)((R + 7) / 8), gy), 256, 0, st>>>(X, ld, R, k, 1,
+                                                                          (int)span, am);
     else
-      row_absmax_kernel<<<dim3((unsigned)((R + 255) / 256), (unsigned)((k + 255) / 256)), 256, 0,
-                           st>>>(X, ld, R, k, 0, am);
+      row_absmax_kernel<<<dim3((unsigned)((R + 255) / 256), gy), 256, 0, st>>>(X, ld, R, k, 0,
+                                                                              (int)span, am);
   };
   absmax(A, lda, m, !an, L.amaxA);
   absmax(B, ldb, n, bn, L.amaxB);
   row_exponent_kernel<<<(unsigned)((L.Mp + L.Np + 255) / 256), 256, 0, st>>>(
       L.amaxA, (int)(L.Mp + L.Np), L.expA);  // amaxB and expB follow amaxA and expA
-  ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Mp / 32)), 256, 0, st>>>(
+  ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Mp)), 256, 0, st>>>(
       A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, S, L.expA, L.As);
-  ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), (unsigned)(L.Np / 32)), 256, 0, st>>>(
+  ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Np)), 256, 0, st>>>(
       B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, S, L.expB, L.Bs);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }

@@ -141,6 +141,42 @@ def test_ozaki_slices_bitexact_and_result(orc, S, ta, tb):
     assert g.device_error() == 0
 
 
+@pytest.mark.parametrize("S", [8, 12])
+@pytest.mark.parametrize("ta", ["N", "T"])
+def test_ozaki_slices_extreme_exponents(orc, S, ta):
+    """Digits of subnormals, of rows spanning ~600 decades and of zero rows:
+    the slice kernel reads them from the significand bits and must agree with
+    the FP64 trunc-by-128 recurrence of the oracle."""
+    m, n, k = 70, 40, 90
+    rng = np.random.default_rng(5)
+    Aop = rng.standard_normal((m, k)) * np.exp2(rng.integers(-40, 40, (m, k)))
+    Aop[0] = rng.standard_normal(k) * 5e-324 * rng.integers(1, 2 ** 20, k)   # subnormal row
+    Aop[1, :] = 0.0
+    Aop[2] = rng.standard_normal(k) * np.exp2(rng.integers(-1000, 1000, k))   # huge spread
+    Aop[3, ::3] = 5e-324                                                     # smallest subnormal
+    Aop[4] = np.exp2(rng.integers(-1074, -1022, k)) * np.sign(rng.standard_normal(k))
+    Aop[5, 0] = np.finfo(np.float64).max
+    Aop[6] = -np.exp2(-7.0 * np.arange(k) / 3.0)                             # digit boundaries
+    A = np.asfortranarray(Aop if ta == "N" else Aop.T)
+    B = orc.uniform((k, n), np.float64, 22, 1)
+    need = g.split_workspace_bytes(1, m, n, k, S)
+    ws = ws_tensor(need)
+    dA, dB = to_dev(A), to_dev(B)
+    dC = to_dev(np.zeros((m, n), order="F"))
+    rc = g.dgemm_ozaki(ta, "N", m, n, k, 1.0, dA.data_ptr(), A.shape[0], dB.data_ptr(), k, 0.0,
+                       dC.data_ptr(), m, slices=S, workspace=ws.data_ptr(), workspace_bytes=need)
+    assert rc == g.OK
+    sync()
+    Kp, Mp = ru(k, 64), ru(m, 128)
+    raw = ws.cpu().numpy()[aligned_view(ws, need):]
+    bf = raw[:2 * S * Mp * Kp].view(np.uint16).astype(np.uint32) << 16
+    As = bf.view(np.float32).astype(np.float64).reshape(S, Mp, Kp)
+    sa, _ = osp.ozaki_slices(Aop, S)
+    for s in range(S):
+        assert np.array_equal(As[s, :m, :k], sa[s]), s
+    assert g.device_error() == 0
+
+
 def test_ozaki_vs_plain_accuracy(orc):
     """At S = 8 the Ozaki form is as accurate as the plain FP64 kernel (uniform data)."""
     m = n = 384
