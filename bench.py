@@ -60,6 +60,14 @@ WORKLOADS = {
     "rank256_s": dict(prec="s", ta="N", tb="T", m=32768, n=32768, k=256, lda=32800, ldb=32800,
                       ldc=32832, alpha=-1.0, beta=1.0, seed=3),
 }
+# complex GEMM (the reference's OpenBLAS-style c/z kernels): the split form on
+# the embedded real problem, at equal error to the plain 4M method
+CWORKLOADS = {
+    "zgemm_nn_4096": dict(prec="z", ta="N", tb="N", m=4096, n=4096, k=4096, alpha=1.0, beta=1.0,
+                          seed=5),
+    "cgemm_nn_8192": dict(prec="c", ta="N", tb="N", m=8192, n=8192, k=8192, alpha=1.0, beta=1.0,
+                          seed=6),
+}
 METRIC = "GEMM TFLOP/s on 1 GB300: tensor-core split vs native FP64/FP32, at equal error"
 L2_BYTES = 129 * 2**20
 
@@ -408,6 +416,200 @@ def run_ours(args, torch, rank, world):
         print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- complex workloads
+def exact_samples_complex(A_rows, B_cols, alpha, beta, c0):
+    """Correctly rounded alpha*dot + beta*c (real alpha, beta) of complex dots."""
+    import numpy as np
+
+    out = np.empty(A_rows.shape[0], np.complex128)
+    for q in range(A_rows.shape[0]):
+        ar, ai = A_rows[q].real.astype(np.float64), A_rows[q].imag.astype(np.float64)
+        br, bi = B_cols[q].real.astype(np.float64), B_cols[q].imag.astype(np.float64)
+        terms_r, terms_i = [], []
+        for x, y, sgn, dst in ((ar, br, 1, terms_r), (ai, bi, -1, terms_r), (ar, bi, 1, terms_i),
+                               (ai, br, 1, terms_i)):
+            p, e = _two_prod(sgn * x, y)
+            dst.extend(p.tolist())
+            dst.extend(e.tolist())
+        re, im = math.fsum(terms_r), math.fsum(terms_i)
+        out[q] = complex(math.fsum([alpha * re, beta * float(c0[q].real)]),
+                         math.fsum([alpha * im, beta * float(c0[q].imag)]))
+    return out
+
+
+def rel_err_c(got, truth):
+    import numpy as np
+
+    d = np.abs(np.asarray(got, np.complex128) - truth)
+    mx = float(np.max(d / np.maximum(np.abs(truth), 1e-300)))
+    fro = float(np.linalg.norm(d) / max(np.linalg.norm(truth), 1e-300))
+    return mx, fro
+
+
+def run_complex(args, torch, rank, world):
+    """ZGEMM / CGEMM NN: split form (Ozaki / BF16xP on the embedded 2m x n x 2k
+    real problem) at equal error to the plain 4M method; 8mnk flops per call."""
+    import numpy as np
+
+    import gemm_avx2_gb300 as g
+
+    w = CWORKLOADS[args.workload]
+    p, m, n, k = w["prec"], w["m"], w["n"], w["k"]
+    dt = torch.complex128 if p == "z" else torch.complex64
+    rdt = torch.float64 if p == "z" else torch.float32
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(int(w["seed"]))
+
+    def cu(rows, cols):  # column-major rows x cols, stored as a (cols, rows) tensor
+        x = torch.rand((cols, rows, 2), generator=gen, device="cuda", dtype=rdt) * 2 - 1
+        return torch.view_as_complex(x.contiguous())
+
+    A, B, C0 = cu(m, k), cu(k, n), cu(m, n)
+    C = C0.clone()
+    stream = torch.cuda.current_stream().cuda_stream
+    flops = 8.0 * m * n * k
+
+    def call(method, param, Cbuf, ws=None, wsb=0):
+        return g.complex_device(p, w["ta"], w["tb"], m, n, k, w["alpha"], A.data_ptr(), m,
+                                B.data_ptr(), k, w["beta"], Cbuf.data_ptr(), m, method=method,
+                                param=param, workspace=ws, workspace_bytes=wsb, stream=stream)
+
+    rng = np.random.default_rng(99)
+    rows, cols = rng.integers(0, m, 512), rng.integers(0, n, 512)
+    Ar = A[:, rows].T.cpu().numpy()
+    Bc = B[cols, :].cpu().numpy()
+    truth = exact_samples_complex(Ar, Bc, w["alpha"], w["beta"], C0[cols, rows].cpu().numpy())
+
+    def measure(method, param, reps):
+        C.copy_(C0)
+        assert call(method, param, C) == g.OK
+        torch.cuda.synchronize()
+        err = rel_err_c(C[cols, rows].cpu().numpy(), truth)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        for _ in range(reps):
+            call(method, param, C)
+        a1.record()
+        torch.cuda.synchronize()
+        return err, a0.elapsed_time(a1) / reps
+
+    plain_err, plain_ms = measure(g.CPLX_4M, 0, 1 if p == "z" else 3)
+    m3_err, m3_ms = measure(g.CPLX_3M, 0, 1 if p == "z" else 3)
+    cands = list(range(6, 13)) if p == "z" else [3, 6]
+    errs, chosen = {}, None
+    for param in cands:
+        C.copy_(C0)
+        assert call(g.CPLX_SPLIT, param, C) == g.OK
+        torch.cuda.synchronize()
+        errs[param] = rel_err_c(C[cols, rows].cpu().numpy(), truth)
+        if errs[param][0] <= plain_err[0] and errs[param][1] <= plain_err[1]:
+            chosen = param
+            break
+    param = chosen if chosen is not None else cands[-1]
+    need = g.complex_workspace_bytes(p, g.CPLX_SPLIT, w["tb"], m, n, k, param)
+    ws = torch.empty(need, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        assert call(g.CPLX_SPLIT, param, C, ws.data_ptr(), need) == g.OK
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    barrier(torch, world)
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for s_ in range(args.steps):
+        evs[s_][0].record()
+        assert call(g.CPLX_SPLIT, param, C, ws.data_ptr(), need) == g.OK
+        evs[s_][1].record()
+    t1.record()
+    torch.cuda.synchronize()
+    barrier(torch, world)
+    clocks = sampler.stop() if sampler else None
+    total_ms = t0.elapsed_time(t1)
+    step_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
+    max_ms = allreduce_max(torch, world, total_ms)
+    value = flops * args.steps * world / (max_ms / 1e3) / 1e12
+    assert g.device_error() == 0
+
+    e2e = {"value": None, "skipped": "--no-e2e"}
+    if not args.no_e2e:
+        try:
+            hA = torch.empty(A.shape, dtype=dt, pin_memory=True)
+            hB = torch.empty(B.shape, dtype=dt, pin_memory=True)
+            hC = torch.empty(C0.shape, dtype=dt, pin_memory=True)
+            hA.copy_(A)
+            hB.copy_(B)
+            hC.copy_(C0)
+            ah, bh, ch = hA.numpy(), hB.numpy(), hC.numpy()
+            for _ in range(2):
+                assert g.host_complex(p, w["ta"], w["tb"], m, n, k, w["alpha"], ah, m, bh, k,
+                                      w["beta"], ch, m, method=g.CPLX_SPLIT, param=param) == g.OK
+            steps_e2e = max(3, min(args.steps, 10))
+            t = time.perf_counter()
+            for _ in range(steps_e2e):
+                assert g.host_complex(p, w["ta"], w["tb"], m, n, k, w["alpha"], ah, m, bh, k,
+                                      w["beta"], ch, m, method=g.CPLX_SPLIT, param=param) == g.OK
+            dts = (time.perf_counter() - t) / steps_e2e
+            esz = 16 if p == "z" else 8
+            e2e = {"value": round(flops / dts / 1e12, 3), "unit": "TFLOP/s",
+                   "h2d_bytes_per_step": (m * k + k * n + m * n) * esz,
+                   "d2h_bytes_per_step": m * n * esz, "ms_per_step": round(dts * 1e3, 3),
+                   "api": "gb300_host_%sgemm (GB300_CPLX_SPLIT)" % p,
+                   "transfer": "pinned host buffers read and written in place over the "
+                               "coherent CPU-GPU link"}
+        except Exception as ex:  # noqa: BLE001
+            e2e = {"value": None, "error": repr(ex)}
+
+    pk = peaks()
+    products = (param * (param + 1)) // 2 if p == "z" else param
+    pipe_flops = products * flops
+    achieved = pipe_flops / (step_ms / 1e3) / 1e12
+    form_name = ("ozaki_s%d" % param) if p == "z" else ("bf16x%d" % param)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(max_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if p == "z" else "c64",
+        "data": "synthetic (seeded uniform[-1,1) real and imaginary parts, on the device)",
+        "config": {"workload": args.workload, "transa": w["ta"], "transb": w["tb"], "m": m,
+                   "n": n, "k": k, "alpha": w["alpha"], "beta": w["beta"], "form": form_name,
+                   "flops_per_call": "8mnk",
+                   "l2": "inputs larger than L2 (%d MB per operand > %d MB)" % (
+                       A.numel() * A.element_size() // 2**20, L2_BYTES // 2**20),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": e2e,
+        "roofline": {"bound": "tensor", "achieved": round(achieved, 2),
+                     "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": round(achieved / pk["bf16_tflops"], 4), "traffic": None,
+                     "kernel": "ozaki_gemm_kernel" if p == "z" else "bf16x_gemm_kernel",
+                     "kernel_ms": round(step_ms, 4),
+                     "timing": "whole step (operand embedding, split kernels and the tcgen05 "
+                               "GEMM): a lower bound on the GEMM kernel's rate",
+                     "peak_source": "%s bf16 burst (MEASURED_PEAKS.json)" % pk["source"],
+                     "algorithmic_flops_per_launch": pipe_flops},
+        "plain": {"kernel": "4M on the plain %s kernel" % ("DMMA" if p == "z" else "FFMA"),
+                  "value": round(flops / (plain_ms / 1e3) / 1e12, 3), "unit": "TFLOP/s",
+                  "ms": round(plain_ms, 3),
+                  "split_speedup": round(value / world / (flops / (plain_ms / 1e3) / 1e12), 3)},
+        "method_3m": {"value": round(flops / (m3_ms / 1e3) / 1e12, 3), "unit": "TFLOP/s (8mnk)",
+                      "ms": round(m3_ms, 3), "max_rel": m3_err[0], "fro_rel": m3_err[1]},
+        "accuracy": {"samples": int(len(truth)), "truth": "exact sampled complex dot products",
+                     "plain_max_rel": plain_err[0], "plain_fro_rel": plain_err[1],
+                     "split": {str(q): {"max_rel": e[0], "fro_rel": e[1]} for q, e in errs.items()},
+                     "chosen": form_name},
+        "clocks": clocks,
+        "gpu_launches": args.steps * ((1 + 6) if p == "z" else (1 + 3)),
+    }
+    if rank == 0:
+        line["cpu_baseline"] = (cpu_baseline_complex(w, args.cpu_seconds) if not args.no_cpu
+                                else {"value": None, "skipped": "--no-cpu"})
+        print(json.dumps(line), flush=True)
+
+
 def exponent_spread(prob):
     """max - min of the binary exponent over the nonzero entries of op(A) and op(B)."""
     import torch
@@ -627,6 +829,55 @@ def cpu_baseline(w, seconds):
         return {"value": None, "error": repr(ex)}
 
 
+def cpu_complex_rate(w, seconds):
+    """8mnk TFLOP/s of the reference's complex kernel on a column sample (all
+    host cores, columns split across threads; the kernels run where they were
+    compiled from the reference sources, x86-64), else of the portable
+    restatement of its arithmetic (OpenMP over columns)."""
+    import numpy as np
+
+    import oracle
+
+    if not os.path.exists(os.path.join(ROOT, "oracle", "liborc.so")):
+        oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    dt = np.complex128 if w["prec"] == "z" else np.complex64
+    m, k = w["m"], w["k"]
+    A = oracle.cuniform((m, k), dt, w["seed"], 0)
+    ref = oracle.RefCplx() if oracle.RefCplx.available() else None
+    kind = "reference" if ref else "port"
+
+    def run(ns):
+        B = oracle.cuniform((k, ns), dt, w["seed"], 1)
+        C = oracle.cuniform((m, ns), dt, w["seed"], 2)
+        t = time.perf_counter()
+        if ref:   # packs A once, then B's columns over the OpenMP team
+            ref.gemm_conj(0, 0, w["alpha"], A, B, C)
+        else:
+            oracle.zgemm_port(0, 0, w["alpha"], A, B, C)
+        return time.perf_counter() - t
+
+    ns = 4 * cores
+    run(ns)
+    t0 = run(ns)
+    ns = int(min(w["n"], max(cores, ns * seconds / max(t0, 1e-3))))
+    t = run(ns)
+    tf = 8.0 * m * ns * k / t / 1e12
+    sample = "%sgemm NN m=%d n=%d (of %d) k=%d: %d columns of C" % (w["prec"], m, ns, w["n"], k,
+                                                                     ns)
+    return kind, cores, tf, t, sample
+
+
+def cpu_baseline_complex(w, seconds):
+    try:
+        kind, cores, tf, t, sample = cpu_complex_rate(w, seconds)
+        return {"value": round(tf, 5), "unit": "TFLOP/s", "cores": cores, "kind": kind,
+                "sample": sample, "seconds": round(t, 2)}
+    except Exception as ex:  # noqa: BLE001
+        return {"value": None, "error": repr(ex)}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -634,12 +885,13 @@ def run_reference(args, rank, world):
         print(json.dumps({"impl": "reference", "metric": METRIC,
                           "unavailable": "the reference has no grouped interface"}))
         return
-    w = WORKLOADS[args.workload]
+    cplx = args.workload in CWORKLOADS
+    w = CWORKLOADS[args.workload] if cplx else WORKLOADS[args.workload]
     per_step = max(1.0, min(10.0, 120.0 / max(1, args.steps + args.warmup)))
     vals = []
     info = None
     for i in range(args.warmup + args.steps):
-        kind, cores, tf, t, sample = cpu_sample_rate(w, per_step)
+        kind, cores, tf, t, sample = (cpu_complex_rate if cplx else cpu_sample_rate)(w, per_step)
         if i >= args.warmup:
             vals.append((tf, t))
         info = (kind, cores, sample)
@@ -648,7 +900,8 @@ def run_reference(args, rank, world):
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * sum(v[1] for v in vals) / len(vals), 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if w["prec"] == "d" else "f32", "data": "synthetic",
+            "dtype": {"d": "f64", "s": "f32", "z": "c128", "c": "c64"}[w["prec"]],
+            "data": "synthetic",
             "config": {"workload": args.workload, "transa": w["ta"], "transb": w["tb"],
                        "m": w["m"], "n": w["n"], "k": w["k"]},
             "impl": "reference",
@@ -679,7 +932,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["grouped_1024"],
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(CWORKLOADS) + ["grouped_1024"],
                     default="sgemm_tn_8192")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--phi", type=float, default=None,
@@ -703,6 +956,8 @@ def main():
         torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
     if args.workload == "grouped_1024":
         run_grouped(args, torch, rank, world)
+    elif args.workload in CWORKLOADS:
+        run_complex(args, torch, rank, world)
     else:
         run_ours(args, torch, rank, world)
     if world > 1:

@@ -4,6 +4,8 @@ The product is native code in this directory:
 
 * ``DGEMM.so`` / ``SGEMM.so`` export exactly ``dgemm_`` / ``sgemm_`` with the
   reference's Fortran-style ABI (reference ``src/gemm_driver.c:118``).
+* ``ZGEMM.so`` / ``CGEMM.so`` export the complex BLAS symbols ``zgemm_`` /
+  ``zgemm3m_`` and ``cgemm_`` / ``cgemm3m_``.
 * ``libgemm_gb300.so`` holds every CUDA kernel and the ``gb300_*`` C ABI
   declared in ``include/gemm_gb300.h`` (device pointers, streams, split forms).
 
@@ -35,6 +37,11 @@ ERR_NOMEM = 4
 ERR_UNSUPPORTED = 5
 ERR_WORKSPACE = 6
 ERR_NOALLOC_LIMIT = 7
+
+# complex GEMM methods (gb300_cgemm / gb300_zgemm)
+CPLX_4M = 0
+CPLX_3M = 1
+CPLX_SPLIT = 2
 
 _core = None
 _drop = {}
@@ -122,15 +129,27 @@ def core() -> ctypes.CDLL:
         L.gb300_grouped_graph_destroy.argtypes = [c_void_p]
         L.gb300_sgemm_bf16x_noalloc.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int,
                                                     c_float, c_void_p, c_int, c_int, c_void_p]
+        cg = [c_char, c_char, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int,
+              c_void_p, c_void_p, c_int, c_int, c_int]
+        L.gb300_cgemm.argtypes = cg + [c_void_p, c_size_t, c_void_p]
+        L.gb300_zgemm.argtypes = cg + [c_void_p, c_size_t, c_void_p]
+        L.gb300_host_cgemm.argtypes = cg
+        L.gb300_host_zgemm.argtypes = cg
+        L.gb300_complex_workspace_bytes.argtypes = [c_int, c_int, c_char, c_int, c_int, c_int,
+                                                    c_int]
+        L.gb300_complex_workspace_bytes.restype = c_size_t
         _core = L
     return _core
 
 
+_DROPIN = {"d": "DGEMM.so", "s": "SGEMM.so", "z": "ZGEMM.so", "c": "CGEMM.so"}
+
+
 def dropin(precision: str) -> ctypes.CDLL:
-    """The drop-in library: 'd' -> DGEMM.so, 's' -> SGEMM.so."""
+    """The drop-in library: 'd' DGEMM.so, 's' SGEMM.so, 'z' ZGEMM.so, 'c' CGEMM.so."""
     if precision not in _drop:
         core()  # resolve libgemm_gb300.so first (RTLD_GLOBAL)
-        _drop[precision] = _load("DGEMM.so" if precision == "d" else "SGEMM.so")
+        _drop[precision] = _load(_DROPIN[precision])
     return _drop[precision]
 
 
@@ -180,6 +199,43 @@ def host_gemm(precision, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c
     f = L.gb300_host_dgemm if precision == "d" else L.gb300_host_sgemm
     return f(_b(transa), _b(transb), m, n, k, alpha, _ptr(a), lda, _ptr(b), ldb, beta, _ptr(c),
              ldc)
+
+
+def _cscalar(v, precision):
+    """(re, im) of a Python number as a ctypes array (complex scalars by pointer)."""
+    v = complex(v)
+    T = c_double if precision == "z" else c_float
+    return (T * 2)(v.real, v.imag)
+
+
+def zgemm(transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, method3m=False) -> None:
+    """zgemm_ (or zgemm3m_) of ZGEMM.so on host complex128 column-major arrays:
+    C = alpha*op(A)*op(B) + beta*C, trans 'N', 'T', 'C' (conjugate transpose) or
+    'R' (conjugate).  Returns nothing; invalid arguments leave ``c`` untouched."""
+    _complex_dropin("z", transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, method3m)
+
+
+def cgemm(transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, method3m=False) -> None:
+    """cgemm_ (or cgemm3m_) of CGEMM.so on complex64 arrays, as :func:`zgemm`."""
+    _complex_dropin("c", transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, method3m)
+
+
+def _complex_dropin(p, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, method3m):
+    L = dropin(p)
+    f = getattr(L, p + ("gemm3m_" if method3m else "gemm_"))
+    i = lambda v: ctypes.byref(c_int(int(v)))
+    al, be = _cscalar(alpha, p), _cscalar(beta, p)
+    f(ctypes.c_char_p(_b(transa)), ctypes.c_char_p(_b(transb)), i(m), i(n), i(k), al, _ptr(a),
+      i(lda), _ptr(b), i(ldb), be, _ptr(c), i(ldc))
+
+
+def host_complex(precision, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
+                 method=CPLX_4M, param=0) -> int:
+    """gb300_host_zgemm / gb300_host_cgemm ('z' / 'c') with a status code."""
+    L = core()
+    f = L.gb300_host_zgemm if precision == "z" else L.gb300_host_cgemm
+    return f(_b(transa), _b(transb), m, n, k, _cscalar(alpha, precision), _ptr(a), lda, _ptr(b),
+             ldb, _cscalar(beta, precision), _ptr(c), ldc, method, param)
 
 
 # ---------------------------------------------------------------------------
@@ -269,6 +325,22 @@ def trmm(precision, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, form=
     f = core().gb300_dtrmm if precision == "d" else core().gb300_strmm
     return f(_b(side), _b(uplo), _b(transa), _b(diag), m, n, alpha, _ptr(A), lda, _ptr(B), ldb,
              form, c_void_p(stream))
+
+
+def complex_device(precision, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                   method=CPLX_4M, param=0, workspace=None, workspace_bytes=0, stream=0) -> int:
+    """gb300_zgemm / gb300_cgemm on device buffers (complex interleaved, ld in
+    complex elements); stream-ordered, returns a status."""
+    L = core()
+    f = L.gb300_zgemm if precision == "z" else L.gb300_cgemm
+    return f(_b(transa), _b(transb), m, n, k, _cscalar(alpha, precision), _ptr(A), lda, _ptr(B),
+             ldb, _cscalar(beta, precision), _ptr(C), ldc, method, param, _ptr(workspace),
+             workspace_bytes, c_void_p(stream))
+
+
+def complex_workspace_bytes(precision, method, transb, m, n, k, param=0) -> int:
+    return core().gb300_complex_workspace_bytes(1 if precision == "z" else 0, method, _b(transb),
+                                                m, n, k, param)
 
 
 def split_workspace_bytes(kind: int, m: int, n: int, k: int, param: int) -> int:
@@ -401,4 +473,6 @@ CORE_SYMBOLS = [
     "gb300_autotune", "gb300_tune_lookup", "gb300_tune_cache_save", "gb300_tune_cache_load",
     "gb300_tune_cache_clear", "gb300_dtrsm", "gb300_strsm", "gb300_dtrmm", "gb300_strmm",
     "gb300_grouped_graph_create", "gb300_grouped_graph_launch", "gb300_grouped_graph_destroy",
+    "gb300_cgemm", "gb300_zgemm", "gb300_host_cgemm", "gb300_host_zgemm",
+    "gb300_complex_workspace_bytes",
 ]

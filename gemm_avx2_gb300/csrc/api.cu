@@ -242,6 +242,90 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
   return word ? GB300_ERR_TIMEOUT : GB300_OK;
 }
 
+// Complex host-pointer path (the pattern of host_gemm above).  Complex
+// elements are 2 * sizeof(T) bytes; leading dimensions are in complex elements.
+template <typename T>
+static int host_complex(char ta, char tb, int m, int n, int k, const T *alpha, const T *a, int lda,
+                        const T *b, int ldb, const T *beta, T *c, int ldc, int method,
+                        int param) {
+  const int ck = complex_check(ta, tb, m, n, k, lda, ldb, ldc, method);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  const bool alpha_zero = alpha[0] == T(0) && alpha[1] == T(0);
+  if (alpha_zero && beta[0] == T(1) && beta[1] == T(0)) return GB300_OK;
+  auto trans = [](char t) { return !(t == 'N' || t == 'n' || t == 'R' || t == 'r'); };
+  const int arows = trans(ta) ? k : m, acols = trans(ta) ? m : k;
+  const int brows = trans(tb) ? n : k, bcols = trans(tb) ? k : n;
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (!s->stage_stream &&
+      cudaStreamCreateWithFlags(&s->stage_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  cudaStream_t st = s->stage_stream;
+  const bool need_ab = !alpha_zero && k > 0;
+  const size_t wneed =
+      need_ab ? complex_workspace_bytes(sizeof(T) == 8, method, tb, m, n, k, param) : 0;
+  if (need_ab && !wneed) return GB300_ERR_ARG;
+  auto run = [&](const T *A, int la, const T *B, int lb, T *C, int lc) -> int {
+    void *ws = wneed ? cached_workspace(s, st, wneed) : nullptr;
+    if (wneed && !ws) return GB300_ERR_NOMEM;
+    if constexpr (sizeof(T) == 8)
+      return complex_gemm_d(ta, tb, m, n, k, alpha, A, la, B, lb, beta, C, lc, method, param, ws,
+                            wneed, st, s->err);
+    else
+      return complex_gemm_s(ta, tb, m, n, k, alpha, A, la, B, lb, beta, C, lc, method, param, ws,
+                            wneed, st, s->err);
+  };
+  auto finish = [&](int rc) -> int {
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (rc != GB300_OK) return rc;
+    if (e != cudaSuccess) return GB300_ERR_CUDA;
+    unsigned word = 0;
+    cudaMemcpy(&word, s->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    return word ? GB300_ERR_TIMEOUT : GB300_OK;
+  };
+  if (method == GB300_CPLX_SPLIT && host_direct_ok(a, b, c)) {
+    // the split method reads A and B once (pack and split kernels) and C once
+    // (epilogue): it runs on the caller's memory over the coherent link
+    return finish(run(a, lda, b, ldb, c, ldc));
+  }
+  const size_t E = 2 * sizeof(T);
+  const int epl = 16 / (int)E > 0 ? 16 / (int)E : 1;
+  auto up = [&](int r) { return ((r > 1 ? r : 1) + epl - 1) / epl * epl; };
+  const int dla = up(arows), dlb = up(brows), dlc = up(m);
+  const size_t bytesA = need_ab ? (size_t)dla * acols * E : 0;
+  const size_t bytesB = need_ab ? (size_t)dlb * bcols * E : 0;
+  const size_t bytesC = (size_t)dlc * n * E;
+  if (!grow(&s->stage[0], &s->stage_bytes[0], bytesA + 16) ||
+      !grow(&s->stage[1], &s->stage_bytes[1], bytesB + 16) ||
+      !grow(&s->stage[2], &s->stage_bytes[2], bytesC + 16))
+    return GB300_ERR_NOMEM;
+  T *dA = static_cast<T *>(s->stage[0]), *dB = static_cast<T *>(s->stage[1]);
+  T *dC = static_cast<T *>(s->stage[2]);
+  cudaError_t e = cudaSuccess;
+  if (need_ab) {
+    e = cudaMemcpy2DAsync(dA, dla * E, a, (size_t)lda * E, arows * E, acols,
+                          cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(dB, dlb * E, b, (size_t)ldb * E, brows * E, bcols,
+                            cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dC, dlc * E, c, (size_t)ldc * E, m * E, n, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return GB300_ERR_CUDA;
+  const int rc = run(need_ab ? dA : nullptr, dla, need_ab ? dB : nullptr, dlb, dC, dlc);
+  if (rc != GB300_OK) {
+    cudaStreamSynchronize(st);
+    return rc;
+  }
+  e = cudaMemcpy2DAsync(c, (size_t)ldc * E, dC, dlc * E, m * E, n, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(st);
+    return GB300_ERR_CUDA;
+  }
+  return finish(GB300_OK);
+}
+
 // Failure-detection self-test: one CTA waits on an mbarrier that nothing ever
 // arrives on, with a short poll limit; the wait gives up, records
 // kErrTimeoutFull in the error word and the kernel returns normally.
@@ -306,6 +390,80 @@ GB300_API int gb300_sgemm(char ta, char tb, int m, int n, int k, float alpha, co
   if (!err) return GB300_ERR_CUDA;
   return plain_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
                      static_cast<cudaStream_t>(stream), err);
+}
+
+// ---------------------------------------------------------------- complex
+static bool complex_param_ok(bool dbl, int method, int param) {
+  if (method != GB300_CPLX_SPLIT) return true;
+  return dbl ? (param == 0 || (param >= 2 && param <= kOzakiMaxSlices))
+             : (param == 0 || param == 3 || param == 6);
+}
+
+GB300_API size_t gb300_complex_workspace_bytes(int is_double, int method, char tb, int m, int n,
+                                               int k, int param) {
+  if (!complex_param_ok(is_double != 0, method, param)) return 0;
+  return complex_workspace_bytes(is_double, method, tb, m, n, k, param);
+}
+
+template <typename T>
+static int device_complex(char ta, char tb, int m, int n, int k, const T *alpha, const T *A,
+                          int lda, const T *B, int ldb, const T *beta, T *C, int ldc, int method,
+                          int param, void *ws, size_t ws_bytes, void *stream) {
+  const bool dbl = sizeof(T) == 8;
+  if (!alpha || !beta || !complex_param_ok(dbl, method, param)) return GB300_ERR_ARG;
+  const int ck = complex_check(ta, tb, m, n, k, lda, ldb, ldc, method);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto call = [&](void *w, size_t wb, unsigned *err) -> int {
+    if constexpr (sizeof(T) == 8)
+      return complex_gemm_d(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, method, param,
+                            w, wb, st, err);
+    else
+      return complex_gemm_s(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, method, param,
+                            w, wb, st, err);
+  };
+  if (ws) {
+    unsigned *err = device_error_word();
+    if (!err) return GB300_ERR_CUDA;
+    return call(ws, ws_bytes, err);
+  }
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  const bool reads_ab = !(alpha[0] == T(0) && alpha[1] == T(0)) && k > 0;
+  const size_t need = reads_ab ? complex_workspace_bytes(dbl, method, tb, m, n, k, param) : 0;
+  if (reads_ab && !need) return GB300_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  void *w = need ? cached_workspace(s, st, need) : nullptr;
+  if (need && !w) return GB300_ERR_NOMEM;
+  return call(w, need, s->err);
+}
+
+GB300_API int gb300_cgemm(char ta, char tb, int m, int n, int k, const float *alpha,
+                          const float *A, int lda, const float *B, int ldb, const float *beta,
+                          float *C, int ldc, int method, int param, void *ws, size_t ws_bytes,
+                          void *stream) {
+  return device_complex<float>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, method,
+                               param, ws, ws_bytes, stream);
+}
+GB300_API int gb300_zgemm(char ta, char tb, int m, int n, int k, const double *alpha,
+                          const double *A, int lda, const double *B, int ldb, const double *beta,
+                          double *C, int ldc, int method, int param, void *ws, size_t ws_bytes,
+                          void *stream) {
+  return device_complex<double>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, method,
+                                param, ws, ws_bytes, stream);
+}
+GB300_API int gb300_host_cgemm(char ta, char tb, int m, int n, int k, const float *alpha,
+                               const float *a, int lda, const float *b, int ldb,
+                               const float *beta, float *c, int ldc, int method, int param) {
+  if (!alpha || !beta || !complex_param_ok(false, method, param)) return GB300_ERR_ARG;
+  return host_complex<float>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, method, param);
+}
+GB300_API int gb300_host_zgemm(char ta, char tb, int m, int n, int k, const double *alpha,
+                               const double *a, int lda, const double *b, int ldb,
+                               const double *beta, double *c, int ldc, int method, int param) {
+  if (!alpha || !beta || !complex_param_ok(true, method, param)) return GB300_ERR_ARG;
+  return host_complex<double>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, method,
+                              param);
 }
 
 GB300_API size_t gb300_split_workspace_bytes(int kind, int m, int n, int k, int param) {

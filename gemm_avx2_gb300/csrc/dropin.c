@@ -2,12 +2,49 @@
  * SGEMM.so.  It is the only symbol each library exports, exactly as the
  * reference's libraries (Makefile:14-18, src/gemm_driver.c:8-14,118), and it
  * forwards to the GB300 host-pointer path in libgemm_gb300.so.  Like the
- * reference it returns nothing; invalid arguments leave C untouched. */
+ * reference it returns nothing; invalid arguments leave C untouched.
+ *
+ * Built with -DZCOMPLEX / -DCCOMPLEX it is ZGEMM.so / CGEMM.so instead: the
+ * complex BLAS symbols zgemm_ and zgemm3m_ (cgemm_, cgemm3m_), complex scalars
+ * and matrices as interleaved (re, im) pairs, trans 'N', 'T', 'C' or 'R'.  The
+ * reference has complex GEMM only as OpenBLAS-style kernels
+ * (OpenBLAS-like_implementation/zgemm_kernel_4x2_haswell.c,
+ * zgemm3m_kernel_4x4_haswell.c and their c counterparts) that an OpenBLAS
+ * driver reaches through these same BLAS names. */
 #include "../../include/gemm_gb300.h"
 
 #define EXPORT __attribute__((visibility("default")))
 
-#ifdef DOUBLE
+#if defined(ZCOMPLEX)
+EXPORT void zgemm_(const char *transa, const char *transb, const int *m, const int *n,
+                   const int *k, const double *alpha, const double *a, const int *lda,
+                   const double *b, const int *ldb, const double *beta, double *c,
+                   const int *ldc) {
+  (void)gb300_host_zgemm(*transa, *transb, *m, *n, *k, alpha, a, *lda, b, *ldb, beta, c, *ldc,
+                         GB300_CPLX_4M, 0);
+}
+EXPORT void zgemm3m_(const char *transa, const char *transb, const int *m, const int *n,
+                     const int *k, const double *alpha, const double *a, const int *lda,
+                     const double *b, const int *ldb, const double *beta, double *c,
+                     const int *ldc) {
+  (void)gb300_host_zgemm(*transa, *transb, *m, *n, *k, alpha, a, *lda, b, *ldb, beta, c, *ldc,
+                         GB300_CPLX_3M, 0);
+}
+#elif defined(CCOMPLEX)
+EXPORT void cgemm_(const char *transa, const char *transb, const int *m, const int *n,
+                   const int *k, const float *alpha, const float *a, const int *lda,
+                   const float *b, const int *ldb, const float *beta, float *c, const int *ldc) {
+  (void)gb300_host_cgemm(*transa, *transb, *m, *n, *k, alpha, a, *lda, b, *ldb, beta, c, *ldc,
+                         GB300_CPLX_4M, 0);
+}
+EXPORT void cgemm3m_(const char *transa, const char *transb, const int *m, const int *n,
+                     const int *k, const float *alpha, const float *a, const int *lda,
+                     const float *b, const int *ldb, const float *beta, float *c,
+                     const int *ldc) {
+  (void)gb300_host_cgemm(*transa, *transb, *m, *n, *k, alpha, a, *lda, b, *ldb, beta, c, *ldc,
+                         GB300_CPLX_3M, 0);
+}
+#elif defined(DOUBLE)
 EXPORT void dgemm_(const char *transa, const char *transb, const int *m, const int *n,
                    const int *k, const double *alpha, const double *a, const int *lda,
                    const double *b, const int *ldb, const double *beta, double *c,

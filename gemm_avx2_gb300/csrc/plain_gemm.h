@@ -68,4 +68,18 @@ int trsm_s(int solve, char side, char uplo, char ta, char diag, int m, int n, fl
            const float *A, int lda, float *B, int ldb, int form, void *ws, size_t wsb,
            cudaStream_t st, unsigned *err);
 
+// Complex GEMM (cplx.cu): method GB300_CPLX_4M / _3M / _SPLIT, complex
+// numbers interleaved, alpha and beta as (re, im) pairs in host memory.
+size_t complex_workspace_bytes(int is_double, int method, char tb, int m, int n, int k,
+                               int param);
+int complex_check(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc, int method);
+int complex_gemm_d(char ta, char tb, int m, int n, int k, const double *alpha, const double *A,
+                   int lda, const double *B, int ldb, const double *beta, double *C, int ldc,
+                   int method, int param, void *ws, size_t ws_bytes, cudaStream_t st,
+                   unsigned *err);
+int complex_gemm_s(char ta, char tb, int m, int n, int k, const float *alpha, const float *A,
+                   int lda, const float *B, int ldb, const float *beta, float *C, int ldc,
+                   int method, int param, void *ws, size_t ws_bytes, cudaStream_t st,
+                   unsigned *err);
+
 }  // namespace gb300

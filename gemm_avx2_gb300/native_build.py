@@ -4,6 +4,8 @@ Produces, in this package directory:
   libgemm_gb300.so  all CUDA kernels (sm_103a) + the gb300_* C ABI
   DGEMM.so          exports only dgemm_ (drop-in for the reference's DGEMM.so)
   SGEMM.so          exports only sgemm_ (drop-in for the reference's SGEMM.so)
+  ZGEMM.so          exports zgemm_ and zgemm3m_ (complex BLAS symbols)
+  CGEMM.so          exports cgemm_ and cgemm3m_
 """
 from __future__ import annotations
 
@@ -17,7 +19,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 CU_SOURCES = ["plain_gemm.cu", "tc_gemm.cu", "grouped.cu", "autotune.cu", "trsm.cu", "api.cu",
-              "noalloc.cu"]
+              "noalloc.cu", "cplx.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -55,7 +57,8 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     lib = os.path.join(PKG, "libgemm_gb300.so")
     _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", lib, *objs, "-lpthread", "-ldl"])
     cc = os.environ.get("CC", "gcc")
-    for name, defs in (("DGEMM.so", ["-DDOUBLE"]), ("SGEMM.so", [])):
+    for name, defs in (("DGEMM.so", ["-DDOUBLE"]), ("SGEMM.so", []),
+                       ("ZGEMM.so", ["-DZCOMPLEX"]), ("CGEMM.so", ["-DCCOMPLEX"])):
         _run([cc, *defs, "-O2", "-fPIC", "-shared", "-fvisibility=hidden",
               os.path.join(CSRC, "dropin.c"), "-o", os.path.join(PKG, name),
               "-L" + PKG, "-lgemm_gb300", "-Wl,-rpath,$ORIGIN"])

@@ -7,7 +7,10 @@
  *     exactly `sgemm_`, with the reference's Fortran-style signature and
  *     semantics (wjc404/GEMM_AVX2 src/gemm_driver.c:118, README.md:10).  They
  *     take HOST pointers, stage the operands through HBM, run the plain
- *     FP64/FP32 kernels and return when C has been written back.
+ *     FP64/FP32 kernels and return when C has been written back.  ZGEMM.so and
+ *     CGEMM.so export the complex BLAS symbols `zgemm_`/`zgemm3m_` and
+ *     `cgemm_`/`cgemm3m_` the same way (complex arguments as interleaved
+ *     (re, im) pairs).
  *
  *  2. Device-pointer entry points in libgemm_gb300.so (prefix gb300_).  All
  *     matrices are column-major device buffers; every call is stream-ordered
@@ -236,6 +239,51 @@ int gb300_dtrmm(char side, char uplo, char transa, char diag, int m, int n, doub
                 const double *A, int lda, double *B, int ldb, int form, void *stream);
 int gb300_strmm(char side, char uplo, char transa, char diag, int m, int n, float alpha,
                 const float *A, int lda, float *B, int ldb, int form, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Complex GEMM: C = alpha*op(A)*op(B) + beta*C on interleaved (re, im)
+ * storage, column-major, leading dimensions in complex elements.  alpha and
+ * beta point to (re, im) pairs in host memory.  trans: 'N' op(X) = X, 'R'
+ * conj(X), 'T' X^T, 'C' conj(X)^T; any other character is a transpose (as in
+ * the real path).  The reference has complex GEMM only as OpenBLAS-style
+ * packed-panel kernels outside its built library; their four conjugation
+ * variants (OpenBLAS-like_implementation/zgemm_kernel_4x2_haswell.c:6-21,
+ * cgemm_kernel_8x2_haswell.c:6-21: C += alpha * conj_a(A) * conj_b(B)) are the
+ * 'N'/'R' combinations here, and their 3M kernels
+ * (zgemm3m_kernel_4x4_haswell.c, cgemm3m_kernel_8x4_haswell.c) the 3M method.
+ *   method GB300_CPLX_4M    one real GEMM on the embedded 2m x n x 2k problem,
+ *                           plain FP64 (DMMA) / FP32 (FFMA) kernels;
+ *   method GB300_CPLX_3M    three real GEMMs (25% fewer flops, the imaginary
+ *                           part's error scales with |Re A + Im A| |Re B + Im B|);
+ *   method GB300_CPLX_SPLIT the embedded problem on the tensor-core split forms:
+ *                           6xBF16/3xBF16 for CGEMM (param = products, 0 =
+ *                           tuned), Ozaki for ZGEMM (param = slices, 0 = tuned).
+ * Same semantics as the real path otherwise: beta*C first (beta == 0 still
+ * multiplies), alpha == 0 or k == 0 reads neither A nor B.  A complex alpha is
+ * folded into op(A) (one rounding per element), a complex beta scales C first.
+ * workspace NULL: a library-owned buffer per stream; otherwise at least
+ * gb300_complex_workspace_bytes(...) bytes of device memory.
+ * ---------------------------------------------------------------------- */
+enum { GB300_CPLX_4M = 0, GB300_CPLX_3M = 1, GB300_CPLX_SPLIT = 2 };
+size_t gb300_complex_workspace_bytes(int is_double, int method, char transb, int m, int n,
+                                     int k, int param);
+int gb300_cgemm(char transa, char transb, int m, int n, int k, const float *alpha,
+                const float *A, int lda, const float *B, int ldb, const float *beta, float *C,
+                int ldc, int method, int param, void *workspace, size_t workspace_bytes,
+                void *stream);
+int gb300_zgemm(char transa, char transb, int m, int n, int k, const double *alpha,
+                const double *A, int lda, const double *B, int ldb, const double *beta,
+                double *C, int ldc, int method, int param, void *workspace,
+                size_t workspace_bytes, void *stream);
+/* Host-pointer forms (synchronous, like the drop-in symbols): the split method
+ * runs directly on host memory where the device can read it (coherent CPU-GPU
+ * systems), everything else stages through HBM. */
+int gb300_host_cgemm(char transa, char transb, int m, int n, int k, const float *alpha,
+                     const float *a, int lda, const float *b, int ldb, const float *beta,
+                     float *c, int ldc, int method, int param);
+int gb300_host_zgemm(char transa, char transb, int m, int n, int k, const double *alpha,
+                     const double *a, int lda, const double *b, int ldb, const double *beta,
+                     double *c, int ldc, int method, int param);
 
 /* Workspace needed by the split forms for one call of the given shape.
  * kind = 0: sgemm_bf16x with `param` = products; kind = 1: dgemm_ozaki with

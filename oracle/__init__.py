@@ -14,6 +14,11 @@ Contents (all thin ctypes wrappers over ``oracle/liborc.so``, built from
   (Ogita-Rump-Oishi Dot2).
 * ``RefLib``: the reference library itself (``oracle/_ref/{D,S}GEMM.so``) when
   it was compiled here from the reference sources (x86-64 only).
+* ``cuniform`` / ``zgemm_dot2`` / ``zgemm_dot2_sampled``: complex inputs and
+  the complex ground truth (trans N/T/C/R, complex alpha and beta).
+* ``zgemm_port``: the complex kernels' arithmetic in portable C (CPU baseline).
+* ``RefCplx``: the reference's OpenBLAS-style complex and 3M kernels
+  (``oracle/_ref/libcplx.so``, x86-64 only) behind ``oracle/ref_cplx.c``.
 * ``split``: numpy restatements of the split-precision decompositions
   (3xBF16 hi/lo and the int8-valued Ozaki slices) used to check the GPU split
   kernels bit for bit.
@@ -65,6 +70,17 @@ def lib():
         L.orc_geometry.argtypes = [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                                    ctypes.POINTER(c_int)]
         L.orc_max_threads.restype = c_int
+        z2 = gemm_args + [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_int]
+        L.orc_zgemm_dot2.argtypes = z2 + [c_void_p, c_int]
+        L.orc_cgemm_dot2.argtypes = z2 + [c_void_p, c_int]
+        zs = [c_char, c_char, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p,
+              c_void_p, c_int, c_void_p, c_void_p, c_int64, c_void_p]
+        L.orc_zgemm_dot2_sampled.argtypes = zs
+        L.orc_cgemm_dot2_sampled.argtypes = zs
+        zp = [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int,
+              c_void_p, c_int]
+        L.orc_zgemm_port.argtypes = zp
+        L.orc_cgemm_port.argtypes = zp
         _LIB = L
     return _LIB
 
@@ -145,6 +161,105 @@ def dot2gemm_sampled(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, rows,
     f(ta.encode(), tb.encode(), m, n, k, float(alpha), _ptr(a), lda, _ptr(b), ldb, float(beta),
       _ptr(c), ldc, _ptr(rows), _ptr(cols), rows.shape[0], _ptr(out))
     return out
+
+
+# ---------------------------------------------------------------- complex
+_REAL_OF = {np.dtype(np.complex128): np.float64, np.dtype(np.complex64): np.float32}
+
+
+def cuniform(shape, dtype, seed: int, stream: int) -> np.ndarray:
+    """Complex column-major matrix whose (re, im) pairs are consecutive U[-1,1)
+    draws of the portable generator (storage order)."""
+    dtype = np.dtype(dtype)
+    rows, cols = shape
+    re = uniform((2 * rows, cols), _REAL_OF[dtype], seed, stream)
+    return re.T.view(dtype).T
+
+
+def _cpair(v) -> np.ndarray:
+    v = complex(v)
+    return np.array([v.real, v.imag], dtype=np.float64)
+
+
+def zgemm_dot2(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc) -> np.ndarray:
+    """complex128 m x n result of alpha*op(A)op(B)+beta*C (Dot2 real and
+    imaginary parts); a, b, c complex64 or complex128 column-major, c may be None."""
+    out = np.zeros((m, n), dtype=np.complex128, order="F")
+    if m == 0 or n == 0:
+        return out
+    f = lib().orc_zgemm_dot2 if a.dtype == np.complex128 else lib().orc_cgemm_dot2
+    al, be = _cpair(alpha), _cpair(beta)
+    f(ta.encode(), tb.encode(), m, n, k, _ptr(al), _ptr(a), lda, _ptr(b), ldb, _ptr(be),
+      _ptr(c), ldc, _ptr(out), max(m, 1))
+    return out
+
+
+def zgemm_dot2_sampled(ta, tb, k, alpha, a, lda, b, ldb, beta, c, ldc, rows, cols):
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    cols = np.ascontiguousarray(cols, dtype=np.int64)
+    out = np.empty(rows.shape[0], dtype=np.complex128)
+    f = lib().orc_zgemm_dot2_sampled if a.dtype == np.complex128 else lib().orc_cgemm_dot2_sampled
+    al, be = _cpair(alpha), _cpair(beta)
+    f(ta.encode(), tb.encode(), k, _ptr(al), _ptr(a), lda, _ptr(b), ldb, _ptr(be), _ptr(c), ldc,
+      _ptr(rows), _ptr(cols), rows.shape[0], _ptr(out))
+    return out
+
+
+def zgemm_port(conj_a, conj_b, alpha, A, B, C) -> None:
+    """In place: C += alpha * conj_a(A) conj_b(B) with the reference complex
+    kernels' operation sequence in portable C (OpenMP over columns of C)."""
+    m, k = A.shape
+    n = B.shape[1]
+    if C.dtype == np.complex128:
+        al, f = np.array([complex(alpha).real, complex(alpha).imag]), lib().orc_zgemm_port
+    else:
+        al = np.array([complex(alpha).real, complex(alpha).imag], np.float32)
+        f = lib().orc_cgemm_port
+    f(int(conj_a), int(conj_b), m, n, k, _ptr(al), _ptr(A), A.shape[0], _ptr(B), B.shape[0],
+      _ptr(C), C.shape[0])
+
+
+class RefCplx:
+    """The reference's complex GEMM kernels and 3M kernels, compiled from their
+    sources into oracle/_ref/libcplx.so (x86-64 only)."""
+
+    PATH = os.path.join(HERE, "_ref", "libcplx.so")
+
+    def __init__(self):
+        if not os.path.exists(self.PATH):
+            raise FileNotFoundError("reference complex kernels not built (x86-64 with sources only)")
+        L = ctypes.CDLL(self.PATH)
+        for name, F in (("ref_zgemm_conj", c_double), ("ref_cgemm_conj", c_float)):
+            getattr(L, name).argtypes = [c_int, c_int, ctypes.c_long, ctypes.c_long, ctypes.c_long,
+                                         F, F, c_void_p, ctypes.c_long, c_void_p, ctypes.c_long,
+                                         c_void_p, ctypes.c_long]
+        for name, F in (("ref_zgemm3m_conj", c_double), ("ref_cgemm3m_conj", c_float)):
+            getattr(L, name).argtypes = [c_int, c_int, ctypes.c_long, ctypes.c_long, ctypes.c_long,
+                                         F, F, c_void_p, ctypes.c_long, c_void_p, ctypes.c_long,
+                                         c_void_p, ctypes.c_long]
+        self.L = L
+
+    @classmethod
+    def available(cls) -> bool:
+        return os.path.exists(cls.PATH)
+
+    def gemm_conj(self, conj_a: bool, conj_b: bool, alpha, A, B, C) -> None:
+        """In place: C += alpha * conj_a(A) * conj_b(B) (A m x k, B k x n, complex F arrays)."""
+        m, k = A.shape
+        n = B.shape[1]
+        f = self.L.ref_zgemm_conj if C.dtype == np.complex128 else self.L.ref_cgemm_conj
+        rc = f(int(conj_a), int(conj_b), m, n, k, complex(alpha).real, complex(alpha).imag,
+               _ptr(A), A.shape[0], _ptr(B), B.shape[0], _ptr(C), C.shape[0])
+        assert rc == 0
+
+    def gemm3m(self, alpha, A, B, C) -> None:
+        """In place: C (complex) += alpha * (A @ B) with real A (m x k) and B (k x n)."""
+        m, k = A.shape
+        n = B.shape[1]
+        f = self.L.ref_zgemm3m_conj if C.dtype == np.complex128 else self.L.ref_cgemm3m_conj
+        rc = f(0, 0, m, n, k, complex(alpha).real, complex(alpha).imag, _ptr(A), A.shape[0],
+               _ptr(B), B.shape[0], _ptr(C), C.shape[0])
+        assert rc == 0
 
 
 def set_threads(n: int) -> None:

@@ -4,6 +4,8 @@
 #   oracle/_ref/*.so    - the reference library itself, compiled straight from its
 #                         sources when they are present (x86-64 only: its kernels
 #                         are x86-64 AVX2 assembly).  Output goes to oracle/_ref/ only.
+#   oracle/_ref/libcplx.so - the reference's OpenBLAS-style complex and 3M kernels
+#                         (four conjugation variants each) behind oracle/ref_cplx.c.
 # Usage: oracle/build.sh [reference-source-dir]
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -19,4 +21,25 @@ if [ -n "$REF" ] && [ -f "$REF/src/gemm_driver.c" ] && [ "$(uname -m)" = "x86_64
       "$REF/src/kernel/gemm_kernel.S" "$REF/src/gemm_driver.c" -o "$HERE/_ref/DGEMM.so" 2>/dev/null
   $cc -fopenmp --shared -fPIC -march=haswell -O2 \
       "$REF/src/kernel/gemm_kernel.S" "$REF/src/gemm_driver.c" -o "$HERE/_ref/SGEMM.so" 2>/dev/null
+fi
+CK="$REF/OpenBLAS-like_implementation"
+if [ -n "$REF" ] && [ -f "$CK/zgemm_kernel_4x2_haswell.c" ] && [ "$(uname -m)" = "x86_64" ]; then
+  # The kernels include OpenBLAS's common.h for BLASLONG only; a two-line
+  # stand-in under oracle/_ref/ provides it.  Variants by the kernels' own
+  # macros (zgemm_kernel_4x2_haswell.c:6-21).
+  mkdir -p "$HERE/_ref/include" "$HERE/_ref/obj"
+  printf '#include <stdint.h>\ntypedef long BLASLONG;\n' > "$HERE/_ref/include/common.h"
+  for v in NN RN NR RR; do
+    lc=$(echo "$v" | tr 'A-Z' 'a-z')
+    $cc -O2 -march=haswell -fPIC -c -D"$v" -DCNAME=ref_zgemm_kernel_"$lc" -I "$HERE/_ref/include" \
+        "$CK/zgemm_kernel_4x2_haswell.c" -o "$HERE/_ref/obj/z_$lc.o"
+    $cc -O2 -march=haswell -fPIC -c -D"$v" -DCNAME=ref_cgemm_kernel_"$lc" -I "$HERE/_ref/include" \
+        "$CK/cgemm_kernel_8x2_haswell.c" -o "$HERE/_ref/obj/c_$lc.o"
+  done
+  $cc -O2 -march=haswell -fPIC -c -DCNAME=ref_zgemm3m_kernel -I "$HERE/_ref/include" \
+      "$CK/zgemm3m_kernel_4x4_haswell.c" -o "$HERE/_ref/obj/z3m.o"
+  $cc -O2 -march=haswell -fPIC -c -DCNAME=ref_cgemm3m_kernel -I "$HERE/_ref/include" \
+      "$CK/cgemm3m_kernel_8x4_haswell.c" -o "$HERE/_ref/obj/c3m.o"
+  $cc -O2 -fopenmp -fPIC -shared -fvisibility=hidden -o "$HERE/_ref/libcplx.so" "$HERE/ref_cplx.c" \
+      "$HERE"/_ref/obj/z_*.o "$HERE"/_ref/obj/c_*.o "$HERE/_ref/obj/z3m.o" "$HERE/_ref/obj/c3m.o"
 fi

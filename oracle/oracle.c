@@ -45,6 +45,12 @@
  *  4. The exponent-spread generator a = (u - 0.5) * exp(phi * g), g ~ N(0,1)
  *     by Box-Muller from the same counter stream.
  *
+ *  5. orc_{z,c}gemm_dot2: the complex ground truth (trans N/T/C/R, complex
+ *     alpha and beta), full and sampled.
+ *
+ *  6. orc_{z,c}gemm_port: the arithmetic of the reference's complex kernels
+ *     in portable C (the CPU baseline where those x86-64 kernels cannot run).
+ *
  * Build with -ffp-contract=off (the recipe in oracle/build.sh does): every
  * rounding here is written out explicitly.
  */
@@ -312,6 +318,158 @@ ORC_API void orc_dot2gemm_sampled_s(char ta, char tb, int m, int n, int k, doubl
     out[q] = dot2_finish(s, err, alpha, beta, c ? (double)c[i + j * ldc] : 0.0);
   }
 }
+
+/* ------------------------------------------------------------------ */
+/* 5. complex ground truth                                             */
+/* ------------------------------------------------------------------ */
+/* Complex GEMM C = alpha*op(A)*op(B) + beta*C on interleaved (re, im) storage,
+ * the semantics of the reference's OpenBLAS-style complex kernels
+ * (OpenBLAS-like_implementation/zgemm_kernel_4x2_haswell.c:6-21: A_CONJ/B_CONJ
+ * per variant; :224-243 CNAME adds alpha*A*B to C) extended with the BLAS
+ * trans codes: 'N' op(X) = X, 'T' X^T, 'C' conj(X)^T, 'R' conj(X); any other
+ * character is a transpose, like the real path.  Real and imaginary parts are
+ * Dot2 sums of 2k exact products; alpha and beta are applied in double-double
+ * and rounded once. */
+static inline int ctrans(char t) { return !(t == 'N' || t == 'n' || t == 'R' || t == 'r'); }
+static inline int cconj(char t) { return t == 'C' || t == 'c' || t == 'R' || t == 'r'; }
+static inline void dd_acc(double *h, double *l, double x, double y) {
+  double p, e, q;
+  two_prod(x, y, &p, &e);
+  two_sum(*h, p, h, &q);
+  *l += q + e;
+}
+
+#define ORC_ZDOT2_ELEM(T)                                                                  \
+  double sr = 0.0, er = 0.0, si = 0.0, ei = 0.0;                                           \
+  for (int p = 0; p < k; p++) {                                                            \
+    const T *ap = ctrans(ta) ? a + 2 * (p + (int64_t)i * lda) : a + 2 * (i + (int64_t)p * lda); \
+    const T *bp = ctrans(tb) ? b + 2 * (j + (int64_t)p * ldb) : b + 2 * (p + (int64_t)j * ldb); \
+    const double ar = ap[0], ai = cconj(ta) ? -(double)ap[1] : (double)ap[1];            \
+    const double br = bp[0], bi = cconj(tb) ? -(double)bp[1] : (double)bp[1];            \
+    dd_acc(&sr, &er, ar, br);                                                              \
+    dd_acc(&sr, &er, -ai, bi);                                                             \
+    dd_acc(&si, &ei, ar, bi);                                                              \
+    dd_acc(&si, &ei, ai, br);                                                              \
+  }
+
+static inline void zdot2_finish(double sr, double er, double si, double ei, const double *alpha,
+                                const double *beta, double cr, double ci, double *out) {
+  double h = 0.0, l = 0.0;
+  dd_acc(&h, &l, alpha[0], sr);
+  l += alpha[0] * er;
+  dd_acc(&h, &l, -alpha[1], si);
+  l -= alpha[1] * ei;
+  dd_acc(&h, &l, beta[0], cr);
+  dd_acc(&h, &l, -beta[1], ci);
+  out[0] = h + l;
+  h = 0.0; l = 0.0;
+  dd_acc(&h, &l, alpha[0], si);
+  l += alpha[0] * ei;
+  dd_acc(&h, &l, alpha[1], sr);
+  l += alpha[1] * er;
+  dd_acc(&h, &l, beta[0], ci);
+  dd_acc(&h, &l, beta[1], cr);
+  out[1] = h + l;
+}
+
+/* out (complex, ld ldo) = alpha*op(A)op(B) + beta*C; c may be NULL (C = 0). */
+ORC_API void orc_zgemm_dot2(char ta, char tb, int m, int n, int k, const double *alpha,
+                            const double *a, int lda, const double *b, int ldb,
+                            const double *beta, const double *c, int ldc, double *out, int ldo) {
+#pragma omp parallel for schedule(dynamic, 1) collapse(2)
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < m; i++) {
+      ORC_ZDOT2_ELEM(double)
+      const double *cp = c ? c + 2 * (i + (int64_t)j * ldc) : NULL;
+      zdot2_finish(sr, er, si, ei, alpha, beta, cp ? cp[0] : 0.0, cp ? cp[1] : 0.0,
+                   out + 2 * (i + (int64_t)j * ldo));
+    }
+}
+ORC_API void orc_cgemm_dot2(char ta, char tb, int m, int n, int k, const double *alpha,
+                            const float *a, int lda, const float *b, int ldb, const double *beta,
+                            const float *c, int ldc, double *out, int ldo) {
+#pragma omp parallel for schedule(dynamic, 1) collapse(2)
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < m; i++) {
+      ORC_ZDOT2_ELEM(float)
+      const float *cp = c ? c + 2 * (i + (int64_t)j * ldc) : NULL;
+      zdot2_finish(sr, er, si, ei, alpha, beta, cp ? cp[0] : 0.0, cp ? cp[1] : 0.0,
+                   out + 2 * (i + (int64_t)j * ldo));
+    }
+}
+/* Sampled entries (rows[q], cols[q]) of the complex result, out[2q], out[2q+1]. */
+ORC_API void orc_zgemm_dot2_sampled(char ta, char tb, int k, const double *alpha, const double *a,
+                                    int lda, const double *b, int ldb, const double *beta,
+                                    const double *c, int ldc, const int64_t *rows,
+                                    const int64_t *cols, int64_t count, double *out) {
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t q = 0; q < count; q++) {
+    const int64_t i = rows[q], j = cols[q];
+    ORC_ZDOT2_ELEM(double)
+    const double *cp = c + 2 * (i + j * ldc);
+    zdot2_finish(sr, er, si, ei, alpha, beta, cp[0], cp[1], out + 2 * q);
+  }
+}
+ORC_API void orc_cgemm_dot2_sampled(char ta, char tb, int k, const double *alpha, const float *a,
+                                    int lda, const float *b, int ldb, const double *beta,
+                                    const float *c, int ldc, const int64_t *rows,
+                                    const int64_t *cols, int64_t count, double *out) {
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t q = 0; q < count; q++) {
+    const int64_t i = rows[q], j = cols[q];
+    ORC_ZDOT2_ELEM(float)
+    const float *cp = c + 2 * (i + j * ldc);
+    zdot2_finish(sr, er, si, ei, alpha, beta, cp[0], cp[1], out + 2 * q);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* 6. complex kernel arithmetic, portable (CPU baseline)               */
+/* ------------------------------------------------------------------ */
+/* The operation sequence of the reference's complex kernels in their
+ * expanded-accumulator form (OpenBLAS-like_implementation/
+ * zgemm_kernel_4x2_haswell.c:26-33 acc_m2n1_exp, :66-71 cont_expacc, :72-80
+ * save): per element four FMA chains over k, s1 = sum ar*br, s2 = sum ai*bi,
+ * s3 = sum ar*bi, s4 = sum ai*br (conjugation flips the sign of the imaginary
+ * part it applies to), combined as (s1 - s2, s3 + s4), then C += alpha * that.
+ * A is m x k, B k x n, complex column-major.  Used as the CPU baseline on hosts
+ * where the kernels themselves (x86-64 AVX2) cannot run; columns of C are
+ * split over the OpenMP team, rows are the vector dimension. */
+#define ORC_ZPORT(NAME, T, FMA)                                                            \
+  ORC_API void NAME(int conj_a, int conj_b, int m, int n, int k, const T *alpha, const T *a, \
+                    int lda, const T *b, int ldb, T *c, int ldc) {                         \
+    _Pragma("omp parallel")                                                                \
+    {                                                                                      \
+      T *acc = (T *)malloc(sizeof(T) * 4 * (size_t)(m > 0 ? m : 1));                      \
+      T *s1 = acc, *s2 = acc + m, *s3 = acc + 2 * m, *s4 = acc + 3 * m;                    \
+      const T sa = conj_a ? (T)-1 : (T)1, sb = conj_b ? (T)-1 : (T)1;                      \
+      _Pragma("omp for schedule(static)")                                                  \
+      for (int j = 0; j < n; j++) {                                                        \
+        for (int i = 0; i < m; i++) s1[i] = s2[i] = s3[i] = s4[i] = (T)0;                 \
+        for (int p = 0; p < k; p++) {                                                      \
+          const T br = b[2 * (p + (int64_t)j * ldb)];                                      \
+          const T bi = sb * b[2 * (p + (int64_t)j * ldb) + 1];                             \
+          const T *ap = a + 2 * (int64_t)p * lda;                                          \
+          for (int i = 0; i < m; i++) {                                                    \
+            const T ar = ap[2 * i], ai = sa * ap[2 * i + 1];                               \
+            s1[i] = FMA(ar, br, s1[i]);                                                    \
+            s2[i] = FMA(ai, bi, s2[i]);                                                    \
+            s3[i] = FMA(ar, bi, s3[i]);                                                    \
+            s4[i] = FMA(ai, br, s4[i]);                                                    \
+          }                                                                                \
+        }                                                                                  \
+        T *cp = c + 2 * (int64_t)j * ldc;                                                  \
+        for (int i = 0; i < m; i++) {                                                      \
+          const T re = s1[i] - s2[i], im = s3[i] + s4[i];                                  \
+          cp[2 * i] = FMA(alpha[0], re, FMA(-alpha[1], im, cp[2 * i]));                    \
+          cp[2 * i + 1] = FMA(alpha[0], im, FMA(alpha[1], re, cp[2 * i + 1]));             \
+        }                                                                                  \
+      }                                                                                    \
+      free(acc);                                                                           \
+    }                                                                                      \
+  }
+ORC_ZPORT(orc_zgemm_port, double, fma)
+ORC_ZPORT(orc_cgemm_port, float, fmaf)
 
 ORC_API int orc_max_threads(void) {
 #ifdef _OPENMP

@@ -24,7 +24,7 @@ def header_functions():
         if fn.endswith(".h"):
             src = open(os.path.join(ROOT, "include", fn)).read()
             src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-            names |= set(re.findall(r"\b((?:gb300_|[ds]gemm_)\w*)\s*\(", src))
+            names |= set(re.findall(r"\b((?:gb300_|[dszc]gemm(?:3m)?_)\w*)\s*\(", src))
     return names
 
 
@@ -37,13 +37,18 @@ def built():
 def test_dropin_exports_exactly_one_symbol():
     assert exported(os.path.join(g.PKG, "DGEMM.so")) == {"dgemm_"}
     assert exported(os.path.join(g.PKG, "SGEMM.so")) == {"sgemm_"}
+    # the complex libraries: the BLAS symbol and its 3M twin, nothing else
+    assert exported(os.path.join(g.PKG, "ZGEMM.so")) == {"zgemm_", "zgemm3m_"}
+    assert exported(os.path.join(g.PKG, "CGEMM.so")) == {"cgemm_", "cgemm3m_"}
 
 
 def test_core_exports_every_declared_function():
     decl = header_functions()
     assert {"dgemm_", "sgemm_", "gb300_dgemm", "gb300_sgemm"} <= decl
     core = exported(os.path.join(g.PKG, "libgemm_gb300.so"))
-    dropin = exported(os.path.join(g.PKG, "DGEMM.so")) | exported(os.path.join(g.PKG, "SGEMM.so"))
+    dropin = set()
+    for lib in ("DGEMM.so", "SGEMM.so", "ZGEMM.so", "CGEMM.so"):
+        dropin |= exported(os.path.join(g.PKG, lib))
     missing = {n for n in decl if n not in core and n not in dropin}
     assert not missing, missing
     # nothing but the declared ABI is exported from the core library
@@ -54,8 +59,8 @@ def test_core_exports_every_declared_function():
 
 def test_libraries_load_and_version():
     assert "sm_103a" in g.version()
-    g.dropin("d")
-    g.dropin("s")
+    for p in "dszc":
+        g.dropin(p)
 
 
 def test_argument_errors_need_no_gpu():
@@ -70,6 +75,39 @@ def test_argument_errors_need_no_gpu():
     assert g.dgemm_ozaki("N", "N", 8, 8, 8, 1.0, 0, 8, 0, 8, 0.0, 0, 8, slices=13) == g.ERR_ARG
     # empty problems are valid no-ops
     assert g.gemm_device("d", "N", "N", 0, 4, 4, 1.0, 0, 1, 0, 4, 0.0, 0, 1) == g.OK
+
+
+@pytest.mark.parametrize("p", ["z", "c"])
+def test_complex_argument_errors_need_no_gpu(p):
+    cd = g.complex_device
+    assert cd(p, "N", "N", -1, 4, 4, 1, 0, 4, 0, 4, 0, 0, 4) == g.ERR_ARG
+    assert cd(p, "N", "N", 8, 4, 4, 1, 0, 7, 0, 4, 0, 0, 8) == g.ERR_ARG       # lda < m
+    assert cd(p, "C", "N", 8, 4, 4, 1, 0, 3, 0, 4, 0, 0, 8) == g.ERR_ARG       # lda < k
+    assert cd(p, "R", "N", 8, 4, 4, 1, 0, 7, 0, 4, 0, 0, 8) == g.ERR_ARG       # 'R' keeps m rows
+    assert cd(p, "N", "C", 8, 4, 4, 1, 0, 8, 0, 3, 0, 0, 8) == g.ERR_ARG       # ldb < n
+    assert cd(p, "N", "N", 8, 4, 4, 1, 0, 8, 0, 4, 0, 0, 7) == g.ERR_ARG       # ldc < m
+    assert cd(p, "N", "N", 8, 4, 4, 1, 0, 8, 0, 4, 0, 0, 8, method=3) == g.ERR_ARG
+    bad = 5 if p == "c" else 13
+    assert cd(p, "N", "N", 8, 4, 4, 1, 0, 8, 0, 4, 0, 0, 8, method=g.CPLX_SPLIT,
+              param=bad) == g.ERR_ARG
+    assert g.host_complex(p, "N", "N", 8, 4, 4, 1, None, 7, None, 4, 0, None, 8) == g.ERR_ARG
+    assert cd(p, "N", "N", 0, 4, 4, 1, 0, 1, 0, 4, 0, 0, 1) == g.OK
+
+
+def test_complex_workspace_sizes():
+    m, n, k = 300, 200, 100
+    for p, e in (("z", 8), ("c", 4)):
+        w4 = g.complex_workspace_bytes(p, g.CPLX_4M, "N", m, n, k)
+        assert w4 >= 2 * m * 2 * k * e                       # the embedded op(A)
+        if p == "z":   # B is used in place when transb is 'N'
+            assert g.complex_workspace_bytes(p, g.CPLX_4M, "T", m, n, k) >= w4 + 2 * k * n * e
+        else:          # FP32 4M always stores op(B) transposed (MN-major for the FFMA kernel)
+            assert w4 >= (2 * m + n) * 2 * k * e
+        w3 = g.complex_workspace_bytes(p, g.CPLX_3M, "N", m, n, k)
+        assert w3 >= 3 * (m * k + k * n + m * n) * e
+        ws = g.complex_workspace_bytes(p, g.CPLX_SPLIT, "N", m, n, k, 8 if p == "z" else 6)
+        assert ws > w4
+        assert g.complex_workspace_bytes(p, g.CPLX_4M, "N", 0, n, k) == 0
 
 
 def test_workspace_sizes():
@@ -91,6 +129,12 @@ def test_dropin_invalid_args_leave_c_untouched():
     assert np.array_equal(c, before)
     g.dgemm("N", "N", 3, -4, 3, 1.0, a, 3, a, 3, 0.0, c, 3)
     assert np.array_equal(c, before)
+    z = (np.arange(12) + 1j).reshape(3, 4, order="F").astype(np.complex128, order="F")
+    zb = z.copy()
+    za = np.ones((3, 3), np.complex128, order="F")
+    g.zgemm("N", "N", 3, 4, 3, 1.0, za, 2, za, 3, 0.0, z, 3)   # lda < m
+    g.zgemm("C", "N", 3, 4, 3, 1.0, za, 3, za, 3, 0.0, z, 2, method3m=True)  # ldc < m
+    assert np.array_equal(z, zb)
 
 
 def test_grouped_problem_struct_layout_and_args():

@@ -59,3 +59,43 @@ def check_close(got, want, bound):
     assert not bad.any(), "max excess %g at %s (got %r want %r bound %r)" % (
         float((diff - bound).max()), np.argwhere(bad)[0], got[bad][0], want[bad][0],
         bound[bad][0] if np.ndim(bound) else bound)
+
+
+# ---------------------------------------------------------------- complex
+def ctrans(t) -> bool:
+    """Complex trans codes: 'N'/'R' keep the shape, anything else transposes."""
+    return t not in "NnRr"
+
+
+def cop(X, trans, rows, cols):
+    """op(X) as a complex128 (rows x cols) array: 'N' X, 'R' conj(X), 'T' X^T,
+    'C' conj(X)^T."""
+    if rows == 0 or cols == 0:
+        return np.zeros((rows, cols), np.complex128)
+    Y = X[:cols, :rows].T if ctrans(trans) else X[:rows, :cols]
+    Y = Y.astype(np.complex128)
+    return np.conj(Y) if trans in "CcRr" else Y
+
+
+def l1(z):
+    """|re| + |im| elementwise (bounds both parts of a complex product sum)."""
+    z = np.asarray(z)
+    return np.abs(z.real) + np.abs(z.imag)
+
+
+def cgemm_bound(Aop, Bop, C, alpha, beta, k, u, factor=1.0):
+    """Elementwise bound on |got - exact| for alpha*Aop@Bop + beta*C computed in
+    unit roundoff u: each part is a dot of 2k products plus the alpha/beta
+    update, so (2k + 8) u (|alpha| |A||B| + |beta| |C|) with l1 moduli."""
+    mag = l1(complex(alpha)) * (l1(Aop) @ l1(Bop))
+    if C is not None:
+        mag = mag + l1(complex(beta)) * l1(C)
+    return factor * (2 * k + 8) * u * mag + np.finfo(np.float64).tiny
+
+
+def check_close_c(got, want, bound):
+    """Real and imaginary parts of got within `bound` of want, elementwise."""
+    dr = np.abs(np.asarray(got, np.complex128).real - want.real)
+    di = np.abs(np.asarray(got, np.complex128).imag - want.imag)
+    bad = (dr > bound) | (di > bound)
+    assert not bad.any(), (int(bad.sum()), float(np.max(dr - bound)), float(np.max(di - bound)))
