@@ -129,6 +129,11 @@ def core() -> ctypes.CDLL:
         L.gb300_grouped_graph_destroy.argtypes = [c_void_p]
         L.gb300_sgemm_bf16x_noalloc.argtypes = g + [c_float, c_void_p, c_int, c_void_p, c_int,
                                                     c_float, c_void_p, c_int, c_int, c_void_p]
+        L.gb300_dgemm_ozaki2.argtypes = g + [c_double, c_void_p, c_int, c_void_p, c_int,
+                                             c_double, c_void_p, c_int, c_int, c_void_p, c_size_t,
+                                             c_void_p]
+        L.gb300_host_dgemm_ozaki2.argtypes = g + [c_double, c_void_p, c_int, c_void_p, c_int,
+                                                  c_double, c_void_p, c_int, c_int]
         cg = [c_char, c_char, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int,
               c_void_p, c_void_p, c_int, c_int, c_int]
         L.gb300_cgemm.argtypes = cg + [c_void_p, c_size_t, c_void_p]
@@ -274,6 +279,15 @@ def dgemm_ozaki(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, sl
                                   workspace_bytes, c_void_p(stream))
 
 
+def dgemm_ozaki2(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, moduli=0,
+                 stream=0, workspace=None, workspace_bytes=0) -> int:
+    """CRT (modular-integer) DGEMM on the tensor cores: the exact integer product
+    of b-bit scaled operands from `moduli` residue GEMMs (0 = 16)."""
+    return core().gb300_dgemm_ozaki2(_b(transa), _b(transb), m, n, k, alpha, _ptr(A), lda,
+                                     _ptr(B), ldb, beta, _ptr(C), ldc, moduli, _ptr(workspace),
+                                     workspace_bytes, c_void_p(stream))
+
+
 def sgemm_bf16x_noalloc(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
                         products=3, stream=0) -> int:
     """BF16xP split SGEMM whose scratch is the library's fixed 32 MiB device array
@@ -304,9 +318,10 @@ def split_run(form, m, n, k, alpha, beta, C, ldc, param, workspace, workspace_by
 
 def host_split_gemm(form, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
                     param) -> int:
-    """Host-pointer split forms (synchronous, staged through HBM)."""
+    """Host-pointer split forms ("bf16x", "ozaki" slices, "crt"; synchronous)."""
     L = core()
-    f = L.gb300_host_sgemm_bf16x if form == "bf16x" else L.gb300_host_dgemm_ozaki
+    f = {"bf16x": L.gb300_host_sgemm_bf16x, "ozaki": L.gb300_host_dgemm_ozaki,
+         "crt": L.gb300_host_dgemm_ozaki2}[form]
     return f(_b(transa), _b(transb), m, n, k, alpha, _ptr(a), lda, _ptr(b), ldb, beta, _ptr(c),
              ldc, param)
 
@@ -474,5 +489,5 @@ CORE_SYMBOLS = [
     "gb300_tune_cache_clear", "gb300_dtrsm", "gb300_strsm", "gb300_dtrmm", "gb300_strmm",
     "gb300_grouped_graph_create", "gb300_grouped_graph_launch", "gb300_grouped_graph_destroy",
     "gb300_cgemm", "gb300_zgemm", "gb300_host_cgemm", "gb300_host_zgemm",
-    "gb300_complex_workspace_bytes",
+    "gb300_complex_workspace_bytes", "gb300_dgemm_ozaki2", "gb300_host_dgemm_ozaki2",
 ]

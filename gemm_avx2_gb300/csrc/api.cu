@@ -145,7 +145,7 @@ static bool host_direct_ok(const void *a, const void *b, const void *c) {
 }
 
 // form: 0 = plain kernel; 1 = BF16xP split (FP32, param = products);
-//       2 = Ozaki (FP64, param = slices).
+//       2 = Ozaki slices (FP64, param = slices); 3 = CRT (FP64, param = moduli).
 template <typename T>
 static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a, int lda,
                      const T *b, int ldb, T beta, T *c, int ldc, int form = 0, int param = 0) {
@@ -167,13 +167,15 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
     // Split forms read A and B once (split / slice kernels, plain loads) and
     // read and write each C element once (GEMM epilogue): they run directly on
     // the caller's host memory over the coherent CPU-GPU link, no staging.
-    const size_t wneed = need_ab ? split_workspace_bytes(form == 1 ? 0 : 1, m, n, k, param) : 0;
+    const size_t wneed = need_ab ? split_workspace_bytes(form - 1, m, n, k, param) : 0;
     void *ws = wneed ? cached_workspace(s, st, wneed) : nullptr;
     if (wneed && !ws) return GB300_ERR_NOMEM;
     int rc;
     if constexpr (sizeof(T) == 8)
-      rc = ozaki_dgemm(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, param, ws, wneed, st,
-                       s->err);
+      rc = form == 3 ? crt_dgemm(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, param, ws,
+                                 wneed, st, s->err)
+                     : ozaki_dgemm(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, param,
+                                   ws, wneed, st, s->err);
     else
       rc = split_sgemm(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, param, ws, wneed, st,
                        s->err);
@@ -213,11 +215,13 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
   int rc;
   const int dlda = need_ab ? dla : up(arows), dldb = need_ab ? dlb : up(brows);
   if (form != 0 && need_ab) {
-    const size_t wneed = split_workspace_bytes(form == 1 ? 0 : 1, m, n, k, param);
+    const size_t wneed = split_workspace_bytes(form - 1, m, n, k, param);
     void *ws = wneed ? cached_workspace(s, st, wneed) : nullptr;
     if (!ws) return GB300_ERR_NOMEM;
     if constexpr (sizeof(T) == 8)
-      rc = ozaki_dgemm(ta, tb, m, n, k, alpha, dA, dlda, dB, dldb, beta, dC, dlc, param, ws,
+      rc = form == 3 ? crt_dgemm(ta, tb, m, n, k, alpha, dA, dlda, dB, dldb, beta, dC, dlc, param,
+                                 ws, wneed, st, s->err)
+                     : ozaki_dgemm(ta, tb, m, n, k, alpha, dA, dlda, dB, dldb, beta, dC, dlc, param, ws,
                        wneed, st, s->err);
     else
       rc = split_sgemm(ta, tb, m, n, k, alpha, dA, dlda, dB, dldb, beta, dC, dlc, param, ws,
@@ -369,6 +373,37 @@ GB300_API int gb300_host_dgemm_ozaki(char ta, char tb, int m, int n, int k, doub
   if (slices != 0 && (slices < 2 || slices > kOzakiMaxSlices)) return GB300_ERR_ARG;
   return host_gemm<double>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, 2,
                            slices > 0 ? slices : ozaki_default_slices(m, n, k));
+}
+
+GB300_API int gb300_host_dgemm_ozaki2(char ta, char tb, int m, int n, int k, double alpha,
+                                      const double *a, int lda, const double *b, int ldb,
+                                      double beta, double *c, int ldc, int moduli) {
+  if (moduli != 0 && (moduli < 2 || moduli > kCrtMaxModuli)) return GB300_ERR_ARG;
+  return host_gemm<double>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, 3, moduli);
+}
+
+GB300_API int gb300_dgemm_ozaki2(char ta, char tb, int m, int n, int k, double alpha,
+                                 const double *A, int lda, const double *B, int ldb, double beta,
+                                 double *C, int ldc, int moduli, void *ws, size_t ws_bytes,
+                                 void *stream) {
+  if (moduli != 0 && (moduli < 2 || moduli > kCrtMaxModuli)) return GB300_ERR_ARG;
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (ws) {
+    unsigned *err = device_error_word();
+    if (!err) return GB300_ERR_CUDA;
+    return crt_dgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, moduli, ws, ws_bytes,
+                     st, err);
+  }
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  const size_t need = (alpha != 0.0 && k > 0) ? crt_workspace_bytes(m, n, k, moduli) : 0;
+  std::lock_guard<std::mutex> lk(s->mu);
+  void *w = need ? cached_workspace(s, st, need) : nullptr;
+  if (need && !w) return GB300_ERR_NOMEM;
+  return crt_dgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, moduli, w, need, st,
+                   s->err);
 }
 
 GB300_API int gb300_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A,

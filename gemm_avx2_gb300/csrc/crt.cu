@@ -1,0 +1,490 @@
+// crt.cu -- the CRT (modular-integer) form of the FP64 GEMM on the BF16 tensor
+// pipe: a tensor-core form of the reference's dgemm_ (wjc404/GEMM_AVX2
+// src/gemm_driver.c:118; same operand semantics), after the published Ozaki
+// scheme II (Ozaki, Uchino & Imamura 2025).
+//
+//   1. Rows of op(A) and columns of op(B) are scaled by powers of two and
+//      truncated to integers of at most b bits: A'_ik = trunc(a_ik 2^(b-E_i)).
+//   2. Their symmetric residues modulo N pairwise coprime odd moduli <= 255
+//      (|r| <= 127: exact in BF16, products < 2^14 exact in FP32) are written
+//      as N K-major BF16 blocks (crt_residue_kernel).
+//   3. One exact integer GEMM per modulus on tcgen05 (the slice GEMM of
+//      tc_gemm.cu in its CRT mode) gives P = A'B' mod p_i for every i.
+//   4. crt_reconstruct_kernel rebuilds P in (-M/2, M/2), M = p_1 ... p_N, with
+//      192-bit integer arithmetic (X = sum r_i w_i, then X mod M), converts it
+//      to FP64 with one rounding and scales by 2^(E_i + F_j - 2b).
+//   b is the largest integer with 2 k (2^b - 1)^2 < M.  The only errors are
+//   the truncations of step 1 (b bits relative to the row / column maximum);
+//   N moduli cost N tensor GEMMs where the slice form needs S(S+1)/2 for
+//   about 7S bits.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "plain_gemm.h"
+#include "split_gemm.h"
+#include "split_tiles.cuh"
+
+namespace gb300 {
+
+namespace {
+
+// pairwise coprime, odd, <= 255 (255 = 3*5*17, 253 = 11*23, 247 = 13*19,
+// 217 = 7*31, the rest prime)
+constexpr int kModuli[kCrtMaxModuli] = {255, 253, 251, 247, 241, 239, 233, 229,
+                                        227, 223, 217, 211, 199, 197, 193, 191,
+                                        181, 179, 173, 167, 163, 157, 151, 149};
+constexpr int kCrtDefaultModuli = 16;
+
+// ------------------------------------------------------------------ residues
+struct CrtModParams {
+  int N, b;
+  unsigned p[kCrtMaxModuli];
+  unsigned mg[kCrtMaxModuli];    // floor(2^32 / p)
+  unsigned pw32[kCrtMaxModuli];  // 2^32 mod p
+};
+
+// x mod p for x < 2^32 (Barrett with mg = floor(2^32/p): q is the quotient or
+// one less, so one correction suffices).
+__device__ __forceinline__ unsigned mod32(unsigned x, unsigned p, unsigned mg) {
+  const unsigned q = __umulhi(x, mg);
+  const unsigned r = x - q * p;
+  return r >= p ? r - p : r;
+}
+__device__ __forceinline__ unsigned mod64(unsigned long long x, unsigned p, unsigned mg,
+                                          unsigned pw32) {
+  const unsigned h = mod32((unsigned)(x >> 32), p, mg), l = mod32((unsigned)x, p, mg);
+  return mod32(h * pw32 + l, p, mg);  // < 255 * 255 + 255
+}
+// 2^t mod p, t >= 0
+__device__ __forceinline__ unsigned pow2mod(int t, unsigned p, unsigned mg, unsigned pw32) {
+  unsigned r = mod32(1u << (t & 31), p, mg);
+  for (int q = t >> 5; q > 0; --q) r = mod32(r * pw32, p, mg);
+  return r;
+}
+
+// Symmetric residues of A' = trunc(x 2^(b - e)) for N moduli, 8 consecutive k
+// of one row per thread, as BF16, block i at dst[i * step] (uint4 units).
+// |x| = M 2^base with M the 53-bit significand, so |x| 2^(b-e) = M 2^t,
+// t = b - e + base: a right shift truncates, a left shift is exact (and
+// reduced through 2^t mod p when M 2^t would not fit 64 bits).
+__global__ void __launch_bounds__(256)
+    crt_residue_kernel(const double *__restrict__ X, int ld, int R, int K, int kcontig, int Rp,
+                       int Kp, const int *__restrict__ ex, CrtModParams mp,
+                       __nv_bfloat16 *__restrict__ out) {
+  __shared__ double tile[32][65];
+  const int k0 = blockIdx.x * 64;
+  const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
+  const int64_t step = (int64_t)Rp * Kp / 8;
+  for (int r0 = blockIdx.y * 32; r0 < Rp; r0 += gridDim.y * 32) {
+    load_tile_32x64<double>(X, ld, R, K, kcontig != 0, r0, k0, tile);
+    __syncthreads();
+    const int gr = r0 + r;
+    const int e = (gr < R) ? ex[gr] : 0;
+    const bool bad = (e == kNonFiniteExp);  // row of Inf/NaN: zeros, the result is NaN
+    uint4 *dst = reinterpret_cast<uint4 *>(out + (int64_t)gr * Kp + k0 + kq);
+    unsigned long long mag[8];
+    int sh[8];
+    unsigned neg = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const unsigned long long u = (unsigned long long)__double_as_longlong(tile[r][kq + j]);
+      const int be = (int)((u >> 52) & 0x7ff);
+      mag[j] = bad ? 0ull : ((u & 0xfffffffffffffull) | (be ? (1ull << 52) : 0ull));
+      sh[j] = mp.b - e + ((be ? be : 1) - 1075);
+      neg |= (unsigned)(u >> 63) << j;
+    }
+    for (int i = 0; i < mp.N; ++i) {
+      const unsigned p = mp.p[i], mg = mp.mg[i], pw = mp.pw32[i];
+      unsigned w[4];
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        unsigned h[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int t = sh[j + q];
+          const unsigned long long M = mag[j + q];
+          unsigned rr;
+          if (t < 0)
+            rr = (t <= -64) ? 0u : mod64(M >> (-t), p, mg, pw);
+          else if (t <= 10)
+            rr = mod64(M << t, p, mg, pw);
+          else
+            rr = mod32(mod64(M, p, mg, pw) * pow2mod(t, p, mg, pw), p, mg);
+          if (((neg >> (j + q)) & 1) && rr) rr = p - rr;
+          const int sres = rr > (p >> 1) ? (int)rr - (int)p : (int)rr;
+          h[q] = __float_as_uint((float)sres) >> 16;  // |sres| <= 127: exact in BF16
+        }
+        w[j / 2] = h[0] | (h[1] << 16);
+      }
+      dst[i * step] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    __syncthreads();  // the tile is refilled for the next row block
+  }
+}
+
+// ------------------------------------------------------------- reconstruction
+struct CrtRecParams {
+  int N, m, n, Mp, Np, two_b;
+  int topshift;    // bitlength(M) - 40
+  float inv_mt;    // 1 / (M >> topshift)
+  unsigned long long w[kCrtMaxModuli][3];  // CRT weights, 192-bit little-endian limbs
+  unsigned long long M[3], half[3];        // M and (M - 1) / 2
+  double alpha, beta;
+  double *C;
+  int ldc;
+};
+
+// 64 bits of a 4-limb number starting at bit s (s < 192)
+__device__ __forceinline__ unsigned long long bits64(const unsigned long long (&x)[4], int s) {
+  const int l = s >> 6, o = s & 63;
+  const unsigned long long lo = x[l], hi = x[l + 1];
+  return o ? (lo >> o) | (hi << (64 - o)) : lo;
+}
+
+__global__ void __launch_bounds__(256)
+    crt_reconstruct_kernel(const uint8_t *__restrict__ rres, const int *__restrict__ expA,
+                           const int *__restrict__ expB, CrtRecParams rp) {
+  const int64_t plane = (int64_t)rp.Mp * rp.Np;
+  for (int j = blockIdx.y; j < rp.n; j += gridDim.y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rp.m) continue;
+    // X = sum r_g w_g (< 2^13 M: four limbs)
+    unsigned long long X[4] = {0ull, 0ull, 0ull, 0ull};
+    const uint8_t *src = rres + (int64_t)j * rp.Mp + i;
+    for (int g = 0; g < rp.N; ++g) {
+      const unsigned long long r = src[g * plane];
+      unsigned long long carry = 0;
+#pragma unroll
+      for (int l = 0; l < 3; ++l) {
+        const unsigned long long lo = r * rp.w[g][l], hi = __umul64hi(r, rp.w[g][l]);
+        unsigned long long s = X[l] + lo;
+        unsigned long long c = s < lo;
+        s += carry;
+        c += s < carry;
+        X[l] = s;
+        carry = hi + c;
+      }
+      X[3] += carry;
+    }
+    // P = X - q M with q = floor(X / M) estimated from the top bits, then corrected
+    const unsigned long long xt = bits64(X, rp.topshift);  // < 2^53
+    unsigned long long q = (unsigned long long)((float)xt * rp.inv_mt);
+    unsigned long long P[4];
+    {
+      unsigned long long borrow = 0, carry = 0;
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const unsigned long long ml = l < 3 ? rp.M[l] : 0ull;
+        const unsigned long long lo = q * ml, hi = __umul64hi(q, ml);
+        unsigned long long qm = lo + carry;
+        carry = hi + (qm < lo);
+        const unsigned long long d = X[l] - qm;
+        const unsigned long long b1 = X[l] < qm;
+        const unsigned long long d2 = d - borrow;
+        const unsigned long long b2 = d < borrow;
+        P[l] = d2;
+        borrow = b1 | b2;
+      }
+    }
+    // P is X - q M in two's complement: add M while negative, subtract while >= M
+    for (int it = 0; it < 3 && (long long)P[3] < 0; ++it) {
+      unsigned long long c = 0;
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const unsigned long long ml = l < 3 ? rp.M[l] : 0ull;
+        const unsigned long long s = P[l] + ml;
+        const unsigned long long c1 = s < ml;
+        P[l] = s + c;
+        c = c1 | (P[l] < c);
+      }
+    }
+    auto ge = [&](const unsigned long long(&a)[4], const unsigned long long(&b)[3]) {
+      if (a[3]) return true;
+      for (int l = 2; l >= 0; --l)
+        if (a[l] != b[l]) return a[l] > b[l];
+      return true;
+    };
+    for (int it = 0; it < 3 && ge(P, rp.M); ++it) {
+      unsigned long long bo = 0;
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const unsigned long long ml = l < 3 ? rp.M[l] : 0ull;
+        const unsigned long long d = P[l] - ml;
+        const unsigned long long b1 = P[l] < ml;
+        P[l] = d - bo;
+        bo = b1 | (d < bo);
+      }
+    }
+    // symmetric: P > (M - 1) / 2 stands for P - M
+    bool neg = false;
+    unsigned long long mg[3] = {P[0], P[1], P[2]};
+    {
+      bool gt = false;
+      for (int l = 2; l >= 0; --l)
+        if (P[l] != rp.half[l]) { gt = P[l] > rp.half[l]; break; }
+      if (gt) {  // magnitude M - P
+        neg = true;
+        unsigned long long bo = 0;
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          const unsigned long long d = rp.M[l] - P[l];
+          const unsigned long long b1 = rp.M[l] < P[l];
+          mg[l] = d - bo;
+          bo = b1 | (d < bo);
+        }
+      }
+    }
+    // magnitude -> FP64 with one rounding: the top 64 bits, the rest as a sticky bit
+    unsigned long long top;
+    int pos;
+    if (mg[2]) {
+      const int lz = __clzll((long long)mg[2]);
+      top = (mg[2] << lz) | (lz ? mg[1] >> (64 - lz) : 0ull);
+      const unsigned long long rest = (lz ? mg[1] << lz : 0ull) | (lz ? 0ull : mg[1]) | mg[0];
+      if (rest) top |= 1ull;
+      pos = 128 - lz;
+    } else if (mg[1]) {
+      const int lz = __clzll((long long)mg[1]);
+      top = (mg[1] << lz) | (lz ? mg[0] >> (64 - lz) : 0ull);
+      const unsigned long long rest = lz ? mg[0] << lz : mg[0];
+      if (rest) top |= 1ull;
+      pos = 64 - lz;
+    } else {
+      top = mg[0];
+      pos = 0;
+    }
+    const int ea = expA[i], eb = expB[j];
+    double v;
+    if (ea == kNonFiniteExp || eb == kNonFiniteExp) {
+      v = __longlong_as_double(0x7ff8000000000000LL);
+    } else {
+      v = scale_pow2(__ull2double_rn(top), pos + ea + eb - rp.two_b);
+      if (neg) v = -v;
+    }
+    double *c = rp.C + (int64_t)j * rp.ldc + i;
+    const double cb = (rp.beta == 1.0) ? *c : *c * rp.beta;
+    *c = cb + rp.alpha * v;
+  }
+}
+
+// ------------------------------------------------------------------ host side
+// Small fixed-width unsigned integers for the CRT constants (5 x 64 bits).
+struct Big {
+  uint64_t l[5] = {0, 0, 0, 0, 0};
+};
+Big big_from(uint64_t v) {
+  Big b;
+  b.l[0] = v;
+  return b;
+}
+Big big_mul(const Big &a, uint64_t s) {
+  Big r;
+  unsigned __int128 c = 0;
+  for (int i = 0; i < 5; ++i) {
+    const unsigned __int128 t = (unsigned __int128)a.l[i] * s + c;
+    r.l[i] = (uint64_t)t;
+    c = t >> 64;
+  }
+  return r;
+}
+uint64_t big_divmod(Big &a, uint64_t d) {  // a /= d, returns the remainder
+  unsigned __int128 rem = 0;
+  for (int i = 4; i >= 0; --i) {
+    const unsigned __int128 cur = (rem << 64) | a.l[i];
+    a.l[i] = (uint64_t)(cur / d);
+    rem = cur % d;
+  }
+  return (uint64_t)rem;
+}
+int big_cmp(const Big &a, const Big &b) {
+  for (int i = 4; i >= 0; --i)
+    if (a.l[i] != b.l[i]) return a.l[i] < b.l[i] ? -1 : 1;
+  return 0;
+}
+Big big_sub(const Big &a, const Big &b) {
+  Big r;
+  uint64_t bo = 0;
+  for (int i = 0; i < 5; ++i) {
+    const uint64_t d = a.l[i] - b.l[i];
+    const uint64_t b1 = a.l[i] < b.l[i];
+    r.l[i] = d - bo;
+    bo = b1 | (d < bo);
+  }
+  return r;
+}
+Big big_shl(const Big &a, int s) {
+  Big r;
+  const int w = s / 64, o = s % 64;
+  for (int i = 4; i >= 0; --i) {
+    uint64_t v = 0;
+    if (i - w >= 0) v = a.l[i - w] << o;
+    if (o && i - w - 1 >= 0) v |= a.l[i - w - 1] >> (64 - o);
+    r.l[i] = v;
+  }
+  return r;
+}
+int big_bitlength(const Big &a) {
+  for (int i = 4; i >= 0; --i)
+    if (a.l[i]) return 64 * i + 64 - __builtin_clzll(a.l[i]);
+  return 0;
+}
+Big modulus_product(int N) {
+  Big M = big_from(1);
+  for (int i = 0; i < N; ++i) M = big_mul(M, (uint64_t)kModuli[i]);
+  return M;
+}
+int64_t inv_mod(int64_t a, int64_t p) {  // a^-1 mod p, gcd(a, p) = 1
+  int64_t t = 0, nt = 1, r = p, nr = a % p;
+  while (nr) {
+    const int64_t q = r / nr;
+    int64_t tmp = t - q * nt;
+    t = nt;
+    nt = tmp;
+    tmp = r - q * nr;
+    r = nr;
+    nr = tmp;
+  }
+  return t < 0 ? t + p : t;
+}
+
+struct CrtLayout {
+  int64_t Kp, Mp, Np;
+  __nv_bfloat16 *As, *Bs;
+  unsigned long long *amax;
+  int *ex;
+  uint8_t *rres;
+};
+CrtLayout crt_layout(int m, int n, int k, int N, void *ws) {
+  CrtLayout L;
+  L.Kp = (k + kSplitBK - 1) / kSplitBK * kSplitBK;
+  L.Mp = (m + kSplitBM - 1) / kSplitBM * kSplitBM;
+  L.Np = (n + kOzakiBN - 1) / kOzakiBN * kOzakiBN;
+  uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(ws) + 1023) &
+                                              ~uintptr_t(1023));
+  L.As = reinterpret_cast<__nv_bfloat16 *>(base);
+  L.Bs = L.As + N * L.Mp * L.Kp;
+  L.amax = reinterpret_cast<unsigned long long *>(L.Bs + N * L.Np * L.Kp);
+  L.ex = reinterpret_cast<int *>(L.amax + L.Mp + L.Np);
+  L.rres = reinterpret_cast<uint8_t *>(
+      (reinterpret_cast<uintptr_t>(L.ex + L.Mp + L.Np) + 255) & ~uintptr_t(255));
+  return L;
+}
+
+int resolve_moduli(int moduli) { return moduli > 0 ? moduli : kCrtDefaultModuli; }
+
+}  // namespace
+
+int crt_bits_for(int moduli, int k) {
+  const int N = resolve_moduli(moduli);
+  if (N < 1 || N > kCrtMaxModuli) return 0;
+  const Big M = modulus_product(N);  // < 2^188
+  const uint64_t twok = 2 * (uint64_t)(k > 1 ? k : 1);
+  int b = 0;
+  while (b < 120) {  // largest b with 2 k (2^b - 1)^2 < M
+    const int nb = b + 1;
+    // (2^nb - 1)^2 = 2^(2 nb) - 2^(nb + 1) + 1, at most 2^240: 2k times it fits 320 bits
+    Big sq = big_sub(big_shl(big_from(1), 2 * nb), big_shl(big_from(1), nb + 1));
+    uint64_t c = 1;
+    for (int i = 0; i < 5 && c; ++i) {
+      sq.l[i] += c;
+      c = sq.l[i] == 0;
+    }
+    if (big_cmp(big_mul(sq, twok), M) >= 0) break;
+    b = nb;
+  }
+  return b;
+}
+
+size_t crt_workspace_bytes(int m, int n, int k, int moduli) {
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  const int N = resolve_moduli(moduli);
+  if (N < 2 || N > kCrtMaxModuli) return 0;
+  const int64_t Kp = (k + kSplitBK - 1) / kSplitBK * kSplitBK;
+  const int64_t Mp = (m + kSplitBM - 1) / kSplitBM * kSplitBM;
+  const int64_t Np = (n + kOzakiBN - 1) / kOzakiBN * kOzakiBN;
+  return (size_t)((Mp + Np) * N * Kp * 2 + (Mp + Np) * 12 + N * Mp * Np + 2048);
+}
+
+int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+              const double *B, int ldb, double beta, double *C, int ldc, int moduli, void *ws,
+              size_t ws_bytes, cudaStream_t st, unsigned *err) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  const int N = resolve_moduli(moduli);
+  if (N < 2 || N > kCrtMaxModuli) return GB300_ERR_ARG;
+  if (alpha == 0.0 || k == 0)
+    return plain_dgemm('N', 'N', m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc,
+                       st, err);
+  const int b = crt_bits_for(N, k);
+  if (b < 1) return GB300_ERR_ARG;  // too few moduli for this k
+  const size_t need = crt_workspace_bytes(m, n, k, N);
+  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
+  const CrtLayout L = crt_layout(m, n, k, N, ws);
+  if (N * L.Mp > 0x7fffffff || N * L.Np > 0x7fffffff || L.Kp > 0x7fffffff) return GB300_ERR_ARG;
+  // 1. scale exponents of the rows of op(A) and columns of op(B)
+  int rc = row_scale_exponents(ta, tb, m, n, k, A, lda, B, ldb, L.amax, L.ex, L.Mp, L.Np, st);
+  if (rc != GB300_OK) return rc;
+  // 2. residues
+  CrtModParams mp;
+  mp.N = N;
+  mp.b = b;
+  for (int i = 0; i < kCrtMaxModuli; ++i) {
+    const unsigned p = (unsigned)kModuli[i];
+    mp.p[i] = p;
+    mp.mg[i] = (unsigned)((1ull << 32) / p);
+    mp.pw32[i] = (unsigned)((1ull << 32) % p);
+  }
+  auto row_blocks = [](int64_t Rp) { return (unsigned)(Rp / 32 < 65535 ? Rp / 32 : 65535); };
+  const bool an = notrans(ta), bn = notrans(tb);
+  crt_residue_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Mp)), 256, 0, st>>>(
+      A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, L.ex, mp, L.As);
+  crt_residue_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Np)), 256, 0, st>>>(
+      B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, L.ex + L.Mp, mp, L.Bs);
+  if (cudaGetLastError() != cudaSuccess) return GB300_ERR_CUDA;
+  // 3. one exact integer GEMM per modulus
+  OzakiGemmArgs a;
+  a.m = m; a.n = n; a.S = N; a.mode = 1;
+  a.Mp = L.Mp; a.Np = L.Np; a.Kp = L.Kp;
+  a.As = L.As; a.Bs = L.Bs;
+  a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc;
+  a.expA = L.ex; a.expB = L.ex + L.Mp; a.res = nullptr; a.rres = L.rres; a.mods = kModuli;
+  rc = ozaki_gemm_launch(a, st, err);
+  if (rc != GB300_OK) return rc;
+  // 4. reconstruction and the C update
+  CrtRecParams rp;
+  std::memset(&rp, 0, sizeof(rp));
+  rp.N = N; rp.m = m; rp.n = n; rp.Mp = (int)L.Mp; rp.Np = (int)L.Np; rp.two_b = 2 * b;
+  const Big M = modulus_product(N);
+  for (int g = 0; g < N; ++g) {
+    Big Mi = M;
+    const uint64_t pg = (uint64_t)kModuli[g];
+    big_divmod(Mi, pg);
+    Big t = Mi;
+    const uint64_t mi_mod = big_divmod(t, pg);
+    const Big w = big_mul(Mi, (uint64_t)inv_mod((int64_t)mi_mod, (int64_t)pg));  // < M
+    for (int l = 0; l < 3; ++l) rp.w[g][l] = w.l[l];
+  }
+  Big half = big_sub(M, big_from(1));
+  big_divmod(half, 2);
+  for (int l = 0; l < 3; ++l) {
+    rp.M[l] = M.l[l];
+    rp.half[l] = half.l[l];
+  }
+  const int bl = big_bitlength(M);
+  rp.topshift = bl - 40;
+  {
+    Big mt = M;
+    for (int s = 0; s < rp.topshift; ++s) big_divmod(mt, 2);
+    rp.inv_mt = 1.0f / (float)mt.l[0];
+  }
+  rp.alpha = alpha; rp.beta = beta; rp.C = C; rp.ldc = ldc;
+  const dim3 grid((unsigned)((m + 255) / 256), (unsigned)(n < 65535 ? n : 65535));
+  crt_reconstruct_kernel<<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+}  // namespace gb300

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstdint>
 
 namespace gb300 {
 
@@ -12,6 +13,7 @@ constexpr int kSplitBM = 128;      // tile rows (TMEM lanes)
 constexpr int kBf16xBN = 256;      // tile columns of the BF16xP SGEMM
 constexpr int kOzakiBN = 256;      // tile columns of the Ozaki DGEMM
 constexpr int kOzakiMaxSlices = 12;
+constexpr int kCrtMaxModuli = 24;  // moduli of the CRT (modular-integer) FP64 form
 
 size_t split_workspace_bytes(int kind, int m, int n, int k, int param);
 
@@ -20,6 +22,35 @@ size_t split_workspace_bytes(int kind, int m, int n, int k, int param);
 int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
                 const float *B, int ldb, float beta, float *C, int ldc, int products, void *ws,
                 size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0 = 0);
+
+// The slice-product tcgen05 GEMM shared by the slice (mode 0) and CRT (mode 1)
+// FP64 forms: operands are S blocks of Mp (Np) rows x Kp of BF16-held integers.
+struct OzakiGemmArgs {
+  int m, n, S, mode;
+  int64_t Mp, Np, Kp;
+  const void *As, *Bs;
+  double alpha, beta;
+  double *C;
+  int ldc;
+  const int *expA, *expB;
+  double *res;        // mode 0: Mp x Np FP64 scratch
+  uint8_t *rres;      // mode 1: S x Mp x Np residues
+  const int *mods;    // mode 1: the S moduli
+};
+int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err);
+// Per-row max |.| of op(A) and per-column max of op(B) and their scale
+// exponents: amax and ex hold Mp entries (rows of op(A)) then Np (columns of op(B)).
+int row_scale_exponents(char ta, char tb, int m, int n, int k, const double *A, int lda,
+                        const double *B, int ldb, unsigned long long *amax, int *ex, int64_t Mp,
+                        int64_t Np, cudaStream_t st);
+
+// CRT form (crt.cu): C = alpha op(A) op(B) + beta C with the FP64 product
+// computed exactly as residues modulo `moduli` (0 = tuned / 16) BF16 GEMMs.
+size_t crt_workspace_bytes(int m, int n, int k, int moduli);
+int crt_bits_for(int moduli, int k);
+int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+              const double *B, int ldb, double beta, double *C, int ldc, int moduli, void *ws,
+              size_t ws_bytes, cudaStream_t st, unsigned *err);
 
 int ozaki_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                 const double *B, int ldb, double beta, double *C, int ldc, int slices, void *ws,

@@ -14,7 +14,9 @@
 //    FP32, and every accumulation chunk is capped at 1024 K-steps so partial sums
 //    stay below 1024*127^2 < 2^24 -- integer-valued FP32 is then exact.  The epilogue warps
 //    drain each chunk from TMEM into 32-bit integer sums (exact), and fold each
-//    slice group t = i + j into an FP64 result held in TMEM with weight 2^-7t.
+//    slice group t = i + j into an FP64 result scratch with weight 2^-7t.  The
+//    same kernel runs the CRT form (crt.cu): one residue pair per modulus,
+//    sums reduced mod p and stored instead of folded.
 //
 // Both GEMMs are persistent, warp-specialised kernels: warp 0 issues TMA loads
 // into a shared-memory ring, warp 1 allocates TMEM and issues tcgen05.mma from
@@ -29,6 +31,7 @@
 #include "common.cuh"
 #include "plain_gemm.h"
 #include "split_gemm.h"
+#include "split_tiles.cuh"
 
 namespace gb300 {
 
@@ -43,27 +46,6 @@ constexpr int kSplitGroupM = 16;
 // tiles through shared memory so that both the read and the K-major write
 // are coalesced whatever the transpose.
 // ===========================================================================
-template <typename T>
-__device__ __forceinline__ void load_tile_32x64(const T *__restrict__ X, int ld, int R, int K,
-                                                bool kcontig, int r0, int k0, T (*tile)[65]) {
-  const int tid = threadIdx.x;  // 256 threads
-  if (kcontig) {  // element (r, k) at X[k + r*ld]: read along k
-#pragma unroll
-    for (int p = 0; p < 8; ++p) {
-      const int r = p * 4 + (tid >> 6), k = tid & 63;
-      const int gr = r0 + r, gk = k0 + k;
-      tile[r][k] = (gr < R && gk < K) ? X[(int64_t)gr * ld + gk] : T(0);
-    }
-  } else {  // element (r, k) at X[r + k*ld]: read along r
-#pragma unroll
-    for (int p = 0; p < 8; ++p) {
-      const int r = tid & 31, k = p * 8 + (tid >> 5);
-      const int gr = r0 + r, gk = k0 + k;
-      tile[r][k] = (gr < R && gk < K) ? X[gr + (int64_t)gk * ld] : T(0);
-    }
-  }
-}
-
 // term[] of x: t0 = bf16(x), t1 = bf16(x - t0), t2 = bf16(x - t0 - t1); every
 // residual is exact in FP32.
 __device__ __forceinline__ void bf16_terms(float x, int nterms, __nv_bfloat16 (&t)[3]) {
@@ -166,30 +148,12 @@ __global__ void __launch_bounds__(256) row_absmax_kernel(const double *__restric
   }
 }
 
-// Scale exponent of a row: 2^-E * max|x| < 1.  Non-finite rows return a marker.
-constexpr int kNonFiniteExp = 0x40000000;
-__device__ __forceinline__ int row_exponent(unsigned long long amax_bits) {
-  const double m = __longlong_as_double((long long)amax_bits);
-  if (!(m <= 1.7976931348623157e308)) return kNonFiniteExp;  // Inf or NaN
-  if (m == 0.0) return 0;
-  int e;
-  frexp(m, &e);  // m = f * 2^e, f in [0.5, 1)
-  return e;
-}
-
 // Ozaki step 1b: the per-row exponents, once (the slice kernel and the GEMM
 // epilogue read them instead of recomputing frexp per element).
 __global__ void row_exponent_kernel(const unsigned long long *__restrict__ amax, int R,
                                     int *__restrict__ ex) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < R) ex[r] = row_exponent(amax[r]);
-}
-
-// 2^e as a double when it is a normal number, built from the exponent bits
-// (one multiply then scales exactly); ldexp outside that range.
-__device__ __forceinline__ double scale_pow2(double v, int e) {
-  if (e >= -1022 && e <= 1023) return v * __longlong_as_double((long long)(e + 1023) << 52);
-  return ldexp(v, e);
 }
 
 // The S digits of 8 consecutive values of one row (row exponent e), packed as
@@ -463,13 +427,16 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 // ===========================================================================
 struct OzakiParams {
   int m, n, tiles_m, tiles_n;
-  int S, KB;   // slices, K blocks of 64 per slice pair
+  int S, KB;   // slices (mode 0) or moduli (mode 1), K blocks of 64 per pair
+  int mode;    // 0: slice products folded into FP64; 1: residues mod mods[g] (CRT form)
   int Mp, Np;  // rows per slice block of A and B
   double alpha, beta;
   double *C;
   int ldc;
   const int *expA, *expB;  // per-row / per-column scale exponents
   double *res;             // Mp x Np FP64 result scratch (ld = Mp)
+  uint8_t *rres;           // mode 1: S blocks of Mp x Np residues in [0, mods[g]) (ld = Mp)
+  int mods[kCrtMaxModuli];
   unsigned *err;
 };
 
@@ -494,6 +461,23 @@ __device__ __forceinline__ void group_pairs(int t, int S, int &lo, int &np) {
   const int hi = min(S, t - 1);
   np = hi - lo + 1;
 }
+
+// Group gi (0-based) of the K sequence.  Mode 0: slice order t = S + 1 - gi,
+// pairs sa in [lo, lo + np), sb = t - sa.  Mode 1: modulus gi, the single pair
+// (gi + 1, gi + 1) of residue blocks (t = 2 gi + 2 makes sb = t - sa hold).
+__device__ __forceinline__ void group_of(int mode, int gi, int S, int &t, int &lo, int &np) {
+  if (mode) {
+    lo = gi + 1;
+    np = 1;
+    t = 2 * gi + 2;
+  } else {
+    t = S + 1 - gi;
+    group_pairs(t, S, lo, np);
+  }
+}
+// mode 1: int32 running sums are reduced mod p at least every 64 chunks:
+// 64 * 1024 * 127^2 < 2^31.
+constexpr int kCrtRunChunks = 64;
 
 __global__ void __launch_bounds__(kOzThreads, 1)
 ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -534,9 +518,9 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         int tm, tn;
         tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
-        for (int t = S + 1; t >= 2 && ok; --t) {
-          int lo, np;
-          group_pairs(t, S, lo, np);
+        for (int gi = 0; gi < S && ok; ++gi) {
+          int t, lo, np;
+          group_of(p.mode, gi, S, t, lo, np);
           const int G = np * KB;
           for (int idx = 0; idx < G; ++idx, ++L) {
             const int kb = idx / np, sa = lo + idx % np, sb = t - sa;
@@ -561,9 +545,9 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        for (int t = S + 1; t >= 2 && ok; --t) {
-          int lo, np;
-          group_pairs(t, S, lo, np);
+        for (int gi = 0; gi < S && ok; ++gi) {
+          int t, lo, np;
+          group_of(p.mode, gi, S, t, lo, np);
           const int G = np * KB;
           for (int c0 = 0; c0 < G && ok; c0 += kOzChunkStages, ++chunk) {
             const int b = chunk & 1;
@@ -612,9 +596,10 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       const int col0 = tn * kOzakiBN + h * kOzCols;          // first of this warp's columns
       double *res = p.res + (int64_t)col0 * p.Mp + row;      // res[j * Mp] is column col0 + j
       bool res_init = false;
-      for (int t = S + 1; t >= 2 && ok; --t) {
-        int lo, np;
-        group_pairs(t, S, lo, np);
+      const int run_limit = p.mode ? kCrtRunChunks : kOzRunChunks;
+      for (int gi = 0; gi < S && ok; ++gi) {
+        int t, lo, np;
+        group_of(p.mode, gi, S, t, lo, np);
         const int G = np * KB;
         const int nch = (G + kOzChunkStages - 1) / kOzChunkStages;
         const double wt = ldexp(1.0, -7 * t);
@@ -641,7 +626,22 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           __syncwarp();
           if (lane == 0) mbar_arrive(&acce[b]);
           const bool last = (c == nch - 1);
-          if (++since_fold == kOzRunChunks || last) {
+          if (p.mode && (++since_fold == run_limit || last)) {
+            // CRT form: reduce the exact sums mod p; at the modulus' end store
+            // the residue in [0, p) for the reconstruction kernel
+            const int pm = p.mods[gi];
+#pragma unroll
+            for (int j = 0; j < kOzCols; ++j) {
+              int r = run[j] % pm;
+              run[j] = r < 0 ? r + pm : r;
+            }
+            if (last) {
+              uint8_t *dst = p.rres + (int64_t)gi * p.Mp * p.Np + (int64_t)col0 * p.Mp + row;
+#pragma unroll
+              for (int j = 0; j < kOzCols; ++j) dst[(int64_t)j * p.Mp] = (uint8_t)run[j];
+            }
+            since_fold = 0;
+          } else if (!p.mode && (++since_fold == kOzRunChunks || last)) {
             // fold the exact group sum into the FP64 result: res += run * 2^-7t
 #pragma unroll
             for (int g = 0; g < kOzCols; g += 8) {
@@ -660,8 +660,9 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         }
       }
       if (!ok) break;
-      // final epilogue: C = alpha * 2^(E_i + F_j) * res + beta * C
-      if (row < p.m) {
+      // final epilogue: C = alpha * 2^(E_i + F_j) * res + beta * C (slice form;
+      // the CRT form's C update is the reconstruction kernel's)
+      if (!p.mode && row < p.m) {
         const int ea = p.expA[row];
 #pragma unroll 1
         for (int g = 0; g < kOzCols; g += 8) {
@@ -728,6 +729,7 @@ static SegMap seg_map(int products, bool is_a) {
 
 size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
+  if (kind == 2) return crt_workspace_bytes(m, n, k, param);
   const int64_t Kp = round_up(k, kSplitBK);
   if (kind == 0) {
     if (param == 0) {
@@ -893,19 +895,12 @@ static OzakiLayout ozaki_layout(int m, int n, int k, int S, void *ws) {
   return L;
 }
 
-int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
-                  int ldb, int slices, void *ws, size_t ws_bytes, cudaStream_t st) {
-  const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
-  const int S = slices > 0 ? slices : ozaki_default_slices(m, n, k);
-  if (ck == GB300_ERR_ARG || S < 2 || S > kOzakiMaxSlices) return GB300_ERR_ARG;
-  if (ck < 0 || k == 0) return GB300_OK;
-  const size_t need = split_workspace_bytes(1, m, n, k, S);
-  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
-  const OzakiLayout L = ozaki_layout(m, n, k, S, ws);
-  if (S * L.Mp > 0x7fffffff || S * L.Np > 0x7fffffff || L.Kp > 0x7fffffff) return GB300_ERR_ARG;
+int row_scale_exponents(char ta, char tb, int m, int n, int k, const double *A, int lda,
+                        const double *B, int ldb, unsigned long long *amax, int *ex, int64_t Mp,
+                        int64_t Np, cudaStream_t st) {
+  // amax / ex hold Mp entries for the rows of op(A), then Np for the columns of op(B)
   const bool an = notrans(ta), bn = notrans(tb);
-  if (cudaMemsetAsync(L.amaxA, 0, (size_t)(L.Mp + L.Np) * 8, st) != cudaSuccess)
-    return GB300_ERR_CUDA;
+  if (cudaMemsetAsync(amax, 0, (size_t)(Mp + Np) * 8, st) != cudaSuccess) return GB300_ERR_CUDA;
   // per-row / per-column max |.|: A rows are k-contiguous when transposed, B
   // columns when not.
   auto absmax = [&](const double *X, int ld, int R, bool kc, unsigned long long *am) {
@@ -919,10 +914,26 @@ int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int ld
       row_absmax_kernel<<<dim3((unsigned)((R + 255) / 256), gy), 256, 0, st>>>(X, ld, R, k, 0,
                                                                               (int)span, am);
   };
-  absmax(A, lda, m, !an, L.amaxA);
-  absmax(B, ldb, n, bn, L.amaxB);
-  row_exponent_kernel<<<(unsigned)((L.Mp + L.Np + 255) / 256), 256, 0, st>>>(
-      L.amaxA, (int)(L.Mp + L.Np), L.expA);  // amaxB and expB follow amaxA and expA
+  absmax(A, lda, m, !an, amax);
+  absmax(B, ldb, n, bn, amax + Mp);
+  row_exponent_kernel<<<(unsigned)((Mp + Np + 255) / 256), 256, 0, st>>>(amax, (int)(Mp + Np), ex);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
+                  int ldb, int slices, void *ws, size_t ws_bytes, cudaStream_t st) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
+  const int S = slices > 0 ? slices : ozaki_default_slices(m, n, k);
+  if (ck == GB300_ERR_ARG || S < 2 || S > kOzakiMaxSlices) return GB300_ERR_ARG;
+  if (ck < 0 || k == 0) return GB300_OK;
+  const size_t need = split_workspace_bytes(1, m, n, k, S);
+  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
+  const OzakiLayout L = ozaki_layout(m, n, k, S, ws);
+  if (S * L.Mp > 0x7fffffff || S * L.Np > 0x7fffffff || L.Kp > 0x7fffffff) return GB300_ERR_ARG;
+  const bool an = notrans(ta), bn = notrans(tb);
+  const int rc = row_scale_exponents(ta, tb, m, n, k, A, lda, B, ldb, L.amaxA, L.expA, L.Mp,
+                                     L.Np, st);
+  if (rc != GB300_OK) return rc;
   ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Mp)), 256, 0, st>>>(
       A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, S, L.expA, L.As);
   ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Np)), 256, 0, st>>>(
@@ -942,18 +953,31 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
   const size_t need = split_workspace_bytes(1, m, n, k, S);
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
   const OzakiLayout L = ozaki_layout(m, n, k, S, const_cast<void *>(ws));
+  OzakiGemmArgs a;
+  a.m = m; a.n = n; a.S = S; a.mode = 0;
+  a.Mp = L.Mp; a.Np = L.Np; a.Kp = L.Kp;
+  a.As = L.As; a.Bs = L.Bs;
+  a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc;
+  a.expA = L.expA; a.expB = L.expB; a.res = L.res; a.rres = nullptr; a.mods = nullptr;
+  return ozaki_gemm_launch(a, st, err);
+}
+
+int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
+  if (a.S < 1 || a.S > (a.mode ? kCrtMaxModuli : kOzakiMaxSlices)) return GB300_ERR_ARG;
   CUtensorMap tA{}, tB{};
-  if (!encode_2d(&tA, L.As, 2, L.Kp, S * L.Mp, L.Kp, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&tB, L.Bs, 2, L.Kp, S * L.Np, L.Kp, kSplitBK, kOzakiBN, true))
+  if (!encode_2d(&tA, a.As, 2, a.Kp, a.S * a.Mp, a.Kp, kSplitBK, kSplitBM, true) ||
+      !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, kOzakiBN, true))
     return GB300_ERR_CUDA;
   OzakiParams p;
-  p.m = m; p.n = n;
-  p.tiles_m = (int)(L.Mp / kSplitBM);
-  p.tiles_n = (int)(L.Np / kOzakiBN);
-  p.S = S; p.KB = (int)(L.Kp / kSplitBK);
-  p.Mp = (int)L.Mp; p.Np = (int)L.Np;
-  p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc;
-  p.expA = L.expA; p.expB = L.expB; p.res = L.res; p.err = err;
+  p.m = a.m; p.n = a.n;
+  p.tiles_m = (int)(a.Mp / kSplitBM);
+  p.tiles_n = (int)(a.Np / kOzakiBN);
+  p.S = a.S; p.KB = (int)(a.Kp / kSplitBK);
+  p.mode = a.mode;
+  p.Mp = (int)a.Mp; p.Np = (int)a.Np;
+  p.alpha = a.alpha; p.beta = a.beta; p.C = a.C; p.ldc = a.ldc;
+  p.expA = a.expA; p.expB = a.expB; p.res = a.res; p.rres = a.rres; p.err = err;
+  for (int i = 0; i < kCrtMaxModuli; ++i) p.mods[i] = (a.mode && i < a.S) ? a.mods[i] : 1;
   if (cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kOzSmem) != cudaSuccess)
     return GB300_ERR_CUDA;

@@ -19,7 +19,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 CU_SOURCES = ["plain_gemm.cu", "tc_gemm.cu", "grouped.cu", "autotune.cu", "trsm.cu", "api.cu",
-              "noalloc.cu", "cplx.cu"]
+              "noalloc.cu", "cplx.cu", "crt.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

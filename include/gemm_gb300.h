@@ -285,9 +285,28 @@ int gb300_host_zgemm(char transa, char transb, int m, int n, int k, const double
                      const double *a, int lda, const double *b, int ldb, const double *beta,
                      double *c, int ldc, int method, int param);
 
+/* FP64 GEMM by the CRT (modular-integer) form on the BF16 tensor pipe, after
+ * Ozaki scheme II: rows of op(A) and columns of op(B) are scaled by powers of
+ * two to integers of b bits, their product is computed exactly as residues
+ * modulo `moduli` pairwise coprime odd moduli <= 255 (one tensor-core GEMM per
+ * modulus) and rebuilt by the Chinese remainder theorem in 192-bit integer
+ * arithmetic, then rounded once to FP64.  b is the largest integer with
+ * 2 k (2^b - 1)^2 < M (M the product of the moduli): 16 moduli give 56 bits at
+ * k = 4096, the accuracy of 8 slices for 16 instead of 36 GEMMs.  moduli 0 =
+ * 16, else 2..24; GB300_ERR_ARG when k is too large for any b at that count.
+ * workspace NULL: a library-owned buffer per stream; otherwise at least
+ * gb300_split_workspace_bytes(2, m, n, k, moduli) bytes. */
+int gb300_dgemm_ozaki2(char transa, char transb, int m, int n, int k, double alpha,
+                       const double *A, int lda, const double *B, int ldb, double beta, double *C,
+                       int ldc, int moduli, void *workspace, size_t workspace_bytes,
+                       void *stream);
+int gb300_host_dgemm_ozaki2(char transa, char transb, int m, int n, int k, double alpha,
+                            const double *a, int lda, const double *b, int ldb, double beta,
+                            double *c, int ldc, int moduli);
+
 /* Workspace needed by the split forms for one call of the given shape.
  * kind = 0: sgemm_bf16x with `param` = products; kind = 1: dgemm_ozaki with
- * `param` = slices. */
+ * `param` = slices; kind = 2: dgemm_ozaki2 with `param` = moduli. */
 size_t gb300_split_workspace_bytes(int kind, int m, int n, int k, int param);
 
 /* After a stream synchronisation: the first error code any kernel of this
