@@ -38,13 +38,16 @@ constexpr int kModuli[kCrtMaxModuli] = {255, 253, 251, 247, 241, 239, 233, 229,
                                         227, 223, 217, 211, 199, 197, 193, 191,
                                         181, 179, 173, 167, 163, 157, 151, 149};
 constexpr int kCrtDefaultModuli = 16;
+constexpr int kCrtPowT = 128;  // 2^t mod p table: t = b - 53 + ... stays below b <= 120
 
 // ------------------------------------------------------------------ residues
 struct CrtModParams {
   int N, b;
   unsigned p[kCrtMaxModuli];
-  unsigned mg[kCrtMaxModuli];    // floor(2^32 / p)
-  unsigned pw32[kCrtMaxModuli];  // 2^32 mod p
+  unsigned mg[kCrtMaxModuli];   // floor(2^32 / p)
+  unsigned c21[kCrtMaxModuli];  // 2^21 mod p
+  unsigned c42[kCrtMaxModuli];  // 2^42 mod p
+  uint8_t pow2[kCrtMaxModuli][kCrtPowT];  // 2^t mod p, t < kCrtPowT
 };
 
 // x mod p for x < 2^32 (Barrett with mg = floor(2^32/p): q is the quotient or
@@ -54,28 +57,22 @@ __device__ __forceinline__ unsigned mod32(unsigned x, unsigned p, unsigned mg) {
   const unsigned r = x - q * p;
   return r >= p ? r - p : r;
 }
-__device__ __forceinline__ unsigned mod64(unsigned long long x, unsigned p, unsigned mg,
-                                          unsigned pw32) {
-  const unsigned h = mod32((unsigned)(x >> 32), p, mg), l = mod32((unsigned)x, p, mg);
-  return mod32(h * pw32 + l, p, mg);  // < 255 * 255 + 255
-}
-// 2^t mod p, t >= 0
-__device__ __forceinline__ unsigned pow2mod(int t, unsigned p, unsigned mg, unsigned pw32) {
-  unsigned r = mod32(1u << (t & 31), p, mg);
-  for (int q = t >> 5; q > 0; --q) r = mod32(r * pw32, p, mg);
-  return r;
-}
 
 // Symmetric residues of A' = trunc(x 2^(b - e)) for N moduli, 8 consecutive k
 // of one row per thread, as BF16, block i at dst[i * step] (uint4 units).
 // |x| = M 2^base with M the 53-bit significand, so |x| 2^(b-e) = M 2^t,
-// t = b - e + base: a right shift truncates, a left shift is exact (and
-// reduced through 2^t mod p when M 2^t would not fit 64 bits).
+// t = b - e + base.  The integer y = M 2^t (right shift: truncation; left
+// shift up to 10: exact, < 2^63) or, for t > 10, y = M with the factor
+// 2^t mod p applied after, is cut into 21-bit chunks y0 + y1 2^21 + y2 2^42;
+// y mod p = (y0 + y1 (2^21 mod p) + y2 (2^42 mod p)) mod p, a sum below 2^31.
 __global__ void __launch_bounds__(256)
     crt_residue_kernel(const double *__restrict__ X, int ld, int R, int K, int kcontig, int Rp,
-                       int Kp, const int *__restrict__ ex, CrtModParams mp,
+                       int Kp, const int *__restrict__ ex, const __grid_constant__ CrtModParams mp,
                        __nv_bfloat16 *__restrict__ out) {
   __shared__ double tile[32][65];
+  __shared__ uint8_t pow2[kCrtMaxModuli][kCrtPowT];
+  for (int i = threadIdx.x; i < mp.N * kCrtPowT; i += blockDim.x)
+    pow2[i / kCrtPowT][i % kCrtPowT] = mp.pow2[i / kCrtPowT][i % kCrtPowT];
   const int k0 = blockIdx.x * 64;
   const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
   const int64_t step = (int64_t)Rp * Kp / 8;
@@ -86,34 +83,34 @@ __global__ void __launch_bounds__(256)
     const int e = (gr < R) ? ex[gr] : 0;
     const bool bad = (e == kNonFiniteExp);  // row of Inf/NaN: zeros, the result is NaN
     uint4 *dst = reinterpret_cast<uint4 *>(out + (int64_t)gr * Kp + k0 + kq);
-    unsigned long long mag[8];
-    int sh[8];
-    unsigned neg = 0;
+    unsigned y0[8], y1[8], y2[8];
+    int tp[8];         // t when t > 10 (the 2^t factor), else -1
+    unsigned neg = 0;  // sign bits
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const unsigned long long u = (unsigned long long)__double_as_longlong(tile[r][kq + j]);
       const int be = (int)((u >> 52) & 0x7ff);
-      mag[j] = bad ? 0ull : ((u & 0xfffffffffffffull) | (be ? (1ull << 52) : 0ull));
-      sh[j] = mp.b - e + ((be ? be : 1) - 1075);
+      const unsigned long long M =
+          bad ? 0ull : ((u & 0xfffffffffffffull) | (be ? (1ull << 52) : 0ull));
+      const int t = mp.b - e + ((be ? be : 1) - 1075);
+      const unsigned long long y =
+          t < 0 ? (t > -64 ? M >> (-t) : 0ull) : (t <= 10 ? M << t : M);
+      y0[j] = (unsigned)y & 0x1fffff;
+      y1[j] = (unsigned)(y >> 21) & 0x1fffff;
+      y2[j] = (unsigned)(y >> 42);
+      tp[j] = t > 10 ? t : -1;
       neg |= (unsigned)(u >> 63) << j;
     }
     for (int i = 0; i < mp.N; ++i) {
-      const unsigned p = mp.p[i], mg = mp.mg[i], pw = mp.pw32[i];
+      const unsigned p = mp.p[i], mg = mp.mg[i], c21 = mp.c21[i], c42 = mp.c42[i];
       unsigned w[4];
 #pragma unroll
       for (int j = 0; j < 8; j += 2) {
         unsigned h[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-          const int t = sh[j + q];
-          const unsigned long long M = mag[j + q];
-          unsigned rr;
-          if (t < 0)
-            rr = (t <= -64) ? 0u : mod64(M >> (-t), p, mg, pw);
-          else if (t <= 10)
-            rr = mod64(M << t, p, mg, pw);
-          else
-            rr = mod32(mod64(M, p, mg, pw) * pow2mod(t, p, mg, pw), p, mg);
+          unsigned rr = mod32(y0[j + q] + y1[j + q] * c21 + y2[j + q] * c42, p, mg);
+          if (tp[j + q] >= 0) rr = mod32(rr * pow2[i][tp[j + q]], p, mg);
           if (((neg >> (j + q)) & 1) && rr) rr = p - rr;
           const int sres = rr > (p >> 1) ? (int)rr - (int)p : (int)rr;
           h[q] = __float_as_uint((float)sres) >> 16;  // |sres| <= 127: exact in BF16
@@ -127,135 +124,142 @@ __global__ void __launch_bounds__(256)
 }
 
 // ------------------------------------------------------------- reconstruction
+constexpr int kLimbs = 6;  // 32-bit limbs of M and the weights (M < 2^188)
 struct CrtRecParams {
   int N, m, n, Mp, Np, two_b;
-  int topshift;    // bitlength(M) - 40
-  float inv_mt;    // 1 / (M >> topshift)
-  unsigned long long w[kCrtMaxModuli][3];  // CRT weights, 192-bit little-endian limbs
-  unsigned long long M[3], half[3];        // M and (M - 1) / 2
+  int topshift;  // bitlength(M) - 40
+  float inv_mt;  // 1 / (M >> topshift)
+  unsigned w[kCrtMaxModuli][kLimbs];  // CRT weights, little-endian 32-bit limbs
+  unsigned M[kLimbs], half[kLimbs];   // M and (M - 1) / 2
   double alpha, beta;
   double *C;
   int ldc;
 };
 
-// 64 bits of a 4-limb number starting at bit s (s < 192)
-__device__ __forceinline__ unsigned long long bits64(const unsigned long long (&x)[4], int s) {
-  const int l = s >> 6, o = s & 63;
-  const unsigned long long lo = x[l], hi = x[l + 1];
-  return o ? (lo >> o) | (hi << (64 - o)) : lo;
-}
-
+// One thread per element of C: X = sum r_g w_g in carry-save 64-bit limb
+// accumulators (r < 2^8, limbs < 2^32, at most 24 terms: no overflow), then
+// P = X - q M with q = floor(X / M) estimated from X's top bits in FP32 and
+// corrected, the symmetric residue, and one rounding to FP64.
 __global__ void __launch_bounds__(256)
     crt_reconstruct_kernel(const uint8_t *__restrict__ rres, const int *__restrict__ expA,
-                           const int *__restrict__ expB, CrtRecParams rp) {
+                           const int *__restrict__ expB, const __grid_constant__ CrtRecParams rp) {
   const int64_t plane = (int64_t)rp.Mp * rp.Np;
   for (int j = blockIdx.y; j < rp.n; j += gridDim.y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= rp.m) continue;
-    // X = sum r_g w_g (< 2^13 M: four limbs)
-    unsigned long long X[4] = {0ull, 0ull, 0ull, 0ull};
+    unsigned long long acc[kLimbs] = {0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
     const uint8_t *src = rres + (int64_t)j * rp.Mp + i;
     for (int g = 0; g < rp.N; ++g) {
-      const unsigned long long r = src[g * plane];
-      unsigned long long carry = 0;
+      const unsigned r = src[g * plane];
 #pragma unroll
-      for (int l = 0; l < 3; ++l) {
-        const unsigned long long lo = r * rp.w[g][l], hi = __umul64hi(r, rp.w[g][l]);
-        unsigned long long s = X[l] + lo;
-        unsigned long long c = s < lo;
-        s += carry;
-        c += s < carry;
-        X[l] = s;
-        carry = hi + c;
-      }
-      X[3] += carry;
+      for (int l = 0; l < kLimbs; ++l) acc[l] += (unsigned long long)r * rp.w[g][l];
     }
-    // P = X - q M with q = floor(X / M) estimated from the top bits, then corrected
-    const unsigned long long xt = bits64(X, rp.topshift);  // < 2^53
-    unsigned long long q = (unsigned long long)((float)xt * rp.inv_mt);
-    unsigned long long P[4];
+    unsigned X[kLimbs + 1];  // X < 2^13 M < 2^201
     {
-      unsigned long long borrow = 0, carry = 0;
-#pragma unroll
-      for (int l = 0; l < 4; ++l) {
-        const unsigned long long ml = l < 3 ? rp.M[l] : 0ull;
-        const unsigned long long lo = q * ml, hi = __umul64hi(q, ml);
-        unsigned long long qm = lo + carry;
-        carry = hi + (qm < lo);
-        const unsigned long long d = X[l] - qm;
-        const unsigned long long b1 = X[l] < qm;
-        const unsigned long long d2 = d - borrow;
-        const unsigned long long b2 = d < borrow;
-        P[l] = d2;
-        borrow = b1 | b2;
-      }
-    }
-    // P is X - q M in two's complement: add M while negative, subtract while >= M
-    for (int it = 0; it < 3 && (long long)P[3] < 0; ++it) {
       unsigned long long c = 0;
 #pragma unroll
-      for (int l = 0; l < 4; ++l) {
-        const unsigned long long ml = l < 3 ? rp.M[l] : 0ull;
-        const unsigned long long s = P[l] + ml;
-        const unsigned long long c1 = s < ml;
-        P[l] = s + c;
-        c = c1 | (P[l] < c);
+      for (int l = 0; l < kLimbs; ++l) {
+        c += acc[l];
+        X[l] = (unsigned)c;
+        c >>= 32;
+      }
+      X[kLimbs] = (unsigned)c;
+    }
+    // 53 bits of X from bit topshift (X >> topshift < 2^53)
+    unsigned long long xt;
+    {
+      const int li = rp.topshift >> 5, o = rp.topshift & 31;
+      unsigned long long lo = 0, hi = 0;
+#pragma unroll
+      for (int l = 0; l < kLimbs + 1; ++l) {
+        if (l == li) lo = X[l];
+        if (l == li + 1) lo |= (unsigned long long)X[l] << 32;
+        if (l == li + 2) hi = X[l];
+      }
+      xt = o ? (lo >> o) | (hi << (64 - o)) : lo;
+    }
+    const unsigned q = (unsigned)((float)xt * rp.inv_mt);
+    // P = X - q M, two's complement over kLimbs + 1 limbs
+    unsigned P[kLimbs + 1];
+    {
+      long long c = 0;
+#pragma unroll
+      for (int l = 0; l < kLimbs + 1; ++l) {
+        const unsigned long long qm = l < kLimbs ? (unsigned long long)q * rp.M[l] : 0ull;
+        c += (long long)X[l] - (long long)(qm & 0xffffffffull);
+        P[l] = (unsigned)c;
+        c = (c >> 32) - (long long)(qm >> 32);
       }
     }
-    auto ge = [&](const unsigned long long(&a)[4], const unsigned long long(&b)[3]) {
-      if (a[3]) return true;
-      for (int l = 2; l >= 0; --l)
+    // add M while negative, subtract M while >= M (q was off by at most one)
+    for (int it = 0; it < 3 && (int)P[kLimbs] < 0; ++it) {
+      unsigned long long c = 0;
+#pragma unroll
+      for (int l = 0; l < kLimbs + 1; ++l) {
+        c += (unsigned long long)P[l] + (l < kLimbs ? rp.M[l] : 0u);
+        P[l] = (unsigned)c;
+        c >>= 32;
+      }
+    }
+    auto geq = [&](const unsigned(&a)[kLimbs + 1], const unsigned *b) {
+      if (a[kLimbs]) return true;
+      for (int l = kLimbs - 1; l >= 0; --l)
         if (a[l] != b[l]) return a[l] > b[l];
       return true;
     };
-    for (int it = 0; it < 3 && ge(P, rp.M); ++it) {
-      unsigned long long bo = 0;
+    for (int it = 0; it < 3 && geq(P, rp.M); ++it) {
+      long long c = 0;
 #pragma unroll
-      for (int l = 0; l < 4; ++l) {
-        const unsigned long long ml = l < 3 ? rp.M[l] : 0ull;
-        const unsigned long long d = P[l] - ml;
-        const unsigned long long b1 = P[l] < ml;
-        P[l] = d - bo;
-        bo = b1 | (d < bo);
+      for (int l = 0; l < kLimbs + 1; ++l) {
+        c += (long long)P[l] - (long long)(l < kLimbs ? rp.M[l] : 0u);
+        P[l] = (unsigned)c;
+        c >>= 32;
       }
     }
-    // symmetric: P > (M - 1) / 2 stands for P - M
-    bool neg = false;
-    unsigned long long mg[3] = {P[0], P[1], P[2]};
-    {
-      bool gt = false;
-      for (int l = 2; l >= 0; --l)
-        if (P[l] != rp.half[l]) { gt = P[l] > rp.half[l]; break; }
-      if (gt) {  // magnitude M - P
-        neg = true;
-        unsigned long long bo = 0;
+    // symmetric: P > (M - 1) / 2 stands for P - M; magnitude in mg
+    bool gt = false;
 #pragma unroll
-        for (int l = 0; l < 3; ++l) {
-          const unsigned long long d = rp.M[l] - P[l];
-          const unsigned long long b1 = rp.M[l] < P[l];
-          mg[l] = d - bo;
-          bo = b1 | (d < bo);
-        }
+    for (int l = kLimbs - 1; l >= 0; --l)
+      if (P[l] != rp.half[l]) { gt = P[l] > rp.half[l]; break; }
+    unsigned mg[kLimbs];
+    if (gt) {
+      long long c = 0;
+#pragma unroll
+      for (int l = 0; l < kLimbs; ++l) {
+        c += (long long)rp.M[l] - (long long)P[l];
+        mg[l] = (unsigned)c;
+        c >>= 32;
       }
+    } else {
+#pragma unroll
+      for (int l = 0; l < kLimbs; ++l) mg[l] = P[l];
     }
     // magnitude -> FP64 with one rounding: the top 64 bits, the rest as a sticky bit
-    unsigned long long top;
-    int pos;
-    if (mg[2]) {
-      const int lz = __clzll((long long)mg[2]);
-      top = (mg[2] << lz) | (lz ? mg[1] >> (64 - lz) : 0ull);
-      const unsigned long long rest = (lz ? mg[1] << lz : 0ull) | (lz ? 0ull : mg[1]) | mg[0];
-      if (rest) top |= 1ull;
-      pos = 128 - lz;
-    } else if (mg[1]) {
-      const int lz = __clzll((long long)mg[1]);
-      top = (mg[1] << lz) | (lz ? mg[0] >> (64 - lz) : 0ull);
-      const unsigned long long rest = lz ? mg[0] << lz : mg[0];
-      if (rest) top |= 1ull;
-      pos = 64 - lz;
-    } else {
+    int tl = -1;
+#pragma unroll
+    for (int l = kLimbs - 1; l >= 0; --l)
+      if (tl < 0 && mg[l]) tl = l;
+    unsigned long long top = 0;
+    int pos = 0;
+    if (tl >= 2) {
+      unsigned a2 = 0, a1 = 0, a0 = 0;
+      bool sticky = false;
+#pragma unroll
+      for (int l = 0; l < kLimbs; ++l) {
+        if (l == tl) a2 = mg[l];
+        else if (l == tl - 1) a1 = mg[l];
+        else if (l == tl - 2) a0 = mg[l];
+        else if (l < tl - 2 && mg[l]) sticky = true;
+      }
+      const int lz = __clz(a2);
+      const unsigned long long w96hi = ((unsigned long long)a2 << 32) | a1;
+      top = lz ? (w96hi << lz) | ((unsigned long long)a0 >> (32 - lz)) : w96hi;
+      if ((lz ? (a0 << lz) : a0) != 0 || sticky) top |= 1ull;  // a0's bits below the window
+      pos = 32 * (tl - 1) - lz;
+    } else if (tl == 1) {
+      top = ((unsigned long long)mg[1] << 32) | mg[0];
+    } else if (tl == 0) {
       top = mg[0];
-      pos = 0;
     }
     const int ea = expA[i], eb = expB[j];
     double v;
@@ -263,7 +267,7 @@ __global__ void __launch_bounds__(256)
       v = __longlong_as_double(0x7ff8000000000000LL);
     } else {
       v = scale_pow2(__ull2double_rn(top), pos + ea + eb - rp.two_b);
-      if (neg) v = -v;
+      if (gt) v = -v;
     }
     double *c = rp.C + (int64_t)j * rp.ldc + i;
     const double cb = (rp.beta == 1.0) ? *c : *c * rp.beta;
@@ -436,7 +440,13 @@ int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double 
     const unsigned p = (unsigned)kModuli[i];
     mp.p[i] = p;
     mp.mg[i] = (unsigned)((1ull << 32) / p);
-    mp.pw32[i] = (unsigned)((1ull << 32) % p);
+    mp.c21[i] = (unsigned)((1ull << 21) % p);
+    mp.c42[i] = (unsigned)((1ull << 42) % p);
+    unsigned v = 1;
+    for (int t = 0; t < kCrtPowT; ++t) {
+      mp.pow2[i][t] = (uint8_t)v;
+      v = (2 * v) % p;
+    }
   }
   auto row_blocks = [](int64_t Rp) { return (unsigned)(Rp / 32 < 65535 ? Rp / 32 : 65535); };
   const bool an = notrans(ta), bn = notrans(tb);
@@ -459,6 +469,9 @@ int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double 
   std::memset(&rp, 0, sizeof(rp));
   rp.N = N; rp.m = m; rp.n = n; rp.Mp = (int)L.Mp; rp.Np = (int)L.Np; rp.two_b = 2 * b;
   const Big M = modulus_product(N);
+  auto limbs32 = [](const Big &x, unsigned *out) {
+    for (int l = 0; l < kLimbs; ++l) out[l] = (unsigned)(x.l[l / 2] >> (32 * (l % 2)));
+  };
   for (int g = 0; g < N; ++g) {
     Big Mi = M;
     const uint64_t pg = (uint64_t)kModuli[g];
@@ -466,14 +479,12 @@ int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double 
     Big t = Mi;
     const uint64_t mi_mod = big_divmod(t, pg);
     const Big w = big_mul(Mi, (uint64_t)inv_mod((int64_t)mi_mod, (int64_t)pg));  // < M
-    for (int l = 0; l < 3; ++l) rp.w[g][l] = w.l[l];
+    limbs32(w, rp.w[g]);
   }
   Big half = big_sub(M, big_from(1));
   big_divmod(half, 2);
-  for (int l = 0; l < 3; ++l) {
-    rp.M[l] = M.l[l];
-    rp.half[l] = half.l[l];
-  }
+  limbs32(M, rp.M);
+  limbs32(half, rp.half);
   const int bl = big_bitlength(M);
   rp.topshift = bl - 40;
   {
