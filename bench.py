@@ -240,7 +240,6 @@ def run_ours(args, torch, rank, world):
     prob = Problem(torch, w)
     stream = torch.cuda.current_stream().cuda_stream
     is_d = w["prec"] == "d"
-    form = "ozaki" if is_d else "bf16x"
     m, n, k = w["m"], w["n"], w["k"]
 
     def plain_call(C):
@@ -254,30 +253,67 @@ def run_ours(args, torch, rank, world):
     assert plain_call(prob.C) == g.OK
     torch.cuda.synchronize()
     plain_err = rel_err(prob.C[cols, rows].cpu().numpy(), truth)
-    cands = list(range(6, 13)) if is_d else [3, 6]
-    chosen, errs = None, {}
+    # candidates: FP32: BF16xP products; FP64: the CRT form's moduli and the
+    # slice form's slice counts.  Per scheme, the smallest one whose max and
+    # Frobenius errors do not exceed the plain kernel's; for FP64 the faster
+    # of the two qualifying schemes is timed below.
+    schemes = [("crt", list(range(11, 25))), ("ozaki", list(range(6, 13)))] if is_d else \
+        [("bf16x", [3, 6])]
+    errs, qualified = {}, []
     ws = None
-    for param in cands:
-        need = g.split_workspace_bytes(1 if is_d else 0, m, n, k, param)
-        if ws is None or ws.numel() < need:
-            ws = torch.empty(need, dtype=torch.uint8, device="cuda")
-        prob.C.copy_(prob.C0)
-        assert g.split_prepare(form, w["ta"], w["tb"], m, n, k, prob.A.data_ptr(), w["lda"],
-                               prob.B.data_ptr(), w["ldb"], param, ws.data_ptr(), need,
+
+    def kind_of(f):
+        return {"bf16x": 0, "ozaki": 1, "crt": 2}[f]
+
+    def run_form(f, prm, need, C):
+        assert g.split_prepare(f, w["ta"], w["tb"], m, n, k, prob.A.data_ptr(), w["lda"],
+                               prob.B.data_ptr(), w["ldb"], prm, ws.data_ptr(), need,
                                stream) == g.OK
-        assert g.split_run(form, m, n, k, w["alpha"], w["beta"], prob.C.data_ptr(), w["ldc"],
-                           param, ws.data_ptr(), need, stream) == g.OK
-        torch.cuda.synchronize()
-        errs[param] = rel_err(prob.C[cols, rows].cpu().numpy(), truth)
-        # equal error: neither the max nor the Frobenius relative error may
-        # exceed the plain kernel's
-        if errs[param][0] <= plain_err[0] and errs[param][1] <= plain_err[1]:
-            chosen = param
-            break
-    if chosen is None:
-        chosen = cands[-1]
-    param = chosen
-    need = g.split_workspace_bytes(1 if is_d else 0, m, n, k, param)
+        assert g.split_run(f, m, n, k, w["alpha"], w["beta"], C.data_ptr(), w["ldc"], prm,
+                           ws.data_ptr(), need, stream) == g.OK
+
+    def name_of(f, prm):
+        return {"bf16x": "bf16x%d", "ozaki": "ozaki_s%d", "crt": "crt_n%d"}[f] % prm
+
+    for f, cands in schemes:
+        for prm in cands:
+            need = g.split_workspace_bytes(kind_of(f), m, n, k, prm)
+            if need == 0:
+                continue
+            if ws is None or ws.numel() < need:
+                ws = None
+                torch.cuda.empty_cache()
+                ws = torch.empty(need, dtype=torch.uint8, device="cuda")
+            prob.C.copy_(prob.C0)
+            run_form(f, prm, need, prob.C)
+            torch.cuda.synchronize()
+            e = rel_err(prob.C[cols, rows].cpu().numpy(), truth)
+            errs[name_of(f, prm)] = e
+            if e[0] <= plain_err[0] and e[1] <= plain_err[1]:
+                qualified.append((f, prm))
+                break
+    if not qualified:
+        f, cands = schemes[-1]
+        qualified.append((f, cands[-1]))
+    if len(qualified) > 1:
+        # time each qualifying form (one warm-up, two calls) and keep the faster
+        best = None
+        for f, prm in qualified:
+            need = g.split_workspace_bytes(kind_of(f), m, n, k, prm)
+            run_form(f, prm, need, prob.C)
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record()
+            for _ in range(2):
+                run_form(f, prm, need, prob.C)
+            a1.record()
+            torch.cuda.synchronize()
+            t_ = a0.elapsed_time(a1)
+            if best is None or t_ < best[0]:
+                best = (t_, f, prm)
+        form, param = best[1], best[2]
+    else:
+        form, param = qualified[0]
+    need = g.split_workspace_bytes(kind_of(form), m, n, k, param)
 
     # ---- timed region: W warm-up + K steps of prepare + run, inputs resident in HBM
     def step(ev0=None, ev1=None, ev2=None):
@@ -361,7 +397,7 @@ def run_ours(args, torch, rank, world):
         e2e = {"value": round(prob.flops / dt / 1e12, 3), "unit": "TFLOP/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": m * n * esz,
                "ms_per_step": round(dt * 1e3, 3), "api": "gb300_host_%s" %
-               ("dgemm_ozaki" if is_d else "sgemm_bf16x"),
+               {"bf16x": "sgemm_bf16x", "ozaki": "dgemm_ozaki", "crt": "dgemm_ozaki2"}[form],
                "transfer": "pinned host buffers; the split/slice kernels read A and B and the "
                            "GEMM epilogue reads and writes C in host memory over the coherent "
                            "CPU-GPU link (bytes above cross it once per step)"}
@@ -372,17 +408,18 @@ def run_ours(args, torch, rank, world):
 
     # ---- roofline of the dominant kernel (the tcgen05 GEMM of the split form)
     pk = peaks()
-    products = (param * (param + 1)) // 2 if is_d else param
+    products = {"bf16x": param, "ozaki": (param * (param + 1)) // 2, "crt": param}[form]
     pipe_flops = products * prob.flops
     achieved = pipe_flops / (gemm_ms / 1e3) / 1e12
     roof = {"bound": "tensor", "achieved": round(achieved, 2), "peak": pk["bf16_tflops"],
             "unit": "TFLOP/s", "frac": round(achieved / pk["bf16_tflops"], 4),
-            "traffic": traffic_from_profile(args.workload, param),
-            "kernel": "ozaki_gemm_kernel" if is_d else "bf16x_gemm_kernel",
+            "traffic": traffic_from_profile(args.workload, name_of(form, param)),
+            "kernel": {"bf16x": "bf16x_gemm_kernel", "ozaki": "ozaki_gemm_kernel",
+                       "crt": "ozaki_gemm_kernel (CRT mode) + crt_reconstruct_kernel"}[form],
             "kernel_ms": round(gemm_ms, 4), "prepare_ms": round(prep_ms, 4),
             "peak_source": "%s bf16 burst (MEASURED_PEAKS.json)" % pk["source"],
             "algorithmic_flops_per_launch": pipe_flops}
-    form_name = ("ozaki_s%d" % param) if is_d else ("bf16x%d" % param)
+    form_name = name_of(form, param)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -405,10 +442,10 @@ def run_ours(args, torch, rank, world):
                   "ms": round(plain_ms, 3), "split_speedup": round(value / world / plain_tflops, 3)},
         "accuracy": {"samples": int(len(truth)), "truth": "exact sampled dot products",
                      "plain_max_rel": plain_err[0], "plain_fro_rel": plain_err[1],
-                     "split": {str(p): {"max_rel": e[0], "fro_rel": e[1]} for p, e in errs.items()},
+                     "split": {p: {"max_rel": e[0], "fro_rel": e[1]} for p, e in errs.items()},
                      "chosen": form_name},
         "clocks": clocks,
-        "gpu_launches": args.steps * (3 if not is_d else 5),
+        "gpu_launches": args.steps * {"bf16x": 3, "ozaki": 6, "crt": 7}[form],
     }
     if rank == 0:
         line["cpu_baseline"] = (cpu_baseline(w, args.cpu_seconds) if not args.no_cpu
@@ -760,12 +797,12 @@ def run_grouped(args, torch, rank, world):
         print(json.dumps(line), flush=True)
 
 
-def traffic_from_profile(workload, param):
+def traffic_from_profile(workload, form_name):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        v = d.get("%s:%s" % (workload, param))
+        v = d.get("%s:%s" % (workload, form_name))
         if v is not None:
             return v
     return None

@@ -134,6 +134,10 @@ def core() -> ctypes.CDLL:
                                              c_void_p]
         L.gb300_host_dgemm_ozaki2.argtypes = g + [c_double, c_void_p, c_int, c_void_p, c_int,
                                                   c_double, c_void_p, c_int, c_int]
+        L.gb300_dgemm_ozaki2_prepare.argtypes = g + [c_void_p, c_int, c_void_p, c_int, c_int,
+                                                     c_void_p, c_size_t, c_void_p]
+        L.gb300_dgemm_ozaki2_run.argtypes = [c_int, c_int, c_int, c_double, c_double, c_void_p,
+                                             c_int, c_int, c_void_p, c_size_t, c_void_p]
         cg = [c_char, c_char, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int,
               c_void_p, c_void_p, c_int, c_int, c_int]
         L.gb300_cgemm.argtypes = cg + [c_void_p, c_size_t, c_void_p]
@@ -300,9 +304,11 @@ def sgemm_bf16x_noalloc(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C,
 
 def split_prepare(form, transa, transb, m, n, k, A, lda, B, ldb, param, workspace,
                   workspace_bytes, stream=0) -> int:
-    """Phase 1 of a split form ('bf16x' or 'ozaki'): split op(A), op(B) into the workspace."""
+    """Phase 1 of a split form ('bf16x', 'ozaki' or 'crt'): split op(A), op(B)
+    into the workspace."""
     L = core()
-    f = L.gb300_sgemm_bf16x_prepare if form == "bf16x" else L.gb300_dgemm_ozaki_prepare
+    f = {"bf16x": L.gb300_sgemm_bf16x_prepare, "ozaki": L.gb300_dgemm_ozaki_prepare,
+         "crt": L.gb300_dgemm_ozaki2_prepare}[form]
     return f(_b(transa), _b(transb), m, n, k, _ptr(A), lda, _ptr(B), ldb, param, _ptr(workspace),
              workspace_bytes, c_void_p(stream))
 
@@ -311,7 +317,8 @@ def split_run(form, m, n, k, alpha, beta, C, ldc, param, workspace, workspace_by
               stream=0) -> int:
     """Phase 2 of a split form: the tensor-core GEMM from a prepared workspace."""
     L = core()
-    f = L.gb300_sgemm_bf16x_run if form == "bf16x" else L.gb300_dgemm_ozaki_run
+    f = {"bf16x": L.gb300_sgemm_bf16x_run, "ozaki": L.gb300_dgemm_ozaki_run,
+         "crt": L.gb300_dgemm_ozaki2_run}[form]
     return f(m, n, k, alpha, beta, _ptr(C), ldc, param, _ptr(workspace), workspace_bytes,
              c_void_p(stream))
 
@@ -490,4 +497,5 @@ CORE_SYMBOLS = [
     "gb300_grouped_graph_create", "gb300_grouped_graph_launch", "gb300_grouped_graph_destroy",
     "gb300_cgemm", "gb300_zgemm", "gb300_host_cgemm", "gb300_host_zgemm",
     "gb300_complex_workspace_bytes", "gb300_dgemm_ozaki2", "gb300_host_dgemm_ozaki2",
+    "gb300_dgemm_ozaki2_prepare", "gb300_dgemm_ozaki2_run",
 ]

@@ -579,6 +579,24 @@ GB300_API int gb300_sgemm_bf16x_run(int m, int n, int k, float alpha, float beta
   return split_sgemm_run(m, n, k, alpha, beta, C, ldc, products, ws, ws_bytes,
                          static_cast<cudaStream_t>(stream), err);
 }
+GB300_API int gb300_dgemm_ozaki2_prepare(char ta, char tb, int m, int n, int k,
+                                         const double *A, int lda, const double *B, int ldb,
+                                         int moduli, void *ws, size_t ws_bytes, void *stream) {
+  return crt_prepare(ta, tb, m, n, k, A, lda, B, ldb, moduli, ws, ws_bytes,
+                     static_cast<cudaStream_t>(stream));
+}
+GB300_API int gb300_dgemm_ozaki2_run(int m, int n, int k, double alpha, double beta, double *C,
+                                     int ldc, int moduli, const void *ws, size_t ws_bytes,
+                                     void *stream) {
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) ||
+      (moduli != 0 && (moduli < 2 || moduli > kCrtMaxModuli)))
+    return GB300_ERR_ARG;
+  if (m == 0 || n == 0) return GB300_OK;
+  unsigned *err = device_error_word();
+  if (!err) return GB300_ERR_CUDA;
+  return crt_run(m, n, k, alpha, beta, C, ldc, moduli, ws, ws_bytes,
+                 static_cast<cudaStream_t>(stream), err);
+}
 GB300_API int gb300_dgemm_ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A,
                                         int lda, const double *B, int ldb, int slices, void *ws,
                                         size_t ws_bytes, void *stream) {

@@ -136,142 +136,172 @@ struct CrtRecParams {
   int ldc;
 };
 
-// One thread per element of C: X = sum r_g w_g in carry-save 64-bit limb
-// accumulators (r < 2^8, limbs < 2^32, at most 24 terms: no overflow), then
-// P = X - q M with q = floor(X / M) estimated from X's top bits in FP32 and
-// corrected, the symmetric residue, and one rounding to FP64.
+// The CRT reconstruction of one element from its residues r[0..N), then the C
+// update: X = sum r_g w_g in carry-save 64-bit limb accumulators (r < 2^8,
+// limbs < 2^32, at most 24 terms: no overflow), P = X - q M with q = floor(X/M)
+// estimated from X's top bits in FP32 and corrected, the symmetric residue, and
+// one rounding to FP64.
+// r_g is byte e of word[g]; the weights of unused moduli (g >= N) are zero.
+__device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli], int e,
+                                          const CrtRecParams &rp, bool &negative,
+                                          unsigned long long &top_out, int &pos_out) {
+  unsigned long long acc[kLimbs] = {0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
+#pragma unroll
+  for (int g = 0; g < kCrtMaxModuli; ++g) {
+    const unsigned r = (word[g] >> (8 * e)) & 0xffu;
+#pragma unroll
+    for (int l = 0; l < kLimbs; ++l) acc[l] += (unsigned long long)r * rp.w[g][l];
+  }
+  unsigned X[kLimbs + 1];  // X < 2^13 M < 2^201
+  {
+    unsigned long long c = 0;
+#pragma unroll
+    for (int l = 0; l < kLimbs; ++l) {
+      c += acc[l];
+      X[l] = (unsigned)c;
+      c >>= 32;
+    }
+    X[kLimbs] = (unsigned)c;
+  }
+  // 53 bits of X from bit topshift (X >> topshift < 2^53)
+  unsigned long long xt;
+  {
+    const int li = rp.topshift >> 5, o = rp.topshift & 31;
+    unsigned long long lo = 0, hi = 0;
+#pragma unroll
+    for (int l = 0; l < kLimbs + 1; ++l) {
+      if (l == li) lo = X[l];
+      if (l == li + 1) lo |= (unsigned long long)X[l] << 32;
+      if (l == li + 2) hi = X[l];
+    }
+    xt = o ? (lo >> o) | (hi << (64 - o)) : lo;
+  }
+  const unsigned q = (unsigned)((float)xt * rp.inv_mt);
+  // P = X - q M, two's complement over kLimbs + 1 limbs
+  unsigned P[kLimbs + 1];
+  {
+    long long c = 0;
+#pragma unroll
+    for (int l = 0; l < kLimbs + 1; ++l) {
+      const unsigned long long qm = l < kLimbs ? (unsigned long long)q * rp.M[l] : 0ull;
+      c += (long long)X[l] - (long long)(qm & 0xffffffffull);
+      P[l] = (unsigned)c;
+      c = (c >> 32) - (long long)(qm >> 32);
+    }
+  }
+  // add M while negative, subtract M while >= M (q was off by at most one)
+  for (int it = 0; it < 3 && (int)P[kLimbs] < 0; ++it) {
+    unsigned long long c = 0;
+#pragma unroll
+    for (int l = 0; l < kLimbs + 1; ++l) {
+      c += (unsigned long long)P[l] + (l < kLimbs ? rp.M[l] : 0u);
+      P[l] = (unsigned)c;
+      c >>= 32;
+    }
+  }
+  for (int it = 0; it < 3; ++it) {
+    bool ge = P[kLimbs] != 0;
+    if (!ge) {
+      ge = true;
+#pragma unroll
+      for (int l = kLimbs - 1; l >= 0; --l)
+        if (P[l] != rp.M[l]) { ge = P[l] > rp.M[l]; break; }
+    }
+    if (!ge) break;
+    long long c = 0;
+#pragma unroll
+    for (int l = 0; l < kLimbs + 1; ++l) {
+      c += (long long)P[l] - (long long)(l < kLimbs ? rp.M[l] : 0u);
+      P[l] = (unsigned)c;
+      c >>= 32;
+    }
+  }
+  // symmetric: P > (M - 1) / 2 stands for P - M; magnitude in mg
+  bool gt = false;
+#pragma unroll
+  for (int l = kLimbs - 1; l >= 0; --l)
+    if (P[l] != rp.half[l]) { gt = P[l] > rp.half[l]; break; }
+  unsigned mg[kLimbs];
+  if (gt) {
+    long long c = 0;
+#pragma unroll
+    for (int l = 0; l < kLimbs; ++l) {
+      c += (long long)rp.M[l] - (long long)P[l];
+      mg[l] = (unsigned)c;
+      c >>= 32;
+    }
+  } else {
+#pragma unroll
+    for (int l = 0; l < kLimbs; ++l) mg[l] = P[l];
+  }
+  negative = gt;
+  // magnitude -> FP64 with one rounding: the top 64 bits, the rest as a sticky bit
+  int tl = -1;
+#pragma unroll
+  for (int l = kLimbs - 1; l >= 0; --l)
+    if (tl < 0 && mg[l]) tl = l;
+  unsigned long long top = 0;
+  int pos = 0;
+  if (tl >= 2) {
+    unsigned a2 = 0, a1 = 0, a0 = 0;
+    bool sticky = false;
+#pragma unroll
+    for (int l = 0; l < kLimbs; ++l) {
+      if (l == tl) a2 = mg[l];
+      else if (l == tl - 1) a1 = mg[l];
+      else if (l == tl - 2) a0 = mg[l];
+      else if (l < tl - 2 && mg[l]) sticky = true;
+    }
+    const int lz = __clz(a2);
+    const unsigned long long w64 = ((unsigned long long)a2 << 32) | a1;
+    top = lz ? (w64 << lz) | ((unsigned long long)a0 >> (32 - lz)) : w64;
+    if ((lz ? (a0 << lz) : a0) != 0 || sticky) top |= 1ull;  // a0's bits below the window
+    pos = 32 * (tl - 1) - lz;
+  } else if (tl == 1) {
+    top = ((unsigned long long)mg[1] << 32) | mg[0];
+  } else if (tl == 0) {
+    top = mg[0];
+  }
+  top_out = top;
+  pos_out = pos;
+}
+
+// 4 consecutive rows of one column of C per thread: one 32-bit load per
+// modulus brings their residues (rows are contiguous in each residue plane).
+constexpr int kRecRows = 4;
 __global__ void __launch_bounds__(256)
     crt_reconstruct_kernel(const uint8_t *__restrict__ rres, const int *__restrict__ expA,
                            const int *__restrict__ expB, const __grid_constant__ CrtRecParams rp) {
   const int64_t plane = (int64_t)rp.Mp * rp.Np;
   for (int j = blockIdx.y; j < rp.n; j += gridDim.y) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= rp.m) continue;
-    unsigned long long acc[kLimbs] = {0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
-    const uint8_t *src = rres + (int64_t)j * rp.Mp + i;
-    for (int g = 0; g < rp.N; ++g) {
-      const unsigned r = src[g * plane];
+    const int i0 = (blockIdx.x * blockDim.x + threadIdx.x) * kRecRows;
+    if (i0 >= rp.m) continue;
+    // i0 + 3 < Mp (a multiple of 128) and Mp * j + i0 is a multiple of 4
+    const unsigned *src = reinterpret_cast<const unsigned *>(rres + (int64_t)j * rp.Mp + i0);
+    unsigned word[kCrtMaxModuli];
 #pragma unroll
-      for (int l = 0; l < kLimbs; ++l) acc[l] += (unsigned long long)r * rp.w[g][l];
-    }
-    unsigned X[kLimbs + 1];  // X < 2^13 M < 2^201
-    {
-      unsigned long long c = 0;
-#pragma unroll
-      for (int l = 0; l < kLimbs; ++l) {
-        c += acc[l];
-        X[l] = (unsigned)c;
-        c >>= 32;
+    for (int g = 0; g < kCrtMaxModuli; ++g) word[g] = g < rp.N ? src[g * (plane / 4)] : 0u;
+    const int eb = expB[j];
+#pragma unroll 1
+    for (int e = 0; e < kRecRows; ++e) {
+      const int i = i0 + e;
+      if (i >= rp.m) break;
+      bool neg;
+      unsigned long long top;
+      int pos;
+      crt_value(word, e, rp, neg, top, pos);
+      const int ea = expA[i];
+      double v;
+      if (ea == kNonFiniteExp || eb == kNonFiniteExp) {
+        v = __longlong_as_double(0x7ff8000000000000LL);
+      } else {
+        v = scale_pow2(__ull2double_rn(top), pos + ea + eb - rp.two_b);
+        if (neg) v = -v;
       }
-      X[kLimbs] = (unsigned)c;
+      double *c = rp.C + (int64_t)j * rp.ldc + i;
+      const double cb = (rp.beta == 1.0) ? *c : *c * rp.beta;
+      *c = cb + rp.alpha * v;
     }
-    // 53 bits of X from bit topshift (X >> topshift < 2^53)
-    unsigned long long xt;
-    {
-      const int li = rp.topshift >> 5, o = rp.topshift & 31;
-      unsigned long long lo = 0, hi = 0;
-#pragma unroll
-      for (int l = 0; l < kLimbs + 1; ++l) {
-        if (l == li) lo = X[l];
-        if (l == li + 1) lo |= (unsigned long long)X[l] << 32;
-        if (l == li + 2) hi = X[l];
-      }
-      xt = o ? (lo >> o) | (hi << (64 - o)) : lo;
-    }
-    const unsigned q = (unsigned)((float)xt * rp.inv_mt);
-    // P = X - q M, two's complement over kLimbs + 1 limbs
-    unsigned P[kLimbs + 1];
-    {
-      long long c = 0;
-#pragma unroll
-      for (int l = 0; l < kLimbs + 1; ++l) {
-        const unsigned long long qm = l < kLimbs ? (unsigned long long)q * rp.M[l] : 0ull;
-        c += (long long)X[l] - (long long)(qm & 0xffffffffull);
-        P[l] = (unsigned)c;
-        c = (c >> 32) - (long long)(qm >> 32);
-      }
-    }
-    // add M while negative, subtract M while >= M (q was off by at most one)
-    for (int it = 0; it < 3 && (int)P[kLimbs] < 0; ++it) {
-      unsigned long long c = 0;
-#pragma unroll
-      for (int l = 0; l < kLimbs + 1; ++l) {
-        c += (unsigned long long)P[l] + (l < kLimbs ? rp.M[l] : 0u);
-        P[l] = (unsigned)c;
-        c >>= 32;
-      }
-    }
-    auto geq = [&](const unsigned(&a)[kLimbs + 1], const unsigned *b) {
-      if (a[kLimbs]) return true;
-      for (int l = kLimbs - 1; l >= 0; --l)
-        if (a[l] != b[l]) return a[l] > b[l];
-      return true;
-    };
-    for (int it = 0; it < 3 && geq(P, rp.M); ++it) {
-      long long c = 0;
-#pragma unroll
-      for (int l = 0; l < kLimbs + 1; ++l) {
-        c += (long long)P[l] - (long long)(l < kLimbs ? rp.M[l] : 0u);
-        P[l] = (unsigned)c;
-        c >>= 32;
-      }
-    }
-    // symmetric: P > (M - 1) / 2 stands for P - M; magnitude in mg
-    bool gt = false;
-#pragma unroll
-    for (int l = kLimbs - 1; l >= 0; --l)
-      if (P[l] != rp.half[l]) { gt = P[l] > rp.half[l]; break; }
-    unsigned mg[kLimbs];
-    if (gt) {
-      long long c = 0;
-#pragma unroll
-      for (int l = 0; l < kLimbs; ++l) {
-        c += (long long)rp.M[l] - (long long)P[l];
-        mg[l] = (unsigned)c;
-        c >>= 32;
-      }
-    } else {
-#pragma unroll
-      for (int l = 0; l < kLimbs; ++l) mg[l] = P[l];
-    }
-    // magnitude -> FP64 with one rounding: the top 64 bits, the rest as a sticky bit
-    int tl = -1;
-#pragma unroll
-    for (int l = kLimbs - 1; l >= 0; --l)
-      if (tl < 0 && mg[l]) tl = l;
-    unsigned long long top = 0;
-    int pos = 0;
-    if (tl >= 2) {
-      unsigned a2 = 0, a1 = 0, a0 = 0;
-      bool sticky = false;
-#pragma unroll
-      for (int l = 0; l < kLimbs; ++l) {
-        if (l == tl) a2 = mg[l];
-        else if (l == tl - 1) a1 = mg[l];
-        else if (l == tl - 2) a0 = mg[l];
-        else if (l < tl - 2 && mg[l]) sticky = true;
-      }
-      const int lz = __clz(a2);
-      const unsigned long long w96hi = ((unsigned long long)a2 << 32) | a1;
-      top = lz ? (w96hi << lz) | ((unsigned long long)a0 >> (32 - lz)) : w96hi;
-      if ((lz ? (a0 << lz) : a0) != 0 || sticky) top |= 1ull;  // a0's bits below the window
-      pos = 32 * (tl - 1) - lz;
-    } else if (tl == 1) {
-      top = ((unsigned long long)mg[1] << 32) | mg[0];
-    } else if (tl == 0) {
-      top = mg[0];
-    }
-    const int ea = expA[i], eb = expB[j];
-    double v;
-    if (ea == kNonFiniteExp || eb == kNonFiniteExp) {
-      v = __longlong_as_double(0x7ff8000000000000LL);
-    } else {
-      v = scale_pow2(__ull2double_rn(top), pos + ea + eb - rp.two_b);
-      if (gt) v = -v;
-    }
-    double *c = rp.C + (int64_t)j * rp.ldc + i;
-    const double cb = (rp.beta == 1.0) ? *c : *c * rp.beta;
-    *c = cb + rp.alpha * v;
   }
 }
 
@@ -413,16 +443,12 @@ size_t crt_workspace_bytes(int m, int n, int k, int moduli) {
   return (size_t)((Mp + Np) * N * Kp * 2 + (Mp + Np) * 12 + N * Mp * Np + 2048);
 }
 
-int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
-              const double *B, int ldb, double beta, double *C, int ldc, int moduli, void *ws,
-              size_t ws_bytes, cudaStream_t st, unsigned *err) {
-  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
-  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+int crt_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
+                int ldb, int moduli, void *ws, size_t ws_bytes, cudaStream_t st) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
   const int N = resolve_moduli(moduli);
-  if (N < 2 || N > kCrtMaxModuli) return GB300_ERR_ARG;
-  if (alpha == 0.0 || k == 0)
-    return plain_dgemm('N', 'N', m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc,
-                       st, err);
+  if (ck == GB300_ERR_ARG || N < 2 || N > kCrtMaxModuli) return GB300_ERR_ARG;
+  if (ck < 0 || k == 0) return GB300_OK;
   const int b = crt_bits_for(N, k);
   if (b < 1) return GB300_ERR_ARG;  // too few moduli for this k
   const size_t need = crt_workspace_bytes(m, n, k, N);
@@ -430,10 +456,12 @@ int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double 
   const CrtLayout L = crt_layout(m, n, k, N, ws);
   if (N * L.Mp > 0x7fffffff || N * L.Np > 0x7fffffff || L.Kp > 0x7fffffff) return GB300_ERR_ARG;
   // 1. scale exponents of the rows of op(A) and columns of op(B)
-  int rc = row_scale_exponents(ta, tb, m, n, k, A, lda, B, ldb, L.amax, L.ex, L.Mp, L.Np, st);
+  const int rc =
+      row_scale_exponents(ta, tb, m, n, k, A, lda, B, ldb, L.amax, L.ex, L.Mp, L.Np, st);
   if (rc != GB300_OK) return rc;
   // 2. residues
   CrtModParams mp;
+  std::memset(&mp, 0, sizeof(mp));
   mp.N = N;
   mp.b = b;
   for (int i = 0; i < kCrtMaxModuli; ++i) {
@@ -454,7 +482,23 @@ int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double 
       A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, L.ex, mp, L.As);
   crt_residue_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Np)), 256, 0, st>>>(
       B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, L.ex + L.Mp, mp, L.Bs);
-  if (cudaGetLastError() != cudaSuccess) return GB300_ERR_CUDA;
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int crt_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int moduli,
+            const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err) {
+  const int N = resolve_moduli(moduli);
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || N < 2 || N > kCrtMaxModuli)
+    return GB300_ERR_ARG;
+  if (m == 0 || n == 0) return GB300_OK;
+  if (alpha == 0.0 || k == 0)
+    return plain_dgemm('N', 'N', m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc,
+                       st, err);
+  const int b = crt_bits_for(N, k);
+  if (b < 1) return GB300_ERR_ARG;
+  const size_t need = crt_workspace_bytes(m, n, k, N);
+  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
+  const CrtLayout L = crt_layout(m, n, k, N, const_cast<void *>(ws));
   // 3. one exact integer GEMM per modulus
   OzakiGemmArgs a;
   a.m = m; a.n = n; a.S = N; a.mode = 1;
@@ -462,7 +506,7 @@ int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double 
   a.As = L.As; a.Bs = L.Bs;
   a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc;
   a.expA = L.ex; a.expB = L.ex + L.Mp; a.res = nullptr; a.rres = L.rres; a.mods = kModuli;
-  rc = ozaki_gemm_launch(a, st, err);
+  const int rc = ozaki_gemm_launch(a, st, err);
   if (rc != GB300_OK) return rc;
   // 4. reconstruction and the C update
   CrtRecParams rp;
@@ -493,9 +537,25 @@ int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double 
     rp.inv_mt = 1.0f / (float)mt.l[0];
   }
   rp.alpha = alpha; rp.beta = beta; rp.C = C; rp.ldc = ldc;
-  const dim3 grid((unsigned)((m + 255) / 256), (unsigned)(n < 65535 ? n : 65535));
+  const dim3 grid((unsigned)((m + 256 * kRecRows - 1) / (256 * kRecRows)),
+                  (unsigned)(n < 65535 ? n : 65535));
   crt_reconstruct_kernel<<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+              const double *B, int ldb, double beta, double *C, int ldc, int moduli, void *ws,
+              size_t ws_bytes, cudaStream_t st, unsigned *err) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  const int N = resolve_moduli(moduli);
+  if (N < 2 || N > kCrtMaxModuli) return GB300_ERR_ARG;
+  if (alpha == 0.0 || k == 0)
+    return plain_dgemm('N', 'N', m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc,
+                       st, err);
+  int rc = crt_prepare(ta, tb, m, n, k, A, lda, B, ldb, N, ws, ws_bytes, st);
+  if (rc != GB300_OK) return rc;
+  return crt_run(m, n, k, alpha, beta, C, ldc, N, ws, ws_bytes, st, err);
 }
 
 }  // namespace gb300

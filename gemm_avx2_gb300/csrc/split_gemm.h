@@ -51,6 +51,12 @@ int crt_bits_for(int moduli, int k);
 int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
               const double *B, int ldb, double beta, double *C, int ldc, int moduli, void *ws,
               size_t ws_bytes, cudaStream_t st, unsigned *err);
+// Two phases: prepare writes the exponents and residue operands, run does the
+// per-modulus GEMMs, the reconstruction and the C update.
+int crt_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
+                int ldb, int moduli, void *ws, size_t ws_bytes, cudaStream_t st);
+int crt_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int moduli,
+            const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err);
 
 int ozaki_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                 const double *B, int ldb, double beta, double *C, int ldc, int slices, void *ws,

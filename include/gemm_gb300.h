@@ -303,6 +303,16 @@ int gb300_dgemm_ozaki2(char transa, char transb, int m, int n, int k, double alp
 int gb300_host_dgemm_ozaki2(char transa, char transb, int m, int n, int k, double alpha,
                             const double *a, int lda, const double *b, int ldb, double beta,
                             double *c, int ldc, int moduli);
+/* Two phases of gb300_dgemm_ozaki2 on a caller workspace: prepare writes the
+ * scale exponents and the residue operands of op(A) and op(B); run performs
+ * the per-modulus GEMMs, the reconstruction and C = alpha*AB + beta*C (same m,
+ * n, k, moduli; run may repeat with other alpha, beta, C). */
+int gb300_dgemm_ozaki2_prepare(char transa, char transb, int m, int n, int k, const double *A,
+                               int lda, const double *B, int ldb, int moduli, void *workspace,
+                               size_t workspace_bytes, void *stream);
+int gb300_dgemm_ozaki2_run(int m, int n, int k, double alpha, double beta, double *C, int ldc,
+                           int moduli, const void *workspace, size_t workspace_bytes,
+                           void *stream);
 
 /* Workspace needed by the split forms for one call of the given shape.
  * kind = 0: sgemm_bf16x with `param` = products; kind = 1: dgemm_ozaki with
