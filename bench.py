@@ -532,22 +532,46 @@ def run_complex(args, torch, rank, world):
 
     plain_err, plain_ms = measure(g.CPLX_4M, 0, 1 if p == "z" else 3)
     m3_err, m3_ms = measure(g.CPLX_3M, 0, 1 if p == "z" else 3)
-    cands = list(range(6, 13)) if p == "z" else [3, 6]
-    errs, chosen = {}, None
-    for param in cands:
-        C.copy_(C0)
-        assert call(g.CPLX_SPLIT, param, C) == g.OK
+    # ZGEMM: the CRT form's moduli and the slice form's slice counts; CGEMM:
+    # BF16xP products.  Per scheme the smallest candidate at equal error to 4M;
+    # of two qualifying schemes the faster one.
+    schemes = [(g.CPLX_CRT, list(range(11, 25))), (g.CPLX_SPLIT, list(range(6, 13)))] \
+        if p == "z" else [(g.CPLX_SPLIT, [3, 6])]
+
+    def cname(meth, prm):
+        return ("crt_n%d" if meth == g.CPLX_CRT else "ozaki_s%d" if p == "z" else "bf16x%d") % prm
+
+    errs, qualified = {}, []
+    for meth, cands in schemes:
+        for prm in cands:
+            C.copy_(C0)
+            if call(meth, prm, C) != g.OK:
+                continue
+            torch.cuda.synchronize()
+            e = rel_err_c(C[cols, rows].cpu().numpy(), truth)
+            errs[cname(meth, prm)] = e
+            if e[0] <= plain_err[0] and e[1] <= plain_err[1]:
+                qualified.append((meth, prm))
+                break
+    if not qualified:
+        qualified.append((schemes[-1][0], schemes[-1][1][-1]))
+    best = None
+    for meth, prm in qualified:
+        call(meth, prm, C)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        for _ in range(2):
+            call(meth, prm, C)
+        a1.record()
         torch.cuda.synchronize()
-        errs[param] = rel_err_c(C[cols, rows].cpu().numpy(), truth)
-        if errs[param][0] <= plain_err[0] and errs[param][1] <= plain_err[1]:
-            chosen = param
-            break
-    param = chosen if chosen is not None else cands[-1]
-    need = g.complex_workspace_bytes(p, g.CPLX_SPLIT, w["tb"], m, n, k, param)
+        if best is None or a0.elapsed_time(a1) < best[0]:
+            best = (a0.elapsed_time(a1), meth, prm)
+    method, param = best[1], best[2]
+    need = g.complex_workspace_bytes(p, method, w["tb"], m, n, k, param)
     ws = torch.empty(need, dtype=torch.uint8, device="cuda")
 
     for _ in range(args.warmup):
-        assert call(g.CPLX_SPLIT, param, C, ws.data_ptr(), need) == g.OK
+        assert call(method, param, C, ws.data_ptr(), need) == g.OK
     torch.cuda.synchronize()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
     sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
@@ -560,7 +584,7 @@ def run_complex(args, torch, rank, world):
     t0.record()
     for s_ in range(args.steps):
         evs[s_][0].record()
-        assert call(g.CPLX_SPLIT, param, C, ws.data_ptr(), need) == g.OK
+        assert call(method, param, C, ws.data_ptr(), need) == g.OK
         evs[s_][1].record()
     t1.record()
     torch.cuda.synchronize()
@@ -584,28 +608,29 @@ def run_complex(args, torch, rank, world):
             ah, bh, ch = hA.numpy(), hB.numpy(), hC.numpy()
             for _ in range(2):
                 assert g.host_complex(p, w["ta"], w["tb"], m, n, k, w["alpha"], ah, m, bh, k,
-                                      w["beta"], ch, m, method=g.CPLX_SPLIT, param=param) == g.OK
+                                      w["beta"], ch, m, method=method, param=param) == g.OK
             steps_e2e = max(3, min(args.steps, 10))
             t = time.perf_counter()
             for _ in range(steps_e2e):
                 assert g.host_complex(p, w["ta"], w["tb"], m, n, k, w["alpha"], ah, m, bh, k,
-                                      w["beta"], ch, m, method=g.CPLX_SPLIT, param=param) == g.OK
+                                      w["beta"], ch, m, method=method, param=param) == g.OK
             dts = (time.perf_counter() - t) / steps_e2e
             esz = 16 if p == "z" else 8
             e2e = {"value": round(flops / dts / 1e12, 3), "unit": "TFLOP/s",
                    "h2d_bytes_per_step": (m * k + k * n + m * n) * esz,
                    "d2h_bytes_per_step": m * n * esz, "ms_per_step": round(dts * 1e3, 3),
-                   "api": "gb300_host_%sgemm (GB300_CPLX_SPLIT)" % p,
+                   "api": "gb300_host_%sgemm (%s)" % (
+                       p, "GB300_CPLX_CRT" if method == g.CPLX_CRT else "GB300_CPLX_SPLIT"),
                    "transfer": "pinned host buffers read and written in place over the "
                                "coherent CPU-GPU link"}
         except Exception as ex:  # noqa: BLE001
             e2e = {"value": None, "error": repr(ex)}
 
     pk = peaks()
-    products = (param * (param + 1)) // 2 if p == "z" else param
+    products = param if (p == "c" or method == g.CPLX_CRT) else (param * (param + 1)) // 2
     pipe_flops = products * flops
     achieved = pipe_flops / (step_ms / 1e3) / 1e12
-    form_name = ("ozaki_s%d" % param) if p == "z" else ("bf16x%d" % param)
+    form_name = cname(method, param)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -622,7 +647,8 @@ def run_complex(args, torch, rank, world):
         "roofline": {"bound": "tensor", "achieved": round(achieved, 2),
                      "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": round(achieved / pk["bf16_tflops"], 4), "traffic": None,
-                     "kernel": "ozaki_gemm_kernel" if p == "z" else "bf16x_gemm_kernel",
+                     "kernel": ("ozaki_gemm_kernel (CRT mode)" if method == g.CPLX_CRT else
+                                "ozaki_gemm_kernel" if p == "z" else "bf16x_gemm_kernel"),
                      "kernel_ms": round(step_ms, 4),
                      "timing": "whole step (operand embedding, split kernels and the tcgen05 "
                                "GEMM): a lower bound on the GEMM kernel's rate",
@@ -636,10 +662,11 @@ def run_complex(args, torch, rank, world):
                       "ms": round(m3_ms, 3), "max_rel": m3_err[0], "fro_rel": m3_err[1]},
         "accuracy": {"samples": int(len(truth)), "truth": "exact sampled complex dot products",
                      "plain_max_rel": plain_err[0], "plain_fro_rel": plain_err[1],
-                     "split": {str(q): {"max_rel": e[0], "fro_rel": e[1]} for q, e in errs.items()},
+                     "split": {q: {"max_rel": e[0], "fro_rel": e[1]} for q, e in errs.items()},
                      "chosen": form_name},
         "clocks": clocks,
-        "gpu_launches": args.steps * ((1 + 6) if p == "z" else (1 + 3)),
+        # per step: the operand embedding, then the form's own kernels
+        "gpu_launches": args.steps * (1 + (7 if method == g.CPLX_CRT else 6 if p == "z" else 3)),
     }
     if rank == 0:
         line["cpu_baseline"] = (cpu_baseline_complex(w, args.cpu_seconds) if not args.no_cpu

@@ -42,6 +42,7 @@ ERR_NOALLOC_LIMIT = 7
 CPLX_4M = 0
 CPLX_3M = 1
 CPLX_SPLIT = 2
+CPLX_CRT = 3
 
 _core = None
 _drop = {}
@@ -381,6 +382,7 @@ def selftest_wait_timeout(poll_limit: int = 4096) -> int:
 TUNE_BF16X_CHUNK = 1
 TUNE_BF16X = 0     # autotuner kinds
 TUNE_OZAKI = 1
+TUNE_CRT = 2
 
 
 def autotune(kind, transa, transb, m, n, k, A, lda, B, ldb, stream=0):

@@ -288,7 +288,7 @@ static int host_complex(char ta, char tb, int m, int n, int k, const T *alpha, c
     cudaMemcpy(&word, s->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
     return word ? GB300_ERR_TIMEOUT : GB300_OK;
   };
-  if (method == GB300_CPLX_SPLIT && host_direct_ok(a, b, c)) {
+  if ((method == GB300_CPLX_SPLIT || method == GB300_CPLX_CRT) && host_direct_ok(a, b, c)) {
     // the split method reads A and B once (pack and split kernels) and C once
     // (epilogue): it runs on the caller's memory over the coherent link
     return finish(run(a, lda, b, ldb, c, ldc));
@@ -429,6 +429,7 @@ GB300_API int gb300_sgemm(char ta, char tb, int m, int n, int k, float alpha, co
 
 // ---------------------------------------------------------------- complex
 static bool complex_param_ok(bool dbl, int method, int param) {
+  if (method == GB300_CPLX_CRT) return dbl && (param == 0 || (param >= 2 && param <= kCrtMaxModuli));
   if (method != GB300_CPLX_SPLIT) return true;
   return dbl ? (param == 0 || (param >= 2 && param <= kOzakiMaxSlices))
              : (param == 0 || param == 3 || param == 6);
@@ -872,7 +873,7 @@ GB300_API int gb300_selftest_wait_timeout(unsigned poll_limit) {
 
 GB300_API int gb300_autotune(int kind, char ta, char tb, int m, int n, int k, const void *A,
                              int lda, const void *B, int ldb, void *stream, int *chosen) {
-  if (kind != 0 && kind != 1) return GB300_ERR_ARG;
+  if (kind < 0 || kind > 2) return GB300_ERR_ARG;
   if (check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1) != GB300_OK || k == 0)
     return GB300_ERR_ARG;
   unsigned *err = device_error_word();
@@ -881,10 +882,11 @@ GB300_API int gb300_autotune(int kind, char ta, char tb, int m, int n, int k, co
                   chosen);
 }
 GB300_API int gb300_tune_lookup(int kind, int m, int n, int k, int *param, int *chunk) {
-  if (kind != 0 && kind != 1) return GB300_ERR_ARG;
+  if (kind < 0 || kind > 2) return GB300_ERR_ARG;
   int p = 0, c = 0;
   if (kind == 0) bf16x_resolve(m, n, k, &p, &c);
-  else p = ozaki_default_slices(m, n, k);
+  else if (kind == 1) p = ozaki_default_slices(m, n, k);
+  else p = crt_default_moduli(m, n, k);
   if (param) *param = p;
   if (chunk) *chunk = c;
   return tune_lookup(kind, m, n, k, nullptr, nullptr) ? GB300_OK : GB300_ERR_UNSUPPORTED;

@@ -57,7 +57,8 @@ static int ilog2(int x) {
 
 static std::string tune_key(int kind, int m, int n, int k) {
   char buf[96];
-  snprintf(buf, sizeof buf, "%s:%d:%d:%d", kind == 0 ? "bf16x" : "ozaki", ilog2(m), ilog2(n),
+  snprintf(buf, sizeof buf, "%s:%d:%d:%d", kind == 0 ? "bf16x" : kind == 1 ? "ozaki" : "crt",
+           ilog2(m), ilog2(n),
            ilog2(k));
   return buf;
 }
@@ -149,7 +150,7 @@ int measure(const void *t, bool t_double, int m, int n, const double *ref, doubl
 
 int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int lda,
              const void *B, int ldb, cudaStream_t st, unsigned *err, int *chosen) {
-  if (kind != 0 && kind != 1) return GB300_ERR_ARG;
+  if (kind < 0 || kind > 2) return GB300_ERR_ARG;
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
   if (ck != GB300_OK || k == 0) return ck == GB300_ERR_ARG ? ck : GB300_ERR_ARG;
   const bool an = notrans(ta), bn = notrans(tb);
@@ -161,6 +162,9 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
   if (kind == 0) {
     const size_t w6 = split_workspace_bytes(0, m, n, k, 6);
     if (w6 > ws_need) ws_need = w6;
+  } else if (kind == 2) {
+    const size_t wc = crt_workspace_bytes(m, n, k, kCrtMaxModuli);
+    if (wc > ws_need) ws_need = wc;
   }
   if (!cref.alloc(mn * 8) || !ctest.alloc(mn * (kind == 0 ? 4 : 8)) || !ws.alloc(ws_need) ||
       !dstats.alloc(3 * sizeof(double)))
@@ -203,6 +207,10 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
     if (form == 0)
       return plain_dgemm(ta, tb, m, n, k, 1.0, static_cast<const double *>(A), lda,
                          static_cast<const double *>(B), ldb, 0.0, Ct, m, st, err);
+    if (kind == 2)
+      return crt_dgemm(ta, tb, m, n, k, 1.0, static_cast<const double *>(A), lda,
+                       static_cast<const double *>(B), ldb, 0.0, Ct, m, param, ws.p, ws_need, st,
+                       err);
     return ozaki_dgemm(ta, tb, m, n, k, 1.0, static_cast<const double *>(A), lda,
                        static_cast<const double *>(B), ldb, 0.0, Ct, m, param, ws.p, ws_need, st,
                        err);
@@ -225,7 +233,7 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
 
   Stats plain{};
   if ((rc = run(0, 0, 0)) != GB300_OK) return rc;
-  if ((rc = measure(ctest.p, kind == 1, m, n, Cr, stats, st, &plain)) != GB300_OK) return rc;
+  if ((rc = measure(ctest.p, kind != 0, m, n, Cr, stats, st, &plain)) != GB300_OK) return rc;
 
   TuneEntry best;
   bool found = false;
@@ -245,6 +253,21 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
         }
       }
     if (!found) { best.param = 6; best.chunk = 2; }  // most accurate candidate
+  } else if (kind == 2) {
+    // the smallest moduli count at equal error is also the fastest
+    for (int N = 11; N <= kCrtMaxModuli; ++N) {
+      if (crt_bits_for(N, k) < 1) continue;
+      double ms = 0;
+      Stats e{};
+      if ((rc = timed(N, 0, &ms)) != GB300_OK) return rc;
+      if ((rc = measure(ctest.p, true, m, n, Cr, stats, st, &e)) != GB300_OK) return rc;
+      if (e.max_rel <= plain.max_rel && e.fro <= plain.fro) {
+        found = true;
+        best.param = N; best.ms = ms; best.err_max = e.max_rel; best.err_fro = e.fro;
+        break;
+      }
+    }
+    if (!found) best.param = kCrtMaxModuli;
   } else {
     for (int S = 4; S <= 12; ++S) {
       double ms = 0;
@@ -317,9 +340,12 @@ int tune_cache_load(const char *path, int *loaded) {
                &e.plain_fro) != 8)
       continue;
     const bool bx = strncmp(key, "bf16x:", 6) == 0, oz = strncmp(key, "ozaki:", 6) == 0;
+    const bool cr = strncmp(key, "crt:", 4) == 0;
     if (bx && (e.param == 3 || e.param == 6) && e.chunk >= 0 && e.chunk <= 64)
       add[key] = e;
     else if (oz && e.param >= 2 && e.param <= kOzakiMaxSlices)
+      add[key] = e;
+    else if (cr && e.param >= 2 && e.param <= kCrtMaxModuli)
       add[key] = e;
   }
   fclose(f);

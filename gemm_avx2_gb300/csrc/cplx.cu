@@ -25,6 +25,7 @@
 //        real products to complex C).
 //  SPLIT the 4M embedding on the tensor-core split forms: BF16xP for CGEMM
 //        (param = products), Ozaki slices for ZGEMM (param = slices).
+//  CRT   (ZGEMM only) the 4M embedding on the CRT form (param = moduli).
 // A complex alpha (nonzero imaginary part) is folded into Ahat, one complex
 // rounding per element of op(A); a complex beta scales C first.  Real alpha and
 // beta reach the real kernel's epilogue unchanged.
@@ -228,8 +229,10 @@ CxLayout cx_layout(size_t e, bool is_double, int method, char tb, int m, int n, 
       L.b_off = off;
       off = al256(off + (size_t)(L.ldbh * n) * e);
     }
-    if (method == GB300_CPLX_SPLIT) {
-      L.s_bytes = split_workspace_bytes(is_double ? 1 : 0, 2 * m, n, 2 * k, param);
+    if (method == GB300_CPLX_SPLIT || method == GB300_CPLX_CRT) {
+      L.s_bytes = method == GB300_CPLX_CRT
+                      ? crt_workspace_bytes(2 * m, n, 2 * k, param)
+                      : split_workspace_bytes(is_double ? 1 : 0, 2 * m, n, 2 * k, param);
       if (!L.s_bytes) return L;
       L.s_off = off;
       off = al256(off + L.s_bytes);
@@ -241,7 +244,7 @@ CxLayout cx_layout(size_t e, bool is_double, int method, char tb, int m, int n, 
 }
 
 int cx_check(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc, int method) {
-  if (method < GB300_CPLX_4M || method > GB300_CPLX_SPLIT) return GB300_ERR_ARG;
+  if (method < GB300_CPLX_4M || method > GB300_CPLX_CRT) return GB300_ERR_ARG;
   const int arows = cx_trans(ta) ? k : m, brows = cx_trans(tb) ? n : k;
   if (m < 0 || n < 0 || k < 0 || lda < (arows > 1 ? arows : 1) ||
       ldb < (brows > 1 ? brows : 1) || ldc < (m > 1 ? m : 1))
@@ -258,6 +261,7 @@ int complex_gemm(char ta, char tb, int m, int n, int k, const T *alpha, const T 
                  void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err) {
   const int ck = cx_check(ta, tb, m, n, k, lda, ldb, ldc, method);
   if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  if (method == GB300_CPLX_CRT && sizeof(T) != 8) return GB300_ERR_ARG;  // ZGEMM only
   const T ar = alpha[0], ai = alpha[1], br = beta[0], bi = beta[1];
   const bool alpha_zero = ar == T(0) && ai == T(0);
   if (alpha_zero || k == 0) {
@@ -328,9 +332,13 @@ int complex_gemm(char ta, char tb, int m, int n, int k, const T *alpha, const T 
     return real_plain<T>('N', tbh, M2, n, K2, alpha_r, Ah, (int)L.lde, Bh, (int)ldbh, beta_r, C,
                          ldc2, st, err);
   void *sws = base + L.s_off;
-  if constexpr (sizeof(T) == 8)
+  if constexpr (sizeof(T) == 8) {
+    if (method == GB300_CPLX_CRT)
+      return crt_dgemm('N', 'N', M2, n, K2, alpha_r, Ah, (int)L.lde, Bh, (int)ldbh, beta_r, C,
+                       ldc2, param, sws, L.s_bytes, st, err);
     return ozaki_dgemm('N', 'N', M2, n, K2, alpha_r, Ah, (int)L.lde, Bh, (int)ldbh, beta_r, C,
                        ldc2, param, sws, L.s_bytes, st, err);
+  }
   else
     return split_sgemm('N', 'N', M2, n, K2, alpha_r, Ah, (int)L.lde, Bh, (int)ldbh, beta_r, C,
                        ldc2, param, sws, L.s_bytes, st, err);
@@ -340,7 +348,8 @@ int complex_gemm(char ta, char tb, int m, int n, int k, const T *alpha, const T 
 
 size_t complex_workspace_bytes(int is_double, int method, char tb, int m, int n, int k,
                                int param) {
-  if (m <= 0 || n <= 0 || k <= 0 || method < GB300_CPLX_4M || method > GB300_CPLX_SPLIT) return 0;
+  if (m <= 0 || n <= 0 || k <= 0 || method < GB300_CPLX_4M || method > GB300_CPLX_CRT) return 0;
+  if (method == GB300_CPLX_CRT && !is_double) return 0;
   const CxLayout L =
       cx_layout(is_double ? 8 : 4, is_double != 0, method, tb, m, n, k, param);
   return L.ok ? L.total : 0;

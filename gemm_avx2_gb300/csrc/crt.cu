@@ -408,9 +408,17 @@ CrtLayout crt_layout(int m, int n, int k, int N, void *ws) {
   return L;
 }
 
-int resolve_moduli(int moduli) { return moduli > 0 ? moduli : kCrtDefaultModuli; }
+// moduli 0: the autotuned count for the shape class, else the default
+int resolve_moduli(int moduli, int m = 0, int n = 0, int k = 0) {
+  if (moduli > 0) return moduli;
+  int N = 0;
+  if (m > 0 && n > 0 && k > 0 && tune_lookup(2, m, n, k, &N, nullptr)) return N;
+  return kCrtDefaultModuli;
+}
 
 }  // namespace
+
+int crt_default_moduli(int m, int n, int k) { return resolve_moduli(0, m, n, k); }
 
 int crt_bits_for(int moduli, int k) {
   const int N = resolve_moduli(moduli);
@@ -435,7 +443,7 @@ int crt_bits_for(int moduli, int k) {
 
 size_t crt_workspace_bytes(int m, int n, int k, int moduli) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
-  const int N = resolve_moduli(moduli);
+  const int N = resolve_moduli(moduli, m, n, k);
   if (N < 2 || N > kCrtMaxModuli) return 0;
   const int64_t Kp = (k + kSplitBK - 1) / kSplitBK * kSplitBK;
   const int64_t Mp = (m + kSplitBM - 1) / kSplitBM * kSplitBM;
@@ -446,7 +454,7 @@ size_t crt_workspace_bytes(int m, int n, int k, int moduli) {
 int crt_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
                 int ldb, int moduli, void *ws, size_t ws_bytes, cudaStream_t st) {
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
-  const int N = resolve_moduli(moduli);
+  const int N = resolve_moduli(moduli, m, n, k);
   if (ck == GB300_ERR_ARG || N < 2 || N > kCrtMaxModuli) return GB300_ERR_ARG;
   if (ck < 0 || k == 0) return GB300_OK;
   const int b = crt_bits_for(N, k);
@@ -487,7 +495,7 @@ int crt_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda,
 
 int crt_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int moduli,
             const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err) {
-  const int N = resolve_moduli(moduli);
+  const int N = resolve_moduli(moduli, m, n, k);
   if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || N < 2 || N > kCrtMaxModuli)
     return GB300_ERR_ARG;
   if (m == 0 || n == 0) return GB300_OK;
@@ -548,7 +556,7 @@ int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double 
               size_t ws_bytes, cudaStream_t st, unsigned *err) {
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
   if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
-  const int N = resolve_moduli(moduli);
+  const int N = resolve_moduli(moduli, m, n, k);
   if (N < 2 || N > kCrtMaxModuli) return GB300_ERR_ARG;
   if (alpha == 0.0 || k == 0)
     return plain_dgemm('N', 'N', m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc,

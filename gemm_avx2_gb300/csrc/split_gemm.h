@@ -48,6 +48,8 @@ int row_scale_exponents(char ta, char tb, int m, int n, int k, const double *A, 
 // computed exactly as residues modulo `moduli` (0 = tuned / 16) BF16 GEMMs.
 size_t crt_workspace_bytes(int m, int n, int k, int moduli);
 int crt_bits_for(int moduli, int k);
+// Moduli count for a shape class (autotune cache, falls back to 16).
+int crt_default_moduli(int m, int n, int k);
 int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
               const double *B, int ldb, double beta, double *C, int ldc, int moduli, void *ws,
               size_t ws_bytes, cudaStream_t st, unsigned *err);

@@ -257,14 +257,16 @@ int gb300_strmm(char side, char uplo, char transa, char diag, int m, int n, floa
  *                           part's error scales with |Re A + Im A| |Re B + Im B|);
  *   method GB300_CPLX_SPLIT the embedded problem on the tensor-core split forms:
  *                           6xBF16/3xBF16 for CGEMM (param = products, 0 =
- *                           tuned), Ozaki for ZGEMM (param = slices, 0 = tuned).
+ *                           tuned), Ozaki for ZGEMM (param = slices, 0 = tuned);
+ *   method GB300_CPLX_CRT   ZGEMM only: the embedded problem on the CRT form
+ *                           of gb300_dgemm_ozaki2 (param = moduli, 0 = tuned).
  * Same semantics as the real path otherwise: beta*C first (beta == 0 still
  * multiplies), alpha == 0 or k == 0 reads neither A nor B.  A complex alpha is
  * folded into op(A) (one rounding per element), a complex beta scales C first.
  * workspace NULL: a library-owned buffer per stream; otherwise at least
  * gb300_complex_workspace_bytes(...) bytes of device memory.
  * ---------------------------------------------------------------------- */
-enum { GB300_CPLX_4M = 0, GB300_CPLX_3M = 1, GB300_CPLX_SPLIT = 2 };
+enum { GB300_CPLX_4M = 0, GB300_CPLX_3M = 1, GB300_CPLX_SPLIT = 2, GB300_CPLX_CRT = 3 };
 size_t gb300_complex_workspace_bytes(int is_double, int method, char transb, int m, int n,
                                      int k, int param);
 int gb300_cgemm(char transa, char transb, int m, int n, int k, const float *alpha,
@@ -335,16 +337,17 @@ int gb300_selftest_wait_timeout(unsigned poll_limit);
 /* Autotuner (replaces the reference's compile-time tune headers dgemm_tune.h /
  * sgemm_tune.h, src/gemm_set_parameters.h:1-61).  kind 0 = BF16xP SGEMM
  * (chooses products 3/6 and the hi*hi chunk length), kind 1 = Ozaki DGEMM
- * (chooses the slice count 4..12).  gb300_autotune runs the candidates on the
- * given device operands (FP32 for kind 0, FP64 for kind 1) and keeps the fastest
+ * (chooses the slice count 4..12), kind 2 = CRT DGEMM (gb300_dgemm_ozaki2;
+ * chooses the moduli count 11..24).  gb300_autotune runs the candidates on the
+ * given device operands (FP32 for kind 0, FP64 for kinds 1, 2) and keeps the fastest
  * whose max and Frobenius relative errors against a near-exact FP64 reference
  * (the Ozaki form with 12 slices) do not exceed the plain kernel's; the result
  * is cached for the shape class (floor(log2) of m, n, k) and used whenever a
- * split entry point gets products = 0 / slices = 0.  It allocates temporary
+ * split entry point gets products = 0 / slices = 0 / moduli = 0.  It allocates temporary
  * device memory and synchronises `stream`.
  * gb300_tune_lookup: the parameters products/slices = 0 resolve to for a
  * shape (GB300_OK if a tuned entry exists, GB300_ERR_UNSUPPORTED if the
- * defaults apply: 6 products, chunk 4, 8 slices).
+ * defaults apply: 6 products, chunk 4, 8 slices, 16 moduli).
  * Cache file: gb300_tune_cache_save/_load (path NULL: $GB300_TUNE_CACHE, else
  * $HOME/.gemm_gb300_tune.json); loading skips malformed or out-of-range
  * entries and returns GB300_ERR_ARG for an unreadable file, keeping the cache. */

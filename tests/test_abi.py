@@ -86,7 +86,12 @@ def test_complex_argument_errors_need_no_gpu(p):
     assert cd(p, "R", "N", 8, 4, 4, 1, 0, 7, 0, 4, 0, 0, 8) == g.ERR_ARG       # 'R' keeps m rows
     assert cd(p, "N", "C", 8, 4, 4, 1, 0, 8, 0, 3, 0, 0, 8) == g.ERR_ARG       # ldb < n
     assert cd(p, "N", "N", 8, 4, 4, 1, 0, 8, 0, 4, 0, 0, 7) == g.ERR_ARG       # ldc < m
-    assert cd(p, "N", "N", 8, 4, 4, 1, 0, 8, 0, 4, 0, 0, 8, method=3) == g.ERR_ARG
+    assert cd(p, "N", "N", 8, 4, 4, 1, 0, 8, 0, 4, 0, 0, 8, method=4) == g.ERR_ARG
+    if p == "c":  # the CRT form is FP64 only
+        assert cd(p, "N", "N", 8, 4, 4, 1, 0, 8, 0, 4, 0, 0, 8, method=g.CPLX_CRT) == g.ERR_ARG
+    else:
+        assert cd(p, "N", "N", 8, 4, 4, 1, 0, 8, 0, 4, 0, 0, 8, method=g.CPLX_CRT,
+                  param=25) == g.ERR_ARG
     bad = 5 if p == "c" else 13
     assert cd(p, "N", "N", 8, 4, 4, 1, 0, 8, 0, 4, 0, 0, 8, method=g.CPLX_SPLIT,
               param=bad) == g.ERR_ARG
@@ -157,6 +162,7 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
     # defaults without a tuned entry
     assert g.tune_lookup(g.TUNE_OZAKI, 1000, 1000, 1000) == (g.ERR_UNSUPPORTED, 8, 0)
     assert g.tune_lookup(g.TUNE_BF16X, 1000, 1000, 1000) == (g.ERR_UNSUPPORTED, 6, 0)
+    assert g.tune_lookup(g.TUNE_CRT, 1000, 1000, 1000) == (g.ERR_UNSUPPORTED, 16, 0)
     # a hand-written cache file with good, malformed and out-of-range lines
     f = tmp_path / "tune.json"
     f.write_text('{"version": 1, "entries": [\n'
@@ -166,8 +172,16 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
                  '"err_fro": 1e-7, "plain_max": 2e-5, "plain_fro": 1e-6},\n'
                  '  {"key": "ozaki:8:8:8", "param": 99, "chunk": 0, "ms": 1, "err_max": 0, '
                  '"err_fro": 0, "plain_max": 0, "plain_fro": 0},\n'
+                 '  {"key": "crt:9:9:9", "param": 14, "chunk": 0, "ms": 1, "err_max": 1e-14, '
+                 '"err_fro": 1e-16, "plain_max": 2e-14, "plain_fro": 1e-15},\n'
+                 '  {"key": "crt:8:8:8", "param": 25, "chunk": 0, "ms": 1, "err_max": 0, '
+                 '"err_fro": 0, "plain_max": 0, "plain_fro": 0},\n'
                  '  garbage line\n]}\n')
-    assert g.tune_cache_load(str(f)) == (g.OK, 2)
+    assert g.tune_cache_load(str(f)) == (g.OK, 3)
+    assert g.tune_lookup(g.TUNE_CRT, 1000, 600, 700) == (g.OK, 14, 0)
+    assert g.tune_lookup(g.TUNE_CRT, 300, 300, 300)[0] == g.ERR_UNSUPPORTED   # 25 rejected
+    # moduli = 0 sizes the workspace with the tuned count
+    assert g.split_workspace_bytes(2, 1000, 600, 700, 0) == g.split_workspace_bytes(2, 1000, 600, 700, 14)
     assert g.tune_lookup(g.TUNE_OZAKI, 1000, 600, 700) == (g.OK, 10, 0)      # log2 buckets 9
     assert g.tune_lookup(g.TUNE_BF16X, 512, 1023, 600) == (g.OK, 3, 8)
     assert g.tune_lookup(g.TUNE_OZAKI, 300, 300, 300)[0] == g.ERR_UNSUPPORTED  # rejected entry
@@ -175,7 +189,7 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
     out = tmp_path / "saved.json"
     assert g.tune_cache_save(str(out)) == g.OK
     g.tune_cache_clear()
-    assert g.tune_cache_load(str(out)) == (g.OK, 2)
+    assert g.tune_cache_load(str(out)) == (g.OK, 3)
     assert g.tune_cache_load(str(tmp_path / "missing.json"))[0] == g.ERR_ARG
     assert g.tune_lookup(g.TUNE_OZAKI, 1000, 600, 700) == (g.OK, 10, 0)        # cache kept
     g.tune_cache_clear()

@@ -37,6 +37,29 @@ def test_autotune_ozaki_and_use(orc):
     g.tune_cache_clear()
 
 
+def test_autotune_crt_and_use(orc):
+    g.tune_cache_clear()
+    m, n, k = 300, 260, 700
+    A = orc.spread((m, k), 52, 0, 2.0)
+    B = orc.spread((n, k), 52, 1, 2.0)          # transb = T
+    dA, dB = to_dev(A), to_dev(B)
+    rc, N = g.autotune(g.TUNE_CRT, "N", "T", m, n, k, dA.data_ptr(), m, dB.data_ptr(), n)
+    assert rc == g.OK and 11 <= N <= 24
+    assert g.tune_lookup(g.TUNE_CRT, m, n, k) == (g.OK, N, 0)
+    C0 = np.zeros((m, n), order="F")
+    truth = orc.dot2gemm("N", "T", m, n, k, 1.0, A, m, B, n, 0.0, C0, m)
+    dC1, dC2 = to_dev(C0), to_dev(C0)
+    assert g.dgemm_ozaki2("N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 0.0,
+                          dC1.data_ptr(), m, moduli=0) == g.OK
+    assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 0.0,
+                         dC2.data_ptr(), m) == g.OK
+    sync()
+    e_tuned, e_plain = rel(from_dev(dC1, m), truth), rel(from_dev(dC2, m), truth)
+    assert e_tuned[0] <= 4 * e_plain[0] and e_tuned[1] <= 4 * e_plain[1], (N, e_tuned, e_plain)
+    g.tune_cache_clear()
+    assert g.tune_lookup(g.TUNE_CRT, m, n, k) == (g.ERR_UNSUPPORTED, 16, 0)
+
+
 def test_autotune_bf16x_and_use(orc):
     g.tune_cache_clear()
     m, n, k = 384, 300, 1000

@@ -119,6 +119,22 @@ def test_split_zgemm_ozaki(ta, tb, S):
         check_close_c(got, truth, bound)
 
 
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("C", "N"), ("T", "C"), ("R", "R")])
+@pytest.mark.parametrize("N", [14, 16])
+def test_crt_zgemm(ta, tb, N):
+    m, n, k = 150, 90, 120
+    A, B, C = inputs("z", ta, tb, m, n, k, 43)
+    al, be = 0.5 + 0.5j, -1.0
+    rc, got = run_device("z", ta, tb, m, n, k, al, A, B, be, C, g.CPLX_CRT, param=N)
+    assert rc == g.OK
+    truth = truth_of(ta, tb, m, n, k, al, A, B, be, C)
+    if N == 16:  # as accurate as plain FP64 on these inputs
+        bound = cgemm_bound(cop(A, ta, m, k), cop(B, tb, k, n), C, al, be, k, U64)
+        check_close_c(got, truth, bound)
+    else:
+        assert rel_fro(got, truth) < 1e-13
+
+
 @pytest.mark.parametrize("p", ["z", "c"])
 @pytest.mark.parametrize("method", [g.CPLX_4M, g.CPLX_3M, g.CPLX_SPLIT])
 def test_k0_and_alpha0_scale_c_only(p, method):
@@ -227,8 +243,8 @@ def test_dropin_symbols(p, three_m):
                                          factor=3.0 if three_m else 1.0))
 
 
-@pytest.mark.parametrize("p,method", [("z", g.CPLX_4M), ("z", g.CPLX_SPLIT), ("c", g.CPLX_4M),
-                                      ("c", g.CPLX_SPLIT)])
+@pytest.mark.parametrize("p,method", [("z", g.CPLX_4M), ("z", g.CPLX_SPLIT), ("z", g.CPLX_CRT),
+                                      ("c", g.CPLX_4M), ("c", g.CPLX_SPLIT)])
 def test_large_sampled(p, method):
     """1024^3 against sampled ground-truth entries."""
     m = n = k = 1024
