@@ -295,7 +295,10 @@ def run_ours(args, torch, rank, world):
     if not qualified:
         f, cands = schemes[-1]
         qualified.append((f, cands[-1]))
-    if len(qualified) > 1:
+    forced = parse_form(args.form) if args.form else None
+    if forced:
+        form, param = forced
+    elif len(qualified) > 1:
         # time each qualifying form (one warm-up, two calls) and keep the faster
         best = None
         for f, prm in qualified:
@@ -314,6 +317,10 @@ def run_ours(args, torch, rank, world):
     else:
         form, param = qualified[0]
     need = g.split_workspace_bytes(kind_of(form), m, n, k, param)
+    if ws is None or ws.numel() < need:
+        ws = None
+        torch.cuda.empty_cache()
+        ws = torch.empty(need, dtype=torch.uint8, device="cuda")
 
     # ---- timed region: W warm-up + K steps of prepare + run, inputs resident in HBM
     def step(ev0=None, ev1=None, ev2=None):
@@ -453,6 +460,14 @@ def run_ours(args, torch, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def parse_form(name):
+    """'crt_n15' -> ('crt', 15), 'ozaki_s8' -> ('ozaki', 8), 'bf16x6' -> ('bf16x', 6)."""
+    for prefix, form in (("crt_n", "crt"), ("ozaki_s", "ozaki"), ("bf16x", "bf16x")):
+        if name.startswith(prefix) and name[len(prefix):].isdigit():
+            return form, int(name[len(prefix):])
+    raise SystemExit("--form: expected crt_nN, ozaki_sS or bf16xP, got %r" % name)
+
+
 # ----------------------------------------------------------------------------- complex workloads
 def exact_samples_complex(A_rows, B_cols, alpha, beta, c0):
     """Correctly rounded alpha*dot + beta*c (real alpha, beta) of complex dots."""
@@ -556,6 +571,10 @@ def run_complex(args, torch, rank, world):
     if not qualified:
         qualified.append((schemes[-1][0], schemes[-1][1][-1]))
     best = None
+    forced = parse_form(args.form) if args.form else None
+    if forced:
+        meth = g.CPLX_CRT if forced[0] == "crt" else g.CPLX_SPLIT
+        qualified = [(meth, forced[1])]
     for meth, prm in qualified:
         call(meth, prm, C)
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1003,6 +1022,9 @@ def main():
                     help="exponent spread of A and B: (u-0.5)*exp(phi*g) (DGEMM NT 16384 sweep)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-pointer leg (profiling runs)")
+    ap.add_argument("--form", default=None,
+                    help="use this split form instead of timing the qualifying ones "
+                         "(crt_nN, ozaki_sS, bf16xP; profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -38,7 +38,6 @@ constexpr int kModuli[kCrtMaxModuli] = {255, 253, 251, 247, 241, 239, 233, 229,
                                         227, 223, 217, 211, 199, 197, 193, 191,
                                         181, 179, 173, 167, 163, 157, 151, 149};
 constexpr int kCrtDefaultModuli = 16;
-constexpr int kCrtPowT = 128;  // 2^t mod p table: t = b - 53 + ... stays below b <= 120
 
 // ------------------------------------------------------------------ residues
 struct CrtModParams {
@@ -46,8 +45,8 @@ struct CrtModParams {
   unsigned p[kCrtMaxModuli];
   unsigned mg[kCrtMaxModuli];   // floor(2^32 / p)
   unsigned c21[kCrtMaxModuli];  // 2^21 mod p
-  unsigned c42[kCrtMaxModuli];  // 2^42 mod p
-  uint8_t pow2[kCrtMaxModuli][kCrtPowT];  // 2^t mod p, t < kCrtPowT
+  unsigned c42[kCrtMaxModuli];   // 2^42 mod p
+  unsigned pw32[kCrtMaxModuli];  // 2^32 mod p
 };
 
 // x mod p for x < 2^32 (Barrett with mg = floor(2^32/p): q is the quotient or
@@ -63,16 +62,14 @@ __device__ __forceinline__ unsigned mod32(unsigned x, unsigned p, unsigned mg) {
 // |x| = M 2^base with M the 53-bit significand, so |x| 2^(b-e) = M 2^t,
 // t = b - e + base.  The integer y = M 2^t (right shift: truncation; left
 // shift up to 10: exact, < 2^63) or, for t > 10, y = M with the factor
-// 2^t mod p applied after, is cut into 21-bit chunks y0 + y1 2^21 + y2 2^42;
+// 2^t mod p (2^(t mod 32) times t/32 factors of 2^32 mod p) applied after, is
+// cut into 21-bit chunks y0 + y1 2^21 + y2 2^42;
 // y mod p = (y0 + y1 (2^21 mod p) + y2 (2^42 mod p)) mod p, a sum below 2^31.
 __global__ void __launch_bounds__(256)
     crt_residue_kernel(const double *__restrict__ X, int ld, int R, int K, int kcontig, int Rp,
                        int Kp, const int *__restrict__ ex, const __grid_constant__ CrtModParams mp,
                        __nv_bfloat16 *__restrict__ out) {
   __shared__ double tile[32][65];
-  __shared__ uint8_t pow2[kCrtMaxModuli][kCrtPowT];
-  for (int i = threadIdx.x; i < mp.N * kCrtPowT; i += blockDim.x)
-    pow2[i / kCrtPowT][i % kCrtPowT] = mp.pow2[i / kCrtPowT][i % kCrtPowT];
   const int k0 = blockIdx.x * 64;
   const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
   const int64_t step = (int64_t)Rp * Kp / 8;
@@ -110,7 +107,12 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
           unsigned rr = mod32(y0[j + q] + y1[j + q] * c21 + y2[j + q] * c42, p, mg);
-          if (tp[j + q] >= 0) rr = mod32(rr * pow2[i][tp[j + q]], p, mg);
+          if (tp[j + q] >= 0) {  // rare: b > 63, or a row whose largest value is subnormal
+            const int t = tp[j + q];
+            unsigned p2 = mod32(1u << (t & 31), p, mg);
+            for (int w32 = t >> 5; w32 > 0; --w32) p2 = mod32(p2 * mp.pw32[i], p, mg);
+            rr = mod32(rr * p2, p, mg);
+          }
           if (((neg >> (j + q)) & 1) && rr) rr = p - rr;
           const int sres = rr > (p >> 1) ? (int)rr - (int)p : (int)rr;
           h[q] = __float_as_uint((float)sres) >> 16;  // |sres| <= 127: exact in BF16
@@ -148,6 +150,7 @@ __device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli],
   unsigned long long acc[kLimbs] = {0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
 #pragma unroll
   for (int g = 0; g < kCrtMaxModuli; ++g) {
+    if (g >= rp.N) break;  // uniform across the grid
     const unsigned r = (word[g] >> (8 * e)) & 0xffu;
 #pragma unroll
     for (int l = 0; l < kLimbs; ++l) acc[l] += (unsigned long long)r * rp.w[g][l];
@@ -478,11 +481,7 @@ int crt_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda,
     mp.mg[i] = (unsigned)((1ull << 32) / p);
     mp.c21[i] = (unsigned)((1ull << 21) % p);
     mp.c42[i] = (unsigned)((1ull << 42) % p);
-    unsigned v = 1;
-    for (int t = 0; t < kCrtPowT; ++t) {
-      mp.pow2[i][t] = (uint8_t)v;
-      v = (2 * v) % p;
-    }
+    mp.pw32[i] = (unsigned)((1ull << 32) % p);
   }
   auto row_blocks = [](int64_t Rp) { return (unsigned)(Rp / 32 < 65535 ? Rp / 32 : 65535); };
   const bool an = notrans(ta), bn = notrans(tb);
