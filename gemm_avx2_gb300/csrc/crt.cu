@@ -269,6 +269,34 @@ __device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli],
   pos_out = pos;
 }
 
+// (-1)^neg * top * 2^e2 as FP64: round top to 53 bits (to nearest, ties to
+// even; bit 0 may be a sticky bit) and assemble the bits when the result is a
+// normal number, otherwise the same rounding through the FP64 pipe (which runs
+// at 1 TFLOP/s here, so the common case stays on the integer pipe).
+__device__ __forceinline__ double crt_compose(unsigned long long top, int e2, bool neg) {
+  if (top == 0) return 0.0;
+  const int lz = __clzll((long long)top);
+  const unsigned long long t = top << lz;  // leading bit at 63
+  int e = e2 + 63 - lz;                    // value = (t / 2^63) 2^e
+  unsigned long long mant = t >> 11;
+  const unsigned long long rem = t & 0x7ffull;
+  if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) {
+    ++mant;
+    if (mant >> 53) {
+      mant >>= 1;
+      ++e;
+    }
+  }
+  if (e < -1022 || e > 1023) {
+    const double v = scale_pow2(__ull2double_rn(top), e2);
+    return neg ? -v : v;
+  }
+  const unsigned long long bits = (neg ? (1ull << 63) : 0ull) |
+                                  ((unsigned long long)(e + 1023) << 52) |
+                                  (mant & 0xfffffffffffffull);
+  return __longlong_as_double((long long)bits);
+}
+
 // 4 consecutive rows of one column of C per thread: one 32-bit load per
 // modulus brings their residues (rows are contiguous in each residue plane).
 constexpr int kRecRows = 4;
@@ -298,8 +326,7 @@ __global__ void __launch_bounds__(256)
       if (ea == kNonFiniteExp || eb == kNonFiniteExp) {
         v = __longlong_as_double(0x7ff8000000000000LL);
       } else {
-        v = scale_pow2(__ull2double_rn(top), pos + ea + eb - rp.two_b);
-        if (neg) v = -v;
+        v = crt_compose(top, pos + ea + eb - rp.two_b, neg);
       }
       double *c = rp.C + (int64_t)j * rp.ldc + i;
       const double cb = (rp.beta == 1.0) ? *c : *c * rp.beta;
