@@ -110,14 +110,20 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
   const int wm = warp & 1, wn = warp >> 1;
   const int tm = wm * 8 + (lane & 7);
   const int tn = wn * 4 + (lane >> 3);
-  // accumulators as column pairs: with MN-major B one packed FMA
-  // (fma.rn.f32x2) updates two outputs per issue slot, with the same
-  // round-to-nearest FMA per element
-  float2 acc[8][4];
+  // Packed FMAs (fma.rn.f32x2, the same round-to-nearest FMA per element) need
+  // both operand pairs in adjacent registers, which a float4 shared-memory load
+  // gives along its contiguous dimension:
+  //   B MN-major:             pairs along j (columns of C): acc[i][j/2]
+  //   A MN-major, B K-major:  pairs along i (rows of C):    acc[i/2][j]
+  //   A and B K-major:        pairs along k: acc[i][j] holds the even-k and
+  //                           odd-k partial sums, added once in the epilogue
+  constexpr int kPairJ = 0, kPairI = 1, kPairK = 2;
+  constexpr int mode = !BK_ ? kPairJ : (AK ? kPairK : kPairI);
+  float2 acc[8][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
+    for (int j = 0; j < 8; ++j) acc[i][j] = make_float2(0.f, 0.f);
 
   for (int kt = 0; kt < kStages - 1 && kt < ktiles; ++kt) fill(kt);
 
@@ -136,13 +142,12 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
     if (!mbar_wait(&full[s], (kt / kStages) & 1, err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
     const float *ta = sA + s * (kBM * BK);
     const float *tb = sB + s * (kBN * BK);
+    if constexpr (mode == kPairJ) {
 #pragma unroll 2
-    for (int kq = 0; kq < BK / 4; ++kq) {
-      float a[8][4], b[8][4];
-      f32_load_frag<AK>(ta, tm, kq, a);
-      f32_load_frag<BK_>(tb, tn, kq, b);
-      if constexpr (!BK_) {
-        // MN-major B: (b[2jp], b[2jp+1]) are neighbours of one float4 load
+      for (int kq = 0; kq < BK / 4; ++kq) {
+        float a[8][4], b[8][4];
+        f32_load_frag<AK>(ta, tm, kq, a);
+        f32_load_frag<BK_>(tb, tn, kq, b);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           float2 bp[4];
@@ -155,17 +160,41 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
             for (int jp = 0; jp < 4; ++jp) acc[i][jp] = __ffma2_rn(ab, bp[jp], acc[i][jp]);
           }
         }
-      } else {
-        // K-major B: pairs would need register moves; scalar FFMA on the halves
+      }
+    } else if constexpr (mode == kPairI) {
+#pragma unroll 2
+      for (int kq = 0; kq < BK / 4; ++kq) {
+        float a[8][4], b[8][4];
+        f32_load_frag<AK>(ta, tm, kq, a);
+        f32_load_frag<BK_>(tb, tn, kq, b);
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
+        for (int q = 0; q < 4; ++q) {
+          float2 ap[4];
 #pragma unroll
-          for (int i = 0; i < 8; ++i)
+          for (int ip = 0; ip < 4; ++ip) ap[ip] = make_float2(a[2 * ip][q], a[2 * ip + 1][q]);
 #pragma unroll
-            for (int jp = 0; jp < 4; ++jp) {
-              acc[i][jp].x = fmaf(a[i][q], b[2 * jp][q], acc[i][jp].x);
-              acc[i][jp].y = fmaf(a[i][q], b[2 * jp + 1][q], acc[i][jp].y);
-            }
+          for (int j = 0; j < 8; ++j) {
+            const float2 bb = make_float2(b[j][q], b[j][q]);
+#pragma unroll
+            for (int ip = 0; ip < 4; ++ip) acc[ip][j] = __ffma2_rn(ap[ip], bb, acc[ip][j]);
+          }
+        }
+      }
+    } else {
+#pragma unroll 1
+      for (int kq = 0; kq < BK / 4; ++kq) {
+        float a[8][4], b[8][4];
+        f32_load_frag<AK>(ta, tm, kq, a);
+        f32_load_frag<BK_>(tb, tn, kq, b);
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const float2 ap = make_float2(a[i][2 * h], a[i][2 * h + 1]);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+              acc[i][j] = __ffma2_rn(ap, make_float2(b[j][2 * h], b[j][2 * h + 1]), acc[i][j]);
+          }
       }
     }
     __syncwarp();
@@ -175,6 +204,11 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 
   // fused alpha/beta epilogue (beta*C first, as src/gemm_driver.c:133 does; beta == 0
   // still multiplies, so NaN/Inf already in C propagate like the reference).
+  auto value = [&](int i, int j) -> float {
+    if constexpr (mode == kPairJ) return (j & 1) ? acc[i][j >> 1].y : acc[i][j >> 1].x;
+    else if constexpr (mode == kPairI) return (i & 1) ? acc[i >> 1][j].y : acc[i >> 1][j].x;
+    else return acc[i][j].x + acc[i][j].y;
+  };
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const int col = n0 + f32_row<BK_>(tn, j);
@@ -191,7 +225,7 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
       const int row = m0 + f32_row<AK>(tm, i);
       if (row < m) {
         const float cb = (beta == 1.0f) ? cv[i] : cv[i] * beta;
-        cc[row] = cb + alpha * ((j & 1) ? acc[i][j >> 1].y : acc[i][j >> 1].x);
+        cc[row] = cb + alpha * value(i, j);
       }
     }
   }
