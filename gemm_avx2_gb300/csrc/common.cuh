@@ -108,6 +108,27 @@ __device__ __forceinline__ void tma_load_2d(void *smem_dst, const void *tmap, in
       : "memory");
 }
 
+// TMA load of one box into the same shared-memory offset of every CTA in
+// `mask` (this cluster only), signalling the mbarrier at the same offset in each.
+__device__ __forceinline__ void tma_load_2d_mc(void *smem_dst, const void *tmap, int32_t x,
+                                               int32_t y, uint64_t *bar, uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      ".multicast::cluster [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(smem_dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Every thread of every CTA of the cluster (release / acquire).
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+
 // ------------------------------------------------------------------ cp.async (fallback loads)
 __device__ __forceinline__ void cp_async_4(void *smem_dst, const void *gsrc, bool valid) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(smem_dst)), "l"(gsrc),
@@ -178,6 +199,13 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(bar))
+      : "memory");
+}
+// Commit that arrives on the mbarrier at the same offset in every CTA of `mask`.
+__device__ __forceinline__ void umma_commit_mc(uint64_t *bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+      "[%0], %1;" ::"r"(smem_u32(bar)), "h"(mask)
       : "memory");
 }
 // 32 lanes x 32 consecutive 32-bit columns: thread l of the warp gets lane

@@ -256,6 +256,12 @@ constexpr int kBxSmem = kBxStages * kBxStage + 1024 + 256;
 constexpr int kBxColsPerWarp = kBf16xBN / 2;        // columns each epilogue warp owns
 constexpr int kBxDefaultChunk = 4;                  // 4 x 64 = 256 K' per chunk
 
+// MC: 2-CTA clusters on the row tiles 2u and 2u + 1 of one column tile, in
+// lockstep over the same unit sequence; each CTA loads its own A tile and half
+// of the shared B tile, multicast into both CTAs' stage (the B tensor map's box
+// is then 128 rows).  Each stage's empty barrier counts both CTAs' MMA commits,
+// since a stage holds data its peer wrote.  This halves the B tile's L2 reads.
+template <bool MC>
 __global__ void __launch_bounds__(kBxThreads, 1)
 bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   Bf16xParams p) {
@@ -272,7 +278,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kBxStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    for (int s = 0; s < kBxStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], MC ? 2 : 1); }
     for (int b = 0; b < 2; ++b) { mbar_init(&accf[b], 1); mbar_init(&acce[b], kBxEpiWarps); }
     mbar_init(done, 1);
     *abort_flag = 0;
@@ -283,9 +289,20 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   if (warp == 1) { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
   tc_fence_before();
   __syncthreads();
+  if (MC) cluster_sync();  // the peer's barriers are initialised before any multicast
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int ntiles = p.tiles_m * p.tiles_n;
+  // work units: tiles, or (MC) row-tile pairs whose rank-th row tile is this CTA's
+  const uint32_t rank = MC ? cluster_ctarank() : 0u;
+  const int pm = MC ? (p.tiles_m + 1) / 2 : p.tiles_m;
+  const int nunits = pm * p.tiles_n;
+  const int first = MC ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+  const int stride = MC ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+  auto unit_tile = [&](int u, int &tm, int &tn) {
+    int um;
+    tile_coords(u, pm, p.tiles_n, MC ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
+    tm = MC ? 2 * um + (int)rank : um;  // MC: a row tile past the end is zero-filled, not stored
+  };
   int nchunks = 0;
   for (int sg = 0; sg < p.nseg; ++sg) {
     const int cl = p.chunk_len[sg] > 0 ? p.chunk_len[sg] : p.seg_kblocks;
@@ -295,17 +312,21 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   if (warp == 0) {
     if (lane == 0) {
       uint32_t L = 0;
-      for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x) {
+      for (int u = first; u < nunits && !*abort_flag; u += stride) {
         int tm, tn;
-        tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
+        unit_tile(u, tm, tn);
         for (int kb = 0; kb < p.kblocks; ++kb, ++L) {
           const int s = L % kBxStages;
           const uint32_t r = L / kBxStages;
           if (!mbar_wait(&empty[s], (r & 1) ^ 1, p.err, kErrTimeoutEmpty, abort_flag)) break;
           uint8_t *sa = smem + s * kBxStage;
-          mbar_arrive_expect_tx(&full[s], kBxStage);
+          mbar_arrive_expect_tx(&full[s], kBxStage);  // own A, both B halves
           tma_load_2d(sa, &tmA, kb * kSplitBK, tm * kSplitBM, &full[s]);
-          tma_load_2d(sa + kBxABytes, &tmB, kb * kSplitBK, tn * kBf16xBN, &full[s]);
+          if (MC)
+            tma_load_2d_mc(sa + kBxABytes + rank * (kBxBBytes / 2), &tmB, kb * kSplitBK,
+                           tn * kBf16xBN + (int)rank * (kBf16xBN / 2), &full[s], 0x3);
+          else
+            tma_load_2d(sa + kBxABytes, &tmB, kb * kSplitBK, tn * kBf16xBN, &full[s]);
         }
       }
     }
@@ -314,7 +335,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       constexpr uint32_t idesc = idesc_bf16_f32(kSplitBM, kBf16xBN);
       uint32_t L = 0, chunk = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      for (int u = first; u < nunits && ok; u += stride) {
         int sg = 0, c0 = 0;
         for (int c = 0; c < nchunks && ok; ++c, ++chunk) {
           // chunk c covers K blocks [c0, c1) of segment sg
@@ -342,7 +363,10 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             for (int kk = 0; kk < kSplitBK / 16; ++kk)
               umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32), idesc,
                         (kb > c0 || kk > 0) ? 1u : 0u);
-            umma_commit(&empty[s]);
+            if (MC)
+              umma_commit_mc(&empty[s], 0x3);  // the stage is free once both CTAs are done
+            else
+              umma_commit(&empty[s]);
           }
           if (ok) umma_commit(&accf[b]);
           c0 = c1;
@@ -360,9 +384,9 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + h * kBxColsPerWarp;
     uint32_t chunk = 0;
     bool ok = true;
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    for (int u = first; u < nunits && ok; u += stride) {
       int tm, tn;
-      tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
+      unit_tile(u, tm, tn);
       float run[kBxColsPerWarp];
 #pragma unroll
       for (int j = 0; j < kBxColsPerWarp; ++j) run[j] = 0.f;
@@ -415,6 +439,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     tc_fence_after();
     tmem_dealloc(tmem, 512);
   }
+  if (MC) cluster_sync();  // no peer multicast or commit can still target this CTA
 }
 
 // ===========================================================================
@@ -479,6 +504,10 @@ __device__ __forceinline__ void group_of(int mode, int gi, int S, int &t, int &l
 // 64 * 1024 * 127^2 < 2^31.
 constexpr int kCrtRunChunks = 64;
 
+// MC: 2-CTA clusters sharing the B tile, as in bf16x_gemm_kernel.  A row tile
+// past the end (odd tile rows) still takes part in the pipeline (its A loads
+// fetch rows of the next block and its sums are discarded) but writes nothing.
+template <bool MC>
 __global__ void __launch_bounds__(kOzThreads, 1)
 ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   OzakiParams p) {
@@ -495,7 +524,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kOzStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    for (int s = 0; s < kOzStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], MC ? 2 : 1); }
     for (int b = 0; b < 2; ++b) { mbar_init(&accf[b], 1); mbar_init(&acce[b], kOzEpiWarps); }
     mbar_init(done, 1);
     *abort_flag = 0;
@@ -506,18 +535,29 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   if (warp == 1) { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
   tc_fence_before();
   __syncthreads();
+  if (MC) cluster_sync();  // the peer's barriers are initialised before any multicast
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int ntiles = p.tiles_m * p.tiles_n;
   const int S = p.S, KB = p.KB;
+  // work units: tiles, or (MC) row-tile pairs whose rank-th row tile is this CTA's
+  const uint32_t rank = MC ? cluster_ctarank() : 0u;
+  const int pm = MC ? (p.tiles_m + 1) / 2 : p.tiles_m;
+  const int nunits = pm * p.tiles_n;
+  const int first = MC ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+  const int stride = MC ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+  auto unit_tile = [&](int u, int &tm, int &tn) {
+    int um;
+    tile_coords(u, pm, p.tiles_n, MC ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
+    tm = MC ? 2 * um + (int)rank : um;
+  };
 
   if (warp == 0) {
     if (lane == 0) {
       uint32_t L = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      for (int u = first; u < nunits && ok; u += stride) {
         int tm, tn;
-        tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
+        unit_tile(u, tm, tn);
         for (int gi = 0; gi < S && ok; ++gi) {
           int t, lo, np;
           group_of(p.mode, gi, S, t, lo, np);
@@ -533,8 +573,13 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             uint8_t *sa_ptr = smem + s * kOzStage;
             mbar_arrive_expect_tx(&full[s], kOzStage);
             tma_load_2d(sa_ptr, &tmA, kb * kSplitBK, (sa - 1) * p.Mp + tm * kSplitBM, &full[s]);
-            tma_load_2d(sa_ptr + kOzABytes, &tmB, kb * kSplitBK, (sb - 1) * p.Np + tn * kOzakiBN,
-                        &full[s]);
+            if (MC)
+              tma_load_2d_mc(sa_ptr + kOzABytes + rank * (kOzBBytes / 2), &tmB, kb * kSplitBK,
+                             (sb - 1) * p.Np + tn * kOzakiBN + (int)rank * (kOzakiBN / 2),
+                             &full[s], 0x3);
+            else
+              tma_load_2d(sa_ptr + kOzABytes, &tmB, kb * kSplitBK,
+                          (sb - 1) * p.Np + tn * kOzakiBN, &full[s]);
           }
         }
       }
@@ -544,7 +589,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       constexpr uint32_t idesc = idesc_bf16_f32(kSplitBM, kOzakiBN);
       uint32_t L = 0, chunk = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      for (int u = first; u < nunits && ok; u += stride) {
         for (int gi = 0; gi < S && ok; ++gi) {
           int t, lo, np;
           group_of(p.mode, gi, S, t, lo, np);
@@ -572,7 +617,10 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               for (int kk = 0; kk < kSplitBK / 16; ++kk)
                 umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32), idesc,
                           (idx > c0 || kk > 0) ? 1u : 0u);
-              umma_commit(&empty[s]);
+              if (MC)
+                umma_commit_mc(&empty[s], 0x3);  // the stage is free once both CTAs are done
+              else
+                umma_commit(&empty[s]);
             }
             if (ok) umma_commit(&accf[b]);
           }
@@ -589,10 +637,11 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + h * kOzCols;
     uint32_t chunk = 0;
     bool ok = true;
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    for (int u = first; u < nunits && ok; u += stride) {
       int tm, tn;
-      tile_coords(tile, p.tiles_m, p.tiles_n, kSplitGroupM, tm, tn);
-      const int row = tm * kSplitBM + row_in_tile;          // < Mp
+      unit_tile(u, tm, tn);
+      const bool real = tm < p.tiles_m;  // MC: a row tile past the end writes nothing
+      const int row = tm * kSplitBM + row_in_tile;          // < Mp when real
       const int col0 = tn * kOzakiBN + h * kOzCols;          // first of this warp's columns
       double *res = p.res + (int64_t)col0 * p.Mp + row;      // res[j * Mp] is column col0 + j
       bool res_init = false;
@@ -635,7 +684,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               int r = run[j] % pm;
               run[j] = r < 0 ? r + pm : r;
             }
-            if (last) {
+            if (last && real) {
               uint8_t *dst = p.rres + (int64_t)gi * p.Mp * p.Np + (int64_t)col0 * p.Mp + row;
 #pragma unroll
               for (int j = 0; j < kOzCols; ++j) dst[(int64_t)j * p.Mp] = (uint8_t)run[j];
@@ -644,7 +693,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           } else if (!p.mode && (++since_fold == kOzRunChunks || last)) {
             // fold the exact group sum into the FP64 result: res += run * 2^-7t
 #pragma unroll
-            for (int g = 0; g < kOzCols; g += 8) {
+            for (int g = 0; g < kOzCols && real; g += 8) {
               double prev[8];
 #pragma unroll
               for (int j = 0; j < 8; ++j) prev[j] = res_init ? res[(int64_t)(g + j) * p.Mp] : 0.0;
@@ -662,7 +711,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       if (!ok) break;
       // final epilogue: C = alpha * 2^(E_i + F_j) * res + beta * C (slice form;
       // the CRT form's C update is the reconstruction kernel's)
-      if (!p.mode && row < p.m) {
+      if (!p.mode && real && row < p.m) {
         const int ea = p.expA[row];
 #pragma unroll 1
         for (int g = 0; g < kOzCols; g += 8) {
@@ -695,6 +744,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     tc_fence_after();
     tmem_dealloc(tmem, 512);
   }
+  if (MC) cluster_sync();  // no peer multicast or commit can still target this CTA
 }
 
 // ===========================================================================
@@ -819,9 +869,10 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
   const size_t need = split_workspace_bytes(0, m, n, k, products);
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
   const Bf16xLayout L = bf16x_layout(m, n, k, products, const_cast<void *>(ws));
+  const bool mc = L.Mp / kSplitBM >= 2;  // 2-CTA clusters sharing the B tile
   CUtensorMap tA{}, tB{};
   if (!encode_2d(&tA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, kBf16xBN, true))
+      !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, mc ? kBf16xBN / 2 : kBf16xBN, true))
     return GB300_ERR_CUDA;
   Bf16xParams p;
   p.m = m; p.n = n;
@@ -842,12 +893,39 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
     }
   }
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.err = err;
-  if (cudaFuncSetAttribute(bf16x_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (!mc) {
+    if (cudaFuncSetAttribute(bf16x_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kBxSmem) != cudaSuccess)
+      return GB300_ERR_CUDA;
+    const int ntiles = p.tiles_m * p.tiles_n;
+    const int grid = ntiles < sm_count() ? ntiles : sm_count();
+    bf16x_gemm_kernel<false><<<grid, kBxThreads, kBxSmem, st>>>(tA, tB, p);
+    return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  }
+  if (cudaFuncSetAttribute(bf16x_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kBxSmem) != cudaSuccess)
     return GB300_ERR_CUDA;
-  const int ntiles = p.tiles_m * p.tiles_n;
-  const int grid = ntiles < sm_count() ? ntiles : sm_count();
-  bf16x_gemm_kernel<<<grid, kBxThreads, kBxSmem, st>>>(tA, tB, p);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kBxThreads);
+  cfg.dynamicSmemBytes = kBxSmem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const int npairs = ((p.tiles_m + 1) / 2) * p.tiles_n;
+  int max_clusters = sm_count() / 2;
+  cfg.gridDim = dim3((unsigned)(2 * max_clusters));
+  int occ = 0;
+  if (cudaOccupancyMaxActiveClusters(&occ, bf16x_gemm_kernel<true>, &cfg) == cudaSuccess && occ > 0 &&
+      occ < max_clusters)
+    max_clusters = occ;
+  cfg.gridDim = dim3((unsigned)(2 * (npairs < max_clusters ? npairs : max_clusters)));
+  if (cudaLaunchKernelEx(&cfg, bf16x_gemm_kernel<true>, tA, tB, p) != cudaSuccess)
+    return GB300_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
@@ -964,9 +1042,11 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
 
 int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
   if (a.S < 1 || a.S > (a.mode ? kCrtMaxModuli : kOzakiMaxSlices)) return GB300_ERR_ARG;
+  const bool mc = a.Mp / kSplitBM >= 2;  // 2-CTA clusters sharing the B tile
   CUtensorMap tA{}, tB{};
   if (!encode_2d(&tA, a.As, 2, a.Kp, a.S * a.Mp, a.Kp, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, kOzakiBN, true))
+      !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, mc ? kOzakiBN / 2 : kOzakiBN,
+                 true))
     return GB300_ERR_CUDA;
   OzakiParams p;
   p.m = a.m; p.n = a.n;
@@ -978,12 +1058,39 @@ int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
   p.alpha = a.alpha; p.beta = a.beta; p.C = a.C; p.ldc = a.ldc;
   p.expA = a.expA; p.expB = a.expB; p.res = a.res; p.rres = a.rres; p.err = err;
   for (int i = 0; i < kCrtMaxModuli; ++i) p.mods[i] = (a.mode && i < a.S) ? a.mods[i] : 1;
-  if (cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (!mc) {
+    if (cudaFuncSetAttribute(ozaki_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kOzSmem) != cudaSuccess)
+      return GB300_ERR_CUDA;
+    const int ntiles = p.tiles_m * p.tiles_n;
+    const int grid = ntiles < sm_count() ? ntiles : sm_count();
+    ozaki_gemm_kernel<false><<<grid, kOzThreads, kOzSmem, st>>>(tA, tB, p);
+    return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  }
+  if (cudaFuncSetAttribute(ozaki_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kOzSmem) != cudaSuccess)
     return GB300_ERR_CUDA;
-  const int ntiles = p.tiles_m * p.tiles_n;
-  const int grid = ntiles < sm_count() ? ntiles : sm_count();
-  ozaki_gemm_kernel<<<grid, kOzThreads, kOzSmem, st>>>(tA, tB, p);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kOzThreads);
+  cfg.dynamicSmemBytes = kOzSmem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const int npairs = ((p.tiles_m + 1) / 2) * p.tiles_n;
+  int max_clusters = sm_count() / 2;
+  cfg.gridDim = dim3((unsigned)(2 * max_clusters));
+  int occ = 0;
+  if (cudaOccupancyMaxActiveClusters(&occ, ozaki_gemm_kernel<true>, &cfg) == cudaSuccess &&
+      occ > 0 && occ < max_clusters)
+    max_clusters = occ;
+  cfg.gridDim = dim3((unsigned)(2 * (npairs < max_clusters ? npairs : max_clusters)));
+  if (cudaLaunchKernelEx(&cfg, ozaki_gemm_kernel<true>, tA, tB, p) != cudaSuccess)
+    return GB300_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
