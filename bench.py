@@ -819,7 +819,7 @@ def run_grouped(args, torch, rank, world):
         "data": "synthetic (seeded uniform[-1,1), generated on the device)",
         "config": {"workload": "grouped_1024", "problems": count, "fp64_share_of_flops":
                    round(fl_d / flops, 4), "total_gflop": round(flops / 1e9, 3),
-                   "form": "split (FP32: bf16x6, FP64: ozaki_s8), CUDA graph",
+                   "form": "split (FP32: bf16x6, FP64: CRT with 16 moduli), CUDA graph",
                    "l2": "%d MB of operands > %d MB" % (
                        sum(sum(t.numel() * t.element_size() for t in b[:3]) for b in bufs) // 2**20,
                        L2_BYTES // 2**20)},
@@ -833,7 +833,7 @@ def run_grouped(args, torch, rank, world):
                      "peak_source": "FP64 1.05 and FP32 73 TFLOP/s measured by microbenchmark"},
         "accuracy": {"plain": err_plain, "split": err_split, "samples": "8 entries x 48 problems"},
         "clocks": clocks,
-        "gpu_launches": args.steps * sum(5 if p["precision"] == "d" else 3 for p in probs),
+        "gpu_launches": args.steps * sum(7 if p["precision"] == "d" else 3 for p in probs),
         "e2e": {"value": None, "skipped": "device-pointer grouped API"},
     }
     gp.destroy()

@@ -710,13 +710,13 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
         rc = GB300_ERR_CUDA;
     }
   } else {
-    // longest work first onto the least-loaded branch (FP64 problems run
-    // S(S+1)/2 slice products, FP32 ones 6)
+    // longest work first onto the least-loaded branch (FP64 problems run the
+    // CRT form's 16 residue GEMMs, FP32 ones 6 products)
     std::vector<int> order(count);
     for (int i = 0; i < count; ++i) order[i] = i;
     auto work = [&](int i) {
       const gb300_gemm_problem &q = problems[i];
-      return (double)q.m * q.n * q.k * (q.precision == 'd' ? 36.0 : 6.0) + 1e6;
+      return (double)q.m * q.n * q.k * (q.precision == 'd' ? 16.0 : 6.0) + 1e6;
     };
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work(a) > work(b); });
     double load[kGraphBranches] = {0};
@@ -727,7 +727,7 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
       load[b] += work(i);
       branch_of[i] = b;
       const gb300_gemm_problem &q = problems[i];
-      const size_t w = q.precision == 'd' ? split_workspace_bytes(1, q.m, q.n, q.k, 0)
+      const size_t w = q.precision == 'd' ? crt_workspace_bytes(q.m, q.n, q.k, 0)
                                           : split_workspace_bytes(0, q.m, q.n, q.k, 6);
       if (w > wneed_b[b]) wneed_b[b] = w;
     }
@@ -759,11 +759,11 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
         const gb300_gemm_problem &q = problems[i];
         const int b = branch_of[i];
         if (q.precision == 'd')
-          rc2 = ozaki_dgemm(q.transa, q.transb, q.m, q.n, q.k, q.alpha,
-                            static_cast<const double *>(q.A), q.lda,
-                            static_cast<const double *>(q.B), q.ldb, q.beta,
-                            static_cast<double *>(q.C), q.ldc, 0, g->ws[b], wneed_b[b], bs[b],
-                            s->err);
+          rc2 = crt_dgemm(q.transa, q.transb, q.m, q.n, q.k, q.alpha,
+                          static_cast<const double *>(q.A), q.lda,
+                          static_cast<const double *>(q.B), q.ldb, q.beta,
+                          static_cast<double *>(q.C), q.ldc, 0, g->ws[b], wneed_b[b], bs[b],
+                          s->err);
         else
           rc2 = split_sgemm(q.transa, q.transb, q.m, q.n, q.k, (float)q.alpha,
                             static_cast<const float *>(q.A), q.lda,

@@ -206,8 +206,8 @@ int gb300_gemm_grouped_ws(const gb300_gemm_problem *problems, int count, void *w
  * no host-side work: the operand pointers are fixed, their contents may
  * change between launches.
  *   form 0: plain forms, one persistent launch (as gb300_gemm_grouped);
- *   form 1: split forms, one call per problem (FP32: 6xBF16, FP64: Ozaki with
- *           the default slice count), captured as 16 parallel branches
+ *   form 1: split forms, one call per problem (FP32: 6xBF16, FP64: the CRT
+ *           form with the tuned / default moduli count), captured as 16 parallel branches
  *           (longest work first onto the least-loaded branch), each branch
  *           with its own workspace. */
 typedef struct gb300_grouped_graph_s *gb300_grouped_graph;
