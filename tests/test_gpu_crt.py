@@ -87,6 +87,22 @@ def test_extreme_exponents_bitexact(orc, N):
     assert np.array_equal(got, model, equal_nan=True), np.nanmax(np.abs(got - model))
 
 
+@pytest.mark.parametrize("m", [300, 129])
+def test_odd_row_tiles_bitexact(orc, m):
+    """3 and 2 row tiles (m = 300: the 2-CTA clusters get a spare tile that
+    must store no residues over a neighbour's; m = 129: a 1-row last tile)."""
+    n, k = 290, 150
+    A = orc.spread((m, k), 58, 0, 1.0)
+    B = orc.spread((k, n), 58, 1, 1.0)
+    C = orc.uniform((m + 3, n), np.float64, 58, 2)
+    rc, got, _ = run_crt("N", "N", m, n, k, A, m, B, k, C, 16, beta=0.5)
+    assert rc == g.OK
+    assert np.array_equal(got[m:], C[m:])
+    model = crt.crt_gemm_model(A, B, 16, alpha=1.0, beta=0.5, C=C[:m])
+    assert np.array_equal(got[:m], model)
+    assert g.device_error() == 0
+
+
 def test_nonfinite_rows_and_columns(orc):
     m, n, k = 40, 30, 50
     A = orc.uniform((m, k), np.float64, 53, 0)

@@ -87,6 +87,7 @@ def test_bf16x_multi_tile_ragged(orc, products):
                          dP.data_ptr(), m + 5) == g.OK
     sync()
     got = from_dev(dC, m + 5)
+    assert np.array_equal(got[m:], C[m:])  # 3 row tiles: the cluster's spare tile writes nothing
     truth = orc.dot2gemm("T", "N", m, n, k, -1.0, A, k, B, k, 1.0, C, m + 5)
     mx, fro = rel_errs(got[:m], truth)
     pmx, pfro = rel_errs(from_dev(dP, m + 5)[:m], truth)
@@ -174,6 +175,24 @@ def test_ozaki_slices_extreme_exponents(orc, S, ta):
     sa, _ = osp.ozaki_slices(Aop, S)
     for s in range(S):
         assert np.array_equal(As[s, :m, :k], sa[s]), s
+    assert g.device_error() == 0
+
+
+def test_ozaki_odd_row_tiles(orc):
+    """3 row tiles: in 2-CTA clusters the spare fourth tile runs through the
+    pipeline but must write neither the FP64 scratch nor C."""
+    m, n, k = 300, 270, 200
+    A = orc.spread((m, k), 23, 0, 1.0)
+    B = orc.spread((k, n), 23, 1, 1.0)
+    C = orc.uniform((m + 3, n), np.float64, 23, 2)
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
+    assert g.dgemm_ozaki("N", "N", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), k, 0.5,
+                         dC.data_ptr(), m + 3, slices=8) == g.OK
+    sync()
+    got = from_dev(dC, m + 3)
+    assert np.array_equal(got[m:], C[m:])
+    model = osp.ozaki_gemm_model(A, B, 8)
+    assert np.allclose(got[:m], model + 0.5 * C[:m], rtol=4e-16, atol=1e-300)
     assert g.device_error() == 0
 
 
