@@ -258,7 +258,7 @@ def run_ours(args, torch, rank, world):
     # Frobenius errors do not exceed the plain kernel's; for FP64 the faster
     # of the two qualifying schemes is timed below.
     schemes = [("crt", list(range(11, 25))), ("ozaki", list(range(6, 13)))] if is_d else \
-        [("bf16x", [3, 6])]
+        [("bf16x", [3, 6]), ("bf16x", [g.FP16X3])]
     errs, qualified = {}, []
     ws = None
 
@@ -273,6 +273,8 @@ def run_ours(args, torch, rank, world):
                            ws.data_ptr(), need, stream) == g.OK
 
     def name_of(f, prm):
+        if f == "bf16x" and prm == g.FP16X3:
+            return "fp16x3"
         return {"bf16x": "bf16x%d", "ozaki": "ozaki_s%d", "crt": "crt_n%d"}[f] % prm
 
     for f, cands in schemes:
@@ -415,7 +417,8 @@ def run_ours(args, torch, rank, world):
 
     # ---- roofline of the dominant kernel (the tcgen05 GEMM of the split form)
     pk = peaks()
-    products = {"bf16x": param, "ozaki": (param * (param + 1)) // 2, "crt": param}[form]
+    products = {"bf16x": 3 if param == g.FP16X3 else param,
+                "ozaki": (param * (param + 1)) // 2, "crt": param}[form]
     pipe_flops = products * prob.flops
     achieved = pipe_flops / (gemm_ms / 1e3) / 1e12
     roof = {"bound": "tensor", "achieved": round(achieved, 2), "peak": pk["bf16_tflops"],
@@ -452,7 +455,9 @@ def run_ours(args, torch, rank, world):
                      "split": {p: {"max_rel": e[0], "fro_rel": e[1]} for p, e in errs.items()},
                      "chosen": form_name},
         "clocks": clocks,
-        "gpu_launches": args.steps * {"bf16x": 3, "ozaki": 6, "crt": 7}[form],
+        # split kernels + GEMM; the FP16 form adds 2 max |.| passes and the exponents
+        "gpu_launches": args.steps * ({"bf16x": 3, "ozaki": 6, "crt": 7}[form] +
+                                      (3 if form == "bf16x" and param == g.FP16X3 else 0)),
     }
     if rank == 0:
         line["cpu_baseline"] = (cpu_baseline(w, args.cpu_seconds) if not args.no_cpu
@@ -461,11 +466,15 @@ def run_ours(args, torch, rank, world):
 
 
 def parse_form(name):
-    """'crt_n15' -> ('crt', 15), 'ozaki_s8' -> ('ozaki', 8), 'bf16x6' -> ('bf16x', 6)."""
+    """'crt_n15' -> ('crt', 15), 'ozaki_s8' -> ('ozaki', 8), 'bf16x6' -> ('bf16x', 6),
+    'fp16x3' -> ('bf16x', FP16X3) (the scaled FP16 form shares the BF16xP entry points)."""
+    if name == "fp16x3":
+        import gemm_avx2_gb300 as g
+        return "bf16x", g.FP16X3
     for prefix, form in (("crt_n", "crt"), ("ozaki_s", "ozaki"), ("bf16x", "bf16x")):
         if name.startswith(prefix) and name[len(prefix):].isdigit():
             return form, int(name[len(prefix):])
-    raise SystemExit("--form: expected crt_nN, ozaki_sS or bf16xP, got %r" % name)
+    raise SystemExit("--form: expected crt_nN, ozaki_sS, bf16xP or fp16x3, got %r" % name)
 
 
 # ----------------------------------------------------------------------------- complex workloads
@@ -551,9 +560,11 @@ def run_complex(args, torch, rank, world):
     # BF16xP products.  Per scheme the smallest candidate at equal error to 4M;
     # of two qualifying schemes the faster one.
     schemes = [(g.CPLX_CRT, list(range(11, 25))), (g.CPLX_SPLIT, list(range(6, 13)))] \
-        if p == "z" else [(g.CPLX_SPLIT, [3, 6])]
+        if p == "z" else [(g.CPLX_SPLIT, [3, 6]), (g.CPLX_SPLIT, [g.FP16X3])]
 
     def cname(meth, prm):
+        if p == "c" and prm == g.FP16X3:
+            return "fp16x3"
         return ("crt_n%d" if meth == g.CPLX_CRT else "ozaki_s%d" if p == "z" else "bf16x%d") % prm
 
     errs, qualified = {}, []
@@ -646,7 +657,8 @@ def run_complex(args, torch, rank, world):
             e2e = {"value": None, "error": repr(ex)}
 
     pk = peaks()
-    products = param if (p == "c" or method == g.CPLX_CRT) else (param * (param + 1)) // 2
+    products = (3 if param == g.FP16X3 else param) if (p == "c" or method == g.CPLX_CRT) \
+        else (param * (param + 1)) // 2
     pipe_flops = products * flops
     achieved = pipe_flops / (step_ms / 1e3) / 1e12
     form_name = cname(method, param)
@@ -685,7 +697,8 @@ def run_complex(args, torch, rank, world):
                      "chosen": form_name},
         "clocks": clocks,
         # per step: the operand embedding, then the form's own kernels
-        "gpu_launches": args.steps * (1 + (7 if method == g.CPLX_CRT else 6 if p == "z" else 3)),
+        "gpu_launches": args.steps * (1 + (7 if method == g.CPLX_CRT else 6 if p == "z" else
+                                           6 if param == g.FP16X3 else 3)),
     }
     if rank == 0:
         line["cpu_baseline"] = (cpu_baseline_complex(w, args.cpu_seconds) if not args.no_cpu
@@ -1024,7 +1037,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-pointer leg (profiling runs)")
     ap.add_argument("--form", default=None,
                     help="use this split form instead of timing the qualifying ones "
-                         "(crt_nN, ozaki_sS, bf16xP; profiling runs)")
+                         "(crt_nN, ozaki_sS, bf16xP, fp16x3; profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

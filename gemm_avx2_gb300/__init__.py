@@ -39,6 +39,8 @@ ERR_WORKSPACE = 6
 ERR_NOALLOC_LIMIT = 7
 
 # complex GEMM methods (gb300_cgemm / gb300_zgemm)
+# `products` code of the scaled 3xFP16 split SGEMM (GB300_SPLIT_FP16X3)
+FP16X3 = 0x103
 CPLX_4M = 0
 CPLX_3M = 1
 CPLX_SPLIT = 2
@@ -262,7 +264,8 @@ def gemm_device(precision, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta,
 
 def sgemm_bf16x(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, products=3,
                 stream=0, workspace=None, workspace_bytes=0) -> int:
-    """Split-precision SGEMM (3xBF16 / 6xBF16) on the tensor cores."""
+    """Split-precision SGEMM on the tensor cores: products 3 / 6 (3xBF16 / 6xBF16)
+    or FP16X3 (row/column-scaled 3xFP16)."""
     L = core()
     if workspace is None:
         return L.gb300_sgemm_bf16x(_b(transa), _b(transb), m, n, k, alpha, _ptr(A), lda,

@@ -164,21 +164,49 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
   cudaStream_t st = s->stage_stream;
   const bool need_ab = alpha != T(0) && k > 0;
   if (form != 0 && host_direct_ok(a, b, c)) {
-    // Split forms read A and B once (split / slice kernels, plain loads) and
-    // read and write each C element once (GEMM epilogue): they run directly on
-    // the caller's host memory over the coherent CPU-GPU link, no staging.
-    const size_t wneed = need_ab ? split_workspace_bytes(form - 1, m, n, k, param) : 0;
+    // Split forms read and write each C element once (GEMM epilogue): C stays
+    // in the caller's host memory, accessed over the coherent CPU-GPU link.
+    // The BF16-term split reads A and B once and does the same; the forms
+    // with a max |.| pass before the split (Ozaki, CRT, scaled FP16) read them
+    // twice, so A and B are first copied to HBM (one pass over the link).
+    int prm = param;
+    if (form == 1 && prm == 0) {
+      int ch = 0;
+      bf16x_resolve(m, n, k, &prm, &ch);
+    }
+    const bool two_pass = form >= 2 || prm == kFp16x3;
+    const T *ua = a, *ub = b;
+    int ulda = lda, uldb = ldb;
+    if (two_pass && need_ab) {
+      const int epl = 16 / (int)sizeof(T);
+      auto up = [&](int r) { return ((r > 1 ? r : 1) + epl - 1) / epl * epl; };
+      ulda = up(arows);
+      uldb = up(brows);
+      const size_t bA = (size_t)ulda * acols * sizeof(T), bB = (size_t)uldb * bcols * sizeof(T);
+      if (!grow(&s->stage[0], &s->stage_bytes[0], bA + 16) ||
+          !grow(&s->stage[1], &s->stage_bytes[1], bB + 16))
+        return GB300_ERR_NOMEM;
+      T *dA = static_cast<T *>(s->stage[0]), *dB = static_cast<T *>(s->stage[1]);
+      if (cudaMemcpy2DAsync(dA, ulda * sizeof(T), a, (size_t)lda * sizeof(T), arows * sizeof(T),
+                            acols, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+          cudaMemcpy2DAsync(dB, uldb * sizeof(T), b, (size_t)ldb * sizeof(T), brows * sizeof(T),
+                            bcols, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return GB300_ERR_CUDA;
+      ua = dA;
+      ub = dB;
+    }
+    const size_t wneed = need_ab ? split_workspace_bytes(form - 1, m, n, k, prm) : 0;
     void *ws = wneed ? cached_workspace(s, st, wneed) : nullptr;
     if (wneed && !ws) return GB300_ERR_NOMEM;
     int rc;
     if constexpr (sizeof(T) == 8)
-      rc = form == 3 ? crt_dgemm(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, param, ws,
-                                 wneed, st, s->err)
-                     : ozaki_dgemm(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, param,
+      rc = form == 3 ? crt_dgemm(ta, tb, m, n, k, alpha, ua, ulda, ub, uldb, beta, c, ldc, prm,
+                                 ws, wneed, st, s->err)
+                     : ozaki_dgemm(ta, tb, m, n, k, alpha, ua, ulda, ub, uldb, beta, c, ldc, prm,
                                    ws, wneed, st, s->err);
     else
-      rc = split_sgemm(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, param, ws, wneed, st,
-                       s->err);
+      rc = split_sgemm(ta, tb, m, n, k, alpha, ua, ulda, ub, uldb, beta, c, ldc, param, ws,
+                       wneed, st, s->err);  // param 0: products and chunk from the tune cache
     const cudaError_t e = cudaStreamSynchronize(st);
     if (rc != GB300_OK) return rc;
     if (e != cudaSuccess) return GB300_ERR_CUDA;
@@ -364,7 +392,7 @@ GB300_API int gb300_host_sgemm(char ta, char tb, int m, int n, int k, float alph
 GB300_API int gb300_host_sgemm_bf16x(char ta, char tb, int m, int n, int k, float alpha,
                                      const float *a, int lda, const float *b, int ldb, float beta,
                                      float *c, int ldc, int products) {
-  if (products != 0 && products != 3 && products != 6) return GB300_ERR_ARG;
+  if (products != 0 && !split_products_ok(products)) return GB300_ERR_ARG;
   return host_gemm<float>(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, 1, products);
 }
 GB300_API int gb300_host_dgemm_ozaki(char ta, char tb, int m, int n, int k, double alpha,
@@ -432,7 +460,7 @@ static bool complex_param_ok(bool dbl, int method, int param) {
   if (method == GB300_CPLX_CRT) return dbl && (param == 0 || (param >= 2 && param <= kCrtMaxModuli));
   if (method != GB300_CPLX_SPLIT) return true;
   return dbl ? (param == 0 || (param >= 2 && param <= kOzakiMaxSlices))
-             : (param == 0 || param == 3 || param == 6);
+             : (param == 0 || split_products_ok(param));
 }
 
 GB300_API size_t gb300_complex_workspace_bytes(int is_double, int method, char tb, int m, int n,
@@ -510,7 +538,7 @@ GB300_API int gb300_sgemm_bf16x_ws(char ta, char tb, int m, int n, int k, float 
                                    const float *A, int lda, const float *B, int ldb, float beta,
                                    float *C, int ldc, int products, void *ws, size_t ws_bytes,
                                    void *stream) {
-  if (products != 0 && products != 3 && products != 6) return GB300_ERR_ARG;
+  if (products != 0 && !split_products_ok(products)) return GB300_ERR_ARG;
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
   if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
   unsigned *err = device_error_word();
@@ -521,7 +549,7 @@ GB300_API int gb300_sgemm_bf16x_ws(char ta, char tb, int m, int n, int k, float 
 GB300_API int gb300_sgemm_bf16x(char ta, char tb, int m, int n, int k, float alpha,
                                 const float *A, int lda, const float *B, int ldb, float beta,
                                 float *C, int ldc, int products, void *stream) {
-  if (products != 0 && products != 3 && products != 6) return GB300_ERR_ARG;
+  if (products != 0 && !split_products_ok(products)) return GB300_ERR_ARG;
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
   if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
   DeviceState *s = dev_state();
@@ -572,7 +600,7 @@ GB300_API int gb300_sgemm_bf16x_run(int m, int n, int k, float alpha, float beta
                                     int ldc, int products, const void *ws, size_t ws_bytes,
                                     void *stream) {
   if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) ||
-      (products != 0 && products != 3 && products != 6))
+      (products != 0 && !split_products_ok(products)))
     return GB300_ERR_ARG;
   if (m == 0 || n == 0) return GB300_OK;
   unsigned *err = device_error_word();

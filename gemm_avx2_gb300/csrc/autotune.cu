@@ -4,7 +4,8 @@
 // src/gemm_set_parameters.h:1-61), which fix block sizes once per build for one
 // CPU model, by a run-time search on the GPU the library runs on:
 //
-//   BF16xP SGEMM: products P in {3, 6} x hi*hi chunk length in {2, 4, 8};
+//   split SGEMM : products P in {3, 6} (BF16 terms) or the scaled 3xFP16
+//                 form, x hi*hi chunk length in {2, 4, 8};
 //   Ozaki DGEMM : slice count S in [4, 12].
 //
 // A candidate qualifies when its max and Frobenius relative errors against a
@@ -238,7 +239,7 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
   TuneEntry best;
   bool found = false;
   if (kind == 0) {
-    const int Ps[2] = {3, 6}, chunks[3] = {2, 4, 8};
+    const int Ps[3] = {3, 6, kFp16x3}, chunks[3] = {2, 4, 8};
     for (int P : Ps)
       for (int c : chunks) {
         double ms = 0;

@@ -67,7 +67,7 @@ using namespace gb300;
 extern "C" __attribute__((visibility("default"))) int gb300_sgemm_bf16x_noalloc(
     char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda, const float *B,
     int ldb, float beta, float *C, int ldc, int products, void *stream) {
-  if (products != 3 && products != 6) return GB300_ERR_ARG;
+  if (!split_products_ok(products)) return GB300_ERR_ARG;
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
   if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
   const size_t need = split_workspace_bytes(0, m, n, k, products);

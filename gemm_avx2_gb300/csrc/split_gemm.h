@@ -15,10 +15,18 @@ constexpr int kOzakiBN = 256;      // tile columns of the Ozaki DGEMM
 constexpr int kOzakiMaxSlices = 12;
 constexpr int kCrtMaxModuli = 24;  // moduli of the CRT (modular-integer) FP64 form
 
+// `products` code of the scaled 3xFP16 SGEMM form (GB300_SPLIT_FP16X3): rows of
+// op(A) / columns of op(B) scaled by powers of two into the FP16 range, FP16
+// hi + lo terms, products hi*hi + (hi*lo + lo*hi) * 2^-11.
+constexpr int kFp16x3 = 0x103;
+inline bool split_products_ok(int p) { return p == 3 || p == 6 || p == kFp16x3; }
+inline int split_segments(int p) { return p == 6 ? 6 : 3; }
+
 size_t split_workspace_bytes(int kind, int m, int n, int k, int param);
 
-// products 0 = the autotuned choice for the shape class (default 6); chunk0 =
-// hi*hi chunk length in 64-wide K blocks (0 = tuned / knob / default).
+// products: 3 / 6 (BF16 terms), kFp16x3, or 0 = the autotuned choice for the
+// shape class (default 6); chunk0 = hi*hi chunk length in 64-wide K blocks
+// (0 = tuned / knob / default).
 int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
                 const float *B, int ldb, float beta, float *C, int ldc, int products, void *ws,
                 size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0 = 0);

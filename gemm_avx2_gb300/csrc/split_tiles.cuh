@@ -1,6 +1,6 @@
 // split_tiles.cuh -- device helpers shared by the split-form prepare kernels
 // (tc_gemm.cu, crt.cu): the coalesced 32 x 64 tile read of op(X), the per-row
-// scale exponent and exact power-of-two scaling.
+// scale exponent and exact power-of-two scaling (FP64 and FP32).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -43,11 +43,31 @@ __device__ __forceinline__ int row_exponent(unsigned long long amax_bits) {
   return e;
 }
 
+// The same for an FP32 row (max |x| in [2^(E-1), 2^E)).
+__device__ __forceinline__ int row_exponent_f32(unsigned amax_bits) {
+  const float m = __uint_as_float(amax_bits);
+  if (!(m <= 3.40282347e38f)) return kNonFiniteExp;  // Inf or NaN
+  if (m == 0.0f) return 0;
+  int e;
+  frexpf(m, &e);
+  return e;
+}
+
+// 2^e for e in [-126, 127], from the exponent bits.
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+
 // 2^e as a double when it is a normal number, built from the exponent bits
 // (one multiply then scales exactly); ldexp outside that range.
 __device__ __forceinline__ double scale_pow2(double v, int e) {
   if (e >= -1022 && e <= 1023) return v * __longlong_as_double((long long)(e + 1023) << 52);
   return ldexp(v, e);
+}
+
+// v * 2^e rounded once to FP32: one multiply when 2^e is a normal float;
+// otherwise exactly in FP64 (|e| < 400 here) and one conversion.
+__device__ __forceinline__ float scale_pow2f(float v, int e) {
+  if (e >= -126 && e <= 127) return v * pow2f(e);
+  return __double2float_rn(scale_pow2((double)v, e));
 }
 
 }  // namespace gb300

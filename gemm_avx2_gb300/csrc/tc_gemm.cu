@@ -24,6 +24,7 @@
 // accumulators let the epilogue of one tile/chunk overlap the next one's MMAs.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -34,6 +35,8 @@
 #include "split_tiles.cuh"
 
 namespace gb300 {
+
+static_assert(kFp16x3 == GB300_SPLIT_FP16X3, "products code of the scaled FP16 form");
 
 static inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 // grid.y of the split / slice kernels: the 32-row blocks of Rp, capped at the
@@ -67,12 +70,30 @@ struct SegMap {
   int term[6];
 };
 
-// out: Rp x (nseg * Kp) row-major BF16 (row stride ldo = nseg*Kp elements);
-// grid.y strides over the Rp / 32 row blocks.  Each thread writes 8
-// consecutive k of one row (16 bytes) per segment.
+// Scaled FP16 terms of one value of a row with scale exponent E (max |x| of
+// the row in [2^(E-1), 2^E)): y = x * 2^(15-E) lies in (-2^15, 2^15); hi =
+// fp16(y), lo = fp16((y - hi) * 2^11).  The residual y - hi is exact in FP32;
+// scaling up by 2^(15-E) is exact, scaling down (E > 15) only rounds values
+// below 2^-126, far under what hi and lo keep.  Returns (hi, lo) as bit patterns.
+__device__ __forceinline__ void f16_terms(float x, int s, unsigned short &hi, unsigned short &lo) {
+  const float y = s > 127 ? (x * pow2f(127)) * pow2f(s - 127) : x * pow2f(s);
+  const __half h = __float2half_rn(y);
+  const __half l = __float2half_rn((y - __half2float(h)) * 2048.0f);
+  hi = __half_as_ushort(h);
+  lo = __half_as_ushort(l);
+}
+
+// out: Rp x (nseg * Kp) row-major 16-bit terms (row stride ldo = nseg*Kp
+// elements); grid.y strides over the Rp / 32 row blocks.  Each thread writes
+// 8 consecutive k of one row (16 bytes) per segment.
+//   F16 = false: BF16 terms t0 = bf16(x), t1 = bf16(x - t0), t2 (nterms of them).
+//   F16 = true : the scaled FP16 (hi, lo) of f16_terms with the row exponents
+//                ex[] (Rp entries); a row whose max is not finite is all NaN.
+template <bool F16>
 __global__ void __launch_bounds__(256) split_bf16_kernel(const float *__restrict__ X, int ld, int R,
                                                          int K, int kcontig, int Rp, int Kp,
                                                          SegMap seg, int nterms,
+                                                         const int *__restrict__ ex,
                                                          __nv_bfloat16 *__restrict__ out,
                                                          int64_t ldo) {
   __shared__ float tile[32][65];
@@ -82,15 +103,36 @@ __global__ void __launch_bounds__(256) split_bf16_kernel(const float *__restrict
     load_tile_32x64<float>(X, ld, R, K, kcontig != 0, r0, k0, tile);
     __syncthreads();
     unsigned w[3][4];  // term t of the 8 values, packed in pairs
+    if (F16) {
+      const int e = ex[r0 + r];
+      if (e == kNonFiniteExp) {
 #pragma unroll
-    for (int j = 0; j < 8; j += 2) {
-      __nv_bfloat16 t0[3], t1[3];
-      bf16_terms(tile[r][kq + j], nterms, t0);
-      bf16_terms(tile[r][kq + j + 1], nterms, t1);
+        for (int t = 0; t < 3; ++t)
 #pragma unroll
-      for (int t = 0; t < 3; ++t)
-        w[t][j / 2] = (unsigned)__bfloat16_as_ushort(t0[t]) |
-                      ((unsigned)__bfloat16_as_ushort(t1[t]) << 16);
+          for (int q = 0; q < 4; ++q) w[t][q] = 0x7e007e00u;
+      } else {
+        const int sc = 15 - e;
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          unsigned short h0, l0, h1, l1;
+          f16_terms(tile[r][kq + j], sc, h0, l0);
+          f16_terms(tile[r][kq + j + 1], sc, h1, l1);
+          w[0][j / 2] = (unsigned)h0 | ((unsigned)h1 << 16);
+          w[1][j / 2] = (unsigned)l0 | ((unsigned)l1 << 16);
+          w[2][j / 2] = 0u;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        __nv_bfloat16 t0[3], t1[3];
+        bf16_terms(tile[r][kq + j], nterms, t0);
+        bf16_terms(tile[r][kq + j + 1], nterms, t1);
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+          w[t][j / 2] = (unsigned)__bfloat16_as_ushort(t0[t]) |
+                        ((unsigned)__bfloat16_as_ushort(t1[t]) << 16);
+      }
     }
     __nv_bfloat16 *row = out + (int64_t)(r0 + r) * ldo + k0 + kq;
     for (int sg = 0; sg < seg.nseg; ++sg) {
@@ -104,31 +146,46 @@ __global__ void __launch_bounds__(256) split_bf16_kernel(const float *__restrict
   }
 }
 
-// Ozaki step 1: per-row max |x| of op(X) as the bit pattern of a non-negative
-// double (monotone as an unsigned integer; NaN/Inf compare above finite values).
+// Ozaki step 1: per-row max |x| of op(X) as the bit pattern of the
+// non-negative value (monotone as an unsigned integer; NaN/Inf compare above
+// finite values), for FP64 and (scaled FP16 split) FP32 rows.
 // Short k ranges per grid row and unrolled loads keep enough reads in flight.
 // The k range of one warp (k-contiguous rows) or one thread (row-contiguous
 // columns) starts at these and doubles until the grid's y extent fits.
 constexpr int kAmaxSpanK = 1024;
 constexpr int kAmaxSpanR = 64;
-__global__ void __launch_bounds__(256) row_absmax_kernel(const double *__restrict__ X, int ld,
-                                                         int R, int K, int kcontig, int span,
-                                                         unsigned long long *__restrict__ amax) {
+template <typename T> struct AbsBits;
+template <> struct AbsBits<double> {
+  using U = unsigned long long;
+  static __device__ __forceinline__ U of(double x) { return (U)__double_as_longlong(fabs(x)); }
+  static __device__ __forceinline__ int exponent(U b) { return row_exponent(b); }
+};
+template <> struct AbsBits<float> {
+  using U = unsigned;
+  static __device__ __forceinline__ U of(float x) { return __float_as_uint(fabsf(x)); }
+  static __device__ __forceinline__ int exponent(U b) { return row_exponent_f32(b); }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) row_absmax_kernel(const T *__restrict__ X, int ld, int R,
+                                                         int K, int kcontig, int span,
+                                                         typename AbsBits<T>::U *__restrict__ amax) {
+  using U = typename AbsBits<T>::U;
   if (kcontig) {
     // one warp per (row, k range)
     const int r = (blockIdx.x * 8) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (r >= R) return;
     const int k0 = blockIdx.y * span, k1 = min(K, k0 + span);
-    unsigned long long m = 0;
-    const double *row = X + (int64_t)r * ld;
+    U m = 0;
+    const T *row = X + (int64_t)r * ld;
 #pragma unroll 8
     for (int kk = k0 + lane; kk < k1; kk += 32) {
-      const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(row[kk]));
+      const U b = AbsBits<T>::of(row[kk]);
       m = b > m ? b : m;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+      const U x = __shfl_xor_sync(0xffffffffu, m, o);
       m = x > m ? x : m;
     }
     if (lane == 0 && m) atomicMax(&amax[r], m);
@@ -137,11 +194,10 @@ __global__ void __launch_bounds__(256) row_absmax_kernel(const double *__restric
     const int r = blockIdx.x * 256 + threadIdx.x;
     if (r >= R) return;
     const int k0 = blockIdx.y * span, k1 = min(K, k0 + span);
-    unsigned long long m = 0;
+    U m = 0;
 #pragma unroll 8
     for (int kk = k0; kk < k1; ++kk) {
-      const unsigned long long b =
-          (unsigned long long)__double_as_longlong(fabs(X[r + (int64_t)kk * ld]));
+      const U b = AbsBits<T>::of(X[r + (int64_t)kk * ld]);
       m = b > m ? b : m;
     }
     if (m) atomicMax(&amax[r], m);
@@ -150,10 +206,11 @@ __global__ void __launch_bounds__(256) row_absmax_kernel(const double *__restric
 
 // Ozaki step 1b: the per-row exponents, once (the slice kernel and the GEMM
 // epilogue read them instead of recomputing frexp per element).
-__global__ void row_exponent_kernel(const unsigned long long *__restrict__ amax, int R,
+template <typename T>
+__global__ void row_exponent_kernel(const typename AbsBits<T>::U *__restrict__ amax, int R,
                                     int *__restrict__ ex) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < R) ex[r] = row_exponent(amax[r]);
+  if (r < R) ex[r] = AbsBits<T>::exponent(amax[r]);
 }
 
 // The S digits of 8 consecutive values of one row (row exponent e), packed as
@@ -227,14 +284,17 @@ __global__ void __launch_bounds__(256) ozaki_slice_kernel(
 //
 // The tensor core's FP32 accumulation over a long K' is less accurate than a
 // round-to-nearest FFMA chain (measured: both 3x and 6x forms ~9e-6 relative
-// at K' = 3*8192 and 6*8192).  So TMEM accumulates bounded chunks only; the 8
-// epilogue warps add every chunk into FP32 running sums in registers (round to
-// nearest) while the MMA warp fills the other TMEM buffer with the next chunk.
-// Chunks never cross a segment (one cross product), and their length follows
-// the segment's magnitude: order-2 products (~2^-16 of the result) need no
-// chunking, order-1 products (~2^-8) chunks of 16 blocks, the hi*hi segment
-// chunks of `chunk0` blocks.  Small segments come first in K', so each tile
-// starts with a long chunk that hides the previous tile's C store.
+// at K' = 3*8192 and 6*8192).  So TMEM accumulates bounded chunks only; the 16
+// epilogue warps (64 columns each) add every chunk into FP32 running sums in
+// registers (round to nearest) while the MMA warp fills the other TMEM buffer
+// with the next chunk.  Chunks never cross a segment (one cross product), and
+// their length follows the segment's magnitude: order-2 products (~2^-16 of
+// the result) need no chunking, order-1 products (~2^-8; ~2^-11 in the scaled
+// FP16 form) chunks of 16 (128) blocks, the hi*hi segment chunks of `chunk0`
+// blocks.  Small segments come first in K', so each tile starts with a long
+// chunk that hides the previous tile's C store.  (8 epilogue warps with 128
+// columns each spilled at the 168-register cap and drained a chunk in about
+// 2.7 us, twice the MMA time of a 4-block chunk.)
 // ===========================================================================
 struct Bf16xParams {
   int m, n, tiles_m, tiles_n, kblocks;
@@ -244,16 +304,22 @@ struct Bf16xParams {
   float *C;
   int ldc;
   unsigned *err;
+  // scaled FP16 form (kernel F16 = true): the running sums are multiplied by
+  // `rescale` before chunk `rescale_chunk` of each tile is added, and the
+  // result is scaled by 2^(expA[row] + expB[col] - 30).
+  int rescale_chunk;
+  float rescale;
+  const int *expA, *expB;
 };
 
 constexpr int kBxStages = 4;
-constexpr int kBxEpiWarps = 8;                      // 2 per TMEM lane quarter
+constexpr int kBxEpiWarps = 16;                     // 4 per TMEM lane quarter
 constexpr int kBxThreads = (2 + kBxEpiWarps) * 32;  // producer, MMA, epilogue
 constexpr int kBxABytes = kSplitBM * 128;
 constexpr int kBxBBytes = kBf16xBN * 128;
 constexpr int kBxStage = kBxABytes + kBxBBytes;
 constexpr int kBxSmem = kBxStages * kBxStage + 1024 + 256;
-constexpr int kBxColsPerWarp = kBf16xBN / 2;        // columns each epilogue warp owns
+constexpr int kBxColsPerWarp = kBf16xBN / (kBxEpiWarps / 4);  // columns each epilogue warp owns
 constexpr int kBxDefaultChunk = 4;                  // 4 x 64 = 256 K' per chunk
 
 // MC: 2-CTA clusters on the row tiles 2u and 2u + 1 of one column tile, in
@@ -261,7 +327,7 @@ constexpr int kBxDefaultChunk = 4;                  // 4 x 64 = 256 K' per chunk
 // of the shared B tile, multicast into both CTAs' stage (the B tensor map's box
 // is then 128 rows).  Each stage's empty barrier counts both CTAs' MMA commits,
 // since a stage holds data its peer wrote.  This halves the B tile's L2 reads.
-template <bool MC>
+template <bool MC, bool F16>
 __global__ void __launch_bounds__(kBxThreads, 1)
 bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   Bf16xParams p) {
@@ -332,7 +398,8 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16_f32(kSplitBM, kBf16xBN);
+      constexpr uint32_t idesc =
+          F16 ? idesc_f16_f32(kSplitBM, kBf16xBN) : idesc_bf16_f32(kSplitBM, kBf16xBN);
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
@@ -379,7 +446,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     }
   } else {
     const int q = warp & 3;             // TMEM lane quarter this warp may access
-    const int h = (warp - 2) >> 2;      // column half of the tile
+    const int h = (warp - 2) >> 2;      // column block of the tile
     const int row_in_tile = q * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + h * kBxColsPerWarp;
     uint32_t chunk = 0;
@@ -395,13 +462,17 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const uint32_t u = chunk >> 1;
         if (!mbar_wait(&accf[b], u & 1, p.err, kErrTimeoutAcc, abort_flag)) { ok = false; break; }
         tc_fence_after();
+        if (F16 && c == p.rescale_chunk) {  // the hi*lo segments end: scale them by 2^-11 (exact)
 #pragma unroll
-        for (int g = 0; g < kBxColsPerWarp / 32; ++g) {
-          uint32_t v[32];
-          tmem_ld32(lane_base + b * kBf16xBN + g * 32, v);
+          for (int j = 0; j < kBxColsPerWarp; ++j) run[j] *= p.rescale;
+        }
+#pragma unroll
+        for (int g = 0; g < kBxColsPerWarp / 16; ++g) {
+          uint32_t v[16];
+          tmem_ld16(lane_base + b * kBf16xBN + g * 16, v);
           tmem_ld_wait();
 #pragma unroll
-          for (int j = 0; j < 32; ++j) run[g * 32 + j] += __uint_as_float(v[j]);
+          for (int j = 0; j < 16; ++j) run[g * 16 + j] += __uint_as_float(v[j]);
         }
         tc_fence_before();
         __syncwarp();
@@ -411,22 +482,27 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       const int row = tm * kSplitBM + row_in_tile;
       if (row < p.m) {
         const int col0 = tn * kBf16xBN + h * kBxColsPerWarp;
+        // scaled FP16 form: the row and column scales come off here (a
+        // non-finite row or column is NaN already; its marker exponent is capped)
+        const int ea = F16 ? min(p.expA[row], 1024) - 30 : 0;
         // C in batches of 16 columns: all loads of a batch are issued before its
         // stores, so the batch pays one memory latency instead of sixteen
 #pragma unroll
-        for (int jb = 0; jb < kBxColsPerWarp; jb += 16) {
-          float cv[16];
+        for (int jb = 0; jb < kBxColsPerWarp; jb += 8) {
+          float cv[8];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < 8; ++j) {
             const int col = col0 + jb + j;
             cv[j] = (col < p.n) ? p.C[(int64_t)col * p.ldc + row] : 0.f;
           }
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < 8; ++j) {
             const int col = col0 + jb + j;
             if (col < p.n) {
+              const float v =
+                  F16 ? scale_pow2f(run[jb + j], ea + min(p.expB[col], 1024)) : run[jb + j];
               const float cb = (p.beta == 1.0f) ? cv[j] : cv[j] * p.beta;
-              p.C[(int64_t)col * p.ldc + row] = cb + p.alpha * run[jb + j];
+              p.C[(int64_t)col * p.ldc + row] = cb + p.alpha * v;
             }
           }
         }
@@ -786,9 +862,11 @@ size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
       int c = 0;
       bf16x_resolve(m, n, k, &param, &c);
     }
-    if (param != 3 && param != 6) return 0;
+    if (!split_products_ok(param)) return 0;
     const int64_t Mp = round_up(m, kSplitBM), Np = round_up(n, kBf16xBN);
-    return (size_t)((Mp + Np) * param * Kp * 2 + 1024);
+    // scaled FP16 form: + the max |.| bit patterns and exponents of rows / columns
+    const int64_t scales = param == kFp16x3 ? (Mp + Np) * 8 + 256 : 0;
+    return (size_t)((Mp + Np) * split_segments(param) * Kp * 2 + 1024 + scales);
   }
   int S = param > 0 ? param : ozaki_default_slices(m, n, k);
   if (S < 2 || S > kOzakiMaxSlices) return 0;
@@ -813,20 +891,60 @@ static int g_bf16x_chunk = 0;
 int bf16x_chunk_kblocks() { return g_bf16x_chunk; }
 void set_bf16x_chunk_kblocks(int c) { g_bf16x_chunk = c < 0 ? 0 : c; }
 
+// Per-row max |.| of op(A) and per-column max |.| of op(B), then their scale
+// exponents.  amax / ex hold Mp entries for the rows of op(A), then Np for
+// the columns of op(B); padding entries get exponent 0.
+template <typename T>
+static int scale_exponents(char ta, char tb, int m, int n, int k, const T *A, int lda, const T *B,
+                           int ldb, typename AbsBits<T>::U *amax, int *ex, int64_t Mp, int64_t Np,
+                           cudaStream_t st) {
+  const bool an = notrans(ta), bn = notrans(tb);
+  if (cudaMemsetAsync(amax, 0, (size_t)(Mp + Np) * sizeof(*amax), st) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  // A rows are k-contiguous when transposed, B columns when not.
+  auto absmax = [&](const T *X, int ld, int R, bool kc, typename AbsBits<T>::U *am) {
+    int64_t span = kc ? kAmaxSpanK : kAmaxSpanR;
+    while ((k + span - 1) / span > 65535) span *= 2;
+    const unsigned gy = (unsigned)((k + span - 1) / span);
+    if (kc)
+      row_absmax_kernel<T><<<dim3((unsigned)((R + 7) / 8), gy), 256, 0, st>>>(X, ld, R, k, 1,
+                                                                             (int)span, am);
+    else
+      row_absmax_kernel<T><<<dim3((unsigned)((R + 255) / 256), gy), 256, 0, st>>>(X, ld, R, k, 0,
+                                                                                 (int)span, am);
+  };
+  absmax(A, lda, m, !an, amax);
+  absmax(B, ldb, n, bn, amax + Mp);
+  row_exponent_kernel<T><<<(unsigned)((Mp + Np + 255) / 256), 256, 0, st>>>(amax, (int)(Mp + Np),
+                                                                             ex);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int row_scale_exponents(char ta, char tb, int m, int n, int k, const double *A, int lda,
+                        const double *B, int ldb, unsigned long long *amax, int *ex, int64_t Mp,
+                        int64_t Np, cudaStream_t st) {
+  return scale_exponents<double>(ta, tb, m, n, k, A, lda, B, ldb, amax, ex, Mp, Np, st);
+}
+
 // ----------------------------------------------------------------- BF16xP
 struct Bf16xLayout {
   int64_t Kp, Kld, Mp, Np;
-  __nv_bfloat16 *Ap, *Bp;
+  __nv_bfloat16 *Ap, *Bp;  // 16-bit terms (FP16 bit patterns in the scaled FP16 form)
+  unsigned *amax;          // scaled FP16 form: max |.| of rows of op(A), columns of op(B)
+  int *ex;                 //   and their scale exponents (Mp then Np entries)
 };
 static Bf16xLayout bf16x_layout(int m, int n, int k, int products, void *ws) {
   Bf16xLayout L;
   L.Kp = round_up(k, kSplitBK);
-  L.Kld = L.Kp * products;
+  L.Kld = L.Kp * split_segments(products);
   L.Mp = round_up(m, kSplitBM);
   L.Np = round_up(n, kBf16xBN);
   L.Ap = reinterpret_cast<__nv_bfloat16 *>((reinterpret_cast<uintptr_t>(ws) + 1023) &
                                            ~uintptr_t(1023));
   L.Bp = L.Ap + L.Mp * L.Kld;
+  L.amax = reinterpret_cast<unsigned *>(
+      (reinterpret_cast<uintptr_t>(L.Bp + L.Np * L.Kld) + 255) & ~uintptr_t(255));
+  L.ex = reinterpret_cast<int *>(L.amax + L.Mp + L.Np);
   return L;
 }
 
@@ -838,18 +956,72 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
     bf16x_resolve(m, n, k, &products, &c);
   }
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
-  if (ck == GB300_ERR_ARG || (products != 3 && products != 6)) return GB300_ERR_ARG;
+  if (ck == GB300_ERR_ARG || !split_products_ok(products)) return GB300_ERR_ARG;
   if (ck < 0 || k == 0) return GB300_OK;
   const size_t need = split_workspace_bytes(0, m, n, k, products);
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
   const Bf16xLayout L = bf16x_layout(m, n, k, products, ws);
   if (L.Kld > 0x7fffffff || L.Mp > 0x7fffffff || L.Np > 0x7fffffff) return GB300_ERR_ARG;
   const bool an = notrans(ta), bn = notrans(tb);
-  const int nterms = products == 3 ? 2 : 3;
-  split_bf16_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Mp)), 256, 0, st>>>(
-      A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, seg_map(products, true), nterms, L.Ap, L.Kld);
-  split_bf16_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Np)), 256, 0, st>>>(
-      B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, seg_map(products, false), nterms, L.Bp, L.Kld);
+  const dim3 ga((unsigned)(L.Kp / 64), row_blocks(L.Mp)), gb((unsigned)(L.Kp / 64), row_blocks(L.Np));
+  if (products == kFp16x3) {
+    const int rc = scale_exponents<float>(ta, tb, m, n, k, A, lda, B, ldb, L.amax, L.ex, L.Mp,
+                                          L.Np, st);
+    if (rc != GB300_OK) return rc;
+    split_bf16_kernel<true><<<ga, 256, 0, st>>>(A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp,
+                                                seg_map(3, true), 2, L.ex, L.Ap, L.Kld);
+    split_bf16_kernel<true><<<gb, 256, 0, st>>>(B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp,
+                                                seg_map(3, false), 2, L.ex + L.Mp, L.Bp, L.Kld);
+  } else {
+    const int nterms = products == 3 ? 2 : 3;
+    split_bf16_kernel<false><<<ga, 256, 0, st>>>(A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp,
+                                                 seg_map(products, true), nterms, nullptr, L.Ap,
+                                                 L.Kld);
+    split_bf16_kernel<false><<<gb, 256, 0, st>>>(B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp,
+                                                 seg_map(products, false), nterms, nullptr, L.Bp,
+                                                 L.Kld);
+  }
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+// Persistent launch: one CTA per SM (plain), or 2-CTA clusters sharing the B
+// tile when there are at least two row tiles (mc).
+template <bool F16>
+static int bf16x_launch(const CUtensorMap &tA, const CUtensorMap &tB, const Bf16xParams &p, bool mc,
+                        cudaStream_t st) {
+  if (!mc) {
+    if (cudaFuncSetAttribute(bf16x_gemm_kernel<false, F16>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kBxSmem) != cudaSuccess)
+      return GB300_ERR_CUDA;
+    const int ntiles = p.tiles_m * p.tiles_n;
+    const int grid = ntiles < sm_count() ? ntiles : sm_count();
+    bf16x_gemm_kernel<false, F16><<<grid, kBxThreads, kBxSmem, st>>>(tA, tB, p);
+    return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  }
+  if (cudaFuncSetAttribute(bf16x_gemm_kernel<true, F16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kBxSmem) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kBxThreads);
+  cfg.dynamicSmemBytes = kBxSmem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const int npairs = ((p.tiles_m + 1) / 2) * p.tiles_n;
+  int max_clusters = sm_count() / 2;
+  cfg.gridDim = dim3((unsigned)(2 * max_clusters));
+  int occ = 0;
+  if (cudaOccupancyMaxActiveClusters(&occ, bf16x_gemm_kernel<true, F16>, &cfg) == cudaSuccess &&
+      occ > 0 && occ < max_clusters)
+    max_clusters = occ;
+  cfg.gridDim = dim3((unsigned)(2 * (npairs < max_clusters ? npairs : max_clusters)));
+  if (cudaLaunchKernelEx(&cfg, bf16x_gemm_kernel<true, F16>, tA, tB, p) != cudaSuccess)
+    return GB300_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
@@ -860,7 +1032,7 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
     bf16x_resolve(m, n, k, &products, &c);
     if (chunk0 == 0) chunk0 = c;
   }
-  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || (products != 3 && products != 6))
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || !split_products_ok(products))
     return GB300_ERR_ARG;
   if (m == 0 || n == 0) return GB300_OK;
   if (alpha == 0.0f || k == 0)
@@ -880,53 +1052,36 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
   p.tiles_n = (int)(L.Np / kBf16xBN);
   p.kblocks = (int)(L.Kld / kSplitBK);
   p.seg_kblocks = (int)(L.Kp / kSplitBK);
-  p.nseg = products;
+  p.nseg = split_segments(products);
   {
     // order (i + j) of each segment's cross product, see seg_map()
     static const int order3[3] = {1, 1, 0}, order6[6] = {2, 2, 2, 1, 1, 0};
     const int c0 = chunk0 > 0                  ? chunk0
                    : bf16x_chunk_kblocks() > 0 ? bf16x_chunk_kblocks()
                                                : kBxDefaultChunk;
+    // order-1 products weigh 2^-8 of the result with BF16 terms, 2^-11 with the
+    // scaled FP16 terms: the latter tolerate 8x longer chunks at the same error
+    const int c1 = (products == kFp16x3 ? 32 : 4) * c0;
     for (int sg = 0; sg < 6; ++sg) {
-      const int ord = sg < products ? (products == 3 ? order3[sg] : order6[sg]) : 2;
-      p.chunk_len[sg] = ord == 0 ? c0 : (ord == 1 ? 4 * c0 : 0);
+      const int ord = sg < p.nseg ? (p.nseg == 3 ? order3[sg] : order6[sg]) : 2;
+      p.chunk_len[sg] = ord == 0 ? c0 : (ord == 1 ? c1 : 0);
     }
   }
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.err = err;
-  if (!mc) {
-    if (cudaFuncSetAttribute(bf16x_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kBxSmem) != cudaSuccess)
-      return GB300_ERR_CUDA;
-    const int ntiles = p.tiles_m * p.tiles_n;
-    const int grid = ntiles < sm_count() ? ntiles : sm_count();
-    bf16x_gemm_kernel<false><<<grid, kBxThreads, kBxSmem, st>>>(tA, tB, p);
-    return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  const bool f16 = products == kFp16x3;
+  p.rescale_chunk = -1;
+  p.rescale = 1.0f;
+  p.expA = p.expB = nullptr;
+  if (f16) {
+    // segments 0 and 1 (lo*hi, hi*lo) carry 2^11 x their value; their chunks
+    // come first, so the running sums are scaled once when segment 2 starts
+    const int cl = p.chunk_len[0] > 0 ? p.chunk_len[0] : p.seg_kblocks;
+    p.rescale_chunk = 2 * ((p.seg_kblocks + cl - 1) / cl);
+    p.rescale = 1.0f / 2048.0f;
+    p.expA = L.ex;
+    p.expB = L.ex + L.Mp;
   }
-  if (cudaFuncSetAttribute(bf16x_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kBxSmem) != cudaSuccess)
-    return GB300_ERR_CUDA;
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = 2;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.blockDim = dim3(kBxThreads);
-  cfg.dynamicSmemBytes = kBxSmem;
-  cfg.stream = st;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  const int npairs = ((p.tiles_m + 1) / 2) * p.tiles_n;
-  int max_clusters = sm_count() / 2;
-  cfg.gridDim = dim3((unsigned)(2 * max_clusters));
-  int occ = 0;
-  if (cudaOccupancyMaxActiveClusters(&occ, bf16x_gemm_kernel<true>, &cfg) == cudaSuccess && occ > 0 &&
-      occ < max_clusters)
-    max_clusters = occ;
-  cfg.gridDim = dim3((unsigned)(2 * (npairs < max_clusters ? npairs : max_clusters)));
-  if (cudaLaunchKernelEx(&cfg, bf16x_gemm_kernel<true>, tA, tB, p) != cudaSuccess)
-    return GB300_ERR_CUDA;
-  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  return f16 ? bf16x_launch<true>(tA, tB, p, mc, st) : bf16x_launch<false>(tA, tB, p, mc, st);
 }
 
 int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
@@ -938,7 +1093,7 @@ int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float 
     if (chunk0 == 0) chunk0 = c;
   }
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
-  if (ck == GB300_ERR_ARG || (products != 3 && products != 6)) return GB300_ERR_ARG;
+  if (ck == GB300_ERR_ARG || !split_products_ok(products)) return GB300_ERR_ARG;
   if (ck < 0) return GB300_OK;
   if (alpha == 0.0f || k == 0)  // no products to form: the plain path's beta handling
     return plain_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err);
@@ -973,30 +1128,6 @@ static OzakiLayout ozaki_layout(int m, int n, int k, int S, void *ws) {
   return L;
 }
 
-int row_scale_exponents(char ta, char tb, int m, int n, int k, const double *A, int lda,
-                        const double *B, int ldb, unsigned long long *amax, int *ex, int64_t Mp,
-                        int64_t Np, cudaStream_t st) {
-  // amax / ex hold Mp entries for the rows of op(A), then Np for the columns of op(B)
-  const bool an = notrans(ta), bn = notrans(tb);
-  if (cudaMemsetAsync(amax, 0, (size_t)(Mp + Np) * 8, st) != cudaSuccess) return GB300_ERR_CUDA;
-  // per-row / per-column max |.|: A rows are k-contiguous when transposed, B
-  // columns when not.
-  auto absmax = [&](const double *X, int ld, int R, bool kc, unsigned long long *am) {
-    int64_t span = kc ? kAmaxSpanK : kAmaxSpanR;
-    while ((k + span - 1) / span > 65535) span *= 2;
-    const unsigned gy = (unsigned)((k + span - 1) / span);
-    if (kc)
-      row_absmax_kernel<<<dim3((unsigned)((R + 7) / 8), gy), 256, 0, st>>>(X, ld, R, k, 1,
-                                                                          (int)span, am);
-    else
-      row_absmax_kernel<<<dim3((unsigned)((R + 255) / 256), gy), 256, 0, st>>>(X, ld, R, k, 0,
-                                                                              (int)span, am);
-  };
-  absmax(A, lda, m, !an, amax);
-  absmax(B, ldb, n, bn, amax + Mp);
-  row_exponent_kernel<<<(unsigned)((Mp + Np + 255) / 256), 256, 0, st>>>(amax, (int)(Mp + Np), ex);
-  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
-}
 
 int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
                   int ldb, int slices, void *ws, size_t ws_bytes, cudaStream_t st) {

@@ -90,10 +90,20 @@ int gb300_sgemm(char transa, char transb, int m, int n, int k, float alpha, cons
  *                 C += Ah*Bh + Ah*Bl + Al*Bh                  ("3xBF16")
  *   products = 6: three BF16 terms per operand, all cross products whose
  *                 order sum is <= 2                              ("6xBF16")
+ *   products = GB300_SPLIT_FP16X3: rows of op(A) and columns of op(B) scaled
+ *                 by powers of two into (-2^15, 2^15), then FP16 hi + FP16 lo
+ *                 (the residual times 2^11) on the FP16 tensor cores,
+ *                 C += 2^(e_i + f_j) (Ah*Bh + (Ah*Bl + Al*Bh) * 2^-11)
+ *                 ("3xFP16", the lo*lo product dropped).  Each operand keeps
+ *                 about 22 bits; values below 2^-50 of their row's (column's)
+ *                 max |.| are lost, so accuracy is normwise per row/column,
+ *                 like the Ozaki form.  A row or column holding Inf/NaN gives
+ *                 a NaN row/column of the product (as the BF16 forms).
  *   products = 0: the autotuned choice for the shape class (gb300_autotune),
  *                 else 6
  * Uses a device workspace of gb300_split_workspace_bytes() bytes, allocated
  * and cached by the library (the _ws variant takes the caller's instead). */
+enum { GB300_SPLIT_FP16X3 = 0x103 };
 int gb300_sgemm_bf16x(char transa, char transb, int m, int n, int k, float alpha, const float *A,
                       int lda, const float *B, int ldb, float beta, float *C, int ldc,
                       int products, void *stream);

@@ -14,6 +14,12 @@ methods so that the GPU split kernels can be checked bit for bit:
 * ozaki_gemm_model: the exact-integer product/recombination model of the GPU
   kernel (slice products grouped by t = i + j, weight 2^-7t, FP64 folding from
   the largest t down).
+* fp16x3_terms / fp16x3_model: the scaled 3xFP16 SGEMM form -- FP16 hi and
+  2^11-scaled lo terms with the lo*lo product dropped (Ootomo & Yokota,
+  "Recovering single precision accuracy from Tensor Cores while surpassing the
+  FP32 theoretical peak performance", IJHPCA 2022), applied to rows / columns
+  scaled by powers of two into the FP16 range (the row scaling of the Ozaki
+  scheme above).
 """
 from __future__ import annotations
 
@@ -97,3 +103,63 @@ def ozaki_gemm_model(A_op: np.ndarray, B_op: np.ndarray, S: int) -> np.ndarray:
             P += (As[sa - 1].astype(np.int64) @ Bs[sb - 1].astype(np.int64).T)
         res = P.astype(np.float64) * 2.0 ** (-7 * t) + res
     return np.ldexp(res, (E[:, None] + F[None, :]).astype(np.int64))
+
+
+NONFINITE_EXP = 0x40000000  # scale exponent marker of a row holding Inf or NaN
+
+
+def row_exponents_f32(X: np.ndarray) -> np.ndarray:
+    """E_r of each FP32 row (frexp exponent of max |x|, 0 for zero rows,
+    NONFINITE_EXP for rows holding Inf or NaN)."""
+    X = np.asarray(X, np.float32)
+    with np.errstate(invalid="ignore"):
+        bad = ~np.isfinite(X).all(axis=1) if X.shape[1] else np.zeros(X.shape[0], bool)
+        m = np.abs(np.where(np.isfinite(X), X, 0)).astype(np.float64).max(axis=1) \
+            if X.shape[1] else np.zeros(X.shape[0])
+    e = np.frexp(m)[1].astype(np.int64)
+    e[m == 0] = 0
+    e[bad] = NONFINITE_EXP
+    return e
+
+
+def fp16x3_terms(X: np.ndarray):
+    """(hi, lo, E) of an R x K FP32 op(X) view: y = x 2^(15 - E_r) in
+    (-2^15, 2^15) rounded once to FP32, hi = fp16(y), lo = fp16((y - hi) 2^11)
+    (float32 arrays holding FP16 values); rows with E = NONFINITE_EXP are NaN."""
+    X = np.asarray(X, np.float32)
+    E = row_exponents_f32(X)
+    ok = E != NONFINITE_EXP
+    s = np.where(ok, 15 - E, 0)
+    y = np.ldexp(X.astype(np.float64), s[:, None]).astype(np.float32)
+    with np.errstate(over="ignore", invalid="ignore"):
+        hi = y.astype(np.float16).astype(np.float32)
+        lo = ((y - hi) * np.float32(2048)).astype(np.float16).astype(np.float32)
+    hi[~ok] = np.nan
+    lo[~ok] = np.nan
+    return hi, lo, E
+
+
+def fp16x3_operand(X: np.ndarray, is_a: bool) -> np.ndarray:
+    """The concatenated K-major operand (R x 3K, FP16 bit patterns as uint16):
+    A = [lo | hi | hi], B = [hi | lo | hi] (products lo*hi, hi*lo, hi*hi)."""
+    hi, lo, _ = fp16x3_terms(X)
+    t = [hi, lo]
+    seg = SEGMENTS[3][0 if is_a else 1]
+    out = np.concatenate([t[i] for i in seg], axis=1).astype(np.float16).view(np.uint16)
+    out = out.copy()
+    out[np.isnan(np.concatenate([t[i] for i in seg], axis=1))] = 0x7E00
+    return out
+
+
+def fp16x3_model(A_op: np.ndarray, B_op: np.ndarray) -> np.ndarray:
+    """op(A) @ op(B) in FP64 from the represented operands: 2^(E_i + F_j - 30)
+    (hiA hiB + (hiA loB + loA hiB) 2^-11).  The GPU differs from it only by the
+    FP32 accumulation."""
+    ha, la, E = fp16x3_terms(A_op)
+    hb, lb, F = fp16x3_terms(np.asarray(B_op).T)
+    ha, la, hb, lb = (np.asarray(v, np.float64) for v in (ha, la, hb, lb))
+    with np.errstate(invalid="ignore", over="ignore"):
+        P = ha @ hb.T + (ha @ lb.T + la @ hb.T) / 2048.0
+    e = np.minimum(E, 1024)[:, None] + np.minimum(F, 1024)[None, :] - 30
+    with np.errstate(invalid="ignore", over="ignore"):
+        return np.ldexp(P, e)
