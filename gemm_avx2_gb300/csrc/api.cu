@@ -69,6 +69,8 @@ struct DeviceState {
   void *stage[3] = {nullptr, nullptr, nullptr};
   size_t stage_bytes[3] = {0, 0, 0};
   cudaStream_t stage_stream = nullptr;
+  cudaStream_t side_stream = nullptr;          // C staging beside the split forms' prepare
+  cudaEvent_t ev_start = nullptr, ev_c = nullptr;
   std::mutex mu;  // guards ws and staging (one host-pointer call at a time per device)
 };
 static constexpr int kMaxDevices = 64;
@@ -163,23 +165,31 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
     return GB300_ERR_CUDA;
   cudaStream_t st = s->stage_stream;
   const bool need_ab = alpha != T(0) && k > 0;
-  if (form != 0 && host_direct_ok(a, b, c)) {
-    // Split forms read and write each C element once (GEMM epilogue): C stays
-    // in the caller's host memory, accessed over the coherent CPU-GPU link.
-    // The BF16-term split reads A and B once and does the same; the forms
-    // with a max |.| pass before the split (Ozaki, CRT, scaled FP16) read them
-    // twice, so A and B are first copied to HBM (one pass over the link).
+  const bool direct = host_direct_ok(a, b, c);
+  if (form != 0 && direct) {
+    // Split forms on host memory the device can read.  The BF16-term split
+    // reads A and B once: it reads them in place over the coherent CPU-GPU
+    // link.  The forms with a max |.| pass before the split (Ozaki, CRT,
+    // scaled FP16) read them twice, so A and B are first copied to HBM.  The
+    // GEMM epilogues of the FP32 and Ozaki forms read and write C in place,
+    // overlapped with other tiles' MMAs.  The CRT form updates C in a
+    // separate, latency-bound reconstruction after its GEMMs: for large C, C
+    // is copied to HBM on a side stream while A and B are prepared and copied
+    // back at the end (measured: rank-256 Ozaki updates lose with staging,
+    // long-K CRT products gain).  All copies are SM loads/stores (about twice
+    // the copy engines' rate over the link).
     int prm = param;
     if (form == 1 && prm == 0) {
       int ch = 0;
       bf16x_resolve(m, n, k, &prm, &ch);
     }
     const bool two_pass = form >= 2 || prm == kFp16x3;
+    const int epl = 16 / (int)sizeof(T);
+    auto up = [&](int r) { return ((r > 1 ? r : 1) + epl - 1) / epl * epl; };
     const T *ua = a, *ub = b;
-    int ulda = lda, uldb = ldb;
+    T *uc = c;
+    int ulda = lda, uldb = ldb, uldc = ldc;
     if (two_pass && need_ab) {
-      const int epl = 16 / (int)sizeof(T);
-      auto up = [&](int r) { return ((r > 1 ? r : 1) + epl - 1) / epl * epl; };
       ulda = up(arows);
       uldb = up(brows);
       const size_t bA = (size_t)ulda * acols * sizeof(T), bB = (size_t)uldb * bcols * sizeof(T);
@@ -187,26 +197,67 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
           !grow(&s->stage[1], &s->stage_bytes[1], bB + 16))
         return GB300_ERR_NOMEM;
       T *dA = static_cast<T *>(s->stage[0]), *dB = static_cast<T *>(s->stage[1]);
-      if (cudaMemcpy2DAsync(dA, ulda * sizeof(T), a, (size_t)lda * sizeof(T), arows * sizeof(T),
-                            acols, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-          cudaMemcpy2DAsync(dB, uldb * sizeof(T), b, (size_t)ldb * sizeof(T), brows * sizeof(T),
-                            bcols, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      if (copy_2d(dA, ulda * sizeof(T), a, (size_t)lda * sizeof(T), arows * sizeof(T), acols,
+                  st) != GB300_OK ||
+          copy_2d(dB, uldb * sizeof(T), b, (size_t)ldb * sizeof(T), brows * sizeof(T), bcols,
+                  st) != GB300_OK)
         return GB300_ERR_CUDA;
       ua = dA;
       ub = dB;
+    }
+    const bool stage_c = need_ab && form == 3 && (size_t)m * n * sizeof(T) >= ((size_t)16 << 20);
+    if (stage_c) {
+      uldc = up(m);
+      if (!grow(&s->stage[2], &s->stage_bytes[2], (size_t)uldc * n * sizeof(T) + 16))
+        return GB300_ERR_NOMEM;
+      if (!s->side_stream &&
+          cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return GB300_ERR_CUDA;
+      if ((!s->ev_start && cudaEventCreateWithFlags(&s->ev_start, cudaEventDisableTiming) !=
+                               cudaSuccess) ||
+          (!s->ev_c && cudaEventCreateWithFlags(&s->ev_c, cudaEventDisableTiming) != cudaSuccess))
+        return GB300_ERR_CUDA;
+      uc = static_cast<T *>(s->stage[2]);
+      if (cudaEventRecord(s->ev_start, st) != cudaSuccess ||
+          cudaStreamWaitEvent(s->side_stream, s->ev_start, 0) != cudaSuccess ||
+          copy_2d(uc, uldc * sizeof(T), c, (size_t)ldc * sizeof(T), m * sizeof(T), n,
+                  s->side_stream) != GB300_OK ||
+          cudaEventRecord(s->ev_c, s->side_stream) != cudaSuccess)
+        return GB300_ERR_CUDA;
     }
     const size_t wneed = need_ab ? split_workspace_bytes(form - 1, m, n, k, prm) : 0;
     void *ws = wneed ? cached_workspace(s, st, wneed) : nullptr;
     if (wneed && !ws) return GB300_ERR_NOMEM;
     int rc;
-    if constexpr (sizeof(T) == 8)
-      rc = form == 3 ? crt_dgemm(ta, tb, m, n, k, alpha, ua, ulda, ub, uldb, beta, c, ldc, prm,
-                                 ws, wneed, st, s->err)
-                     : ozaki_dgemm(ta, tb, m, n, k, alpha, ua, ulda, ub, uldb, beta, c, ldc, prm,
-                                   ws, wneed, st, s->err);
-    else
-      rc = split_sgemm(ta, tb, m, n, k, alpha, ua, ulda, ub, uldb, beta, c, ldc, param, ws,
-                       wneed, st, s->err);  // param 0: products and chunk from the tune cache
+    if (!need_ab) {  // alpha == 0 or k == 0: the beta update only
+      if constexpr (sizeof(T) == 8)
+        rc = plain_dgemm(ta, tb, m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, c, ldc,
+                         st, s->err);
+      else
+        rc = plain_sgemm(ta, tb, m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, c, ldc,
+                         st, s->err);
+    } else {
+      // prepare (exponents, split / slices / residues of A and B), then the GEMM on C
+      if constexpr (sizeof(T) == 8)
+        rc = form == 3 ? crt_prepare(ta, tb, m, n, k, ua, ulda, ub, uldb, prm, ws, wneed, st)
+                       : ozaki_prepare(ta, tb, m, n, k, ua, ulda, ub, uldb, prm, ws, wneed, st);
+      else
+        rc = split_sgemm_prepare(ta, tb, m, n, k, ua, ulda, ub, uldb, param, ws, wneed, st);
+      if (rc == GB300_OK && stage_c && cudaStreamWaitEvent(st, s->ev_c, 0) != cudaSuccess)
+        rc = GB300_ERR_CUDA;
+      if (rc == GB300_OK) {
+        if constexpr (sizeof(T) == 8)
+          rc = form == 3 ? crt_run(m, n, k, alpha, beta, uc, uldc, prm, ws, wneed, st, s->err)
+                         : ozaki_run(m, n, k, alpha, beta, uc, uldc, prm, ws, wneed, st, s->err);
+        else  // param 0: products and chunk from the tune cache
+          rc = split_sgemm_run(m, n, k, alpha, beta, uc, uldc, param, ws, wneed, st, s->err);
+      }
+      if (rc == GB300_OK && stage_c)
+        rc = copy_2d(c, (size_t)ldc * sizeof(T), uc, uldc * sizeof(T), m * sizeof(T), n, st);
+    }
+    // the side stream's copy has finished too (also when a launch above failed)
+    if (stage_c && cudaStreamSynchronize(s->side_stream) != cudaSuccess && rc == GB300_OK)
+      rc = GB300_ERR_CUDA;
     const cudaError_t e = cudaStreamSynchronize(st);
     if (rc != GB300_OK) return rc;
     if (e != cudaSuccess) return GB300_ERR_CUDA;
@@ -228,17 +279,25 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
     return GB300_ERR_NOMEM;
   T *dA = static_cast<T *>(s->stage[0]), *dB = static_cast<T *>(s->stage[1]);
   T *dC = static_cast<T *>(s->stage[2]);
+  // SM loads/stores where the device can read the host memory (about twice
+  // the copy engines' rate over the coherent link), else the copy engines
+  auto copy = [&](void *dst, size_t dp, const void *src, size_t sp, size_t w, int cols,
+                  cudaMemcpyKind kind) -> cudaError_t {
+    if (direct) return copy_2d(dst, dp, src, sp, w, cols, st) == GB300_OK ? cudaSuccess
+                                                                        : cudaErrorUnknown;
+    return cudaMemcpy2DAsync(dst, dp, src, sp, w, cols, kind, st);
+  };
   cudaError_t e = cudaSuccess;
   if (need_ab) {
-    e = cudaMemcpy2DAsync(dA, dla * sizeof(T), a, (size_t)lda * sizeof(T), arows * sizeof(T),
-                          acols, cudaMemcpyHostToDevice, st);
+    e = copy(dA, dla * sizeof(T), a, (size_t)lda * sizeof(T), arows * sizeof(T), acols,
+             cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
-      e = cudaMemcpy2DAsync(dB, dlb * sizeof(T), b, (size_t)ldb * sizeof(T), brows * sizeof(T),
-                            bcols, cudaMemcpyHostToDevice, st);
+      e = copy(dB, dlb * sizeof(T), b, (size_t)ldb * sizeof(T), brows * sizeof(T), bcols,
+               cudaMemcpyHostToDevice);
   }
   if (e == cudaSuccess)
-    e = cudaMemcpy2DAsync(dC, dlc * sizeof(T), c, (size_t)ldc * sizeof(T), m * sizeof(T), n,
-                          cudaMemcpyHostToDevice, st);
+    e = copy(dC, dlc * sizeof(T), c, (size_t)ldc * sizeof(T), m * sizeof(T), n,
+             cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return GB300_ERR_CUDA;
   int rc;
   const int dlda = need_ab ? dla : up(arows), dldb = need_ab ? dlb : up(brows);
@@ -265,8 +324,8 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
     cudaStreamSynchronize(st);
     return rc;
   }
-  e = cudaMemcpy2DAsync(c, (size_t)ldc * sizeof(T), dC, dlc * sizeof(T), m * sizeof(T), n,
-                        cudaMemcpyDeviceToHost, st);
+  e = copy(c, (size_t)ldc * sizeof(T), dC, dlc * sizeof(T), m * sizeof(T), n,
+           cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return GB300_ERR_CUDA;
   unsigned word = 0;
@@ -316,11 +375,22 @@ static int host_complex(char ta, char tb, int m, int n, int k, const T *alpha, c
     cudaMemcpy(&word, s->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
     return word ? GB300_ERR_TIMEOUT : GB300_OK;
   };
-  if ((method == GB300_CPLX_SPLIT || method == GB300_CPLX_CRT) && host_direct_ok(a, b, c)) {
-    // the split method reads A and B once (pack and split kernels) and C once
-    // (epilogue): it runs on the caller's memory over the coherent link
+  const bool direct = host_direct_ok(a, b, c);
+  if (method == GB300_CPLX_SPLIT && sizeof(T) == 4 && direct) {
+    // the FP32 split method reads A and B once (pack and split kernels) and C
+    // once (GEMM epilogue, overlapped with the MMAs): it runs on the caller's
+    // memory over the coherent link.  The FP64 split forms read B twice and
+    // end in a latency-bound C update, so they take the staged path below.
     return finish(run(a, lda, b, ldb, c, ldc));
   }
+  // host <-> HBM copies: SM loads/stores where the device can read the host
+  // memory (about twice the copy engines' rate over the link)
+  auto copy = [&](void *dst, size_t dp, const void *src, size_t sp, size_t w, int cols,
+                  cudaMemcpyKind kind) -> cudaError_t {
+    if (direct) return copy_2d(dst, dp, src, sp, w, cols, st) == GB300_OK ? cudaSuccess
+                                                                        : cudaErrorUnknown;
+    return cudaMemcpy2DAsync(dst, dp, src, sp, w, cols, kind, st);
+  };
   const size_t E = 2 * sizeof(T);
   const int epl = 16 / (int)E > 0 ? 16 / (int)E : 1;
   auto up = [&](int r) { return ((r > 1 ? r : 1) + epl - 1) / epl * epl; };
@@ -336,21 +406,19 @@ static int host_complex(char ta, char tb, int m, int n, int k, const T *alpha, c
   T *dC = static_cast<T *>(s->stage[2]);
   cudaError_t e = cudaSuccess;
   if (need_ab) {
-    e = cudaMemcpy2DAsync(dA, dla * E, a, (size_t)lda * E, arows * E, acols,
-                          cudaMemcpyHostToDevice, st);
+    e = copy(dA, dla * E, a, (size_t)lda * E, arows * E, acols, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
-      e = cudaMemcpy2DAsync(dB, dlb * E, b, (size_t)ldb * E, brows * E, bcols,
-                            cudaMemcpyHostToDevice, st);
+      e = copy(dB, dlb * E, b, (size_t)ldb * E, brows * E, bcols, cudaMemcpyHostToDevice);
   }
   if (e == cudaSuccess)
-    e = cudaMemcpy2DAsync(dC, dlc * E, c, (size_t)ldc * E, m * E, n, cudaMemcpyHostToDevice, st);
+    e = copy(dC, dlc * E, c, (size_t)ldc * E, m * E, n, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return GB300_ERR_CUDA;
   const int rc = run(need_ab ? dA : nullptr, dla, need_ab ? dB : nullptr, dlb, dC, dlc);
   if (rc != GB300_OK) {
     cudaStreamSynchronize(st);
     return rc;
   }
-  e = cudaMemcpy2DAsync(c, (size_t)ldc * E, dC, dlc * E, m * E, n, cudaMemcpyDeviceToHost, st);
+  e = copy(c, (size_t)ldc * E, dC, dlc * E, m * E, n, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) {
     cudaStreamSynchronize(st);
     return GB300_ERR_CUDA;

@@ -57,6 +57,49 @@ __device__ __forceinline__ unsigned mod32(unsigned x, unsigned p, unsigned mg) {
   return r >= p ? r - p : r;
 }
 
+// BF16 bit patterns of two integers |v| < 2^22 packed in one word: 1.5 * 2^23
+// + v is exact in FP32, so subtracting 1.5 * 2^23 leaves v exactly; |v| <= 127
+// keeps the top 16 bits exact.
+__device__ __forceinline__ unsigned bf16x2_of_small_ints(int v0, int v1) {
+  const float f0 = __int_as_float(0x4B400000 + v0) - 12582912.0f;
+  const float f1 = __int_as_float(0x4B400000 + v1) - 12582912.0f;
+  return __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
+}
+
+// The N residue blocks of one thread's 8 values.  s = y0 + y1 (2^21 mod p) +
+// y2 (2^42 mod p) < 2^31 is y mod p up to multiples of p; Barrett with
+// mg = floor(2^32 / p) leaves r in [0, 2p), and min(r, r - p) (unsigned) maps
+// it into [0, p).  The symmetric residue of -y is minus that of y (p odd).
+// SLOW: some value needs the factor 2^t mod p (b > 63, or a row whose largest
+// value is subnormal).
+template <bool SLOW>
+__device__ __forceinline__ void residue_blocks(const unsigned (&y0)[8], const unsigned (&y1)[8],
+                                               const unsigned (&y2)[8], const int (&tp)[8],
+                                               const int (&sgn)[8], const CrtModParams &mp,
+                                               uint4 *dst, int64_t step) {
+  for (int i = 0; i < mp.N; ++i) {
+    const unsigned p = mp.p[i], mg = mp.mg[i], c21 = mp.c21[i], c42 = mp.c42[i];
+    const unsigned half = p >> 1;
+    int v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const unsigned sm = y0[j] + y1[j] * c21 + y2[j] * c42;
+      unsigned r = sm - __umulhi(sm, mg) * p;
+      r = min(r, r - p);
+      if (SLOW && tp[j] >= 0) {
+        const int t = tp[j];
+        unsigned p2 = mod32(1u << (t & 31), p, mg);
+        for (int w32 = t >> 5; w32 > 0; --w32) p2 = mod32(p2 * mp.pw32[i], p, mg);
+        r = mod32(r * p2, p, mg);
+      }
+      const int sym = (int)r - (r > half ? (int)p : 0);
+      v[j] = (sym ^ sgn[j]) - sgn[j];
+    }
+    dst[i * step] = make_uint4(bf16x2_of_small_ints(v[0], v[1]), bf16x2_of_small_ints(v[2], v[3]),
+                               bf16x2_of_small_ints(v[4], v[5]), bf16x2_of_small_ints(v[6], v[7]));
+  }
+}
+
 // Symmetric residues of A' = trunc(x 2^(b - e)) for N moduli, 8 consecutive k
 // of one row per thread, as BF16, block i at dst[i * step] (uint4 units).
 // |x| = M 2^base with M the 53-bit significand, so |x| 2^(b-e) = M 2^t,
@@ -65,7 +108,7 @@ __device__ __forceinline__ unsigned mod32(unsigned x, unsigned p, unsigned mg) {
 // 2^t mod p (2^(t mod 32) times t/32 factors of 2^32 mod p) applied after, is
 // cut into 21-bit chunks y0 + y1 2^21 + y2 2^42;
 // y mod p = (y0 + y1 (2^21 mod p) + y2 (2^42 mod p)) mod p, a sum below 2^31.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
     crt_residue_kernel(const double *__restrict__ X, int ld, int R, int K, int kcontig, int Rp,
                        int Kp, const int *__restrict__ ex, const __grid_constant__ CrtModParams mp,
                        __nv_bfloat16 *__restrict__ out) {
@@ -81,8 +124,9 @@ __global__ void __launch_bounds__(256)
     const bool bad = (e == kNonFiniteExp);  // row of Inf/NaN: zeros, the result is NaN
     uint4 *dst = reinterpret_cast<uint4 *>(out + (int64_t)gr * Kp + k0 + kq);
     unsigned y0[8], y1[8], y2[8];
-    int tp[8];         // t when t > 10 (the 2^t factor), else -1
-    unsigned neg = 0;  // sign bits
+    int tp[8];   // t when t > 10 (the 2^t factor), else -1
+    int sgn[8];  // -1 for negative values, else 0
+    bool slow = false;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const unsigned long long u = (unsigned long long)__double_as_longlong(tile[r][kq + j]);
@@ -96,31 +140,13 @@ __global__ void __launch_bounds__(256)
       y1[j] = (unsigned)(y >> 21) & 0x1fffff;
       y2[j] = (unsigned)(y >> 42);
       tp[j] = t > 10 ? t : -1;
-      neg |= (unsigned)(u >> 63) << j;
+      slow |= t > 10;
+      sgn[j] = -(int)(u >> 63);
     }
-    for (int i = 0; i < mp.N; ++i) {
-      const unsigned p = mp.p[i], mg = mp.mg[i], c21 = mp.c21[i], c42 = mp.c42[i];
-      unsigned w[4];
-#pragma unroll
-      for (int j = 0; j < 8; j += 2) {
-        unsigned h[2];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          unsigned rr = mod32(y0[j + q] + y1[j + q] * c21 + y2[j + q] * c42, p, mg);
-          if (tp[j + q] >= 0) {  // rare: b > 63, or a row whose largest value is subnormal
-            const int t = tp[j + q];
-            unsigned p2 = mod32(1u << (t & 31), p, mg);
-            for (int w32 = t >> 5; w32 > 0; --w32) p2 = mod32(p2 * mp.pw32[i], p, mg);
-            rr = mod32(rr * p2, p, mg);
-          }
-          if (((neg >> (j + q)) & 1) && rr) rr = p - rr;
-          const int sres = rr > (p >> 1) ? (int)rr - (int)p : (int)rr;
-          h[q] = __float_as_uint((float)sres) >> 16;  // |sres| <= 127: exact in BF16
-        }
-        w[j / 2] = h[0] | (h[1] << 16);
-      }
-      dst[i * step] = make_uint4(w[0], w[1], w[2], w[3]);
-    }
+    if (slow)
+      residue_blocks<true>(y0, y1, y2, tp, sgn, mp, dst, step);
+    else
+      residue_blocks<false>(y0, y1, y2, tp, sgn, mp, dst, step);
     __syncthreads();  // the tile is refilled for the next row block
   }
 }
@@ -144,27 +170,31 @@ struct CrtRecParams {
 // estimated from X's top bits in FP32 and corrected, the symmetric residue, and
 // one rounding to FP64.
 // r_g is byte e of word[g]; the weights of unused moduli (g >= N) are zero.
+// L = 32-bit limbs of M and the weights (M < 2^(32 L)); X needs L + 1.
+template <int L>
 __device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli], int e,
                                           const CrtRecParams &rp, bool &negative,
                                           unsigned long long &top_out, int &pos_out) {
-  unsigned long long acc[kLimbs] = {0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
+  unsigned long long acc[L];
+#pragma unroll
+  for (int l = 0; l < L; ++l) acc[l] = 0ull;
 #pragma unroll
   for (int g = 0; g < kCrtMaxModuli; ++g) {
     if (g >= rp.N) break;  // uniform across the grid
-    const unsigned r = (word[g] >> (8 * e)) & 0xffu;
+    const unsigned r = __byte_perm(word[g], 0u, 0x4440u + (unsigned)e);
 #pragma unroll
-    for (int l = 0; l < kLimbs; ++l) acc[l] += (unsigned long long)r * rp.w[g][l];
+    for (int l = 0; l < L; ++l) acc[l] += (unsigned long long)r * rp.w[g][l];
   }
-  unsigned X[kLimbs + 1];  // X < 2^13 M < 2^201
+  unsigned X[L + 1];  // X < 2^13 M
   {
     unsigned long long c = 0;
 #pragma unroll
-    for (int l = 0; l < kLimbs; ++l) {
+    for (int l = 0; l < L; ++l) {
       c += acc[l];
       X[l] = (unsigned)c;
       c >>= 32;
     }
-    X[kLimbs] = (unsigned)c;
+    X[L] = (unsigned)c;
   }
   // 53 bits of X from bit topshift (X >> topshift < 2^53)
   unsigned long long xt;
@@ -172,7 +202,7 @@ __device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli],
     const int li = rp.topshift >> 5, o = rp.topshift & 31;
     unsigned long long lo = 0, hi = 0;
 #pragma unroll
-    for (int l = 0; l < kLimbs + 1; ++l) {
+    for (int l = 0; l < L + 1; ++l) {
       if (l == li) lo = X[l];
       if (l == li + 1) lo |= (unsigned long long)X[l] << 32;
       if (l == li + 2) hi = X[l];
@@ -180,41 +210,41 @@ __device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli],
     xt = o ? (lo >> o) | (hi << (64 - o)) : lo;
   }
   const unsigned q = (unsigned)((float)xt * rp.inv_mt);
-  // P = X - q M, two's complement over kLimbs + 1 limbs
-  unsigned P[kLimbs + 1];
+  // P = X - q M, two's complement over L + 1 limbs
+  unsigned P[L + 1];
   {
     long long c = 0;
 #pragma unroll
-    for (int l = 0; l < kLimbs + 1; ++l) {
-      const unsigned long long qm = l < kLimbs ? (unsigned long long)q * rp.M[l] : 0ull;
+    for (int l = 0; l < L + 1; ++l) {
+      const unsigned long long qm = l < L ? (unsigned long long)q * rp.M[l] : 0ull;
       c += (long long)X[l] - (long long)(qm & 0xffffffffull);
       P[l] = (unsigned)c;
       c = (c >> 32) - (long long)(qm >> 32);
     }
   }
   // add M while negative, subtract M while >= M (q was off by at most one)
-  for (int it = 0; it < 3 && (int)P[kLimbs] < 0; ++it) {
+  for (int it = 0; it < 3 && (int)P[L] < 0; ++it) {
     unsigned long long c = 0;
 #pragma unroll
-    for (int l = 0; l < kLimbs + 1; ++l) {
-      c += (unsigned long long)P[l] + (l < kLimbs ? rp.M[l] : 0u);
+    for (int l = 0; l < L + 1; ++l) {
+      c += (unsigned long long)P[l] + (l < L ? rp.M[l] : 0u);
       P[l] = (unsigned)c;
       c >>= 32;
     }
   }
   for (int it = 0; it < 3; ++it) {
-    bool ge = P[kLimbs] != 0;
+    bool ge = P[L] != 0;
     if (!ge) {
       ge = true;
 #pragma unroll
-      for (int l = kLimbs - 1; l >= 0; --l)
+      for (int l = L - 1; l >= 0; --l)
         if (P[l] != rp.M[l]) { ge = P[l] > rp.M[l]; break; }
     }
     if (!ge) break;
     long long c = 0;
 #pragma unroll
-    for (int l = 0; l < kLimbs + 1; ++l) {
-      c += (long long)P[l] - (long long)(l < kLimbs ? rp.M[l] : 0u);
+    for (int l = 0; l < L + 1; ++l) {
+      c += (long long)P[l] - (long long)(l < L ? rp.M[l] : 0u);
       P[l] = (unsigned)c;
       c >>= 32;
     }
@@ -222,26 +252,26 @@ __device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli],
   // symmetric: P > (M - 1) / 2 stands for P - M; magnitude in mg
   bool gt = false;
 #pragma unroll
-  for (int l = kLimbs - 1; l >= 0; --l)
+  for (int l = L - 1; l >= 0; --l)
     if (P[l] != rp.half[l]) { gt = P[l] > rp.half[l]; break; }
-  unsigned mg[kLimbs];
+  unsigned mg[L];
   if (gt) {
     long long c = 0;
 #pragma unroll
-    for (int l = 0; l < kLimbs; ++l) {
+    for (int l = 0; l < L; ++l) {
       c += (long long)rp.M[l] - (long long)P[l];
       mg[l] = (unsigned)c;
       c >>= 32;
     }
   } else {
 #pragma unroll
-    for (int l = 0; l < kLimbs; ++l) mg[l] = P[l];
+    for (int l = 0; l < L; ++l) mg[l] = P[l];
   }
   negative = gt;
   // magnitude -> FP64 with one rounding: the top 64 bits, the rest as a sticky bit
   int tl = -1;
 #pragma unroll
-  for (int l = kLimbs - 1; l >= 0; --l)
+  for (int l = L - 1; l >= 0; --l)
     if (tl < 0 && mg[l]) tl = l;
   unsigned long long top = 0;
   int pos = 0;
@@ -249,7 +279,7 @@ __device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli],
     unsigned a2 = 0, a1 = 0, a0 = 0;
     bool sticky = false;
 #pragma unroll
-    for (int l = 0; l < kLimbs; ++l) {
+    for (int l = 0; l < L; ++l) {
       if (l == tl) a2 = mg[l];
       else if (l == tl - 1) a1 = mg[l];
       else if (l == tl - 2) a0 = mg[l];
@@ -300,6 +330,7 @@ __device__ __forceinline__ double crt_compose(unsigned long long top, int e2, bo
 // 4 consecutive rows of one column of C per thread: one 32-bit load per
 // modulus brings their residues (rows are contiguous in each residue plane).
 constexpr int kRecRows = 4;
+template <int L>
 __global__ void __launch_bounds__(256)
     crt_reconstruct_kernel(const uint8_t *__restrict__ rres, const int *__restrict__ expA,
                            const int *__restrict__ expB, const __grid_constant__ CrtRecParams rp) {
@@ -320,7 +351,7 @@ __global__ void __launch_bounds__(256)
       bool neg;
       unsigned long long top;
       int pos;
-      crt_value(word, e, rp, neg, top, pos);
+      crt_value<L>(word, e, rp, neg, top, pos);
       const int ea = expA[i];
       double v;
       if (ea == kNonFiniteExp || eb == kNonFiniteExp) {
@@ -573,7 +604,15 @@ int crt_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, 
   rp.alpha = alpha; rp.beta = beta; rp.C = C; rp.ldc = ldc;
   const dim3 grid((unsigned)((m + 256 * kRecRows - 1) / (256 * kRecRows)),
                   (unsigned)(n < 65535 ? n : 65535));
-  crt_reconstruct_kernel<<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp);
+  // limbs of M: 4 up to 16 moduli, 5 up to 20, 6 up to 24
+  const int limbs = (bl + 31) / 32 < 2 ? 2 : (bl + 31) / 32;
+  switch (limbs) {
+    case 2: crt_reconstruct_kernel<2><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
+    case 3: crt_reconstruct_kernel<3><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
+    case 4: crt_reconstruct_kernel<4><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
+    case 5: crt_reconstruct_kernel<5><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
+    default: crt_reconstruct_kernel<6><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
+  }
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 

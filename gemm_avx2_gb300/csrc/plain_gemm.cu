@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 #include "plain_gemm.h"
@@ -339,6 +340,50 @@ dgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 }
 
 // C *= beta over the m x n window (alpha == 0, or k == 0 with the +0 of an empty sum).
+// Column c of the copy is `wv` vectors V; each thread moves 4 of them (loads
+// issued before stores), 256 threads cover 1024 vectors of one column.
+template <typename V>
+__global__ void __launch_bounds__(256) copy_2d_kernel(V *__restrict__ dst, size_t dp,
+                                                      const V *__restrict__ src, size_t sp,
+                                                      size_t wv, int cols) {
+  const size_t c0 = (size_t)blockIdx.x * 1024 + threadIdx.x;
+  for (int col = blockIdx.y; col < cols; col += gridDim.y) {
+    const V *s = src + (size_t)col * sp;
+    V *d = dst + (size_t)col * dp;
+    V v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (c0 + 256 * u < wv) v[u] = s[c0 + 256 * u];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (c0 + 256 * u < wv) d[c0 + 256 * u] = v[u];
+  }
+}
+
+int copy_2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, int cols,
+            cudaStream_t st) {
+  if (width == 0 || cols <= 0) return GB300_OK;
+  const uintptr_t align = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) |
+                          dpitch | spitch | width;
+  auto launch = [&](auto *tag) {
+    using V = std::remove_pointer_t<decltype(tag)>;
+    const size_t wv = width / sizeof(V);
+    const dim3 grid((unsigned)((wv + 1023) / 1024), (unsigned)(cols < 65535 ? cols : 65535));
+    copy_2d_kernel<V><<<grid, 256, 0, st>>>(static_cast<V *>(dst), dpitch / sizeof(V),
+                                             static_cast<const V *>(src), spitch / sizeof(V), wv,
+                                             cols);
+  };
+  if ((align & 15) == 0)
+    launch(static_cast<uint4 *>(nullptr));
+  else if ((align & 7) == 0)
+    launch(static_cast<uint2 *>(nullptr));
+  else if ((align & 3) == 0)
+    launch(static_cast<unsigned *>(nullptr));
+  else
+    launch(static_cast<uint8_t *>(nullptr));
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
 template <typename T>
 __global__ void scale_c_kernel(int m, int n, T beta, T add, T *__restrict__ C, int ldc) {
   const int64_t total = (int64_t)m * n;

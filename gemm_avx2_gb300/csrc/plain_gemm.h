@@ -40,6 +40,13 @@ inline bool tma_ok(const void *p, int ld, size_t elem) {
 bool encode_2d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t rows, int64_t cols,
                int64_t ld, int box_rows, int box_cols, bool swizzle128);
 
+// dst (dpitch bytes between columns) = src (spitch) over `cols` columns of
+// `width` bytes each, by SM loads and stores: on a coherent CPU-GPU link the
+// SMs read host memory faster than the copy engines.  Either side may be host
+// memory the device can dereference.
+int copy_2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, int cols,
+            cudaStream_t st);
+
 int plain_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                 const double *B, int ldb, double beta, double *C, int ldc, cudaStream_t st,
                 unsigned *err);
