@@ -432,6 +432,14 @@ def run_ours(args, torch, rank, world):
             "kernel_ms": round(gemm_ms, 4), "prepare_ms": round(prep_ms, 4),
             "peak_source": "%s bf16 burst (MEASURED_PEAKS.json)" % pk["source"],
             "algorithmic_flops_per_launch": pipe_flops}
+    # the operands' and C's own bytes (A and B read once, C read and written)
+    # over the same GEMM time: the HBM side of the roofline (skinny shapes)
+    esz = 8 if is_d else 4
+    io_bytes = esz * (m * k + k * n + 2 * m * n)
+    roof["hbm"] = {"achieved": round(io_bytes / (gemm_ms / 1e3) / 1e9, 1), "unit": "GB/s",
+                   "peak": pk["hbm_gbs"], "frac": round(io_bytes / (gemm_ms / 1e3) / 1e9 /
+                                                        pk["hbm_gbs"], 4),
+                   "algorithmic_bytes": io_bytes}
     form_name = name_of(form, param)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world,

@@ -298,8 +298,13 @@ __global__ void __launch_bounds__(256) ozaki_slice_kernel(
 // ===========================================================================
 struct Bf16xParams {
   int m, n, tiles_m, tiles_n, kblocks;
-  int seg_kblocks, nseg;
-  int chunk_len[6];  // per segment: 64-wide K blocks per chunk (0 = whole segment)
+  // K' is cut into runs of consecutive segments whose products have the same
+  // order (i + j): run r ends at block run_end<r> and is accumulated in TMEM
+  // chunks of run_chunk<r> blocks (0 = the whole run).  Scalars, not arrays,
+  // so that no parameter is indexed at run time.
+  int nruns;
+  int run_end0, run_end1, run_end2;
+  int run_chunk0, run_chunk1, run_chunk2;
   float alpha, beta;
   float *C;
   int ldc;
@@ -369,10 +374,16 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     tile_coords(u, pm, p.tiles_n, MC ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
     tm = MC ? 2 * um + (int)rank : um;  // MC: a row tile past the end is zero-filled, not stored
   };
+  auto run_end = [&](int r) { return r == 0 ? p.run_end0 : (r == 1 ? p.run_end1 : p.run_end2); };
+  auto run_chunk = [&](int r) {  // chunk length of run r in K blocks
+    const int len = run_end(r) - (r == 0 ? 0 : run_end(r - 1));
+    const int cl = r == 0 ? p.run_chunk0 : (r == 1 ? p.run_chunk1 : p.run_chunk2);
+    return cl > 0 ? cl : len;
+  };
   int nchunks = 0;
-  for (int sg = 0; sg < p.nseg; ++sg) {
-    const int cl = p.chunk_len[sg] > 0 ? p.chunk_len[sg] : p.seg_kblocks;
-    nchunks += (p.seg_kblocks + cl - 1) / cl;
+  for (int r = 0; r < p.nruns; ++r) {
+    const int len = run_end(r) - (r == 0 ? 0 : run_end(r - 1));
+    nchunks += (len + run_chunk(r) - 1) / run_chunk(r);
   }
 
   if (warp == 0) {
@@ -403,12 +414,11 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
-        int sg = 0, c0 = 0;
+        int rn = 0, c0 = 0;
         for (int c = 0; c < nchunks && ok; ++c, ++chunk) {
-          // chunk c covers K blocks [c0, c1) of segment sg
-          const int cl = p.chunk_len[sg] > 0 ? p.chunk_len[sg] : p.seg_kblocks;
-          const int seg_end = (sg + 1) * p.seg_kblocks;
-          const int c1 = min(seg_end, c0 + cl);
+          // chunk c covers K blocks [c0, c1) of run rn
+          const int rend = run_end(rn);
+          const int c1 = min(rend, c0 + run_chunk(rn));
           const int b = chunk & 1;
           const uint32_t u = chunk >> 1;
           if (!mbar_wait(&acce[b], (u & 1) ^ 1, p.err, kErrTimeoutMma, abort_flag)) {
@@ -437,7 +447,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           }
           if (ok) umma_commit(&accf[b]);
           c0 = c1;
-          if (c0 == seg_end) ++sg;
+          if (c0 == rend) ++rn;
         }
       }
       // every issued MMA has completed before TMEM is released
@@ -1051,20 +1061,28 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
   p.tiles_m = (int)(L.Mp / kSplitBM);
   p.tiles_n = (int)(L.Np / kBf16xBN);
   p.kblocks = (int)(L.Kld / kSplitBK);
-  p.seg_kblocks = (int)(L.Kp / kSplitBK);
-  p.nseg = split_segments(products);
+  const int skb = (int)(L.Kp / kSplitBK);  // K blocks of one segment
   {
-    // order (i + j) of each segment's cross product, see seg_map()
-    static const int order3[3] = {1, 1, 0}, order6[6] = {2, 2, 2, 1, 1, 0};
+    // segments by order (i + j) of their cross product, see seg_map():
+    // P = 6: 2 2 2 1 1 0; P = 3 and the scaled FP16 form: 1 1 0.  Segments
+    // of one order share chunks, so short K (k = 256: 4 blocks a segment)
+    // gets few TMEM drains per tile.
     const int c0 = chunk0 > 0                  ? chunk0
                    : bf16x_chunk_kblocks() > 0 ? bf16x_chunk_kblocks()
                                                : kBxDefaultChunk;
     // order-1 products weigh 2^-8 of the result with BF16 terms, 2^-11 with the
     // scaled FP16 terms: the latter tolerate 8x longer chunks at the same error
     const int c1 = (products == kFp16x3 ? 32 : 4) * c0;
-    for (int sg = 0; sg < 6; ++sg) {
-      const int ord = sg < p.nseg ? (p.nseg == 3 ? order3[sg] : order6[sg]) : 2;
-      p.chunk_len[sg] = ord == 0 ? c0 : (ord == 1 ? c1 : 0);
+    if (split_segments(products) == 6) {
+      p.nruns = 3;
+      p.run_end0 = 3 * skb; p.run_chunk0 = 0;   // order 2: unchunked
+      p.run_end1 = 5 * skb; p.run_chunk1 = c1;  // order 1
+      p.run_end2 = 6 * skb; p.run_chunk2 = c0;  // hi*hi
+    } else {
+      p.nruns = 2;
+      p.run_end0 = 2 * skb; p.run_chunk0 = c1;
+      p.run_end1 = 3 * skb; p.run_chunk1 = c0;
+      p.run_end2 = 3 * skb; p.run_chunk2 = c0;
     }
   }
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.err = err;
@@ -1073,10 +1091,9 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
   p.rescale = 1.0f;
   p.expA = p.expB = nullptr;
   if (f16) {
-    // segments 0 and 1 (lo*hi, hi*lo) carry 2^11 x their value; their chunks
-    // come first, so the running sums are scaled once when segment 2 starts
-    const int cl = p.chunk_len[0] > 0 ? p.chunk_len[0] : p.seg_kblocks;
-    p.rescale_chunk = 2 * ((p.seg_kblocks + cl - 1) / cl);
+    // segments 0 and 1 (lo*hi, hi*lo, run 0) carry 2^11 x their value; their
+    // chunks come first, so the running sums are scaled once when run 1 starts
+    p.rescale_chunk = (p.run_end0 + p.run_chunk0 - 1) / p.run_chunk0;
     p.rescale = 1.0f / 2048.0f;
     p.expA = L.ex;
     p.expB = L.ex + L.Mp;
