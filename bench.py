@@ -466,9 +466,11 @@ def run_ours(args, torch, rank, world):
                      "split": {p: {"max_rel": e[0], "fro_rel": e[1]} for p, e in errs.items()},
                      "chosen": form_name},
         "clocks": clocks,
-        # split kernels + GEMM; the FP16 form adds 2 max |.| passes and the exponents
-        "gpu_launches": args.steps * ({"bf16x": 3, "ozaki": 6, "crt": 7}[form] +
-                                      (3 if form == "bf16x" and param == g.FP16X3 else 0)),
+        # per step: the split (both operands in one launch) and the GEMM; the
+        # two-pass forms add one max |.| launch (both operands, exponents by
+        # its last CTA); the CRT form adds the reconstruction
+        "gpu_launches": args.steps * ({"bf16x": 2, "ozaki": 3, "crt": 4}[form] +
+                                      (1 if form == "bf16x" and param == g.FP16X3 else 0)),
     }
     if rank == 0:
         line["cpu_baseline"] = (cpu_baseline(w, args.cpu_seconds) if not args.no_cpu
@@ -708,8 +710,8 @@ def run_complex(args, torch, rank, world):
                      "chosen": form_name},
         "clocks": clocks,
         # per step: the operand embedding, then the form's own kernels
-        "gpu_launches": args.steps * (1 + (7 if method == g.CPLX_CRT else 6 if p == "z" else
-                                           6 if param == g.FP16X3 else 3)),
+        "gpu_launches": args.steps * (1 + (4 if method == g.CPLX_CRT else 3 if p == "z" else
+                                           3 if param == g.FP16X3 else 2)),
     }
     if rank == 0:
         line["cpu_baseline"] = (cpu_baseline_complex(w, args.cpu_seconds) if not args.no_cpu
@@ -857,7 +859,7 @@ def run_grouped(args, torch, rank, world):
                      "peak_source": "FP64 1.05 and FP32 73 TFLOP/s measured by microbenchmark"},
         "accuracy": {"plain": err_plain, "split": err_split, "samples": "8 entries x 48 problems"},
         "clocks": clocks,
-        "gpu_launches": args.steps * sum(7 if p["precision"] == "d" else 3 for p in probs),
+        "gpu_launches": args.steps * sum(4 if p["precision"] == "d" else 2 for p in probs),
         "e2e": {"value": None, "skipped": "device-pointer grouped API"},
     }
     gp.destroy()

@@ -750,10 +750,14 @@ GB300_API int gb300_gemm_grouped(const gb300_gemm_problem *problems, int count, 
   return grouped_plain(problems, count, ws, need, st, s->err);
 }
 
-// Split-form batches are captured as kGraphBranches parallel branches (forked
-// from and joined into the capture stream), problems assigned longest-work-
-// first to the least-loaded branch; each branch has its own workspace.
-constexpr int kGraphBranches = 16;
+// Split-form batches are captured as parallel branches (forked from and
+// joined into the capture stream), problems assigned longest-work-first to the
+// least-loaded branch; each branch has its own workspace.  Small problems fill
+// a few SMs each, so the branch count sets how much of the GPU a batch uses
+// (GB300_TUNE_GRAPH_BRANCHES, read when a graph is created).
+constexpr int kGraphBranches = 64;  // upper bound
+constexpr int kDefaultGraphBranches = 32;  // 10.3 TFLOP/s at 16, 11.9 at 32, 12.0 at 64 (1024 problems)
+static int g_graph_branches = kDefaultGraphBranches;
 
 struct gb300_grouped_graph_s {
   cudaGraph_t graph = nullptr;
@@ -795,6 +799,7 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
   std::vector<uint8_t> blob;
   int used = 0, tiles = 0;
   std::vector<int> branch_of(count > 0 ? count : 1, 0);
+  const int nbr = g_graph_branches;
   size_t wneed_b[kGraphBranches] = {0};
   cudaStream_t bs[kGraphBranches] = {nullptr};
   cudaEvent_t fork = nullptr, join[kGraphBranches] = {nullptr};
@@ -818,7 +823,7 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
     double load[kGraphBranches] = {0};
     for (int i : order) {
       int b = 0;
-      for (int j = 1; j < kGraphBranches; ++j)
+      for (int j = 1; j < nbr; ++j)
         if (load[j] < load[b]) b = j;
       load[b] += work(i);
       branch_of[i] = b;
@@ -842,11 +847,11 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
         else rc2 = grouped_launch_blob(g->meta, used, tiles, cs, s->err);
       }
     } else {
-      // fork kGraphBranches branches off the capture stream; each branch runs
-      // its problems' split-form calls in order on its own workspace; join.
+      // fork nbr branches off the capture stream; each branch runs its
+      // problems' split-form calls in order on its own workspace; join.
       bool forked = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess &&
                     cudaEventRecord(fork, cs) == cudaSuccess;
-      for (int b = 0; b < kGraphBranches && forked; ++b)
+      for (int b = 0; b < nbr && forked; ++b)
         forked = cudaStreamCreateWithFlags(&bs[b], cudaStreamNonBlocking) == cudaSuccess &&
                  cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming) == cudaSuccess &&
                  cudaStreamWaitEvent(bs[b], fork, 0) == cudaSuccess;
@@ -867,7 +872,7 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
                             static_cast<float *>(q.C), q.ldc, 6, g->ws[b], wneed_b[b], bs[b],
                             s->err);
       }
-      for (int b = 0; b < kGraphBranches && forked; ++b)
+      for (int b = 0; b < nbr && forked; ++b)
         if (cudaEventRecord(join[b], bs[b]) != cudaSuccess ||
             cudaStreamWaitEvent(cs, join[b], 0) != cudaSuccess)
           rc2 = GB300_ERR_CUDA;
@@ -997,6 +1002,10 @@ GB300_API int gb300_tune_param(int param, int value) {
   switch (param) {
     case GB300_TUNE_BF16X_CHUNK:
       set_bf16x_chunk_kblocks(value);
+      return GB300_OK;
+    case GB300_TUNE_GRAPH_BRANCHES:
+      if (value < 0 || value > kGraphBranches) return GB300_ERR_ARG;
+      g_graph_branches = value ? value : kDefaultGraphBranches;
       return GB300_OK;
     default:
       return GB300_ERR_ARG;

@@ -108,10 +108,16 @@ __device__ __forceinline__ void residue_blocks(const unsigned (&y0)[8], const un
 // 2^t mod p (2^(t mod 32) times t/32 factors of 2^32 mod p) applied after, is
 // cut into 21-bit chunks y0 + y1 2^21 + y2 2^42;
 // y mod p = (y0 + y1 (2^21 mod p) + y2 (2^42 mod p)) mod p, a sum below 2^31.
+// Both operands in one launch (blockIdx.z).
 __global__ void __launch_bounds__(256, 3)
-    crt_residue_kernel(const double *__restrict__ X, int ld, int R, int K, int kcontig, int Rp,
-                       int Kp, const int *__restrict__ ex, const __grid_constant__ CrtModParams mp,
-                       __nv_bfloat16 *__restrict__ out) {
+    crt_residue_kernel(const __grid_constant__ OperandPair op,
+                       const __grid_constant__ CrtModParams mp) {
+  const int z = blockIdx.z;
+  const double *__restrict__ X = z ? op.X1 : op.X0;
+  const int ld = z ? op.ld1 : op.ld0, R = z ? op.R1 : op.R0, kcontig = z ? op.kc1 : op.kc0;
+  const int Rp = z ? op.Rp1 : op.Rp0, K = op.K, Kp = op.Kp;
+  const int *__restrict__ ex = z ? op.ex1 : op.ex0;
+  __nv_bfloat16 *__restrict__ out = static_cast<__nv_bfloat16 *>(z ? op.out1 : op.out0);
   __shared__ double tile[32][65];
   const int k0 = blockIdx.x * 64;
   const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
@@ -463,7 +469,8 @@ CrtLayout crt_layout(int m, int n, int k, int N, void *ws) {
   L.As = reinterpret_cast<__nv_bfloat16 *>(base);
   L.Bs = L.As + N * L.Mp * L.Kp;
   L.amax = reinterpret_cast<unsigned long long *>(L.Bs + N * L.Np * L.Kp);
-  L.ex = reinterpret_cast<int *>(L.amax + L.Mp + L.Np);
+  // 16 bytes after amax: the max pass's completion counter
+  L.ex = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(L.amax + L.Mp + L.Np) + 16);
   L.rres = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(L.ex + L.Mp + L.Np) + 255) & ~uintptr_t(255));
   return L;
@@ -543,10 +550,13 @@ int crt_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda,
   }
   auto row_blocks = [](int64_t Rp) { return (unsigned)(Rp / 32 < 65535 ? Rp / 32 : 65535); };
   const bool an = notrans(ta), bn = notrans(tb);
-  crt_residue_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Mp)), 256, 0, st>>>(
-      A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, L.ex, mp, L.As);
-  crt_residue_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Np)), 256, 0, st>>>(
-      B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, L.ex + L.Mp, mp, L.Bs);
+  OperandPair op;
+  op.X0 = A; op.ld0 = lda; op.R0 = m; op.kc0 = an ? 0 : 1; op.Rp0 = (int)L.Mp;
+  op.X1 = B; op.ld1 = ldb; op.R1 = n; op.kc1 = bn ? 1 : 0; op.Rp1 = (int)L.Np;
+  op.ex0 = L.ex; op.ex1 = L.ex + L.Mp; op.out0 = L.As; op.out1 = L.Bs;
+  op.K = k; op.Kp = (int)L.Kp;
+  crt_residue_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Mp > L.Np ? L.Mp : L.Np), 2), 256,
+                       0, st>>>(op, mp);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 

@@ -32,6 +32,16 @@ __device__ __forceinline__ void load_tile_32x64(const T *__restrict__ X, int ld,
   }
 }
 
+// The two FP64 operands of a slice / residue pass, launched together:
+// blockIdx.z = 0 is op(A) (R = m rows), 1 is op(B) read as its n x k transpose.
+struct OperandPair {
+  const double *X0, *X1;
+  int ld0, ld1, R0, R1, kc0, kc1, Rp0, Rp1;
+  const int *ex0, *ex1;  // row exponents
+  void *out0, *out1;     // 16-bit blocks of Rp rows x Kp
+  int K, Kp;
+};
+
 // Scale exponent of a row: 2^-E * max|x| < 1.  Non-finite rows return a marker.
 constexpr int kNonFiniteExp = 0x40000000;
 __device__ __forceinline__ int row_exponent(unsigned long long amax_bits) {

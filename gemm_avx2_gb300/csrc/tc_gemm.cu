@@ -83,19 +83,35 @@ __device__ __forceinline__ void f16_terms(float x, int s, unsigned short &hi, un
   lo = __half_as_ushort(l);
 }
 
+// Both operands of one split in a single launch (blockIdx.z = 0: op(A),
+// 1: op(B) read as its n x k transpose).
+struct SplitArgs {
+  const float *X0, *X1;
+  int ld0, ld1, R0, R1, kc0, kc1, Rp0, Rp1;
+  SegMap seg0, seg1;
+  const int *ex0, *ex1;
+  __nv_bfloat16 *out0, *out1;
+  int K, Kp, nterms;
+  int64_t ldo;
+};
+
 // out: Rp x (nseg * Kp) row-major 16-bit terms (row stride ldo = nseg*Kp
-// elements); grid.y strides over the Rp / 32 row blocks.  Each thread writes
-// 8 consecutive k of one row (16 bytes) per segment.
+// elements); grid.y strides over the Rp / 32 row blocks (CTAs past the
+// smaller operand's rows do nothing).  Each thread writes 8 consecutive k of
+// one row (16 bytes) per segment.
 //   F16 = false: BF16 terms t0 = bf16(x), t1 = bf16(x - t0), t2 (nterms of them).
 //   F16 = true : the scaled FP16 (hi, lo) of f16_terms with the row exponents
 //                ex[] (Rp entries); a row whose max is not finite is all NaN.
 template <bool F16>
-__global__ void __launch_bounds__(256) split_bf16_kernel(const float *__restrict__ X, int ld, int R,
-                                                         int K, int kcontig, int Rp, int Kp,
-                                                         SegMap seg, int nterms,
-                                                         const int *__restrict__ ex,
-                                                         __nv_bfloat16 *__restrict__ out,
-                                                         int64_t ldo) {
+__global__ void __launch_bounds__(256) split_bf16_kernel(const __grid_constant__ SplitArgs p) {
+  const int z = blockIdx.z;
+  const float *__restrict__ X = z ? p.X1 : p.X0;
+  const int ld = z ? p.ld1 : p.ld0, R = z ? p.R1 : p.R0, kcontig = z ? p.kc1 : p.kc0;
+  const int Rp = z ? p.Rp1 : p.Rp0, K = p.K, Kp = p.Kp, nterms = p.nterms;
+  const SegMap &seg = z ? p.seg1 : p.seg0;
+  const int *__restrict__ ex = z ? p.ex1 : p.ex0;
+  __nv_bfloat16 *__restrict__ out = z ? p.out1 : p.out0;
+  const int64_t ldo = p.ldo;
   __shared__ float tile[32][65];
   const int k0 = blockIdx.x * 64;
   const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
@@ -166,51 +182,70 @@ template <> struct AbsBits<float> {
   static __device__ __forceinline__ int exponent(U b) { return row_exponent_f32(b); }
 };
 
+// Both operands in one launch: blockIdx.z = 0 reads the rows of op(A) into
+// amax[0, Mp), z = 1 the columns of op(B) into amax[Mp, Mp + Np).  The last
+// CTA to finish (a counter the caller zeroes with amax) writes the exponents
+// of all Mp + Np entries, so no separate exponent launch is needed.
 template <typename T>
-__global__ void __launch_bounds__(256) row_absmax_kernel(const T *__restrict__ X, int ld, int R,
-                                                         int K, int kcontig, int span,
-                                                         typename AbsBits<T>::U *__restrict__ amax) {
+struct AbsmaxArgs {
+  const T *X0, *X1;
+  int ld0, ld1, R0, R1, kc0, kc1, span0, span1, K, Mp, total;
+  typename AbsBits<T>::U *amax;
+  int *ex;
+  unsigned *counter;
+  unsigned nblocks;  // CTAs in the grid
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) row_absmax_kernel(const __grid_constant__ AbsmaxArgs<T> p) {
   using U = typename AbsBits<T>::U;
+  const int z = blockIdx.z;
+  const T *X = z ? p.X1 : p.X0;
+  const int ld = z ? p.ld1 : p.ld0, R = z ? p.R1 : p.R0, span = z ? p.span1 : p.span0;
+  const bool kcontig = (z ? p.kc1 : p.kc0) != 0;
+  U *amax = p.amax + (z ? p.Mp : 0);
+  const int k0 = blockIdx.y * span, k1 = min(p.K, k0 + span);
   if (kcontig) {
     // one warp per (row, k range)
     const int r = (blockIdx.x * 8) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (r >= R) return;
-    const int k0 = blockIdx.y * span, k1 = min(K, k0 + span);
-    U m = 0;
-    const T *row = X + (int64_t)r * ld;
+    if (r < R && k0 < p.K) {
+      U m = 0;
+      const T *row = X + (int64_t)r * ld;
 #pragma unroll 8
-    for (int kk = k0 + lane; kk < k1; kk += 32) {
-      const U b = AbsBits<T>::of(row[kk]);
-      m = b > m ? b : m;
-    }
+      for (int kk = k0 + lane; kk < k1; kk += 32) {
+        const U b = AbsBits<T>::of(row[kk]);
+        m = b > m ? b : m;
+      }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const U x = __shfl_xor_sync(0xffffffffu, m, o);
-      m = x > m ? x : m;
+      for (int o = 16; o > 0; o >>= 1) {
+        const U x = __shfl_xor_sync(0xffffffffu, m, o);
+        m = x > m ? x : m;
+      }
+      if (lane == 0 && m) atomicMax(&amax[r], m);
     }
-    if (lane == 0 && m) atomicMax(&amax[r], m);
   } else {
     // one thread per row, one k range per grid row
     const int r = blockIdx.x * 256 + threadIdx.x;
-    if (r >= R) return;
-    const int k0 = blockIdx.y * span, k1 = min(K, k0 + span);
-    U m = 0;
+    if (r < R && k0 < p.K) {
+      U m = 0;
 #pragma unroll 8
-    for (int kk = k0; kk < k1; ++kk) {
-      const U b = AbsBits<T>::of(X[r + (int64_t)kk * ld]);
-      m = b > m ? b : m;
+      for (int kk = k0; kk < k1; ++kk) {
+        const U b = AbsBits<T>::of(X[r + (int64_t)kk * ld]);
+        m = b > m ? b : m;
+      }
+      if (m) atomicMax(&amax[r], m);
     }
-    if (m) atomicMax(&amax[r], m);
   }
-}
-
-// Ozaki step 1b: the per-row exponents, once (the slice kernel and the GEMM
-// epilogue read them instead of recomputing frexp per element).
-template <typename T>
-__global__ void row_exponent_kernel(const typename AbsBits<T>::U *__restrict__ amax, int R,
-                                    int *__restrict__ ex) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < R) ex[r] = AbsBits<T>::exponent(amax[r]);
+  // every thread's atomics are visible before the CTA counts itself done
+  __threadfence();
+  __syncthreads();
+  __shared__ bool last;
+  if (threadIdx.x == 0) last = atomicAdd(p.counter, 1u) == p.nblocks - 1;
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    for (int i = threadIdx.x; i < p.total; i += blockDim.x) p.ex[i] = AbsBits<T>::exponent(__ldcg(&p.amax[i]));
+  }
 }
 
 // The S digits of 8 consecutive values of one row (row exponent e), packed as
@@ -255,10 +290,16 @@ __device__ __forceinline__ void slice_digits(const double *x, int e, int S, uint
 // d_s = floor(M * 2^(b - E + 7s)) mod 128, a shift and a mask (the GPU's FP64
 // rate would make the recurrence itself the bottleneck of this pass).
 // out: S blocks of Rp rows x Kp (row-major BF16), slice s at rows (s-1)*Rp;
-// each thread writes 8 consecutive k of one row (16 bytes) per slice.
-__global__ void __launch_bounds__(256) ozaki_slice_kernel(
-    const double *__restrict__ X, int ld, int R, int K, int kcontig, int Rp, int Kp, int S,
-    const int *__restrict__ ex, __nv_bfloat16 *__restrict__ out) {
+// each thread writes 8 consecutive k of one row (16 bytes) per slice.  Both
+// operands in one launch (blockIdx.z).
+__global__ void __launch_bounds__(256) ozaki_slice_kernel(const __grid_constant__ OperandPair p,
+                                                          int S) {
+  const int z = blockIdx.z;
+  const double *__restrict__ X = z ? p.X1 : p.X0;
+  const int ld = z ? p.ld1 : p.ld0, R = z ? p.R1 : p.R0, kcontig = z ? p.kc1 : p.kc0;
+  const int Rp = z ? p.Rp1 : p.Rp0, K = p.K, Kp = p.Kp;
+  const int *__restrict__ ex = z ? p.ex1 : p.ex0;
+  __nv_bfloat16 *__restrict__ out = static_cast<__nv_bfloat16 *>(z ? p.out1 : p.out0);
   __shared__ double tile[32][65];
   const int k0 = blockIdx.x * 64;
   const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
@@ -875,7 +916,7 @@ size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
     if (!split_products_ok(param)) return 0;
     const int64_t Mp = round_up(m, kSplitBM), Np = round_up(n, kBf16xBN);
     // scaled FP16 form: + the max |.| bit patterns and exponents of rows / columns
-    const int64_t scales = param == kFp16x3 ? (Mp + Np) * 8 + 256 : 0;
+    const int64_t scales = param == kFp16x3 ? (Mp + Np) * 8 + 512 : 0;
     return (size_t)((Mp + Np) * split_segments(param) * Kp * 2 + 1024 + scales);
   }
   int S = param > 0 ? param : ozaki_default_slices(m, n, k);
@@ -903,30 +944,38 @@ void set_bf16x_chunk_kblocks(int c) { g_bf16x_chunk = c < 0 ? 0 : c; }
 
 // Per-row max |.| of op(A) and per-column max |.| of op(B), then their scale
 // exponents.  amax / ex hold Mp entries for the rows of op(A), then Np for
-// the columns of op(B); padding entries get exponent 0.
+// the columns of op(B); padding entries get exponent 0.  The completion
+// counter sits in the 16 bytes after amax and is zeroed with it: one memset
+// and one launch.
 template <typename T>
 static int scale_exponents(char ta, char tb, int m, int n, int k, const T *A, int lda, const T *B,
                            int ldb, typename AbsBits<T>::U *amax, int *ex, int64_t Mp, int64_t Np,
                            cudaStream_t st) {
   const bool an = notrans(ta), bn = notrans(tb);
-  if (cudaMemsetAsync(amax, 0, (size_t)(Mp + Np) * sizeof(*amax), st) != cudaSuccess)
+  using U = typename AbsBits<T>::U;
+  if (cudaMemsetAsync(amax, 0, (size_t)(Mp + Np) * sizeof(U) + 16, st) != cudaSuccess)
     return GB300_ERR_CUDA;
+  AbsmaxArgs<T> p;
   // A rows are k-contiguous when transposed, B columns when not.
-  auto absmax = [&](const T *X, int ld, int R, bool kc, typename AbsBits<T>::U *am) {
+  p.X0 = A; p.ld0 = lda; p.R0 = m; p.kc0 = an ? 0 : 1;
+  p.X1 = B; p.ld1 = ldb; p.R1 = n; p.kc1 = bn ? 1 : 0;
+  unsigned gx = 1, gy = 1;
+  for (int z = 0; z < 2; ++z) {
+    const bool kc = (z ? p.kc1 : p.kc0) != 0;
+    const int R = z ? p.R1 : p.R0;
     int64_t span = kc ? kAmaxSpanK : kAmaxSpanR;
     while ((k + span - 1) / span > 65535) span *= 2;
-    const unsigned gy = (unsigned)((k + span - 1) / span);
-    if (kc)
-      row_absmax_kernel<T><<<dim3((unsigned)((R + 7) / 8), gy), 256, 0, st>>>(X, ld, R, k, 1,
-                                                                             (int)span, am);
-    else
-      row_absmax_kernel<T><<<dim3((unsigned)((R + 255) / 256), gy), 256, 0, st>>>(X, ld, R, k, 0,
-                                                                                 (int)span, am);
-  };
-  absmax(A, lda, m, !an, amax);
-  absmax(B, ldb, n, bn, amax + Mp);
-  row_exponent_kernel<T><<<(unsigned)((Mp + Np + 255) / 256), 256, 0, st>>>(amax, (int)(Mp + Np),
-                                                                             ex);
+    (z ? p.span1 : p.span0) = (int)span;
+    const unsigned x = (unsigned)(kc ? (R + 7) / 8 : (R + 255) / 256);
+    const unsigned y = (unsigned)((k + span - 1) / span);
+    gx = x > gx ? x : gx;
+    gy = y > gy ? y : gy;
+  }
+  p.K = k; p.Mp = (int)Mp; p.total = (int)(Mp + Np);
+  p.amax = amax; p.ex = ex;
+  p.counter = reinterpret_cast<unsigned *>(amax + Mp + Np);
+  p.nblocks = gx * gy * 2;
+  row_absmax_kernel<T><<<dim3(gx, gy, 2), 256, 0, st>>>(p);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
@@ -954,7 +1003,8 @@ static Bf16xLayout bf16x_layout(int m, int n, int k, int products, void *ws) {
   L.Bp = L.Ap + L.Mp * L.Kld;
   L.amax = reinterpret_cast<unsigned *>(
       (reinterpret_cast<uintptr_t>(L.Bp + L.Np * L.Kld) + 255) & ~uintptr_t(255));
-  L.ex = reinterpret_cast<int *>(L.amax + L.Mp + L.Np);
+  // 16 bytes after amax: the max pass's completion counter
+  L.ex = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(L.amax + L.Mp + L.Np) + 16);
   return L;
 }
 
@@ -973,23 +1023,26 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
   const Bf16xLayout L = bf16x_layout(m, n, k, products, ws);
   if (L.Kld > 0x7fffffff || L.Mp > 0x7fffffff || L.Np > 0x7fffffff) return GB300_ERR_ARG;
   const bool an = notrans(ta), bn = notrans(tb);
-  const dim3 ga((unsigned)(L.Kp / 64), row_blocks(L.Mp)), gb((unsigned)(L.Kp / 64), row_blocks(L.Np));
-  if (products == kFp16x3) {
+  const bool f16 = products == kFp16x3;
+  SplitArgs sa;
+  sa.X0 = A; sa.ld0 = lda; sa.R0 = m; sa.kc0 = an ? 0 : 1; sa.Rp0 = (int)L.Mp;
+  sa.X1 = B; sa.ld1 = ldb; sa.R1 = n; sa.kc1 = bn ? 1 : 0; sa.Rp1 = (int)L.Np;
+  sa.seg0 = seg_map(f16 ? 3 : products, true);
+  sa.seg1 = seg_map(f16 ? 3 : products, false);
+  sa.ex0 = f16 ? L.ex : nullptr;
+  sa.ex1 = f16 ? L.ex + L.Mp : nullptr;
+  sa.out0 = L.Ap; sa.out1 = L.Bp;
+  sa.K = k; sa.Kp = (int)L.Kp; sa.nterms = products == 6 ? 3 : 2;
+  sa.ldo = L.Kld;
+  const unsigned rb = row_blocks(L.Mp > L.Np ? L.Mp : L.Np);
+  const dim3 grid((unsigned)(L.Kp / 64), rb, 2);
+  if (f16) {
     const int rc = scale_exponents<float>(ta, tb, m, n, k, A, lda, B, ldb, L.amax, L.ex, L.Mp,
                                           L.Np, st);
     if (rc != GB300_OK) return rc;
-    split_bf16_kernel<true><<<ga, 256, 0, st>>>(A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp,
-                                                seg_map(3, true), 2, L.ex, L.Ap, L.Kld);
-    split_bf16_kernel<true><<<gb, 256, 0, st>>>(B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp,
-                                                seg_map(3, false), 2, L.ex + L.Mp, L.Bp, L.Kld);
+    split_bf16_kernel<true><<<grid, 256, 0, st>>>(sa);
   } else {
-    const int nterms = products == 3 ? 2 : 3;
-    split_bf16_kernel<false><<<ga, 256, 0, st>>>(A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp,
-                                                 seg_map(products, true), nterms, nullptr, L.Ap,
-                                                 L.Kld);
-    split_bf16_kernel<false><<<gb, 256, 0, st>>>(B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp,
-                                                 seg_map(products, false), nterms, nullptr, L.Bp,
-                                                 L.Kld);
+    split_bf16_kernel<false><<<grid, 256, 0, st>>>(sa);
   }
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
@@ -1138,7 +1191,8 @@ static OzakiLayout ozaki_layout(int m, int n, int k, int S, void *ws) {
   L.Bs = L.As + S * L.Mp * L.Kp;
   L.amaxA = reinterpret_cast<unsigned long long *>(L.Bs + S * L.Np * L.Kp);
   L.amaxB = L.amaxA + L.Mp;
-  L.expA = reinterpret_cast<int *>(L.amaxB + L.Np);
+  // 16 bytes after amaxB: the max pass's completion counter
+  L.expA = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(L.amaxB + L.Np) + 16);
   L.expB = L.expA + L.Mp;
   L.res = reinterpret_cast<double *>(
       (reinterpret_cast<uintptr_t>(L.expB + L.Np) + 255) & ~uintptr_t(255));
@@ -1160,10 +1214,13 @@ int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int ld
   const int rc = row_scale_exponents(ta, tb, m, n, k, A, lda, B, ldb, L.amaxA, L.expA, L.Mp,
                                      L.Np, st);
   if (rc != GB300_OK) return rc;
-  ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Mp)), 256, 0, st>>>(
-      A, lda, m, k, an ? 0 : 1, (int)L.Mp, (int)L.Kp, S, L.expA, L.As);
-  ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Np)), 256, 0, st>>>(
-      B, ldb, n, k, bn ? 1 : 0, (int)L.Np, (int)L.Kp, S, L.expB, L.Bs);
+  OperandPair op;
+  op.X0 = A; op.ld0 = lda; op.R0 = m; op.kc0 = an ? 0 : 1; op.Rp0 = (int)L.Mp;
+  op.X1 = B; op.ld1 = ldb; op.R1 = n; op.kc1 = bn ? 1 : 0; op.Rp1 = (int)L.Np;
+  op.ex0 = L.expA; op.ex1 = L.expB; op.out0 = L.As; op.out1 = L.Bs;
+  op.K = k; op.Kp = (int)L.Kp;
+  ozaki_slice_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(L.Mp > L.Np ? L.Mp : L.Np), 2), 256,
+                       0, st>>>(op, S);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 

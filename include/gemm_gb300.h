@@ -372,9 +372,12 @@ void gb300_tune_cache_clear(void);
  * headers, dgemm_tune.h / sgemm_tune.h via src/gemm_set_parameters.h:1-61).
  *   GB300_TUNE_BF16X_CHUNK: K extent (in 64-wide blocks) of one TMEM
  *   accumulation chunk of the BF16xP SGEMM's hi*hi product; products of
- *   order 1 use 4x that, order-2 products are not chunked.  0 restores the
- *   default (4). */
-enum { GB300_TUNE_BF16X_CHUNK = 1 };
+ *   order 1 use 4x that (32x with the scaled FP16 terms), order-2 products
+ *   are not chunked.  0 restores the default (4).
+ *   GB300_TUNE_GRAPH_BRANCHES: parallel branches (1..64) of the CUDA graph
+ *   that gb300_grouped_graph_create captures for the split form (form 1);
+ *   read at creation.  0 restores the default. */
+enum { GB300_TUNE_BF16X_CHUNK = 1, GB300_TUNE_GRAPH_BRANCHES = 2 };
 int gb300_tune_param(int param, int value);
 
 /* Library version string. */

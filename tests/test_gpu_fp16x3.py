@@ -45,7 +45,7 @@ def workspace_parts(ws, m, n, k):
     Ap, Bp = h[:Mp * kld].reshape(Mp, kld), h[Mp * kld:].reshape(Np, kld)
     end = base + off + 2 * (Mp + Np) * kld
     a_off = (-end) % 256 + off + 2 * (Mp + Np) * kld
-    ex_off = a_off + 4 * (Mp + Np)
+    ex_off = a_off + 4 * (Mp + Np) + 16  # past the max pass's completion counter
     ex = raw[ex_off:ex_off + 4 * (Mp + Np)].view(np.int32)
     return Ap, Bp, ex[:Mp], ex[Mp:], Mp, Np, Kp
 
