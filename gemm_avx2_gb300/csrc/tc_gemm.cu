@@ -589,6 +589,7 @@ struct OzakiParams {
   double *res;             // Mp x Np FP64 result scratch (ld = Mp)
   uint8_t *rres;           // mode 1: S blocks of Mp x Np residues in [0, mods[g]) (ld = Mp)
   int mods[kCrtMaxModuli];
+  unsigned mods_mg[kCrtMaxModuli];  // floor(2^32 / mods[g]) for the Barrett reduction
   unsigned *err;
 };
 
@@ -805,11 +806,15 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           if (p.mode && (++since_fold == run_limit || last)) {
             // CRT form: reduce the exact sums mod p; at the modulus' end store
             // the residue in [0, p) for the reconstruction kernel
-            const int pm = p.mods[gi];
+            // |run| < 64 chunks x 2^24 = 2^30 < 149 * 2^23, so run + pm * 2^23 is in
+            // [0, 2^32): one Barrett step (q = the quotient or one less) and an
+            // unsigned-min correction give run mod pm in [0, pm)
+            const unsigned pm = (unsigned)p.mods[gi], mg = p.mods_mg[gi], off = pm << 23;
 #pragma unroll
             for (int j = 0; j < kOzCols; ++j) {
-              int r = run[j] % pm;
-              run[j] = r < 0 ? r + pm : r;
+              const unsigned x = (unsigned)run[j] + off;
+              const unsigned r = x - __umulhi(x, mg) * pm;
+              run[j] = (int)min(r, r - pm);
             }
             if (last && real) {
               uint8_t *dst = p.rres + (int64_t)gi * p.Mp * p.Np + (int64_t)col0 * p.Mp + row;
@@ -1262,7 +1267,10 @@ int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
   p.Mp = (int)a.Mp; p.Np = (int)a.Np;
   p.alpha = a.alpha; p.beta = a.beta; p.C = a.C; p.ldc = a.ldc;
   p.expA = a.expA; p.expB = a.expB; p.res = a.res; p.rres = a.rres; p.err = err;
-  for (int i = 0; i < kCrtMaxModuli; ++i) p.mods[i] = (a.mode && i < a.S) ? a.mods[i] : 1;
+  for (int i = 0; i < kCrtMaxModuli; ++i) {
+    p.mods[i] = (a.mode && i < a.S) ? a.mods[i] : 1;
+    p.mods_mg[i] = p.mods[i] > 1 ? (unsigned)((1ull << 32) / (unsigned)p.mods[i]) : 0u;
+  }
   if (!mc) {
     if (cudaFuncSetAttribute(ozaki_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              kOzSmem) != cudaSuccess)

@@ -25,14 +25,15 @@ def device_result(form, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, param):
     return from_dev(dC, C.shape[0])
 
 
-@pytest.mark.parametrize("form,param,dt,size", [
-    ("crt", 16, np.float64, 1500),
-    ("ozaki", 8, np.float64, 1500),
-    ("bf16x", g.FP16X3, np.float32, 2100),
-    ("bf16x", 6, np.float32, 2100),
+@pytest.mark.parametrize("form,param,dt,size,k", [
+    ("crt", 16, np.float64, 1500, 1100),
+    ("crt", 16, np.float64, 1500, 200),
+    ("ozaki", 8, np.float64, 1500, 200),
+    ("bf16x", g.FP16X3, np.float32, 2100, 200),
+    ("bf16x", 6, np.float32, 2100, 200),
 ])
-def test_staged_host_path_matches_device(orc, form, param, dt, size):
-    m, n, k = size, size - 40, 200
+def test_staged_host_path_matches_device(orc, form, param, dt, size, k):
+    m, n = size, size - 40
     A = orc.uniform((k, m), dt, 81, 0)       # transa = T
     B = orc.uniform((n + 2, k), dt, 81, 1)   # transb = T, ldb = n + 2
     C = orc.uniform((m + 3, n), dt, 81, 2)   # ldc = m + 3
