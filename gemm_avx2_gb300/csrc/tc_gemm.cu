@@ -594,13 +594,13 @@ struct OzakiParams {
 };
 
 constexpr int kOzStages = 4;
-constexpr int kOzEpiWarps = 8;
+constexpr int kOzEpiWarps = 16;  // 4 per TMEM lane quarter, 64 columns each
 constexpr int kOzThreads = (2 + kOzEpiWarps) * 32;
 constexpr int kOzABytes = kSplitBM * 128;
 constexpr int kOzBBytes = kOzakiBN * 128;
 constexpr int kOzStage = kOzABytes + kOzBBytes;
 constexpr int kOzSmem = kOzStages * kOzStage + 1024 + 256;
-constexpr int kOzCols = kOzakiBN / 2;  // output columns per epilogue warp
+constexpr int kOzCols = kOzakiBN / (kOzEpiWarps / 4);  // output columns per epilogue warp
 // 16 x 64 = 1024 K-steps per exact chunk: |partial sum| <= 1024 * 127^2 =
 // 16,516,096 < 2^24, so every partial sum is an exactly representable FP32 integer.
 constexpr int kOzChunkStages = 16;
@@ -758,7 +758,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       mbar_wait(done, 0, p.err, kErrTimeoutMma, nullptr);
     }
   } else {
-    // 8 epilogue warps: lane quarter q = warp % 4, column half h (128 columns each)
+    // 16 epilogue warps: lane quarter q = warp % 4, column block h (64 columns each)
     const int q = warp & 3;
     const int h = (warp - 2) >> 2;
     const int row_in_tile = q * 32 + lane;
