@@ -342,7 +342,7 @@ int tune_cache_load(const char *path, int *loaded) {
       continue;
     const bool bx = strncmp(key, "bf16x:", 6) == 0, oz = strncmp(key, "ozaki:", 6) == 0;
     const bool cr = strncmp(key, "crt:", 4) == 0;
-    if (bx && (e.param == 3 || e.param == 6) && e.chunk >= 0 && e.chunk <= 64)
+    if (bx && split_products_ok(e.param) && e.chunk >= 0 && e.chunk <= 64)
       add[key] = e;
     else if (oz && e.param >= 2 && e.param <= kOzakiMaxSlices)
       add[key] = e;

@@ -170,6 +170,8 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
                  '"err_fro": 1e-16, "plain_max": 2e-14, "plain_fro": 1e-15},\n'
                  '  {"key": "bf16x:9:9:9", "param": 3, "chunk": 8, "ms": 1, "err_max": 1e-5, '
                  '"err_fro": 1e-7, "plain_max": 2e-5, "plain_fro": 1e-6},\n'
+                 '  {"key": "bf16x:12:12:12", "param": 259, "chunk": 4, "ms": 1, "err_max": 1e-5, '
+                 '"err_fro": 1e-7, "plain_max": 2e-5, "plain_fro": 1e-6},\n'
                  '  {"key": "ozaki:8:8:8", "param": 99, "chunk": 0, "ms": 1, "err_max": 0, '
                  '"err_fro": 0, "plain_max": 0, "plain_fro": 0},\n'
                  '  {"key": "crt:9:9:9", "param": 14, "chunk": 0, "ms": 1, "err_max": 1e-14, '
@@ -177,8 +179,12 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
                  '  {"key": "crt:8:8:8", "param": 25, "chunk": 0, "ms": 1, "err_max": 0, '
                  '"err_fro": 0, "plain_max": 0, "plain_fro": 0},\n'
                  '  garbage line\n]}\n')
-    assert g.tune_cache_load(str(f)) == (g.OK, 3)
+    assert g.tune_cache_load(str(f)) == (g.OK, 4)
     assert g.tune_lookup(g.TUNE_CRT, 1000, 600, 700) == (g.OK, 14, 0)
+    # the scaled FP16 form is a valid tuned choice and sizes the workspace
+    assert g.tune_lookup(g.TUNE_BF16X, 4096, 5000, 8000) == (g.OK, g.FP16X3, 4)
+    assert g.split_workspace_bytes(0, 4096, 5000, 8000, 0) == \
+        g.split_workspace_bytes(0, 4096, 5000, 8000, g.FP16X3)
     assert g.tune_lookup(g.TUNE_CRT, 300, 300, 300)[0] == g.ERR_UNSUPPORTED   # 25 rejected
     # moduli = 0 sizes the workspace with the tuned count
     assert g.split_workspace_bytes(2, 1000, 600, 700, 0) == g.split_workspace_bytes(2, 1000, 600, 700, 14)
@@ -189,7 +195,15 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
     out = tmp_path / "saved.json"
     assert g.tune_cache_save(str(out)) == g.OK
     g.tune_cache_clear()
-    assert g.tune_cache_load(str(out)) == (g.OK, 3)
+    assert g.tune_cache_load(str(out)) == (g.OK, 4)
     assert g.tune_cache_load(str(tmp_path / "missing.json"))[0] == g.ERR_ARG
     assert g.tune_lookup(g.TUNE_OZAKI, 1000, 600, 700) == (g.OK, 10, 0)        # cache kept
     g.tune_cache_clear()
+
+
+def test_tuning_knobs_validate():
+    assert g.tune_param(g.TUNE_GRAPH_BRANCHES, 64) == g.OK
+    assert g.tune_param(g.TUNE_GRAPH_BRANCHES, 65) == g.ERR_ARG
+    assert g.tune_param(g.TUNE_GRAPH_BRANCHES, -1) == g.ERR_ARG
+    assert g.tune_param(g.TUNE_GRAPH_BRANCHES, 0) == g.OK   # back to the default
+    assert g.tune_param(99, 1) == g.ERR_ARG

@@ -98,6 +98,28 @@ def test_grouped_graph_replay(orc):
     assert g.device_error() == 0
 
 
+def test_grouped_split_graph_branch_count_is_invisible(orc):
+    """The same batch captured in 2 and in 64 branches gives identical results
+    (each problem runs the same kernels; only their concurrency differs)."""
+    probs, host, dev = make_batch(orc, 40, 5, max_dim=300)
+    outs = []
+    try:
+        for nb in (2, 64):
+            assert g.tune_param(g.TUNE_GRAPH_BRANCHES, nb) == g.OK
+            for d, h in zip(dev, host):
+                d[2].copy_(to_dev(h[2]))   # C back to its initial values
+            graph = g.GroupedGraph(probs, form=1)
+            assert graph.launch() == g.OK
+            sync()
+            outs.append([from_dev(d[2], h[2].shape[0]) for d, h in zip(dev, host)])
+            graph.destroy()
+    finally:
+        g.tune_param(g.TUNE_GRAPH_BRANCHES, 0)
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+    assert g.device_error() == 0
+
+
 def test_grouped_split_graph(orc):
     """Split forms (6xBF16 for FP32, Ozaki for FP64) captured per problem."""
     probs, host, dev = make_batch(orc, 12, 4, max_dim=260)
