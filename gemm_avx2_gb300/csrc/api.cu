@@ -177,7 +177,8 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
     // is copied to HBM on a side stream while A and B are prepared and copied
     // back at the end (measured: DGEMM 16384^3 54.6 -> 69.0 TFLOP/s end to
     // end; a rank-256 update with 8.6 GB of C 2.2 -> 3.9).  All copies are SM
-    // loads/stores (about twice the copy engines' rate over the link).
+    // loads/stores: about 200 GB/s host to device, the copy engines' rate on
+    // pinned memory, and the same on pageable memory the device reads.
     int prm = param;
     if (form == 1 && prm == 0) {
       int ch = 0;
@@ -279,8 +280,9 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
     return GB300_ERR_NOMEM;
   T *dA = static_cast<T *>(s->stage[0]), *dB = static_cast<T *>(s->stage[1]);
   T *dC = static_cast<T *>(s->stage[2]);
-  // SM loads/stores where the device can read the host memory (about twice
-  // the copy engines' rate over the coherent link), else the copy engines
+  // SM loads/stores where the device can read the host memory (the copy
+  // engines' rate on pinned memory, and no driver staging for pageable
+  // memory), else the copy engines
   auto copy = [&](void *dst, size_t dp, const void *src, size_t sp, size_t w, int cols,
                   cudaMemcpyKind kind) -> cudaError_t {
     if (direct) return copy_2d(dst, dp, src, sp, w, cols, st) == GB300_OK ? cudaSuccess
@@ -384,7 +386,8 @@ static int host_complex(char ta, char tb, int m, int n, int k, const T *alpha, c
     return finish(run(a, lda, b, ldb, c, ldc));
   }
   // host <-> HBM copies: SM loads/stores where the device can read the host
-  // memory (about twice the copy engines' rate over the link)
+  // memory (the copy engines' rate on pinned memory, and no driver staging
+  // for pageable memory)
   auto copy = [&](void *dst, size_t dp, const void *src, size_t sp, size_t w, int cols,
                   cudaMemcpyKind kind) -> cudaError_t {
     if (direct) return copy_2d(dst, dp, src, sp, w, cols, st) == GB300_OK ? cudaSuccess
