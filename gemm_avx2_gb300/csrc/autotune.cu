@@ -6,6 +6,7 @@
 //
 //   split SGEMM : products P in {3, 6} (BF16 terms) or the scaled 3xFP16
 //                 form, x hi*hi chunk length in {2, 4, 8};
+//   all forms   : then the output tile width (128 / 256) of the chosen one;
 //   Ozaki DGEMM : slice count S in [4, 12].
 //
 // A candidate qualifies when its max and Frobenius relative errors against a
@@ -42,6 +43,7 @@ namespace gb300 {
 struct TuneEntry {
   int param = 0;       // products (BF16xP) or slices (Ozaki)
   int chunk = 0;       // BF16xP hi*hi chunk length (0 for Ozaki)
+  int tile = 0;        // output tile width of the GEMM (128 / 256; 0 = by shape)
   double ms = 0;       // measured time of the chosen candidate
   double err_max = 0, err_fro = 0;              // chosen candidate vs reference
   double plain_max = 0, plain_fro = 0;          // plain kernel vs reference
@@ -71,6 +73,12 @@ bool tune_lookup(int kind, int m, int n, int k, int *param, int *chunk) {
   if (param) *param = it->second.param;
   if (chunk) *chunk = it->second.chunk;
   return true;
+}
+
+int tune_tile_n(int kind, int m, int n, int k) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(tune_key(kind, m, n, k));
+  return it == g_tune.end() ? 0 : it->second.tile;
 }
 
 // ---------------------------------------------------------------- device helpers
@@ -283,6 +291,22 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
     }
     if (!found) best.param = 12;
   }
+  // the output tile width: the results are the same bit for bit, so only
+  // the time decides (the caller's own override is restored afterwards)
+  {
+    const int user_tile = split_tile_override();
+    double t128 = 0, t256 = 0;
+    set_split_tile_n(128);
+    rc = timed(best.param, best.chunk, &t128);
+    if (rc == GB300_OK) {
+      set_split_tile_n(256);
+      rc = timed(best.param, best.chunk, &t256);
+    }
+    set_split_tile_n(user_tile);
+    if (rc != GB300_OK) return rc;
+    best.tile = t128 < t256 ? 128 : 256;
+    best.ms = t128 < t256 ? t128 : t256;
+  }
   best.plain_max = plain.max_rel;
   best.plain_fro = plain.fro;
   {
@@ -313,9 +337,9 @@ int tune_cache_save(const char *path) {
     const TuneEntry &e = kv.second;
     fprintf(f,
             "  {\"key\": \"%s\", \"param\": %d, \"chunk\": %d, \"ms\": %.6g, \"err_max\": %.6g, "
-            "\"err_fro\": %.6g, \"plain_max\": %.6g, \"plain_fro\": %.6g}%s\n",
+            "\"err_fro\": %.6g, \"plain_max\": %.6g, \"plain_fro\": %.6g, \"tile\": %d}%s\n",
             kv.first.c_str(), e.param, e.chunk, e.ms, e.err_max, e.err_fro, e.plain_max,
-            e.plain_fro, ++i < g_tune.size() ? "," : "");
+            e.plain_fro, e.tile, ++i < g_tune.size() ? "," : "");
   }
   fprintf(f, "]}\n");
   return fclose(f) == 0 ? GB300_OK : GB300_ERR_ARG;
@@ -340,6 +364,10 @@ int tune_cache_load(const char *path, int *loaded) {
                key, &e.param, &e.chunk, &e.ms, &e.err_max, &e.err_fro, &e.plain_max,
                &e.plain_fro) != 8)
       continue;
+    // optional (files from before it was tuned have no tile width)
+    const char *tp = strstr(line, "\"tile\":");
+    if (tp && sscanf(tp, "\"tile\": %d", &e.tile) != 1) e.tile = 0;
+    if (e.tile != 128 && e.tile != 256) e.tile = 0;
     const bool bx = strncmp(key, "bf16x:", 6) == 0, oz = strncmp(key, "ozaki:", 6) == 0;
     const bool cr = strncmp(key, "crt:", 4) == 0;
     if (bx && split_products_ok(e.param) && e.chunk >= 0 && e.chunk <= 64)

@@ -576,7 +576,7 @@ int crt_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, 
   const CrtLayout L = crt_layout(m, n, k, N, const_cast<void *>(ws));
   // 3. one exact integer GEMM per modulus
   OzakiGemmArgs a;
-  a.m = m; a.n = n; a.S = N; a.mode = 1;
+  a.m = m; a.n = n; a.k = k; a.S = N; a.mode = 1;
   a.Mp = L.Mp; a.Np = L.Np; a.Kp = L.Kp;
   a.As = L.As; a.Bs = L.Bs;
   a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc;

@@ -35,6 +35,7 @@ int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float 
 // FP64 forms: operands are S blocks of Mp (Np) rows x Kp of BF16-held integers.
 struct OzakiGemmArgs {
   int m, n, S, mode;
+  int k;  // the problem's K (its shape class picks the tuned tile width)
   int64_t Mp, Np, Kp;
   const void *As, *Bs;
   double alpha, beta;
@@ -84,6 +85,15 @@ int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int ld
                   int ldb, int slices, void *ws, size_t ws_bytes, cudaStream_t st);
 int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int slices,
               const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err);
+
+// Tile width (128 or 256) of the split GEMMs (kind as for the autotuner:
+// 0 BF16xP, 1 Ozaki, 2 CRT) for an m x n x k problem: the override, else the
+// tuned width of the shape class, else by shape.  The override: 0 = none.
+int split_tile_n(int kind, int m, int n, int k);
+void set_split_tile_n(int v);
+int split_tile_override();
+// Tuned tile width of a shape class (0 = none).
+int tune_tile_n(int kind, int m, int n, int k);
 
 // Accumulation chunk of the BF16xP GEMM in 64-wide K blocks (0 = default, 4).
 int bf16x_chunk_kblocks();

@@ -358,25 +358,36 @@ struct Bf16xParams {
   const int *expA, *expB;
 };
 
-constexpr int kBxStages = 4;
 constexpr int kBxEpiWarps = 16;                     // 4 per TMEM lane quarter
 constexpr int kBxThreads = (2 + kBxEpiWarps) * 32;  // producer, MMA, epilogue
 constexpr int kBxABytes = kSplitBM * 128;
-constexpr int kBxBBytes = kBf16xBN * 128;
-constexpr int kBxStage = kBxABytes + kBxBBytes;
-constexpr int kBxSmem = kBxStages * kBxStage + 1024 + 256;
-constexpr int kBxColsPerWarp = kBf16xBN / (kBxEpiWarps / 4);  // columns each epilogue warp owns
 constexpr int kBxDefaultChunk = 4;                  // 4 x 64 = 256 K' per chunk
+
+// Geometry of a 128 x BN output tile (BN = 256, or 128 for shapes with few
+// tiles): B tile bytes per 64-wide K block, the stage (A + B), the ring depth
+// that fits in shared memory (4 stages of 48 KB or 6 of 32 KB), and the
+// columns each of the 16 epilogue warps owns (BN / 4).
+template <int BN>
+struct TileN {
+  static constexpr int kBBytes = BN * 128;
+  static constexpr int kStage = kSplitBM * 128 + kBBytes;
+  static constexpr int kStages = BN == 256 ? 4 : 6;
+  static constexpr int kSmem = kStages * kStage + 1024 + 256;
+  static constexpr int kCols = BN / 4;
+};
 
 // MC: 2-CTA clusters on the row tiles 2u and 2u + 1 of one column tile, in
 // lockstep over the same unit sequence; each CTA loads its own A tile and half
 // of the shared B tile, multicast into both CTAs' stage (the B tensor map's box
 // is then 128 rows).  Each stage's empty barrier counts both CTAs' MMA commits,
 // since a stage holds data its peer wrote.  This halves the B tile's L2 reads.
-template <bool MC, bool F16>
+template <bool MC, bool F16, int BN>
 __global__ void __launch_bounds__(kBxThreads, 1)
 bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   Bf16xParams p) {
+  using T = TileN<BN>;
+  constexpr int kBxStages = T::kStages, kBxStage = T::kStage, kBxBBytes = T::kBBytes;
+  constexpr int kBxColsPerWarp = T::kCols;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
@@ -442,16 +453,16 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           tma_load_2d(sa, &tmA, kb * kSplitBK, tm * kSplitBM, &full[s]);
           if (MC)
             tma_load_2d_mc(sa + kBxABytes + rank * (kBxBBytes / 2), &tmB, kb * kSplitBK,
-                           tn * kBf16xBN + (int)rank * (kBf16xBN / 2), &full[s], 0x3);
+                           tn * BN + (int)rank * (BN / 2), &full[s], 0x3);
           else
-            tma_load_2d(sa + kBxABytes, &tmB, kb * kSplitBK, tn * kBf16xBN, &full[s]);
+            tma_load_2d(sa + kBxABytes, &tmB, kb * kSplitBK, tn * BN, &full[s]);
         }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc =
-          F16 ? idesc_f16_f32(kSplitBM, kBf16xBN) : idesc_bf16_f32(kSplitBM, kBf16xBN);
+          F16 ? idesc_f16_f32(kSplitBM, BN) : idesc_bf16_f32(kSplitBM, BN);
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
@@ -467,7 +478,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             break;
           }
           tc_fence_after();
-          const uint32_t dt = tmem + b * kBf16xBN;
+          const uint32_t dt = tmem + b * BN;
           for (int kb = c0; kb < c1; ++kb, ++L) {
             const int s = L % kBxStages;
             const uint32_t r = L / kBxStages;
@@ -520,7 +531,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 #pragma unroll
         for (int g = 0; g < kBxColsPerWarp / 16; ++g) {
           uint32_t v[16];
-          tmem_ld16(lane_base + b * kBf16xBN + g * 16, v);
+          tmem_ld16(lane_base + b * BN + g * 16, v);
           tmem_ld_wait();
 #pragma unroll
           for (int j = 0; j < 16; ++j) run[g * 16 + j] += __uint_as_float(v[j]);
@@ -532,7 +543,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       if (!ok) break;
       const int row = tm * kSplitBM + row_in_tile;
       if (row < p.m) {
-        const int col0 = tn * kBf16xBN + h * kBxColsPerWarp;
+        const int col0 = tn * BN + h * kBxColsPerWarp;
         // scaled FP16 form: the row and column scales come off here (a
         // non-finite row or column is NaN already; its marker exponent is capped)
         const int ea = F16 ? min(p.expA[row], 1024) - 30 : 0;
@@ -593,14 +604,9 @@ struct OzakiParams {
   unsigned *err;
 };
 
-constexpr int kOzStages = 4;
-constexpr int kOzEpiWarps = 16;  // 4 per TMEM lane quarter, 64 columns each
+constexpr int kOzEpiWarps = 16;  // 4 per TMEM lane quarter, BN / 4 columns each
 constexpr int kOzThreads = (2 + kOzEpiWarps) * 32;
 constexpr int kOzABytes = kSplitBM * 128;
-constexpr int kOzBBytes = kOzakiBN * 128;
-constexpr int kOzStage = kOzABytes + kOzBBytes;
-constexpr int kOzSmem = kOzStages * kOzStage + 1024 + 256;
-constexpr int kOzCols = kOzakiBN / (kOzEpiWarps / 4);  // output columns per epilogue warp
 // 16 x 64 = 1024 K-steps per exact chunk: |partial sum| <= 1024 * 127^2 =
 // 16,516,096 < 2^24, so every partial sum is an exactly representable FP32 integer.
 constexpr int kOzChunkStages = 16;
@@ -635,10 +641,13 @@ constexpr int kCrtRunChunks = 64;
 // MC: 2-CTA clusters sharing the B tile, as in bf16x_gemm_kernel.  A row tile
 // past the end (odd tile rows) still takes part in the pipeline (its A loads
 // fetch rows of the next block and its sums are discarded) but writes nothing.
-template <bool MC>
+template <bool MC, int BN>
 __global__ void __launch_bounds__(kOzThreads, 1)
 ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   OzakiParams p) {
+  using T = TileN<BN>;
+  constexpr int kOzStages = T::kStages, kOzStage = T::kStage, kOzBBytes = T::kBBytes;
+  constexpr int kOzCols = T::kCols;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
@@ -703,18 +712,18 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             tma_load_2d(sa_ptr, &tmA, kb * kSplitBK, (sa - 1) * p.Mp + tm * kSplitBM, &full[s]);
             if (MC)
               tma_load_2d_mc(sa_ptr + kOzABytes + rank * (kOzBBytes / 2), &tmB, kb * kSplitBK,
-                             (sb - 1) * p.Np + tn * kOzakiBN + (int)rank * (kOzakiBN / 2),
+                             (sb - 1) * p.Np + tn * BN + (int)rank * (BN / 2),
                              &full[s], 0x3);
             else
               tma_load_2d(sa_ptr + kOzABytes, &tmB, kb * kSplitBK,
-                          (sb - 1) * p.Np + tn * kOzakiBN, &full[s]);
+                          (sb - 1) * p.Np + tn * BN, &full[s]);
           }
         }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16_f32(kSplitBM, kOzakiBN);
+      constexpr uint32_t idesc = idesc_bf16_f32(kSplitBM, BN);
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
@@ -730,7 +739,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               break;
             }
             tc_fence_after();
-            const uint32_t dt = tmem + b * kOzakiBN;
+            const uint32_t dt = tmem + b * BN;
             const int c1 = min(G, c0 + kOzChunkStages);
             for (int idx = c0; idx < c1; ++idx, ++L) {
               const int s = L % kOzStages;
@@ -770,7 +779,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       unit_tile(u, tm, tn);
       const bool real = tm < p.tiles_m;  // MC: a row tile past the end writes nothing
       const int row = tm * kSplitBM + row_in_tile;          // < Mp when real
-      const int col0 = tn * kOzakiBN + h * kOzCols;          // first of this warp's columns
+      const int col0 = tn * BN + h * kOzCols;          // first of this warp's columns
       double *res = p.res + (int64_t)col0 * p.Mp + row;      // res[j * Mp] is column col0 + j
       bool res_init = false;
       const int run_limit = p.mode ? kCrtRunChunks : kOzRunChunks;
@@ -792,7 +801,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 #pragma unroll
           for (int g = 0; g < kOzCols / 16; ++g) {
             uint32_t v[16];
-            tmem_ld16(lane_base + b * kOzakiBN + g * 16, v);
+            tmem_ld16(lane_base + b * BN + g * 16, v);
             tmem_ld_wait();
 #pragma unroll
             for (int j = 0; j < 16; ++j)
@@ -1052,22 +1061,24 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
-// Persistent launch: one CTA per SM (plain), or 2-CTA clusters sharing the B
-// tile when there are at least two row tiles (mc).
-template <bool F16>
-static int bf16x_launch(const CUtensorMap &tA, const CUtensorMap &tB, const Bf16xParams &p, bool mc,
-                        cudaStream_t st) {
+// Persistent launch of a tile kernel: one CTA per SM (plain), or 2-CTA
+// clusters sharing the B tile when there are at least two row tiles (mc).
+template <typename P>
+static int persistent_launch(void (*plain)(const CUtensorMap, const CUtensorMap, P),
+                             void (*clustered)(const CUtensorMap, const CUtensorMap, P),
+                             int threads, int smem, const CUtensorMap &tA, const CUtensorMap &tB,
+                             const P &p, int tiles_m, int tiles_n, bool mc, cudaStream_t st) {
   if (!mc) {
-    if (cudaFuncSetAttribute(bf16x_gemm_kernel<false, F16>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, kBxSmem) != cudaSuccess)
+    if (cudaFuncSetAttribute(plain, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+        cudaSuccess)
       return GB300_ERR_CUDA;
-    const int ntiles = p.tiles_m * p.tiles_n;
+    const int ntiles = tiles_m * tiles_n;
     const int grid = ntiles < sm_count() ? ntiles : sm_count();
-    bf16x_gemm_kernel<false, F16><<<grid, kBxThreads, kBxSmem, st>>>(tA, tB, p);
+    plain<<<grid, threads, smem, st>>>(tA, tB, p);
     return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
   }
-  if (cudaFuncSetAttribute(bf16x_gemm_kernel<true, F16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kBxSmem) != cudaSuccess)
+  if (cudaFuncSetAttribute(clustered, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+      cudaSuccess)
     return GB300_ERR_CUDA;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -1075,22 +1086,49 @@ static int bf16x_launch(const CUtensorMap &tA, const CUtensorMap &tB, const Bf16
   attr[0].val.clusterDim.x = 2;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
-  cfg.blockDim = dim3(kBxThreads);
-  cfg.dynamicSmemBytes = kBxSmem;
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const int npairs = ((p.tiles_m + 1) / 2) * p.tiles_n;
+  const int npairs = ((tiles_m + 1) / 2) * tiles_n;
   int max_clusters = sm_count() / 2;
   cfg.gridDim = dim3((unsigned)(2 * max_clusters));
   int occ = 0;
-  if (cudaOccupancyMaxActiveClusters(&occ, bf16x_gemm_kernel<true, F16>, &cfg) == cudaSuccess &&
-      occ > 0 && occ < max_clusters)
+  if (cudaOccupancyMaxActiveClusters(&occ, clustered, &cfg) == cudaSuccess && occ > 0 &&
+      occ < max_clusters)
     max_clusters = occ;
   cfg.gridDim = dim3((unsigned)(2 * (npairs < max_clusters ? npairs : max_clusters)));
-  if (cudaLaunchKernelEx(&cfg, bf16x_gemm_kernel<true, F16>, tA, tB, p) != cudaSuccess)
-    return GB300_ERR_CUDA;
+  if (cudaLaunchKernelEx(&cfg, clustered, tA, tB, p) != cudaSuccess) return GB300_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+// Tile width of the split GEMMs: 128 for problems with fewer 128 x 256 tiles
+// than SMs whose width would fill less than half of its last 256-wide tile
+// (the grouped batches' small shapes), else 256; GB300_TUNE_TILE_N overrides.
+static int g_tile_n = 0;
+int split_tile_n(int kind, int m, int n, int k) {
+  if (g_tile_n == 128 || g_tile_n == 256) return g_tile_n;
+  const int tuned = tune_tile_n(kind, m, n, k);
+  if (tuned) return tuned;
+  const int64_t tiles256 = ((int64_t)m + kSplitBM - 1) / kSplitBM * (((int64_t)n + 255) / 256);
+  const int rem = n % 256;
+  return (tiles256 < sm_count() && rem != 0 && rem <= 128) ? 128 : 256;
+}
+void set_split_tile_n(int v) { g_tile_n = v; }
+int split_tile_override() { return g_tile_n; }
+
+template <bool F16, int BN>
+static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, cudaStream_t st) {
+  const bool mc = L.Mp / kSplitBM >= 2;  // 2-CTA clusters sharing the B tile
+  CUtensorMap tA{}, tB{};
+  if (!encode_2d(&tA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
+      !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, mc ? BN / 2 : BN, true))
+    return GB300_ERR_CUDA;
+  p.tiles_n = (p.n + BN - 1) / BN;
+  return persistent_launch<Bf16xParams>(bf16x_gemm_kernel<false, F16, BN>,
+                                        bf16x_gemm_kernel<true, F16, BN>, kBxThreads,
+                                        TileN<BN>::kSmem, tA, tB, p, p.tiles_m, p.tiles_n, mc, st);
 }
 
 int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int ldc, int products,
@@ -1109,15 +1147,10 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
   const size_t need = split_workspace_bytes(0, m, n, k, products);
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
   const Bf16xLayout L = bf16x_layout(m, n, k, products, const_cast<void *>(ws));
-  const bool mc = L.Mp / kSplitBM >= 2;  // 2-CTA clusters sharing the B tile
-  CUtensorMap tA{}, tB{};
-  if (!encode_2d(&tA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, mc ? kBf16xBN / 2 : kBf16xBN, true))
-    return GB300_ERR_CUDA;
   Bf16xParams p;
   p.m = m; p.n = n;
   p.tiles_m = (int)(L.Mp / kSplitBM);
-  p.tiles_n = (int)(L.Np / kBf16xBN);
+  p.tiles_n = 0;  // set by the launch for its tile width
   p.kblocks = (int)(L.Kld / kSplitBK);
   const int skb = (int)(L.Kp / kSplitBK);  // K blocks of one segment
   {
@@ -1156,7 +1189,10 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
     p.expA = L.ex;
     p.expB = L.ex + L.Mp;
   }
-  return f16 ? bf16x_launch<true>(tA, tB, p, mc, st) : bf16x_launch<false>(tA, tB, p, mc, st);
+  const int bn = split_tile_n(0, m, n, k);
+  if (f16)
+    return bn == 128 ? bf16x_launch<true, 128>(L, p, st) : bf16x_launch<true, 256>(L, p, st);
+  return bn == 128 ? bf16x_launch<false, 128>(L, p, st) : bf16x_launch<false, 256>(L, p, st);
 }
 
 int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
@@ -1242,7 +1278,7 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
   const OzakiLayout L = ozaki_layout(m, n, k, S, const_cast<void *>(ws));
   OzakiGemmArgs a;
-  a.m = m; a.n = n; a.S = S; a.mode = 0;
+  a.m = m; a.n = n; a.k = k; a.S = S; a.mode = 0;
   a.Mp = L.Mp; a.Np = L.Np; a.Kp = L.Kp;
   a.As = L.As; a.Bs = L.Bs;
   a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc;
@@ -1250,18 +1286,25 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
   return ozaki_gemm_launch(a, st, err);
 }
 
-int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
-  if (a.S < 1 || a.S > (a.mode ? kCrtMaxModuli : kOzakiMaxSlices)) return GB300_ERR_ARG;
+template <int BN>
+static int ozaki_launch_bn(const OzakiGemmArgs &a, OzakiParams p, cudaStream_t st) {
   const bool mc = a.Mp / kSplitBM >= 2;  // 2-CTA clusters sharing the B tile
   CUtensorMap tA{}, tB{};
   if (!encode_2d(&tA, a.As, 2, a.Kp, a.S * a.Mp, a.Kp, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, mc ? kOzakiBN / 2 : kOzakiBN,
-                 true))
+      !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, mc ? BN / 2 : BN, true))
     return GB300_ERR_CUDA;
+  p.tiles_n = (p.n + BN - 1) / BN;
+  return persistent_launch<OzakiParams>(ozaki_gemm_kernel<false, BN>, ozaki_gemm_kernel<true, BN>,
+                                        kOzThreads, TileN<BN>::kSmem, tA, tB, p, p.tiles_m,
+                                        p.tiles_n, mc, st);
+}
+
+int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
+  if (a.S < 1 || a.S > (a.mode ? kCrtMaxModuli : kOzakiMaxSlices)) return GB300_ERR_ARG;
   OzakiParams p;
   p.m = a.m; p.n = a.n;
   p.tiles_m = (int)(a.Mp / kSplitBM);
-  p.tiles_n = (int)(a.Np / kOzakiBN);
+  p.tiles_n = 0;  // set by the launch for its tile width
   p.S = a.S; p.KB = (int)(a.Kp / kSplitBK);
   p.mode = a.mode;
   p.Mp = (int)a.Mp; p.Np = (int)a.Np;
@@ -1271,40 +1314,8 @@ int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
     p.mods[i] = (a.mode && i < a.S) ? a.mods[i] : 1;
     p.mods_mg[i] = p.mods[i] > 1 ? (unsigned)((1ull << 32) / (unsigned)p.mods[i]) : 0u;
   }
-  if (!mc) {
-    if (cudaFuncSetAttribute(ozaki_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kOzSmem) != cudaSuccess)
-      return GB300_ERR_CUDA;
-    const int ntiles = p.tiles_m * p.tiles_n;
-    const int grid = ntiles < sm_count() ? ntiles : sm_count();
-    ozaki_gemm_kernel<false><<<grid, kOzThreads, kOzSmem, st>>>(tA, tB, p);
-    return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
-  }
-  if (cudaFuncSetAttribute(ozaki_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kOzSmem) != cudaSuccess)
-    return GB300_ERR_CUDA;
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = 2;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.blockDim = dim3(kOzThreads);
-  cfg.dynamicSmemBytes = kOzSmem;
-  cfg.stream = st;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  const int npairs = ((p.tiles_m + 1) / 2) * p.tiles_n;
-  int max_clusters = sm_count() / 2;
-  cfg.gridDim = dim3((unsigned)(2 * max_clusters));
-  int occ = 0;
-  if (cudaOccupancyMaxActiveClusters(&occ, ozaki_gemm_kernel<true>, &cfg) == cudaSuccess &&
-      occ > 0 && occ < max_clusters)
-    max_clusters = occ;
-  cfg.gridDim = dim3((unsigned)(2 * (npairs < max_clusters ? npairs : max_clusters)));
-  if (cudaLaunchKernelEx(&cfg, ozaki_gemm_kernel<true>, tA, tB, p) != cudaSuccess)
-    return GB300_ERR_CUDA;
-  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  return split_tile_n(a.mode ? 2 : 1, a.m, a.n, a.k) == 128 ? ozaki_launch_bn<128>(a, p, st)
+                                                           : ozaki_launch_bn<256>(a, p, st);
 }
 
 int ozaki_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,

@@ -27,3 +27,14 @@ def golden():
     import numpy as np
 
     return np.load(os.path.join(ROOT, "tests", "golden", "golden.npz"))
+
+
+@pytest.fixture(params=[128, 256], ids=["tile128", "tile256"])
+def tile_n(request):
+    """Runs a split-form test with each output tile width of the tensor-core
+    GEMMs (the library picks one by shape otherwise)."""
+    import gemm_avx2_gb300 as g
+
+    assert g.tune_param(g.TUNE_TILE_N, request.param) == g.OK
+    yield request.param
+    assert g.tune_param(g.TUNE_TILE_N, 0) == g.OK

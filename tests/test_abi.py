@@ -171,7 +171,7 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
                  '  {"key": "bf16x:9:9:9", "param": 3, "chunk": 8, "ms": 1, "err_max": 1e-5, '
                  '"err_fro": 1e-7, "plain_max": 2e-5, "plain_fro": 1e-6},\n'
                  '  {"key": "bf16x:12:12:12", "param": 259, "chunk": 4, "ms": 1, "err_max": 1e-5, '
-                 '"err_fro": 1e-7, "plain_max": 2e-5, "plain_fro": 1e-6},\n'
+                 '"err_fro": 1e-7, "plain_max": 2e-5, "plain_fro": 1e-6, "tile": 128},\n'
                  '  {"key": "ozaki:8:8:8", "param": 99, "chunk": 0, "ms": 1, "err_max": 0, '
                  '"err_fro": 0, "plain_max": 0, "plain_fro": 0},\n'
                  '  {"key": "crt:9:9:9", "param": 14, "chunk": 0, "ms": 1, "err_max": 1e-14, '
@@ -194,6 +194,8 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
     assert g.split_workspace_bytes(0, 512, 512, 512, 0) == g.split_workspace_bytes(0, 512, 512, 512, 3)
     out = tmp_path / "saved.json"
     assert g.tune_cache_save(str(out)) == g.OK
+    assert '"key": "bf16x:12:12:12", "param": 259, "chunk": 4' in out.read_text()
+    assert '"tile": 128}' in out.read_text()
     g.tune_cache_clear()
     assert g.tune_cache_load(str(out)) == (g.OK, 4)
     assert g.tune_cache_load(str(tmp_path / "missing.json"))[0] == g.ERR_ARG
@@ -202,6 +204,9 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
 
 
 def test_tuning_knobs_validate():
+    assert g.tune_param(g.TUNE_TILE_N, 128) == g.OK
+    assert g.tune_param(g.TUNE_TILE_N, 192) == g.ERR_ARG
+    assert g.tune_param(g.TUNE_TILE_N, 0) == g.OK
     assert g.tune_param(g.TUNE_GRAPH_BRANCHES, 64) == g.OK
     assert g.tune_param(g.TUNE_GRAPH_BRANCHES, 65) == g.ERR_ARG
     assert g.tune_param(g.TUNE_GRAPH_BRANCHES, -1) == g.ERR_ARG

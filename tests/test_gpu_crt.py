@@ -38,7 +38,7 @@ def residue_blocks(ws, N, Mp, Np, Kp):
 
 @pytest.mark.parametrize("N", [8, 16])
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
-def test_residues_and_result_bitexact(orc, N, ta, tb):
+def test_residues_and_result_bitexact(orc, N, ta, tb, tile_n):
     m, n, k = 150, 140, 200
     ar, ac = (m, k) if ta == "N" else (k, m)
     br, bc = (k, n) if tb == "N" else (n, k)
@@ -88,7 +88,7 @@ def test_extreme_exponents_bitexact(orc, N):
 
 
 @pytest.mark.parametrize("m", [300, 129])
-def test_odd_row_tiles_bitexact(orc, m):
+def test_odd_row_tiles_bitexact(orc, m, tile_n):
     """3 and 2 row tiles (m = 300: the 2-CTA clusters get a spare tile that
     must store no residues over a neighbour's; m = 129: a 1-row last tile)."""
     n, k = 290, 150

@@ -59,7 +59,7 @@ def model_check(got, Aop, Bop, alpha, beta, C):
 
 
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
-def test_split_bitexact_and_result(orc, ta, tb):
+def test_split_bitexact_and_result(orc, ta, tb, tile_n):
     m, n, k = 200, 300, 100
     ar, ac = (m, k) if ta == "N" else (k, m)
     br, bc = (k, n) if tb == "N" else (n, k)
@@ -82,7 +82,7 @@ def test_split_bitexact_and_result(orc, ta, tb):
     assert g.device_error() == 0
 
 
-def test_multi_tile_ragged_and_odd_row_tiles(orc):
+def test_multi_tile_ragged_and_odd_row_tiles(orc, tile_n):
     m, n, k = 300, 520, 333
     A = orc.uniform((k, m), np.float32, 72, 0)
     B = orc.uniform((k, n), np.float32, 72, 1)

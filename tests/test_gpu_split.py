@@ -35,7 +35,7 @@ def rel_errs(x, truth):
 
 @pytest.mark.parametrize("products", [3, 6])
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
-def test_bf16x_split_bitexact_and_result(orc, products, ta, tb):
+def test_bf16x_split_bitexact_and_result(orc, products, ta, tb, tile_n):
     m, n, k = 200, 300, 100
     ar, ac = (m, k) if ta == "N" else (k, m)
     br, bc = (k, n) if tb == "N" else (n, k)
@@ -75,7 +75,7 @@ def test_bf16x_split_bitexact_and_result(orc, products, ta, tb):
 
 
 @pytest.mark.parametrize("products", [3, 6])
-def test_bf16x_multi_tile_ragged(orc, products):
+def test_bf16x_multi_tile_ragged(orc, products, tile_n):
     m, n, k = 300, 520, 333
     A = orc.uniform((k, m), np.float32, 12, 0)   # transa = T
     B = orc.uniform((k, n), np.float32, 12, 1)   # transb = N
@@ -102,7 +102,7 @@ def test_bf16x_multi_tile_ragged(orc, products):
 
 @pytest.mark.parametrize("S", [4, 8])
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
-def test_ozaki_slices_bitexact_and_result(orc, S, ta, tb):
+def test_ozaki_slices_bitexact_and_result(orc, S, ta, tb, tile_n):
     m, n, k = 150, 140, 200
     ar, ac = (m, k) if ta == "N" else (k, m)
     br, bc = (k, n) if tb == "N" else (n, k)
@@ -178,7 +178,7 @@ def test_ozaki_slices_extreme_exponents(orc, S, ta):
     assert g.device_error() == 0
 
 
-def test_ozaki_odd_row_tiles(orc):
+def test_ozaki_odd_row_tiles(orc, tile_n):
     """3 row tiles: in 2-CTA clusters the spare fourth tile runs through the
     pipeline but must write neither the FP64 scratch nor C."""
     m, n, k = 300, 270, 200
