@@ -1103,17 +1103,18 @@ static int persistent_launch(void (*plain)(const CUtensorMap, const CUtensorMap,
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
-// Tile width of the split GEMMs: 128 for problems with fewer 128 x 256 tiles
-// than SMs whose width would fill less than half of its last 256-wide tile
-// (the grouped batches' small shapes), else 256; GB300_TUNE_TILE_N overrides.
+// Tile width of the split GEMMs: 128 for outputs at most 128 columns wide
+// (the grouped batches' small shapes: a 256-wide tile would be at most half
+// used), else 256.  128-wide tiles run 1.4-1.6x longer per column (measured
+// from 2048 to 8192, all split forms), so they pay only where they halve the
+// padding.  A tuned width of the shape class, or GB300_TUNE_TILE_N, wins.
 static int g_tile_n = 0;
 int split_tile_n(int kind, int m, int n, int k) {
   if (g_tile_n == 128 || g_tile_n == 256) return g_tile_n;
   const int tuned = tune_tile_n(kind, m, n, k);
   if (tuned) return tuned;
-  const int64_t tiles256 = ((int64_t)m + kSplitBM - 1) / kSplitBM * (((int64_t)n + 255) / 256);
-  const int rem = n % 256;
-  return (tiles256 < sm_count() && rem != 0 && rem <= 128) ? 128 : 256;
+  (void)m;
+  return n <= 128 ? 128 : 256;
 }
 void set_split_tile_n(int v) { g_tile_n = v; }
 int split_tile_override() { return g_tile_n; }

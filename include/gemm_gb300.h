@@ -378,9 +378,9 @@ void gb300_tune_cache_clear(void);
  *   that gb300_grouped_graph_create captures for the split form (form 1);
  *   read at creation.  0 restores the default.
  *   GB300_TUNE_TILE_N: output tile width (128 or 256) of the tensor-core
- *   GEMMs of all split forms; 0 restores the choice by shape (128 for
- *   problems with fewer 128 x 256 tiles than SMs whose last 256-wide tile
- *   would be at most half used, else 256). */
+ *   GEMMs of all split forms; 0 restores the choice by shape (the tuned
+ *   width of the shape class, else 128 for outputs at most 128 columns wide
+ *   and 256 otherwise). */
 enum { GB300_TUNE_BF16X_CHUNK = 1, GB300_TUNE_GRAPH_BRANCHES = 2, GB300_TUNE_TILE_N = 3 };
 int gb300_tune_param(int param, int value);
 
