@@ -385,6 +385,7 @@ def selftest_wait_timeout(poll_limit: int = 4096) -> int:
 TUNE_BF16X_CHUNK = 1
 TUNE_GRAPH_BRANCHES = 2
 TUNE_TILE_N = 3
+TUNE_PAIR_MMA = 4
 TUNE_BF16X = 0     # autotuner kinds
 TUNE_OZAKI = 1
 TUNE_CRT = 2

@@ -1010,6 +1010,10 @@ GB300_API int gb300_tune_param(int param, int value) {
       if (value != 0 && value != 128 && value != 256) return GB300_ERR_ARG;
       set_split_tile_n(value);
       return GB300_OK;
+    case GB300_TUNE_PAIR_MMA:
+      if (value < 0 || value > 2) return GB300_ERR_ARG;
+      set_pair_mma(value);
+      return GB300_OK;
     case GB300_TUNE_GRAPH_BRANCHES:
       if (value < 0 || value > kGraphBranches) return GB300_ERR_ARG;
       g_graph_branches = value ? value : kDefaultGraphBranches;

@@ -6,7 +6,9 @@
 //
 //   split SGEMM : products P in {3, 6} (BF16 terms) or the scaled 3xFP16
 //                 form, x hi*hi chunk length in {2, 4, 8};
-//   all forms   : then the output tile width (128 / 256) of the chosen one;
+//   all forms   : then the output tile width (128 / 256) of the chosen one,
+//                 and for the split SGEMM its cluster mode (pair MMAs or
+//                 multicast B tile);
 //   Ozaki DGEMM : slice count S in [4, 12].
 //
 // A candidate qualifies when its max and Frobenius relative errors against a
@@ -44,6 +46,7 @@ struct TuneEntry {
   int param = 0;       // products (BF16xP) or slices (Ozaki)
   int chunk = 0;       // BF16xP hi*hi chunk length (0 for Ozaki)
   int tile = 0;        // output tile width of the GEMM (128 / 256; 0 = by shape)
+  int pair = 0;        // BF16xP cluster mode (1 pair MMAs, 2 multicast; 0 = default)
   double ms = 0;       // measured time of the chosen candidate
   double err_max = 0, err_fro = 0;              // chosen candidate vs reference
   double plain_max = 0, plain_fro = 0;          // plain kernel vs reference
@@ -79,6 +82,12 @@ int tune_tile_n(int kind, int m, int n, int k) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tune.find(tune_key(kind, m, n, k));
   return it == g_tune.end() ? 0 : it->second.tile;
+}
+
+int tune_pair_mma(int kind, int m, int n, int k) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(tune_key(kind, m, n, k));
+  return it == g_tune.end() ? 0 : it->second.pair;
 }
 
 // ---------------------------------------------------------------- device helpers
@@ -307,6 +316,23 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
     best.tile = t128 < t256 ? 128 : 256;
     best.ms = t128 < t256 ? t128 : t256;
   }
+  // the BF16xP GEMM's cluster mode at that width (same results bit for bit)
+  if (kind == 0) {
+    const int user_tile = split_tile_override(), user_pair = pair_mma_override();
+    double tp = 0, tm = 0;
+    set_split_tile_n(best.tile);
+    set_pair_mma(1);
+    rc = timed(best.param, best.chunk, &tp);
+    if (rc == GB300_OK) {
+      set_pair_mma(2);
+      rc = timed(best.param, best.chunk, &tm);
+    }
+    set_pair_mma(user_pair);
+    set_split_tile_n(user_tile);
+    if (rc != GB300_OK) return rc;
+    best.pair = tp < tm ? 1 : 2;
+    best.ms = tp < tm ? tp : tm;
+  }
   best.plain_max = plain.max_rel;
   best.plain_fro = plain.fro;
   {
@@ -337,9 +363,10 @@ int tune_cache_save(const char *path) {
     const TuneEntry &e = kv.second;
     fprintf(f,
             "  {\"key\": \"%s\", \"param\": %d, \"chunk\": %d, \"ms\": %.6g, \"err_max\": %.6g, "
-            "\"err_fro\": %.6g, \"plain_max\": %.6g, \"plain_fro\": %.6g, \"tile\": %d}%s\n",
+            "\"err_fro\": %.6g, \"plain_max\": %.6g, \"plain_fro\": %.6g, \"tile\": %d, "
+            "\"pair\": %d}%s\n",
             kv.first.c_str(), e.param, e.chunk, e.ms, e.err_max, e.err_fro, e.plain_max,
-            e.plain_fro, e.tile, ++i < g_tune.size() ? "," : "");
+            e.plain_fro, e.tile, e.pair, ++i < g_tune.size() ? "," : "");
   }
   fprintf(f, "]}\n");
   return fclose(f) == 0 ? GB300_OK : GB300_ERR_ARG;
@@ -368,6 +395,9 @@ int tune_cache_load(const char *path, int *loaded) {
     const char *tp = strstr(line, "\"tile\":");
     if (tp && sscanf(tp, "\"tile\": %d", &e.tile) != 1) e.tile = 0;
     if (e.tile != 128 && e.tile != 256) e.tile = 0;
+    const char *pp = strstr(line, "\"pair\":");
+    if (pp && sscanf(pp, "\"pair\": %d", &e.pair) != 1) e.pair = 0;
+    if (e.pair != 1 && e.pair != 2) e.pair = 0;
     const bool bx = strncmp(key, "bf16x:", 6) == 0, oz = strncmp(key, "ozaki:", 6) == 0;
     const bool cr = strncmp(key, "crt:", 4) == 0;
     if (bx && split_products_ok(e.param) && e.chunk >= 0 && e.chunk <= 64)

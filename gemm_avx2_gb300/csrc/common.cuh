@@ -80,6 +80,28 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsign
   if (cta_abort) *cta_abort = 1;
   return false;
 }
+// The same for a barrier whose arrivals come from the other CTA of a cluster
+// (released at cluster scope): the wait acquires at cluster scope.
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t *bar, uint32_t parity, unsigned *err,
+                                                  unsigned code, volatile int *cta_abort) {
+  for (uint32_t i = 0; i < GB300_SPIN_LIMIT; ++i) {
+    if (mbar_try_wait_cluster(bar, parity)) return true;
+    if ((i & 1023u) == 1023u && cta_abort && *cta_abort) return false;
+  }
+  record_error(err, code);
+  if (cta_abort) *cta_abort = 1;
+  return false;
+}
 // Same with a caller-chosen poll limit (used by the timeout self-test).
 __device__ __forceinline__ bool mbar_wait_limit(uint64_t *bar, uint32_t parity, uint32_t limit,
                                                 unsigned *err, unsigned code) {
@@ -108,6 +130,23 @@ __device__ __forceinline__ void tma_load_2d(void *smem_dst, const void *tmap, in
       : "memory");
 }
 
+// Pair form (cta_group::2): the completion is signalled on `bar_cluster`, a
+// shared::cluster address that may lie in the other CTA of the pair (the
+// even CTA's barrier counts both CTAs' bytes).
+__device__ __forceinline__ void tma_load_2d_pair(void *smem_dst, const void *tmap, int32_t x,
+                                                 int32_t y, uint32_t bar_cluster) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(smem_dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(bar_cluster)
+      : "memory");
+}
+// Shared::cluster address of `p` (this CTA's shared memory) as seen in CTA `rank`.
+__device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
+  uint32_t a;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(p)), "r"(rank));
+  return a;
+}
 // TMA load of one box into the same shared-memory offset of every CTA in
 // `mask` (this cluster only), signalling the mbarrier at the same offset in each.
 __device__ __forceinline__ void tma_load_2d_mc(void *smem_dst, const void *tmap, int32_t x,
@@ -155,6 +194,35 @@ __device__ __forceinline__ void tmem_relinquish() {
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
                : "memory");
+}
+// The same for a CTA pair (cta_group::2): one warp of each of the two CTAs
+// of the cluster performs the allocation collectively, and both receive the
+// same TMEM address.
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t *dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish_pair() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+// Arrive on the mbarrier at the same shared-memory offset in CTA `rank` of
+// this cluster.  RELEASE_CLUSTER: release at cluster scope; else the default
+// semantics of mbarrier.arrive.
+template <bool RELEASE_CLUSTER = true>
+__device__ __forceinline__ void mbar_arrive_cluster(uint64_t *bar, uint32_t rank) {
+  uint32_t remote;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(smem_u32(bar)), "r"(rank));
+  if (RELEASE_CLUSTER)
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(remote)
+                 : "memory");
+  else
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(remote) : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -208,6 +276,26 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
       : "memory");
 }
 // Commit that arrives on the mbarrier at the same offset in every CTA of `mask`.
+// Pair MMA (cta_group::2, issued by one thread of the even CTA of the
+// cluster): M = 256 rows, each CTA supplying its 128 rows of A and half of
+// the N columns of B from the same shared-memory offsets; each CTA's TMEM
+// receives its 128 rows of D at the same address.
+__device__ __forceinline__ void umma_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// Arrive once on `bar` in every CTA of `mask` when the pair MMAs issued so far
+// by this thread complete.
+__device__ __forceinline__ void umma_commit_pair(uint64_t *bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+      "[%0], %1;" ::"r"(smem_u32(bar)), "h"(mask)
+      : "memory");
+}
 __device__ __forceinline__ void umma_commit_mc(uint64_t *bar, uint16_t mask) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "

@@ -92,8 +92,14 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
 int split_tile_n(int kind, int m, int n, int k);
 void set_split_tile_n(int v);
 int split_tile_override();
-// Tuned tile width of a shape class (0 = none).
+// Cluster mode of the split GEMMs with two or more row tiles: 0 = default,
+// 1 = pair MMAs (cta_group::2), 2 = per-CTA MMAs with the B tile multicast.
+void set_pair_mma(int v);
+int pair_mma_override();
+// Tuned tile width (0 = none) and cluster mode (0 = none, 1 = pair MMAs,
+// 2 = multicast) of a shape class.
 int tune_tile_n(int kind, int m, int n, int k);
+int tune_pair_mma(int kind, int m, int n, int k);
 
 // Accumulation chunk of the BF16xP GEMM in 64-wide K blocks (0 = default, 4).
 int bf16x_chunk_kblocks();

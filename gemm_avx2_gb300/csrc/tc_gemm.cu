@@ -381,12 +381,32 @@ struct TileN {
 // of the shared B tile, multicast into both CTAs' stage (the B tensor map's box
 // is then 128 rows).  Each stage's empty barrier counts both CTAs' MMA commits,
 // since a stage holds data its peer wrote.  This halves the B tile's L2 reads.
-template <bool MC, bool F16, int BN>
+// Cluster modes of the tile kernels: 0 = one CTA per tile; 1 = 2-CTA
+// clusters, each CTA's own MMAs (cta_group::1) on the B tile it shares with
+// its peer by TMA multicast; 2 = pair MMAs (cta_group::2, M = 256): each CTA
+// holds its 128 rows of A and half of B, the even CTA issues the MMAs for
+// both, so a stage is 32 KB instead of 48 KB and the ring 6 deep instead of 4.
+// In mode 2 both CTAs' TMA loads complete on the even CTA's full barrier,
+// and the odd CTA's epilogue warps report drained TMEM buffers to the even
+// CTA with plain (default-semantics) remote arrives: cluster-scope release
+// arrives made the kernel 2.5x slower.
+template <int CL, int BN>
+struct ClusterTile {
+  static constexpr bool kPair = CL == 2;
+  static constexpr int kBBytes = (kPair ? BN / 2 : BN) * 128;  // B bytes in one CTA's stage
+  static constexpr int kStage = kSplitBM * 128 + kBBytes;
+  static constexpr int kStages = kPair ? (BN == 256 ? 6 : 8) : TileN<BN>::kStages;
+  static constexpr int kSmem = kStages * kStage + 1024 + 256;
+};
+
+template <int CL, bool F16, int BN>
 __global__ void __launch_bounds__(kBxThreads, 1)
 bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   Bf16xParams p) {
   using T = TileN<BN>;
-  constexpr int kBxStages = T::kStages, kBxStage = T::kStage, kBxBBytes = T::kBBytes;
+  using CT = ClusterTile<CL, BN>;
+  constexpr bool MC = CL != 0, PAIR = CT::kPair;
+  constexpr int kBxStages = CT::kStages, kBxStage = CT::kStage, kBxBBytes = CT::kBBytes;
   constexpr int kBxColsPerWarp = T::kCols;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -401,18 +421,27 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kBxStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], MC ? 2 : 1); }
-    for (int b = 0; b < 2; ++b) { mbar_init(&accf[b], 1); mbar_init(&acce[b], kBxEpiWarps); }
+    for (int s = 0; s < kBxStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], CL == 1 ? 2 : 1);  // multicast: both CTAs' commits; pair: one
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], PAIR ? 2 * kBxEpiWarps : kBxEpiWarps);  // pair: both CTAs drain
+    }
     mbar_init(done, 1);
     *abort_flag = 0;
     fence_barrier_init();
     tma_prefetch_desc(&tmA);
     tma_prefetch_desc(&tmB);
   }
-  if (warp == 1) { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
+  if (warp == 1) {
+    if (PAIR) { tmem_alloc_pair(tmem_slot, 512); tmem_relinquish_pair(); }
+    else { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
+  }
   tc_fence_before();
   __syncthreads();
-  if (MC) cluster_sync();  // the peer's barriers are initialised before any multicast
+  if (MC) cluster_sync();  // the peer's barriers are initialised before any remote arrive
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   // work units: tiles, or (MC) row-tile pairs whose rank-th row tile is this CTA's
@@ -449,7 +478,16 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           const uint32_t r = L / kBxStages;
           if (!mbar_wait(&empty[s], (r & 1) ^ 1, p.err, kErrTimeoutEmpty, abort_flag)) break;
           uint8_t *sa = smem + s * kBxStage;
-          mbar_arrive_expect_tx(&full[s], kBxStage);  // own A, both B halves
+          if (PAIR) {
+            // both CTAs' A rows and B halves land on the even CTA's full barrier
+            if (rank == 0) mbar_arrive_expect_tx(&full[s], 2 * kBxStage);
+            const uint32_t fb = cluster_addr(&full[s], 0);
+            tma_load_2d_pair(sa, &tmA, kb * kSplitBK, tm * kSplitBM, fb);
+            tma_load_2d_pair(sa + kBxABytes, &tmB, kb * kSplitBK, tn * BN + (int)rank * (BN / 2),
+                             fb);
+            continue;
+          }
+          mbar_arrive_expect_tx(&full[s], kBxStage);  // own A and B rows (both B halves: MC)
           tma_load_2d(sa, &tmA, kb * kSplitBK, tm * kSplitBM, &full[s]);
           if (MC)
             tma_load_2d_mc(sa + kBxABytes + rank * (kBxBBytes / 2), &tmB, kb * kSplitBK,
@@ -459,10 +497,12 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         }
       }
     }
+  } else if (warp == 1 && PAIR && rank == 1) {
+    // odd CTA of a pair: the even CTA issues the MMAs of both
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc =
-          F16 ? idesc_f16_f32(kSplitBM, BN) : idesc_bf16_f32(kSplitBM, BN);
+      constexpr int kM = PAIR ? 2 * kSplitBM : kSplitBM;
+      constexpr uint32_t idesc = F16 ? idesc_f16_f32(kM, BN) : idesc_bf16_f32(kM, BN);
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
@@ -473,6 +513,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           const int c1 = min(rend, c0 + run_chunk(rn));
           const int b = chunk & 1;
           const uint32_t u = chunk >> 1;
+          // pair: half of the arrivals come from the odd CTA's epilogue warps
           if (!mbar_wait(&acce[b], (u & 1) ^ 1, p.err, kErrTimeoutMma, abort_flag)) {
             ok = false;
             break;
@@ -489,21 +530,36 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             tc_fence_after();
             const uint32_t sa = smem_u32(smem + s * kBxStage), sb = sa + kBxABytes;
 #pragma unroll
-            for (int kk = 0; kk < kSplitBK / 16; ++kk)
-              umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32), idesc,
-                        (kb > c0 || kk > 0) ? 1u : 0u);
-            if (MC)
+            for (int kk = 0; kk < kSplitBK / 16; ++kk) {
+              if (PAIR)
+                umma_pair(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32), idesc,
+                          (kb > c0 || kk > 0) ? 1u : 0u);
+              else
+                umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32),
+                          idesc, (kb > c0 || kk > 0) ? 1u : 0u);
+            }
+            if (PAIR)
+              umma_commit_pair(&empty[s], 0x3);  // both CTAs' stage s is free
+            else if (MC)
               umma_commit_mc(&empty[s], 0x3);  // the stage is free once both CTAs are done
             else
               umma_commit(&empty[s]);
           }
-          if (ok) umma_commit(&accf[b]);
+          if (ok) {
+            if (PAIR)
+              umma_commit_pair(&accf[b], 0x3);
+            else
+              umma_commit(&accf[b]);
+          }
           c0 = c1;
           if (c0 == rend) ++rn;
         }
       }
       // every issued MMA has completed before TMEM is released
-      umma_commit(done);
+      if (PAIR)
+        umma_commit_pair(done, 0x1);
+      else
+        umma_commit(done);
       mbar_wait(done, 0, p.err, kErrTimeoutMma, nullptr);
     }
   } else {
@@ -538,7 +594,12 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&acce[b]);
+        if (lane == 0) {
+          if (PAIR)
+            mbar_arrive_cluster<false>(&acce[b], 0);  // the even CTA issues the MMAs of both
+          else
+            mbar_arrive(&acce[b]);
+        }
       }
       if (!ok) break;
       const int row = tm * kSplitBM + row_in_tile;
@@ -573,11 +634,15 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   }
   tc_fence_before();
   __syncthreads();
+  if (PAIR) cluster_sync();  // both CTAs are done with the pair's TMEM
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, 512);
+    if (PAIR)
+      tmem_dealloc_pair(tmem, 512);
+    else
+      tmem_dealloc(tmem, 512);
   }
-  if (MC) cluster_sync();  // no peer multicast or commit can still target this CTA
+  if (MC) cluster_sync();  // no peer multicast, commit or arrive can still target this CTA
 }
 
 // ===========================================================================
@@ -1119,17 +1184,37 @@ int split_tile_n(int kind, int m, int n, int k) {
 void set_split_tile_n(int v) { g_tile_n = v; }
 int split_tile_override() { return g_tile_n; }
 
+// Cluster mode of the BF16xP GEMM with two or more row tiles: pair MMAs
+// (kernel mode 2) or per-CTA MMAs on a multicast B tile (mode 1).  Same
+// results bit for bit; neither is faster everywhere (pair: 3-4% faster on
+// SGEMM 8192^3, 5% slower on the 16384 x 8192 x 16384 problem of CGEMM 8192^3
+// under the power cap), so the autotuner times both per shape class.  Order:
+// GB300_TUNE_PAIR_MMA, the tuned mode of the shape class, multicast.
+static int g_pair_mma = 0;  // 0: none, 1: pair MMAs, 2: multicast
+void set_pair_mma(int v) { g_pair_mma = v; }
+int pair_mma_override() { return g_pair_mma; }
+static bool use_pair_mma(int m, int n, int k) {
+  const int v = g_pair_mma ? g_pair_mma : tune_pair_mma(0, m, n, k);
+  return v == 1;
+}
+
 template <bool F16, int BN>
-static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, cudaStream_t st) {
-  const bool mc = L.Mp / kSplitBM >= 2;  // 2-CTA clusters sharing the B tile
+static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, int k, cudaStream_t st) {
+  const bool mc = L.Mp / kSplitBM >= 2;  // 2-CTA clusters on row-tile pairs
   CUtensorMap tA{}, tB{};
   if (!encode_2d(&tA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
       !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, mc ? BN / 2 : BN, true))
     return GB300_ERR_CUDA;
   p.tiles_n = (p.n + BN - 1) / BN;
-  return persistent_launch<Bf16xParams>(bf16x_gemm_kernel<false, F16, BN>,
-                                        bf16x_gemm_kernel<true, F16, BN>, kBxThreads,
-                                        TileN<BN>::kSmem, tA, tB, p, p.tiles_m, p.tiles_n, mc, st);
+  if (mc && use_pair_mma(p.m, p.n, k))
+    return persistent_launch<Bf16xParams>(bf16x_gemm_kernel<0, F16, BN>,
+                                          bf16x_gemm_kernel<2, F16, BN>, kBxThreads,
+                                          ClusterTile<2, BN>::kSmem, tA, tB, p, p.tiles_m,
+                                          p.tiles_n, true, st);
+  return persistent_launch<Bf16xParams>(bf16x_gemm_kernel<0, F16, BN>,
+                                        bf16x_gemm_kernel<1, F16, BN>, kBxThreads,
+                                        ClusterTile<1, BN>::kSmem, tA, tB, p, p.tiles_m, p.tiles_n,
+                                        mc, st);
 }
 
 int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int ldc, int products,
@@ -1192,8 +1277,8 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
   }
   const int bn = split_tile_n(0, m, n, k);
   if (f16)
-    return bn == 128 ? bf16x_launch<true, 128>(L, p, st) : bf16x_launch<true, 256>(L, p, st);
-  return bn == 128 ? bf16x_launch<false, 128>(L, p, st) : bf16x_launch<false, 256>(L, p, st);
+    return bn == 128 ? bf16x_launch<true, 128>(L, p, k, st) : bf16x_launch<true, 256>(L, p, k, st);
+  return bn == 128 ? bf16x_launch<false, 128>(L, p, k, st) : bf16x_launch<false, 256>(L, p, k, st);
 }
 
 int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,

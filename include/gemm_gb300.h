@@ -380,8 +380,19 @@ void gb300_tune_cache_clear(void);
  *   GB300_TUNE_TILE_N: output tile width (128 or 256) of the tensor-core
  *   GEMMs of all split forms; 0 restores the choice by shape (the tuned
  *   width of the shape class, else 128 for outputs at most 128 columns wide
- *   and 256 otherwise). */
-enum { GB300_TUNE_BF16X_CHUNK = 1, GB300_TUNE_GRAPH_BRANCHES = 2, GB300_TUNE_TILE_N = 3 };
+ *   and 256 otherwise).
+ *   GB300_TUNE_PAIR_MMA: how the BF16xP GEMM runs problems with two or more
+ *   128-row tiles: 1 = pair MMAs (tcgen05 cta_group::2: two CTAs compute a
+ *   256-row tile, each holding half of the B tile), 2 = one MMA issuer per
+ *   CTA with the B tile multicast to both CTAs of the cluster; 0 restores
+ *   the default (the tuned mode of the shape class, else multicast).  Both
+ *   give the same results bit for bit. */
+enum {
+  GB300_TUNE_BF16X_CHUNK = 1,
+  GB300_TUNE_GRAPH_BRANCHES = 2,
+  GB300_TUNE_TILE_N = 3,
+  GB300_TUNE_PAIR_MMA = 4
+};
 int gb300_tune_param(int param, int value);
 
 /* Library version string. */

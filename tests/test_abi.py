@@ -195,7 +195,7 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
     out = tmp_path / "saved.json"
     assert g.tune_cache_save(str(out)) == g.OK
     assert '"key": "bf16x:12:12:12", "param": 259, "chunk": 4' in out.read_text()
-    assert '"tile": 128}' in out.read_text()
+    assert '"tile": 128, "pair": 0}' in out.read_text()
     g.tune_cache_clear()
     assert g.tune_cache_load(str(out)) == (g.OK, 4)
     assert g.tune_cache_load(str(tmp_path / "missing.json"))[0] == g.ERR_ARG
@@ -207,6 +207,9 @@ def test_tuning_knobs_validate():
     assert g.tune_param(g.TUNE_TILE_N, 128) == g.OK
     assert g.tune_param(g.TUNE_TILE_N, 192) == g.ERR_ARG
     assert g.tune_param(g.TUNE_TILE_N, 0) == g.OK
+    assert g.tune_param(g.TUNE_PAIR_MMA, 2) == g.OK
+    assert g.tune_param(g.TUNE_PAIR_MMA, 3) == g.ERR_ARG
+    assert g.tune_param(g.TUNE_PAIR_MMA, 0) == g.OK
     assert g.tune_param(g.TUNE_GRAPH_BRANCHES, 64) == g.OK
     assert g.tune_param(g.TUNE_GRAPH_BRANCHES, 65) == g.ERR_ARG
     assert g.tune_param(g.TUNE_GRAPH_BRANCHES, -1) == g.ERR_ARG

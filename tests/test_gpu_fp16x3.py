@@ -175,3 +175,35 @@ def test_host_and_noalloc_paths(orc):
                                  dC.data_ptr(), m, products=g.FP16X3) == g.OK
     sync()
     assert np.array_equal(from_dev(dC, m), Ch)
+
+
+@pytest.mark.parametrize("products", [6, g.FP16X3])
+@pytest.mark.parametrize("tile", [128, 256])
+def test_pair_and_multicast_modes_agree(orc, products, tile):
+    """The pair MMAs (cta_group::2, two CTAs per 256-row tile, each holding half
+    of the B tile) and the per-CTA MMAs on a multicast B tile give the same
+    result bit for bit, for even and odd numbers of row tiles."""
+    outs = []
+    try:
+        assert g.tune_param(g.TUNE_TILE_N, tile) == g.OK
+        for mode in (1, 2):
+            assert g.tune_param(g.TUNE_PAIR_MMA, mode) == g.OK
+            res = []
+            for m, n, k in ((256, 300, 200), (640, 520, 333)):
+                A = orc.uniform((k, m), np.float32, 77, 0)
+                B = orc.uniform((k, n), np.float32, 77, 1)
+                C = orc.uniform((m + 3, n), np.float32, 77, 2)
+                dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
+                assert g.sgemm_bf16x("T", "N", m, n, k, 1.0, dA.data_ptr(), k, dB.data_ptr(), k,
+                                     0.5, dC.data_ptr(), m + 3, products=products) == g.OK
+                sync()
+                got = from_dev(dC, m + 3)
+                assert np.array_equal(got[m:], C[m:])
+                res.append(got)
+            outs.append(res)
+    finally:
+        g.tune_param(g.TUNE_PAIR_MMA, 0)
+        g.tune_param(g.TUNE_TILE_N, 0)
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+    assert g.device_error() == 0
