@@ -262,6 +262,18 @@ def run_ours(args, torch, rank, world):
     # of the two qualifying schemes is timed below.
     schemes = [("crt", list(range(11, 25))), ("ozaki", list(range(6, 13)))] if is_d else \
         [("bf16x", [3, 6]), ("bf16x", [g.FP16X3])]
+    # FP32: the autotuner's choice for this shape class on these operands
+    # (form, chunk length, tile width, cluster mode), products = 0 below
+    tuned = None
+    if not is_d and not args.form:
+        rc, chosen = g.autotune(g.TUNE_BF16X, w["ta"], w["tb"], m, n, k, prob.A.data_ptr(),
+                                w["lda"], prob.B.data_ptr(), w["ldb"], stream)
+        if rc == g.OK:
+            _, tp, tc = g.tune_lookup(g.TUNE_BF16X, m, n, k)
+            _, tile, mode = g.tune_layout(g.TUNE_BF16X, m, n, k)
+            tuned = {"products": tp, "chunk": tc, "tile_n": tile,
+                     "cluster": "pair MMAs" if mode == 1 else "multicast B"}
+            schemes.append(("bf16x", [0]))
     errs, qualified = {}, []
     ws = None
 
@@ -276,6 +288,10 @@ def run_ours(args, torch, rank, world):
                            ws.data_ptr(), need, stream) == g.OK
 
     def name_of(f, prm):
+        if f == "bf16x" and prm == 0 and tuned:
+            base = "fp16x3" if tuned["products"] == g.FP16X3 else "bf16x%d" % tuned["products"]
+            return "tuned:%s_c%d_t%d_%s" % (base, tuned["chunk"], tuned["tile_n"],
+                                            "pair" if tuned["cluster"] == "pair MMAs" else "mc")
         if f == "bf16x" and prm == g.FP16X3:
             return "fp16x3"
         return {"bf16x": "bf16x%d", "ozaki": "ozaki_s%d", "crt": "crt_n%d"}[f] % prm
@@ -420,7 +436,8 @@ def run_ours(args, torch, rank, world):
 
     # ---- roofline of the dominant kernel (the tcgen05 GEMM of the split form)
     pk = peaks()
-    products = {"bf16x": 3 if param == g.FP16X3 else param,
+    eff = tuned["products"] if (form == "bf16x" and param == 0 and tuned) else param
+    products = {"bf16x": 3 if eff == g.FP16X3 else eff,
                 "ozaki": (param * (param + 1)) // 2, "crt": param}[form]
     pipe_flops = products * prob.flops
     achieved = pipe_flops / (gemm_ms / 1e3) / 1e12
@@ -452,6 +469,7 @@ def run_ours(args, torch, rank, world):
                    "n": n, "k": k, "lda": w["lda"], "ldb": w["ldb"], "ldc": w["ldc"],
                    "alpha": w["alpha"], "beta": w["beta"], "form": form_name,
                    "phi": float(w.get("phi", 0.0)),
+                   "autotuned": tuned,
                    "exponent_spread": exponent_spread(prob),
                    "l2": "inputs larger than L2 (%d MB per operand > %d MB)" % (
                        prob.A.numel() * prob.A.element_size() // 2**20, L2_BYTES // 2**20),
@@ -470,7 +488,7 @@ def run_ours(args, torch, rank, world):
         # two-pass forms add one max |.| launch (both operands, exponents by
         # its last CTA); the CRT form adds the reconstruction
         "gpu_launches": args.steps * ({"bf16x": 2, "ozaki": 3, "crt": 4}[form] +
-                                      (1 if form == "bf16x" and param == g.FP16X3 else 0)),
+                                      (1 if form == "bf16x" and eff == g.FP16X3 else 0)),
     }
     if rank == 0:
         line["cpu_baseline"] = (cpu_baseline(w, args.cpu_seconds) if not args.no_cpu

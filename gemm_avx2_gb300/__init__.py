@@ -116,6 +116,8 @@ def core() -> ctypes.CDLL:
                                      c_void_p, c_int, c_void_p, ctypes.POINTER(c_int)]
         L.gb300_tune_lookup.argtypes = [c_int, c_int, c_int, c_int, ctypes.POINTER(c_int),
                                         ctypes.POINTER(c_int)]
+        L.gb300_tune_layout.argtypes = [c_int, c_int, c_int, c_int, ctypes.POINTER(c_int),
+                                        ctypes.POINTER(c_int)]
         L.gb300_tune_cache_save.argtypes = [ctypes.c_char_p]
         L.gb300_tune_cache_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(c_int)]
         L.gb300_tune_cache_clear.restype = None
@@ -407,6 +409,13 @@ def tune_lookup(kind, m, n, k):
     return rc, p.value, c.value
 
 
+def tune_layout(kind, m, n, k):
+    """(status, tile width, cluster mode) the split GEMMs use for this shape."""
+    t, pm = c_int(0), c_int(0)
+    rc = core().gb300_tune_layout(kind, m, n, k, ctypes.byref(t), ctypes.byref(pm))
+    return rc, t.value, pm.value
+
+
 def tune_cache_save(path=None) -> int:
     return core().gb300_tune_cache_save(path.encode() if path else None)
 
@@ -500,7 +509,8 @@ CORE_SYMBOLS = [
     "gb300_dgemm_ozaki_run", "gb300_host_sgemm_bf16x", "gb300_host_dgemm_ozaki",
     "gb300_selftest_wait_timeout", "gb300_sgemm_bf16x_noalloc", "gb300_tune_param",
     "gb300_grouped_workspace_bytes", "gb300_gemm_grouped", "gb300_gemm_grouped_ws",
-    "gb300_autotune", "gb300_tune_lookup", "gb300_tune_cache_save", "gb300_tune_cache_load",
+    "gb300_autotune", "gb300_tune_lookup", "gb300_tune_layout", "gb300_tune_cache_save",
+    "gb300_tune_cache_load",
     "gb300_tune_cache_clear", "gb300_dtrsm", "gb300_strsm", "gb300_dtrmm", "gb300_strmm",
     "gb300_grouped_graph_create", "gb300_grouped_graph_launch", "gb300_grouped_graph_destroy",
     "gb300_cgemm", "gb300_zgemm", "gb300_host_cgemm", "gb300_host_zgemm",

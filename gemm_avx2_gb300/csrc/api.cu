@@ -995,6 +995,15 @@ GB300_API int gb300_tune_lookup(int kind, int m, int n, int k, int *param, int *
   if (chunk) *chunk = c;
   return tune_lookup(kind, m, n, k, nullptr, nullptr) ? GB300_OK : GB300_ERR_UNSUPPORTED;
 }
+GB300_API int gb300_tune_layout(int kind, int m, int n, int k, int *tile_n, int *pair_mma) {
+  if (kind < 0 || kind > 2) return GB300_ERR_ARG;
+  if (tile_n) *tile_n = split_tile_n(kind, m, n, k);
+  if (pair_mma) {
+    const int v = kind == 0 ? tune_pair_mma(kind, m, n, k) : 0;
+    *pair_mma = v ? v : 2;
+  }
+  return tune_lookup(kind, m, n, k, nullptr, nullptr) ? GB300_OK : GB300_ERR_UNSUPPORTED;
+}
 GB300_API int gb300_tune_cache_save(const char *path) { return tune_cache_save(path); }
 GB300_API int gb300_tune_cache_load(const char *path, int *loaded) {
   return tune_cache_load(path, loaded);

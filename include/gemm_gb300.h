@@ -364,6 +364,11 @@ int gb300_selftest_wait_timeout(unsigned poll_limit);
 int gb300_autotune(int kind, char transa, char transb, int m, int n, int k, const void *A,
                    int lda, const void *B, int ldb, void *stream, int *chosen);
 int gb300_tune_lookup(int kind, int m, int n, int k, int *param, int *chunk);
+/* The output tile width (128 / 256) and, for kind 0, the cluster mode (1 =
+ * pair MMAs, 2 = multicast B tile) the split GEMMs use for this shape (knob,
+ * tuned entry or default, in that order); GB300_ERR_UNSUPPORTED when the
+ * shape class has no tuned entry. */
+int gb300_tune_layout(int kind, int m, int n, int k, int *tile_n, int *pair_mma);
 int gb300_tune_cache_save(const char *path);
 int gb300_tune_cache_load(const char *path, int *loaded);
 void gb300_tune_cache_clear(void);
