@@ -9,8 +9,9 @@ split form at equal error to the native FP32/FP64 kernel.  A step is one call
 of the split form (split kernels + tcgen05 GEMM) over the workload's inputs,
 already resident in HBM.  The default workload is SGEMM TN m=n=k=8192,
 alpha=1, beta=0 (the configuration the metric is quoted on); the split form
-(3xBF16 or 6xBF16) is the smallest one whose max relative error on sampled
-entries does not exceed the plain FP32 kernel's.
+(3xBF16, 6xBF16, scaled 3xFP16, or the autotuned layout of the shape class)
+is the fastest of those whose max relative error on sampled entries does not
+exceed the plain FP32 kernel's; --form pins one (e.g. fp16x3_c8_t256_pair).
 
 Printed JSON line (rank 0): metric/value/unit, ms_per_step, e2e (the same
 metric through the host-pointer C ABI with host<->device copies inside the
@@ -337,6 +338,9 @@ def run_ours(args, torch, rank, world):
         form, param = best[1], best[2]
     else:
         form, param = qualified[0]
+    # a pinned layout keeps its full name (chunk, tile width, cluster mode)
+    form_name = (args.form[len("tuned:"):] if args.form.startswith("tuned:") else args.form) \
+        if forced else name_of(form, param)
     need = g.split_workspace_bytes(kind_of(form), m, n, k, param)
     if ws is None or ws.numel() < need:
         ws = None
@@ -443,7 +447,7 @@ def run_ours(args, torch, rank, world):
     achieved = pipe_flops / (gemm_ms / 1e3) / 1e12
     roof = {"bound": "tensor", "achieved": round(achieved, 2), "peak": pk["bf16_tflops"],
             "unit": "TFLOP/s", "frac": round(achieved / pk["bf16_tflops"], 4),
-            "traffic": traffic_from_profile(args.workload, name_of(form, param)),
+            "traffic": traffic_from_profile(args.workload, form_name),
             "kernel": {"bf16x": "bf16x_gemm_kernel", "ozaki": "ozaki_gemm_kernel",
                        "crt": "ozaki_gemm_kernel (CRT mode) + crt_reconstruct_kernel"}[form],
             "kernel_ms": round(gemm_ms, 4), "prepare_ms": round(prep_ms, 4),
@@ -457,7 +461,6 @@ def run_ours(args, torch, rank, world):
                    "peak": pk["hbm_gbs"], "frac": round(io_bytes / (gemm_ms / 1e3) / 1e9 /
                                                         pk["hbm_gbs"], 4),
                    "algorithmic_bytes": io_bytes}
-    form_name = name_of(form, param)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -498,14 +501,30 @@ def run_ours(args, torch, rank, world):
 
 def parse_form(name):
     """'crt_n15' -> ('crt', 15), 'ozaki_s8' -> ('ozaki', 8), 'bf16x6' -> ('bf16x', 6),
-    'fp16x3' -> ('bf16x', FP16X3) (the scaled FP16 form shares the BF16xP entry points)."""
-    if name == "fp16x3":
-        import gemm_avx2_gb300 as g
+    'fp16x3' -> ('bf16x', FP16X3) (the scaled FP16 form shares the BF16xP entry points).
+    A tuned name such as 'tuned:fp16x3_c8_t256_pair' (or without 'tuned:') pins
+    the layout the autotuner chose: hi*hi chunk length (_cN), tile width (_tN)
+    and cluster mode (_pair / _mc) are set as the library's tuning knobs."""
+    import gemm_avx2_gb300 as g
+
+    name = name[len("tuned:"):] if name.startswith("tuned:") else name
+    base, *opts = name.split("_") if not name.startswith(("crt_n", "ozaki_s")) else (name,)
+    for o in opts:
+        if o[:1] == "c" and o[1:].isdigit():
+            g.tune_param(g.TUNE_BF16X_CHUNK, int(o[1:]))
+        elif o[:1] == "t" and o[1:].isdigit():
+            assert g.tune_param(g.TUNE_TILE_N, int(o[1:])) == g.OK
+        elif o in ("pair", "mc"):
+            g.tune_param(g.TUNE_PAIR_MMA, 1 if o == "pair" else 2)
+        else:
+            raise SystemExit("--form: unknown option %r in %r" % (o, name))
+    if base == "fp16x3":
         return "bf16x", g.FP16X3
     for prefix, form in (("crt_n", "crt"), ("ozaki_s", "ozaki"), ("bf16x", "bf16x")):
-        if name.startswith(prefix) and name[len(prefix):].isdigit():
-            return form, int(name[len(prefix):])
-    raise SystemExit("--form: expected crt_nN, ozaki_sS, bf16xP or fp16x3, got %r" % name)
+        if base.startswith(prefix) and base[len(prefix):].isdigit():
+            return form, int(base[len(prefix):])
+    raise SystemExit("--form: expected crt_nN, ozaki_sS, bf16xP or fp16x3 (optionally with "
+                     "_cN, _tN, _pair or _mc), got %r" % name)
 
 
 # ----------------------------------------------------------------------------- complex workloads
@@ -888,10 +907,13 @@ def run_grouped(args, torch, rank, world):
 
 
 def traffic_from_profile(workload, form_name):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary
+    (a tuned layout is looked up under its pinned name, without 'tuned:')."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         d = json.load(open(p))
+        if form_name.startswith("tuned:"):
+            form_name = form_name[len("tuned:"):]
         v = d.get("%s:%s" % (workload, form_name))
         if v is not None:
             return v
@@ -1068,7 +1090,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-pointer leg (profiling runs)")
     ap.add_argument("--form", default=None,
                     help="use this split form instead of timing the qualifying ones "
-                         "(crt_nN, ozaki_sS, bf16xP, fp16x3; profiling runs)")
+                         "(crt_nN, ozaki_sS, bf16xP, fp16x3, optionally with _cN chunk, _tN "
+                         "tile width, _pair / _mc cluster mode; profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
