@@ -19,6 +19,8 @@ Contents (all thin ctypes wrappers over ``oracle/liborc.so``, built from
 * ``zgemm_port``: the complex kernels' arithmetic in portable C (CPU baseline).
 * ``RefCplx``: the reference's OpenBLAS-style complex and 3M kernels
   (``oracle/_ref/libcplx.so``, x86-64 only) behind ``oracle/ref_cplx.c``.
+* ``RefBlas3``: the reference's OpenBLAS-style TRSM and TRMM kernels
+  (``oracle/_ref/libblas3.so``, x86-64 only) behind ``oracle/ref_blas3.c``.
 * ``split``: numpy restatements of the split-precision decompositions
   (3xBF16 hi/lo and the int8-valued Ozaki slices) used to check the GPU split
   kernels bit for bit.
@@ -260,6 +262,42 @@ class RefCplx:
         rc = f(0, 0, m, n, k, complex(alpha).real, complex(alpha).imag, _ptr(A), A.shape[0],
                _ptr(B), B.shape[0], _ptr(C), C.shape[0])
         assert rc == 0
+
+
+class RefBlas3:
+    """The reference's TRSM kernels (TRSM_KERNEL_*_simplified.c over its
+    dgemm_kernel_4x4_haswell.c; strsm_kernel_8x4_haswell_*.c) and TRMM kernel
+    (trmm_kernel_4x8_simplified.c), compiled from their sources into
+    oracle/_ref/libblas3.so (x86-64 only), called on the whole problem as one
+    packed block."""
+
+    PATH = os.path.join(HERE, "_ref", "libblas3.so")
+
+    def __init__(self):
+        if not os.path.exists(self.PATH):
+            raise FileNotFoundError("reference TRSM/TRMM kernels not built (x86-64 with sources only)")
+        L = ctypes.CDLL(self.PATH)
+        lng = ctypes.c_long
+        for r in ("trsm", "trmm"):
+            for p, F in (("d", c_double), ("s", c_float)):
+                getattr(L, "ref_%s_%s" % (r, p)).argtypes = [c_char, c_char, c_char, c_char, lng,
+                                                             lng, F, c_void_p, lng, c_void_p, lng]
+        self.L = L
+
+    @classmethod
+    def available(cls) -> bool:
+        return os.path.exists(cls.PATH)
+
+    def call(self, routine, side, uplo, transa, diag, m, n, alpha, A, B) -> np.ndarray:
+        """B := alpha inv(op(A)) B / B inv(op(A)) (trsm) or alpha op(A) B / B op(A)
+        (trmm); A and B Fortran arrays of one dtype; returns the updated copy of B."""
+        assert A.dtype == B.dtype and A.flags.f_contiguous and B.flags.f_contiguous
+        out = np.array(B, order="F", copy=True)
+        f = getattr(self.L, "ref_%s_%s" % (routine, "d" if B.dtype == np.float64 else "s"))
+        rc = f(side.encode(), uplo.encode(), transa.encode(), diag.encode(), m, n, alpha,
+               _ptr(A), A.shape[0], _ptr(out), out.shape[0])
+        assert rc == 0
+        return out
 
 
 def set_threads(n: int) -> None:

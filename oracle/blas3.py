@@ -2,8 +2,12 @@
 
 The reference has TRSM/TRMM only as OpenBLAS-style packed-panel kernels outside
 its built library (OpenBLAS-like_implementation/TRSM_KERNEL_*_simplified.c,
-trmm_kernel_4x8_simplified.c), so there is nothing of it to run: these follow
-the BLAS definitions directly, in FP64 (parity unpinned for these two routines).
+strsm_kernel_8x4_haswell_*.c, trmm_kernel_4x8_simplified.c).  These follow the
+BLAS definitions directly, in FP64; they are pinned to those kernels, compiled
+from their sources and driven on packed panels by oracle/ref_blas3.c
+(tests/test_oracle_blas3.py: every side/uplo/trans/diag variant agrees to
+rounding), and the fixtures in tests/golden/blas3.npz hold the kernels' own
+outputs on inputs from ``generator_inputs``.
 
   trsm: side 'L': solve op(A) X = alpha B;  'R': X op(A) = alpha B
   trmm: side 'L': alpha op(A) B;            'R': alpha B op(A)
@@ -49,3 +53,18 @@ def well_conditioned_triangle(rng, na, lda, dtype):
     for i in range(na):
         A[i, i] = dtype(1.0 + rng.uniform())
     return np.asfortranarray(A)
+
+
+def generator_inputs(na, lda, m, ldb, n, dtype, seed):
+    """Inputs from the portable counter-based generator (bit-identical on x86-64
+    and aarch64): a well-conditioned triangle source A (lda x na; diagonal in
+    [1, 2), off-diagonal U[-1,1)/na) and B (ldb x n, U[-1,1))."""
+    import oracle
+
+    A = oracle.uniform((lda, na), np.float64, seed, 0) / max(na, 1)
+    d = oracle.uniform((na,), np.float64, seed, 1)
+    for i in range(na):
+        A[i, i] = 1.5 + 0.5 * d[i]
+    B = oracle.uniform((ldb, n), np.float64, seed, 2)
+    return np.asfortranarray(A.astype(dtype)), np.asfortranarray(B.astype(dtype))
+

@@ -43,3 +43,38 @@ if [ -n "$REF" ] && [ -f "$CK/zgemm_kernel_4x2_haswell.c" ] && [ "$(uname -m)" =
   $cc -O2 -fopenmp -fPIC -shared -fvisibility=hidden -o "$HERE/_ref/libcplx.so" "$HERE/ref_cplx.c" \
       "$HERE"/_ref/obj/z_*.o "$HERE"/_ref/obj/c_*.o "$HERE/_ref/obj/z3m.o" "$HERE/_ref/obj/c3m.o"
 fi
+if [ -n "$REF" ] && [ -f "$CK/TRSM_KERNEL_LN_simplified.c" ] && [ "$(uname -m)" = "x86_64" ]; then
+  # The reference's TRSM and TRMM kernels behind oracle/ref_blas3.c.  The
+  # stand-in common.h gives BLASLONG and, for the TRSM kernels, a prototype of
+  # the GEMM kernel they call (GEMM_KERNEL_N, set per precision below).
+  B3="$HERE/_ref/include3"
+  mkdir -p "$B3" "$HERE/_ref/obj3"
+  printf '%s\n' '#include <stdint.h>' 'typedef long BLASLONG;' \
+      '#if defined(GEMM_KERNEL_N) && defined(FLOAT)' \
+      'int GEMM_KERNEL_N(BLASLONG, BLASLONG, BLASLONG, FLOAT, FLOAT *, FLOAT *, FLOAT *, BLASLONG);' \
+      '#endif' > "$B3/common.h"
+  O3="$HERE/_ref/obj3"
+  OPT="-O2 -march=haswell -fPIC -fvisibility=hidden -c -I $B3"
+  # dgemm_kernel_4x4_haswell.c names its kernel KERNELFUNC (its own #define CNAME)
+  $cc $OPT -DKERNELFUNC=ref_dgemm_kernel_4x4 "$CK/dgemm_kernel_4x4_haswell.c" -o "$O3/dgemm44.o"
+  $cc $OPT -DCNAME=ref_sgemm_kernel_8x4 "$CK/sgemm_kernel_8x4_haswell.c" -o "$O3/sgemm84.o"
+  for v in LN LT RN RT; do
+    lc=$(echo "$v" | tr 'A-Z' 'a-z')
+    $cc $OPT -DFLOAT=double -DGEMM_UNROLL_M=4 -DGEMM_UNROLL_N=4 \
+        -DGEMM_KERNEL_N=ref_dgemm_kernel_long -DCNAME=ref_dtrsm_kernel_"$lc" \
+        "$CK/TRSM_KERNEL_${v}_simplified.c" -o "$O3/dtrsm_$lc.o"
+    $cc $OPT -DFLOAT=float -DGEMM_KERNEL_N=ref_sgemm_kernel_8x4 -DCNAME=ref_strsm_kernel_"$lc" \
+        "$CK/strsm_kernel_8x4_haswell_$v.c" -o "$O3/strsm_$lc.o"
+  done
+  # TRMM variants by the kernel's LEFT / TRANSA macros (trmm_kernel_4x8_simplified.c:4-29)
+  for v in ln:-DLEFT lt:-DLEFT:-DTRANSA rn: rt:-DTRANSA; do
+    lc=${v%%:*}
+    fl=$(echo "${v#*:}" | tr ':' ' ')
+    for p in d:double s:float; do
+      $cc $OPT -DFLOAT="${p#*:}" $fl -DCNAME=ref_"${p%%:*}"trmm_kernel_"$lc" \
+          "$CK/trmm_kernel_4x8_simplified.c" -o "$O3/${p%%:*}trmm_$lc.o"
+    done
+  done
+  $cc -O2 -fPIC -shared -fvisibility=hidden -o "$HERE/_ref/libblas3.so" "$HERE/ref_blas3.c" \
+      "$O3"/*.o
+fi
