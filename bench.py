@@ -430,9 +430,7 @@ def run_ours(args, torch, rank, world):
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": m * n * esz,
                "ms_per_step": round(dt * 1e3, 3), "api": "gb300_host_%s" %
                {"bf16x": "sgemm_bf16x", "ozaki": "dgemm_ozaki", "crt": "dgemm_ozaki2"}[form],
-               "transfer": "pinned host buffers; the split/slice kernels read A and B and the "
-                           "GEMM epilogue reads and writes C in host memory over the coherent "
-                           "CPU-GPU link (bytes above cross it once per step)"}
+               "transfer": transfer_note(form)}
     except StopIteration:
         pass
     except Exception as ex:  # noqa: BLE001
@@ -904,6 +902,16 @@ def run_grouped(args, torch, rank, world):
     if rank == 0:
         line["cpu_baseline"] = {"value": None, "skipped": "grouped workload"}
         print(json.dumps(line), flush=True)
+
+
+def transfer_note(form):
+    """How the host-pointer call moves the step's bytes over the CPU-GPU link."""
+    if form == "bf16x":
+        return ("pinned host buffers; A and B are copied to HBM in row / column parts by the copy "
+                "engines while earlier parts are split and their C blocks multiplied; the GEMM "
+                "epilogue reads and writes C in host memory (bytes above cross the link once)")
+    return ("pinned host buffers; A and B are copied to HBM, C is read and written in host memory "
+            "by the epilogue or staged in HBM beside the prepare (bytes above cross the link once)")
 
 
 def traffic_from_profile(workload, form_name):

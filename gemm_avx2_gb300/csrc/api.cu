@@ -71,6 +71,11 @@ struct DeviceState {
   cudaStream_t stage_stream = nullptr;
   cudaStream_t side_stream = nullptr;          // C staging beside the split forms' prepare
   cudaEvent_t ev_start = nullptr, ev_c = nullptr;
+  cudaStream_t copy_stream = nullptr;          // operand parts of the pipelined host path
+  cudaStream_t out_stream = nullptr;           // its finished C blocks
+  cudaStream_t prep_stream = nullptr;          // its operand splits
+  cudaStream_t block_stream = nullptr;         // its second stream of C blocks
+  std::vector<cudaEvent_t> part_ev;            // one per operand part
   std::mutex mu;  // guards ws and staging (one host-pointer call at a time per device)
 };
 static constexpr int kMaxDevices = 64;
@@ -124,16 +129,8 @@ void *cached_workspace(DeviceState *s, cudaStream_t st, size_t need) {
 }
 
 // ---------------------------------------------------------------- host-pointer staging
-// True when kernels may dereference these host pointers directly: the device
-// reads pageable memory through the host's page tables (coherent CPU-GPU
-// systems such as Grace + GB300), or every pointer is page-locked / registered.
-static bool host_direct_ok(const void *a, const void *b, const void *c) {
-  int dev = 0, pageable = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return false;
-  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) ==
-          cudaSuccess &&
-      pageable == 1)
-    return true;
+// True when every non-null pointer is page-locked (or registered) host memory.
+static bool host_pinned(const void *a, const void *b, const void *c) {
   for (const void *p : {a, b, c}) {
     if (!p) continue;
     cudaPointerAttributes at{};
@@ -144,6 +141,176 @@ static bool host_direct_ok(const void *a, const void *b, const void *c) {
     if (at.type != cudaMemoryTypeHost) return false;
   }
   return true;
+}
+
+// True when kernels may dereference these host pointers directly: the device
+// reads pageable memory through the host's page tables (coherent CPU-GPU
+// systems such as Grace + GB300), or every pointer is page-locked / registered.
+static bool host_direct_ok(const void *a, const void *b, const void *c) {
+  int dev = 0, pageable = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) ==
+          cudaSuccess &&
+      pageable == 1)
+    return true;
+  return host_pinned(a, b, c);
+}
+
+// Operand parts of the pipelined host path (GB300_TUNE_HOST_PARTS): 0 =
+// by shape, 1 = no pipeline, P = P row parts of op(A) and P column parts of
+// op(B).
+static int g_host_parts = 0;
+static int host_parts_for(int R, int k, bool pinned) {
+  if (g_host_parts) return g_host_parts;
+  // four parts of at least 1024 rows / columns once the operands are large
+  // enough for the link to matter: measured best of 1-6 parts at SGEMM TN
+  // 8192^3 (5.04 ms a call against 5.47 unpipelined) and 16384^3 (23.5 ms
+  // against 30.4).  Pageable memory is moved by SM copies, which compete
+  // with the GEMM for SMs (slower pipelined): no pipeline by default.
+  return pinned && R >= 4096 && k >= 1024 ? 4 : 1;
+}
+
+// Boundaries of `parts` parts of [0, R), each starting on a multiple of align.
+static std::vector<int> part_bounds(int R, int parts, int align) {
+  std::vector<int> b{0};
+  const int64_t step = ((int64_t)(R + parts - 1) / parts + align - 1) / align * align;
+  for (int64_t x = step; x < R; x += step) b.push_back((int)x);
+  b.push_back(R);
+  return b;
+}
+
+// Pipelined host-pointer call of the FP32 split form.  op(A) goes in row
+// parts and op(B) in column parts; a copy stream moves them to HBM in the
+// order A0 B0 A1 B1 ... (with B part j, the columns of C it covers), and the
+// compute stream prepares each part once it has arrived and
+// runs every C block (i, j) into HBM as soon as both of its parts are
+// prepared; an output stream copies each finished block back.  So the link
+// transfers (about 210 GB/s one way, 320 GB/s both ways together: the bound
+// of this path) overlap the GEMMs of other blocks.  The splits run on a
+// stream of their own and the blocks alternate between two streams, so one
+// block's partial last wave of tiles overlaps the next block.  The epilogues stay in
+// HBM: writing C over the link from the epilogue slowed the blocks 1.5-3x
+// while the operand copies ran.  The results equal the whole-problem call's
+// bit for bit: the exponents are per row / column over all of K, and every C
+// element's K order is the same.  Caller holds s->mu; st is s->stage_stream.
+static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char tb, int m, int n,
+                                int k, float alpha, const float *a, int lda, const float *b,
+                                int ldb, float beta, float *c, int ldc, int prm, bool ce) {
+  const bool an = notrans(ta), bn = notrans(tb);
+  const int arows = an ? m : k, acols = an ? k : m;
+  const int brows = bn ? k : n, bcols = bn ? n : k;
+  const std::vector<int> rb = part_bounds(m, host_parts_for(m, k, ce), kSplitBM);
+  const std::vector<int> cb = part_bounds(n, host_parts_for(n, k, ce), kBf16xBN);
+  const int P = (int)rb.size() - 1, Q = (int)cb.size() - 1;
+  auto up = [](int r) { return ((r > 1 ? r : 1) + 3) / 4 * 4; };
+  const int ulda = up(arows), uldb = up(brows), uldc = up(m);
+  if (!grow(&s->stage[0], &s->stage_bytes[0], (size_t)ulda * acols * sizeof(float) + 16) ||
+      !grow(&s->stage[1], &s->stage_bytes[1], (size_t)uldb * bcols * sizeof(float) + 16) ||
+      !grow(&s->stage[2], &s->stage_bytes[2], (size_t)uldc * n * sizeof(float) + 16))
+    return GB300_ERR_NOMEM;
+  float *dA = static_cast<float *>(s->stage[0]), *dB = static_cast<float *>(s->stage[1]);
+  float *dC = static_cast<float *>(s->stage[2]);
+  for (cudaStream_t *q : {&s->copy_stream, &s->out_stream, &s->prep_stream, &s->block_stream})
+    if (!*q && cudaStreamCreateWithFlags(q, cudaStreamNonBlocking) != cudaSuccess)
+      return GB300_ERR_CUDA;
+  while ((int)s->part_ev.size() < 1 + 2 * (P + Q) + P * Q) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return GB300_ERR_CUDA;
+    s->part_ev.push_back(e);
+  }
+  const size_t wneed = split_workspace_bytes(0, m, n, k, prm);
+  void *ws = wneed ? cached_workspace(s, st, wneed) : nullptr;
+  if (!ws) return GB300_ERR_NOMEM;
+  cudaStream_t cs = s->copy_stream, os = s->out_stream, ps = s->prep_stream;
+  const cudaStream_t bs[2] = {st, s->block_stream};
+  // copy engines for page-locked memory, else SM copies (the device reads the
+  // host memory); one 2-D copy per part or block (w elements x cols)
+  auto copy = [&](float *dst, int dp, const float *src, int sp, int w, int cols,
+                  cudaMemcpyKind kind, cudaStream_t q) {
+    if (ce)
+      return cudaMemcpy2DAsync(dst, (size_t)dp * sizeof(float), src, (size_t)sp * sizeof(float),
+                               (size_t)w * sizeof(float), cols, kind, q) == cudaSuccess;
+    return copy_2d(dst, (size_t)dp * sizeof(float), src, (size_t)sp * sizeof(float),
+                   (size_t)w * sizeof(float), cols, q) == GB300_OK;
+  };
+  const cudaMemcpyKind h2d = cudaMemcpyHostToDevice, d2h = cudaMemcpyDeviceToHost;
+  // arrival of the parts in HBM, their splits done, the blocks done
+  cudaEvent_t *evA = s->part_ev.data() + 1, *evB = evA + P, *evPA = evB + Q, *evPB = evPA + P;
+  cudaEvent_t *evC = evPB + Q;
+  // the side streams start after the work already queued on st (buffer reuse)
+  bool ok = cudaEventRecord(s->part_ev[0], st) == cudaSuccess;
+  for (cudaStream_t q : {cs, os, ps, bs[1]})
+    ok = ok && cudaStreamWaitEvent(q, s->part_ev[0], 0) == cudaSuccess;
+  for (int sh = 0; ok && sh < (P > Q ? P : Q); ++sh) {
+    if (sh < P) {  // op(A) rows [r0, r1): rows of A, or columns of A when transposed
+      const int r0 = rb[sh], h = rb[sh + 1] - r0;
+      ok = (an ? copy(dA + r0, ulda, a + r0, lda, h, k, h2d, cs)
+               : copy(dA + (int64_t)r0 * ulda, ulda, a + (int64_t)r0 * lda, lda, k, h, h2d, cs)) &&
+           cudaEventRecord(evA[sh], cs) == cudaSuccess;
+    }
+    if (ok && sh < Q) {  // op(B) columns [c0, c1), and those columns of C (read also when
+                         // beta == 0: C * 0 keeps the NaN / Inf of C, as C_MULT_BETA does)
+      const int c0 = cb[sh], w = cb[sh + 1] - c0;
+      ok = (bn ? copy(dB + (int64_t)c0 * uldb, uldb, b + (int64_t)c0 * ldb, ldb, k, w, h2d, cs)
+               : copy(dB + c0, uldb, b + c0, ldb, w, k, h2d, cs)) &&
+           copy(dC + (int64_t)c0 * uldc, uldc, c + (int64_t)c0 * ldc, ldc, m, w, h2d, cs) &&
+           cudaEventRecord(evB[sh], cs) == cudaSuccess;
+    }
+  }
+  int rc = ok ? GB300_OK : GB300_ERR_CUDA;
+  // the splits, each once its part has arrived (all enqueued before the
+  // blocks wait on their events)
+  for (int sh = 0; rc == GB300_OK && sh < (P > Q ? P : Q); ++sh) {
+    if (sh < P) {
+      rc = cudaStreamWaitEvent(ps, evA[sh], 0) == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+      if (rc == GB300_OK)
+        rc = split_sgemm_prepare_part(0, ta, m, n, k, dA, ulda, rb[sh], rb[sh + 1] - rb[sh], prm,
+                                      ws, wneed, ps);
+      if (rc == GB300_OK && cudaEventRecord(evPA[sh], ps) != cudaSuccess) rc = GB300_ERR_CUDA;
+    }
+    if (rc == GB300_OK && sh < Q) {
+      rc = cudaStreamWaitEvent(ps, evB[sh], 0) == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+      if (rc == GB300_OK)
+        rc = split_sgemm_prepare_part(1, tb, m, n, k, dB, uldb, cb[sh], cb[sh + 1] - cb[sh], prm,
+                                      ws, wneed, ps);
+      if (rc == GB300_OK && cudaEventRecord(evPB[sh], ps) != cudaSuccess) rc = GB300_ERR_CUDA;
+    }
+  }
+  int nblk = 0;
+  auto block = [&](int i, int j) {
+    const int i0 = rb[i], h = rb[i + 1] - i0, j0 = cb[j], w = cb[j + 1] - j0;
+    const cudaStream_t q = bs[nblk & 1];
+    if (cudaStreamWaitEvent(q, evPA[i], 0) != cudaSuccess ||
+        cudaStreamWaitEvent(q, evPB[j], 0) != cudaSuccess)
+      return (int)GB300_ERR_CUDA;
+    int r = split_sgemm_run_block(m, n, k, i0, h, j0, w, alpha, beta, dC, uldc, prm, ws, wneed,
+                                  q, s->err);
+    // the finished block goes back while the next ones compute
+    cudaEvent_t e = evC[nblk++];
+    if (r == GB300_OK &&
+        (cudaEventRecord(e, q) != cudaSuccess || cudaStreamWaitEvent(os, e, 0) != cudaSuccess ||
+         !copy(c + i0 + (int64_t)j0 * ldc, ldc, dC + i0 + (int64_t)j0 * uldc, uldc, h, w, d2h,
+               os)))
+      r = GB300_ERR_CUDA;
+    return r;
+  };
+  // the blocks in the order their second part arrives
+  for (int sh = 0; rc == GB300_OK && sh < (P > Q ? P : Q); ++sh) {
+    if (sh < P)
+      for (int j = 0; rc == GB300_OK && j < Q && j <= sh; ++j) rc = block(sh, j);
+    if (sh < Q)
+      for (int i = 0; rc == GB300_OK && i < P && i < sh; ++i) rc = block(i, sh);
+  }
+  cudaError_t e = cudaSuccess;
+  for (cudaStream_t q : {cs, ps, bs[0], bs[1], os}) {
+    const cudaError_t eq = cudaStreamSynchronize(q);
+    if (e == cudaSuccess) e = eq;
+  }
+  if (rc != GB300_OK) return rc;
+  if (e != cudaSuccess) return GB300_ERR_CUDA;
+  unsigned word = 0;
+  cudaMemcpy(&word, s->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  return word ? GB300_ERR_TIMEOUT : GB300_OK;
 }
 
 // form: 0 = plain kernel; 1 = BF16xP split (FP32, param = products);
@@ -183,6 +350,13 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
     if (form == 1 && prm == 0) {
       int ch = 0;
       bf16x_resolve(m, n, k, &prm, &ch);
+    }
+    if constexpr (sizeof(T) == 4) {
+      const bool pinned = host_pinned(a, b, c);
+      if (form == 1 && need_ab &&
+          (host_parts_for(m, k, pinned) > 1 || host_parts_for(n, k, pinned) > 1))
+        return host_split_pipelined(s, st, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
+                                    param, pinned);
     }
     const bool two_pass = form >= 2 || prm == kFp16x3;
     const int epl = 16 / (int)sizeof(T);
@@ -1026,6 +1200,10 @@ GB300_API int gb300_tune_param(int param, int value) {
     case GB300_TUNE_GRAPH_BRANCHES:
       if (value < 0 || value > kGraphBranches) return GB300_ERR_ARG;
       g_graph_branches = value ? value : kDefaultGraphBranches;
+      return GB300_OK;
+    case GB300_TUNE_HOST_PARTS:
+      if (value < 0 || value > 8) return GB300_ERR_ARG;
+      g_host_parts = value;
       return GB300_OK;
     default:
       return GB300_ERR_ARG;

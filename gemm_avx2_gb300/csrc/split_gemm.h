@@ -81,6 +81,17 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
 int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int ldc, int products,
                     const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err,
                     int chunk0 = 0);
+// Parts of the same two phases for a pipelined call, in the whole m x n x k
+// problem's workspace.  prepare_part: rows [r0, r0 + rows) of op(A) (z = 0,
+// X = A, r0 a multiple of 128) or columns of op(B) (z = 1, X = B, r0 a
+// multiple of 256).  run_block: C rows [i0, i0 + h) x columns [j0, j0 + w)
+// (C = the whole C) from prepared parts covering them.  Same results bit for
+// bit as the whole-problem calls.
+int split_sgemm_prepare_part(int z, char t, int m, int n, int k, const float *X, int ldx, int r0,
+                             int rows, int products, void *ws, size_t ws_bytes, cudaStream_t st);
+int split_sgemm_run_block(int m, int n, int k, int i0, int h, int j0, int w, float alpha,
+                          float beta, float *C, int ldc, int products, const void *ws,
+                          size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0 = 0);
 int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
                   int ldb, int slices, void *ws, size_t ws_bytes, cudaStream_t st);
 int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int slices,

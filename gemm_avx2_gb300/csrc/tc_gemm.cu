@@ -93,6 +93,7 @@ struct SplitArgs {
   __nv_bfloat16 *out0, *out1;
   int K, Kp, nterms;
   int64_t ldo;
+  int zbase;  // operand of blockIdx.z = 0 (1: a launch over op(B) alone)
 };
 
 // out: Rp x (nseg * Kp) row-major 16-bit terms (row stride ldo = nseg*Kp
@@ -104,7 +105,7 @@ struct SplitArgs {
 //                ex[] (Rp entries); a row whose max is not finite is all NaN.
 template <bool F16>
 __global__ void __launch_bounds__(256) split_bf16_kernel(const __grid_constant__ SplitArgs p) {
-  const int z = blockIdx.z;
+  const int z = blockIdx.z + p.zbase;
   const float *__restrict__ X = z ? p.X1 : p.X0;
   const int ld = z ? p.ld1 : p.ld0, R = z ? p.R1 : p.R0, kcontig = z ? p.kc1 : p.kc0;
   const int Rp = z ? p.Rp1 : p.Rp0, K = p.K, Kp = p.Kp, nterms = p.nterms;
@@ -185,11 +186,13 @@ template <> struct AbsBits<float> {
 // Both operands in one launch: blockIdx.z = 0 reads the rows of op(A) into
 // amax[0, Mp), z = 1 the columns of op(B) into amax[Mp, Mp + Np).  The last
 // CTA to finish (a counter the caller zeroes with amax) writes the exponents
-// of all Mp + Np entries, so no separate exponent launch is needed.
+// of entries [first, first + total), so no separate exponent launch is
+// needed.  A launch over one operand part (zbase = its operand, gridDim.z = 1)
+// gets amax / ex offset to the part's first row.
 template <typename T>
 struct AbsmaxArgs {
   const T *X0, *X1;
-  int ld0, ld1, R0, R1, kc0, kc1, span0, span1, K, Mp, total;
+  int ld0, ld1, R0, R1, kc0, kc1, span0, span1, K, Mp, first, total, zbase;
   typename AbsBits<T>::U *amax;
   int *ex;
   unsigned *counter;
@@ -199,7 +202,7 @@ struct AbsmaxArgs {
 template <typename T>
 __global__ void __launch_bounds__(256) row_absmax_kernel(const __grid_constant__ AbsmaxArgs<T> p) {
   using U = typename AbsBits<T>::U;
-  const int z = blockIdx.z;
+  const int z = blockIdx.z + p.zbase;
   const T *X = z ? p.X1 : p.X0;
   const int ld = z ? p.ld1 : p.ld0, R = z ? p.R1 : p.R0, span = z ? p.span1 : p.span0;
   const bool kcontig = (z ? p.kc1 : p.kc0) != 0;
@@ -244,7 +247,8 @@ __global__ void __launch_bounds__(256) row_absmax_kernel(const __grid_constant__
   __syncthreads();
   if (last) {
     __threadfence();
-    for (int i = threadIdx.x; i < p.total; i += blockDim.x) p.ex[i] = AbsBits<T>::exponent(__ldcg(&p.amax[i]));
+    for (int i = p.first + threadIdx.x; i < p.first + p.total; i += blockDim.x)
+      p.ex[i] = AbsBits<T>::exponent(__ldcg(&p.amax[i]));
   }
 }
 
@@ -1021,6 +1025,17 @@ static int g_bf16x_chunk = 0;
 int bf16x_chunk_kblocks() { return g_bf16x_chunk; }
 void set_bf16x_chunk_kblocks(int c) { g_bf16x_chunk = c < 0 ? 0 : c; }
 
+// Grid of the max pass over one operand (R rows of op(X), k long): one warp
+// (k-contiguous rows) or one thread (row-contiguous columns) per row and k
+// range; the k range doubles until the grid's y extent fits.
+static void absmax_grid(bool kc, int R, int k, int *span, unsigned *gx, unsigned *gy) {
+  int64_t sp = kc ? kAmaxSpanK : kAmaxSpanR;
+  while ((k + sp - 1) / sp > 65535) sp *= 2;
+  *span = (int)sp;
+  *gx = (unsigned)(kc ? (R + 7) / 8 : (R + 255) / 256);
+  *gy = (unsigned)((k + sp - 1) / sp);
+}
+
 // Per-row max |.| of op(A) and per-column max |.| of op(B), then their scale
 // exponents.  amax / ex hold Mp entries for the rows of op(A), then Np for
 // the columns of op(B); padding entries get exponent 0.  The completion
@@ -1040,21 +1055,45 @@ static int scale_exponents(char ta, char tb, int m, int n, int k, const T *A, in
   p.X1 = B; p.ld1 = ldb; p.R1 = n; p.kc1 = bn ? 1 : 0;
   unsigned gx = 1, gy = 1;
   for (int z = 0; z < 2; ++z) {
-    const bool kc = (z ? p.kc1 : p.kc0) != 0;
-    const int R = z ? p.R1 : p.R0;
-    int64_t span = kc ? kAmaxSpanK : kAmaxSpanR;
-    while ((k + span - 1) / span > 65535) span *= 2;
-    (z ? p.span1 : p.span0) = (int)span;
-    const unsigned x = (unsigned)(kc ? (R + 7) / 8 : (R + 255) / 256);
-    const unsigned y = (unsigned)((k + span - 1) / span);
+    unsigned x, y;
+    absmax_grid((z ? p.kc1 : p.kc0) != 0, z ? n : m, k, z ? &p.span1 : &p.span0, &x, &y);
     gx = x > gx ? x : gx;
     gy = y > gy ? y : gy;
   }
-  p.K = k; p.Mp = (int)Mp; p.total = (int)(Mp + Np);
+  p.K = k; p.Mp = (int)Mp; p.first = 0; p.total = (int)(Mp + Np); p.zbase = 0;
   p.amax = amax; p.ex = ex;
   p.counter = reinterpret_cast<unsigned *>(amax + Mp + Np);
   p.nblocks = gx * gy * 2;
   row_absmax_kernel<T><<<dim3(gx, gy, 2), 256, 0, st>>>(p);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+// The same over one operand part: rows [r0, r0 + R) of op(A) (z = 0) or
+// columns of op(B) (z = 1), X pointing at the part's first row; the entries
+// [r0, r0 + Rpart) of the operand's amax / ex range are written.  The counter
+// (after all Mp + Np entries) is zeroed for this launch: parts on one stream
+// run one after another.
+template <typename T>
+static int scale_exponents_part(int z, bool kc, int R, int Rpart, int r0, int k, const T *X,
+                                int ldx, typename AbsBits<T>::U *amax, int *ex, int64_t Mp,
+                                int64_t Np, cudaStream_t st) {
+  using U = typename AbsBits<T>::U;
+  U *mine = amax + (z ? Mp : 0) + r0;
+  unsigned *counter = reinterpret_cast<unsigned *>(amax + Mp + Np);
+  if (cudaMemsetAsync(mine, 0, (size_t)Rpart * sizeof(U), st) != cudaSuccess ||
+      cudaMemsetAsync(counter, 0, sizeof(unsigned), st) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  AbsmaxArgs<T> p;
+  p.X0 = p.X1 = X; p.ld0 = p.ld1 = ldx; p.R0 = p.R1 = R; p.kc0 = p.kc1 = kc ? 1 : 0;
+  unsigned gx, gy;
+  absmax_grid(kc, R, k, &p.span0, &gx, &gy);
+  p.span1 = p.span0;
+  p.K = k; p.Mp = (int)Mp; p.zbase = z;
+  p.amax = amax + r0; p.ex = ex + r0;  // z = 1 adds Mp in the kernel
+  p.first = z ? (int)Mp : 0; p.total = Rpart;
+  p.counter = counter;
+  p.nblocks = gx * gy;
+  row_absmax_kernel<T><<<dim3(gx, gy, 1), 256, 0, st>>>(p);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
@@ -1113,11 +1152,54 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
   sa.out0 = L.Ap; sa.out1 = L.Bp;
   sa.K = k; sa.Kp = (int)L.Kp; sa.nterms = products == 6 ? 3 : 2;
   sa.ldo = L.Kld;
+  sa.zbase = 0;
   const unsigned rb = row_blocks(L.Mp > L.Np ? L.Mp : L.Np);
   const dim3 grid((unsigned)(L.Kp / 64), rb, 2);
   if (f16) {
     const int rc = scale_exponents<float>(ta, tb, m, n, k, A, lda, B, ldb, L.amax, L.ex, L.Mp,
                                           L.Np, st);
+    if (rc != GB300_OK) return rc;
+    split_bf16_kernel<true><<<grid, 256, 0, st>>>(sa);
+  } else {
+    split_bf16_kernel<false><<<grid, 256, 0, st>>>(sa);
+  }
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int split_sgemm_prepare_part(int z, char t, int m, int n, int k, const float *X, int ldx, int r0,
+                             int rows, int products, void *ws, size_t ws_bytes, cudaStream_t st) {
+  if (products == 0) {
+    int c = 0;
+    bf16x_resolve(m, n, k, &products, &c);
+  }
+  const int align = z ? kBf16xBN : kSplitBM, R = z ? n : m;
+  if (!split_products_ok(products) || m <= 0 || n <= 0 || k <= 0 || r0 < 0 || rows <= 0 ||
+      r0 % align || r0 + rows > R || ldx < 1)
+    return GB300_ERR_ARG;
+  const size_t need = split_workspace_bytes(0, m, n, k, products);
+  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
+  const Bf16xLayout L = bf16x_layout(m, n, k, products, ws);
+  // op(A) rows are k-contiguous when A is transposed, op(B) columns when B is not
+  const bool kc = z ? notrans(t) : !notrans(t);
+  const float *Xp = kc ? X + (int64_t)r0 * ldx : X + r0;
+  const int Rpart = (int)round_up(rows, align);
+  const bool f16 = products == kFp16x3;
+  SplitArgs sa;
+  sa.X0 = sa.X1 = Xp; sa.ld0 = sa.ld1 = ldx; sa.R0 = sa.R1 = rows;
+  sa.kc0 = sa.kc1 = kc ? 1 : 0; sa.Rp0 = sa.Rp1 = Rpart;
+  sa.seg0 = seg_map(f16 ? 3 : products, true);
+  sa.seg1 = seg_map(f16 ? 3 : products, false);
+  int *ex = f16 ? L.ex + (z ? L.Mp : 0) + r0 : nullptr;
+  sa.ex0 = sa.ex1 = ex;
+  __nv_bfloat16 *out = (z ? L.Bp : L.Ap) + (int64_t)r0 * L.Kld;
+  sa.out0 = sa.out1 = out;
+  sa.K = k; sa.Kp = (int)L.Kp; sa.nterms = products == 6 ? 3 : 2;
+  sa.ldo = L.Kld;
+  sa.zbase = z;
+  const dim3 grid((unsigned)(L.Kp / 64), row_blocks(Rpart), 1);
+  if (f16) {
+    const int rc = scale_exponents_part<float>(z, kc, rows, Rpart, r0, k, Xp, ldx, L.amax, L.ex,
+                                               L.Mp, L.Np, st);
     if (rc != GB300_OK) return rc;
     split_bf16_kernel<true><<<grid, 256, 0, st>>>(sa);
   } else {
@@ -1198,15 +1280,18 @@ static bool use_pair_mma(int m, int n, int k) {
   return v == 1;
 }
 
+// L: the layout of the rows / columns this launch covers; (tm, tn, k): the
+// problem whose shape class picks the cluster mode.
 template <bool F16, int BN>
-static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, int k, cudaStream_t st) {
+static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, int tm, int tn, int k,
+                        cudaStream_t st) {
   const bool mc = L.Mp / kSplitBM >= 2;  // 2-CTA clusters on row-tile pairs
   CUtensorMap tA{}, tB{};
   if (!encode_2d(&tA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
       !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, mc ? BN / 2 : BN, true))
     return GB300_ERR_CUDA;
   p.tiles_n = (p.n + BN - 1) / BN;
-  if (mc && use_pair_mma(p.m, p.n, k))
+  if (mc && use_pair_mma(tm, tn, k))
     return persistent_launch<Bf16xParams>(bf16x_gemm_kernel<0, F16, BN>,
                                           bf16x_gemm_kernel<2, F16, BN>, kBxThreads,
                                           ClusterTile<2, BN>::kSmem, tA, tB, p, p.tiles_m,
@@ -1219,22 +1304,38 @@ static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, int k, cudaStream_t
 
 int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int ldc, int products,
                     const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0) {
+  return split_sgemm_run_block(m, n, k, 0, m, 0, n, alpha, beta, C, ldc, products, ws, ws_bytes,
+                               st, err, chunk0);
+}
+
+int split_sgemm_run_block(int m, int n, int k, int i0, int h, int j0, int w, float alpha,
+                          float beta, float *C, int ldc, int products, const void *ws,
+                          size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0) {
   if (products == 0) {
     int c = 0;
     bf16x_resolve(m, n, k, &products, &c);
     if (chunk0 == 0) chunk0 = c;
   }
-  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || !split_products_ok(products))
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || !split_products_ok(products) ||
+      i0 < 0 || j0 < 0 || h < 0 || w < 0 || i0 % kSplitBM || j0 % kBf16xBN || i0 + h > m ||
+      j0 + w > n)
     return GB300_ERR_ARG;
-  if (m == 0 || n == 0) return GB300_OK;
+  if (h == 0 || w == 0) return GB300_OK;
+  float *Cb = C + i0 + (int64_t)j0 * ldc;
   if (alpha == 0.0f || k == 0)
-    return plain_sgemm('N', 'N', m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc,
-                       st, err);
+    return plain_sgemm('N', 'N', h, w, 0, alpha, nullptr, h > 1 ? h : 1, nullptr, 1, beta, Cb,
+                       ldc, st, err);
   const size_t need = split_workspace_bytes(0, m, n, k, products);
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
-  const Bf16xLayout L = bf16x_layout(m, n, k, products, const_cast<void *>(ws));
+  const Bf16xLayout Lf = bf16x_layout(m, n, k, products, const_cast<void *>(ws));
+  // the block's rows of A' and columns of B' (tile-aligned offsets)
+  Bf16xLayout L = Lf;
+  L.Ap = Lf.Ap + (int64_t)i0 * Lf.Kld;
+  L.Bp = Lf.Bp + (int64_t)j0 * Lf.Kld;
+  L.Mp = round_up(h, kSplitBM);
+  L.Np = round_up(w, kBf16xBN);
   Bf16xParams p;
-  p.m = m; p.n = n;
+  p.m = h; p.n = w;
   p.tiles_m = (int)(L.Mp / kSplitBM);
   p.tiles_n = 0;  // set by the launch for its tile width
   p.kblocks = (int)(L.Kld / kSplitBK);
@@ -1262,7 +1363,7 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
       p.run_end2 = 3 * skb; p.run_chunk2 = c0;
     }
   }
-  p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.err = err;
+  p.alpha = alpha; p.beta = beta; p.C = Cb; p.ldc = ldc; p.err = err;
   const bool f16 = products == kFp16x3;
   p.rescale_chunk = -1;
   p.rescale = 1.0f;
@@ -1272,13 +1373,15 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
     // chunks come first, so the running sums are scaled once when run 1 starts
     p.rescale_chunk = (p.run_end0 + p.run_chunk0 - 1) / p.run_chunk0;
     p.rescale = 1.0f / 2048.0f;
-    p.expA = L.ex;
-    p.expB = L.ex + L.Mp;
+    p.expA = Lf.ex + i0;
+    p.expB = Lf.ex + Lf.Mp + j0;
   }
   const int bn = split_tile_n(0, m, n, k);
   if (f16)
-    return bn == 128 ? bf16x_launch<true, 128>(L, p, k, st) : bf16x_launch<true, 256>(L, p, k, st);
-  return bn == 128 ? bf16x_launch<false, 128>(L, p, k, st) : bf16x_launch<false, 256>(L, p, k, st);
+    return bn == 128 ? bf16x_launch<true, 128>(L, p, m, n, k, st)
+                     : bf16x_launch<true, 256>(L, p, m, n, k, st);
+  return bn == 128 ? bf16x_launch<false, 128>(L, p, m, n, k, st)
+                   : bf16x_launch<false, 256>(L, p, m, n, k, st);
 }
 
 int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,

@@ -391,12 +391,22 @@ void gb300_tune_cache_clear(void);
  *   256-row tile, each holding half of the B tile), 2 = one MMA issuer per
  *   CTA with the B tile multicast to both CTAs of the cluster; 0 restores
  *   the default (the tuned mode of the shape class, else multicast).  Both
- *   give the same results bit for bit. */
+ *   give the same results bit for bit.
+ *   GB300_TUNE_HOST_PARTS: operand parts (1..8) of the pipelined host-pointer
+ *   path of the FP32 split form (gb300_host_sgemm_bf16x, the drop-in with
+ *   GB300_DROPIN_FORM=split): op(A) in that many row parts and op(B) in that
+ *   many column parts, copied to HBM on a copy stream while the compute
+ *   stream prepares the parts that have arrived and multiplies the C blocks
+ *   whose parts are ready, and C blocks go back as they finish.  1 turns
+ *   the pipeline off; 0 restores the choice by shape (page-locked buffers: 4
+ *   parts per dimension of 4096 or more when k >= 1024; pageable: off).  The
+ *   results are the same bit for bit. */
 enum {
   GB300_TUNE_BF16X_CHUNK = 1,
   GB300_TUNE_GRAPH_BRANCHES = 2,
   GB300_TUNE_TILE_N = 3,
-  GB300_TUNE_PAIR_MMA = 4
+  GB300_TUNE_PAIR_MMA = 4,
+  GB300_TUNE_HOST_PARTS = 5
 };
 int gb300_tune_param(int param, int value);
 

@@ -214,4 +214,7 @@ def test_tuning_knobs_validate():
     assert g.tune_param(g.TUNE_GRAPH_BRANCHES, 65) == g.ERR_ARG
     assert g.tune_param(g.TUNE_GRAPH_BRANCHES, -1) == g.ERR_ARG
     assert g.tune_param(g.TUNE_GRAPH_BRANCHES, 0) == g.OK   # back to the default
+    assert g.tune_param(g.TUNE_HOST_PARTS, 8) == g.OK
+    assert g.tune_param(g.TUNE_HOST_PARTS, 9) == g.ERR_ARG
+    assert g.tune_param(g.TUNE_HOST_PARTS, 0) == g.OK
     assert g.tune_param(99, 1) == g.ERR_ARG

@@ -43,3 +43,53 @@ def test_staged_host_path_matches_device(orc, form, param, dt, size, k):
                              param) == g.OK
     assert np.array_equal(Ch[m:], C[m:])
     assert np.array_equal(Ch[:m], ref[:m])
+
+
+@pytest.fixture
+def host_parts():
+    yield lambda v: g.tune_param(g.TUNE_HOST_PARTS, v)
+    g.tune_param(g.TUNE_HOST_PARTS, 0)
+
+
+@pytest.mark.parametrize("parts", [2, 3])
+@pytest.mark.parametrize("param", [g.FP16X3, 6, 3])
+@pytest.mark.parametrize("ta,tb", [("T", "N"), ("N", "N"), ("N", "T"), ("T", "T")])
+def test_pipelined_host_sgemm_matches_device(orc, host_parts, parts, param, ta, tb):
+    """The FP32 split form with op(A) in row parts and op(B) in column parts
+    (ragged last parts, padded ld): bit for bit the device-pointer result."""
+    m, n, k = 700, 900, 300
+    ar, ac = (m, k) if ta == "N" else (k, m)
+    br, bc = (k, n) if tb == "N" else (n, k)
+    A = orc.uniform((ar + 1, ac), np.float32, 82, 0)
+    B = orc.uniform((br + 3, bc), np.float32, 82, 1)
+    C = orc.uniform((m + 2, n), np.float32, 82, 2)
+    ref = device_result("bf16x", ta, tb, m, n, k, 0.75, A, ar + 1, B, br + 3, -1.0, C, param)
+    assert host_parts(parts) == g.OK
+    Ch = C.copy(order="F")
+    assert g.host_split_gemm("bf16x", ta, tb, m, n, k, 0.75, A, ar + 1, B, br + 3, -1.0, Ch, m + 2,
+                             param) == g.OK
+    assert np.array_equal(Ch[m:], C[m:])
+    assert np.array_equal(Ch[:m], ref[:m])
+    assert g.device_error() == 0
+
+
+def test_pipelined_host_sgemm_pinned_buffers(orc, host_parts):
+    """Page-locked host buffers take the copy engines: same result bit for bit,
+    including beta = 0 with NaN and Inf in C (C * 0 propagates them, as the
+    reference's C_MULT_BETA does)."""
+    torch = torch_cuda()
+    m, n, k = 1100, 800, 1030
+    A = orc.uniform((k, m), np.float32, 83, 0)
+    B = orc.uniform((k, n), np.float32, 83, 1)
+    C = orc.uniform((m, n), np.float32, 83, 2)
+    C[5, 700] = np.nan
+    C[1000, 3] = -np.inf
+    ref = device_result("bf16x", "T", "N", m, n, k, 1.0, A, k, B, k, 0.0, C, g.FP16X3)
+    pa, pb, pc = (torch.from_numpy(x.ravel(order="F").copy()).pin_memory() for x in (A, B, C))
+    assert host_parts(4) == g.OK
+    assert g.core().gb300_host_sgemm_bf16x(b"T", b"N", m, n, k, 1.0, pa.data_ptr(), k,
+                                           pb.data_ptr(), k, 0.0, pc.data_ptr(), m,
+                                           g.FP16X3) == g.OK
+    got = pc.numpy().reshape((n, m)).T
+    assert np.isnan(got[5, 700]) and np.isnan(got[1000, 3])
+    assert np.array_equal(got, ref, equal_nan=True)
