@@ -907,9 +907,9 @@ def run_grouped(args, torch, rank, world):
 def transfer_note(form):
     """How the host-pointer call moves the step's bytes over the CPU-GPU link."""
     if form == "bf16x":
-        return ("pinned host buffers; A and B are copied to HBM in row / column parts by the copy "
-                "engines while earlier parts are split and their C blocks multiplied; the GEMM "
-                "epilogue reads and writes C in host memory (bytes above cross the link once)")
+        return ("pinned host buffers; A, B and C are copied to HBM in row / column parts by the "
+                "copy engines while earlier parts are split and their C blocks multiplied, and "
+                "each C block is copied back as it finishes (bytes above cross the link once)")
     return ("pinned host buffers; A and B are copied to HBM, C is read and written in host memory "
             "by the epilogue or staged in HBM beside the prepare (bytes above cross the link once)")
 
