@@ -389,6 +389,7 @@ TUNE_GRAPH_BRANCHES = 2
 TUNE_TILE_N = 3
 TUNE_PAIR_MMA = 4
 TUNE_HOST_PARTS = 5
+TUNE_MODULUS_SPLIT = 6
 TUNE_BF16X = 0     # autotuner kinds
 TUNE_OZAKI = 1
 TUNE_CRT = 2

@@ -1205,6 +1205,10 @@ GB300_API int gb300_tune_param(int param, int value) {
       if (value < 0 || value > 8) return GB300_ERR_ARG;
       g_host_parts = value;
       return GB300_OK;
+    case GB300_TUNE_MODULUS_SPLIT:
+      if (value < 0 || value > 2) return GB300_ERR_ARG;
+      set_modulus_split(value);
+      return GB300_OK;
     default:
       return GB300_ERR_ARG;
   }

@@ -107,6 +107,10 @@ int split_tile_override();
 // 1 = pair MMAs (cta_group::2), 2 = per-CTA MMAs with the B tile multicast.
 void set_pair_mma(int v);
 int pair_mma_override();
+// Work units of the CRT GEMM: 0 = by shape, 1 = whole tiles, 2 = one modulus
+// of one tile (the moduli are independent GEMMs).
+void set_modulus_split(int v);
+int modulus_split_override();
 // Tuned tile width (0 = none) and cluster mode (0 = none, 1 = pair MMAs,
 // 2 = multicast) of a shape class.
 int tune_tile_n(int kind, int m, int n, int k);

@@ -671,6 +671,9 @@ struct OzakiParams {
   int mods[kCrtMaxModuli];
   unsigned mods_mg[kCrtMaxModuli];  // floor(2^32 / mods[g]) for the Barrett reduction
   unsigned *err;
+  // work units per tile: the S groups in gsplit ranges (CRT form only, whose
+  // moduli are independent GEMMs; 1 in the slice form, which sums its groups)
+  int gsplit;
 };
 
 constexpr int kOzEpiWarps = 16;  // 4 per TMEM lane quarter, BN / 4 columns each
@@ -748,13 +751,21 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   // work units: tiles, or (MC) row-tile pairs whose rank-th row tile is this CTA's
   const uint32_t rank = MC ? cluster_ctarank() : 0u;
   const int pm = MC ? (p.tiles_m + 1) / 2 : p.tiles_m;
-  const int nunits = pm * p.tiles_n;
+  // units: (group range, tile), group-range major so that neighbouring units
+  // share the residue planes of their moduli in L2
+  const int ntu = pm * p.tiles_n;
+  const int nunits = ntu * p.gsplit;
   const int first = MC ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
   const int stride = MC ? (int)(gridDim.x >> 1) : (int)gridDim.x;
   auto unit_tile = [&](int u, int &tm, int &tn) {
     int um;
-    tile_coords(u, pm, p.tiles_n, MC ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
+    tile_coords(u % ntu, pm, p.tiles_n, MC ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
     tm = MC ? 2 * um + (int)rank : um;
+  };
+  auto unit_groups = [&](int u, int &g0, int &g1) {
+    const int gp = u / ntu;
+    g0 = gp * S / p.gsplit;
+    g1 = (gp + 1) * S / p.gsplit;
   };
 
   if (warp == 0) {
@@ -762,9 +773,10 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t L = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
-        int tm, tn;
+        int tm, tn, g0, g1;
         unit_tile(u, tm, tn);
-        for (int gi = 0; gi < S && ok; ++gi) {
+        unit_groups(u, g0, g1);
+        for (int gi = g0; gi < g1 && ok; ++gi) {
           int t, lo, np;
           group_of(p.mode, gi, S, t, lo, np);
           const int G = np * KB;
@@ -796,7 +808,9 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
-        for (int gi = 0; gi < S && ok; ++gi) {
+        int g0, g1;
+        unit_groups(u, g0, g1);
+        for (int gi = g0; gi < g1 && ok; ++gi) {
           int t, lo, np;
           group_of(p.mode, gi, S, t, lo, np);
           const int G = np * KB;
@@ -844,15 +858,16 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     uint32_t chunk = 0;
     bool ok = true;
     for (int u = first; u < nunits && ok; u += stride) {
-      int tm, tn;
+      int tm, tn, g0, g1;
       unit_tile(u, tm, tn);
+      unit_groups(u, g0, g1);
       const bool real = tm < p.tiles_m;  // MC: a row tile past the end writes nothing
       const int row = tm * kSplitBM + row_in_tile;          // < Mp when real
       const int col0 = tn * BN + h * kOzCols;          // first of this warp's columns
       double *res = p.res + (int64_t)col0 * p.Mp + row;      // res[j * Mp] is column col0 + j
       bool res_init = false;
       const int run_limit = p.mode ? kCrtRunChunks : kOzRunChunks;
-      for (int gi = 0; gi < S && ok; ++gi) {
+      for (int gi = g0; gi < g1 && ok; ++gi) {
         int t, lo, np;
         group_of(p.mode, gi, S, t, lo, np);
         const int G = np * KB;
@@ -1275,6 +1290,11 @@ int split_tile_override() { return g_tile_n; }
 static int g_pair_mma = 0;  // 0: none, 1: pair MMAs, 2: multicast
 void set_pair_mma(int v) { g_pair_mma = v; }
 int pair_mma_override() { return g_pair_mma; }
+// Work units of the CRT GEMM: 0 = by shape, 1 = whole tiles (all moduli),
+// 2 = one modulus of one tile.  Same results bit for bit.
+static int g_modulus_split = 0;
+void set_modulus_split(int v) { g_modulus_split = v; }
+int modulus_split_override() { return g_modulus_split; }
 static bool use_pair_mma(int m, int n, int k) {
   const int v = g_pair_mma ? g_pair_mma : tune_pair_mma(0, m, n, k);
   return v == 1;
@@ -1483,9 +1503,15 @@ static int ozaki_launch_bn(const OzakiGemmArgs &a, OzakiParams p, cudaStream_t s
       !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, mc ? BN / 2 : BN, true))
     return GB300_ERR_CUDA;
   p.tiles_n = (p.n + BN - 1) / BN;
+  // CRT form: one modulus per work unit when the tiles alone fill fewer than
+  // four waves (a 2048^2 output has 128 tiles for 152 SMs)
+  const int stride = mc ? sm_count() / 2 : sm_count();
+  const int ntu = (mc ? (p.tiles_m + 1) / 2 : p.tiles_m) * p.tiles_n;
+  const int mode = modulus_split_override();
+  p.gsplit = !p.mode || mode == 1 ? 1 : (mode == 2 || ntu < 4 * stride) ? p.S : 1;
   return persistent_launch<OzakiParams>(ozaki_gemm_kernel<false, BN>, ozaki_gemm_kernel<true, BN>,
                                         kOzThreads, TileN<BN>::kSmem, tA, tB, p, p.tiles_m,
-                                        p.tiles_n, mc, st);
+                                        p.tiles_n * p.gsplit, mc, st);
 }
 
 int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {

@@ -400,13 +400,20 @@ void gb300_tune_cache_clear(void);
  *   whose parts are ready, and C blocks go back as they finish.  1 turns
  *   the pipeline off; 0 restores the choice by shape (page-locked buffers: 4
  *   parts per dimension of 4096 or more when k >= 1024; pageable: off).  The
- *   results are the same bit for bit. */
+ *   results are the same bit for bit.
+ *   GB300_TUNE_MODULUS_SPLIT: work units of the CRT form's GEMM
+ *   (gb300_dgemm_ozaki2): 1 = whole output tiles, each CTA running all
+ *   moduli of its tile; 2 = one modulus of one tile (the moduli are
+ *   independent GEMMs, so small outputs still fill the GPU); 0 restores the
+ *   choice by shape (2 when the tiles alone fill fewer than four waves).
+ *   Same results bit for bit. */
 enum {
   GB300_TUNE_BF16X_CHUNK = 1,
   GB300_TUNE_GRAPH_BRANCHES = 2,
   GB300_TUNE_TILE_N = 3,
   GB300_TUNE_PAIR_MMA = 4,
-  GB300_TUNE_HOST_PARTS = 5
+  GB300_TUNE_HOST_PARTS = 5,
+  GB300_TUNE_MODULUS_SPLIT = 6
 };
 int gb300_tune_param(int param, int value);
 

@@ -217,4 +217,7 @@ def test_tuning_knobs_validate():
     assert g.tune_param(g.TUNE_HOST_PARTS, 8) == g.OK
     assert g.tune_param(g.TUNE_HOST_PARTS, 9) == g.ERR_ARG
     assert g.tune_param(g.TUNE_HOST_PARTS, 0) == g.OK
+    assert g.tune_param(g.TUNE_MODULUS_SPLIT, 2) == g.OK
+    assert g.tune_param(g.TUNE_MODULUS_SPLIT, 3) == g.ERR_ARG
+    assert g.tune_param(g.TUNE_MODULUS_SPLIT, 0) == g.OK
     assert g.tune_param(99, 1) == g.ERR_ARG

@@ -174,3 +174,23 @@ def test_host_path(orc):
     assert g.host_split_gemm("crt", "T", "N", m, n, k, 1.0, A, k, B, k, 0.5, Cg, m, 16) == g.OK
     model = crt.crt_gemm_model(A.T, B, 16, alpha=1.0, beta=0.5, C=C)
     assert np.array_equal(Cg, model)
+
+
+@pytest.mark.parametrize("shape", [(700, 600, 500), (2100, 1900, 300)])
+def test_modulus_split_units_bitexact(orc, shape):
+    """Whole-tile units and one-modulus units give the same result bit for bit
+    (the moduli are independent GEMMs)."""
+    m, n, k = shape
+    A = orc.spread((m, k), 59, 0, 1.0)
+    B = orc.spread((n, k), 59, 1, 1.0)
+    C = orc.uniform((m, n), np.float64, 59, 2)
+    got = {}
+    try:
+        for mode in (1, 2):
+            assert g.tune_param(g.TUNE_MODULUS_SPLIT, mode) == g.OK
+            rc, got[mode], _ = run_crt("N", "T", m, n, k, A, m, B, n, C, 15, beta=0.5)
+            assert rc == g.OK
+    finally:
+        g.tune_param(g.TUNE_MODULUS_SPLIT, 0)
+    assert np.array_equal(got[1], got[2])
+    assert g.device_error() == 0
