@@ -179,7 +179,8 @@ static std::vector<int> part_bounds(int R, int parts, int align) {
   return b;
 }
 
-// Pipelined host-pointer call of the FP32 split form.  op(A) goes in row
+// Pipelined host-pointer call of the FP32 split forms and the FP64 CRT form
+// (T = float / double; the same part and block structure).  op(A) goes in row
 // parts and op(B) in column parts; a copy stream moves them to HBM in the
 // order A0 B0 A1 B1 ... (with B part j, the columns of C it covers), and the
 // compute stream prepares each part once it has arrived and
@@ -193,23 +194,25 @@ static std::vector<int> part_bounds(int R, int parts, int align) {
 // while the operand copies ran.  The results equal the whole-problem call's
 // bit for bit: the exponents are per row / column over all of K, and every C
 // element's K order is the same.  Caller holds s->mu; st is s->stage_stream.
+template <typename T>
 static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char tb, int m, int n,
-                                int k, float alpha, const float *a, int lda, const float *b,
-                                int ldb, float beta, float *c, int ldc, int prm, bool ce) {
+                                int k, T alpha, const T *a, int lda, const T *b, int ldb, T beta,
+                                T *c, int ldc, int prm, bool ce) {
   const bool an = notrans(ta), bn = notrans(tb);
   const int arows = an ? m : k, acols = an ? k : m;
   const int brows = bn ? k : n, bcols = bn ? n : k;
   const std::vector<int> rb = part_bounds(m, host_parts_for(m, k, ce), kSplitBM);
   const std::vector<int> cb = part_bounds(n, host_parts_for(n, k, ce), kBf16xBN);
   const int P = (int)rb.size() - 1, Q = (int)cb.size() - 1;
-  auto up = [](int r) { return ((r > 1 ? r : 1) + 3) / 4 * 4; };
+  constexpr int epl = 16 / (int)sizeof(T);  // 16-byte aligned columns in HBM
+  auto up = [](int r) { return ((r > 1 ? r : 1) + epl - 1) / epl * epl; };
   const int ulda = up(arows), uldb = up(brows), uldc = up(m);
-  if (!grow(&s->stage[0], &s->stage_bytes[0], (size_t)ulda * acols * sizeof(float) + 16) ||
-      !grow(&s->stage[1], &s->stage_bytes[1], (size_t)uldb * bcols * sizeof(float) + 16) ||
-      !grow(&s->stage[2], &s->stage_bytes[2], (size_t)uldc * n * sizeof(float) + 16))
+  if (!grow(&s->stage[0], &s->stage_bytes[0], (size_t)ulda * acols * sizeof(T) + 16) ||
+      !grow(&s->stage[1], &s->stage_bytes[1], (size_t)uldb * bcols * sizeof(T) + 16) ||
+      !grow(&s->stage[2], &s->stage_bytes[2], (size_t)uldc * n * sizeof(T) + 16))
     return GB300_ERR_NOMEM;
-  float *dA = static_cast<float *>(s->stage[0]), *dB = static_cast<float *>(s->stage[1]);
-  float *dC = static_cast<float *>(s->stage[2]);
+  T *dA = static_cast<T *>(s->stage[0]), *dB = static_cast<T *>(s->stage[1]);
+  T *dC = static_cast<T *>(s->stage[2]);
   for (cudaStream_t *q : {&s->copy_stream, &s->out_stream, &s->prep_stream, &s->block_stream})
     if (!*q && cudaStreamCreateWithFlags(q, cudaStreamNonBlocking) != cudaSuccess)
       return GB300_ERR_CUDA;
@@ -218,20 +221,37 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return GB300_ERR_CUDA;
     s->part_ev.push_back(e);
   }
-  const size_t wneed = split_workspace_bytes(0, m, n, k, prm);
+  // FP32: the BF16xP / scaled FP16 split; FP64: the CRT form
+  const size_t wneed = sizeof(T) == 4 ? split_workspace_bytes(0, m, n, k, prm)
+                                      : crt_workspace_bytes(m, n, k, prm);
+  auto prepare_part = [&](int z, char t, const T *X, int ldx, int r0, int rows, void *w,
+                          cudaStream_t q) {
+    if constexpr (sizeof(T) == 4)
+      return split_sgemm_prepare_part(z, t, m, n, k, X, ldx, r0, rows, prm, w, wneed, q);
+    else
+      return crt_prepare_part(z, t, m, n, k, X, ldx, r0, rows, prm, w, wneed, q);
+  };
+  auto run_block = [&](int i0, int h, int j0, int w, void *wsp, cudaStream_t q) {
+    if constexpr (sizeof(T) == 4)
+      return split_sgemm_run_block(m, n, k, i0, h, j0, w, alpha, beta, dC, uldc, prm, wsp, wneed,
+                                   q, s->err);
+    else
+      return crt_run_block(m, n, k, i0, h, j0, w, alpha, beta, dC, uldc, prm, wsp, wneed, q,
+                           s->err);
+  };
   void *ws = wneed ? cached_workspace(s, st, wneed) : nullptr;
   if (!ws) return GB300_ERR_NOMEM;
   cudaStream_t cs = s->copy_stream, os = s->out_stream, ps = s->prep_stream;
   const cudaStream_t bs[2] = {st, s->block_stream};
   // copy engines for page-locked memory, else SM copies (the device reads the
   // host memory); one 2-D copy per part or block (w elements x cols)
-  auto copy = [&](float *dst, int dp, const float *src, int sp, int w, int cols,
+  auto copy = [&](T *dst, int dp, const T *src, int sp, int w, int cols,
                   cudaMemcpyKind kind, cudaStream_t q) {
     if (ce)
-      return cudaMemcpy2DAsync(dst, (size_t)dp * sizeof(float), src, (size_t)sp * sizeof(float),
-                               (size_t)w * sizeof(float), cols, kind, q) == cudaSuccess;
-    return copy_2d(dst, (size_t)dp * sizeof(float), src, (size_t)sp * sizeof(float),
-                   (size_t)w * sizeof(float), cols, q) == GB300_OK;
+      return cudaMemcpy2DAsync(dst, (size_t)dp * sizeof(T), src, (size_t)sp * sizeof(T),
+                               (size_t)w * sizeof(T), cols, kind, q) == cudaSuccess;
+    return copy_2d(dst, (size_t)dp * sizeof(T), src, (size_t)sp * sizeof(T),
+                   (size_t)w * sizeof(T), cols, q) == GB300_OK;
   };
   const cudaMemcpyKind h2d = cudaMemcpyHostToDevice, d2h = cudaMemcpyDeviceToHost;
   // arrival of the parts in HBM, their splits done, the blocks done
@@ -264,15 +284,13 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
     if (sh < P) {
       rc = cudaStreamWaitEvent(ps, evA[sh], 0) == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
       if (rc == GB300_OK)
-        rc = split_sgemm_prepare_part(0, ta, m, n, k, dA, ulda, rb[sh], rb[sh + 1] - rb[sh], prm,
-                                      ws, wneed, ps);
+        rc = prepare_part(0, ta, dA, ulda, rb[sh], rb[sh + 1] - rb[sh], ws, ps);
       if (rc == GB300_OK && cudaEventRecord(evPA[sh], ps) != cudaSuccess) rc = GB300_ERR_CUDA;
     }
     if (rc == GB300_OK && sh < Q) {
       rc = cudaStreamWaitEvent(ps, evB[sh], 0) == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
       if (rc == GB300_OK)
-        rc = split_sgemm_prepare_part(1, tb, m, n, k, dB, uldb, cb[sh], cb[sh + 1] - cb[sh], prm,
-                                      ws, wneed, ps);
+        rc = prepare_part(1, tb, dB, uldb, cb[sh], cb[sh + 1] - cb[sh], ws, ps);
       if (rc == GB300_OK && cudaEventRecord(evPB[sh], ps) != cudaSuccess) rc = GB300_ERR_CUDA;
     }
   }
@@ -283,8 +301,7 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
     if (cudaStreamWaitEvent(q, evPA[i], 0) != cudaSuccess ||
         cudaStreamWaitEvent(q, evPB[j], 0) != cudaSuccess)
       return (int)GB300_ERR_CUDA;
-    int r = split_sgemm_run_block(m, n, k, i0, h, j0, w, alpha, beta, dC, uldc, prm, ws, wneed,
-                                  q, s->err);
+    int r = run_block(i0, h, j0, w, ws, q);
     // the finished block goes back while the next ones compute
     cudaEvent_t e = evC[nblk++];
     if (r == GB300_OK &&
@@ -351,12 +368,13 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
       int ch = 0;
       bf16x_resolve(m, n, k, &prm, &ch);
     }
-    if constexpr (sizeof(T) == 4) {
+    {
+      // the FP32 split forms and the FP64 CRT form
       const bool pinned = host_pinned(a, b, c);
-      if (form == 1 && need_ab &&
+      if ((form == 1 || form == 3) && need_ab &&
           (host_parts_for(m, k, pinned) > 1 || host_parts_for(n, k, pinned) > 1))
-        return host_split_pipelined(s, st, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
-                                    param, pinned);
+        return host_split_pipelined<T>(s, st, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c,
+                                       ldc, param, pinned);
     }
     const bool two_pass = form >= 2 || prm == kFp16x3;
     const int epl = 16 / (int)sizeof(T);

@@ -112,7 +112,7 @@ __device__ __forceinline__ void residue_blocks(const unsigned (&y0)[8], const un
 __global__ void __launch_bounds__(256, 3)
     crt_residue_kernel(const __grid_constant__ OperandPair op,
                        const __grid_constant__ CrtModParams mp) {
-  const int z = blockIdx.z;
+  const int z = blockIdx.z + op.zbase;
   const double *__restrict__ X = z ? op.X1 : op.X0;
   const int ld = z ? op.ld1 : op.ld0, R = z ? op.R1 : op.R0, kcontig = z ? op.kc1 : op.kc0;
   const int Rp = z ? op.Rp1 : op.Rp0, K = op.K, Kp = op.Kp;
@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(256, 3)
   __shared__ double tile[32][65];
   const int k0 = blockIdx.x * 64;
   const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
-  const int64_t step = (int64_t)Rp * Kp / 8;
+  const int64_t plane = z ? op.plane1 : op.plane0;
+  const int64_t step = (plane ? plane : (int64_t)Rp * Kp) / 8;  // one residue block, in uint4
   for (int r0 = blockIdx.y * 32; r0 < Rp; r0 += gridDim.y * 32) {
     load_tile_32x64<double>(X, ld, R, K, kcontig != 0, r0, k0, tile);
     __syncthreads();
@@ -476,6 +477,25 @@ CrtLayout crt_layout(int m, int n, int k, int N, void *ws) {
   return L;
 }
 
+// Constants of the residue kernel for N moduli and b-bit scaled integers.
+CrtModParams mod_params(int N, int b) {
+  CrtModParams mp;
+  std::memset(&mp, 0, sizeof(mp));
+  mp.N = N;
+  mp.b = b;
+  for (int i = 0; i < kCrtMaxModuli; ++i) {
+    const unsigned p = (unsigned)kModuli[i];
+    mp.p[i] = p;
+    mp.mg[i] = (unsigned)((1ull << 32) / p);
+    mp.c21[i] = (unsigned)((1ull << 21) % p);
+    mp.c42[i] = (unsigned)((1ull << 42) % p);
+    mp.pw32[i] = (unsigned)((1ull << 32) % p);
+  }
+  return mp;
+}
+
+unsigned row_blocks(int64_t Rp) { return (unsigned)(Rp / 32 < 65535 ? Rp / 32 : 65535); }
+
 // moduli 0: the autotuned count for the shape class, else the default
 int resolve_moduli(int moduli, int m = 0, int n = 0, int k = 0) {
   if (moduli > 0) return moduli;
@@ -536,19 +556,7 @@ int crt_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda,
       row_scale_exponents(ta, tb, m, n, k, A, lda, B, ldb, L.amax, L.ex, L.Mp, L.Np, st);
   if (rc != GB300_OK) return rc;
   // 2. residues
-  CrtModParams mp;
-  std::memset(&mp, 0, sizeof(mp));
-  mp.N = N;
-  mp.b = b;
-  for (int i = 0; i < kCrtMaxModuli; ++i) {
-    const unsigned p = (unsigned)kModuli[i];
-    mp.p[i] = p;
-    mp.mg[i] = (unsigned)((1ull << 32) / p);
-    mp.c21[i] = (unsigned)((1ull << 21) % p);
-    mp.c42[i] = (unsigned)((1ull << 42) % p);
-    mp.pw32[i] = (unsigned)((1ull << 32) % p);
-  }
-  auto row_blocks = [](int64_t Rp) { return (unsigned)(Rp / 32 < 65535 ? Rp / 32 : 65535); };
+  const CrtModParams mp = mod_params(N, b);
   const bool an = notrans(ta), bn = notrans(tb);
   OperandPair op;
   op.X0 = A; op.ld0 = lda; op.R0 = m; op.kc0 = an ? 0 : 1; op.Rp0 = (int)L.Mp;
@@ -560,33 +568,78 @@ int crt_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda,
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }
 
+int crt_prepare_part(int z, char t, int m, int n, int k, const double *X, int ldx, int r0,
+                     int rows, int moduli, void *ws, size_t ws_bytes, cudaStream_t st) {
+  const int N = resolve_moduli(moduli, m, n, k);
+  const int align = z ? kOzakiBN : kSplitBM, R = z ? n : m;
+  if (N < 2 || N > kCrtMaxModuli || m <= 0 || n <= 0 || k <= 0 || r0 < 0 || rows <= 0 ||
+      r0 % align || r0 + rows > R || ldx < 1)
+    return GB300_ERR_ARG;
+  const int b = crt_bits_for(N, k);
+  if (b < 1) return GB300_ERR_ARG;
+  const size_t need = crt_workspace_bytes(m, n, k, N);
+  if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
+  const CrtLayout L = crt_layout(m, n, k, N, ws);
+  // op(A) rows are k-contiguous when A is transposed, op(B) columns when B is not
+  const bool kc = z ? notrans(t) : !notrans(t);
+  const double *Xp = kc ? X + (int64_t)r0 * ldx : X + r0;
+  const int Rpart = (rows + align - 1) / align * align;
+  int rc = row_scale_exponents_part(z, kc, rows, Rpart, r0, k, Xp, ldx, L.amax, L.ex, L.Mp, L.Np,
+                                    st);
+  if (rc != GB300_OK) return rc;
+  OperandPair op;
+  op.X0 = op.X1 = Xp; op.ld0 = op.ld1 = ldx; op.R0 = op.R1 = rows;
+  op.kc0 = op.kc1 = kc ? 1 : 0; op.Rp0 = op.Rp1 = Rpart;
+  op.ex0 = op.ex1 = L.ex + (z ? L.Mp : 0) + r0;
+  op.out0 = op.out1 = (z ? L.Bs : L.As) + (int64_t)r0 * L.Kp;
+  op.K = k; op.Kp = (int)L.Kp;
+  op.zbase = z;
+  op.plane0 = op.plane1 = (z ? L.Np : L.Mp) * L.Kp;
+  crt_residue_kernel<<<dim3((unsigned)(L.Kp / 64), row_blocks(Rpart), 1), 256, 0, st>>>(
+      op, mod_params(N, b));
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
 int crt_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int moduli,
             const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err) {
+  return crt_run_block(m, n, k, 0, m, 0, n, alpha, beta, C, ldc, moduli, ws, ws_bytes, st, err);
+}
+
+int crt_run_block(int m, int n, int k, int i0, int h, int j0, int w, double alpha, double beta,
+                  double *C, int ldc, int moduli, const void *ws, size_t ws_bytes,
+                  cudaStream_t st, unsigned *err) {
   const int N = resolve_moduli(moduli, m, n, k);
-  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || N < 2 || N > kCrtMaxModuli)
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || N < 2 || N > kCrtMaxModuli ||
+      i0 < 0 || j0 < 0 || h < 0 || w < 0 || i0 % kSplitBM || j0 % kOzakiBN || i0 + h > m ||
+      j0 + w > n)
     return GB300_ERR_ARG;
-  if (m == 0 || n == 0) return GB300_OK;
+  if (h == 0 || w == 0) return GB300_OK;
+  double *Cb = C + i0 + (int64_t)j0 * ldc;
   if (alpha == 0.0 || k == 0)
-    return plain_dgemm('N', 'N', m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc,
-                       st, err);
+    return plain_dgemm('N', 'N', h, w, 0, alpha, nullptr, h > 1 ? h : 1, nullptr, 1, beta, Cb,
+                       ldc, st, err);
   const int b = crt_bits_for(N, k);
   if (b < 1) return GB300_ERR_ARG;
   const size_t need = crt_workspace_bytes(m, n, k, N);
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
   const CrtLayout L = crt_layout(m, n, k, N, const_cast<void *>(ws));
+  // the block's residues: plane g, column j0 + j, row i0 + i at g Mp Np + (j0 + j) Mp + i0 + i
+  uint8_t *rres = L.rres + (int64_t)j0 * L.Mp + i0;
+  const int *expA = L.ex + i0, *expB = L.ex + L.Mp + j0;
   // 3. one exact integer GEMM per modulus
   OzakiGemmArgs a;
-  a.m = m; a.n = n; a.k = k; a.S = N; a.mode = 1;
+  a.m = h; a.n = w; a.k = k; a.S = N; a.mode = 1;
   a.Mp = L.Mp; a.Np = L.Np; a.Kp = L.Kp;
   a.As = L.As; a.Bs = L.Bs;
-  a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc;
-  a.expA = L.ex; a.expB = L.ex + L.Mp; a.res = nullptr; a.rres = L.rres; a.mods = kModuli;
+  a.row0 = i0; a.col0 = j0;
+  a.alpha = alpha; a.beta = beta; a.C = Cb; a.ldc = ldc;
+  a.expA = expA; a.expB = expB; a.res = nullptr; a.rres = rres; a.mods = kModuli;
   const int rc = ozaki_gemm_launch(a, st, err);
   if (rc != GB300_OK) return rc;
   // 4. reconstruction and the C update
   CrtRecParams rp;
   std::memset(&rp, 0, sizeof(rp));
-  rp.N = N; rp.m = m; rp.n = n; rp.Mp = (int)L.Mp; rp.Np = (int)L.Np; rp.two_b = 2 * b;
+  rp.N = N; rp.m = h; rp.n = w; rp.Mp = (int)L.Mp; rp.Np = (int)L.Np; rp.two_b = 2 * b;
   const Big M = modulus_product(N);
   auto limbs32 = [](const Big &x, unsigned *out) {
     for (int l = 0; l < kLimbs; ++l) out[l] = (unsigned)(x.l[l / 2] >> (32 * (l % 2)));
@@ -611,17 +664,17 @@ int crt_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, 
     for (int s = 0; s < rp.topshift; ++s) big_divmod(mt, 2);
     rp.inv_mt = 1.0f / (float)mt.l[0];
   }
-  rp.alpha = alpha; rp.beta = beta; rp.C = C; rp.ldc = ldc;
-  const dim3 grid((unsigned)((m + 256 * kRecRows - 1) / (256 * kRecRows)),
-                  (unsigned)(n < 65535 ? n : 65535));
+  rp.alpha = alpha; rp.beta = beta; rp.C = Cb; rp.ldc = ldc;
+  const dim3 grid((unsigned)((h + 256 * kRecRows - 1) / (256 * kRecRows)),
+                  (unsigned)(w < 65535 ? w : 65535));
   // limbs of M: 4 up to 16 moduli, 5 up to 20, 6 up to 24
   const int limbs = (bl + 31) / 32 < 2 ? 2 : (bl + 31) / 32;
   switch (limbs) {
-    case 2: crt_reconstruct_kernel<2><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
-    case 3: crt_reconstruct_kernel<3><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
-    case 4: crt_reconstruct_kernel<4><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
-    case 5: crt_reconstruct_kernel<5><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
-    default: crt_reconstruct_kernel<6><<<grid, 256, 0, st>>>(L.rres, L.ex, L.ex + L.Mp, rp); break;
+    case 2: crt_reconstruct_kernel<2><<<grid, 256, 0, st>>>(rres, expA, expB, rp); break;
+    case 3: crt_reconstruct_kernel<3><<<grid, 256, 0, st>>>(rres, expA, expB, rp); break;
+    case 4: crt_reconstruct_kernel<4><<<grid, 256, 0, st>>>(rres, expA, expB, rp); break;
+    case 5: crt_reconstruct_kernel<5><<<grid, 256, 0, st>>>(rres, expA, expB, rp); break;
+    default: crt_reconstruct_kernel<6><<<grid, 256, 0, st>>>(rres, expA, expB, rp); break;
   }
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
 }

@@ -45,6 +45,10 @@ struct OzakiGemmArgs {
   double *res;        // mode 0: Mp x Np FP64 scratch
   uint8_t *rres;      // mode 1: S x Mp x Np residues
   const int *mods;    // mode 1: the S moduli
+  // mode 1, a sub-block of a larger problem: its first row of op(A) and
+  // column of op(B) in the operand blocks (Mp, Np: the whole problem's; m, n:
+  // the block's; rres, expA, expB point at the block's first entries)
+  int row0 = 0, col0 = 0;
 };
 int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err);
 // Per-row max |.| of op(A) and per-column max of op(B) and their scale
@@ -52,6 +56,12 @@ int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err);
 int row_scale_exponents(char ta, char tb, int m, int n, int k, const double *A, int lda,
                         const double *B, int ldb, unsigned long long *amax, int *ex, int64_t Mp,
                         int64_t Np, cudaStream_t st);
+// The same over one operand part: rows [r0, r0 + R) of op(A) (z = 0) or
+// columns of op(B) (z = 1), X at the part's first one (kc: k-contiguous);
+// writes entries [r0, r0 + Rpart) of that operand's range.
+int row_scale_exponents_part(int z, bool kc, int R, int Rpart, int r0, int k, const double *X,
+                             int ldx, unsigned long long *amax, int *ex, int64_t Mp, int64_t Np,
+                             cudaStream_t st);
 
 // CRT form (crt.cu): C = alpha op(A) op(B) + beta C with the FP64 product
 // computed exactly as residues modulo `moduli` (0 = tuned / 16) BF16 GEMMs.
@@ -68,6 +78,14 @@ int crt_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda,
                 int ldb, int moduli, void *ws, size_t ws_bytes, cudaStream_t st);
 int crt_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int moduli,
             const void *ws, size_t ws_bytes, cudaStream_t st, unsigned *err);
+// Parts of the two phases for a pipelined call, in the whole problem's
+// workspace (as split_sgemm_prepare_part / split_sgemm_run_block: row parts
+// start on multiples of 128, column parts on multiples of 256).
+int crt_prepare_part(int z, char t, int m, int n, int k, const double *X, int ldx, int r0,
+                     int rows, int moduli, void *ws, size_t ws_bytes, cudaStream_t st);
+int crt_run_block(int m, int n, int k, int i0, int h, int j0, int w, double alpha, double beta,
+                  double *C, int ldc, int moduli, const void *ws, size_t ws_bytes,
+                  cudaStream_t st, unsigned *err);
 
 int ozaki_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                 const double *B, int ldb, double beta, double *C, int ldc, int slices, void *ws,

@@ -40,6 +40,11 @@ struct OperandPair {
   const int *ex0, *ex1;  // row exponents
   void *out0, *out1;     // 16-bit blocks of Rp rows x Kp
   int K, Kp;
+  // a launch over one operand part (CRT residues): blockIdx.z + zbase is the
+  // operand, and the blocks of the whole operand are plane elements apart
+  // (0: Rp x Kp)
+  int zbase = 0;
+  int64_t plane0 = 0, plane1 = 0;
 };
 
 // Scale exponent of a row: 2^-E * max|x| < 1.  Non-finite rows return a marker.

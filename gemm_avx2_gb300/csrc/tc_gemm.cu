@@ -674,6 +674,9 @@ struct OzakiParams {
   // work units per tile: the S groups in gsplit ranges (CRT form only, whose
   // moduli are independent GEMMs; 1 in the slice form, which sums its groups)
   int gsplit;
+  // first row of op(A) / column of op(B) in each operand block (a sub-block
+  // of a larger problem's workspace; 0 for a whole problem)
+  int row0, col0;
 };
 
 constexpr int kOzEpiWarps = 16;  // 4 per TMEM lane quarter, BN / 4 columns each
@@ -790,14 +793,15 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             }
             uint8_t *sa_ptr = smem + s * kOzStage;
             mbar_arrive_expect_tx(&full[s], kOzStage);
-            tma_load_2d(sa_ptr, &tmA, kb * kSplitBK, (sa - 1) * p.Mp + tm * kSplitBM, &full[s]);
+            tma_load_2d(sa_ptr, &tmA, kb * kSplitBK, (sa - 1) * p.Mp + p.row0 + tm * kSplitBM,
+                        &full[s]);
             if (MC)
               tma_load_2d_mc(sa_ptr + kOzABytes + rank * (kOzBBytes / 2), &tmB, kb * kSplitBK,
-                             (sb - 1) * p.Np + tn * BN + (int)rank * (BN / 2),
+                             (sb - 1) * p.Np + p.col0 + tn * BN + (int)rank * (BN / 2),
                              &full[s], 0x3);
             else
               tma_load_2d(sa_ptr + kOzABytes, &tmB, kb * kSplitBK,
-                          (sb - 1) * p.Np + tn * BN, &full[s]);
+                          (sb - 1) * p.Np + p.col0 + tn * BN, &full[s]);
           }
         }
       }
@@ -1110,6 +1114,12 @@ static int scale_exponents_part(int z, bool kc, int R, int Rpart, int r0, int k,
   p.nblocks = gx * gy;
   row_absmax_kernel<T><<<dim3(gx, gy, 1), 256, 0, st>>>(p);
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int row_scale_exponents_part(int z, bool kc, int R, int Rpart, int r0, int k, const double *X,
+                             int ldx, unsigned long long *amax, int *ex, int64_t Mp, int64_t Np,
+                             cudaStream_t st) {
+  return scale_exponents_part<double>(z, kc, R, Rpart, r0, k, X, ldx, amax, ex, Mp, Np, st);
 }
 
 int row_scale_exponents(char ta, char tb, int m, int n, int k, const double *A, int lda,
@@ -1497,7 +1507,7 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
 
 template <int BN>
 static int ozaki_launch_bn(const OzakiGemmArgs &a, OzakiParams p, cudaStream_t st) {
-  const bool mc = a.Mp / kSplitBM >= 2;  // 2-CTA clusters sharing the B tile
+  const bool mc = p.tiles_m >= 2;  // 2-CTA clusters sharing the B tile
   CUtensorMap tA{}, tB{};
   if (!encode_2d(&tA, a.As, 2, a.Kp, a.S * a.Mp, a.Kp, kSplitBK, kSplitBM, true) ||
       !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, mc ? BN / 2 : BN, true))
@@ -1518,7 +1528,8 @@ int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
   if (a.S < 1 || a.S > (a.mode ? kCrtMaxModuli : kOzakiMaxSlices)) return GB300_ERR_ARG;
   OzakiParams p;
   p.m = a.m; p.n = a.n;
-  p.tiles_m = (int)(a.Mp / kSplitBM);
+  p.tiles_m = (a.m + kSplitBM - 1) / kSplitBM;  // Mp / 128 for a whole problem
+  p.row0 = a.row0; p.col0 = a.col0;
   p.tiles_n = 0;  // set by the launch for its tile width
   p.S = a.S; p.KB = (int)(a.Kp / kSplitBK);
   p.mode = a.mode;

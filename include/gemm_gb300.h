@@ -393,8 +393,9 @@ void gb300_tune_cache_clear(void);
  *   the default (the tuned mode of the shape class, else multicast).  Both
  *   give the same results bit for bit.
  *   GB300_TUNE_HOST_PARTS: operand parts (1..8) of the pipelined host-pointer
- *   path of the FP32 split form (gb300_host_sgemm_bf16x, the drop-in with
- *   GB300_DROPIN_FORM=split): op(A) in that many row parts and op(B) in that
+ *   path of the FP32 split form and the FP64 CRT form (gb300_host_sgemm_bf16x,
+ *   gb300_host_dgemm_ozaki2, the drop-ins with GB300_DROPIN_FORM=split):
+ *   op(A) in that many row parts and op(B) in that
  *   many column parts, copied to HBM on a copy stream while the compute
  *   stream prepares the parts that have arrived and multiplies the C blocks
  *   whose parts are ready, and C blocks go back as they finish.  1 turns

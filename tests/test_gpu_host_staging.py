@@ -93,3 +93,43 @@ def test_pipelined_host_sgemm_pinned_buffers(orc, host_parts):
     got = pc.numpy().reshape((n, m)).T
     assert np.isnan(got[5, 700]) and np.isnan(got[1000, 3])
     assert np.array_equal(got, ref, equal_nan=True)
+
+
+@pytest.mark.parametrize("parts", [2, 3])
+@pytest.mark.parametrize("ta,tb", [("T", "N"), ("N", "N"), ("N", "T"), ("T", "T")])
+def test_pipelined_host_crt_matches_device(orc, host_parts, parts, ta, tb):
+    """The FP64 CRT form in row / column parts: bit for bit the device-pointer
+    result (ragged last parts, padded ld, beta != 0)."""
+    m, n, k = 700, 900, 300
+    ar, ac = (m, k) if ta == "N" else (k, m)
+    br, bc = (k, n) if tb == "N" else (n, k)
+    A = orc.spread((ar + 1, ac), 84, 0, 1.0)
+    B = orc.spread((br + 3, bc), 84, 1, 1.0)
+    C = orc.uniform((m + 2, n), np.float64, 84, 2)
+    ref = device_result("crt", ta, tb, m, n, k, -0.5, A, ar + 1, B, br + 3, 0.75, C, 15)
+    assert host_parts(parts) == g.OK
+    Ch = C.copy(order="F")
+    assert g.host_split_gemm("crt", ta, tb, m, n, k, -0.5, A, ar + 1, B, br + 3, 0.75, Ch, m + 2,
+                             15) == g.OK
+    assert np.array_equal(Ch[m:], C[m:])
+    assert np.array_equal(Ch[:m], ref[:m])
+    assert g.device_error() == 0
+
+
+def test_pipelined_host_crt_pinned_beta0_nan(orc, host_parts):
+    """Copy-engine path of the CRT form, beta = 0 with NaN / Inf in C."""
+    torch = torch_cuda()
+    m, n, k = 1100, 800, 530
+    A = orc.spread((m, k), 85, 0, 1.0)
+    B = orc.spread((n, k), 85, 1, 1.0)
+    C = orc.uniform((m, n), np.float64, 85, 2)
+    C[7, 650] = np.nan
+    C[900, 2] = np.inf
+    ref = device_result("crt", "N", "T", m, n, k, 1.0, A, m, B, n, 0.0, C, 16)
+    pa, pb, pc = (torch.from_numpy(x.ravel(order="F").copy()).pin_memory() for x in (A, B, C))
+    assert host_parts(4) == g.OK
+    assert g.core().gb300_host_dgemm_ozaki2(b"N", b"T", m, n, k, 1.0, pa.data_ptr(), m,
+                                            pb.data_ptr(), n, 0.0, pc.data_ptr(), m, 16) == g.OK
+    got = pc.numpy().reshape((n, m)).T
+    assert np.isnan(got[7, 650]) and np.isnan(got[900, 2])
+    assert np.array_equal(got, ref, equal_nan=True)
