@@ -1051,6 +1051,8 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
                  cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming) == cudaSuccess &&
                  cudaStreamWaitEvent(bs[b], fork, 0) == cudaSuccess;
       if (!forked) rc2 = GB300_ERR_CUDA;
+      // the branches run their problems side by side: whole-tile CRT units
+      set_modulus_split_hint(1);
       for (int i = 0; i < count && rc2 == GB300_OK; ++i) {
         const gb300_gemm_problem &q = problems[i];
         const int b = branch_of[i];
@@ -1067,6 +1069,7 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
                             static_cast<float *>(q.C), q.ldc, 6, g->ws[b], wneed_b[b], bs[b],
                             s->err);
       }
+      set_modulus_split_hint(0);
       for (int b = 0; b < nbr && forked; ++b)
         if (cudaEventRecord(join[b], bs[b]) != cudaSuccess ||
             cudaStreamWaitEvent(cs, join[b], 0) != cudaSuccess)

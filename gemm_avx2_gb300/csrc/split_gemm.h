@@ -128,6 +128,8 @@ int pair_mma_override();
 // Work units of the CRT GEMM: 0 = by shape, 1 = whole tiles, 2 = one modulus
 // of one tile (the moduli are independent GEMMs).
 void set_modulus_split(int v);
+// The same for launches from the calling thread only (the knob wins).
+void set_modulus_split_hint(int v);
 int modulus_split_override();
 // Tuned tile width (0 = none) and cluster mode (0 = none, 1 = pair MMAs,
 // 2 = multicast) of a shape class.

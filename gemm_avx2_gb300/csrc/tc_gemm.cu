@@ -163,6 +163,111 @@ __global__ void __launch_bounds__(256) split_bf16_kernel(const __grid_constant__
   }
 }
 
+// Fused max pass and scaled FP16 split of k-contiguous rows (rows of op(A)
+// when A is transposed, columns of op(B) when B is not): one CTA per row, the
+// row held in registers (VPT values a thread, Kp <= 256 VPT) between the
+// block-wide max and the split, so it is read from memory once.  Writes the
+// row's exponent and its segments exactly as row_absmax_kernel followed by
+// split_bf16_kernel<true> do (columns [K, Kp) and rows [R, Rp) as zeros).
+struct RowSplitArgs {
+  const float *X0, *X1;  // first row of each operand (part)
+  int ld0, ld1, R0, R1, Rp0, Rp1;
+  SegMap seg0, seg1;
+  int *ex0, *ex1;
+  __nv_bfloat16 *out0, *out1;
+  int K, Kp;
+  int64_t ldo;
+  int zbase;  // operand of blockIdx.z = 0
+  int vec;    // every row starts on 16 bytes: float4 loads
+};
+
+template <int VPT>
+__global__ void __launch_bounds__(256) f16_row_split_kernel(const __grid_constant__ RowSplitArgs p) {
+  const int z = blockIdx.z + p.zbase;
+  const int R = z ? p.R1 : p.R0, Rp = z ? p.Rp1 : p.Rp0;
+  const int row = blockIdx.x;
+  if (row >= Rp) return;  // the other operand has more rows (uniform per CTA)
+  const float *__restrict__ X = (z ? p.X1 : p.X0) + (int64_t)row * (z ? p.ld1 : p.ld0);
+  const SegMap &seg = z ? p.seg1 : p.seg0;
+  const int K = p.K, Kp = p.Kp, t = threadIdx.x;
+  // value 4 j + q of this thread is element 1024 j + 4 t + q: a warp reads and
+  // writes contiguous runs
+  float v[VPT];
+  const bool live = row < R;
+#pragma unroll
+  for (int j = 0; j < VPT / 4; ++j) {
+    const int e0 = 1024 * j + 4 * t;
+    if (live && p.vec && e0 + 3 < K) {
+      const float4 f = *reinterpret_cast<const float4 *>(X + e0);
+      v[4 * j] = f.x; v[4 * j + 1] = f.y; v[4 * j + 2] = f.z; v[4 * j + 3] = f.w;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[4 * j + q] = (live && e0 + q < K) ? X[e0 + q] : 0.0f;
+    }
+  }
+  // max |x| as a bit pattern (NaN and Inf above every finite value)
+  unsigned mx = 0;
+#pragma unroll
+  for (int i = 0; i < VPT; ++i) mx = max(mx, __float_as_uint(fabsf(v[i])));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  __shared__ unsigned wmax[8];
+  if ((t & 31) == 0) wmax[t >> 5] = mx;
+  __syncthreads();
+  mx = wmax[0];
+#pragma unroll
+  for (int w = 1; w < 8; ++w) mx = max(mx, wmax[w]);
+  const int e = live ? row_exponent_f32(mx) : 0;
+  if (t == 0) (z ? p.ex1 : p.ex0)[row] = e;
+  __nv_bfloat16 *out = (z ? p.out1 : p.out0) + (int64_t)row * p.ldo;
+  const bool bad = e == kNonFiniteExp;  // a row of Inf / NaN: all terms NaN
+#pragma unroll
+  for (int j = 0; j < VPT / 4; ++j) {
+    const int e0 = 1024 * j + 4 * t;
+    if (e0 >= Kp) continue;  // Kp is a multiple of 64: e0 < Kp covers e0 + 3
+    uint2 w0, w1, w2;  // hi, lo and the zero term of the 4 values
+    if (bad) {
+      w0 = w1 = w2 = make_uint2(0x7e007e00u, 0x7e007e00u);
+    } else {
+      unsigned short h[4], l[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) f16_terms(v[4 * j + q], 15 - e, h[q], l[q]);
+      w0 = make_uint2((unsigned)h[0] | ((unsigned)h[1] << 16),
+                      (unsigned)h[2] | ((unsigned)h[3] << 16));
+      w1 = make_uint2((unsigned)l[0] | ((unsigned)l[1] << 16),
+                      (unsigned)l[2] | ((unsigned)l[3] << 16));
+      w2 = make_uint2(0u, 0u);
+    }
+#pragma unroll
+    for (int sg = 0; sg < 3; ++sg) {  // the scaled FP16 form has 3 segments
+      const int ti = seg.term[sg];
+      *reinterpret_cast<uint2 *>(out + (int64_t)sg * Kp + e0) = ti == 0 ? w0 : ti == 1 ? w1 : w2;
+    }
+  }
+}
+
+// Values a thread holds in the fused row split for k (0: k outside its range;
+// short rows stay with the two-pass kernels, which cover 32 rows a CTA).
+static int row_split_vpt(int k) {
+  const int64_t kp = (k + 63) / 64 * 64;
+  if (k < 1024) return 0;
+  for (int v = 4; v <= 64; v *= 2)
+    if (256 * v >= kp) return v;
+  return 0;
+}
+
+static void row_split_launch(const RowSplitArgs &a, int vpt, unsigned rows, unsigned nz,
+                             cudaStream_t st) {
+  const dim3 grid(rows, 1, nz);
+  switch (vpt) {
+    case 4: f16_row_split_kernel<4><<<grid, 256, 0, st>>>(a); break;
+    case 8: f16_row_split_kernel<8><<<grid, 256, 0, st>>>(a); break;
+    case 16: f16_row_split_kernel<16><<<grid, 256, 0, st>>>(a); break;
+    case 32: f16_row_split_kernel<32><<<grid, 256, 0, st>>>(a); break;
+    default: f16_row_split_kernel<64><<<grid, 256, 0, st>>>(a); break;
+  }
+}
+
 // Ozaki step 1: per-row max |x| of op(X) as the bit pattern of the
 // non-negative value (monotone as an unsigned integer; NaN/Inf compare above
 // finite values), for FP64 and (scaled FP16 split) FP32 rows.
@@ -1180,7 +1285,34 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
   sa.zbase = 0;
   const unsigned rb = row_blocks(L.Mp > L.Np ? L.Mp : L.Np);
   const dim3 grid((unsigned)(L.Kp / 64), rb, 2);
-  if (f16) {
+  const int vpt = f16 ? row_split_vpt(k) : 0;
+  const bool fz[2] = {vpt && sa.kc0, vpt && sa.kc1};  // operands for the fused row split
+  if (f16 && (fz[0] || fz[1])) {
+    RowSplitArgs ra;
+    ra.X0 = A; ra.X1 = B; ra.ld0 = lda; ra.ld1 = ldb; ra.R0 = m; ra.R1 = n;
+    ra.Rp0 = (int)L.Mp; ra.Rp1 = (int)L.Np;
+    ra.seg0 = sa.seg0; ra.seg1 = sa.seg1;
+    ra.ex0 = L.ex; ra.ex1 = L.ex + L.Mp; ra.out0 = L.Ap; ra.out1 = L.Bp;
+    ra.K = k; ra.Kp = (int)L.Kp; ra.ldo = L.Kld;
+    ra.vec = (reinterpret_cast<uintptr_t>(A) % 16 == 0 && lda % 4 == 0 || !fz[0]) &&
+             (reinterpret_cast<uintptr_t>(B) % 16 == 0 && ldb % 4 == 0 || !fz[1]);
+    if (fz[0] && fz[1]) {
+      ra.zbase = 0;
+      row_split_launch(ra, vpt, (unsigned)(L.Mp > L.Np ? L.Mp : L.Np), 2, st);
+    } else {
+      // one operand fused, the other through the max pass and the tile split
+      const int zf = fz[0] ? 0 : 1, zo = 1 - zf;
+      ra.zbase = zf;
+      row_split_launch(ra, vpt, (unsigned)(zf ? L.Np : L.Mp), 1, st);
+      const int rc = scale_exponents_part<float>(
+          zo, zo ? sa.kc1 != 0 : sa.kc0 != 0, zo ? n : m, (int)(zo ? L.Np : L.Mp), 0, k,
+          zo ? B : A, zo ? ldb : lda, L.amax, L.ex, L.Mp, L.Np, st);
+      if (rc != GB300_OK) return rc;
+      sa.zbase = zo;
+      split_bf16_kernel<true><<<dim3((unsigned)(L.Kp / 64), row_blocks(zo ? L.Np : L.Mp), 1), 256,
+                                 0, st>>>(sa);
+    }
+  } else if (f16) {
     const int rc = scale_exponents<float>(ta, tb, m, n, k, A, lda, B, ldb, L.amax, L.ex, L.Mp,
                                           L.Np, st);
     if (rc != GB300_OK) return rc;
@@ -1222,7 +1354,16 @@ int split_sgemm_prepare_part(int z, char t, int m, int n, int k, const float *X,
   sa.ldo = L.Kld;
   sa.zbase = z;
   const dim3 grid((unsigned)(L.Kp / 64), row_blocks(Rpart), 1);
-  if (f16) {
+  const int vpt = f16 && kc ? row_split_vpt(k) : 0;
+  if (vpt) {  // k-contiguous rows: the fused max pass and split
+    RowSplitArgs ra;
+    ra.X0 = ra.X1 = Xp; ra.ld0 = ra.ld1 = ldx; ra.R0 = ra.R1 = rows; ra.Rp0 = ra.Rp1 = Rpart;
+    ra.seg0 = sa.seg0; ra.seg1 = sa.seg1;
+    ra.ex0 = ra.ex1 = ex; ra.out0 = ra.out1 = out;
+    ra.K = k; ra.Kp = (int)L.Kp; ra.ldo = L.Kld; ra.zbase = z;
+    ra.vec = reinterpret_cast<uintptr_t>(Xp) % 16 == 0 && ldx % 4 == 0;
+    row_split_launch(ra, vpt, (unsigned)Rpart, 1, st);
+  } else if (f16) {
     const int rc = scale_exponents_part<float>(z, kc, rows, Rpart, r0, k, Xp, ldx, L.amax, L.ex,
                                                L.Mp, L.Np, st);
     if (rc != GB300_OK) return rc;
@@ -1301,10 +1442,17 @@ static int g_pair_mma = 0;  // 0: none, 1: pair MMAs, 2: multicast
 void set_pair_mma(int v) { g_pair_mma = v; }
 int pair_mma_override() { return g_pair_mma; }
 // Work units of the CRT GEMM: 0 = by shape, 1 = whole tiles (all moduli),
-// 2 = one modulus of one tile.  Same results bit for bit.
+// 2 = one modulus of one tile.  Same results bit for bit.  The knob wins over
+// the calling thread's hint (the grouped graph's capture asks for whole
+// tiles: its problems run side by side, and one-modulus units would multiply
+// each small problem's CTAs and their setup).
 static int g_modulus_split = 0;
+static thread_local int t_modulus_split_hint = 0;
 void set_modulus_split(int v) { g_modulus_split = v; }
-int modulus_split_override() { return g_modulus_split; }
+void set_modulus_split_hint(int v) { t_modulus_split_hint = v; }
+int modulus_split_override() {
+  return g_modulus_split ? g_modulus_split : t_modulus_split_hint;
+}
 static bool use_pair_mma(int m, int n, int k) {
   const int v = g_pair_mma ? g_pair_mma : tune_pair_mma(0, m, n, k);
   return v == 1;

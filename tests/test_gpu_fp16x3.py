@@ -207,3 +207,37 @@ def test_pair_and_multicast_modes_agree(orc, products, tile):
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
     assert g.device_error() == 0
+
+
+@pytest.mark.parametrize("k", [1100, 2048, 4500])
+@pytest.mark.parametrize("ta,tb,pad", [("T", "N", 0), ("T", "N", 1), ("T", "T", 4), ("N", "N", 1)])
+def test_fused_row_split_bitexact(orc, k, ta, tb, pad):
+    """k >= 1024 with k-contiguous rows: the fused max pass and split (both
+    operands for TN, one for TT / NN; pad 0 or 4: float4 loads, pad 1: scalar
+    loads) write the same exponents and terms as the model, including a row of
+    NaN, an Inf column, a zero row and rows scaled by 2^40."""
+    m, n = 150, 260
+    ar, ac = (m, k) if ta == "N" else (k, m)
+    br, bc = (k, n) if tb == "N" else (n, k)
+    A = orc.uniform((ar + pad, ac), np.float32, 73, 0)
+    B = orc.uniform((br + pad, bc), np.float32, 73, 1)
+    Av = A[:m, :k] if ta == "N" else A[:k, :m].T  # op(A) and op(B) as views
+    Bv = B[:k, :n] if tb == "N" else B[:n, :k].T
+    Av[3, :] *= np.float32(2.0 ** 40)
+    Av[5, :] = 0.0
+    Av[7, 11] = np.nan
+    Bv[17, 9] = np.inf
+    C = orc.uniform((m, n), np.float32, 73, 2)
+    rc, got, ws = run(ta, tb, m, n, k, 1.0, A, ar + pad, B, br + pad, 0.0, C)
+    assert rc == g.OK
+    Ap, Bp, eA, eB, Mp, Np, Kp = workspace_parts(ws, m, n, k)
+    Aop = np.zeros((Mp, Kp), np.float32)
+    Aop[:m, :k] = op(A, ta, m, k)
+    Bop = np.zeros((Np, Kp), np.float32)
+    Bop[:n, :k] = op(B, tb, k, n).T
+    assert np.array_equal(eA, osp.row_exponents_f32(Aop))
+    assert np.array_equal(eB, osp.row_exponents_f32(Bop))
+    assert np.array_equal(Ap, osp.fp16x3_operand(Aop, True))
+    assert np.array_equal(Bp, osp.fp16x3_operand(Bop, False))
+    assert np.isnan(got[7]).all() and np.isnan(got[:, 9]).all()
+    assert g.device_error() == 0
