@@ -45,7 +45,7 @@ typedef enum {
   GB300_ERR_CUDA = 2,        /* a CUDA runtime call failed                    */
   GB300_ERR_TIMEOUT = 3,     /* a kernel's bounded wait expired (device error word set) */
   GB300_ERR_NOMEM = 4,       /* device workspace could not be allocated       */
-  GB300_ERR_UNSUPPORTED = 5, /* option outside what this build implements     */
+  GB300_ERR_UNSUPPORTED = 5, /* option this library does not implement       */
   GB300_ERR_WORKSPACE = 6,   /* caller-provided workspace too small           */
   GB300_ERR_NOALLOC_LIMIT = 7 /* problem needs more scratch than gb300_sgemm_bf16x_noalloc's fixed array */
 } gb300_status;

@@ -32,7 +32,7 @@ def test_autotune_ozaki_and_use(orc):
                          dC2.data_ptr(), m) == g.OK
     sync()
     e_tuned, e_plain = rel(from_dev(dC1, m), truth), rel(from_dev(dC2, m), truth)
-    # tuned against the S = 12 reference, judged here against Dot2: same order as plain
+    # tuned against the S = 12 reference, checked here against Dot2: same order as plain
     assert e_tuned[0] <= 4 * e_plain[0] and e_tuned[1] <= 4 * e_plain[1], (S, e_tuned, e_plain)
     g.tune_cache_clear()
 
