@@ -486,10 +486,13 @@ def run_ours(args, torch, rank, world):
                      "chosen": form_name},
         "clocks": clocks,
         # per step: the split (both operands in one launch) and the GEMM; the
-        # two-pass forms add one max |.| launch (both operands, exponents by
-        # its last CTA); the CRT form adds the reconstruction
-        "gpu_launches": args.steps * ({"bf16x": 2, "ozaki": 3, "crt": 4}[form] +
-                                      (1 if form == "bf16x" and eff == g.FP16X3 else 0)),
+        # Ozaki form adds one max |.| launch (both operands, exponents by its
+        # last CTA), the CRT form also the reconstruction; the scaled FP16
+        # form's prepare as fp16x3_prepare_launches counts it
+        "gpu_launches": args.steps * (
+            1 + fp16x3_prepare_launches(w["ta"], w["tb"], k)
+            if form == "bf16x" and eff == g.FP16X3
+            else {"bf16x": 2, "ozaki": 3, "crt": 4}[form]),
     }
     if rank == 0:
         line["cpu_baseline"] = (cpu_baseline(w, args.cpu_seconds) if not args.no_cpu
@@ -744,9 +747,11 @@ def run_complex(args, torch, rank, world):
                      "split": {q: {"max_rel": e[0], "fro_rel": e[1]} for q, e in errs.items()},
                      "chosen": form_name},
         "clocks": clocks,
-        # per step: the operand embedding, then the form's own kernels
+        # per step: the operand embedding, then the form's own kernels (the
+        # embedded real problem is NN with 2k)
         "gpu_launches": args.steps * (1 + (4 if method == g.CPLX_CRT else 3 if p == "z" else
-                                           3 if param == g.FP16X3 else 2)),
+                                           1 + fp16x3_prepare_launches("N", "N", 2 * k)
+                                           if param == g.FP16X3 else 2)),
     }
     if rank == 0:
         line["cpu_baseline"] = (cpu_baseline_complex(w, args.cpu_seconds) if not args.no_cpu
@@ -902,6 +907,19 @@ def run_grouped(args, torch, rank, world):
     if rank == 0:
         line["cpu_baseline"] = {"value": None, "skipped": "grouped workload"}
         print(json.dumps(line), flush=True)
+
+
+def fp16x3_prepare_launches(ta, tb, k):
+    """Kernel launches of the scaled 3xFP16 prepare: k-contiguous operands (op(A)
+    rows when A is transposed, op(B) columns when B is not) take the fused max
+    pass and split when 1024 <= k and k rounded up to 64 is at most 16384; the
+    others a max pass and a tile split.  Each kind is one launch for both
+    operands."""
+    fusable = k >= 1024 and (k + 63) // 64 * 64 <= 16384
+    fa, fb = fusable and ta != "N", fusable and tb == "N"
+    if fa and fb:
+        return 1
+    return 3 if (fa or fb) else 2
 
 
 def transfer_note(form):
