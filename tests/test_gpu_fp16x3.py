@@ -209,7 +209,7 @@ def test_pair_and_multicast_modes_agree(orc, products, tile):
     assert g.device_error() == 0
 
 
-@pytest.mark.parametrize("k", [1100, 2048, 4500])
+@pytest.mark.parametrize("k", [1027, 1100, 2048, 4500])
 @pytest.mark.parametrize("ta,tb,pad", [("T", "N", 0), ("T", "N", 1), ("T", "T", 4), ("N", "N", 1)])
 def test_fused_row_split_bitexact(orc, k, ta, tb, pad):
     """k >= 1024 with k-contiguous rows: the fused max pass and split (both
