@@ -182,22 +182,12 @@ struct RowSplitArgs {
 };
 
 template <int VPT>
-__global__ void __launch_bounds__(256) f16_row_split_kernel(const __grid_constant__ RowSplitArgs p) {
-  const int z = blockIdx.z + p.zbase;
-  const int R = z ? p.R1 : p.R0, Rp = z ? p.Rp1 : p.Rp0;
-  const int row = blockIdx.x;
-  if (row >= Rp) return;  // the other operand has more rows (uniform per CTA)
-  const float *__restrict__ X = (z ? p.X1 : p.X0) + (int64_t)row * (z ? p.ld1 : p.ld0);
-  const SegMap &seg = z ? p.seg1 : p.seg0;
-  const int K = p.K, Kp = p.Kp, t = threadIdx.x;
-  // value 4 j + q of this thread is element 1024 j + 4 t + q: a warp reads and
-  // writes contiguous runs
-  float v[VPT];
-  const bool live = row < R;
+__device__ __forceinline__ void row_load(const float *__restrict__ X, int K, bool live, bool vec,
+                                         int t, float (&v)[VPT]) {
 #pragma unroll
   for (int j = 0; j < VPT / 4; ++j) {
     const int e0 = 1024 * j + 4 * t;
-    if (live && p.vec && e0 + 3 < K) {
+    if (live && vec && e0 + 3 < K) {
       const float4 f = *reinterpret_cast<const float4 *>(X + e0);
       v[4 * j] = f.x; v[4 * j + 1] = f.y; v[4 * j + 2] = f.z; v[4 * j + 3] = f.w;
     } else {
@@ -205,44 +195,73 @@ __global__ void __launch_bounds__(256) f16_row_split_kernel(const __grid_constan
       for (int q = 0; q < 4; ++q) v[4 * j + q] = (live && e0 + q < K) ? X[e0 + q] : 0.0f;
     }
   }
-  // max |x| as a bit pattern (NaN and Inf above every finite value)
-  unsigned mx = 0;
+}
+
+// Persistent over rows blockIdx.x, + gridDim.x, ...: the next row's loads are
+// issued before the current row is reduced and written, so each CTA keeps
+// reads in flight while it stores.
+template <int VPT>
+__global__ void __launch_bounds__(256) f16_row_split_kernel(const __grid_constant__ RowSplitArgs p) {
+  const int z = blockIdx.z + p.zbase;
+  const int R = z ? p.R1 : p.R0, Rp = z ? p.Rp1 : p.Rp0;
+  const int ld = z ? p.ld1 : p.ld0;
+  const float *__restrict__ X0 = z ? p.X1 : p.X0;
+  int *__restrict__ exo = z ? p.ex1 : p.ex0;
+  __nv_bfloat16 *__restrict__ out0 = z ? p.out1 : p.out0;
+  const SegMap &seg = z ? p.seg1 : p.seg0;
+  const int K = p.K, Kp = p.Kp, t = threadIdx.x;
+  const bool vec = p.vec != 0;
+  __shared__ unsigned wmax[2][8];  // by row parity: a fast warp may start the next row
+  int row = blockIdx.x;
+  if (row >= Rp) return;  // the other operand has more rows (uniform per CTA)
+  // value 4 j + q of this thread is element 1024 j + 4 t + q: a warp reads and
+  // writes contiguous runs
+  float v[VPT], nv[VPT];
+  row_load<VPT>(X0 + (int64_t)row * ld, K, row < R, vec, t, v);
+  for (int it = 0; row < Rp; row += gridDim.x, ++it) {
+    const int next = row + gridDim.x;
+    if (next < Rp) row_load<VPT>(X0 + (int64_t)next * ld, K, next < R, vec, t, nv);
+    const bool live = row < R;
+    // max |x| as a bit pattern (NaN and Inf above every finite value)
+    unsigned mx = 0;
 #pragma unroll
-  for (int i = 0; i < VPT; ++i) mx = max(mx, __float_as_uint(fabsf(v[i])));
+    for (int i = 0; i < VPT; ++i) mx = max(mx, __float_as_uint(fabsf(v[i])));
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  __shared__ unsigned wmax[8];
-  if ((t & 31) == 0) wmax[t >> 5] = mx;
-  __syncthreads();
-  mx = wmax[0];
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((t & 31) == 0) wmax[it & 1][t >> 5] = mx;
+    __syncthreads();
+    mx = wmax[it & 1][0];
 #pragma unroll
-  for (int w = 1; w < 8; ++w) mx = max(mx, wmax[w]);
-  const int e = live ? row_exponent_f32(mx) : 0;
-  if (t == 0) (z ? p.ex1 : p.ex0)[row] = e;
-  __nv_bfloat16 *out = (z ? p.out1 : p.out0) + (int64_t)row * p.ldo;
-  const bool bad = e == kNonFiniteExp;  // a row of Inf / NaN: all terms NaN
+    for (int w = 1; w < 8; ++w) mx = max(mx, wmax[it & 1][w]);
+    const int e = live ? row_exponent_f32(mx) : 0;
+    if (t == 0) exo[row] = e;
+    __nv_bfloat16 *out = out0 + (int64_t)row * p.ldo;
+    const bool bad = e == kNonFiniteExp;  // a row of Inf / NaN: all terms NaN
 #pragma unroll
-  for (int j = 0; j < VPT / 4; ++j) {
-    const int e0 = 1024 * j + 4 * t;
-    if (e0 >= Kp) continue;  // Kp is a multiple of 64: e0 < Kp covers e0 + 3
-    uint2 w0, w1, w2;  // hi, lo and the zero term of the 4 values
-    if (bad) {
-      w0 = w1 = w2 = make_uint2(0x7e007e00u, 0x7e007e00u);
-    } else {
-      unsigned short h[4], l[4];
+    for (int j = 0; j < VPT / 4; ++j) {
+      const int e0 = 1024 * j + 4 * t;
+      if (e0 >= Kp) continue;  // Kp is a multiple of 64: e0 < Kp covers e0 + 3
+      uint2 w0, w1, w2;  // hi, lo and the zero term of the 4 values
+      if (bad) {
+        w0 = w1 = w2 = make_uint2(0x7e007e00u, 0x7e007e00u);
+      } else {
+        unsigned short h[4], l[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) f16_terms(v[4 * j + q], 15 - e, h[q], l[q]);
-      w0 = make_uint2((unsigned)h[0] | ((unsigned)h[1] << 16),
-                      (unsigned)h[2] | ((unsigned)h[3] << 16));
-      w1 = make_uint2((unsigned)l[0] | ((unsigned)l[1] << 16),
-                      (unsigned)l[2] | ((unsigned)l[3] << 16));
-      w2 = make_uint2(0u, 0u);
+        for (int q = 0; q < 4; ++q) f16_terms(v[4 * j + q], 15 - e, h[q], l[q]);
+        w0 = make_uint2((unsigned)h[0] | ((unsigned)h[1] << 16),
+                        (unsigned)h[2] | ((unsigned)h[3] << 16));
+        w1 = make_uint2((unsigned)l[0] | ((unsigned)l[1] << 16),
+                        (unsigned)l[2] | ((unsigned)l[3] << 16));
+        w2 = make_uint2(0u, 0u);
+      }
+#pragma unroll
+      for (int sg = 0; sg < 3; ++sg) {  // the scaled FP16 form has 3 segments
+        const int ti = seg.term[sg];
+        *reinterpret_cast<uint2 *>(out + (int64_t)sg * Kp + e0) = ti == 0 ? w0 : ti == 1 ? w1 : w2;
+      }
     }
 #pragma unroll
-    for (int sg = 0; sg < 3; ++sg) {  // the scaled FP16 form has 3 segments
-      const int ti = seg.term[sg];
-      *reinterpret_cast<uint2 *>(out + (int64_t)sg * Kp + e0) = ti == 0 ? w0 : ti == 1 ? w1 : w2;
-    }
+    for (int i = 0; i < VPT; ++i) v[i] = nv[i];
   }
 }
 
@@ -256,9 +275,12 @@ static int row_split_vpt(int k) {
   return 0;
 }
 
+static int sm_count();
 static void row_split_launch(const RowSplitArgs &a, int vpt, unsigned rows, unsigned nz,
                              cudaStream_t st) {
-  const dim3 grid(rows, 1, nz);
+  // persistent CTAs: 4 per SM per operand (each holds two rows in registers)
+  const unsigned ctas = (unsigned)sm_count() * 4u;
+  const dim3 grid(rows < ctas ? rows : ctas, 1, nz);
   switch (vpt) {
     case 4: f16_row_split_kernel<4><<<grid, 256, 0, st>>>(a); break;
     case 8: f16_row_split_kernel<8><<<grid, 256, 0, st>>>(a); break;
