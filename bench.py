@@ -274,7 +274,7 @@ def run_ours(args, torch, rank, world):
             _, tp, tc = g.tune_lookup(g.TUNE_BF16X, m, n, k)
             _, tile, mode = g.tune_layout(g.TUNE_BF16X, m, n, k)
             tuned = {"products": tp, "chunk": tc, "tile_n": tile,
-                     "cluster": "pair MMAs" if mode == 1 else "multicast B"}
+                     "cluster": "pair MMAs" if mode == 1 else "one CTA per tile"}
             schemes.append(("bf16x", [0]))
     errs, qualified = {}, []
     ws = None
@@ -293,7 +293,7 @@ def run_ours(args, torch, rank, world):
         if f == "bf16x" and prm == 0 and tuned:
             base = "fp16x3" if tuned["products"] == g.FP16X3 else "bf16x%d" % tuned["products"]
             return "tuned:%s_c%d_t%d_%s" % (base, tuned["chunk"], tuned["tile_n"],
-                                            "pair" if tuned["cluster"] == "pair MMAs" else "mc")
+                                            "pair" if tuned["cluster"] == "pair MMAs" else "cta")
         if f == "bf16x" and prm == g.FP16X3:
             return "fp16x3"
         return {"bf16x": "bf16x%d", "ozaki": "ozaki_s%d", "crt": "crt_n%d"}[f] % prm
@@ -511,7 +511,7 @@ def parse_form(name):
     'fp16x3' -> ('bf16x', FP16X3) (the scaled FP16 form shares the BF16xP entry points).
     A tuned name such as 'tuned:fp16x3_c8_t256_pair' (or without 'tuned:') pins
     the layout the autotuner chose: hi*hi chunk length (_cN), tile width (_tN)
-    and cluster mode (_pair / _mc) are set as the library's tuning knobs."""
+    and cluster mode (_pair: pair MMAs, _cta: one CTA per tile) are set as the library's tuning knobs."""
     import gemm_avx2_gb300 as g
 
     name = name[len("tuned:"):] if name.startswith("tuned:") else name
@@ -521,7 +521,7 @@ def parse_form(name):
             g.tune_param(g.TUNE_BF16X_CHUNK, int(o[1:]))
         elif o[:1] == "t" and o[1:].isdigit():
             assert g.tune_param(g.TUNE_TILE_N, int(o[1:])) == g.OK
-        elif o in ("pair", "mc"):
+        elif o in ("pair", "cta"):
             g.tune_param(g.TUNE_PAIR_MMA, 1 if o == "pair" else 2)
         else:
             raise SystemExit("--form: unknown option %r in %r" % (o, name))
@@ -531,7 +531,7 @@ def parse_form(name):
         if base.startswith(prefix) and base[len(prefix):].isdigit():
             return form, int(base[len(prefix):])
     raise SystemExit("--form: expected crt_nN, ozaki_sS, bf16xP or fp16x3 (optionally with "
-                     "_cN, _tN, _pair or _mc), got %r" % name)
+                     "_cN, _tN, _pair or _cta), got %r" % name)
 
 
 # ----------------------------------------------------------------------------- complex workloads
@@ -1123,7 +1123,7 @@ def main():
     ap.add_argument("--form", default=None,
                     help="use this split form instead of timing the qualifying ones "
                          "(crt_nN, ozaki_sS, bf16xP, fp16x3, optionally with _cN chunk, _tN "
-                         "tile width, _pair / _mc cluster mode; profiling runs)")
+                         "tile width, _pair / _cta cluster mode; profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -1143,14 +1143,25 @@ GB300_API int gb300_strmm(char side, char uplo, char transa, char diag, int m, i
   return tr_api<float>(0, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, form, stream);
 }
 
+// Reads the per-device word and the no-allocation entry point's word without
+// allocating either: a device on which no kernel has run yet has no error.
 GB300_API unsigned gb300_device_error(int clear) {
-  unsigned *err = device_error_word();
-  if (!err) return 0xFFFFFFFFu;
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) return 0xFFFFFFFFu;
+  unsigned *err = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    err = g_dev[d].err;
+  }
   unsigned w = 0;
-  if (cudaMemcpy(&w, err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess)
-    return 0xFFFFFFFFu;
-  if (clear) cudaMemset(err, 0, sizeof(unsigned));
-  return w;
+  if (err) {
+    if (cudaMemcpy(&w, err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return 0xFFFFFFFFu;
+    if (clear && w && cudaMemset(err, 0, sizeof(unsigned)) != cudaSuccess) return 0xFFFFFFFFu;
+  }
+  unsigned wn = 0;
+  if (noalloc_error_read(clear, &wn) != GB300_OK) return 0xFFFFFFFFu;
+  return w ? w : wn;
 }
 
 GB300_API int gb300_selftest_wait_timeout(unsigned poll_limit) {
@@ -1194,8 +1205,9 @@ GB300_API int gb300_tune_layout(int kind, int m, int n, int k, int *tile_n, int 
   if (kind < 0 || kind > 2) return GB300_ERR_ARG;
   if (tile_n) *tile_n = split_tile_n(kind, m, n, k);
   if (pair_mma) {
-    const int v = kind == 0 ? tune_pair_mma(kind, m, n, k) : 0;
-    *pair_mma = v ? v : 2;
+    const int o = pair_mma_override();
+    const int v = o ? o : tune_pair_mma(kind, m, n, k);
+    *pair_mma = v ? v : 1;
   }
   return tune_lookup(kind, m, n, k, nullptr, nullptr) ? GB300_OK : GB300_ERR_UNSUPPORTED;
 }

@@ -7,8 +7,8 @@
 //   split SGEMM : products P in {3, 6} (BF16 terms) or the scaled 3xFP16
 //                 form, x hi*hi chunk length in {2, 4, 8};
 //   all forms   : then the output tile width (128 / 256) of the chosen one,
-//                 and for the split SGEMM its cluster mode (pair MMAs or
-//                 multicast B tile);
+//                 and its cluster mode (pair MMAs on 2-CTA clusters or one
+//                 CTA per tile);
 //   Ozaki DGEMM : slice count S in [4, 12].
 //
 // A candidate qualifies when its max and Frobenius relative errors against a
@@ -46,7 +46,7 @@ struct TuneEntry {
   int param = 0;       // products (BF16xP) or slices (Ozaki)
   int chunk = 0;       // BF16xP hi*hi chunk length (0 for Ozaki)
   int tile = 0;        // output tile width of the GEMM (128 / 256; 0 = by shape)
-  int pair = 0;        // BF16xP cluster mode (1 pair MMAs, 2 multicast; 0 = default)
+  int pair = 0;        // cluster mode (1 pair MMAs, 2 one CTA per tile; 0 = default)
   double ms = 0;       // measured time of the chosen candidate
   double err_max = 0, err_fro = 0;              // chosen candidate vs reference
   double plain_max = 0, plain_fro = 0;          // plain kernel vs reference
@@ -316,8 +316,8 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
     best.tile = t128 < t256 ? 128 : 256;
     best.ms = t128 < t256 ? t128 : t256;
   }
-  // the BF16xP GEMM's cluster mode at that width (same results bit for bit)
-  if (kind == 0) {
+  // the tensor-core GEMM's cluster mode at that width (same results bit for bit)
+  {
     const int user_tile = split_tile_override(), user_pair = pair_mma_override();
     double tp = 0, tm = 0;
     set_split_tile_n(best.tile);

@@ -147,16 +147,6 @@ __device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(p)), "r"(rank));
   return a;
 }
-// TMA load of one box into the same shared-memory offset of every CTA in
-// `mask` (this cluster only), signalling the mbarrier at the same offset in each.
-__device__ __forceinline__ void tma_load_2d_mc(void *smem_dst, const void *tmap, int32_t x,
-                                               int32_t y, uint64_t *bar, uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      ".multicast::cluster [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(smem_dst)),
-      "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
-      : "memory");
-}
 __device__ __forceinline__ uint32_t cluster_ctarank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -275,7 +265,6 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
           smem_u32(bar))
       : "memory");
 }
-// Commit that arrives on the mbarrier at the same offset in every CTA of `mask`.
 // Pair MMA (cta_group::2, issued by one thread of the even CTA of the
 // cluster): M = 256 rows, each CTA supplying its 128 rows of A and half of
 // the N columns of B from the same shared-memory offsets; each CTA's TMEM
@@ -289,16 +278,12 @@ __device__ __forceinline__ void umma_pair(uint32_t d_tmem, uint64_t adesc, uint6
       : "memory");
 }
 // Arrive once on `bar` in every CTA of `mask` when the pair MMAs issued so far
-// by this thread complete.
+// by this thread complete.  This signals mbarriers only; no data is moved
+// (every TMA load of the library is a plain or cta_group::2 tile load into the
+// issuing CTA's own shared memory).
 __device__ __forceinline__ void umma_commit_pair(uint64_t *bar, uint16_t mask) {
   asm volatile(
       "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
-      "[%0], %1;" ::"r"(smem_u32(bar)), "h"(mask)
-      : "memory");
-}
-__device__ __forceinline__ void umma_commit_mc(uint64_t *bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
       "[%0], %1;" ::"r"(smem_u32(bar)), "h"(mask)
       : "memory");
 }

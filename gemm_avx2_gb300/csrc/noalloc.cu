@@ -60,6 +60,29 @@ int noalloc_setup(NoAllocSlot **out) {
 }
 }  // namespace
 
+// The error word of the no-allocation entry point on the current device: 0
+// if no call has set up this device yet.  Reads it (and, with `clear`, zeroes
+// it) through the symbol, so nothing is allocated.
+int noalloc_error_read(int clear, unsigned *out) {
+  *out = 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return GB300_ERR_CUDA;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_slots[dev].ready) return GB300_OK;
+  }
+  unsigned w = 0;
+  if (cudaMemcpyFromSymbol(&w, g_noalloc_error_word, sizeof w) != cudaSuccess)
+    return GB300_ERR_CUDA;
+  if (clear && w) {
+    const unsigned zero = 0;
+    if (cudaMemcpyToSymbol(g_noalloc_error_word, &zero, sizeof zero) != cudaSuccess)
+      return GB300_ERR_CUDA;
+  }
+  *out = w;
+  return GB300_OK;
+}
+
 }  // namespace gb300
 
 using namespace gb300;

@@ -122,7 +122,7 @@ int split_tile_n(int kind, int m, int n, int k);
 void set_split_tile_n(int v);
 int split_tile_override();
 // Cluster mode of the split GEMMs with two or more row tiles: 0 = default,
-// 1 = pair MMAs (cta_group::2), 2 = per-CTA MMAs with the B tile multicast.
+// 1 = pair MMAs (cta_group::2 on 2-CTA clusters), 2 = one CTA per tile.
 void set_pair_mma(int v);
 int pair_mma_override();
 // Work units of the CRT GEMM: 0 = by shape, 1 = whole tiles, 2 = one modulus
@@ -132,7 +132,7 @@ void set_modulus_split(int v);
 void set_modulus_split_hint(int v);
 int modulus_split_override();
 // Tuned tile width (0 = none) and cluster mode (0 = none, 1 = pair MMAs,
-// 2 = multicast) of a shape class.
+// 2 = one CTA per tile) of a shape class.
 int tune_tile_n(int kind, int m, int n, int k);
 int tune_pair_mma(int kind, int m, int n, int k);
 
@@ -144,6 +144,10 @@ void set_bf16x_chunk_kblocks(int c);
 int ozaki_default_slices(int m, int n, int k);
 // Products / chunk of the BF16xP form for a shape class (cache, else 6 / 0).
 void bf16x_resolve(int m, int n, int k, int *products, int *chunk);
+
+// Error word of gb300_sgemm_bf16x_noalloc on the current device (noalloc.cu),
+// read (and with `clear` zeroed) without allocating; 0 before its first call.
+int noalloc_error_read(int clear, unsigned *out);
 
 // Autotuner (autotune.cu): kind 0 = BF16xP SGEMM, 1 = Ozaki DGEMM.
 bool tune_lookup(int kind, int m, int n, int k, int *param, int *chunk);

@@ -507,20 +507,16 @@ struct TileN {
   static constexpr int kCols = BN / 4;
 };
 
-// MC: 2-CTA clusters on the row tiles 2u and 2u + 1 of one column tile, in
-// lockstep over the same unit sequence; each CTA loads its own A tile and half
-// of the shared B tile, multicast into both CTAs' stage (the B tensor map's box
-// is then 128 rows).  Each stage's empty barrier counts both CTAs' MMA commits,
-// since a stage holds data its peer wrote.  This halves the B tile's L2 reads.
-// Cluster modes of the tile kernels: 0 = one CTA per tile; 1 = 2-CTA
-// clusters, each CTA's own MMAs (cta_group::1) on the B tile it shares with
-// its peer by TMA multicast; 2 = pair MMAs (cta_group::2, M = 256): each CTA
-// holds its 128 rows of A and half of B, the even CTA issues the MMAs for
-// both, so a stage is 32 KB instead of 48 KB and the ring 6 deep instead of 4.
-// In mode 2 both CTAs' TMA loads complete on the even CTA's full barrier,
-// and the odd CTA's epilogue warps report drained TMEM buffers to the even
-// CTA with plain (default-semantics) remote arrives: cluster-scope release
-// arrives made the kernel 2.5x slower.
+// Cluster modes of the tile kernels: 0 = one CTA per tile, loading its own A
+// and B tiles; 2 = pair MMAs (cta_group::2, M = 256) on 2-CTA clusters over
+// the row tiles 2u and 2u + 1 of one column tile: each CTA holds its 128 rows
+// of A and half of the B tile, the even CTA issues the MMAs for both, so a
+// stage is 32 KB instead of 48 KB, the ring is 6 deep instead of 4, and each
+// B tile is read from L2 once per pair.  In mode 2 both CTAs' TMA loads
+// complete on the even CTA's full barrier, and the odd CTA's epilogue warps
+// report drained TMEM buffers to the even CTA with plain (default-semantics)
+// remote arrives: cluster-scope release arrives made the kernel 2.5x slower.
+// Every TMA load lands in the issuing CTA's own shared memory.
 template <int CL, int BN>
 struct ClusterTile {
   static constexpr bool kPair = CL == 2;
@@ -536,8 +532,9 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                   Bf16xParams p) {
   using T = TileN<BN>;
   using CT = ClusterTile<CL, BN>;
-  constexpr bool MC = CL != 0, PAIR = CT::kPair;
-  constexpr int kBxStages = CT::kStages, kBxStage = CT::kStage, kBxBBytes = CT::kBBytes;
+  static_assert(CL == 0 || CL == 2, "cluster modes: 0 (one CTA per tile) or 2 (pair MMAs)");
+  constexpr bool PAIR = CT::kPair;
+  constexpr int kBxStages = CT::kStages, kBxStage = CT::kStage;
   constexpr int kBxColsPerWarp = T::kCols;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -554,7 +551,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   if (threadIdx.x == 0) {
     for (int s = 0; s < kBxStages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], CL == 1 ? 2 : 1);  // multicast: both CTAs' commits; pair: one
+      mbar_init(&empty[s], 1);  // pair: one multicast commit frees both CTAs' stage
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf[b], 1);
@@ -572,19 +569,19 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   }
   tc_fence_before();
   __syncthreads();
-  if (MC) cluster_sync();  // the peer's barriers are initialised before any remote arrive
+  if (PAIR) cluster_sync();  // the peer's barriers are initialised before any remote arrive
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  // work units: tiles, or (MC) row-tile pairs whose rank-th row tile is this CTA's
-  const uint32_t rank = MC ? cluster_ctarank() : 0u;
-  const int pm = MC ? (p.tiles_m + 1) / 2 : p.tiles_m;
+  // work units: tiles, or (PAIR) row-tile pairs whose rank-th row tile is this CTA's
+  const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
+  const int pm = PAIR ? (p.tiles_m + 1) / 2 : p.tiles_m;
   const int nunits = pm * p.tiles_n;
-  const int first = MC ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
-  const int stride = MC ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+  const int first = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+  const int stride = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
   auto unit_tile = [&](int u, int &tm, int &tn) {
     int um;
-    tile_coords(u, pm, p.tiles_n, MC ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
-    tm = MC ? 2 * um + (int)rank : um;  // MC: a row tile past the end is zero-filled, not stored
+    tile_coords(u, pm, p.tiles_n, PAIR ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
+    tm = PAIR ? 2 * um + (int)rank : um;  // PAIR: a row tile past the end is zero-filled, not stored
   };
   auto run_end = [&](int r) { return r == 0 ? p.run_end0 : (r == 1 ? p.run_end1 : p.run_end2); };
   auto run_chunk = [&](int r) {  // chunk length of run r in K blocks
@@ -618,13 +615,9 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                              fb);
             continue;
           }
-          mbar_arrive_expect_tx(&full[s], kBxStage);  // own A and B rows (both B halves: MC)
+          mbar_arrive_expect_tx(&full[s], kBxStage);  // own A and B tiles
           tma_load_2d(sa, &tmA, kb * kSplitBK, tm * kSplitBM, &full[s]);
-          if (MC)
-            tma_load_2d_mc(sa + kBxABytes + rank * (kBxBBytes / 2), &tmB, kb * kSplitBK,
-                           tn * BN + (int)rank * (BN / 2), &full[s], 0x3);
-          else
-            tma_load_2d(sa + kBxABytes, &tmB, kb * kSplitBK, tn * BN, &full[s]);
+          tma_load_2d(sa + kBxABytes, &tmB, kb * kSplitBK, tn * BN, &full[s]);
         }
       }
     }
@@ -671,8 +664,6 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             }
             if (PAIR)
               umma_commit_pair(&empty[s], 0x3);  // both CTAs' stage s is free
-            else if (MC)
-              umma_commit_mc(&empty[s], 0x3);  // the stage is free once both CTAs are done
             else
               umma_commit(&empty[s]);
           }
@@ -773,7 +764,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     else
       tmem_dealloc(tmem, 512);
   }
-  if (MC) cluster_sync();  // no peer multicast, commit or arrive can still target this CTA
+  if (PAIR) cluster_sync();  // no peer commit or arrive can still target this CTA
 }
 
 // ===========================================================================
@@ -840,15 +831,21 @@ __device__ __forceinline__ void group_of(int mode, int gi, int S, int &t, int &l
 // 64 * 1024 * 127^2 < 2^31.
 constexpr int kCrtRunChunks = 64;
 
-// MC: 2-CTA clusters sharing the B tile, as in bf16x_gemm_kernel.  A row tile
+// CL: the cluster mode of bf16x_gemm_kernel (0: one CTA per tile; 2: pair
+// MMAs over the row tiles 2u and 2u + 1, each CTA loading its A tile and half
+// of the B tile, the even CTA issuing the MMAs of both).  In mode 2 a row tile
 // past the end (odd tile rows) still takes part in the pipeline (its A loads
-// fetch rows of the next block and its sums are discarded) but writes nothing.
-template <bool MC, int BN>
+// fetch rows of the next block, or zeros past the last, and its sums are
+// discarded) but writes nothing.
+template <int CL, int BN>
 __global__ void __launch_bounds__(kOzThreads, 1)
 ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   OzakiParams p) {
   using T = TileN<BN>;
-  constexpr int kOzStages = T::kStages, kOzStage = T::kStage, kOzBBytes = T::kBBytes;
+  using CT = ClusterTile<CL, BN>;
+  static_assert(CL == 0 || CL == 2, "cluster modes: 0 (one CTA per tile) or 2 (pair MMAs)");
+  constexpr bool PAIR = CT::kPair;
+  constexpr int kOzStages = CT::kStages, kOzStage = CT::kStage;
   constexpr int kOzCols = T::kCols;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -863,34 +860,40 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kOzStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], MC ? 2 : 1); }
-    for (int b = 0; b < 2; ++b) { mbar_init(&accf[b], 1); mbar_init(&acce[b], kOzEpiWarps); }
+    for (int s = 0; s < kOzStages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], PAIR ? 2 * kOzEpiWarps : kOzEpiWarps);  // pair: both CTAs drain
+    }
     mbar_init(done, 1);
     *abort_flag = 0;
     fence_barrier_init();
     tma_prefetch_desc(&tmA);
     tma_prefetch_desc(&tmB);
   }
-  if (warp == 1) { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
+  if (warp == 1) {
+    if (PAIR) { tmem_alloc_pair(tmem_slot, 512); tmem_relinquish_pair(); }
+    else { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
+  }
   tc_fence_before();
   __syncthreads();
-  if (MC) cluster_sync();  // the peer's barriers are initialised before any multicast
+  if (PAIR) cluster_sync();  // the peer's barriers are initialised before any remote arrive
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const int S = p.S, KB = p.KB;
-  // work units: tiles, or (MC) row-tile pairs whose rank-th row tile is this CTA's
-  const uint32_t rank = MC ? cluster_ctarank() : 0u;
-  const int pm = MC ? (p.tiles_m + 1) / 2 : p.tiles_m;
+  // work units: tiles, or (PAIR) row-tile pairs whose rank-th row tile is this CTA's
+  const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
+  const int pm = PAIR ? (p.tiles_m + 1) / 2 : p.tiles_m;
   // units: (group range, tile), group-range major so that neighbouring units
   // share the residue planes of their moduli in L2
   const int ntu = pm * p.tiles_n;
   const int nunits = ntu * p.gsplit;
-  const int first = MC ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
-  const int stride = MC ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+  const int first = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+  const int stride = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
   auto unit_tile = [&](int u, int &tm, int &tn) {
     int um;
-    tile_coords(u % ntu, pm, p.tiles_n, MC ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
-    tm = MC ? 2 * um + (int)rank : um;
+    tile_coords(u % ntu, pm, p.tiles_n, PAIR ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
+    tm = PAIR ? 2 * um + (int)rank : um;
   };
   auto unit_groups = [&](int u, int &g0, int &g1) {
     const int gp = u / ntu;
@@ -919,23 +922,29 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               break;
             }
             uint8_t *sa_ptr = smem + s * kOzStage;
+            const int arow = (sa - 1) * p.Mp + p.row0 + tm * kSplitBM;
+            if (PAIR) {
+              // both CTAs' A rows and B halves land on the even CTA's full barrier
+              if (rank == 0) mbar_arrive_expect_tx(&full[s], 2 * kOzStage);
+              const uint32_t fb = cluster_addr(&full[s], 0);
+              tma_load_2d_pair(sa_ptr, &tmA, kb * kSplitBK, arow, fb);
+              tma_load_2d_pair(sa_ptr + kOzABytes, &tmB, kb * kSplitBK,
+                               (sb - 1) * p.Np + p.col0 + tn * BN + (int)rank * (BN / 2), fb);
+              continue;
+            }
             mbar_arrive_expect_tx(&full[s], kOzStage);
-            tma_load_2d(sa_ptr, &tmA, kb * kSplitBK, (sa - 1) * p.Mp + p.row0 + tm * kSplitBM,
-                        &full[s]);
-            if (MC)
-              tma_load_2d_mc(sa_ptr + kOzABytes + rank * (kOzBBytes / 2), &tmB, kb * kSplitBK,
-                             (sb - 1) * p.Np + p.col0 + tn * BN + (int)rank * (BN / 2),
-                             &full[s], 0x3);
-            else
-              tma_load_2d(sa_ptr + kOzABytes, &tmB, kb * kSplitBK,
-                          (sb - 1) * p.Np + p.col0 + tn * BN, &full[s]);
+            tma_load_2d(sa_ptr, &tmA, kb * kSplitBK, arow, &full[s]);
+            tma_load_2d(sa_ptr + kOzABytes, &tmB, kb * kSplitBK,
+                        (sb - 1) * p.Np + p.col0 + tn * BN, &full[s]);
           }
         }
       }
     }
+  } else if (warp == 1 && PAIR && rank == 1) {
+    // odd CTA of a pair: the even CTA issues the MMAs of both
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16_f32(kSplitBM, BN);
+      constexpr uint32_t idesc = idesc_bf16_f32(PAIR ? 2 * kSplitBM : kSplitBM, BN);
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
@@ -965,19 +974,33 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               tc_fence_after();
               const uint32_t sa = smem_u32(smem + s * kOzStage), sb = sa + kOzABytes;
 #pragma unroll
-              for (int kk = 0; kk < kSplitBK / 16; ++kk)
-                umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32), idesc,
-                          (idx > c0 || kk > 0) ? 1u : 0u);
-              if (MC)
-                umma_commit_mc(&empty[s], 0x3);  // the stage is free once both CTAs are done
+              for (int kk = 0; kk < kSplitBK / 16; ++kk) {
+                if (PAIR)
+                  umma_pair(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32),
+                            idesc, (idx > c0 || kk > 0) ? 1u : 0u);
+                else
+                  umma_bf16(dt, umma_desc_sw128(sa + kk * 32), umma_desc_sw128(sb + kk * 32),
+                            idesc, (idx > c0 || kk > 0) ? 1u : 0u);
+              }
+              if (PAIR)
+                umma_commit_pair(&empty[s], 0x3);  // both CTAs' stage s is free
               else
                 umma_commit(&empty[s]);
             }
-            if (ok) umma_commit(&accf[b]);
+            if (ok) {
+              if (PAIR)
+                umma_commit_pair(&accf[b], 0x3);
+              else
+                umma_commit(&accf[b]);
+            }
           }
         }
       }
-      umma_commit(done);
+      // every issued MMA has completed before TMEM is released
+      if (PAIR)
+        umma_commit_pair(done, 0x1);
+      else
+        umma_commit(done);
       mbar_wait(done, 0, p.err, kErrTimeoutMma, nullptr);
     }
   } else {
@@ -992,7 +1015,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       int tm, tn, g0, g1;
       unit_tile(u, tm, tn);
       unit_groups(u, g0, g1);
-      const bool real = tm < p.tiles_m;  // MC: a row tile past the end writes nothing
+      const bool real = tm < p.tiles_m;  // PAIR: a row tile past the end writes nothing
       const int row = tm * kSplitBM + row_in_tile;          // < Mp when real
       const int col0 = tn * BN + h * kOzCols;          // first of this warp's columns
       double *res = p.res + (int64_t)col0 * p.Mp + row;      // res[j * Mp] is column col0 + j
@@ -1025,7 +1048,12 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           }
           tc_fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&acce[b]);
+          if (lane == 0) {
+            if (PAIR)
+              mbar_arrive_cluster<false>(&acce[b], 0);  // the even CTA issues the MMAs of both
+            else
+              mbar_arrive(&acce[b]);
+          }
           const bool last = (c == nch - 1);
           if (p.mode && (++since_fold == run_limit || last)) {
             // CRT form: reduce the exact sums mod p; at the modulus' end store
@@ -1096,11 +1124,15 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   }
   tc_fence_before();
   __syncthreads();
+  if (PAIR) cluster_sync();  // both CTAs are done with the pair's TMEM
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, 512);
+    if (PAIR)
+      tmem_dealloc_pair(tmem, 512);
+    else
+      tmem_dealloc(tmem, 512);
   }
-  if (MC) cluster_sync();  // no peer multicast or commit can still target this CTA
+  if (PAIR) cluster_sync();  // no peer commit or arrive can still target this CTA
 }
 
 // ===========================================================================
@@ -1397,13 +1429,13 @@ int split_sgemm_prepare_part(int z, char t, int m, int n, int k, const float *X,
 }
 
 // Persistent launch of a tile kernel: one CTA per SM (plain), or 2-CTA
-// clusters sharing the B tile when there are at least two row tiles (mc).
+// clusters running pair MMAs on row-tile pairs (pair).
 template <typename P>
 static int persistent_launch(void (*plain)(const CUtensorMap, const CUtensorMap, P),
                              void (*clustered)(const CUtensorMap, const CUtensorMap, P),
                              int threads, int smem, const CUtensorMap &tA, const CUtensorMap &tB,
-                             const P &p, int tiles_m, int tiles_n, bool mc, cudaStream_t st) {
-  if (!mc) {
+                             const P &p, int tiles_m, int tiles_n, bool pair, cudaStream_t st) {
+  if (!pair) {
     if (cudaFuncSetAttribute(plain, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
         cudaSuccess)
       return GB300_ERR_CUDA;
@@ -1454,13 +1486,12 @@ int split_tile_n(int kind, int m, int n, int k) {
 void set_split_tile_n(int v) { g_tile_n = v; }
 int split_tile_override() { return g_tile_n; }
 
-// Cluster mode of the BF16xP GEMM with two or more row tiles: pair MMAs
-// (kernel mode 2) or per-CTA MMAs on a multicast B tile (mode 1).  Same
-// results bit for bit; neither is faster everywhere (pair: 3-4% faster on
-// SGEMM 8192^3, 5% slower on the 16384 x 8192 x 16384 problem of CGEMM 8192^3
-// under the power cap), so the autotuner times both per shape class.  Order:
-// GB300_TUNE_PAIR_MMA, the tuned mode of the shape class, multicast.
-static int g_pair_mma = 0;  // 0: none, 1: pair MMAs, 2: multicast
+// Cluster mode of the tensor-core GEMMs (BF16xP and Ozaki / CRT) with two or
+// more row tiles: pair MMAs on 2-CTA clusters (kernel mode 2) or one CTA per
+// tile (mode 0).  Same results bit for bit, so the autotuner times both per
+// shape class.  Order: GB300_TUNE_PAIR_MMA, the tuned mode of the shape
+// class, pair MMAs.
+static int g_pair_mma = 0;  // 0: none, 1: pair MMAs, 2: one CTA per tile
 void set_pair_mma(int v) { g_pair_mma = v; }
 int pair_mma_override() { return g_pair_mma; }
 // Work units of the CRT GEMM: 0 = by shape, 1 = whole tiles (all moduli),
@@ -1475,9 +1506,9 @@ void set_modulus_split_hint(int v) { t_modulus_split_hint = v; }
 int modulus_split_override() {
   return g_modulus_split ? g_modulus_split : t_modulus_split_hint;
 }
-static bool use_pair_mma(int m, int n, int k) {
-  const int v = g_pair_mma ? g_pair_mma : tune_pair_mma(0, m, n, k);
-  return v == 1;
+static bool use_pair_mma(int kind, int m, int n, int k) {
+  const int v = g_pair_mma ? g_pair_mma : tune_pair_mma(kind, m, n, k);
+  return v != 2;
 }
 
 // L: the layout of the rows / columns this launch covers; (tm, tn, k): the
@@ -1485,21 +1516,17 @@ static bool use_pair_mma(int m, int n, int k) {
 template <bool F16, int BN>
 static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, int tm, int tn, int k,
                         cudaStream_t st) {
-  const bool mc = L.Mp / kSplitBM >= 2;  // 2-CTA clusters on row-tile pairs
+  // pair MMAs on row-tile pairs (2-CTA clusters) when there are two or more row tiles
+  const bool pair = L.Mp / kSplitBM >= 2 && use_pair_mma(0, tm, tn, k);
   CUtensorMap tA{}, tB{};
   if (!encode_2d(&tA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, mc ? BN / 2 : BN, true))
+      !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, pair ? BN / 2 : BN, true))
     return GB300_ERR_CUDA;
   p.tiles_n = (p.n + BN - 1) / BN;
-  if (mc && use_pair_mma(tm, tn, k))
-    return persistent_launch<Bf16xParams>(bf16x_gemm_kernel<0, F16, BN>,
-                                          bf16x_gemm_kernel<2, F16, BN>, kBxThreads,
-                                          ClusterTile<2, BN>::kSmem, tA, tB, p, p.tiles_m,
-                                          p.tiles_n, true, st);
-  return persistent_launch<Bf16xParams>(bf16x_gemm_kernel<0, F16, BN>,
-                                        bf16x_gemm_kernel<1, F16, BN>, kBxThreads,
-                                        ClusterTile<1, BN>::kSmem, tA, tB, p, p.tiles_m, p.tiles_n,
-                                        mc, st);
+  return persistent_launch<Bf16xParams>(
+      bf16x_gemm_kernel<0, F16, BN>, bf16x_gemm_kernel<2, F16, BN>, kBxThreads,
+      pair ? ClusterTile<2, BN>::kSmem : ClusterTile<0, BN>::kSmem, tA, tB, p, p.tiles_m,
+      p.tiles_n, pair, st);
 }
 
 int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int ldc, int products,
@@ -1677,21 +1704,23 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
 
 template <int BN>
 static int ozaki_launch_bn(const OzakiGemmArgs &a, OzakiParams p, cudaStream_t st) {
-  const bool mc = p.tiles_m >= 2;  // 2-CTA clusters sharing the B tile
+  // pair MMAs on row-tile pairs (2-CTA clusters) when there are two or more row tiles
+  const bool pair = p.tiles_m >= 2 && use_pair_mma(a.mode ? 2 : 1, a.m, a.n, a.k);
   CUtensorMap tA{}, tB{};
   if (!encode_2d(&tA, a.As, 2, a.Kp, a.S * a.Mp, a.Kp, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, mc ? BN / 2 : BN, true))
+      !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, pair ? BN / 2 : BN, true))
     return GB300_ERR_CUDA;
   p.tiles_n = (p.n + BN - 1) / BN;
   // CRT form: one modulus per work unit when the tiles alone fill fewer than
   // four waves (a 2048^2 output has 128 tiles for 152 SMs)
-  const int stride = mc ? sm_count() / 2 : sm_count();
-  const int ntu = (mc ? (p.tiles_m + 1) / 2 : p.tiles_m) * p.tiles_n;
+  const int stride = pair ? sm_count() / 2 : sm_count();
+  const int ntu = (pair ? (p.tiles_m + 1) / 2 : p.tiles_m) * p.tiles_n;
   const int mode = modulus_split_override();
   p.gsplit = !p.mode || mode == 1 ? 1 : (mode == 2 || ntu < 4 * stride) ? p.S : 1;
-  return persistent_launch<OzakiParams>(ozaki_gemm_kernel<false, BN>, ozaki_gemm_kernel<true, BN>,
-                                        kOzThreads, TileN<BN>::kSmem, tA, tB, p, p.tiles_m,
-                                        p.tiles_n * p.gsplit, mc, st);
+  return persistent_launch<OzakiParams>(
+      ozaki_gemm_kernel<0, BN>, ozaki_gemm_kernel<2, BN>, kOzThreads,
+      pair ? ClusterTile<2, BN>::kSmem : ClusterTile<0, BN>::kSmem, tA, tB, p, p.tiles_m,
+      p.tiles_n * p.gsplit, pair, st);
 }
 
 int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {

@@ -133,7 +133,7 @@ int gb300_dgemm_ozaki_ws(char transa, char transb, int m, int n, int k, double a
  * For callers that may not call cudaMalloc/cudaFree: code running under a
  * framework that owns all device memory (a pool or a fixed budget that must
  * not be bypassed) and code on a latency-critical path.  Same arguments and
- * result as gb300_sgemm_bf16x (products 3 or 6), but the scratch is a fixed
+ * result as gb300_sgemm_bf16x (products 3, 6 or GB300_SPLIT_FP16X3), but the scratch is a fixed
  * 32 MiB array that is part of the library's device image (each GPU that loads
  * the library holds it until exit); the call allocates and frees nothing.
  *   - Problems whose scratch (gb300_split_workspace_bytes(0, m, n, k,
@@ -145,8 +145,15 @@ int gb300_dgemm_ozaki_ws(char transa, char transb, int m, int n, int k, double a
  *     GPU (different streams, or different host threads) race on it; order
  *     them on one stream.  Each call writes all the scratch it reads, so no
  *     state carries over from the previous call.
- *   - Kernel time-outs are recorded in a separate error word of this entry
- *     point, not the one gb300_device_error reads. */
+ *   - products may also be GB300_SPLIT_FP16X3 (the scaled FP16 form); its
+ *     scratch includes the row / column scale exponents and is sized by the
+ *     same gb300_split_workspace_bytes(0, m, n, k, GB300_SPLIT_FP16X3).
+ *   - The GEMM runs pair MMAs on 2-CTA clusters when op(A) has more than
+ *     128 rows (the default cluster mode; GB300_TUNE_PAIR_MMA = 2 makes it
+ *     one CTA per tile); every load lands in the issuing CTA's own memory.
+ *   - Kernel time-outs are recorded in an error word of this entry point
+ *     (a static device variable, so no allocation either);
+ *     gb300_device_error reports it after a stream synchronisation. */
 int gb300_sgemm_bf16x_noalloc(char transa, char transb, int m, int n, int k, float alpha,
                               const float *A, int lda, const float *B, int ldb, float beta,
                               float *C, int ldc, int products, void *stream);
@@ -332,8 +339,11 @@ int gb300_dgemm_ozaki2_run(int m, int n, int k, double alpha, double beta, doubl
 size_t gb300_split_workspace_bytes(int kind, int m, int n, int k, int param);
 
 /* After a stream synchronisation: the first error code any kernel of this
- * library recorded on the current device since the last clear (0 = none).
- * Bounded waits that expired record codes 0x10-0x14.  clear != 0 resets it. */
+ * library recorded on the current device since the last clear (0 = none),
+ * including calls of gb300_sgemm_bf16x_noalloc (which keeps its own word;
+ * when both are set the library-wide word's code is returned).  Bounded
+ * waits that expired record codes 0x10-0x14.  clear != 0 resets both words.
+ * Allocates nothing, so callers of the no-allocation entry point can use it. */
 unsigned gb300_device_error(int clear);
 
 /* Failure-detection self-test (no reference counterpart; the reference has no
@@ -364,9 +374,10 @@ int gb300_selftest_wait_timeout(unsigned poll_limit);
 int gb300_autotune(int kind, char transa, char transb, int m, int n, int k, const void *A,
                    int lda, const void *B, int ldb, void *stream, int *chosen);
 int gb300_tune_lookup(int kind, int m, int n, int k, int *param, int *chunk);
-/* The output tile width (128 / 256) and, for kind 0, the cluster mode (1 =
- * pair MMAs, 2 = multicast B tile) the split GEMMs use for this shape (knob,
- * tuned entry or default, in that order); GB300_ERR_UNSUPPORTED when the
+/* The output tile width (128 / 256) and the cluster mode (1 = pair MMAs on
+ * 2-CTA clusters, 2 = one CTA per tile) the split GEMMs use for this shape
+ * (knob, tuned entry or default, in that order; a problem with a single
+ * 128-row tile always runs one CTA per tile); GB300_ERR_UNSUPPORTED when the
  * shape class has no tuned entry. */
 int gb300_tune_layout(int kind, int m, int n, int k, int *tile_n, int *pair_mma);
 int gb300_tune_cache_save(const char *path);
@@ -386,12 +397,13 @@ void gb300_tune_cache_clear(void);
  *   GEMMs of all split forms; 0 restores the choice by shape (the tuned
  *   width of the shape class, else 128 for outputs at most 128 columns wide
  *   and 256 otherwise).
- *   GB300_TUNE_PAIR_MMA: how the BF16xP GEMM runs problems with two or more
- *   128-row tiles: 1 = pair MMAs (tcgen05 cta_group::2: two CTAs compute a
- *   256-row tile, each holding half of the B tile), 2 = one MMA issuer per
- *   CTA with the B tile multicast to both CTAs of the cluster; 0 restores
- *   the default (the tuned mode of the shape class, else multicast).  Both
- *   give the same results bit for bit.
+ *   GB300_TUNE_PAIR_MMA: how the tensor-core GEMMs of all split forms run
+ *   problems with two or more 128-row tiles: 1 = pair MMAs (tcgen05
+ *   cta_group::2: two CTAs of a cluster compute a 256-row tile, each loading
+ *   its A rows and half of the B tile into its own shared memory), 2 = one
+ *   CTA per tile, loading its whole A and B tiles; 0 restores the default
+ *   (the tuned mode of the shape class, else pair MMAs).  Both give the same
+ *   results bit for bit.
  *   GB300_TUNE_HOST_PARTS: operand parts (1..8) of the pipelined host-pointer
  *   path of the FP32 split form and the FP64 CRT form (gb300_host_sgemm_bf16x,
  *   gb300_host_dgemm_ozaki2, the drop-ins with GB300_DROPIN_FORM=split):

@@ -7,12 +7,14 @@
 #   oracle/_ref/libcplx.so - the reference's OpenBLAS-style complex and 3M kernels
 #                         (four conjugation variants each) behind oracle/ref_cplx.c.
 # Usage: oracle/build.sh [reference-source-dir]
+#   (default: $GB300_REFERENCE_SOURCES, else /root/reference, the read-only
+#   checkout of the reference in the build container; absent on GPU hosts)
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 cc=${CC:-gcc}
 $cc -O3 -fopenmp -ffp-contract=off -fno-math-errno -fPIC -shared -fvisibility=hidden \
     -o "$HERE/liborc.so" "$HERE/oracle.c" -lm
-REF=${1:-}
+REF=${1:-${GB300_REFERENCE_SOURCES:-/root/reference}}
 if [ -n "$REF" ] && [ -f "$REF/src/gemm_driver.c" ] && [ "$(uname -m)" = "x86_64" ]; then
   mkdir -p "$HERE/_ref"
   # Same flags as the reference's own Makefile (Makefile:2,14-18), run on its

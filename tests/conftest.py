@@ -38,3 +38,14 @@ def tile_n(request):
     assert g.tune_param(g.TUNE_TILE_N, request.param) == g.OK
     yield request.param
     assert g.tune_param(g.TUNE_TILE_N, 0) == g.OK
+
+
+@pytest.fixture(params=[1, 2], ids=["pair", "cta"])
+def cluster_mode(request):
+    """Runs a split-form test with each cluster mode of the tensor-core GEMMs:
+    pair MMAs on 2-CTA clusters (1) and one CTA per tile (2)."""
+    import gemm_avx2_gb300 as g
+
+    assert g.tune_param(g.TUNE_PAIR_MMA, request.param) == g.OK
+    yield request.param
+    assert g.tune_param(g.TUNE_PAIR_MMA, 0) == g.OK

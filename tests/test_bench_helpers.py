@@ -26,7 +26,9 @@ def test_parse_form_names(knobs):
     assert bench.parse_form("fp16x3") == ("bf16x", g.FP16X3)
     # a tuned name pins chunk, tile width and cluster mode as knobs
     assert bench.parse_form("tuned:fp16x3_c8_t256_pair") == ("bf16x", g.FP16X3)
-    assert bench.parse_form("bf16x6_c4_t128_mc") == ("bf16x", 6)
+    assert bench.parse_form("bf16x6_c4_t128_cta") == ("bf16x", 6)
+    with pytest.raises(SystemExit):
+        bench.parse_form("bf16x6_mc")  # the multicast mode no longer exists
     with pytest.raises(SystemExit):
         bench.parse_form("fp16x3_q9")
     with pytest.raises(SystemExit):

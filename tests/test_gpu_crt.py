@@ -88,9 +88,10 @@ def test_extreme_exponents_bitexact(orc, N):
 
 
 @pytest.mark.parametrize("m", [300, 129])
-def test_odd_row_tiles_bitexact(orc, m, tile_n):
-    """3 and 2 row tiles (m = 300: the 2-CTA clusters get a spare tile that
-    must store no residues over a neighbour's; m = 129: a 1-row last tile)."""
+def test_odd_row_tiles_bitexact(orc, m, tile_n, cluster_mode):
+    """3 and 2 row tiles, in each cluster mode (m = 300: the pair MMAs' 2-CTA
+    clusters get a spare tile that must store no residues over a neighbour's;
+    m = 129: a 1-row last tile)."""
     n, k = 290, 150
     A = orc.spread((m, k), 58, 0, 1.0)
     B = orc.spread((k, n), 58, 1, 1.0)

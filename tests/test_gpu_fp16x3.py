@@ -179,10 +179,10 @@ def test_host_and_noalloc_paths(orc):
 
 @pytest.mark.parametrize("products", [6, g.FP16X3])
 @pytest.mark.parametrize("tile", [128, 256])
-def test_pair_and_multicast_modes_agree(orc, products, tile):
+def test_pair_and_single_cta_modes_agree(orc, products, tile):
     """The pair MMAs (cta_group::2, two CTAs per 256-row tile, each holding half
-    of the B tile) and the per-CTA MMAs on a multicast B tile give the same
-    result bit for bit, for even and odd numbers of row tiles."""
+    of the B tile) and one CTA per 128-row tile give the same result bit for
+    bit, for even and odd numbers of row tiles."""
     outs = []
     try:
         assert g.tune_param(g.TUNE_TILE_N, tile) == g.OK

@@ -178,9 +178,9 @@ def test_ozaki_slices_extreme_exponents(orc, S, ta):
     assert g.device_error() == 0
 
 
-def test_ozaki_odd_row_tiles(orc, tile_n):
-    """3 row tiles: in 2-CTA clusters the spare fourth tile runs through the
-    pipeline but must write neither the FP64 scratch nor C."""
+def test_ozaki_odd_row_tiles(orc, tile_n, cluster_mode):
+    """3 row tiles, in each cluster mode: with pair MMAs the spare fourth tile
+    runs through the pipeline but must write neither the FP64 scratch nor C."""
     m, n, k = 300, 270, 200
     A = orc.spread((m, k), 23, 0, 1.0)
     B = orc.spread((k, n), 23, 1, 1.0)
