@@ -20,9 +20,11 @@ kernel's TFLOP/s and errors of both forms against exact sampled dot products,
 clocks sampled during the timed region, gpu_launches, and a CPU baseline.
 
 --impl reference times the reference's CPU implementation of the same
-workload on the host cores (the reference library compiled from its sources
-when this host can run it, else the oracle's C restatement of its algorithm)
-on a bounded column sample of the workload.
+workload on all host cores (the reference library compiled from its sources
+when this host can run it, else the oracle's C restatement of its algorithm).
+Every step of that arm, and the GPU arm's cpu_baseline leg, compute the same
+thing: the whole workload when its work is at most SGEMM 8192^3's, else a
+fixed leading block of columns of C with that much work.
 
 N > 1 (torchrun): every rank runs the same single-GPU workload (the path
 shards by whole problems; replicas only), value = sum over ranks of the work /
@@ -234,6 +236,31 @@ def sample_truth(prob, n_samples=1024):
 
 
 # ----------------------------------------------------------------------------- our arm
+def workload_config(name, w, world):
+    """The `config` object of a workload's JSON line, the same in both arms:
+    the workload and its call arguments (the split form the GPU arm chose is
+    reported beside it, under "form")."""
+    cplx = name in CWORKLOADS
+    esz = {"d": 8, "s": 4, "z": 16, "c": 8}[w["prec"]]
+    if cplx:
+        a_bytes = w["m"] * w["k"] * esz
+        cfg = {"workload": name, "transa": w["ta"], "transb": w["tb"], "m": w["m"], "n": w["n"],
+               "k": w["k"], "alpha": w["alpha"], "beta": w["beta"], "flops_per_call": "8mnk"}
+    else:
+        a_bytes = w["lda"] * (w["k"] if w["ta"] == "N" else w["m"]) * esz
+        cfg = {"workload": name, "transa": w["ta"], "transb": w["tb"], "m": w["m"], "n": w["n"],
+               "k": w["k"], "lda": w["lda"], "ldb": w["ldb"], "ldc": w["ldc"],
+               "alpha": w["alpha"], "beta": w["beta"], "phi": float(w.get("phi", 0.0))}
+    if a_bytes > L2_BYTES:
+        cfg["l2"] = "inputs larger than L2 (%d MB per operand > %d MB)" % (a_bytes // 2**20,
+                                                                           L2_BYTES // 2**20)
+    else:
+        cfg["l2"] = "inputs fit in L2 (%d MB per operand <= %d MB): warm-L2 timing" % (
+            a_bytes // 2**20, L2_BYTES // 2**20)
+    cfg["parallelism"] = "replicas" if world > 1 else "single"
+    return cfg
+
+
 def run_ours(args, torch, rank, world):
     import numpy as np
 
@@ -472,15 +499,9 @@ def run_ours(args, torch, rank, world):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if is_d else "f32",
         "data": "synthetic (seeded uniform[-1,1), generated on the device)",
-        "config": {"workload": args.workload, "transa": w["ta"], "transb": w["tb"], "m": m,
-                   "n": n, "k": k, "lda": w["lda"], "ldb": w["ldb"], "ldc": w["ldc"],
-                   "alpha": w["alpha"], "beta": w["beta"], "form": form_name,
-                   "phi": float(w.get("phi", 0.0)),
-                   "autotuned": tuned,
-                   "exponent_spread": exponent_spread(prob),
-                   "l2": "inputs larger than L2 (%d MB per operand > %d MB)" % (
-                       prob.A.numel() * prob.A.element_size() // 2**20, L2_BYTES // 2**20),
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": workload_config(args.workload, w, world),
+        "form": {"name": form_name, "autotuned": tuned,
+                 "exponent_spread": exponent_spread(prob)},
         "e2e": e2e,
         "roofline": roof,
         "plain": {"kernel": "dgemm_plain (DMMA)" if is_d else "sgemm_plain (FFMA)",
@@ -501,7 +522,7 @@ def run_ours(args, torch, rank, world):
             else {"bf16x": 2, "ozaki": 3, "crt": 4}[form]),
     }
     if rank == 0:
-        line["cpu_baseline"] = (cpu_baseline(w, args.cpu_seconds) if not args.no_cpu
+        line["cpu_baseline"] = (cpu_baseline(w) if not args.no_cpu
                                 else {"value": None, "skipped": "--no-cpu"})
         print(json.dumps(line), flush=True)
 
@@ -725,12 +746,8 @@ def run_complex(args, torch, rank, world):
         "ms_per_step": round(max_ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128" if p == "z" else "c64",
         "data": "synthetic (seeded uniform[-1,1) real and imaginary parts, on the device)",
-        "config": {"workload": args.workload, "transa": w["ta"], "transb": w["tb"], "m": m,
-                   "n": n, "k": k, "alpha": w["alpha"], "beta": w["beta"], "form": form_name,
-                   "flops_per_call": "8mnk",
-                   "l2": "inputs larger than L2 (%d MB per operand > %d MB)" % (
-                       A.numel() * A.element_size() // 2**20, L2_BYTES // 2**20),
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": workload_config(args.workload, w, world),
+        "form": {"name": form_name},
         "e2e": e2e,
         "roofline": {"bound": "tensor", "achieved": round(achieved, 2),
                      "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
@@ -760,7 +777,7 @@ def run_complex(args, torch, rank, world):
                                            if param == g.FP16X3 else 2)),
     }
     if rank == 0:
-        line["cpu_baseline"] = (cpu_baseline_complex(w, args.cpu_seconds) if not args.no_cpu
+        line["cpu_baseline"] = (cpu_baseline(w, cplx=True) if not args.no_cpu
                                 else {"value": None, "skipped": "--no-cpu"})
         print(json.dumps(line), flush=True)
 
@@ -953,108 +970,100 @@ def traffic_from_profile(workload, form_name):
 
 
 # ----------------------------------------------------------------------------- CPU side
-def cpu_gemm_callable():
-    """(kind, cores, f): the reference library when it runs on this host, else the
-    oracle's C restatement of its algorithm ("port")."""
-    import oracle
-
-    lib = os.path.join(ROOT, "oracle", "liborc.so")
-    if not os.path.exists(lib):
-        oracle.build()
-    cores = os.cpu_count() or 1
-    oracle.set_threads(cores)
-    if oracle.RefLib.available():
-        ref = oracle.RefLib()
-        return "reference", cores, lambda *a: ref.gemm(*a)
-    return "port", cores, lambda *a: oracle.refgemm(*a, cores)
+# One CPU step computes the whole workload when its work is at most SGEMM
+# 8192^3's (about 12 s with the port on 16 Grace cores), else the leading
+# block of columns of C with that much work.  The block is fixed by the
+# workload alone, so the CPU-baseline leg of the GPU arm and every step of the
+# reference arm time the same computation.
+CPU_STEP_FLOPS = 1.1e12
 
 
-def cpu_sample_rate(w, seconds):
-    """TFLOP/s of the CPU implementation on a column sample of the workload."""
-    import numpy as np
-
-    import oracle
-
-    kind, cores, f = cpu_gemm_callable()
-    dt = np.float64 if w["prec"] == "d" else np.float32
-    m, k = w["m"], w["k"]
-    ar, ac = (m, k) if w["ta"] == "N" else (k, m)
-    A = oracle.storage(ar, ac, w["lda"], dt, w["seed"], 0)
-
-    def run(ns):
-        br, bc = (k, ns) if w["tb"] == "N" else (ns, k)
-        B = oracle.storage(br, bc, max(br, 1), dt, w["seed"], 1)
-        C = oracle.storage(m, ns, w["ldc"], dt, w["seed"], 2)
-        t = time.perf_counter()
-        f(w["ta"], w["tb"], m, ns, k, w["alpha"], A, w["lda"], B, max(br, 1), w["beta"], C,
-          w["ldc"])
-        return time.perf_counter() - t
-
-    ns = 16
-    run(ns)          # warm-up (thread team start, page faults)
-    dt0 = run(ns)
-    ns = int(min(w["n"], max(16, ns * seconds / max(dt0, 1e-3))))
-    t = run(ns)
-    tf = 2.0 * m * ns * k / t / 1e12
-    sample = "%s%s m=%d n=%d (of %d) k=%d, %d columns of C" % (
-        w["ta"], w["tb"], m, ns, w["n"], k, ns)
-    return kind, cores, tf, t, sample
+def cpu_columns(n, flops_per_column):
+    if flops_per_column * n <= CPU_STEP_FLOPS:
+        return n
+    ns = int(CPU_STEP_FLOPS / flops_per_column)
+    return max(16, ns - ns % 16)
 
 
-def cpu_baseline(w, seconds):
-    try:
-        kind, cores, tf, t, sample = cpu_sample_rate(w, seconds)
-        return {"value": round(tf, 5), "unit": "TFLOP/s", "cores": cores, "kind": kind,
-                "sample": sample, "seconds": round(t, 2)}
-    except Exception as ex:  # noqa: BLE001
-        return {"value": None, "error": repr(ex)}
+class CpuWorkload:
+    """The workload's CPU computation (the reference library where it runs on
+    this host, else the oracle's restatement of its algorithm, on all host
+    cores): `warmup()` runs a few columns (thread team start; it reads all of
+    A, whose pages the generator already touched), `step()` times the step's
+    columns of C and returns the seconds."""
 
+    def __init__(self, w, cplx=False):
+        import numpy as np
 
-def cpu_complex_rate(w, seconds):
-    """8mnk TFLOP/s of the reference's complex kernel on a column sample (all
-    host cores, columns split across threads; the kernels run where they were
-    compiled from the reference sources, x86-64), else of the portable
-    restatement of its arithmetic (OpenMP over columns)."""
-    import numpy as np
+        import oracle
 
-    import oracle
+        if not os.path.exists(os.path.join(ROOT, "oracle", "liborc.so")):
+            oracle.build()
+        self.cores = os.cpu_count() or 1
+        oracle.set_threads(self.cores)
+        m, n, k = w["m"], w["n"], w["k"]
+        self.w, self.cplx = w, cplx
+        self.ns = cpu_columns(n, (8.0 if cplx else 2.0) * m * k)
+        self.flops = (8.0 if cplx else 2.0) * m * self.ns * k
+        if cplx:
+            dt = np.complex128 if w["prec"] == "z" else np.complex64
+            self.A = oracle.cuniform((m, k), dt, w["seed"], 0)
+            self.B = oracle.cuniform((k, self.ns), dt, w["seed"], 1)
+            self.C = oracle.cuniform((m, self.ns), dt, w["seed"], 2)
+            ref = oracle.RefCplx() if oracle.RefCplx.available() else None
+            self.kind = "reference" if ref else "port"
 
-    if not os.path.exists(os.path.join(ROOT, "oracle", "liborc.so")):
-        oracle.build()
-    cores = os.cpu_count() or 1
-    oracle.set_threads(cores)
-    dt = np.complex128 if w["prec"] == "z" else np.complex64
-    m, k = w["m"], w["k"]
-    A = oracle.cuniform((m, k), dt, w["seed"], 0)
-    ref = oracle.RefCplx() if oracle.RefCplx.available() else None
-    kind = "reference" if ref else "port"
-
-    def run(ns):
-        B = oracle.cuniform((k, ns), dt, w["seed"], 1)
-        C = oracle.cuniform((m, ns), dt, w["seed"], 2)
-        t = time.perf_counter()
-        if ref:   # packs A once, then B's columns over the OpenMP team
-            ref.gemm_conj(0, 0, w["alpha"], A, B, C)
+            def f(ns):  # NN: packs A once, then B's columns over the OpenMP team
+                if ref:
+                    ref.gemm_conj(0, 0, w["alpha"], self.A, self.B[:, :ns], self.C[:, :ns])
+                else:
+                    oracle.zgemm_port(0, 0, w["alpha"], self.A, self.B[:, :ns], self.C[:, :ns])
+            self.f = f
+            self.sample = "%sgemm NN m=%d n=%d (of %d) k=%d" % (w["prec"], m, self.ns, n, k)
         else:
-            oracle.zgemm_port(0, 0, w["alpha"], A, B, C)
+            dt = np.float64 if w["prec"] == "d" else np.float32
+            ar, ac = (m, k) if w["ta"] == "N" else (k, m)
+            br, bc = (k, self.ns) if w["tb"] == "N" else (self.ns, k)
+            phi = w.get("phi") or None  # exponent-spread inputs where the workload has them
+            self.A = oracle.storage(ar, ac, w["lda"], dt, w["seed"], 0, phi)
+            self.B = oracle.storage(br, bc, max(br, 1), dt, w["seed"], 1, phi)
+            self.C = oracle.storage(m, self.ns, w["ldc"], dt, w["seed"], 2)
+            ldb = max(br, 1)
+            if oracle.RefLib.available():
+                ref = oracle.RefLib()
+                self.kind = "reference"
+                g = ref.gemm
+            else:
+                self.kind = "port"
+                g = lambda *a: oracle.refgemm(*a, self.cores)
+
+            def f(ns):  # op(B)'s first ns columns: the leading columns (N) or rows (T) of B
+                g(w["ta"], w["tb"], m, ns, k, w["alpha"], self.A, w["lda"], self.B, ldb,
+                  w["beta"], self.C, w["ldc"])
+            self.f = f
+            self.sample = "%s%s m=%d n=%d (of %d) k=%d" % (w["ta"], w["tb"], m, self.ns, n, k)
+        if self.ns == n:
+            self.sample += ", the whole workload"
+        else:
+            self.sample += ", the first %d columns of C" % self.ns
+
+    def warmup(self):
+        self.f(min(self.ns, 16 * self.cores))
+
+    def step(self):
+        t = time.perf_counter()
+        self.f(self.ns)
         return time.perf_counter() - t
 
-    ns = 4 * cores
-    run(ns)
-    t0 = run(ns)
-    ns = int(min(w["n"], max(cores, ns * seconds / max(t0, 1e-3))))
-    t = run(ns)
-    tf = 8.0 * m * ns * k / t / 1e12
-    sample = "%sgemm NN m=%d n=%d (of %d) k=%d: %d columns of C" % (w["prec"], m, ns, w["n"], k,
-                                                                     ns)
-    return kind, cores, tf, t, sample
 
-
-def cpu_baseline_complex(w, seconds):
+def cpu_baseline(w, cplx=False):
+    """One warm-up, then the step's computation timed once."""
     try:
-        kind, cores, tf, t, sample = cpu_complex_rate(w, seconds)
-        return {"value": round(tf, 5), "unit": "TFLOP/s", "cores": cores, "kind": kind,
-                "sample": sample, "seconds": round(t, 2)}
+        cw = CpuWorkload(w, cplx)
+        cw.warmup()
+        t = cw.step()
+        return {"value": round(cw.flops / t / 1e12, 5), "unit": "TFLOP/s", "cores": cw.cores,
+                "kind": cw.kind, "sample": cw.sample, "seconds": round(t, 2)}
     except Exception as ex:  # noqa: BLE001
         return {"value": None, "error": repr(ex)}
 
@@ -1067,27 +1076,27 @@ def run_reference(args, rank, world):
                           "unavailable": "the reference has no grouped interface"}))
         return
     cplx = args.workload in CWORKLOADS
-    w = CWORKLOADS[args.workload] if cplx else WORKLOADS[args.workload]
-    per_step = max(1.0, min(10.0, 120.0 / max(1, args.steps + args.warmup)))
-    vals = []
-    info = None
-    for i in range(args.warmup + args.steps):
-        kind, cores, tf, t, sample = (cpu_complex_rate if cplx else cpu_sample_rate)(w, per_step)
-        if i >= args.warmup:
-            vals.append((tf, t))
-        info = (kind, cores, sample)
-    tf = sum(v[0] for v in vals) / len(vals)
+    w = dict(CWORKLOADS[args.workload] if cplx else WORKLOADS[args.workload])
+    if args.phi is not None and not cplx:
+        w["phi"] = args.phi
+    # every step is the same computation as the GPU arm's CPU-baseline leg:
+    # the whole workload up to SGEMM 8192^3's work (else a fixed leading
+    # column block); the warm-up steps start the thread team on a few columns
+    cw = CpuWorkload(w, cplx)
+    for _ in range(args.warmup):
+        cw.warmup()
+    times = [cw.step() for _ in range(args.steps)]
+    tf = cw.flops * len(times) / sum(times) / 1e12
     line = {"metric": METRIC, "value": round(tf, 5), "unit": "TFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(1e3 * sum(v[1] for v in vals) / len(vals), 2),
+            "ms_per_step": round(1e3 * sum(times) / len(times), 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"d": "f64", "s": "f32", "z": "c128", "c": "c64"}[w["prec"]],
-            "data": "synthetic",
-            "config": {"workload": args.workload, "transa": w["ta"], "transb": w["tb"],
-                       "m": w["m"], "n": w["n"], "k": w["k"]},
+            "data": "synthetic (the portable generator's seeded uniform[-1,1) inputs)",
+            "config": workload_config(args.workload, w, world),
             "impl": "reference",
-            "cpu_baseline": {"value": round(tf, 5), "unit": "TFLOP/s", "cores": info[1],
-                             "kind": info[0], "sample": info[2]},
+            "cpu_baseline": {"value": round(tf, 5), "unit": "TFLOP/s", "cores": cw.cores,
+                             "kind": cw.kind, "sample": cw.sample},
             "e2e": {"value": round(tf, 5), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -1115,7 +1124,6 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(CWORKLOADS) + ["grouped_1024"],
                     default="sgemm_tn_8192")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--phi", type=float, default=None,
                     help="exponent spread of A and B: (u-0.5)*exp(phi*g) (DGEMM NT 16384 sweep)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")

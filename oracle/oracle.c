@@ -303,7 +303,7 @@ ORC_API void orc_dot2gemm_sampled_d(char ta, char tb, int m, int n, int k, doubl
   for (int64_t q = 0; q < count; q++) {
     const int64_t i = rows[q], j = cols[q];
     ORC_DOT2_ELEM(double, double)
-    out[q] = dot2_finish(s, err, alpha, beta, c[i + j * ldc]);
+    out[q] = dot2_finish(s, err, alpha, beta, c ? c[i + j * ldc] : 0.0);
   }
 }
 ORC_API void orc_dot2gemm_sampled_s(char ta, char tb, int m, int n, int k, double alpha,

@@ -1,0 +1,215 @@
+"""Parity at the benchmark configurations' full sizes (GPU).
+
+  * SGEMM TN m = n = k = 8192, alpha = 1, beta = 0 (the headline workload);
+  * DGEMM NT m = n = k = 16384, alpha = beta = 1, entries (u - 0.5) exp(phi g)
+    with phi in {0, 4} (the exponent-spread sweep's ends);
+  * the rank-256 update, D and S: NT, m = n = 32768, k = 256, lda = m + 32,
+    ldb = n + 32, ldc = m + 64, alpha = -1, beta = 1.
+
+The plain kernels are checked against the oracle's restatement of the
+reference (`orc_refgemm`, src/gemm_driver.c:118-197) on a sample of 64
+columns: every element within the summation-order bound, DGEMM also within
+1e-13 relative Frobenius.  The split forms are checked against exact sampled
+dot products (Dot2, 1024 entries in those columns): their max and Frobenius
+relative errors must not exceed the plain kernel's on the same entries
+(equal error), with the form each workload's benchmark line uses there.
+A and B come from the oracle's portable generator; C is drawn on the device
+(torch, seeded) and its sampled columns are read back before the call.
+The padding rows of the sampled columns of C must come back untouched."""
+import math
+
+import numpy as np
+import pytest
+
+import gemm_avx2_gb300 as g
+from gpu_util import torch_cuda
+from util import U32, U64
+
+pytestmark = pytest.mark.gpu
+
+NCOLS, ROWS_PER_COL = 64, 16  # 1024 sampled entries
+
+
+def sample(m, n, seed):
+    rng = np.random.default_rng(seed)
+    cols = np.sort(rng.choice(n, NCOLS, replace=False))
+    rows = np.stack([rng.choice(m, ROWS_PER_COL, replace=False) for _ in cols])
+    return cols, rows  # rows[j] are the sampled rows of column cols[j]
+
+
+def device_C(torch, m, n, ldc, dt, seed):
+    """ldc x n column-major C on the device, U[-1,1) from a seeded generator."""
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    t = torch.empty((n, ldc), dtype=dt, device="cuda")
+    t.uniform_(-1.0, 1.0, generator=gen)
+    return t
+
+
+def cols_of(t, cols, rows):
+    """The given columns of a device column-major matrix, first `rows` rows."""
+    import torch
+
+    idx = torch.as_tensor(cols, device=t.device)
+    return np.asfortranarray(t.index_select(0, idx)[:, :rows].cpu().numpy().T)
+
+
+def dev(x):
+    torch = torch_cuda()
+    return torch.from_numpy(np.ascontiguousarray(np.asfortranarray(x).T)).cuda()
+
+
+def b_cols(B, tb, cols):
+    """The stored B restricted to the columns `cols` of op(B), with its ld."""
+    Bs = B[:, cols] if tb == "N" else B[cols, :]
+    Bs = np.asfortranarray(Bs)
+    return Bs, Bs.shape[0]
+
+
+def exact_samples(orc, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, Ccols, cols, rows):
+    """alpha * (op(A) op(B))_ij + beta * c_ij at the sampled entries: the dot
+    product from the Dot2 oracle, then the two-term sum rounded once."""
+    ri = rows.ravel()
+    ci = np.repeat(cols, rows.shape[1])
+    dots = orc.dot2gemm_sampled(ta, tb, m, n, k, 1.0, A, lda, B, ldb, 0.0, None, 1, ri, ci)
+    cv = np.asarray(Ccols, np.float64)[rows, np.arange(len(cols))[:, None]].ravel()
+    out = np.array([math.fsum((alpha * d, beta * c)) for d, c in zip(dots.tolist(), cv.tolist())])
+    return out.reshape(rows.shape)
+
+
+def at_samples(Ccols, rows):
+    return np.asarray(Ccols, np.float64)[rows, np.arange(rows.shape[0])[:, None]]
+
+
+def errors(x, truth):
+    d = np.abs(x - truth)
+    mx = float(np.max(d / np.maximum(np.abs(truth), 1e-300)))
+    return mx, float(np.linalg.norm(d) / np.linalg.norm(truth))
+
+
+def check_plain_vs_reference(orc, ta, tb, m, k, alpha, A, lda, B, ldb, beta, C0cols, got, u,
+                             cols):
+    """got (m x 64): the GPU plain kernel's sampled columns; the oracle's
+    restatement of the reference on the same columns; summation-order bound."""
+    Bs, ldbs = b_cols(B, tb, cols)
+    want = np.array(C0cols, order="F", copy=True)
+    orc.refgemm(ta, tb, m, len(cols), k, alpha, A, lda, Bs, ldbs, beta, want, m,
+                orc.max_threads())
+    a = np.abs(A[:m, :k] if ta == "N" else A[:k, :m].T).astype(np.float64)
+    b = np.abs(Bs[:k, :] if tb == "N" else Bs[:, :k].T).astype(np.float64)
+    bound = 2 * (k + 2) * u * (abs(alpha) * (a @ b) + abs(beta) * np.abs(C0cols)) + 1e-300
+    diff = np.abs(got.astype(np.float64) - want)
+    assert np.all(diff <= bound), float((diff - bound).max())
+    fro = float(np.linalg.norm(diff) / np.linalg.norm(want))
+    if u == U64:
+        assert fro <= 1e-13, fro
+    return want
+
+
+def test_config2_sgemm_tn_8192(orc):
+    torch = torch_cuda()
+    m = n = k = 8192
+    A = orc.uniform((k, m), np.float32, 1, 0)  # transa = T: stored k x m
+    B = orc.uniform((k, n), np.float32, 1, 1)
+    dA, dB = dev(A), dev(B)
+    cols, rows = sample(m, n, 201)
+    truth = exact_samples(orc, "T", "N", m, n, k, 1.0, A, k, B, k, 0.0,
+                          np.zeros((m, NCOLS)), cols, rows)
+    zeros = np.zeros((m, NCOLS), np.float32, order="F")
+    # plain FFMA kernel
+    dC = torch.zeros((n, m), dtype=torch.float32, device="cuda")
+    assert g.gemm_device("s", "T", "N", m, n, k, 1.0, dA.data_ptr(), k, dB.data_ptr(), k, 0.0,
+                         dC.data_ptr(), m) == g.OK
+    plain = cols_of(dC, cols, m)
+    check_plain_vs_reference(orc, "T", "N", m, k, 1.0, A, k, B, k, 0.0, zeros, plain, U32, cols)
+    e_plain = errors(at_samples(plain, rows), truth)
+    # the split forms: the autotuned choice for this shape class (products = 0)
+    # and the untuned default, 6xBF16
+    rc, _ = g.autotune(g.TUNE_BF16X, "T", "N", m, n, k, dA.data_ptr(), k, dB.data_ptr(), k)
+    assert rc == g.OK
+    try:
+        for products in (0, 6):
+            dC.zero_()
+            assert g.sgemm_bf16x("T", "N", m, n, k, 1.0, dA.data_ptr(), k, dB.data_ptr(), k, 0.0,
+                                 dC.data_ptr(), m, products=products) == g.OK
+            e = errors(at_samples(cols_of(dC, cols, m), rows), truth)
+            assert e[0] <= e_plain[0] and e[1] <= e_plain[1], (products, e, e_plain)
+    finally:
+        g.tune_cache_clear()
+    assert g.device_error() == 0
+    del dA, dB, dC
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("phi,moduli", [(0.0, 15), (4.0, 20)])
+def test_config3_dgemm_nt_16384(orc, phi, moduli):
+    """The CRT form with the moduli count the benchmark selects at each spread."""
+    torch = torch_cuda()
+    m = n = k = 16384
+    A = orc.spread((m, k), 2, 0, phi)
+    B = orc.spread((n, k), 2, 1, phi)  # transb = T: stored n x k
+    dA, dB = dev(A), dev(B)
+    dC = device_C(torch, m, n, m, torch.float64, 2)
+    cols, rows = sample(m, n, 300 + int(phi))
+    C0 = cols_of(dC, cols, m)
+    truth = exact_samples(orc, "N", "T", m, n, k, 1.0, A, m, B, n, 1.0, C0, cols, rows)
+    # plain DMMA kernel on the sampled columns (an element's result does not
+    # depend on which other columns are computed with it)
+    Bs, _ = b_cols(B, "T", cols)
+    dBs, dCs = dev(Bs), dev(C0)
+    assert g.gemm_device("d", "N", "T", m, NCOLS, k, 1.0, dA.data_ptr(), m, dBs.data_ptr(),
+                         NCOLS, 1.0, dCs.data_ptr(), m) == g.OK
+    torch.cuda.synchronize()
+    plain = np.asfortranarray(dCs.cpu().numpy().T)
+    check_plain_vs_reference(orc, "N", "T", m, k, 1.0, A, m, B, n, 1.0, C0, plain, U64, cols)
+    e_plain = errors(at_samples(plain, rows), truth)
+    # the CRT form at full size
+    assert g.dgemm_ozaki2("N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 1.0,
+                          dC.data_ptr(), m, moduli=moduli) == g.OK
+    e = errors(at_samples(cols_of(dC, cols, m), rows), truth)
+    assert e[0] <= e_plain[0] and e[1] <= e_plain[1], (e, e_plain)
+    assert g.device_error() == 0
+    del dA, dB, dC, dBs, dCs
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("prec", ["d", "s"])
+def test_config4_rank256_update(orc, prec):
+    """Plain kernel against the reference restatement; the split form the
+    benchmark uses there (D: CRT, 15 moduli; S: 6xBF16) at equal error."""
+    torch = torch_cuda()
+    m = n = 32768
+    k = 256
+    lda, ldb, ldc = m + 32, n + 32, m + 64
+    dt, tdt, u = (np.float64, torch.float64, U64) if prec == "d" else (np.float32, torch.float32,
+                                                                       U32)
+    A = orc.uniform((lda, k), dt, 3, 0)  # transa = N: stored m x k (lda rows)
+    B = orc.uniform((ldb, k), dt, 3, 1)  # transb = T: stored n x k (ldb rows)
+    dA, dB = dev(A), dev(B)
+    dC = device_C(torch, m, n, ldc, tdt, 3)
+    dC2 = dC.clone()
+    cols, rows = sample(m, n, 400)
+    C0full = cols_of(dC, cols, ldc)
+    C0 = np.asfortranarray(C0full[:m])
+    truth = exact_samples(orc, "N", "T", m, n, k, -1.0, A, lda, B, ldb, 1.0, C0, cols, rows)
+    assert g.gemm_device(prec, "N", "T", m, n, k, -1.0, dA.data_ptr(), lda, dB.data_ptr(), ldb,
+                         1.0, dC.data_ptr(), ldc) == g.OK
+    plain_full = cols_of(dC, cols, ldc)
+    assert np.array_equal(plain_full[m:], C0full[m:])  # ldc padding untouched
+    plain = np.asfortranarray(plain_full[:m])
+    check_plain_vs_reference(orc, "N", "T", m, k, -1.0, A, lda, B, ldb, 1.0, C0, plain, u, cols)
+    e_plain = errors(at_samples(plain, rows), truth)
+    if prec == "d":
+        rc = g.dgemm_ozaki2("N", "T", m, n, k, -1.0, dA.data_ptr(), lda, dB.data_ptr(), ldb, 1.0,
+                            dC2.data_ptr(), ldc, moduli=15)
+    else:
+        rc = g.sgemm_bf16x("N", "T", m, n, k, -1.0, dA.data_ptr(), lda, dB.data_ptr(), ldb, 1.0,
+                           dC2.data_ptr(), ldc, products=6)
+    assert rc == g.OK
+    split_full = cols_of(dC2, cols, ldc)
+    assert np.array_equal(split_full[m:], C0full[m:])
+    e = errors(at_samples(split_full[:m], rows), truth)
+    assert e[0] <= e_plain[0] and e[1] <= e_plain[1], (e, e_plain)
+    assert g.device_error() == 0
+    del dA, dB, dC, dC2
+    torch.cuda.empty_cache()
