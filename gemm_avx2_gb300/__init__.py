@@ -118,6 +118,8 @@ def core() -> ctypes.CDLL:
                                         ctypes.POINTER(c_int)]
         L.gb300_tune_layout.argtypes = [c_int, c_int, c_int, c_int, ctypes.POINTER(c_int),
                                         ctypes.POINTER(c_int)]
+        L.gb300_plain_layout.argtypes = [c_int, c_int, c_int, c_int, ctypes.POINTER(c_int),
+                                         ctypes.POINTER(c_int)]
         L.gb300_tune_cache_save.argtypes = [ctypes.c_char_p]
         L.gb300_tune_cache_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(c_int)]
         L.gb300_tune_cache_clear.restype = None
@@ -390,9 +392,13 @@ TUNE_TILE_N = 3
 TUNE_PAIR_MMA = 4
 TUNE_HOST_PARTS = 5
 TUNE_MODULUS_SPLIT = 6
+TUNE_SPLIT_K = 7
+TUNE_PLAIN_STAGES = 8
 TUNE_BF16X = 0     # autotuner kinds
 TUNE_OZAKI = 1
 TUNE_CRT = 2
+TUNE_PLAIN_D = 3
+TUNE_PLAIN_S = 4
 
 
 def autotune(kind, transa, transb, m, n, k, A, lda, B, ldb, stream=0):
@@ -416,6 +422,14 @@ def tune_layout(kind, m, n, k):
     t, pm = c_int(0), c_int(0)
     rc = core().gb300_tune_layout(kind, m, n, k, ctypes.byref(t), ctypes.byref(pm))
     return rc, t.value, pm.value
+
+
+def plain_layout(precision, m, n, k):
+    """(status, split-K factor, ring depth) the plain kernels use for this shape."""
+    sk, st = c_int(0), c_int(0)
+    rc = core().gb300_plain_layout(1 if precision == "d" else 0, m, n, k, ctypes.byref(sk),
+                                   ctypes.byref(st))
+    return rc, sk.value, st.value
 
 
 def tune_cache_save(path=None) -> int:
@@ -511,7 +525,8 @@ CORE_SYMBOLS = [
     "gb300_dgemm_ozaki_run", "gb300_host_sgemm_bf16x", "gb300_host_dgemm_ozaki",
     "gb300_selftest_wait_timeout", "gb300_sgemm_bf16x_noalloc", "gb300_tune_param",
     "gb300_grouped_workspace_bytes", "gb300_gemm_grouped", "gb300_gemm_grouped_ws",
-    "gb300_autotune", "gb300_tune_lookup", "gb300_tune_layout", "gb300_tune_cache_save",
+    "gb300_autotune", "gb300_tune_lookup", "gb300_tune_layout", "gb300_plain_layout",
+    "gb300_tune_cache_save",
     "gb300_tune_cache_load",
     "gb300_tune_cache_clear", "gb300_dtrsm", "gb300_strsm", "gb300_dtrmm", "gb300_strmm",
     "gb300_grouped_graph_create", "gb300_grouped_graph_launch", "gb300_grouped_graph_destroy",

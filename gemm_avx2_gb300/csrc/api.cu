@@ -507,12 +507,17 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
     else
       rc = split_sgemm(ta, tb, m, n, k, alpha, dA, dlda, dB, dldb, beta, dC, dlc, param, ws,
                        wneed, st, s->err);
-  } else if constexpr (sizeof(T) == 8) {
-    rc = plain_dgemm(ta, tb, m, n, k, alpha, need_ab ? dA : nullptr, dlda,
-                     need_ab ? dB : nullptr, dldb, beta, dC, dlc, st, s->err);
   } else {
-    rc = plain_sgemm(ta, tb, m, n, k, alpha, need_ab ? dA : nullptr, dlda,
-                     need_ab ? dB : nullptr, dldb, beta, dC, dlc, st, s->err);
+    // the plain kernels, split along K where the shape asks for it
+    const size_t pneed = need_ab ? plain_workspace_bytes(sizeof(T) == 8, m, n, k) : 0;
+    void *pw = pneed ? cached_workspace(s, st, pneed) : nullptr;
+    const size_t pwb = pw ? pneed : 0;
+    if constexpr (sizeof(T) == 8)
+      rc = plain_dgemm(ta, tb, m, n, k, alpha, need_ab ? dA : nullptr, dlda,
+                       need_ab ? dB : nullptr, dldb, beta, dC, dlc, st, s->err, pw, pwb);
+    else
+      rc = plain_sgemm(ta, tb, m, n, k, alpha, need_ab ? dA : nullptr, dlda,
+                       need_ab ? dB : nullptr, dldb, beta, dC, dlc, st, s->err, pw, pwb);
   }
   if (rc != GB300_OK) {
     cudaStreamSynchronize(st);
@@ -697,25 +702,42 @@ GB300_API int gb300_dgemm_ozaki2(char ta, char tb, int m, int n, int k, double a
                    s->err);
 }
 
+// The plain kernels on device pointers.  A split-K call gets room for its
+// slices from the stream's cached workspace; if that cannot grow, it runs
+// unsplit.
+template <typename T>
+static int plain_api(char ta, char tb, int m, int n, int k, T alpha, const T *A, int lda,
+                     const T *B, int ldb, T beta, T *C, int ldc, void *stream) {
+  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
+  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
+  DeviceState *s = dev_state();
+  if (!s) return GB300_ERR_CUDA;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t need = alpha != T(0) ? plain_workspace_bytes(sizeof(T) == 8, m, n, k) : 0;
+  if (!need) {
+    if constexpr (sizeof(T) == 8)
+      return plain_dgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, s->err);
+    else
+      return plain_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, s->err);
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  void *w = cached_workspace(s, st, need);
+  const size_t wb = w ? need : 0;
+  if constexpr (sizeof(T) == 8)
+    return plain_dgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, s->err, w, wb);
+  else
+    return plain_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, s->err, w, wb);
+}
+
 GB300_API int gb300_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A,
                           int lda, const double *B, int ldb, double beta, double *C, int ldc,
                           void *stream) {
-  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
-  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
-  unsigned *err = device_error_word();
-  if (!err) return GB300_ERR_CUDA;
-  return plain_dgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
-                     static_cast<cudaStream_t>(stream), err);
+  return plain_api<double>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream);
 }
 GB300_API int gb300_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A,
                           int lda, const float *B, int ldb, float beta, float *C, int ldc,
                           void *stream) {
-  const int ck = check_args(ta, tb, m, n, k, lda, ldb, ldc);
-  if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
-  unsigned *err = device_error_word();
-  if (!err) return GB300_ERR_CUDA;
-  return plain_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
-                     static_cast<cudaStream_t>(stream), err);
+  return plain_api<float>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream);
 }
 
 // ---------------------------------------------------------------- complex
@@ -1183,7 +1205,7 @@ GB300_API int gb300_selftest_wait_timeout(unsigned poll_limit) {
 
 GB300_API int gb300_autotune(int kind, char ta, char tb, int m, int n, int k, const void *A,
                              int lda, const void *B, int ldb, void *stream, int *chosen) {
-  if (kind < 0 || kind > 2) return GB300_ERR_ARG;
+  if (kind < 0 || kind > 4) return GB300_ERR_ARG;
   if (check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1) != GB300_OK || k == 0)
     return GB300_ERR_ARG;
   unsigned *err = device_error_word();
@@ -1192,11 +1214,12 @@ GB300_API int gb300_autotune(int kind, char ta, char tb, int m, int n, int k, co
                   chosen);
 }
 GB300_API int gb300_tune_lookup(int kind, int m, int n, int k, int *param, int *chunk) {
-  if (kind < 0 || kind > 2) return GB300_ERR_ARG;
+  if (kind < 0 || kind > 4) return GB300_ERR_ARG;
   int p = 0, c = 0;
   if (kind == 0) bf16x_resolve(m, n, k, &p, &c);
   else if (kind == 1) p = ozaki_default_slices(m, n, k);
-  else p = crt_default_moduli(m, n, k);
+  else if (kind == 2) p = crt_default_moduli(m, n, k);
+  else p = plain_split_k(kind == 3, m, n, k);
   if (param) *param = p;
   if (chunk) *chunk = c;
   return tune_lookup(kind, m, n, k, nullptr, nullptr) ? GB300_OK : GB300_ERR_UNSUPPORTED;
@@ -1208,6 +1231,17 @@ GB300_API int gb300_tune_layout(int kind, int m, int n, int k, int *tile_n, int 
     const int o = pair_mma_override();
     const int v = o ? o : tune_pair_mma(kind, m, n, k);
     *pair_mma = v ? v : 1;
+  }
+  return tune_lookup(kind, m, n, k, nullptr, nullptr) ? GB300_OK : GB300_ERR_UNSUPPORTED;
+}
+GB300_API int gb300_plain_layout(int is_double, int m, int n, int k, int *split_k, int *stages) {
+  if (m < 0 || n < 0 || k < 0) return GB300_ERR_ARG;
+  const int kind = is_double ? 3 : 4;
+  if (split_k) *split_k = plain_split_k(is_double != 0, m, n, k);
+  if (stages) {
+    const int o = plain_stages_override();
+    const int v = o ? o : tune_plain_stages(kind, m, n, k);
+    *stages = v ? v : 4;
   }
   return tune_lookup(kind, m, n, k, nullptr, nullptr) ? GB300_OK : GB300_ERR_UNSUPPORTED;
 }
@@ -1241,6 +1275,14 @@ GB300_API int gb300_tune_param(int param, int value) {
     case GB300_TUNE_MODULUS_SPLIT:
       if (value < 0 || value > 2) return GB300_ERR_ARG;
       set_modulus_split(value);
+      return GB300_OK;
+    case GB300_TUNE_SPLIT_K:
+      if (value < 0 || value > 65535) return GB300_ERR_ARG;
+      set_plain_split_k(value);
+      return GB300_OK;
+    case GB300_TUNE_PLAIN_STAGES:
+      if (value != 0 && value != 4 && value != 6) return GB300_ERR_ARG;
+      set_plain_stages(value);
       return GB300_OK;
     default:
       return GB300_ERR_ARG;

@@ -9,7 +9,12 @@
 //   all forms   : then the output tile width (128 / 256) of the chosen one,
 //                 and its cluster mode (pair MMAs on 2-CTA clusters or one
 //                 CTA per tile);
-//   Ozaki DGEMM : slice count S in [4, 12].
+//   Ozaki DGEMM : slice count S in [4, 12];
+//   plain D/SGEMM (kinds 3, 4): split-K factor in {1, 2, 3, 4, 6, 8, 12, 16}
+//                 (at least 8 k-tiles a slice) x ring depth {4, 6}: the
+//                 fastest, since every split sums the same products in K
+//                 order within the same rounding bound (the reference's own
+//                 K blocking, src/gemm_driver.c:156-190).
 //
 // A candidate qualifies when its max and Frobenius relative errors against a
 // near-exact FP64 reference do not exceed those of the plain kernel on the
@@ -43,10 +48,11 @@
 namespace gb300 {
 
 struct TuneEntry {
-  int param = 0;       // products (BF16xP) or slices (Ozaki)
+  int param = 0;       // products (BF16xP), slices (Ozaki), moduli (CRT) or split-K (plain)
   int chunk = 0;       // BF16xP hi*hi chunk length (0 for Ozaki)
   int tile = 0;        // output tile width of the GEMM (128 / 256; 0 = by shape)
   int pair = 0;        // cluster mode (1 pair MMAs, 2 one CTA per tile; 0 = default)
+  int stages = 0;      // plain kernels' ring depth (4 / 6; 0 = default)
   double ms = 0;       // measured time of the chosen candidate
   double err_max = 0, err_fro = 0;              // chosen candidate vs reference
   double plain_max = 0, plain_fro = 0;          // plain kernel vs reference
@@ -61,11 +67,14 @@ static int ilog2(int x) {
   return l;
 }
 
+static const char *kind_name(int kind) {
+  static const char *names[5] = {"bf16x", "ozaki", "crt", "plain_d", "plain_s"};
+  return kind >= 0 && kind < 5 ? names[kind] : "?";
+}
+
 static std::string tune_key(int kind, int m, int n, int k) {
   char buf[96];
-  snprintf(buf, sizeof buf, "%s:%d:%d:%d", kind == 0 ? "bf16x" : kind == 1 ? "ozaki" : "crt",
-           ilog2(m), ilog2(n),
-           ilog2(k));
+  snprintf(buf, sizeof buf, "%s:%d:%d:%d", kind_name(kind), ilog2(m), ilog2(n), ilog2(k));
   return buf;
 }
 
@@ -88,6 +97,18 @@ int tune_pair_mma(int kind, int m, int n, int k) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tune.find(tune_key(kind, m, n, k));
   return it == g_tune.end() ? 0 : it->second.pair;
+}
+
+int tune_plain_split(int kind, int m, int n, int k) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(tune_key(kind, m, n, k));
+  return it == g_tune.end() ? 0 : it->second.param;
+}
+
+int tune_plain_stages(int kind, int m, int n, int k) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(tune_key(kind, m, n, k));
+  return it == g_tune.end() ? 0 : it->second.stages;
 }
 
 // ---------------------------------------------------------------- device helpers
@@ -168,9 +189,11 @@ int measure(const void *t, bool t_double, int m, int n, const double *ref, doubl
 
 int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int lda,
              const void *B, int ldb, cudaStream_t st, unsigned *err, int *chosen) {
-  if (kind < 0 || kind > 2) return GB300_ERR_ARG;
+  if (kind < 0 || kind > 4) return GB300_ERR_ARG;
   const int ck = check_args(ta, tb, m, n, k, lda, ldb, m > 1 ? m : 1);
   if (ck != GB300_OK || k == 0) return ck == GB300_ERR_ARG ? ck : GB300_ERR_ARG;
+  const bool f32 = kind == 0 || kind == 4;   // FP32 operands
+  const bool plain_kind = kind >= 3;         // the plain kernels' split-K and ring depth
   const bool an = notrans(ta), bn = notrans(tb);
   const int ar = an ? m : k, ac = an ? k : m, br = bn ? k : n, bc = bn ? n : k;
   const size_t mn = (size_t)m * n;
@@ -183,13 +206,16 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
   } else if (kind == 2) {
     const size_t wc = crt_workspace_bytes(m, n, k, kCrtMaxModuli);
     if (wc > ws_need) ws_need = wc;
+  } else if (plain_kind) {
+    const size_t wp = 16 * mn * (f32 ? 4 : 8);  // the slices of the largest split
+    if (wp > ws_need) ws_need = wp;
   }
-  if (!cref.alloc(mn * 8) || !ctest.alloc(mn * (kind == 0 ? 4 : 8)) || !ws.alloc(ws_need) ||
+  if (!cref.alloc(mn * 8) || !ctest.alloc(mn * (f32 ? 4 : 8)) || !ws.alloc(ws_need) ||
       !dstats.alloc(3 * sizeof(double)))
     return GB300_ERR_NOMEM;
   const double *Ad = static_cast<const double *>(A), *Bd = static_cast<const double *>(B);
   int Alda = lda, Bldb = ldb;
-  if (kind == 0) {  // exact FP64 copies of the FP32 operands for the reference
+  if (f32) {  // exact FP64 copies of the FP32 operands for the reference
     if (!a64.alloc((size_t)ar * ac * 8) || !b64.alloc((size_t)br * bc * 8)) return GB300_ERR_NOMEM;
     widen_kernel<<<1024, 256, 0, st>>>(static_cast<const float *>(A), lda, ar, ac,
                                        static_cast<double *>(a64.p));
@@ -209,22 +235,26 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
   if (rc != GB300_OK) return rc;
 
   // run one candidate into ctest (C = 0 first: beta = 0 still multiplies C)
+  // (plain kinds: form 1 is the plain kernel with room for the split-K
+  // slices, split and depth as set by the knobs)
   auto run = [&](int form, int param, int chunk) -> int {
-    if (cudaMemsetAsync(ctest.p, 0, mn * (kind == 0 ? 4 : 8), st) != cudaSuccess)
+    if (cudaMemsetAsync(ctest.p, 0, mn * (f32 ? 4 : 8), st) != cudaSuccess)
       return GB300_ERR_CUDA;
-    if (kind == 0) {
+    void *pws = (plain_kind && form == 1) ? ws.p : nullptr;
+    const size_t pwb = pws ? ws_need : 0;
+    if (f32) {
       float *Ct = static_cast<float *>(ctest.p);
-      if (form == 0)
+      if (form == 0 || plain_kind)
         return plain_sgemm(ta, tb, m, n, k, 1.0f, static_cast<const float *>(A), lda,
-                           static_cast<const float *>(B), ldb, 0.0f, Ct, m, st, err);
+                           static_cast<const float *>(B), ldb, 0.0f, Ct, m, st, err, pws, pwb);
       return split_sgemm(ta, tb, m, n, k, 1.0f, static_cast<const float *>(A), lda,
                          static_cast<const float *>(B), ldb, 0.0f, Ct, m, param, ws.p, ws_need,
                          st, err, chunk);
     }
     double *Ct = static_cast<double *>(ctest.p);
-    if (form == 0)
+    if (form == 0 || plain_kind)
       return plain_dgemm(ta, tb, m, n, k, 1.0, static_cast<const double *>(A), lda,
-                         static_cast<const double *>(B), ldb, 0.0, Ct, m, st, err);
+                         static_cast<const double *>(B), ldb, 0.0, Ct, m, st, err, pws, pwb);
     if (kind == 2)
       return crt_dgemm(ta, tb, m, n, k, 1.0, static_cast<const double *>(A), lda,
                        static_cast<const double *>(B), ldb, 0.0, Ct, m, param, ws.p, ws_need, st,
@@ -251,10 +281,45 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
 
   Stats plain{};
   if ((rc = run(0, 0, 0)) != GB300_OK) return rc;
-  if ((rc = measure(ctest.p, kind != 0, m, n, Cr, stats, st, &plain)) != GB300_OK) return rc;
+  if ((rc = measure(ctest.p, !f32, m, n, Cr, stats, st, &plain)) != GB300_OK) return rc;
 
   TuneEntry best;
   bool found = false;
+  if (plain_kind) {
+    // split-K x ring depth: the fastest (the caller's knobs are restored)
+    const int user_split = plain_split_override(), user_stages = plain_stages_override();
+    const int BK = f32 ? 32 : 16, ktiles = (k + BK - 1) / BK;
+    const int splits[8] = {1, 2, 3, 4, 6, 8, 12, 16}, depths[2] = {4, 6};
+    for (int S : splits) {
+      if (S > 1 && ktiles / S < 8) break;
+      for (int d : depths) {
+        set_plain_split_k(S);
+        set_plain_stages(d);
+        double ms = 0;
+        rc = timed(0, 0, &ms);
+        Stats e{};
+        if (rc == GB300_OK) rc = measure(ctest.p, !f32, m, n, Cr, stats, st, &e);
+        if (rc != GB300_OK) break;
+        if (!found || ms < best.ms) {
+          found = true;
+          best.param = S; best.stages = d; best.ms = ms;
+          best.err_max = e.max_rel; best.err_fro = e.fro;
+        }
+      }
+      if (rc != GB300_OK) break;
+    }
+    set_plain_split_k(user_split);
+    set_plain_stages(user_stages);
+    if (rc != GB300_OK) return rc;
+    best.plain_max = plain.max_rel;
+    best.plain_fro = plain.fro;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune[tune_key(kind, m, n, k)] = best;
+    }
+    if (chosen) *chosen = best.param;
+    return GB300_OK;
+  }
   if (kind == 0) {
     const int Ps[3] = {3, 6, kFp16x3}, chunks[3] = {2, 4, 8};
     for (int P : Ps)
@@ -364,9 +429,9 @@ int tune_cache_save(const char *path) {
     fprintf(f,
             "  {\"key\": \"%s\", \"param\": %d, \"chunk\": %d, \"ms\": %.6g, \"err_max\": %.6g, "
             "\"err_fro\": %.6g, \"plain_max\": %.6g, \"plain_fro\": %.6g, \"tile\": %d, "
-            "\"pair\": %d}%s\n",
+            "\"pair\": %d, \"stages\": %d}%s\n",
             kv.first.c_str(), e.param, e.chunk, e.ms, e.err_max, e.err_fro, e.plain_max,
-            e.plain_fro, e.tile, e.pair, ++i < g_tune.size() ? "," : "");
+            e.plain_fro, e.tile, e.pair, e.stages, ++i < g_tune.size() ? "," : "");
   }
   fprintf(f, "]}\n");
   return fclose(f) == 0 ? GB300_OK : GB300_ERR_ARG;
@@ -398,13 +463,19 @@ int tune_cache_load(const char *path, int *loaded) {
     const char *pp = strstr(line, "\"pair\":");
     if (pp && sscanf(pp, "\"pair\": %d", &e.pair) != 1) e.pair = 0;
     if (e.pair != 1 && e.pair != 2) e.pair = 0;
+    const char *sp = strstr(line, "\"stages\":");
+    if (sp && sscanf(sp, "\"stages\": %d", &e.stages) != 1) e.stages = 0;
+    if (e.stages != 4 && e.stages != 6) e.stages = 0;
     const bool bx = strncmp(key, "bf16x:", 6) == 0, oz = strncmp(key, "ozaki:", 6) == 0;
     const bool cr = strncmp(key, "crt:", 4) == 0;
+    const bool pl = strncmp(key, "plain_d:", 8) == 0 || strncmp(key, "plain_s:", 8) == 0;
     if (bx && split_products_ok(e.param) && e.chunk >= 0 && e.chunk <= 64)
       add[key] = e;
     else if (oz && e.param >= 2 && e.param <= kOzakiMaxSlices)
       add[key] = e;
     else if (cr && e.param >= 2 && e.param <= kCrtMaxModuli)
+      add[key] = e;
+    else if (pl && e.param >= 1 && e.param <= 16)
       add[key] = e;
   }
   fclose(f);

@@ -33,35 +33,37 @@ namespace gb300 {
 
 // The FP32 kernel has no dedicated producer warp: 8 warps (256 threads, up to
 // 255 registers each) all compute, and thread 0 also refills the ring with TMA
-// kStages-1 tiles ahead.  With a ninth warp the register budget drops to 168
+// ST - 1 tiles ahead.  With a ninth warp the register budget drops to 168
 // and the K-major variants spill into the inner loop.
 constexpr int kThreadsS = kConsumerWarps * 32;
 
-template <bool AK, bool BK_>
+template <bool AK, bool BK_, int ST>
 __global__ void __launch_bounds__(kThreadsS, 1)
 sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    OperandDesc opA, OperandDesc opB, int use_tma, int m, int n, int k, float alpha,
                    float beta, float *__restrict__ C, int ldc, int tiles_m, int tiles_n,
-                   unsigned *err) {
+                   int kt_per, float *__restrict__ part, unsigned *err) {
   constexpr int BK = PlainTraits<float>::BK;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
   float *sA = reinterpret_cast<float *>(smem);
-  float *sB = sA + kStages * kBM * BK;
-  uint64_t *full = reinterpret_cast<uint64_t *>(sB + kStages * kBN * BK);
-  uint64_t *empty = full + kStages;
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kStages);
+  float *sB = sA + ST * kBM * BK;
+  uint64_t *full = reinterpret_cast<uint64_t *>(sB + ST * kBN * BK);
+  uint64_t *empty = full + ST;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + ST);
 
   int tmi, tni;
   tile_coords(blockIdx.x, tiles_m, tiles_n, kGroupM, tmi, tni);
   const int m0 = tmi * kBM, n0 = tni * kBN;
-  const int ktiles = (k + BK - 1) / BK;
+  // K slice blockIdx.y: k-tiles [kt0, kt0 + ktiles) (split-K; one slice otherwise)
+  const int kt0 = (int)blockIdx.y * kt_per;
+  const int ktiles = max(0, min((k + BK - 1) / BK - kt0, kt_per));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool tma = use_tma != 0;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < ST; ++s) {
       mbar_init(&full[s], tma ? 1 : kThreadsS);
       mbar_init(&empty[s], kConsumerWarps);
     }
@@ -71,13 +73,13 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
   }
   __syncthreads();
 
-  // Fill k-tile kt into its stage.  TMA: thread 0 only.  Fallback: every thread
-  // copies a strided share of the elements with cp.async and arrives once.
+  // Fill the slice's k-tile kt into its stage.  TMA: thread 0 only.  Fallback:
+  // every thread copies a strided share of the elements with cp.async and arrives once.
   auto fill = [&](int kt) {
-    const int s = kt % kStages;
+    const int s = kt % ST;
     float *ta = sA + s * (kBM * BK);
     float *tb = sB + s * (kBN * BK);
-    const int k0 = kt * BK;
+    const int k0 = (kt0 + kt) * BK;
     if (tma) {
       if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(&full[s], 2 * tile_bytes<float>());
@@ -126,21 +128,21 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = make_float2(0.f, 0.f);
 
-  for (int kt = 0; kt < kStages - 1 && kt < ktiles; ++kt) fill(kt);
+  for (int kt = 0; kt < ST - 1 && kt < ktiles; ++kt) fill(kt);
 
   bool ok = true;
   for (int kt = 0; kt < ktiles; ++kt) {
-    // refill the stage consumed in iteration kt-1 with k-tile kt + kStages - 1
-    const int nk = kt + kStages - 1;
+    // refill the stage consumed in iteration kt-1 with k-tile kt + ST - 1
+    const int nk = kt + ST - 1;
     if (nk < ktiles) {
       if (kt >= 1 && (!tma || threadIdx.x == 0)) {
-        if (!mbar_wait(&empty[nk % kStages], ((nk / kStages) - 1) & 1, err, kErrTimeoutEmpty,
+        if (!mbar_wait(&empty[nk % ST], ((nk / ST) - 1) & 1, err, kErrTimeoutEmpty,
                        abort_flag)) { ok = false; break; }
       }
       fill(nk);
     }
-    const int s = kt % kStages;
-    if (!mbar_wait(&full[s], (kt / kStages) & 1, err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
+    const int s = kt % ST;
+    if (!mbar_wait(&full[s], (kt / ST) & 1, err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
     const float *ta = sA + s * (kBM * BK);
     const float *tb = sB + s * (kBN * BK);
     if constexpr (mode == kPairJ) {
@@ -210,6 +212,20 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
     else if constexpr (mode == kPairI) return (i & 1) ? acc[i >> 1][j].y : acc[i >> 1][j].x;
     else return acc[i][j].x + acc[i][j].y;
   };
+  if (part) {  // split-K: the slice's raw sums, combined by splitk_reduce_kernel
+    float *ps = part + (int64_t)blockIdx.y * m * n;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int col = n0 + f32_row<BK_>(tn, j);
+      if (col >= n) continue;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int row = m0 + f32_row<AK>(tm, i);
+        if (row < m) ps[(int64_t)col * m + row] = value(i, j);
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const int col = n0 + f32_row<BK_>(tn, j);
@@ -235,30 +251,32 @@ sgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 // ---------------------------------------------------------------------------
 // FP64 consumer: m16n8k8 DMMA fragments, warp tile 64 (m) x 32 (n)
 // ---------------------------------------------------------------------------
-template <bool AK, bool BK_>
+template <bool AK, bool BK_, int ST>
 __global__ void __launch_bounds__(kThreads, 1)
 dgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    OperandDesc opA, OperandDesc opB, int use_tma, int m, int n, int k,
                    double alpha, double beta, double *__restrict__ C, int ldc, int tiles_m,
-                   int tiles_n, unsigned *err) {
+                   int tiles_n, int kt_per, double *__restrict__ part, unsigned *err) {
   constexpr int BK = PlainTraits<double>::BK;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
   double *sA = reinterpret_cast<double *>(smem);
-  double *sB = sA + kStages * kBM * BK;
-  uint64_t *full = reinterpret_cast<uint64_t *>(sB + kStages * kBN * BK);
-  uint64_t *empty = full + kStages;
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kStages);
+  double *sB = sA + ST * kBM * BK;
+  uint64_t *full = reinterpret_cast<uint64_t *>(sB + ST * kBN * BK);
+  uint64_t *empty = full + ST;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + ST);
 
   int tmi, tni;
   tile_coords(blockIdx.x, tiles_m, tiles_n, kGroupM, tmi, tni);
   const int m0 = tmi * kBM, n0 = tni * kBN;
-  const int ktiles = (k + BK - 1) / BK;
+  // K slice blockIdx.y: k-tiles [kt0, kt0 + ktiles) (split-K; one slice otherwise)
+  const int kt0 = (int)blockIdx.y * kt_per;
+  const int ktiles = max(0, min((k + BK - 1) / BK - kt0, kt_per));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < ST; ++s) {
       mbar_init(&full[s], use_tma ? 1 : 32);
       mbar_init(&empty[s], kConsumerWarps);
     }
@@ -269,8 +287,8 @@ dgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
   __syncthreads();
 
   if (warp == kConsumerWarps) {
-    producer_loop<double, AK, BK_>(&tmA, &tmB, opA, opB, use_tma != 0, sA, sB, full, empty, m0,
-                                   n0, ktiles, err, abort_flag);
+    producer_loop<double, AK, BK_, ST>(&tmA, &tmB, opA, opB, use_tma != 0, sA, sB, full, empty,
+                                       m0, n0, kt0, ktiles, err, abort_flag);
     return;
   }
 
@@ -286,8 +304,8 @@ dgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 
   bool ok = true;
   for (int kt = 0; kt < ktiles; ++kt) {
-    const int s = kt % kStages;
-    if (!mbar_wait(&full[s], (kt / kStages) & 1, err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
+    const int s = kt % ST;
+    if (!mbar_wait(&full[s], (kt / ST) & 1, err, kErrTimeoutFull, abort_flag)) { ok = false; break; }
     const double *ta = sA + s * (kBM * BK);
     const double *tb = sB + s * (kBN * BK);
 #pragma unroll
@@ -316,6 +334,24 @@ dgemm_plain_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
   }
   if (!ok) return;
 
+  if (part) {  // split-K: the slice's raw sums, combined by splitk_reduce_kernel
+    double *ps = part + (int64_t)blockIdx.y * m * n;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int cj = 0; cj < 2; ++cj) {
+        const int col = n0 + wn * 32 + j * 8 + 2 * t + cj;
+        if (col >= n) continue;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int ri = 0; ri < 2; ++ri) {
+            const int row = m0 + wm * 64 + i * 16 + g + 8 * ri;
+            if (row < m) ps[(int64_t)col * m + row] = acc[i][j][2 * ri + cj];
+          }
+      }
+    return;
+  }
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
 #pragma unroll
@@ -395,38 +431,151 @@ __global__ void scale_c_kernel(int m, int n, T beta, T add, T *__restrict__ C, i
   }
 }
 
+// Split-K combination: C = beta * C, then C += alpha * P_s for s = 0, 1, ...
+// in slice order (the reference applies C_MULT_BETA first and then adds each
+// K block's sum to C, src/gemm_driver.c:133,156-190).  P: S slices of m x n
+// (ld m).  beta == 0 still multiplies, so NaN / Inf in C propagate.
+template <typename T>
+__global__ void __launch_bounds__(256) splitk_reduce_kernel(int m, int n, int S,
+                                                            const T *__restrict__ P, T alpha,
+                                                            T beta, T *__restrict__ C, int ldc) {
+  const int64_t total = (int64_t)m * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int col = (int)(e / m), row = (int)(e % m);
+    T *p = C + (int64_t)col * ldc + row;
+    T c = (beta == T(1)) ? *p : *p * beta;
+    for (int sl = 0; sl < S; ++sl) c = fma(alpha, P[sl * total + e], c);
+    *p = c;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+  }
+  return n;
+}
+
+// Split-K factor and ring depth of the plain kernels (GB300_TUNE_SPLIT_K,
+// GB300_TUNE_PLAIN_STAGES; 0 = the tuned value of the shape class, else by
+// shape / the default depth).
+static int g_split_k = 0, g_plain_stages = 0;
+void set_plain_split_k(int v) { g_split_k = v; }
+void set_plain_stages(int v) { g_plain_stages = v; }
+int plain_split_override() { return g_split_k; }
+int plain_stages_override() { return g_plain_stages; }
+
+// Split-K by shape: the factor S in 1..16 that minimises the modelled time
+// ceil(tiles * S / SMs) waves x (ceil(ktiles / S) + 2) k-tiles (2: the ring's
+// fill and drain) plus the combination pass (S + 2 slices of m x n through
+// HBM, in k-tile times), with at least 8 k-tiles (128 or 256 K) per slice.
+// Outputs of two or more full waves keep S = 1.
+static int split_k_by_shape(bool dbl, int m, int n, int k) {
+  const int64_t tiles = (int64_t)((m + kBM - 1) / kBM) * ((n + kBN - 1) / kBN);
+  const int BK = dbl ? PlainTraits<double>::BK : PlainTraits<float>::BK;
+  const int ktiles = (k + BK - 1) / BK;
+  const int sms = sm_count();
+  if (tiles >= 2 * sms || ktiles < 16) return 1;
+  // one k-tile of one CTA: 2 * 128 * 128 * BK flop at the pipe's per-SM rate
+  // (FP64 1.05 TFLOP/s, FFMA about 55 TFLOP/s over 152 SMs)
+  const double ktile_s = 2.0 * kBM * kBN * BK / ((dbl ? 1.05e12 : 55e12) / 152);
+  const double slice_s = (double)m * n * (dbl ? 8 : 4) / 6.5e12;
+  double best = 0;
+  int bs = 1;
+  for (int S = 1; S <= 16 && (S == 1 || ktiles / S >= 8); ++S) {
+    const double waves = (double)((tiles * S + sms - 1) / sms);
+    const double t = waves * ((ktiles + S - 1) / S + 2) * ktile_s +
+                     (S > 1 ? (S + 2) * slice_s : 0.0);
+    if (S == 1 || t < best) { best = t; bs = S; }
+  }
+  return bs;
+}
+
+int plain_split_k(int is_double, int m, int n, int k) {
+  const int BK = is_double ? PlainTraits<double>::BK : PlainTraits<float>::BK;
+  const int ktiles = (k + BK - 1) / BK;
+  int S = g_split_k;
+  if (!S) S = tune_plain_split(is_double ? 3 : 4, m, n, k);
+  if (!S) S = split_k_by_shape(is_double != 0, m, n, k);
+  if (S > ktiles) S = ktiles;
+  if (S > 65535) S = 65535;
+  return S < 1 ? 1 : S;
+}
+
+static int plain_stages_for(int is_double, int m, int n, int k) {
+  int st = g_plain_stages;
+  if (!st) st = tune_plain_stages(is_double ? 3 : 4, m, n, k);
+  return st == 6 ? 6 : kStages;
+}
+
+size_t plain_workspace_bytes(int is_double, int m, int n, int k) {
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  const int S = plain_split_k(is_double, m, n, k);
+  return S > 1 ? (size_t)S * m * n * (is_double ? 8 : 4) : 0;
+}
 template <typename T>
 static void make_desc(OperandDesc &d, const T *p, int ld, int rows, int cols) {
   d.ptr = p; d.ld = ld; d.rows = rows; d.cols = cols;
 }
 
-template <typename T, bool AK, bool BK_>
+template <typename T, bool AK, bool BK_, int ST>
 static int launch_one(const CUtensorMap &tA, const CUtensorMap &tB, const OperandDesc &oA,
                       const OperandDesc &oB, bool tma, int m, int n, int k, T alpha, T beta, T *C,
-                      int ldc, cudaStream_t st, unsigned *err) {
+                      int ldc, int S, T *part, cudaStream_t st, unsigned *err) {
   const int tiles_m = (m + kBM - 1) / kBM, tiles_n = (n + kBN - 1) / kBN;
-  const int smem = plain_smem_bytes<T>();
+  const int smem = plain_smem_bytes<T, ST>();
   void (*kern)(const CUtensorMap, const CUtensorMap, OperandDesc, OperandDesc, int, int, int, int,
-               T, T, T *, int, int, int, unsigned *);
+               T, T, T *, int, int, int, int, T *, unsigned *);
   if constexpr (sizeof(T) == 4)
-    kern = sgemm_plain_kernel<AK, BK_>;
+    kern = sgemm_plain_kernel<AK, BK_, ST>;
   else
-    kern = dgemm_plain_kernel<AK, BK_>;
+    kern = dgemm_plain_kernel<AK, BK_, ST>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return GB300_ERR_CUDA;
   const int64_t ntiles = (int64_t)tiles_m * tiles_n;
   if (ntiles > 0x7fffffff) return GB300_ERR_ARG;
-  kern<<<(unsigned)ntiles, sizeof(T) == 4 ? kThreadsS : kThreads, smem, st>>>(tA, tB, oA, oB, tma ? 1 : 0, m, n, k, alpha, beta,
-                                                  C, ldc, tiles_m, tiles_n, err);
-  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+  constexpr int BK = PlainTraits<T>::BK;
+  const int ktiles = (k + BK - 1) / BK;
+  const int kt_per = (ktiles + S - 1) / S;
+  const int slices = (ktiles + kt_per - 1) / kt_per;  // every slice has a k-tile
+  kern<<<dim3((unsigned)ntiles, (unsigned)slices), sizeof(T) == 4 ? kThreadsS : kThreads, smem,
+         st>>>(tA, tB, oA, oB, tma ? 1 : 0, m, n, k, alpha, beta, C, ldc, tiles_m, tiles_n,
+               kt_per, slices > 1 ? part : nullptr, err);
+  if (cudaGetLastError() != cudaSuccess) return GB300_ERR_CUDA;
+  if (slices > 1) {
+    const int64_t total = (int64_t)m * n;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > sm_count() * 8) blocks = sm_count() * 8;
+    splitk_reduce_kernel<T><<<blocks, 256, 0, st>>>(m, n, slices, part, alpha, beta, C, ldc);
+    if (cudaGetLastError() != cudaSuccess) return GB300_ERR_CUDA;
+  }
+  return GB300_OK;
+}
+
+template <typename T, bool AK, bool BK_>
+static int launch_depth(int ST, const CUtensorMap &tA, const CUtensorMap &tB,
+                        const OperandDesc &oA, const OperandDesc &oB, bool tma, int m, int n,
+                        int k, T alpha, T beta, T *C, int ldc, int S, T *part, cudaStream_t st,
+                        unsigned *err) {
+  if (ST == 6)
+    return launch_one<T, AK, BK_, 6>(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, S, part,
+                                     st, err);
+  return launch_one<T, AK, BK_, kStages>(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, S,
+                                         part, st, err);
 }
 
 template <typename T>
 static int plain_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *A, int lda,
-                      const T *B, int ldb, T beta, T *C, int ldc, cudaStream_t st, unsigned *err) {
+                      const T *B, int ldb, T beta, T *C, int ldc, cudaStream_t st, unsigned *err,
+                      void *ws, size_t ws_bytes) {
   const bool an = notrans(ta), bn = notrans(tb);
   const int arows = an ? m : k, brows = bn ? k : n;
   if (m < 0 || n < 0 || k < 0 || lda < (arows > 1 ? arows : 1) ||
@@ -458,22 +607,37 @@ static int plain_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *A
           encode_2d(&tB, B, sizeof(T), oB.rows, oB.cols, ldb, bn ? BK : kBN, bn ? kBN : BK,
                     /*swizzle128=*/bn);
   }
+  // split-K where the caller gave room for its slices (else one slice)
+  const int dbl = sizeof(T) == 8 ? 1 : 0;
+  int S = plain_split_k(dbl, m, n, k);
+  if (S > 1 && (!ws || ws_bytes < (size_t)S * m * n * sizeof(T))) S = 1;
+  T *part = static_cast<T *>(ws);
+  const int ST = plain_stages_for(dbl, m, n, k);
   const bool AK = !an, BKm = bn;
-  if (!AK && !BKm) return launch_one<T, false, false>(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, st, err);
-  if (!AK && BKm)  return launch_one<T, false, true >(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, st, err);
-  if (AK && !BKm)  return launch_one<T, true,  false>(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, st, err);
-  return launch_one<T, true, true>(tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, st, err);
+  if (!AK && !BKm)
+    return launch_depth<T, false, false>(ST, tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc,
+                                         S, part, st, err);
+  if (!AK && BKm)
+    return launch_depth<T, false, true>(ST, tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc,
+                                        S, part, st, err);
+  if (AK && !BKm)
+    return launch_depth<T, true, false>(ST, tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc,
+                                        S, part, st, err);
+  return launch_depth<T, true, true>(ST, tA, tB, oA, oB, tma, m, n, k, alpha, beta, C, ldc, S,
+                                     part, st, err);
 }
 
 int plain_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                 const double *B, int ldb, double beta, double *C, int ldc, cudaStream_t st,
-                unsigned *err) {
-  return plain_gemm<double>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err);
+                unsigned *err, void *ws, size_t ws_bytes) {
+  return plain_gemm<double>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err, ws,
+                            ws_bytes);
 }
 int plain_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
                 const float *B, int ldb, float beta, float *C, int ldc, cudaStream_t st,
-                unsigned *err) {
-  return plain_gemm<float>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err);
+                unsigned *err, void *ws, size_t ws_bytes) {
+  return plain_gemm<float>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, st, err, ws,
+                           ws_bytes);
 }
 
 }  // namespace gb300

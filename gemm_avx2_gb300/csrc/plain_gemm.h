@@ -49,12 +49,28 @@ bool encode_2d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t ro
 int copy_2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, int cols,
             cudaStream_t st);
 
+// ws / ws_bytes: room for the split-K slices (plain_workspace_bytes); without
+// it (or too little) the call runs as one K slice.
 int plain_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                 const double *B, int ldb, double beta, double *C, int ldc, cudaStream_t st,
-                unsigned *err);
+                unsigned *err, void *ws = nullptr, size_t ws_bytes = 0);
 int plain_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
                 const float *B, int ldb, float beta, float *C, int ldc, cudaStream_t st,
-                unsigned *err);
+                unsigned *err, void *ws = nullptr, size_t ws_bytes = 0);
+// Split-K of the plain kernels: the factor a call of this shape uses (knob,
+// tuned value of the shape class, else by shape: only outputs of less than
+// two waves of tiles are split) and the workspace its slices need (0: none).
+// The slices' sums are combined in K order by a second kernel.
+int plain_split_k(int is_double, int m, int n, int k);
+size_t plain_workspace_bytes(int is_double, int m, int n, int k);
+void set_plain_split_k(int v);
+void set_plain_stages(int v);
+int plain_split_override();
+int plain_stages_override();
+// Tuned split-K factor and ring depth of the plain kernels for a shape class
+// (kind 3: FP64, 4: FP32; 0 = not tuned).
+int tune_plain_split(int kind, int m, int n, int k);
+int tune_plain_stages(int kind, int m, int n, int k);
 
 // Grouped plain GEMMs (grouped.cu).
 size_t grouped_workspace_bytes(int count);

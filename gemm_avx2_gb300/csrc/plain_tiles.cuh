@@ -30,9 +30,11 @@ template <typename T>
 __host__ __device__ constexpr int tile_bytes() {
   return kBM * PlainTraits<T>::BK * (int)sizeof(T);
 }
-template <typename T>
+// ST: ring depth (stages) of the single-problem kernels (kStages by default;
+// the tuned depth of the shape class otherwise).
+template <typename T, int ST = kStages>
 __host__ __device__ constexpr int plain_smem_bytes() {
-  return kStages * 2 * tile_bytes<T>() + 1024 /*alignment slack*/ + 256 /*barriers*/;
+  return ST * 2 * tile_bytes<T>() + 1024 /*alignment slack*/ + 256 /*barriers*/;
 }
 
 constexpr int kGroupM = 16;
@@ -84,22 +86,24 @@ __device__ __forceinline__ void fallback_fill(T *tile, const OperandDesc &op, in
   }
 }
 
-template <typename T, bool AK, bool BK_>
+// Fills k-tiles kt0 .. kt0 + ktiles - 1 (a K slice) into an ST-deep ring.
+template <typename T, bool AK, bool BK_, int ST>
 __device__ __forceinline__ void producer_loop(const CUtensorMap *tmA, const CUtensorMap *tmB,
                                               const OperandDesc &opA, const OperandDesc &opB,
                                               bool use_tma, T *sA, T *sB, uint64_t *full,
-                                              uint64_t *empty, int m0, int n0, int ktiles,
-                                              unsigned *err, volatile int *abort_flag) {
+                                              uint64_t *empty, int m0, int n0, int kt0,
+                                              int ktiles, unsigned *err,
+                                              volatile int *abort_flag) {
   constexpr int BK = PlainTraits<T>::BK;
   const int lane = threadIdx.x & 31;
   for (int kt = 0; kt < ktiles; ++kt) {
-    const int s = kt % kStages;
-    if (kt >= kStages) {
-      if (!mbar_wait(&empty[s], ((kt / kStages) - 1) & 1, err, kErrTimeoutEmpty, abort_flag)) return;
+    const int s = kt % ST;
+    if (kt >= ST) {
+      if (!mbar_wait(&empty[s], ((kt / ST) - 1) & 1, err, kErrTimeoutEmpty, abort_flag)) return;
     }
     T *ta = sA + s * (kBM * BK);
     T *tb = sB + s * (kBN * BK);
-    const int k0 = kt * BK;
+    const int k0 = (kt0 + kt) * BK;
     if (use_tma) {
       if (lane == 0) {
         mbar_arrive_expect_tx(&full[s], 2 * tile_bytes<T>());

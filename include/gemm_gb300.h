@@ -358,13 +358,19 @@ int gb300_selftest_wait_timeout(unsigned poll_limit);
  * sgemm_tune.h, src/gemm_set_parameters.h:1-61).  kind 0 = BF16xP SGEMM
  * (chooses products 3/6 and the hi*hi chunk length), kind 1 = Ozaki DGEMM
  * (chooses the slice count 4..12), kind 2 = CRT DGEMM (gb300_dgemm_ozaki2;
- * chooses the moduli count 11..24).  gb300_autotune runs the candidates on the
- * given device operands (FP32 for kind 0, FP64 for kinds 1, 2) and keeps the fastest
- * whose max and Frobenius relative errors against a near-exact FP64 reference
- * (the Ozaki form with 12 slices) do not exceed the plain kernel's; the result
- * is cached for the shape class (floor(log2) of m, n, k) and used whenever a
- * split entry point gets products = 0 / slices = 0 / moduli = 0.  It allocates temporary
- * device memory and synchronises `stream`.
+ * chooses the moduli count 11..24), then for these three the output tile
+ * width and the cluster mode; kind 3 / 4 = the plain DGEMM / SGEMM kernels
+ * (gb300_dgemm / gb300_sgemm and the drop-ins: chooses the split-K factor
+ * 1..16 and the ring depth 4 / 6 -- the reference's BDK / LOOP_TIMES_K
+ * blocking, dgemm_tune.h:6-10, sgemm_tune.h:7-11).  gb300_autotune runs the
+ * candidates on the given device operands (FP32 for kinds 0 and 4, FP64 for
+ * kinds 1, 2, 3).  For kinds 0-2 it keeps the fastest whose max and Frobenius
+ * relative errors against a near-exact FP64 reference (the Ozaki form with 12
+ * slices) do not exceed the plain kernel's; for kinds 3, 4 the fastest (every
+ * split sums the same products in K order).  The result is cached for the
+ * shape class (floor(log2) of m, n, k) and used whenever a split entry point
+ * gets products = 0 / slices = 0 / moduli = 0, and by every plain call of the
+ * class.  It allocates temporary device memory and synchronises `stream`.
  * gb300_tune_lookup: the parameters products/slices = 0 resolve to for a
  * shape (GB300_OK if a tuned entry exists, GB300_ERR_UNSUPPORTED if the
  * defaults apply: 6 products, chunk 4, 8 slices, 16 moduli).
@@ -380,6 +386,11 @@ int gb300_tune_lookup(int kind, int m, int n, int k, int *param, int *chunk);
  * 128-row tile always runs one CTA per tile); GB300_ERR_UNSUPPORTED when the
  * shape class has no tuned entry. */
 int gb300_tune_layout(int kind, int m, int n, int k, int *tile_n, int *pair_mma);
+/* The split-K factor and ring depth the plain kernels use for this shape
+ * (knob, tuned entry of the shape class, else by shape / 4 stages; without
+ * room for the slices -- no cached workspace -- a call runs unsplit);
+ * GB300_ERR_UNSUPPORTED when the shape class has no tuned entry. */
+int gb300_plain_layout(int is_double, int m, int n, int k, int *split_k, int *stages);
 int gb300_tune_cache_save(const char *path);
 int gb300_tune_cache_load(const char *path, int *loaded);
 void gb300_tune_cache_clear(void);
@@ -419,14 +430,25 @@ void gb300_tune_cache_clear(void);
  *   moduli of its tile; 2 = one modulus of one tile (the moduli are
  *   independent GEMMs, so small outputs still fill the GPU); 0 restores the
  *   choice by shape (2 when the tiles alone fill fewer than four waves).
- *   Same results bit for bit. */
+ *   Same results bit for bit.
+ *   GB300_TUNE_SPLIT_K: K slices of the plain kernels (gb300_dgemm,
+ *   gb300_sgemm, the drop-ins; the role of the reference's K blocking,
+ *   src/gemm_driver.c:156-190): 1 = none, S = 2..65535 (at most one slice per
+ *   k-tile); each slice's sums go to library-owned scratch and a second
+ *   kernel adds them to beta*C in K order.  0 restores the choice by shape
+ *   (tuned, else split outputs of less than two waves of tiles).  Results
+ *   differ from the unsplit call only in the grouping of the K sum.
+ *   GB300_TUNE_PLAIN_STAGES: ring depth of the plain kernels, 4 or 6; 0
+ *   restores the default (tuned, else 4). */
 enum {
   GB300_TUNE_BF16X_CHUNK = 1,
   GB300_TUNE_GRAPH_BRANCHES = 2,
   GB300_TUNE_TILE_N = 3,
   GB300_TUNE_PAIR_MMA = 4,
   GB300_TUNE_HOST_PARTS = 5,
-  GB300_TUNE_MODULUS_SPLIT = 6
+  GB300_TUNE_MODULUS_SPLIT = 6,
+  GB300_TUNE_SPLIT_K = 7,
+  GB300_TUNE_PLAIN_STAGES = 8
 };
 int gb300_tune_param(int param, int value);
 

@@ -195,7 +195,7 @@ def test_tune_cache_roundtrip_and_corruption(tmp_path):
     out = tmp_path / "saved.json"
     assert g.tune_cache_save(str(out)) == g.OK
     assert '"key": "bf16x:12:12:12", "param": 259, "chunk": 4' in out.read_text()
-    assert '"tile": 128, "pair": 0}' in out.read_text()
+    assert '"tile": 128, "pair": 0, "stages": 0}' in out.read_text()
     g.tune_cache_clear()
     assert g.tune_cache_load(str(out)) == (g.OK, 4)
     assert g.tune_cache_load(str(tmp_path / "missing.json"))[0] == g.ERR_ARG
@@ -220,4 +220,42 @@ def test_tuning_knobs_validate():
     assert g.tune_param(g.TUNE_MODULUS_SPLIT, 2) == g.OK
     assert g.tune_param(g.TUNE_MODULUS_SPLIT, 3) == g.ERR_ARG
     assert g.tune_param(g.TUNE_MODULUS_SPLIT, 0) == g.OK
+    assert g.tune_param(g.TUNE_SPLIT_K, 65535) == g.OK
+    assert g.tune_param(g.TUNE_SPLIT_K, 65536) == g.ERR_ARG
+    assert g.tune_param(g.TUNE_SPLIT_K, -1) == g.ERR_ARG
+    assert g.tune_param(g.TUNE_SPLIT_K, 0) == g.OK
+    assert g.tune_param(g.TUNE_PLAIN_STAGES, 6) == g.OK
+    assert g.tune_param(g.TUNE_PLAIN_STAGES, 5) == g.ERR_ARG
+    assert g.tune_param(g.TUNE_PLAIN_STAGES, 0) == g.OK
     assert g.tune_param(99, 1) == g.ERR_ARG
+
+
+def test_plain_split_k_by_shape_and_cache(tmp_path):
+    """Host logic of the plain kernels' split-K (no GPU needed): outputs of two
+    or more waves of 128 x 128 tiles stay unsplit; a few tiles with a long K
+    are split, at least 8 k-tiles a slice; a tuned entry and the knob win."""
+    g.tune_cache_clear()
+    assert g.plain_layout("d", 8192, 8192, 8192)[1:] == (1, 4)     # 4096 tiles
+    rc, sk, st = g.plain_layout("d", 256, 256, 65536)               # 4 tiles, 4096 k-tiles
+    assert rc == g.ERR_UNSUPPORTED and 2 <= sk <= 16 and st == 4
+    assert g.plain_layout("s", 256, 256, 100)[1] == 1               # 4 k-tiles: too short
+    sk = g.plain_layout("s", 300, 200, 20000)[1]
+    assert 2 <= sk <= 16 and (20000 + 31) // 32 // sk >= 8
+    assert g.tune_param(g.TUNE_SPLIT_K, 5) == g.OK
+    try:
+        assert g.plain_layout("d", 8192, 8192, 8192)[1] == 5
+        assert g.plain_layout("d", 100, 100, 40)[1] == 3            # at most one per k-tile
+    finally:
+        g.tune_param(g.TUNE_SPLIT_K, 0)
+    f = tmp_path / "plain.json"
+    f.write_text('{"version": 1, "entries": [\n'
+                 '  {"key": "plain_d:8:8:16", "param": 6, "chunk": 0, "ms": 1, "err_max": 0, '
+                 '"err_fro": 0, "plain_max": 0, "plain_fro": 0, "tile": 0, "pair": 0, '
+                 '"stages": 6},\n'
+                 '  {"key": "plain_s:8:8:16", "param": 17, "chunk": 0, "ms": 1, "err_max": 0, '
+                 '"err_fro": 0, "plain_max": 0, "plain_fro": 0},\n'
+                 ']}\n')
+    assert g.tune_cache_load(str(f)) == (g.OK, 1)                   # split 17 rejected
+    assert g.plain_layout("d", 256, 256, 65536) == (g.OK, 6, 6)
+    assert g.tune_lookup(g.TUNE_PLAIN_D, 256, 256, 65536) == (g.OK, 6, 0)
+    g.tune_cache_clear()
