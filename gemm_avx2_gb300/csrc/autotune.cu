@@ -10,7 +10,7 @@
 //                 and its cluster mode (pair MMAs on 2-CTA clusters or one
 //                 CTA per tile);
 //   Ozaki DGEMM : slice count S in [4, 12];
-//   plain D/SGEMM (kinds 3, 4): split-K factor in {1, 2, 3, 4, 6, 8, 12, 16}
+//   plain D/SGEMM (kinds 3, 4): split-K factor in {1, 2, 3, 4, 6, 8, 12, 16, 24, 32}
 //                 (at least 8 k-tiles a slice) x ring depth {4, 6}: the
 //                 fastest, since every split sums the same products in K
 //                 order within the same rounding bound (the reference's own
@@ -289,7 +289,7 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
     // split-K x ring depth: the fastest (the caller's knobs are restored)
     const int user_split = plain_split_override(), user_stages = plain_stages_override();
     const int BK = f32 ? 32 : 16, ktiles = (k + BK - 1) / BK;
-    const int splits[8] = {1, 2, 3, 4, 6, 8, 12, 16}, depths[2] = {4, 6};
+    const int splits[10] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32}, depths[2] = {4, 6};
     for (int S : splits) {
       if (S > 1 && ktiles / S < 8) break;
       for (int d : depths) {
@@ -475,7 +475,7 @@ int tune_cache_load(const char *path, int *loaded) {
       add[key] = e;
     else if (cr && e.param >= 2 && e.param <= kCrtMaxModuli)
       add[key] = e;
-    else if (pl && e.param >= 1 && e.param <= 16)
+    else if (pl && e.param >= 1 && e.param <= 32)
       add[key] = e;
   }
   fclose(f);

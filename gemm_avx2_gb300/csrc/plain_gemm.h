@@ -58,8 +58,8 @@ int plain_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float 
                 const float *B, int ldb, float beta, float *C, int ldc, cudaStream_t st,
                 unsigned *err, void *ws = nullptr, size_t ws_bytes = 0);
 // Split-K of the plain kernels: the factor a call of this shape uses (knob,
-// tuned value of the shape class, else by shape: only outputs of less than
-// two waves of tiles are split) and the workspace its slices need (0: none).
+// tuned value of the shape class, else by a model of waves and ring fill) and
+// the workspace its slices need (0: none).
 // The slices' sums are combined in K order by a second kernel.
 int plain_split_k(int is_double, int m, int n, int k);
 size_t plain_workspace_bytes(int is_double, int m, int n, int k);

@@ -361,7 +361,7 @@ int gb300_selftest_wait_timeout(unsigned poll_limit);
  * chooses the moduli count 11..24), then for these three the output tile
  * width and the cluster mode; kind 3 / 4 = the plain DGEMM / SGEMM kernels
  * (gb300_dgemm / gb300_sgemm and the drop-ins: chooses the split-K factor
- * 1..16 and the ring depth 4 / 6 -- the reference's BDK / LOOP_TIMES_K
+ * 1..32 and the ring depth 4 / 6 -- the reference's BDK / LOOP_TIMES_K
  * blocking, dgemm_tune.h:6-10, sgemm_tune.h:7-11).  gb300_autotune runs the
  * candidates on the given device operands (FP32 for kinds 0 and 4, FP64 for
  * kinds 1, 2, 3).  For kinds 0-2 it keeps the fastest whose max and Frobenius
@@ -436,7 +436,8 @@ void gb300_tune_cache_clear(void);
  *   src/gemm_driver.c:156-190): 1 = none, S = 2..65535 (at most one slice per
  *   k-tile); each slice's sums go to library-owned scratch and a second
  *   kernel adds them to beta*C in K order.  0 restores the choice by shape
- *   (tuned, else split outputs of less than two waves of tiles).  Results
+ *   (tuned, else the factor 1..32 that a model of waves of 128 x 128 tiles
+ *   and ring fill finds fastest, at least 8 k-tiles a slice).  Results
  *   differ from the unsplit call only in the grouping of the K sum.
  *   GB300_TUNE_PLAIN_STAGES: ring depth of the plain kernels, 4 or 6; 0
  *   restores the default (tuned, else 4). */

@@ -231,16 +231,18 @@ def test_tuning_knobs_validate():
 
 
 def test_plain_split_k_by_shape_and_cache(tmp_path):
-    """Host logic of the plain kernels' split-K (no GPU needed): outputs of two
-    or more waves of 128 x 128 tiles stay unsplit; a few tiles with a long K
-    are split, at least 8 k-tiles a slice; a tuned entry and the knob win."""
+    """Host logic of the plain kernels' split-K (no GPU needed): many waves of
+    128 x 128 tiles stay unsplit; a few tiles with a long K are split, at
+    least 8 k-tiles a slice; a tuned entry and the knob win."""
     g.tune_cache_clear()
     assert g.plain_layout("d", 8192, 8192, 8192)[1:] == (1, 4)     # 4096 tiles
+    assert g.plain_layout("d", 32768, 32768, 256)[1] == 1           # rank-256 update
+    assert g.plain_layout("d", 2048, 2048, 2048)[1] > 1             # 1.7 waves
     rc, sk, st = g.plain_layout("d", 256, 256, 65536)               # 4 tiles, 4096 k-tiles
-    assert rc == g.ERR_UNSUPPORTED and 2 <= sk <= 16 and st == 4
+    assert rc == g.ERR_UNSUPPORTED and 16 <= sk <= 32 and st == 4
     assert g.plain_layout("s", 256, 256, 100)[1] == 1               # 4 k-tiles: too short
     sk = g.plain_layout("s", 300, 200, 20000)[1]
-    assert 2 <= sk <= 16 and (20000 + 31) // 32 // sk >= 8
+    assert 2 <= sk <= 32 and (20000 + 31) // 32 // sk >= 8
     assert g.tune_param(g.TUNE_SPLIT_K, 5) == g.OK
     try:
         assert g.plain_layout("d", 8192, 8192, 8192)[1] == 5
@@ -252,10 +254,10 @@ def test_plain_split_k_by_shape_and_cache(tmp_path):
                  '  {"key": "plain_d:8:8:16", "param": 6, "chunk": 0, "ms": 1, "err_max": 0, '
                  '"err_fro": 0, "plain_max": 0, "plain_fro": 0, "tile": 0, "pair": 0, '
                  '"stages": 6},\n'
-                 '  {"key": "plain_s:8:8:16", "param": 17, "chunk": 0, "ms": 1, "err_max": 0, '
+                 '  {"key": "plain_s:8:8:16", "param": 33, "chunk": 0, "ms": 1, "err_max": 0, '
                  '"err_fro": 0, "plain_max": 0, "plain_fro": 0},\n'
                  ']}\n')
-    assert g.tune_cache_load(str(f)) == (g.OK, 1)                   # split 17 rejected
+    assert g.tune_cache_load(str(f)) == (g.OK, 1)                   # split 33 rejected
     assert g.plain_layout("d", 256, 256, 65536) == (g.OK, 6, 6)
     assert g.tune_lookup(g.TUNE_PLAIN_D, 256, 256, 65536) == (g.OK, 6, 0)
     g.tune_cache_clear()
