@@ -66,6 +66,17 @@ WORKLOADS = {
                       ldc=32832, alpha=-1.0, beta=1.0, seed=3),
     "rank256_s": dict(prec="s", ta="N", tb="T", m=32768, n=32768, k=256, lda=32800, ldb=32800,
                       ldc=32832, alpha=-1.0, beta=1.0, seed=3),
+    # the rank-256 updates at a sixteenth of the output, for ncu captures (C still > L2)
+    "rank256_d_8192": dict(prec="d", ta="N", tb="T", m=8192, n=8192, k=256, lda=8224, ldb=8224,
+                           ldc=8256, alpha=-1.0, beta=1.0, seed=3),
+    "rank256_s_8192": dict(prec="s", ta="N", tb="T", m=8192, n=8192, k=256, lda=8224, ldb=8224,
+                           ldc=8256, alpha=-1.0, beta=1.0, seed=3),
+}
+# blocked TRSM (X = alpha inv(op(A)) B, left, lower, no transpose, non-unit
+# diagonal) on the GEMM kernels: m^2 n flops per call
+TRSM_WORKLOADS = {
+    "dtrsm_lln_8192": dict(prec="d", m=8192, n=8192, alpha=1.0, seed=7),
+    "strsm_lln_8192": dict(prec="s", m=8192, n=8192, alpha=1.0, seed=7),
 }
 # complex GEMM (the reference's OpenBLAS-style c/z kernels): the split form on
 # the embedded real problem, at equal error to the plain 4M method
@@ -536,7 +547,11 @@ def parse_form(name):
     import gemm_avx2_gb300 as g
 
     name = name[len("tuned:"):] if name.startswith("tuned:") else name
-    base, *opts = name.split("_") if not name.startswith(("crt_n", "ozaki_s")) else (name,)
+    parts = name.split("_")
+    if name.startswith(("crt_n", "ozaki_s")):  # crt_nN / ozaki_sS, options after
+        base, opts = "_".join(parts[:2]), parts[2:]
+    else:
+        base, opts = parts[0], parts[1:]
     for o in opts:
         if o[:1] == "c" and o[1:].isdigit():
             g.tune_param(g.TUNE_BF16X_CHUNK, int(o[1:]))
@@ -932,6 +947,95 @@ def run_grouped(args, torch, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_trsm(args, torch, rank, world):
+    """TRSM on the GEMM kernels: the diagonal blocks solved by diag_left_kernel,
+    the rest of B updated by GEMMs (plain form, or the split form: Ozaki
+    slices for FP64, 6xBF16 for FP32).  A is lower triangular with a raised
+    diagonal (well conditioned); the accuracy is the sampled backward residual
+    ||op(A) x - alpha b|| / (||A|| ||x||) over 64 columns of the solution."""
+    import numpy as np
+
+    import gemm_avx2_gb300 as g
+
+    w = TRSM_WORKLOADS[args.workload]
+    p, m, n = w["prec"], w["m"], w["n"]
+    dt = torch.float64 if p == "d" else torch.float32
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(w["seed"])
+    # column-major m x m stored as a (cols, rows) tensor: its upper triangle is
+    # A's lower triangle
+    A = (torch.rand((m, m), generator=gen, device="cuda", dtype=dt) * 2 - 1).triu()
+    d = A.diagonal()
+    d.add_(float(m) ** 0.5 * torch.where(d < 0, -1.0, 1.0).to(dt))
+    B0 = torch.rand((n, m), generator=gen, device="cuda", dtype=dt) * 2 - 1
+    B = B0.clone()
+    stream = torch.cuda.current_stream().cuda_stream
+    flops = float(m) * m * n
+
+    def call(form):
+        return g.trsm(p, "L", "L", "N", "N", m, n, w["alpha"], A.data_ptr(), m, B.data_ptr(), m,
+                      form=form, stream=stream)
+
+    def timed(form, steps, warmup):
+        for _ in range(warmup):
+            B.copy_(B0)
+            assert call(form) == g.OK
+        total = 0.0
+        for _ in range(steps):
+            B.copy_(B0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            assert call(form) == g.OK
+            e1.record()
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        return total / steps
+
+    def residual(form):
+        B.copy_(B0)
+        assert call(form) == g.OK
+        torch.cuda.synchronize()
+        cols = np.random.default_rng(5).choice(n, 64, replace=False)
+        Al = A.double().cpu().numpy().T          # A (lower triangular), row-major
+        idx = torch.as_tensor(cols, device="cuda")
+        X = B.index_select(0, idx).double().cpu().numpy().T          # m x 64
+        Bc = B0.index_select(0, idx).double().cpu().numpy().T
+        R = Al @ X - w["alpha"] * Bc
+        return float(np.linalg.norm(R) / (np.linalg.norm(Al) * np.linalg.norm(X)))
+
+    res = {"plain": residual(0), "split": residual(1)}
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    barrier(torch, world)
+    ms_split = timed(1, args.steps, args.warmup)
+    ms_plain = timed(0, max(3, args.steps // 2), args.warmup)
+    barrier(torch, world)
+    clocks = sampler.stop() if sampler else None
+    max_ms = allreduce_max(torch, world, ms_split)
+    value = flops * world / (max_ms / 1e3) / 1e12
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(max_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if p == "d" else "f32",
+        "data": "synthetic (seeded uniform[-1,1), diagonal raised by sqrt(m), on the device)",
+        "config": {"workload": args.workload, "side": "L", "uplo": "L", "transa": "N",
+                   "diag": "N", "m": m, "n": n, "alpha": w["alpha"], "flops_per_call": "m^2 n",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "form": {"name": "split updates (%s)" % ("Ozaki slices" if p == "d" else "6xBF16")},
+        "plain": {"value": round(flops / (ms_plain / 1e3) / 1e12, 3), "unit": "TFLOP/s",
+                  "ms": round(ms_plain, 3)},
+        "accuracy": {"backward_residual": res, "columns": 64},
+        "clocks": clocks,
+        "e2e": {"value": None, "skipped": "device-pointer TRSM API"},
+    }
+    if rank == 0:
+        line["cpu_baseline"] = {"value": None, "skipped": "TRSM workload"}
+        print(json.dumps(line), flush=True)
+
+
 def fp16x3_prepare_launches(ta, tb, k):
     """Kernel launches of the scaled 3xFP16 prepare: k-contiguous operands (op(A)
     rows when A is transposed, op(B) columns when B is not) take the fused max
@@ -1075,6 +1179,11 @@ def run_reference(args, rank, world):
         print(json.dumps({"impl": "reference", "metric": METRIC,
                           "unavailable": "the reference has no grouped interface"}))
         return
+    if args.workload in TRSM_WORKLOADS:
+        print(json.dumps({"impl": "reference", "metric": METRIC,
+                          "unavailable": "the reference's TRSM kernels are x86 AVX2 code "
+                                         "without a driver; they serve as an oracle here"}))
+        return
     cplx = args.workload in CWORKLOADS
     w = dict(CWORKLOADS[args.workload] if cplx else WORKLOADS[args.workload])
     if args.phi is not None and not cplx:
@@ -1122,7 +1231,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(CWORKLOADS) + ["grouped_1024"],
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(CWORKLOADS) +
+                    sorted(TRSM_WORKLOADS) + ["grouped_1024"],
                     default="sgemm_tn_8192")
     ap.add_argument("--phi", type=float, default=None,
                     help="exponent spread of A and B: (u-0.5)*exp(phi*g) (DGEMM NT 16384 sweep)")
@@ -1149,6 +1259,8 @@ def main():
         torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
     if args.workload == "grouped_1024":
         run_grouped(args, torch, rank, world)
+    elif args.workload in TRSM_WORKLOADS:
+        run_trsm(args, torch, rank, world)
     elif args.workload in CWORKLOADS:
         run_complex(args, torch, rank, world)
     else:

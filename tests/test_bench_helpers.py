@@ -27,6 +27,8 @@ def test_parse_form_names(knobs):
     # a tuned name pins chunk, tile width and cluster mode as knobs
     assert bench.parse_form("tuned:fp16x3_c8_t256_pair") == ("bf16x", g.FP16X3)
     assert bench.parse_form("bf16x6_c4_t128_cta") == ("bf16x", 6)
+    assert bench.parse_form("crt_n15_cta") == ("crt", 15)
+    assert bench.parse_form("ozaki_s8_pair_t128") == ("ozaki", 8)
     with pytest.raises(SystemExit):
         bench.parse_form("bf16x6_mc")  # the multicast mode no longer exists
     with pytest.raises(SystemExit):
