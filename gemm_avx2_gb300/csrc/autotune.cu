@@ -279,6 +279,8 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
     return r;
   };
 
+  // the bar: the plain kernel with one K slice (no workspace, so split-K
+  // off), the full-K accumulation whose error the split forms must match
   Stats plain{};
   if ((rc = run(0, 0, 0)) != GB300_OK) return rc;
   if ((rc = measure(ctest.p, !f32, m, n, Cr, stats, st, &plain)) != GB300_OK) return rc;

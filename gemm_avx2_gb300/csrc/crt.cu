@@ -163,7 +163,7 @@ constexpr int kLimbs = 6;  // 32-bit limbs of M and the weights (M < 2^188)
 struct CrtRecParams {
   int N, m, n, Mp, Np, two_b;
   int topshift;  // bitlength(M) - 40
-  float inv_mt;  // 1 / (M >> topshift)
+  float inv_mt;  // 2^30 / (M >> topshift)
   unsigned w[kCrtMaxModuli][kLimbs];  // CRT weights, little-endian 32-bit limbs
   unsigned M[kLimbs], half[kLimbs];   // M and (M - 1) / 2
   double alpha, beta;
@@ -173,9 +173,9 @@ struct CrtRecParams {
 
 // The CRT reconstruction of one element from its residues r[0..N), then the C
 // update: X = sum r_g w_g in carry-save 64-bit limb accumulators (r < 2^8,
-// limbs < 2^32, at most 24 terms: no overflow), P = X - q M with q = floor(X/M)
-// estimated from X's top bits in FP32 and corrected, the symmetric residue, and
-// one rounding to FP64.
+// limbs < 2^32, at most 24 terms: no overflow), P = X - q M with q ~ X / M
+// estimated from X's top bits in FP32 (floor(X / M) or one more), the symmetric
+// residue from |P|, and one rounding to FP64.
 // r_g is byte e of word[g]; the weights of unused moduli (g >= N) are zero.
 // L = 32-bit limbs of M and the weights (M < 2^(32 L)); X needs L + 1.
 template <int L>
@@ -216,7 +216,13 @@ __device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli],
     }
     xt = o ? (lo >> o) | (hi << (64 - o)) : lo;
   }
-  const unsigned q = (unsigned)((float)xt * rp.inv_mt);
+  // q ~ X / M from the top 23 bits of xt (X >> (topshift + 30) < 2^23, exact in
+  // FP32 by the 2^23 constant), rounded to an integer by the same constant:
+  // the truncation costs < 2^-9 and the FP32 rounding < 2^-11 of a unit, so q
+  // is floor(X / M) or one more; all on the FP32 / integer pipes (conversions
+  // from 64-bit integers would occupy the FP64 pipe)
+  const float xf = __uint_as_float(0x4B000000u | (unsigned)(xt >> 30)) - 8388608.0f;
+  const unsigned q = __float_as_uint(fmaf(xf, rp.inv_mt, 8388608.0f)) & 0x7fffffu;
   // P = X - q M, two's complement over L + 1 limbs
   unsigned P[L + 1];
   {
@@ -229,52 +235,41 @@ __device__ __forceinline__ void crt_value(const unsigned (&word)[kCrtMaxModuli],
       c = (c >> 32) - (long long)(qm >> 32);
     }
   }
-  // add M while negative, subtract M while >= M (q was off by at most one)
-  for (int it = 0; it < 3 && (int)P[L] < 0; ++it) {
-    unsigned long long c = 0;
+  // q is floor(X / M) or one more (the estimate is within 0.0025 of X / M), so
+  // P lies in [-M, M).  The symmetric residue Y of X mod M (in (-M/2, M/2],
+  // where P_mod > (M - 1) / 2 stands for P_mod - M) then follows from a = |P|:
+  // over = a > (M - 1) / 2; |Y| = over ? M - a : a; Y < 0 iff (P < 0) != over.
+  const bool pneg = (int)P[L] < 0;
+  unsigned a[L];
+  {
+    // a = pneg ? -P : P over L limbs (a <= M < 2^(32 L))
+    unsigned long long c = pneg ? 1ull : 0ull;
+    const unsigned flip = pneg ? 0xffffffffu : 0u;
 #pragma unroll
-    for (int l = 0; l < L + 1; ++l) {
-      c += (unsigned long long)P[l] + (l < L ? rp.M[l] : 0u);
-      P[l] = (unsigned)c;
+    for (int l = 0; l < L; ++l) {
+      c += (unsigned long long)(P[l] ^ flip);
+      a[l] = (unsigned)c;
       c >>= 32;
     }
   }
-  for (int it = 0; it < 3; ++it) {
-    bool ge = P[L] != 0;
-    if (!ge) {
-      ge = true;
-#pragma unroll
-      for (int l = L - 1; l >= 0; --l)
-        if (P[l] != rp.M[l]) { ge = P[l] > rp.M[l]; break; }
-    }
-    if (!ge) break;
-    long long c = 0;
-#pragma unroll
-    for (int l = 0; l < L + 1; ++l) {
-      c += (long long)P[l] - (long long)(l < L ? rp.M[l] : 0u);
-      P[l] = (unsigned)c;
-      c >>= 32;
-    }
-  }
-  // symmetric: P > (M - 1) / 2 stands for P - M; magnitude in mg
-  bool gt = false;
+  bool over = false;
 #pragma unroll
   for (int l = L - 1; l >= 0; --l)
-    if (P[l] != rp.half[l]) { gt = P[l] > rp.half[l]; break; }
+    if (a[l] != rp.half[l]) { over = a[l] > rp.half[l]; break; }
   unsigned mg[L];
-  if (gt) {
+  if (over) {
     long long c = 0;
 #pragma unroll
     for (int l = 0; l < L; ++l) {
-      c += (long long)rp.M[l] - (long long)P[l];
+      c += (long long)rp.M[l] - (long long)a[l];
       mg[l] = (unsigned)c;
       c >>= 32;
     }
   } else {
 #pragma unroll
-    for (int l = 0; l < L; ++l) mg[l] = P[l];
+    for (int l = 0; l < L; ++l) mg[l] = a[l];
   }
-  negative = gt;
+  negative = pneg != over;
   // magnitude -> FP64 with one rounding: the top 64 bits, the rest as a sticky bit
   int tl = -1;
 #pragma unroll
@@ -334,32 +329,34 @@ __device__ __forceinline__ double crt_compose(unsigned long long top, int e2, bo
   return __longlong_as_double((long long)bits);
 }
 
-// 4 consecutive rows of one column of C per thread: one 32-bit load per
-// modulus brings their residues (rows are contiguous in each residue plane).
-constexpr int kRecRows = 4;
+// One row and 4 consecutive columns of C per thread: a residue plane holds
+// words of 4 columns (word (col / 4) Mp + row), so one 32-bit load per
+// modulus brings the thread's residues, and a warp's 32 rows load 128
+// contiguous bytes and update 32 contiguous elements of each column of C.
 template <int L>
 __global__ void __launch_bounds__(256)
     crt_reconstruct_kernel(const uint8_t *__restrict__ rres, const int *__restrict__ expA,
                            const int *__restrict__ expB, const __grid_constant__ CrtRecParams rp) {
-  const int64_t plane = (int64_t)rp.Mp * rp.Np;
-  for (int j = blockIdx.y; j < rp.n; j += gridDim.y) {
-    const int i0 = (blockIdx.x * blockDim.x + threadIdx.x) * kRecRows;
-    if (i0 >= rp.m) continue;
-    // i0 + 3 < Mp (a multiple of 128) and Mp * j + i0 is a multiple of 4
-    const unsigned *src = reinterpret_cast<const unsigned *>(rres + (int64_t)j * rp.Mp + i0);
+  const int64_t plane_w = (int64_t)rp.Mp * rp.Np / 4;  // words per residue plane
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rp.m) return;
+  const int ea = expA[i];
+  const int ngroups = (rp.n + 3) / 4;
+  const unsigned *base = reinterpret_cast<const unsigned *>(rres);
+  for (int jg = blockIdx.y; jg < ngroups; jg += gridDim.y) {
+    const unsigned *src = base + (int64_t)jg * rp.Mp + i;
     unsigned word[kCrtMaxModuli];
 #pragma unroll
-    for (int g = 0; g < kCrtMaxModuli; ++g) word[g] = g < rp.N ? src[g * (plane / 4)] : 0u;
-    const int eb = expB[j];
+    for (int g = 0; g < kCrtMaxModuli; ++g) word[g] = g < rp.N ? src[g * plane_w] : 0u;
 #pragma unroll 1
-    for (int e = 0; e < kRecRows; ++e) {
-      const int i = i0 + e;
-      if (i >= rp.m) break;
+    for (int e = 0; e < 4; ++e) {
+      const int j = 4 * jg + e;
+      if (j >= rp.n) break;
       bool neg;
       unsigned long long top;
       int pos;
       crt_value<L>(word, e, rp, neg, top, pos);
-      const int ea = expA[i];
+      const int eb = expB[j];
       double v;
       if (ea == kNonFiniteExp || eb == kNonFiniteExp) {
         v = __longlong_as_double(0x7ff8000000000000LL);
@@ -623,8 +620,9 @@ int crt_run_block(int m, int n, int k, int i0, int h, int j0, int w, double alph
   const size_t need = crt_workspace_bytes(m, n, k, N);
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
   const CrtLayout L = crt_layout(m, n, k, N, const_cast<void *>(ws));
-  // the block's residues: plane g, column j0 + j, row i0 + i at g Mp Np + (j0 + j) Mp + i0 + i
-  uint8_t *rres = L.rres + (int64_t)j0 * L.Mp + i0;
+  // the block's residues: plane g, column j0 + j, row i0 + i in the word
+  // g Mp Np / 4 + ((j0 + j) / 4) Mp + i0 + i (j0 is a multiple of 256)
+  uint8_t *rres = L.rres + ((int64_t)(j0 >> 2) * L.Mp + i0) * 4;
   const int *expA = L.ex + i0, *expB = L.ex + L.Mp + j0;
   // 3. one exact integer GEMM per modulus
   OzakiGemmArgs a;
@@ -662,11 +660,11 @@ int crt_run_block(int m, int n, int k, int i0, int h, int j0, int w, double alph
   {
     Big mt = M;
     for (int s = 0; s < rp.topshift; ++s) big_divmod(mt, 2);
-    rp.inv_mt = 1.0f / (float)mt.l[0];
+    rp.inv_mt = (float)(1073741824.0 / (double)mt.l[0]);
   }
   rp.alpha = alpha; rp.beta = beta; rp.C = Cb; rp.ldc = ldc;
-  const dim3 grid((unsigned)((h + 256 * kRecRows - 1) / (256 * kRecRows)),
-                  (unsigned)(w < 65535 ? w : 65535));
+  const int ngroups = (w + 3) / 4;
+  const dim3 grid((unsigned)((h + 255) / 256), (unsigned)(ngroups < 65535 ? ngroups : 65535));
   // limbs of M: 4 up to 16 moduli, 5 up to 20, 6 up to 24
   const int limbs = (bl + 31) / 32 < 2 ? 2 : (bl + 31) / 32;
   switch (limbs) {

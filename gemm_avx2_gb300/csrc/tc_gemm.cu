@@ -785,9 +785,11 @@ struct OzakiParams {
   int ldc;
   const int *expA, *expB;  // per-row / per-column scale exponents
   double *res;             // Mp x Np FP64 result scratch (ld = Mp)
-  uint8_t *rres;           // mode 1: S blocks of Mp x Np residues in [0, mods[g]) (ld = Mp)
+  uint8_t *rres;           // mode 1: S planes of Mp x Np residues in [0, mods[g]), each in
+                           // words of 4 columns: byte (col / 4) * 4 Mp + 4 row + col % 4
   int mods[kCrtMaxModuli];
   unsigned mods_mg[kCrtMaxModuli];  // floor(2^32 / mods[g]) for the Barrett reduction
+  float mods_f[kCrtMaxModuli], mods_inv[kCrtMaxModuli];  // mods[g] and 1 / mods[g] in FP32
   unsigned *err;
   // work units per tile: the S groups in gsplit ranges (CRT form only, whose
   // moduli are independent GEMMs; 1 in the slice form, which sums its groups)
@@ -837,7 +839,10 @@ constexpr int kCrtRunChunks = 64;
 // past the end (odd tile rows) still takes part in the pipeline (its A loads
 // fetch rows of the next block, or zeros past the last, and its sums are
 // discarded) but writes nothing.
-template <int CL, int BN>
+// MODE: 0 = slice products folded into FP64, 1 = the CRT form's residue GEMMs
+// (p.mode holds the same value; the template keeps the two epilogues' register
+// allocations apart).
+template <int CL, int BN, int MODE>
 __global__ void __launch_bounds__(kOzThreads, 1)
 ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   OzakiParams p) {
@@ -911,7 +916,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         unit_groups(u, g0, g1);
         for (int gi = g0; gi < g1 && ok; ++gi) {
           int t, lo, np;
-          group_of(p.mode, gi, S, t, lo, np);
+          group_of(MODE, gi, S, t, lo, np);
           const int G = np * KB;
           for (int idx = 0; idx < G; ++idx, ++L) {
             const int kb = idx / np, sa = lo + idx % np, sb = t - sa;
@@ -952,7 +957,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         unit_groups(u, g0, g1);
         for (int gi = g0; gi < g1 && ok; ++gi) {
           int t, lo, np;
-          group_of(p.mode, gi, S, t, lo, np);
+          group_of(MODE, gi, S, t, lo, np);
           const int G = np * KB;
           for (int c0 = 0; c0 < G && ok; c0 += kOzChunkStages, ++chunk) {
             const int b = chunk & 1;
@@ -1020,12 +1025,74 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       const int col0 = tn * BN + h * kOzCols;          // first of this warp's columns
       double *res = p.res + (int64_t)col0 * p.Mp + row;      // res[j * Mp] is column col0 + j
       bool res_init = false;
-      const int run_limit = p.mode ? kCrtRunChunks : kOzRunChunks;
+      const int run_limit = MODE ? kCrtRunChunks : kOzRunChunks;
       for (int gi = g0; gi < g1 && ok; ++gi) {
         int t, lo, np;
-        group_of(p.mode, gi, S, t, lo, np);
+        group_of(MODE, gi, S, t, lo, np);
         const int G = np * KB;
         const int nch = (G + kOzChunkStages - 1) / kOzChunkStages;
+        // residue plane of modulus gi: words of 4 consecutive columns,
+        // word (col / 4) * Mp + row (the reconstruction reads one word per
+        // modulus for 4 columns of a row; a warp's 32 rows store 128 bytes)
+        uint32_t *plane = MODE ? reinterpret_cast<uint32_t *>(p.rres + (int64_t)gi * p.Mp * p.Np) +
+                                     (int64_t)(col0 >> 2) * p.Mp + row
+                               : nullptr;
+        if (MODE && nch == 1) {
+          // CRT form, K of this modulus in one chunk (k <= 1024): each chunk
+          // sum x is an integer with |x| <= 1024 * 127^2 < 2^24, exact in FP32.
+          // x mod p in FP32: q = rint(x / p) from x * (1 / p) (rounded to an
+          // integer by the 1.5 * 2^23 constant; |x / p| < 2^17 and the product's
+          // error below 0.01 leave q the nearest integer or its neighbour),
+          // r = x - q p exact by one FMA (|r| < p), then r in [0, p).
+          const int b = chunk & 1;
+          const uint32_t uph = chunk >> 1;
+          ++chunk;
+          if (!mbar_wait(&accf[b], uph & 1, p.err, kErrTimeoutAcc, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+          const float pf = p.mods_f[gi], ip = p.mods_inv[gi];
+          // two halves of the warp's columns: the second half's TMEM loads
+          // release the accumulator, the first half is stored meanwhile
+          constexpr int kHalf = kOzCols / 2;
+#pragma unroll
+          for (int hf = 0; hf < 2; ++hf) {
+            uint32_t v[kHalf];
+#pragma unroll
+            for (int g = 0; g < kHalf / 16; ++g) {
+              uint32_t t16[16];
+              tmem_ld16(lane_base + b * BN + hf * kHalf + g * 16, t16);
+#pragma unroll
+              for (int j = 0; j < 16; ++j) v[g * 16 + j] = t16[j];
+            }
+            tmem_ld_wait();
+            if (hf == 1) {
+              tc_fence_before();
+              __syncwarp();
+              if (lane == 0) {
+                if (PAIR)
+                  mbar_arrive_cluster<false>(&acce[b], 0);  // the even CTA issues the MMAs of both
+                else
+                  mbar_arrive(&acce[b]);
+              }
+            }
+            if (real) {
+#pragma unroll
+              for (int qd = 0; qd < kHalf / 4; ++qd) {
+                uint32_t w = 0;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                  const float x = __uint_as_float(v[4 * qd + e]);
+                  const float qf = fmaf(x, ip, 12582912.0f) - 12582912.0f;
+                  float r = fmaf(-qf, pf, x);
+                  r = r < 0.0f ? r + pf : r;
+                  // r + 2^23 holds r in its low mantissa bits (0 <= r < 256)
+                  w |= (__float_as_uint(r + 8388608.0f) & 0xffu) << (8 * e);
+                }
+                plane[(int64_t)(hf * kHalf / 4 + qd) * p.Mp] = w;
+              }
+            }
+          }
+          continue;
+        }
         const double wt = ldexp(1.0, -7 * t);
         int run[kOzCols];
 #pragma unroll
@@ -1055,7 +1122,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               mbar_arrive(&acce[b]);
           }
           const bool last = (c == nch - 1);
-          if (p.mode && (++since_fold == run_limit || last)) {
+          if (MODE && (++since_fold == run_limit || last)) {
             // CRT form: reduce the exact sums mod p; at the modulus' end store
             // the residue in [0, p) for the reconstruction kernel
             // |run| < 64 chunks x 2^24 = 2^30 < 149 * 2^23, so run + pm * 2^23 is in
@@ -1069,12 +1136,15 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               run[j] = (int)min(r, r - pm);
             }
             if (last && real) {
-              uint8_t *dst = p.rres + (int64_t)gi * p.Mp * p.Np + (int64_t)col0 * p.Mp + row;
 #pragma unroll
-              for (int j = 0; j < kOzCols; ++j) dst[(int64_t)j * p.Mp] = (uint8_t)run[j];
+              for (int qd = 0; qd < kOzCols / 4; ++qd)
+                plane[(int64_t)qd * p.Mp] = (uint32_t)run[4 * qd] |
+                                            ((uint32_t)run[4 * qd + 1] << 8) |
+                                            ((uint32_t)run[4 * qd + 2] << 16) |
+                                            ((uint32_t)run[4 * qd + 3] << 24);
             }
             since_fold = 0;
-          } else if (!p.mode && (++since_fold == kOzRunChunks || last)) {
+          } else if (!MODE && (++since_fold == kOzRunChunks || last)) {
             // fold the exact group sum into the FP64 result: res += run * 2^-7t
 #pragma unroll
             for (int g = 0; g < kOzCols && real; g += 8) {
@@ -1095,7 +1165,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       if (!ok) break;
       // final epilogue: C = alpha * 2^(E_i + F_j) * res + beta * C (slice form;
       // the CRT form's C update is the reconstruction kernel's)
-      if (!p.mode && real && row < p.m) {
+      if (!MODE && real && row < p.m) {
         const int ea = p.expA[row];
 #pragma unroll 1
         for (int g = 0; g < kOzCols; g += 8) {
@@ -1717,10 +1787,14 @@ static int ozaki_launch_bn(const OzakiGemmArgs &a, OzakiParams p, cudaStream_t s
   const int ntu = (pair ? (p.tiles_m + 1) / 2 : p.tiles_m) * p.tiles_n;
   const int mode = modulus_split_override();
   p.gsplit = !p.mode || mode == 1 ? 1 : (mode == 2 || ntu < 4 * stride) ? p.S : 1;
-  return persistent_launch<OzakiParams>(
-      ozaki_gemm_kernel<0, BN>, ozaki_gemm_kernel<2, BN>, kOzThreads,
-      pair ? ClusterTile<2, BN>::kSmem : ClusterTile<0, BN>::kSmem, tA, tB, p, p.tiles_m,
-      p.tiles_n * p.gsplit, pair, st);
+  const int smem = pair ? ClusterTile<2, BN>::kSmem : ClusterTile<0, BN>::kSmem;
+  if (p.mode)
+    return persistent_launch<OzakiParams>(ozaki_gemm_kernel<0, BN, 1>,
+                                          ozaki_gemm_kernel<2, BN, 1>, kOzThreads, smem, tA, tB,
+                                          p, p.tiles_m, p.tiles_n * p.gsplit, pair, st);
+  return persistent_launch<OzakiParams>(ozaki_gemm_kernel<0, BN, 0>, ozaki_gemm_kernel<2, BN, 0>,
+                                        kOzThreads, smem, tA, tB, p, p.tiles_m,
+                                        p.tiles_n * p.gsplit, pair, st);
 }
 
 int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
@@ -1738,6 +1812,8 @@ int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
   for (int i = 0; i < kCrtMaxModuli; ++i) {
     p.mods[i] = (a.mode && i < a.S) ? a.mods[i] : 1;
     p.mods_mg[i] = p.mods[i] > 1 ? (unsigned)((1ull << 32) / (unsigned)p.mods[i]) : 0u;
+    p.mods_f[i] = (float)p.mods[i];
+    p.mods_inv[i] = 1.0f / (float)p.mods[i];
   }
   return split_tile_n(a.mode ? 2 : 1, a.m, a.n, a.k) == 128 ? ozaki_launch_bn<128>(a, p, st)
                                                            : ozaki_launch_bn<256>(a, p, st);

@@ -2,6 +2,8 @@
 device-memory allocator here) and calls through the C ABI."""
 from __future__ import annotations
 
+import contextlib
+
 import numpy as np
 
 
@@ -26,3 +28,19 @@ def from_dev(t, rows: int) -> np.ndarray:
 
 def sync():
     torch_cuda().cuda.synchronize()
+
+
+@contextlib.contextmanager
+def plain_unsplit():
+    """The plain kernels with one K slice (split-K off): the full-K FMA / DMMA
+    chain whose error the split forms' equal-error rule is measured against
+    (the autotuner's bar; the plain kernel also runs unsplit at the benchmark
+    shapes).  Split-K shortens the chains of few-tile shapes and lowers the
+    plain kernel's own error there."""
+    import gemm_avx2_gb300 as g
+
+    assert g.tune_param(g.TUNE_SPLIT_K, 1) == g.OK
+    try:
+        yield
+    finally:
+        g.tune_param(g.TUNE_SPLIT_K, 0)

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import gemm_avx2_gb300 as g
-from gpu_util import from_dev, sync, to_dev
+from gpu_util import from_dev, plain_unsplit, sync, to_dev
 
 pytestmark = pytest.mark.gpu
 
@@ -28,8 +28,9 @@ def test_autotune_ozaki_and_use(orc):
     dC1, dC2 = to_dev(C0), to_dev(C0)
     assert g.dgemm_ozaki("N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 0.0,
                          dC1.data_ptr(), m, slices=0) == g.OK
-    assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 0.0,
-                         dC2.data_ptr(), m) == g.OK
+    with plain_unsplit():
+        assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n,
+                             0.0, dC2.data_ptr(), m) == g.OK
     sync()
     e_tuned, e_plain = rel(from_dev(dC1, m), truth), rel(from_dev(dC2, m), truth)
     # tuned against the S = 12 reference, checked here against Dot2: same order as plain
@@ -51,8 +52,9 @@ def test_autotune_crt_and_use(orc):
     dC1, dC2 = to_dev(C0), to_dev(C0)
     assert g.dgemm_ozaki2("N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 0.0,
                           dC1.data_ptr(), m, moduli=0) == g.OK
-    assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 0.0,
-                         dC2.data_ptr(), m) == g.OK
+    with plain_unsplit():
+        assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n,
+                             0.0, dC2.data_ptr(), m) == g.OK
     sync()
     e_tuned, e_plain = rel(from_dev(dC1, m), truth), rel(from_dev(dC2, m), truth)
     assert e_tuned[0] <= 4 * e_plain[0] and e_tuned[1] <= 4 * e_plain[1], (N, e_tuned, e_plain)

@@ -6,7 +6,7 @@ import pytest
 
 import gemm_avx2_gb300 as g
 import oracle
-from gpu_util import from_dev, sync, to_dev, torch_cuda
+from gpu_util import from_dev, plain_unsplit, sync, to_dev, torch_cuda
 from oracle import crt
 from util import op
 
@@ -104,6 +104,23 @@ def test_odd_row_tiles_bitexact(orc, m, tile_n, cluster_mode):
     assert g.device_error() == 0
 
 
+@pytest.mark.parametrize("k", [1100, 2100])
+def test_multi_chunk_bitexact(orc, k, cluster_mode):
+    """K beyond one 1024-step TMEM chunk (2 and 3 chunks per modulus): the
+    epilogue's integer path that reduces the chunk sums mod p and packs the
+    residues of 4 columns per word; 2 row tiles, both cluster modes."""
+    m, n = 140, 36
+    A = orc.spread((m, k), 59, 0, 1.0)
+    B = orc.spread((k, n), 59, 1, 1.0)
+    C = orc.uniform((m + 1, n), np.float64, 59, 2)
+    rc, got, _ = run_crt("N", "N", m, n, k, A, m, B, k, C, 15, alpha=-1.0, beta=1.0)
+    assert rc == g.OK
+    assert np.array_equal(got[m:], C[m:])
+    model = crt.crt_gemm_model(A, B, 15, alpha=-1.0, beta=1.0, C=C[:m])
+    assert np.array_equal(got[:m], model)
+    assert g.device_error() == 0
+
+
 def test_nonfinite_rows_and_columns(orc):
     m, n, k = 40, 30, 50
     A = orc.uniform((m, k), np.float64, 53, 0)
@@ -131,8 +148,9 @@ def test_accuracy_vs_plain(orc):
     assert rc == g.OK
     dC = to_dev(C)
     dA, dB = to_dev(A), to_dev(B)
-    assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 1.0,
-                         dC.data_ptr(), m) == g.OK
+    with plain_unsplit():
+        assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n,
+                             1.0, dC.data_ptr(), m) == g.OK
     sync()
     plain = from_dev(dC, m)
     truth = orc.dot2gemm("N", "T", m, n, k, 1.0, A, m, B, n, 1.0, C, m)

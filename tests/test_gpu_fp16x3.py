@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import gemm_avx2_gb300 as g
-from gpu_util import from_dev, sync, to_dev, torch_cuda
+from gpu_util import from_dev, plain_unsplit, sync, to_dev, torch_cuda
 from oracle import split as osp
 from util import op
 
@@ -151,8 +151,9 @@ def test_accuracy_vs_plain_and_6xbf16(orc):
     rc, got, _ = run("T", "N", m, n, k, 1.0, A, k, B, k, 0.0, C)
     assert rc == g.OK
     dA, dB, dP = to_dev(A), to_dev(B), to_dev(C)
-    assert g.gemm_device("s", "T", "N", m, n, k, 1.0, dA.data_ptr(), k, dB.data_ptr(), k, 0.0,
-                         dP.data_ptr(), m) == g.OK
+    with plain_unsplit():
+        assert g.gemm_device("s", "T", "N", m, n, k, 1.0, dA.data_ptr(), k, dB.data_ptr(), k,
+                             0.0, dP.data_ptr(), m) == g.OK
     sync()
     truth = orc.dot2gemm("T", "N", m, n, k, 1.0, A, k, B, k, 0.0, C, m)
     mx, fro = rel_errs(got, truth)

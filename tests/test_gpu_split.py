@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import gemm_avx2_gb300 as g
-from gpu_util import from_dev, sync, to_dev, torch_cuda
+from gpu_util import from_dev, plain_unsplit, sync, to_dev, torch_cuda
 from oracle import split as osp
 from util import op
 
@@ -207,8 +207,9 @@ def test_ozaki_vs_plain_accuracy(orc):
     dC1, dC2 = to_dev(C), to_dev(C)
     assert g.dgemm_ozaki("N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 1.0,
                          dC1.data_ptr(), m, slices=8) == g.OK
-    assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n, 1.0,
-                         dC2.data_ptr(), m) == g.OK
+    with plain_unsplit():
+        assert g.gemm_device("d", "N", "T", m, n, k, 1.0, dA.data_ptr(), m, dB.data_ptr(), n,
+                             1.0, dC2.data_ptr(), m) == g.OK
     sync()
     truth = orc.dot2gemm("N", "T", m, n, k, 1.0, A, m, B, n, 1.0, C, m)
     e_oz = rel_errs(from_dev(dC1, m), truth)
