@@ -826,8 +826,9 @@ def run_grouped(args, torch, rank, world):
     """1024 independent GEMMs: m, n, k = round(exp(U[ln 16, ln 2048])), transa/transb
     N or T with p = 0.5, 60% FP64 / 40% FP32, alpha ~ U[0.5, 2], beta in {0, 1},
     entries U[-1,1), ld = rows of the stored matrix (seed 4).  A step replays a
-    captured CUDA graph: the split forms (one call per problem) for the headline,
-    the plain forms (one persistent launch) for the comparison."""
+    captured CUDA graph: the split forms (per-problem operand preparation, one
+    grouped GEMM launch per precision, per-problem FP64 reconstruction) for the
+    headline, the plain forms (one persistent launch) for the comparison."""
     import numpy as np
 
     import gemm_avx2_gb300 as g
@@ -886,6 +887,7 @@ def run_grouped(args, torch, rank, world):
 
     gp = g.GroupedGraph(probs, form=0)
     gs = g.GroupedGraph(probs, form=1)
+    kernels_split, gemm_launches_split = gs.stats()
     # accuracy of both forms on sampled entries of 48 problems (exact sampled dots)
     def sampled_errors(graph):
         reset()
@@ -930,7 +932,9 @@ def run_grouped(args, torch, rank, world):
         "data": "synthetic (seeded uniform[-1,1), generated on the device)",
         "config": {"workload": "grouped_1024", "problems": count, "fp64_share_of_flops":
                    round(fl_d / flops, 4), "total_gflop": round(flops / 1e9, 3),
-                   "form": "split (FP32: bf16x6, FP64: CRT with 16 moduli), CUDA graph",
+                   "form": "split (FP32: bf16x6, FP64: CRT with 16 moduli), CUDA graph: "
+                           "operand preparation in branches, one grouped GEMM launch per "
+                           "precision, FP64 reconstruction in branches",
                    "l2": "%d MB of operands > %d MB" % (
                        sum(sum(t.numel() * t.element_size() for t in b[:3]) for b in bufs) // 2**20,
                        L2_BYTES // 2**20)},
@@ -944,7 +948,8 @@ def run_grouped(args, torch, rank, world):
                      "peak_source": "FP64 1.05 and FP32 73 TFLOP/s measured by microbenchmark"},
         "accuracy": {"plain": err_plain, "split": err_split, "samples": "8 entries x 48 problems"},
         "clocks": clocks,
-        "gpu_launches": args.steps * sum(4 if p["precision"] == "d" else 2 for p in probs),
+        "gpu_launches": args.steps * kernels_split,
+        "gemm_launches_per_step": gemm_launches_split,
         "e2e": {"value": None, "skipped": "device-pointer grouped API"},
     }
     gp.destroy()

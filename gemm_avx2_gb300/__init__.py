@@ -495,6 +495,14 @@ class GroupedGraph:
     def launch(self, stream=0) -> int:
         return core().gb300_grouped_graph_launch(self.handle, c_void_p(stream))
 
+    def stats(self):
+        """(kernel nodes of the graph, of which GEMM launches)."""
+        kn, gl = ctypes.c_int(0), ctypes.c_int(0)
+        rc = core().gb300_grouped_graph_stats(self.handle, ctypes.byref(kn), ctypes.byref(gl))
+        if rc != OK:
+            raise RuntimeError("gb300_grouped_graph_stats failed: status %d" % rc)
+        return kn.value, gl.value
+
     def destroy(self) -> None:
         if self.handle:
             core().gb300_grouped_graph_destroy(self.handle)
@@ -530,6 +538,7 @@ CORE_SYMBOLS = [
     "gb300_tune_cache_load",
     "gb300_tune_cache_clear", "gb300_dtrsm", "gb300_strsm", "gb300_dtrmm", "gb300_strmm",
     "gb300_grouped_graph_create", "gb300_grouped_graph_launch", "gb300_grouped_graph_destroy",
+    "gb300_grouped_graph_stats",
     "gb300_cgemm", "gb300_zgemm", "gb300_host_cgemm", "gb300_host_zgemm",
     "gb300_complex_workspace_bytes", "gb300_dgemm_ozaki2", "gb300_host_dgemm_ozaki2",
     "gb300_dgemm_ozaki2_prepare", "gb300_dgemm_ozaki2_run",

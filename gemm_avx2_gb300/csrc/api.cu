@@ -967,21 +967,26 @@ GB300_API int gb300_gemm_grouped(const gb300_gemm_problem *problems, int count, 
   return grouped_plain(problems, count, ws, need, st, s->err);
 }
 
-// Split-form batches are captured as parallel branches (forked from and
-// joined into the capture stream), problems assigned longest-work-first to the
-// least-loaded branch; each branch has its own workspace.  Small problems fill
-// a few SMs each, so the branch count sets how much of the GPU a batch uses
-// (GB300_TUNE_GRAPH_BRANCHES, read when a graph is created).
+// Split-form batches (form 1) are captured in three phases: the problems'
+// operand preparation in parallel branches (forked from and joined into the
+// capture stream, problems assigned longest-work-first to the least-loaded
+// branch), one grouped persistent launch of the CRT residue GEMMs of all FP64
+// problems and one of the 6xBF16 GEMMs of all FP32 problems, then the FP64
+// problems' reconstructions in branches.  Every problem has its own
+// workspace (one allocation).  Problems with alpha = 0 or k = 0 run their
+// per-problem call in a branch.  GB300_TUNE_GRAPH_BRANCHES (read when a graph
+// is created) sets the branch count.
 constexpr int kGraphBranches = 64;  // upper bound
-constexpr int kDefaultGraphBranches = 32;  // 10.3 TFLOP/s at 16, 11.9 at 32, 12.0 at 64 (1024 problems)
+constexpr int kDefaultGraphBranches = 32;
 static int g_graph_branches = kDefaultGraphBranches;
 
 struct gb300_grouped_graph_s {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  void *meta = nullptr;                   // grouped metadata blob (form 0)
-  void *ws[kGraphBranches] = {nullptr};   // split-form workspaces (form 1), one per branch
+  void *meta = nullptr;  // form 0: grouped metadata blob; form 1: the grouped GEMM tables
+  void *ws = nullptr;    // form 1: the problems' workspaces
   int device = 0;
+  int kernel_nodes = 0, gemm_launches = 0;
 };
 
 GB300_API int gb300_grouped_graph_destroy(gb300_grouped_graph g) {
@@ -989,11 +994,30 @@ GB300_API int gb300_grouped_graph_destroy(gb300_grouped_graph g) {
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   if (g->meta) cudaFree(g->meta);
-  for (int b = 0; b < kGraphBranches; ++b)
-    if (g->ws[b]) cudaFree(g->ws[b]);
+  if (g->ws) cudaFree(g->ws);
   delete g;
   return GB300_OK;
 }
+
+GB300_API int gb300_grouped_graph_stats(gb300_grouped_graph g, int *kernel_nodes,
+                                        int *gemm_launches) {
+  if (!g || !g->exec) return GB300_ERR_ARG;
+  if (kernel_nodes) *kernel_nodes = g->kernel_nodes;
+  if (gemm_launches) *gemm_launches = g->gemm_launches;
+  return GB300_OK;
+}
+
+namespace {
+// One problem of a split-form graph: its class, workspace and branch.
+struct GraphItem {
+  int cls = 0;        // 0: nothing to do, 1: per-problem call, 2: FP64 CRT, 3: FP32 6xBF16
+  size_t ws_off = 0, ws_bytes = 0;
+  int branch = 0;
+  double work = 0;    // LPT weight
+  int cost = 0;       // tensor work per tile unit (order inside the grouped launch)
+};
+constexpr int kGroupProducts = 6;
+}  // namespace
 
 GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int count, int form,
                                          gb300_grouped_graph *out) {
@@ -1015,11 +1039,15 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
   int rc = GB300_OK;
   std::vector<uint8_t> blob;
   int used = 0, tiles = 0;
-  std::vector<int> branch_of(count > 0 ? count : 1, 0);
   const int nbr = g_graph_branches;
-  size_t wneed_b[kGraphBranches] = {0};
   cudaStream_t bs[kGraphBranches] = {nullptr};
   cudaEvent_t fork = nullptr, join[kGraphBranches] = {nullptr};
+  std::vector<GraphItem> items(count > 0 ? count : 1);
+  // form 1: the grouped GEMM tables (FP64 entries, then FP32), in device order
+  std::vector<int> ord_d, ord_s;
+  std::vector<uint8_t> table;
+  int units_d = 0, units_s = 0;
+  const size_t eb_d = ozaki_group_entry_bytes(), eb_s = bf16x_group_entry_bytes();
   if (form == 0) {
     rc = grouped_build(problems, count, nullptr, blob, used, tiles);
     if (rc == GB300_OK && used > 0) {
@@ -1028,74 +1056,162 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
         rc = GB300_ERR_CUDA;
     }
   } else {
-    // longest work first onto the least-loaded branch (FP64 problems run the
-    // CRT form's 16 residue GEMMs, FP32 ones 6 products)
-    std::vector<int> order(count);
-    for (int i = 0; i < count; ++i) order[i] = i;
-    auto work = [&](int i) {
+    size_t total_ws = 0;
+    for (int i = 0; i < count; ++i) {
       const gb300_gemm_problem &q = problems[i];
-      return (double)q.m * q.n * q.k * (q.precision == 'd' ? 16.0 : 6.0) + 1e6;
-    };
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work(a) > work(b); });
+      GraphItem &it = items[i];
+      if (check_args(q.transa, q.transb, q.m, q.n, q.k, q.lda, q.ldb, q.ldc) < 0) continue;
+      const int64_t kb = (q.k + 63) / 64;
+      if (q.alpha == 0.0 || q.k == 0) {
+        it.cls = 1;
+        it.work = (double)q.m * q.n + 1e6;
+      } else if (q.precision == 'd') {
+        it.cls = 2;
+        const int N = crt_default_moduli(q.m, q.n, q.k);
+        it.ws_bytes = crt_workspace_bytes(q.m, q.n, q.k, N);
+        it.cost = (int)(N * kb);
+        it.work = (double)(q.m + q.n) * q.k * N + 1e6;
+      } else {
+        it.cls = 3;
+        it.ws_bytes = split_workspace_bytes(0, q.m, q.n, q.k, kGroupProducts);
+        it.cost = (int)(6 * kb);
+        it.work = (double)(q.m + q.n) * q.k * 3 + 1e6;
+      }
+      if (it.ws_bytes) {
+        it.ws_off = total_ws;
+        total_ws += (it.ws_bytes + 1023) / 1024 * 1024;
+      }
+      if (it.cls == 2) ord_d.push_back(i);
+      if (it.cls == 3) ord_s.push_back(i);
+    }
+    // longest work first onto the least-loaded branch
+    std::vector<int> order;
+    for (int i = 0; i < count; ++i)
+      if (items[i].cls) order.push_back(i);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return items[a].work > items[b].work; });
     double load[kGraphBranches] = {0};
     for (int i : order) {
       int b = 0;
       for (int j = 1; j < nbr; ++j)
         if (load[j] < load[b]) b = j;
-      load[b] += work(i);
-      branch_of[i] = b;
-      const gb300_gemm_problem &q = problems[i];
-      const size_t w = q.precision == 'd' ? crt_workspace_bytes(q.m, q.n, q.k, 0)
-                                          : split_workspace_bytes(0, q.m, q.n, q.k, 6);
-      if (w > wneed_b[b]) wneed_b[b] = w;
+      load[b] += items[i].work;
+      items[i].branch = b;
     }
-    for (int b = 0; b < kGraphBranches && rc == GB300_OK; ++b)
-      if (wneed_b[b] && cudaMalloc(&g->ws[b], wneed_b[b]) != cudaSuccess) rc = GB300_ERR_NOMEM;
+    // inside a grouped launch the CTAs take units round-robin: the problems
+    // with the costliest tiles go first
+    auto by_cost = [&](int a, int b) { return items[a].cost > items[b].cost; };
+    std::stable_sort(ord_d.begin(), ord_d.end(), by_cost);
+    std::stable_sort(ord_s.begin(), ord_s.end(), by_cost);
+    if (total_ws && cudaMalloc(&g->ws, total_ws) != cudaSuccess) rc = GB300_ERR_NOMEM;
+    table.resize(ord_d.size() * eb_d + ord_s.size() * eb_s);
+    for (size_t j = 0; j < ord_d.size() && rc == GB300_OK; ++j) {
+      const gb300_gemm_problem &q = problems[ord_d[j]];
+      const GraphItem &it = items[ord_d[j]];
+      int u = 0;
+      rc = crt_group_entry(q.m, q.n, q.k, q.alpha, q.beta, static_cast<double *>(q.C), q.ldc, 0,
+                           static_cast<uint8_t *>(g->ws) + it.ws_off, it.ws_bytes, s->err,
+                           units_d, table.data() + j * eb_d, &u);
+      units_d += u;
+    }
+    for (size_t j = 0; j < ord_s.size() && rc == GB300_OK; ++j) {
+      const gb300_gemm_problem &q = problems[ord_s[j]];
+      const GraphItem &it = items[ord_s[j]];
+      int u = 0;
+      rc = bf16x_group_entry(q.m, q.n, q.k, (float)q.alpha, (float)q.beta,
+                             static_cast<float *>(q.C), q.ldc, kGroupProducts,
+                             static_cast<uint8_t *>(g->ws) + it.ws_off, it.ws_bytes, s->err,
+                             units_s, table.data() + ord_d.size() * eb_d + j * eb_s, &u);
+      units_s += u;
+    }
+    if (rc == GB300_OK && !table.empty()) {
+      if (cudaMalloc(&g->meta, table.size()) != cudaSuccess) rc = GB300_ERR_NOMEM;
+      else if (cudaMemcpy(g->meta, table.data(), table.size(), cudaMemcpyHostToDevice) !=
+               cudaSuccess)
+        rc = GB300_ERR_CUDA;
+    }
   }
   if (rc == GB300_OK && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
     rc = GB300_ERR_CUDA;
+  if (rc == GB300_OK && form == 1) {
+    bool ok = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int b = 0; b < nbr && ok; ++b)
+      ok = cudaStreamCreateWithFlags(&bs[b], cudaStreamNonBlocking) == cudaSuccess &&
+           cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) rc = GB300_ERR_CUDA;
+  }
   if (rc == GB300_OK && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     rc = GB300_ERR_CUDA;
   if (rc == GB300_OK) {
     int rc2 = GB300_OK;
+    // fork the branches off the capture stream / join them back into it
+    auto fork_all = [&]() {
+      if (cudaEventRecord(fork, cs) != cudaSuccess) return false;
+      for (int b = 0; b < nbr; ++b)
+        if (cudaStreamWaitEvent(bs[b], fork, 0) != cudaSuccess) return false;
+      return true;
+    };
+    auto join_all = [&]() {
+      bool ok = true;
+      for (int b = 0; b < nbr; ++b)
+        ok = cudaEventRecord(join[b], bs[b]) == cudaSuccess &&
+             cudaStreamWaitEvent(cs, join[b], 0) == cudaSuccess && ok;
+      return ok;
+    };
     if (form == 0) {
       if (used > 0) {
         if (cudaMemsetAsync(g->meta, 0, sizeof(int), cs) != cudaSuccess) rc2 = GB300_ERR_CUDA;
         else rc2 = grouped_launch_blob(g->meta, used, tiles, cs, s->err);
       }
     } else {
-      // fork nbr branches off the capture stream; each branch runs its
-      // problems' split-form calls in order on its own workspace; join.
-      bool forked = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess &&
-                    cudaEventRecord(fork, cs) == cudaSuccess;
-      for (int b = 0; b < nbr && forked; ++b)
-        forked = cudaStreamCreateWithFlags(&bs[b], cudaStreamNonBlocking) == cudaSuccess &&
-                 cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming) == cudaSuccess &&
-                 cudaStreamWaitEvent(bs[b], fork, 0) == cudaSuccess;
-      if (!forked) rc2 = GB300_ERR_CUDA;
-      // the branches run their problems side by side: whole-tile CRT units
-      set_modulus_split_hint(1);
+      // 1. preparation (and the per-problem calls)
+      if (!fork_all()) rc2 = GB300_ERR_CUDA;
       for (int i = 0; i < count && rc2 == GB300_OK; ++i) {
         const gb300_gemm_problem &q = problems[i];
-        const int b = branch_of[i];
-        if (q.precision == 'd')
-          rc2 = crt_dgemm(q.transa, q.transb, q.m, q.n, q.k, q.alpha,
-                          static_cast<const double *>(q.A), q.lda,
-                          static_cast<const double *>(q.B), q.ldb, q.beta,
-                          static_cast<double *>(q.C), q.ldc, 0, g->ws[b], wneed_b[b], bs[b],
-                          s->err);
-        else
-          rc2 = split_sgemm(q.transa, q.transb, q.m, q.n, q.k, (float)q.alpha,
-                            static_cast<const float *>(q.A), q.lda,
-                            static_cast<const float *>(q.B), q.ldb, (float)q.beta,
-                            static_cast<float *>(q.C), q.ldc, 6, g->ws[b], wneed_b[b], bs[b],
-                            s->err);
+        const GraphItem &it = items[i];
+        cudaStream_t st = bs[it.branch];
+        void *ws = static_cast<uint8_t *>(g->ws) + it.ws_off;
+        if (it.cls == 1) {  // C = beta C, as the split calls do it
+          const int ld1 = q.m > 1 ? q.m : 1;
+          rc2 = q.precision == 'd'
+                    ? plain_dgemm('N', 'N', q.m, q.n, 0, q.alpha, nullptr, ld1, nullptr, 1, q.beta,
+                                  static_cast<double *>(q.C), q.ldc, st, s->err)
+                    : plain_sgemm('N', 'N', q.m, q.n, 0, (float)q.alpha, nullptr, ld1, nullptr, 1,
+                                  (float)q.beta, static_cast<float *>(q.C), q.ldc, st, s->err);
+        } else if (it.cls == 2) {
+          rc2 = crt_prepare(q.transa, q.transb, q.m, q.n, q.k, static_cast<const double *>(q.A),
+                            q.lda, static_cast<const double *>(q.B), q.ldb, 0, ws, it.ws_bytes,
+                            st);
+        } else if (it.cls == 3) {
+          rc2 = split_sgemm_prepare(q.transa, q.transb, q.m, q.n, q.k,
+                                    static_cast<const float *>(q.A), q.lda,
+                                    static_cast<const float *>(q.B), q.ldb, kGroupProducts, ws,
+                                    it.ws_bytes, st);
+        }
       }
-      set_modulus_split_hint(0);
-      for (int b = 0; b < nbr && forked; ++b)
-        if (cudaEventRecord(join[b], bs[b]) != cudaSuccess ||
-            cudaStreamWaitEvent(cs, join[b], 0) != cudaSuccess)
-          rc2 = GB300_ERR_CUDA;
+      if (rc2 == GB300_OK && !join_all()) rc2 = GB300_ERR_CUDA;
+      // 2. the grouped GEMMs
+      if (rc2 == GB300_OK && !ord_d.empty()) {
+        rc2 = ozaki_group_launch(g->meta, (int)ord_d.size(), units_d, cs, s->err);
+        ++g->gemm_launches;
+      }
+      if (rc2 == GB300_OK && !ord_s.empty()) {
+        rc2 = bf16x_group_launch(static_cast<uint8_t *>(g->meta) + ord_d.size() * eb_d,
+                                 (int)ord_s.size(), units_s, cs, s->err);
+        ++g->gemm_launches;
+      }
+      // 3. the FP64 problems' reconstruction
+      if (rc2 == GB300_OK && !ord_d.empty()) {
+        if (!fork_all()) rc2 = GB300_ERR_CUDA;
+        for (size_t j = 0; j < ord_d.size() && rc2 == GB300_OK; ++j) {
+          const gb300_gemm_problem &q = problems[ord_d[j]];
+          const GraphItem &it = items[ord_d[j]];
+          rc2 = crt_group_reconstruct(q.m, q.n, q.k, q.alpha, q.beta, static_cast<double *>(q.C),
+                                      q.ldc, 0, static_cast<uint8_t *>(g->ws) + it.ws_off,
+                                      it.ws_bytes, bs[it.branch]);
+        }
+        if (rc2 == GB300_OK && !join_all()) rc2 = GB300_ERR_CUDA;
+      }
     }
     cudaGraph_t graph = nullptr;
     const cudaError_t e = cudaStreamEndCapture(cs, &graph);
@@ -1103,6 +1219,19 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
     if (rc2 != GB300_OK) rc = rc2;
     else if (e != cudaSuccess || !graph) rc = GB300_ERR_CUDA;
     else if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) rc = GB300_ERR_CUDA;
+    if (rc == GB300_OK) {
+      size_t nn = 0;
+      if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn) {
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (cudaGraphGetNodes(graph, nodes.data(), &nn) == cudaSuccess)
+          for (size_t j = 0; j < nn; ++j) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[j], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+              ++g->kernel_nodes;
+          }
+      }
+      if (form == 0 && used > 0) g->gemm_launches = 1;
+    }
   }
   if (cs) cudaStreamDestroy(cs);
   for (int b = 0; b < kGraphBranches; ++b) {

@@ -364,8 +364,9 @@ __global__ void __launch_bounds__(256)
         v = crt_compose(top, pos + ea + eb - rp.two_b, neg);
       }
       double *c = rp.C + (int64_t)j * rp.ldc + i;
-      const double cb = (rp.beta == 1.0) ? *c : *c * rp.beta;
-      *c = cb + rp.alpha * v;
+      // beta C + alpha v rounded as written, as the model in the oracle
+      const double cb = (rp.beta == 1.0) ? *c : __dmul_rn(*c, rp.beta);
+      *c = __dadd_rn(cb, __dmul_rn(rp.alpha, v));
     }
   }
 }
@@ -602,42 +603,38 @@ int crt_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, 
   return crt_run_block(m, n, k, 0, m, 0, n, alpha, beta, C, ldc, moduli, ws, ws_bytes, st, err);
 }
 
-int crt_run_block(int m, int n, int k, int i0, int h, int j0, int w, double alpha, double beta,
-                  double *C, int ldc, int moduli, const void *ws, size_t ws_bytes,
-                  cudaStream_t st, unsigned *err) {
-  const int N = resolve_moduli(moduli, m, n, k);
-  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || N < 2 || N > kCrtMaxModuli ||
-      i0 < 0 || j0 < 0 || h < 0 || w < 0 || i0 % kSplitBM || j0 % kOzakiBN || i0 + h > m ||
-      j0 + w > n)
-    return GB300_ERR_ARG;
-  if (h == 0 || w == 0) return GB300_OK;
-  double *Cb = C + i0 + (int64_t)j0 * ldc;
-  if (alpha == 0.0 || k == 0)
-    return plain_dgemm('N', 'N', h, w, 0, alpha, nullptr, h > 1 ? h : 1, nullptr, 1, beta, Cb,
-                       ldc, st, err);
-  const int b = crt_bits_for(N, k);
+namespace {
+
+// The residue GEMM's arguments for the C block (i0, h) x (j0, w) of a
+// prepared problem (N moduli, b-bit scaled integers).
+int crt_block_args(int m, int n, int k, int i0, int h, int j0, int w, double alpha, double beta,
+                   double *C, int ldc, int N, const void *ws, size_t ws_bytes, OzakiGemmArgs &a,
+                   int &b) {
+  b = crt_bits_for(N, k);
   if (b < 1) return GB300_ERR_ARG;
   const size_t need = crt_workspace_bytes(m, n, k, N);
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
   const CrtLayout L = crt_layout(m, n, k, N, const_cast<void *>(ws));
   // the block's residues: plane g, column j0 + j, row i0 + i in the word
   // g Mp Np / 4 + ((j0 + j) / 4) Mp + i0 + i (j0 is a multiple of 256)
-  uint8_t *rres = L.rres + ((int64_t)(j0 >> 2) * L.Mp + i0) * 4;
-  const int *expA = L.ex + i0, *expB = L.ex + L.Mp + j0;
-  // 3. one exact integer GEMM per modulus
-  OzakiGemmArgs a;
   a.m = h; a.n = w; a.k = k; a.S = N; a.mode = 1;
   a.Mp = L.Mp; a.Np = L.Np; a.Kp = L.Kp;
   a.As = L.As; a.Bs = L.Bs;
   a.row0 = i0; a.col0 = j0;
-  a.alpha = alpha; a.beta = beta; a.C = Cb; a.ldc = ldc;
-  a.expA = expA; a.expB = expB; a.res = nullptr; a.rres = rres; a.mods = kModuli;
-  const int rc = ozaki_gemm_launch(a, st, err);
-  if (rc != GB300_OK) return rc;
-  // 4. reconstruction and the C update
+  a.alpha = alpha; a.beta = beta; a.C = C + i0 + (int64_t)j0 * ldc; a.ldc = ldc;
+  a.expA = L.ex + i0; a.expB = L.ex + L.Mp + j0;
+  a.res = nullptr;
+  a.rres = L.rres + ((int64_t)(j0 >> 2) * L.Mp + i0) * 4;
+  a.mods = kModuli;
+  return GB300_OK;
+}
+
+// Reconstruction of the block of a (after its residue GEMM) and the C update.
+int crt_reconstruct_launch(const OzakiGemmArgs &a, int b, cudaStream_t st) {
+  const int N = a.S, h = a.m, w = a.n;
   CrtRecParams rp;
   std::memset(&rp, 0, sizeof(rp));
-  rp.N = N; rp.m = h; rp.n = w; rp.Mp = (int)L.Mp; rp.Np = (int)L.Np; rp.two_b = 2 * b;
+  rp.N = N; rp.m = h; rp.n = w; rp.Mp = (int)a.Mp; rp.Np = (int)a.Np; rp.two_b = 2 * b;
   const Big M = modulus_product(N);
   auto limbs32 = [](const Big &x, unsigned *out) {
     for (int l = 0; l < kLimbs; ++l) out[l] = (unsigned)(x.l[l / 2] >> (32 * (l % 2)));
@@ -648,8 +645,8 @@ int crt_run_block(int m, int n, int k, int i0, int h, int j0, int w, double alph
     big_divmod(Mi, pg);
     Big t = Mi;
     const uint64_t mi_mod = big_divmod(t, pg);
-    const Big w = big_mul(Mi, (uint64_t)inv_mod((int64_t)mi_mod, (int64_t)pg));  // < M
-    limbs32(w, rp.w[g]);
+    const Big wg = big_mul(Mi, (uint64_t)inv_mod((int64_t)mi_mod, (int64_t)pg));  // < M
+    limbs32(wg, rp.w[g]);
   }
   Big half = big_sub(M, big_from(1));
   big_divmod(half, 2);
@@ -662,7 +659,9 @@ int crt_run_block(int m, int n, int k, int i0, int h, int j0, int w, double alph
     for (int s = 0; s < rp.topshift; ++s) big_divmod(mt, 2);
     rp.inv_mt = (float)(1073741824.0 / (double)mt.l[0]);
   }
-  rp.alpha = alpha; rp.beta = beta; rp.C = Cb; rp.ldc = ldc;
+  rp.alpha = a.alpha; rp.beta = a.beta; rp.C = a.C; rp.ldc = a.ldc;
+  const uint8_t *rres = a.rres;
+  const int *expA = a.expA, *expB = a.expB;
   const int ngroups = (w + 3) / 4;
   const dim3 grid((unsigned)((h + 255) / 256), (unsigned)(ngroups < 65535 ? ngroups : 65535));
   // limbs of M: 4 up to 16 moduli, 5 up to 20, 6 up to 24
@@ -675,6 +674,58 @@ int crt_run_block(int m, int n, int k, int i0, int h, int j0, int w, double alph
     default: crt_reconstruct_kernel<6><<<grid, 256, 0, st>>>(rres, expA, expB, rp); break;
   }
   return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+}  // namespace
+
+int crt_run_block(int m, int n, int k, int i0, int h, int j0, int w, double alpha, double beta,
+                  double *C, int ldc, int moduli, const void *ws, size_t ws_bytes,
+                  cudaStream_t st, unsigned *err) {
+  const int N = resolve_moduli(moduli, m, n, k);
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || N < 2 || N > kCrtMaxModuli ||
+      i0 < 0 || j0 < 0 || h < 0 || w < 0 || i0 % kSplitBM || j0 % kOzakiBN || i0 + h > m ||
+      j0 + w > n)
+    return GB300_ERR_ARG;
+  if (h == 0 || w == 0) return GB300_OK;
+  if (alpha == 0.0 || k == 0)
+    return plain_dgemm('N', 'N', h, w, 0, alpha, nullptr, h > 1 ? h : 1, nullptr, 1, beta,
+                       C + i0 + (int64_t)j0 * ldc, ldc, st, err);
+  OzakiGemmArgs a;
+  int b = 0;
+  int rc = crt_block_args(m, n, k, i0, h, j0, w, alpha, beta, C, ldc, N, ws, ws_bytes, a, b);
+  if (rc != GB300_OK) return rc;
+  // 3. one exact integer GEMM per modulus
+  rc = ozaki_gemm_launch(a, st, err);
+  if (rc != GB300_OK) return rc;
+  // 4. reconstruction and the C update
+  return crt_reconstruct_launch(a, b, st);
+}
+
+// Grouped launches: the table entry of a prepared problem's residue GEMM, and
+// its reconstruction once the grouped GEMM has run (alpha != 0, k > 0).
+int crt_group_entry(int m, int n, int k, double alpha, double beta, double *C, int ldc,
+                    int moduli, const void *ws, size_t ws_bytes, unsigned *err, int unit0,
+                    void *entry, int *units) {
+  const int N = resolve_moduli(moduli, m, n, k);
+  if (m <= 0 || n <= 0 || k <= 0 || alpha == 0.0 || ldc < m || N < 2 || N > kCrtMaxModuli)
+    return GB300_ERR_ARG;
+  OzakiGemmArgs a;
+  int b = 0;
+  const int rc = crt_block_args(m, n, k, 0, m, 0, n, alpha, beta, C, ldc, N, ws, ws_bytes, a, b);
+  if (rc != GB300_OK) return rc;
+  return ozaki_group_entry(a, err, unit0, entry, units);
+}
+
+int crt_group_reconstruct(int m, int n, int k, double alpha, double beta, double *C, int ldc,
+                          int moduli, const void *ws, size_t ws_bytes, cudaStream_t st) {
+  const int N = resolve_moduli(moduli, m, n, k);
+  if (m <= 0 || n <= 0 || k <= 0 || alpha == 0.0 || ldc < m || N < 2 || N > kCrtMaxModuli)
+    return GB300_ERR_ARG;
+  OzakiGemmArgs a;
+  int b = 0;
+  const int rc = crt_block_args(m, n, k, 0, m, 0, n, alpha, beta, C, ldc, N, ws, ws_bytes, a, b);
+  if (rc != GB300_OK) return rc;
+  return crt_reconstruct_launch(a, b, st);
 }
 
 int crt_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,

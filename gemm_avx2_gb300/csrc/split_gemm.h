@@ -110,6 +110,30 @@ int split_sgemm_prepare_part(int z, char t, int m, int n, int k, const float *X,
 int split_sgemm_run_block(int m, int n, int k, int i0, int h, int j0, int w, float alpha,
                           float beta, float *C, int ldc, int products, const void *ws,
                           size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0 = 0);
+// Grouped launches of the tensor-core GEMMs: one persistent launch over the
+// 128 x 128 tiles of many prepared problems, each problem described by one
+// table entry (entry_bytes() bytes, 128-byte aligned) that *_group_entry
+// fills on the host from the problem's prepared workspace, with its first
+// work unit unit0 (the units of the entries before it; *units returns its
+// own); the caller copies the table to device memory and launches.  alpha != 0
+// and k > 0 (other problems need no GEMM).  The CRT
+// problems' reconstruction runs after the launch (crt_group_reconstruct).
+// Results are bit-identical to the per-problem calls.
+size_t bf16x_group_entry_bytes();
+size_t ozaki_group_entry_bytes();
+int bf16x_group_entry(int m, int n, int k, float alpha, float beta, float *C, int ldc,
+                      int products, const void *ws, size_t ws_bytes, unsigned *err, int unit0,
+                      void *entry, int *units);
+int ozaki_group_entry(const OzakiGemmArgs &a, unsigned *err, int unit0, void *entry, int *units);
+int crt_group_entry(int m, int n, int k, double alpha, double beta, double *C, int ldc,
+                    int moduli, const void *ws, size_t ws_bytes, unsigned *err, int unit0,
+                    void *entry, int *units);
+int crt_group_reconstruct(int m, int n, int k, double alpha, double beta, double *C, int ldc,
+                          int moduli, const void *ws, size_t ws_bytes, cudaStream_t st);
+int bf16x_group_launch(const void *table, int nprob, int total_units, cudaStream_t st,
+                       unsigned *err);
+int ozaki_group_launch(const void *table, int nprob, int total_units, cudaStream_t st,
+                       unsigned *err);
 int ozaki_prepare(char ta, char tb, int m, int n, int k, const double *A, int lda, const double *B,
                   int ldb, int slices, void *ws, size_t ws_bytes, cudaStream_t st);
 int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc, int slices,
@@ -128,8 +152,6 @@ int pair_mma_override();
 // Work units of the CRT GEMM: 0 = by shape, 1 = whole tiles, 2 = one modulus
 // of one tile (the moduli are independent GEMMs).
 void set_modulus_split(int v);
-// The same for launches from the calling thread only (the knob wins).
-void set_modulus_split_hint(int v);
 int modulus_split_override();
 // Tuned tile width (0 = none) and cluster mode (0 = none, 1 = pair MMAs,
 // 2 = one CTA per tile) of a shape class.

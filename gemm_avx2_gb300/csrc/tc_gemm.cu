@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 #include "common.cuh"
 #include "plain_gemm.h"
@@ -487,6 +488,19 @@ struct Bf16xParams {
   int rescale_chunk;
   float rescale;
   const int *expA, *expB;
+  // grouped launches (kernel GR = true): the table of GBxProblem, its length
+  // and the total number of work units (tiles) over all problems
+  const void *grp;
+  int nprob, total_units;
+};
+
+// One problem of a grouped launch of bf16x_gemm_kernel: its tensor maps over
+// its own prepared operands, its parameters and its first work unit; the
+// problems' units are concatenated in table order.
+struct alignas(128) GBxProblem {
+  CUtensorMap tmA, tmB;
+  Bf16xParams prm;
+  int unit0;
 };
 
 constexpr int kBxEpiWarps = 16;                     // 4 per TMEM lane quarter
@@ -526,13 +540,17 @@ struct ClusterTile {
   static constexpr int kSmem = kStages * kStage + 1024 + 256;
 };
 
-template <int CL, bool F16, int BN>
+// GR: a grouped launch over the problems of p.grp (one CTA per tile; the
+// kernel parameters' maps are unused), each unit a tile of one problem, with
+// that problem's K extent, chunk runs and epilogue parameters.
+template <int CL, bool F16, int BN, bool GR = false>
 __global__ void __launch_bounds__(kBxThreads, 1)
 bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                  Bf16xParams p) {
+                  const __grid_constant__ Bf16xParams p) {
   using T = TileN<BN>;
   using CT = ClusterTile<CL, BN>;
   static_assert(CL == 0 || CL == 2, "cluster modes: 0 (one CTA per tile) or 2 (pair MMAs)");
+  static_assert(!GR || CL == 0, "grouped launches run one CTA per tile");
   constexpr bool PAIR = CT::kPair;
   constexpr int kBxStages = CT::kStages, kBxStage = CT::kStage;
   constexpr int kBxColsPerWarp = T::kCols;
@@ -560,8 +578,10 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     mbar_init(done, 1);
     *abort_flag = 0;
     fence_barrier_init();
-    tma_prefetch_desc(&tmA);
-    tma_prefetch_desc(&tmB);
+    if (!GR) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+    }
   }
   if (warp == 1) {
     if (PAIR) { tmem_alloc_pair(tmem_slot, 512); tmem_relinquish_pair(); }
@@ -574,34 +594,71 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   const uint32_t tmem = *tmem_slot;
   // work units: tiles, or (PAIR) row-tile pairs whose rank-th row tile is this CTA's
   const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
+  const GBxProblem *grp = static_cast<const GBxProblem *>(p.grp);
   const int pm = PAIR ? (p.tiles_m + 1) / 2 : p.tiles_m;
-  const int nunits = pm * p.tiles_n;
+  const int nunits = GR ? p.total_units : pm * p.tiles_n;
   const int first = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
   const int stride = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
-  auto unit_tile = [&](int u, int &tm, int &tn) {
-    int um;
-    tile_coords(u, pm, p.tiles_n, PAIR ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
-    tm = PAIR ? 2 * um + (int)rank : um;  // PAIR: a row tile past the end is zero-filled, not stored
+  // grouped: the problem of unit u (the last whose unit0 <= u) and its parameters
+  auto prob_of = [&](int u) -> int {
+    if constexpr (!GR) return 0;
+    int lo = 0, hi = p.nprob - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (grp[mid].unit0 <= u) lo = mid; else hi = mid - 1;
+    }
+    return lo;
   };
-  auto run_end = [&](int r) { return r == 0 ? p.run_end0 : (r == 1 ? p.run_end1 : p.run_end2); };
-  auto run_chunk = [&](int r) {  // chunk length of run r in K blocks
-    const int len = run_end(r) - (r == 0 ? 0 : run_end(r - 1));
-    const int cl = r == 0 ? p.run_chunk0 : (r == 1 ? p.run_chunk1 : p.run_chunk2);
+  auto prm = [&](int i) -> const Bf16xParams * {
+    if constexpr (GR) return &grp[i].prm;
+    else return &p;
+  };
+  auto map_a = [&](int i) -> const void * {
+    if constexpr (GR) return &grp[i].tmA;
+    else return &tmA;
+  };
+  auto map_b = [&](int i) -> const void * {
+    if constexpr (GR) return &grp[i].tmB;
+    else return &tmB;
+  };
+  auto unit_tile = [&](int u, int i, int &tm, int &tn) {
+    if constexpr (GR) {
+      const Bf16xParams &q = grp[i].prm;
+      tile_coords(u - grp[i].unit0, q.tiles_m, q.tiles_n, kSplitGroupM, tm, tn);
+    } else {
+      int um;
+      tile_coords(u, pm, p.tiles_n, PAIR ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
+      tm = PAIR ? 2 * um + (int)rank : um;  // PAIR: a row tile past the end is zero-filled, not stored
+    }
+  };
+  auto run_end = [&](const Bf16xParams &q, int r) {
+    return r == 0 ? q.run_end0 : (r == 1 ? q.run_end1 : q.run_end2);
+  };
+  auto run_chunk = [&](const Bf16xParams &q, int r) {  // chunk length of run r in K blocks
+    const int len = run_end(q, r) - (r == 0 ? 0 : run_end(q, r - 1));
+    const int cl = r == 0 ? q.run_chunk0 : (r == 1 ? q.run_chunk1 : q.run_chunk2);
     return cl > 0 ? cl : len;
   };
-  int nchunks = 0;
-  for (int r = 0; r < p.nruns; ++r) {
-    const int len = run_end(r) - (r == 0 ? 0 : run_end(r - 1));
-    nchunks += (len + run_chunk(r) - 1) / run_chunk(r);
-  }
+  auto nchunks_of = [&](const Bf16xParams &q) {
+    int nc = 0;
+    for (int r = 0; r < q.nruns; ++r) {
+      const int len = run_end(q, r) - (r == 0 ? 0 : run_end(q, r - 1));
+      nc += (len + run_chunk(q, r) - 1) / run_chunk(q, r);
+    }
+    return nc;
+  };
+  const int nchunks1 = GR ? 0 : nchunks_of(p);  // the single problem's chunks per tile
 
   if (warp == 0) {
     if (lane == 0) {
       uint32_t L = 0;
       for (int u = first; u < nunits && !*abort_flag; u += stride) {
+        const int pi = prob_of(u);
+        const int kblocks = prm(pi)->kblocks;
+        const void *mA = map_a(pi), *mB = map_b(pi);
         int tm, tn;
-        unit_tile(u, tm, tn);
-        for (int kb = 0; kb < p.kblocks; ++kb, ++L) {
+        unit_tile(u, pi, tm, tn);
+        for (int kb = 0; kb < kblocks; ++kb, ++L) {
           const int s = L % kBxStages;
           const uint32_t r = L / kBxStages;
           if (!mbar_wait(&empty[s], (r & 1) ^ 1, p.err, kErrTimeoutEmpty, abort_flag)) break;
@@ -610,14 +667,14 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             // both CTAs' A rows and B halves land on the even CTA's full barrier
             if (rank == 0) mbar_arrive_expect_tx(&full[s], 2 * kBxStage);
             const uint32_t fb = cluster_addr(&full[s], 0);
-            tma_load_2d_pair(sa, &tmA, kb * kSplitBK, tm * kSplitBM, fb);
-            tma_load_2d_pair(sa + kBxABytes, &tmB, kb * kSplitBK, tn * BN + (int)rank * (BN / 2),
+            tma_load_2d_pair(sa, mA, kb * kSplitBK, tm * kSplitBM, fb);
+            tma_load_2d_pair(sa + kBxABytes, mB, kb * kSplitBK, tn * BN + (int)rank * (BN / 2),
                              fb);
             continue;
           }
           mbar_arrive_expect_tx(&full[s], kBxStage);  // own A and B tiles
-          tma_load_2d(sa, &tmA, kb * kSplitBK, tm * kSplitBM, &full[s]);
-          tma_load_2d(sa + kBxABytes, &tmB, kb * kSplitBK, tn * BN, &full[s]);
+          tma_load_2d(sa, mA, kb * kSplitBK, tm * kSplitBM, &full[s]);
+          tma_load_2d(sa + kBxABytes, mB, kb * kSplitBK, tn * BN, &full[s]);
         }
       }
     }
@@ -630,11 +687,13 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
+        const Bf16xParams &q = *prm(prob_of(u));
+        const int nchunks = GR ? nchunks_of(q) : nchunks1;
         int rn = 0, c0 = 0;
         for (int c = 0; c < nchunks && ok; ++c, ++chunk) {
           // chunk c covers K blocks [c0, c1) of run rn
-          const int rend = run_end(rn);
-          const int c1 = min(rend, c0 + run_chunk(rn));
+          const int rend = run_end(q, rn);
+          const int c1 = min(rend, c0 + run_chunk(q, rn));
           const int b = chunk & 1;
           const uint32_t u = chunk >> 1;
           // pair: half of the arrivals come from the odd CTA's epilogue warps
@@ -692,8 +751,11 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     uint32_t chunk = 0;
     bool ok = true;
     for (int u = first; u < nunits && ok; u += stride) {
+      const int pi = prob_of(u);
+      const Bf16xParams &pq = *prm(pi);
+      const int nchunks = GR ? nchunks_of(pq) : nchunks1;
       int tm, tn;
-      unit_tile(u, tm, tn);
+      unit_tile(u, pi, tm, tn);
       float run[kBxColsPerWarp];
 #pragma unroll
       for (int j = 0; j < kBxColsPerWarp; ++j) run[j] = 0.f;
@@ -702,9 +764,9 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const uint32_t u = chunk >> 1;
         if (!mbar_wait(&accf[b], u & 1, p.err, kErrTimeoutAcc, abort_flag)) { ok = false; break; }
         tc_fence_after();
-        if (F16 && c == p.rescale_chunk) {  // the hi*lo segments end: scale them by 2^-11 (exact)
+        if (F16 && c == pq.rescale_chunk) {  // the hi*lo segments end: scale them by 2^-11 (exact)
 #pragma unroll
-          for (int j = 0; j < kBxColsPerWarp; ++j) run[j] *= p.rescale;
+          for (int j = 0; j < kBxColsPerWarp; ++j) run[j] *= pq.rescale;
         }
 #pragma unroll
         for (int g = 0; g < kBxColsPerWarp / 16; ++g) {
@@ -725,11 +787,11 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       }
       if (!ok) break;
       const int row = tm * kSplitBM + row_in_tile;
-      if (row < p.m) {
+      if (row < pq.m) {
         const int col0 = tn * BN + h * kBxColsPerWarp;
         // scaled FP16 form: the row and column scales come off here (a
         // non-finite row or column is NaN already; its marker exponent is capped)
-        const int ea = F16 ? min(p.expA[row], 1024) - 30 : 0;
+        const int ea = F16 ? min(pq.expA[row], 1024) - 30 : 0;
         // C in batches of 16 columns: all loads of a batch are issued before its
         // stores, so the batch pays one memory latency instead of sixteen
 #pragma unroll
@@ -738,16 +800,18 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int col = col0 + jb + j;
-            cv[j] = (col < p.n) ? p.C[(int64_t)col * p.ldc + row] : 0.f;
+            cv[j] = (col < pq.n) ? pq.C[(int64_t)col * pq.ldc + row] : 0.f;
           }
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int col = col0 + jb + j;
-            if (col < p.n) {
+            if (col < pq.n) {
               const float v =
-                  F16 ? scale_pow2f(run[jb + j], ea + min(p.expB[col], 1024)) : run[jb + j];
-              const float cb = (p.beta == 1.0f) ? cv[j] : cv[j] * p.beta;
-              p.C[(int64_t)col * p.ldc + row] = cb + p.alpha * v;
+                  F16 ? scale_pow2f(run[jb + j], ea + min(pq.expB[col], 1024)) : run[jb + j];
+              // beta C + alpha v rounded as written (no contraction: every
+              // instantiation and the grouped launch round alike)
+              const float cb = (pq.beta == 1.0f) ? cv[j] : __fmul_rn(cv[j], pq.beta);
+              pq.C[(int64_t)col * pq.ldc + row] = __fadd_rn(cb, __fmul_rn(pq.alpha, v));
             }
           }
         }
@@ -797,6 +861,18 @@ struct OzakiParams {
   // first row of op(A) / column of op(B) in each operand block (a sub-block
   // of a larger problem's workspace; 0 for a whole problem)
   int row0, col0;
+  // grouped launches (kernel GR = true): the table of GOzProblem, its length
+  // and the total number of work units (whole tiles) over all problems
+  const void *grp;
+  int nprob, total_units;
+};
+
+// One problem of a grouped launch of ozaki_gemm_kernel (CRT mode, one CTA per
+// tile, whole-tile units): its tensor maps, parameters and first unit.
+struct alignas(128) GOzProblem {
+  CUtensorMap tmA, tmB;
+  OzakiParams prm;
+  int unit0;
 };
 
 constexpr int kOzEpiWarps = 16;  // 4 per TMEM lane quarter, BN / 4 columns each
@@ -842,13 +918,16 @@ constexpr int kCrtRunChunks = 64;
 // MODE: 0 = slice products folded into FP64, 1 = the CRT form's residue GEMMs
 // (p.mode holds the same value; the template keeps the two epilogues' register
 // allocations apart).
-template <int CL, int BN, int MODE>
+// GR: a grouped launch over the problems of p.grp (CRT mode, one CTA per tile,
+// each unit a whole tile of one problem with all its moduli).
+template <int CL, int BN, int MODE, bool GR = false>
 __global__ void __launch_bounds__(kOzThreads, 1)
 ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                  OzakiParams p) {
+                  const __grid_constant__ OzakiParams p) {
   using T = TileN<BN>;
   using CT = ClusterTile<CL, BN>;
   static_assert(CL == 0 || CL == 2, "cluster modes: 0 (one CTA per tile) or 2 (pair MMAs)");
+  static_assert(!GR || (CL == 0 && MODE == 1), "grouped launches: CRT mode, one CTA per tile");
   constexpr bool PAIR = CT::kPair;
   constexpr int kOzStages = CT::kStages, kOzStage = CT::kStage;
   constexpr int kOzCols = T::kCols;
@@ -873,8 +952,10 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     mbar_init(done, 1);
     *abort_flag = 0;
     fence_barrier_init();
-    tma_prefetch_desc(&tmA);
-    tma_prefetch_desc(&tmB);
+    if (!GR) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+    }
   }
   if (warp == 1) {
     if (PAIR) { tmem_alloc_pair(tmem_slot, 512); tmem_relinquish_pair(); }
@@ -885,25 +966,57 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   if (PAIR) cluster_sync();  // the peer's barriers are initialised before any remote arrive
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int S = p.S, KB = p.KB;
   // work units: tiles, or (PAIR) row-tile pairs whose rank-th row tile is this CTA's
   const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
   const int pm = PAIR ? (p.tiles_m + 1) / 2 : p.tiles_m;
   // units: (group range, tile), group-range major so that neighbouring units
   // share the residue planes of their moduli in L2
   const int ntu = pm * p.tiles_n;
-  const int nunits = ntu * p.gsplit;
+  const int nunits = GR ? p.total_units : ntu * p.gsplit;
   const int first = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
   const int stride = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
-  auto unit_tile = [&](int u, int &tm, int &tn) {
-    int um;
-    tile_coords(u % ntu, pm, p.tiles_n, PAIR ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
-    tm = PAIR ? 2 * um + (int)rank : um;
+  const GOzProblem *grp = static_cast<const GOzProblem *>(p.grp);
+  // grouped: the problem of unit u (the last whose unit0 <= u) and its parameters
+  auto prob_of = [&](int u) -> int {
+    if constexpr (!GR) return 0;
+    int lo = 0, hi = p.nprob - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (grp[mid].unit0 <= u) lo = mid; else hi = mid - 1;
+    }
+    return lo;
   };
-  auto unit_groups = [&](int u, int &g0, int &g1) {
-    const int gp = u / ntu;
-    g0 = gp * S / p.gsplit;
-    g1 = (gp + 1) * S / p.gsplit;
+  auto prm = [&](int i) -> const OzakiParams * {
+    if constexpr (GR) return &grp[i].prm;
+    else return &p;
+  };
+  auto map_a = [&](int i) -> const void * {
+    if constexpr (GR) return &grp[i].tmA;
+    else return &tmA;
+  };
+  auto map_b = [&](int i) -> const void * {
+    if constexpr (GR) return &grp[i].tmB;
+    else return &tmB;
+  };
+  auto unit_tile = [&](int u, int i, int &tm, int &tn) {
+    if constexpr (GR) {
+      const OzakiParams &q = grp[i].prm;
+      tile_coords(u - grp[i].unit0, q.tiles_m, q.tiles_n, kSplitGroupM, tm, tn);
+    } else {
+      int um;
+      tile_coords(u % ntu, pm, p.tiles_n, PAIR ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
+      tm = PAIR ? 2 * um + (int)rank : um;
+    }
+  };
+  auto unit_groups = [&](int u, const OzakiParams &q, int &g0, int &g1) {
+    if constexpr (GR) {
+      g0 = 0;
+      g1 = q.S;
+    } else {
+      const int gp = u / ntu;
+      g0 = gp * q.S / q.gsplit;
+      g1 = (gp + 1) * q.S / q.gsplit;
+    }
   };
 
   if (warp == 0) {
@@ -911,9 +1024,13 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t L = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
+        const int pi = prob_of(u);
+        const OzakiParams &q = *prm(pi);
+        const int S = q.S, KB = q.KB;
+        const void *mA = map_a(pi), *mB = map_b(pi);
         int tm, tn, g0, g1;
-        unit_tile(u, tm, tn);
-        unit_groups(u, g0, g1);
+        unit_tile(u, pi, tm, tn);
+        unit_groups(u, q, g0, g1);
         for (int gi = g0; gi < g1 && ok; ++gi) {
           int t, lo, np;
           group_of(MODE, gi, S, t, lo, np);
@@ -927,20 +1044,20 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               break;
             }
             uint8_t *sa_ptr = smem + s * kOzStage;
-            const int arow = (sa - 1) * p.Mp + p.row0 + tm * kSplitBM;
+            const int arow = (sa - 1) * q.Mp + q.row0 + tm * kSplitBM;
             if (PAIR) {
               // both CTAs' A rows and B halves land on the even CTA's full barrier
               if (rank == 0) mbar_arrive_expect_tx(&full[s], 2 * kOzStage);
               const uint32_t fb = cluster_addr(&full[s], 0);
-              tma_load_2d_pair(sa_ptr, &tmA, kb * kSplitBK, arow, fb);
-              tma_load_2d_pair(sa_ptr + kOzABytes, &tmB, kb * kSplitBK,
-                               (sb - 1) * p.Np + p.col0 + tn * BN + (int)rank * (BN / 2), fb);
+              tma_load_2d_pair(sa_ptr, mA, kb * kSplitBK, arow, fb);
+              tma_load_2d_pair(sa_ptr + kOzABytes, mB, kb * kSplitBK,
+                               (sb - 1) * q.Np + q.col0 + tn * BN + (int)rank * (BN / 2), fb);
               continue;
             }
             mbar_arrive_expect_tx(&full[s], kOzStage);
-            tma_load_2d(sa_ptr, &tmA, kb * kSplitBK, arow, &full[s]);
-            tma_load_2d(sa_ptr + kOzABytes, &tmB, kb * kSplitBK,
-                        (sb - 1) * p.Np + p.col0 + tn * BN, &full[s]);
+            tma_load_2d(sa_ptr, mA, kb * kSplitBK, arow, &full[s]);
+            tma_load_2d(sa_ptr + kOzABytes, mB, kb * kSplitBK,
+                        (sb - 1) * q.Np + q.col0 + tn * BN, &full[s]);
           }
         }
       }
@@ -953,8 +1070,10 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t L = 0, chunk = 0;
       bool ok = true;
       for (int u = first; u < nunits && ok; u += stride) {
+        const OzakiParams &q = *prm(prob_of(u));
+        const int S = q.S, KB = q.KB;
         int g0, g1;
-        unit_groups(u, g0, g1);
+        unit_groups(u, q, g0, g1);
         for (int gi = g0; gi < g1 && ok; ++gi) {
           int t, lo, np;
           group_of(MODE, gi, S, t, lo, np);
@@ -1017,13 +1136,16 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     uint32_t chunk = 0;
     bool ok = true;
     for (int u = first; u < nunits && ok; u += stride) {
+      const int pi = prob_of(u);
+      const OzakiParams &pq = *prm(pi);
+      const int S = pq.S, KB = pq.KB;
       int tm, tn, g0, g1;
-      unit_tile(u, tm, tn);
-      unit_groups(u, g0, g1);
-      const bool real = tm < p.tiles_m;  // PAIR: a row tile past the end writes nothing
+      unit_tile(u, pi, tm, tn);
+      unit_groups(u, pq, g0, g1);
+      const bool real = tm < pq.tiles_m;  // PAIR: a row tile past the end writes nothing
       const int row = tm * kSplitBM + row_in_tile;          // < Mp when real
       const int col0 = tn * BN + h * kOzCols;          // first of this warp's columns
-      double *res = p.res + (int64_t)col0 * p.Mp + row;      // res[j * Mp] is column col0 + j
+      double *res = pq.res + (int64_t)col0 * pq.Mp + row;      // res[j * Mp] is column col0 + j
       bool res_init = false;
       const int run_limit = MODE ? kCrtRunChunks : kOzRunChunks;
       for (int gi = g0; gi < g1 && ok; ++gi) {
@@ -1034,8 +1156,8 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         // residue plane of modulus gi: words of 4 consecutive columns,
         // word (col / 4) * Mp + row (the reconstruction reads one word per
         // modulus for 4 columns of a row; a warp's 32 rows store 128 bytes)
-        uint32_t *plane = MODE ? reinterpret_cast<uint32_t *>(p.rres + (int64_t)gi * p.Mp * p.Np) +
-                                     (int64_t)(col0 >> 2) * p.Mp + row
+        uint32_t *plane = MODE ? reinterpret_cast<uint32_t *>(pq.rres + (int64_t)gi * pq.Mp * pq.Np) +
+                                     (int64_t)(col0 >> 2) * pq.Mp + row
                                : nullptr;
         if (MODE && nch == 1) {
           // CRT form, K of this modulus in one chunk (k <= 1024): each chunk
@@ -1049,7 +1171,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           ++chunk;
           if (!mbar_wait(&accf[b], uph & 1, p.err, kErrTimeoutAcc, abort_flag)) { ok = false; break; }
           tc_fence_after();
-          const float pf = p.mods_f[gi], ip = p.mods_inv[gi];
+          const float pf = pq.mods_f[gi], ip = pq.mods_inv[gi];
           // two halves of the warp's columns: the second half's TMEM loads
           // release the accumulator, the first half is stored meanwhile
           constexpr int kHalf = kOzCols / 2;
@@ -1087,7 +1209,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                   // r + 2^23 holds r in its low mantissa bits (0 <= r < 256)
                   w |= (__float_as_uint(r + 8388608.0f) & 0xffu) << (8 * e);
                 }
-                plane[(int64_t)(hf * kHalf / 4 + qd) * p.Mp] = w;
+                plane[(int64_t)(hf * kHalf / 4 + qd) * pq.Mp] = w;
               }
             }
           }
@@ -1128,7 +1250,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             // |run| < 64 chunks x 2^24 = 2^30 < 149 * 2^23, so run + pm * 2^23 is in
             // [0, 2^32): one Barrett step (q = the quotient or one less) and an
             // unsigned-min correction give run mod pm in [0, pm)
-            const unsigned pm = (unsigned)p.mods[gi], mg = p.mods_mg[gi], off = pm << 23;
+            const unsigned pm = (unsigned)pq.mods[gi], mg = pq.mods_mg[gi], off = pm << 23;
 #pragma unroll
             for (int j = 0; j < kOzCols; ++j) {
               const unsigned x = (unsigned)run[j] + off;
@@ -1138,7 +1260,7 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             if (last && real) {
 #pragma unroll
               for (int qd = 0; qd < kOzCols / 4; ++qd)
-                plane[(int64_t)qd * p.Mp] = (uint32_t)run[4 * qd] |
+                plane[(int64_t)qd * pq.Mp] = (uint32_t)run[4 * qd] |
                                             ((uint32_t)run[4 * qd + 1] << 8) |
                                             ((uint32_t)run[4 * qd + 2] << 16) |
                                             ((uint32_t)run[4 * qd + 3] << 24);
@@ -1150,10 +1272,10 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             for (int g = 0; g < kOzCols && real; g += 8) {
               double prev[8];
 #pragma unroll
-              for (int j = 0; j < 8; ++j) prev[j] = res_init ? res[(int64_t)(g + j) * p.Mp] : 0.0;
+              for (int j = 0; j < 8; ++j) prev[j] = res_init ? res[(int64_t)(g + j) * pq.Mp] : 0.0;
 #pragma unroll
               for (int j = 0; j < 8; ++j) {
-                res[(int64_t)(g + j) * p.Mp] = fma((double)run[g + j], wt, prev[j]);
+                res[(int64_t)(g + j) * pq.Mp] = fma((double)run[g + j], wt, prev[j]);
                 run[g + j] = 0;
               }
             }
@@ -1165,27 +1287,27 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       if (!ok) break;
       // final epilogue: C = alpha * 2^(E_i + F_j) * res + beta * C (slice form;
       // the CRT form's C update is the reconstruction kernel's)
-      if (!MODE && real && row < p.m) {
-        const int ea = p.expA[row];
+      if (!MODE && real && row < pq.m) {
+        const int ea = pq.expA[row];
 #pragma unroll 1
         for (int g = 0; g < kOzCols; g += 8) {
           double rv[8], cv[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int col = col0 + g + j;
-            rv[j] = res[(int64_t)(g + j) * p.Mp];
-            cv[j] = (col < p.n) ? p.C[(int64_t)col * p.ldc + row] : 0.0;
+            rv[j] = res[(int64_t)(g + j) * pq.Mp];
+            cv[j] = (col < pq.n) ? pq.C[(int64_t)col * pq.ldc + row] : 0.0;
           }
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int col = col0 + g + j;
-            if (col < p.n) {
-              const int eb = p.expB[col];
+            if (col < pq.n) {
+              const int eb = pq.expB[col];
               const double v = (ea == kNonFiniteExp || eb == kNonFiniteExp)
                                    ? __longlong_as_double(0x7ff8000000000000LL)
                                    : scale_pow2(rv[j], ea + eb);
-              const double cb = (p.beta == 1.0) ? cv[j] : cv[j] * p.beta;
-              p.C[(int64_t)col * p.ldc + row] = cb + p.alpha * v;
+              const double cb = (pq.beta == 1.0) ? cv[j] : __dmul_rn(cv[j], pq.beta);
+              pq.C[(int64_t)col * pq.ldc + row] = __dadd_rn(cb, __dmul_rn(pq.alpha, v));
             }
           }
         }
@@ -1565,17 +1687,10 @@ static int g_pair_mma = 0;  // 0: none, 1: pair MMAs, 2: one CTA per tile
 void set_pair_mma(int v) { g_pair_mma = v; }
 int pair_mma_override() { return g_pair_mma; }
 // Work units of the CRT GEMM: 0 = by shape, 1 = whole tiles (all moduli),
-// 2 = one modulus of one tile.  Same results bit for bit.  The knob wins over
-// the calling thread's hint (the grouped graph's capture asks for whole
-// tiles: its problems run side by side, and one-modulus units would multiply
-// each small problem's CTAs and their setup).
+// 2 = one modulus of one tile.  Same results bit for bit.
 static int g_modulus_split = 0;
-static thread_local int t_modulus_split_hint = 0;
 void set_modulus_split(int v) { g_modulus_split = v; }
-void set_modulus_split_hint(int v) { t_modulus_split_hint = v; }
-int modulus_split_override() {
-  return g_modulus_split ? g_modulus_split : t_modulus_split_hint;
-}
+int modulus_split_override() { return g_modulus_split; }
 static bool use_pair_mma(int kind, int m, int n, int k) {
   const int v = g_pair_mma ? g_pair_mma : tune_pair_mma(kind, m, n, k);
   return v != 2;
@@ -1605,33 +1720,23 @@ int split_sgemm_run(int m, int n, int k, float alpha, float beta, float *C, int 
                                st, err, chunk0);
 }
 
-int split_sgemm_run_block(int m, int n, int k, int i0, int h, int j0, int w, float alpha,
-                          float beta, float *C, int ldc, int products, const void *ws,
-                          size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0) {
-  if (products == 0) {
-    int c = 0;
-    bf16x_resolve(m, n, k, &products, &c);
-    if (chunk0 == 0) chunk0 = c;
-  }
-  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || !split_products_ok(products) ||
-      i0 < 0 || j0 < 0 || h < 0 || w < 0 || i0 % kSplitBM || j0 % kBf16xBN || i0 + h > m ||
-      j0 + w > n)
-    return GB300_ERR_ARG;
-  if (h == 0 || w == 0) return GB300_OK;
-  float *Cb = C + i0 + (int64_t)j0 * ldc;
-  if (alpha == 0.0f || k == 0)
-    return plain_sgemm('N', 'N', h, w, 0, alpha, nullptr, h > 1 ? h : 1, nullptr, 1, beta, Cb,
-                       ldc, st, err);
+// The layout and kernel parameters of the C block (i0, h) x (j0, w) of a
+// prepared problem (the tile width is set by the launch).  products and
+// chunk0 as resolved by the caller.
+static int bf16x_block_setup(int m, int n, int k, int i0, int h, int j0, int w, float alpha,
+                             float beta, float *C, int ldc, int products, int chunk0,
+                             const void *ws, size_t ws_bytes, unsigned *err, Bf16xLayout &L,
+                             Bf16xParams &p) {
   const size_t need = split_workspace_bytes(0, m, n, k, products);
   if (!ws || ws_bytes < need) return GB300_ERR_WORKSPACE;
   const Bf16xLayout Lf = bf16x_layout(m, n, k, products, const_cast<void *>(ws));
   // the block's rows of A' and columns of B' (tile-aligned offsets)
-  Bf16xLayout L = Lf;
+  L = Lf;
   L.Ap = Lf.Ap + (int64_t)i0 * Lf.Kld;
   L.Bp = Lf.Bp + (int64_t)j0 * Lf.Kld;
   L.Mp = round_up(h, kSplitBM);
   L.Np = round_up(w, kBf16xBN);
-  Bf16xParams p;
+  std::memset(&p, 0, sizeof(p));
   p.m = h; p.n = w;
   p.tiles_m = (int)(L.Mp / kSplitBM);
   p.tiles_n = 0;  // set by the launch for its tile width
@@ -1660,12 +1765,11 @@ int split_sgemm_run_block(int m, int n, int k, int i0, int h, int j0, int w, flo
       p.run_end2 = 3 * skb; p.run_chunk2 = c0;
     }
   }
-  p.alpha = alpha; p.beta = beta; p.C = Cb; p.ldc = ldc; p.err = err;
-  const bool f16 = products == kFp16x3;
+  p.alpha = alpha; p.beta = beta; p.C = C + i0 + (int64_t)j0 * ldc; p.ldc = ldc; p.err = err;
   p.rescale_chunk = -1;
   p.rescale = 1.0f;
   p.expA = p.expB = nullptr;
-  if (f16) {
+  if (products == kFp16x3) {
     // segments 0 and 1 (lo*hi, hi*lo, run 0) carry 2^11 x their value; their
     // chunks come first, so the running sums are scaled once when run 1 starts
     p.rescale_chunk = (p.run_end0 + p.run_chunk0 - 1) / p.run_chunk0;
@@ -1673,12 +1777,92 @@ int split_sgemm_run_block(int m, int n, int k, int i0, int h, int j0, int w, flo
     p.expA = Lf.ex + i0;
     p.expB = Lf.ex + Lf.Mp + j0;
   }
+  return GB300_OK;
+}
+
+int split_sgemm_run_block(int m, int n, int k, int i0, int h, int j0, int w, float alpha,
+                          float beta, float *C, int ldc, int products, const void *ws,
+                          size_t ws_bytes, cudaStream_t st, unsigned *err, int chunk0) {
+  if (products == 0) {
+    int c = 0;
+    bf16x_resolve(m, n, k, &products, &c);
+    if (chunk0 == 0) chunk0 = c;
+  }
+  if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || !split_products_ok(products) ||
+      i0 < 0 || j0 < 0 || h < 0 || w < 0 || i0 % kSplitBM || j0 % kBf16xBN || i0 + h > m ||
+      j0 + w > n)
+    return GB300_ERR_ARG;
+  if (h == 0 || w == 0) return GB300_OK;
+  if (alpha == 0.0f || k == 0)
+    return plain_sgemm('N', 'N', h, w, 0, alpha, nullptr, h > 1 ? h : 1, nullptr, 1, beta,
+                       C + i0 + (int64_t)j0 * ldc, ldc, st, err);
+  Bf16xLayout L;
+  Bf16xParams p;
+  const int rc = bf16x_block_setup(m, n, k, i0, h, j0, w, alpha, beta, C, ldc, products, chunk0,
+                                   ws, ws_bytes, err, L, p);
+  if (rc != GB300_OK) return rc;
   const int bn = split_tile_n(0, m, n, k);
-  if (f16)
+  if (products == kFp16x3)
     return bn == 128 ? bf16x_launch<true, 128>(L, p, m, n, k, st)
                      : bf16x_launch<true, 256>(L, p, m, n, k, st);
   return bn == 128 ? bf16x_launch<false, 128>(L, p, m, n, k, st)
                    : bf16x_launch<false, 256>(L, p, m, n, k, st);
+}
+
+// ---------------------------------------------------------- grouped launches
+// The grouped batch's GEMMs in one persistent launch per kind: every problem's
+// operands are prepared in its own workspace first, then one launch runs the
+// concatenated tiles of all problems (128 x 128 tiles, one CTA per tile), each
+// tile with its problem's tensor maps and parameters from a device table.
+// The tiles of a problem are computed exactly as by its own call (same K
+// order and chunks), so results are bit-identical to the per-problem calls.
+constexpr int kGroupBN = 128;  // tile width of grouped launches (least padding)
+size_t bf16x_group_entry_bytes() { return sizeof(GBxProblem); }
+size_t ozaki_group_entry_bytes() { return sizeof(GOzProblem); }
+
+int bf16x_group_entry(int m, int n, int k, float alpha, float beta, float *C, int ldc,
+                      int products, const void *ws, size_t ws_bytes, unsigned *err, int unit0,
+                      void *entry, int *units) {
+  if (m <= 0 || n <= 0 || k <= 0 || alpha == 0.0f || ldc < m ||
+      (products != 6 && products != 3))
+    return GB300_ERR_ARG;
+  Bf16xLayout L;
+  GBxProblem e;
+  std::memset(&e, 0, sizeof(e));
+  const int rc = bf16x_block_setup(m, n, k, 0, m, 0, n, alpha, beta, C, ldc, products, 0, ws,
+                                   ws_bytes, err, L, e.prm);
+  if (rc != GB300_OK) return rc;
+  if (!encode_2d(&e.tmA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
+      !encode_2d(&e.tmB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, kGroupBN, true))
+    return GB300_ERR_CUDA;
+  e.prm.tiles_n = (n + kGroupBN - 1) / kGroupBN;
+  e.unit0 = unit0;
+  *units = e.prm.tiles_m * e.prm.tiles_n;
+  std::memcpy(entry, &e, sizeof(e));
+  return GB300_OK;
+}
+
+// table: nprob entries in device memory, in the order of their unit0.
+template <typename P>
+static int group_launch(void (*kern)(const CUtensorMap, const CUtensorMap, P), int threads,
+                        int smem, const P &p, cudaStream_t st) {
+  if (p.total_units <= 0) return GB300_OK;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+      cudaSuccess)
+    return GB300_ERR_CUDA;
+  const CUtensorMap unused{};  // each problem's maps come from the table
+  const int grid = p.total_units < sm_count() ? p.total_units : sm_count();
+  kern<<<grid, threads, smem, st>>>(unused, unused, p);
+  return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+}
+
+int bf16x_group_launch(const void *table, int nprob, int total_units, cudaStream_t st,
+                       unsigned *err) {
+  Bf16xParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.grp = table; p.nprob = nprob; p.total_units = total_units; p.err = err;
+  return group_launch<Bf16xParams>(bf16x_gemm_kernel<0, false, kGroupBN, true>, kBxThreads,
+                                   ClusterTile<0, kGroupBN>::kSmem, p, st);
 }
 
 int split_sgemm(char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
@@ -1797,9 +1981,8 @@ static int ozaki_launch_bn(const OzakiGemmArgs &a, OzakiParams p, cudaStream_t s
                                         p.tiles_n * p.gsplit, pair, st);
 }
 
-int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
-  if (a.S < 1 || a.S > (a.mode ? kCrtMaxModuli : kOzakiMaxSlices)) return GB300_ERR_ARG;
-  OzakiParams p;
+static void ozaki_params(const OzakiGemmArgs &a, unsigned *err, OzakiParams &p) {
+  std::memset(&p, 0, sizeof(p));
   p.m = a.m; p.n = a.n;
   p.tiles_m = (a.m + kSplitBM - 1) / kSplitBM;  // Mp / 128 for a whole problem
   p.row0 = a.row0; p.col0 = a.col0;
@@ -1815,8 +1998,43 @@ int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
     p.mods_f[i] = (float)p.mods[i];
     p.mods_inv[i] = 1.0f / (float)p.mods[i];
   }
+}
+
+int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err) {
+  if (a.S < 1 || a.S > (a.mode ? kCrtMaxModuli : kOzakiMaxSlices)) return GB300_ERR_ARG;
+  OzakiParams p;
+  ozaki_params(a, err, p);
   return split_tile_n(a.mode ? 2 : 1, a.m, a.n, a.k) == 128 ? ozaki_launch_bn<128>(a, p, st)
                                                            : ozaki_launch_bn<256>(a, p, st);
+}
+
+// One CRT problem (mode 1, a whole problem) of a grouped launch: its table
+// entry, whole-tile units (all moduli of a tile in one unit).
+int ozaki_group_entry(const OzakiGemmArgs &a, unsigned *err, int unit0, void *entry, int *units) {
+  if (a.mode != 1 || a.S < 2 || a.S > kCrtMaxModuli || a.row0 || a.col0 || a.m <= 0 || a.n <= 0)
+    return GB300_ERR_ARG;
+  GOzProblem e;
+  std::memset(&e, 0, sizeof(e));
+  ozaki_params(a, err, e.prm);
+  if (!encode_2d(&e.tmA, a.As, 2, a.Kp, a.S * a.Mp, a.Kp, kSplitBK, kSplitBM, true) ||
+      !encode_2d(&e.tmB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, kGroupBN, true))
+    return GB300_ERR_CUDA;
+  e.prm.tiles_n = (a.n + kGroupBN - 1) / kGroupBN;
+  e.prm.gsplit = 1;
+  e.unit0 = unit0;
+  *units = e.prm.tiles_m * e.prm.tiles_n;
+  std::memcpy(entry, &e, sizeof(e));
+  return GB300_OK;
+}
+
+int ozaki_group_launch(const void *table, int nprob, int total_units, cudaStream_t st,
+                       unsigned *err) {
+  OzakiParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.mode = 1; p.gsplit = 1;
+  p.grp = table; p.nprob = nprob; p.total_units = total_units; p.err = err;
+  return group_launch<OzakiParams>(ozaki_gemm_kernel<0, kGroupBN, 1, true>, kOzThreads,
+                                   ClusterTile<0, kGroupBN>::kSmem, p, st);
 }
 
 int ozaki_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,

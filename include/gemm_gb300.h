@@ -223,14 +223,23 @@ int gb300_gemm_grouped_ws(const gb300_gemm_problem *problems, int count, void *w
  * no host-side work: the operand pointers are fixed, their contents may
  * change between launches.
  *   form 0: plain forms, one persistent launch (as gb300_gemm_grouped);
- *   form 1: split forms, one call per problem (FP32: 6xBF16, FP64: the CRT
- *           form with the tuned / default moduli count), captured as 16 parallel branches
- *           (longest work first onto the least-loaded branch), each branch
- *           with its own workspace. */
+ *   form 1: split forms (FP32: 6xBF16, FP64: the CRT form with the tuned /
+ *           default moduli count): the operands of every problem are
+ *           prepared in parallel branches (GB300_TUNE_GRAPH_BRANCHES), then
+ *           ONE persistent launch runs the residue GEMMs of all FP64
+ *           problems and ONE the 6xBF16 GEMMs of all FP32 problems (128 x 128
+ *           tiles of all problems, costliest first), then the FP64 problems'
+ *           reconstructions run in branches.  Each problem has its own
+ *           workspace (the graph holds the sum of the per-problem workspace
+ *           sizes).  Results are bit-identical to gb300_dgemm_ozaki2 /
+ *           gb300_sgemm_bf16x(products = 6) called on each problem.
+ * gb300_grouped_graph_stats: the graph's kernel nodes and, of those, its
+ * GEMM launches (1 for form 0; at most 2 for form 1). */
 typedef struct gb300_grouped_graph_s *gb300_grouped_graph;
 int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int count, int form,
                                gb300_grouped_graph *out);
 int gb300_grouped_graph_launch(gb300_grouped_graph graph, void *stream);
+int gb300_grouped_graph_stats(gb300_grouped_graph graph, int *kernel_nodes, int *gemm_launches);
 int gb300_grouped_graph_destroy(gb300_grouped_graph graph);
 
 /* ------------------------------------------------------------------------

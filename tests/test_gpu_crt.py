@@ -121,6 +121,21 @@ def test_multi_chunk_bitexact(orc, k, cluster_mode):
     assert g.device_error() == 0
 
 
+def test_general_alpha_beta_bitexact(orc, cluster_mode):
+    """alpha and beta that are not powers of two: the C update is
+    beta c + alpha v with each product and the sum rounded once, as in the
+    model (no fused multiply-add, whatever the kernel instantiation)."""
+    m, n, k = 260, 150, 300
+    A = orc.spread((m, k), 60, 0, 1.0)
+    B = orc.spread((k, n), 60, 1, 1.0)
+    C = orc.uniform((m, n), np.float64, 60, 2)
+    rc, got, _ = run_crt("N", "N", m, n, k, A, m, B, k, C, 16, alpha=0.7318, beta=-1.3)
+    assert rc == g.OK
+    model = crt.crt_gemm_model(A, B, 16, alpha=0.7318, beta=-1.3, C=C)
+    assert np.array_equal(got, model), np.abs(got - model).max()
+    assert g.device_error() == 0
+
+
 def test_nonfinite_rows_and_columns(orc):
     m, n, k = 40, 30, 50
     A = orc.uniform((m, k), np.float64, 53, 0)
