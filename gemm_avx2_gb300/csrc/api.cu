@@ -972,10 +972,15 @@ GB300_API int gb300_gemm_grouped(const gb300_gemm_problem *problems, int count, 
 // capture stream, problems assigned longest-work-first to the least-loaded
 // branch), one grouped persistent launch of the CRT residue GEMMs of all FP64
 // problems and one of the 6xBF16 GEMMs of all FP32 problems, then the FP64
-// problems' reconstructions in branches.  Every problem has its own
-// workspace (one allocation).  Problems with alpha = 0 or k = 0 run their
-// per-problem call in a branch.  GB300_TUNE_GRAPH_BRANCHES (read when a graph
-// is created) sets the branch count.
+// problems' reconstructions in branches.  Each branch prepares its FP32
+// problems first: their GEMM launch (on a forked stream) then overlaps the
+// FP64 problems' preparation.  Every problem has its own workspace (one
+// allocation).  Problems with alpha = 0 or k = 0 run their per-problem call
+// in a branch.  GB300_TUNE_GRAPH_BRANCHES (read when a graph is created) sets
+// the branch count.  (Grouped launches of the preparation and
+// reconstruction kernels too, one per kernel over all problems, measured
+// slower on the 1024-problem batch: 12.3 against 10.5 ms, as the phases no
+// longer overlap.)
 constexpr int kGraphBranches = 64;  // upper bound
 constexpr int kDefaultGraphBranches = 32;
 static int g_graph_branches = kDefaultGraphBranches;
@@ -1035,13 +1040,13 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
   gb300_grouped_graph g = new (std::nothrow) gb300_grouped_graph_s();
   if (!g) return GB300_ERR_NOMEM;
   cudaGetDevice(&g->device);
-  cudaStream_t cs = nullptr;
+  cudaStream_t cs = nullptr, fs = nullptr;  // capture stream, the FP32 GEMM's stream
   int rc = GB300_OK;
   std::vector<uint8_t> blob;
   int used = 0, tiles = 0;
   const int nbr = g_graph_branches;
   cudaStream_t bs[kGraphBranches] = {nullptr};
-  cudaEvent_t fork = nullptr, join[kGraphBranches] = {nullptr};
+  cudaEvent_t fork = nullptr, fdone = nullptr, join[kGraphBranches] = {nullptr};
   std::vector<GraphItem> items(count > 0 ? count : 1);
   // form 1: the grouped GEMM tables (FP64 entries, then FP32), in device order
   std::vector<int> ord_d, ord_s;
@@ -1134,7 +1139,9 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
   if (rc == GB300_OK && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
     rc = GB300_ERR_CUDA;
   if (rc == GB300_OK && form == 1) {
-    bool ok = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess;
+    bool ok = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&fdone, cudaEventDisableTiming) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&fs, cudaStreamNonBlocking) == cudaSuccess;
     for (int b = 0; b < nbr && ok; ++b)
       ok = cudaStreamCreateWithFlags(&bs[b], cudaStreamNonBlocking) == cudaSuccess &&
            cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming) == cudaSuccess;
@@ -1164,11 +1171,27 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
         else rc2 = grouped_launch_blob(g->meta, used, tiles, cs, s->err);
       }
     } else {
-      // 1. preparation (and the per-problem calls)
+      // 1. preparation (and the per-problem calls): each branch prepares its
+      // FP32 problems first, so that their grouped GEMM (on the forked stream
+      // fs) runs while the branches prepare the FP64 problems
       if (!fork_all()) rc2 = GB300_ERR_CUDA;
+      for (int pass = 0; pass < 2 && rc2 == GB300_OK; ++pass) {
+      if (pass == 1 && !ord_s.empty()) {
+        for (int b = 0; b < nbr && rc2 == GB300_OK; ++b)
+          if (cudaEventRecord(join[b], bs[b]) != cudaSuccess ||
+              cudaStreamWaitEvent(fs, join[b], 0) != cudaSuccess)
+            rc2 = GB300_ERR_CUDA;
+        if (rc2 == GB300_OK) {
+          rc2 = bf16x_group_launch(static_cast<uint8_t *>(g->meta) + ord_d.size() * eb_d,
+                                   (int)ord_s.size(), units_s, fs, s->err);
+          ++g->gemm_launches;
+        }
+        if (rc2 == GB300_OK && cudaEventRecord(fdone, fs) != cudaSuccess) rc2 = GB300_ERR_CUDA;
+      }
       for (int i = 0; i < count && rc2 == GB300_OK; ++i) {
         const gb300_gemm_problem &q = problems[i];
         const GraphItem &it = items[i];
+        if ((it.cls == 2) != (pass == 1)) continue;
         cudaStream_t st = bs[it.branch];
         void *ws = static_cast<uint8_t *>(g->ws) + it.ws_off;
         if (it.cls == 1) {  // C = beta C, as the split calls do it
@@ -1189,15 +1212,11 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
                                     it.ws_bytes, st);
         }
       }
+      }
       if (rc2 == GB300_OK && !join_all()) rc2 = GB300_ERR_CUDA;
-      // 2. the grouped GEMMs
+      // 2. the FP64 problems' grouped GEMM
       if (rc2 == GB300_OK && !ord_d.empty()) {
         rc2 = ozaki_group_launch(g->meta, (int)ord_d.size(), units_d, cs, s->err);
-        ++g->gemm_launches;
-      }
-      if (rc2 == GB300_OK && !ord_s.empty()) {
-        rc2 = bf16x_group_launch(static_cast<uint8_t *>(g->meta) + ord_d.size() * eb_d,
-                                 (int)ord_s.size(), units_s, cs, s->err);
         ++g->gemm_launches;
       }
       // 3. the FP64 problems' reconstruction
@@ -1212,6 +1231,8 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
         }
         if (rc2 == GB300_OK && !join_all()) rc2 = GB300_ERR_CUDA;
       }
+      if (rc2 == GB300_OK && !ord_s.empty() && cudaStreamWaitEvent(cs, fdone, 0) != cudaSuccess)
+        rc2 = GB300_ERR_CUDA;
     }
     cudaGraph_t graph = nullptr;
     const cudaError_t e = cudaStreamEndCapture(cs, &graph);
@@ -1239,6 +1260,8 @@ GB300_API int gb300_grouped_graph_create(const gb300_gemm_problem *problems, int
     if (join[b]) cudaEventDestroy(join[b]);
   }
   if (fork) cudaEventDestroy(fork);
+  if (fdone) cudaEventDestroy(fdone);
+  if (fs) cudaStreamDestroy(fs);
   if (rc != GB300_OK) {
     gb300_grouped_graph_destroy(g);
     return rc;

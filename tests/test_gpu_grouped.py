@@ -140,47 +140,59 @@ def test_grouped_split_graph(orc):
     assert g.device_error() == 0
 
 
+def per_problem_split_calls(probs, dev, C_inputs):
+    """Each problem's own split call (CRT form / 6xBF16) from C_inputs; the results."""
+    for p, (dA, dB, dC), C0 in zip(probs, dev, C_inputs):
+        dC.copy_(to_dev(C0))
+        args = (p["transa"], p["transb"], p["m"], p["n"], p["k"], p["alpha"], dA.data_ptr(),
+                p["lda"], dB.data_ptr(), p["ldb"], p["beta"], dC.data_ptr(), p["ldc"])
+        rc = g.dgemm_ozaki2(*args) if p["precision"] == "d" else g.sgemm_bf16x(*args, products=6)
+        assert rc == g.OK
+    sync()
+    return [from_dev(d[2], C0.shape[0]) for d, C0 in zip(dev, C_inputs)]
+
+
 def test_grouped_split_graph_matches_per_problem_calls(orc):
     """The split-form graph runs the GEMMs of all FP64 problems in one grouped
     launch and those of all FP32 problems in another (128 x 128 tiles of many
-    problems, each tile with its problem's tensor maps and parameters); every
-    result is bit-identical to the problem's own gb300_dgemm_ozaki2 /
-    gb300_sgemm_bf16x(products = 6) call.  Dimensions up to 700 (several row
-    and column tiles per problem), odd leading dimensions, alpha == 0 and
-    k == 0 problems."""
+    problems, each tile with its problem's tensor maps and parameters from a
+    device table); every result is bit-identical to the problem's own
+    gb300_dgemm_ozaki2 / gb300_sgemm_bf16x(products = 6) call, on the first
+    replay and on a second one with new operand values.  Dimensions up to 700
+    (several row and column tiles per problem), odd leading dimensions,
+    alpha == 0 and k == 0 problems."""
     probs, host, dev = make_batch(orc, 40, 6, max_dim=700)
     C_init = [h[2].copy(order="F") for h in host]
     graph = g.GroupedGraph(probs, form=1)
     kernels, gemms = graph.stats()
-    n_d = sum(1 for p in probs if p["precision"] == "d" and p["m"] and p["n"] and p["k"]
-              and p["alpha"] != 0)
-    n_s = sum(1 for p in probs if p["precision"] == "s" and p["m"] and p["n"] and p["k"]
-              and p["alpha"] != 0)
+    live = [p for p in probs if p["m"] and p["n"]]
+    n_d = sum(1 for p in live if p["precision"] == "d" and p["k"] and p["alpha"] != 0)
+    n_s = sum(1 for p in live if p["precision"] == "s" and p["k"] and p["alpha"] != 0)
+    n_calls = sum(1 for p in live if not p["k"] or p["alpha"] == 0)
     assert gemms == (n_d > 0) + (n_s > 0) and gemms <= 2
-    assert kernels >= gemms + 3 * n_d + n_s
-    assert graph.launch() == g.OK
-    sync()
-    grouped = [from_dev(d[2], h[2].shape[0]) for d, h in zip(dev, host)]
-    for p, (dA, dB, dC), C0 in zip(probs, dev, C_init):
-        dC.copy_(to_dev(C0))
-        args = (p["transa"], p["transb"], p["m"], p["n"], p["k"], p["alpha"], dA.data_ptr(),
-                p["lda"], dB.data_ptr(), p["ldb"], p["beta"], dC.data_ptr(), p["ldc"])
-        if p["precision"] == "d":
-            assert g.dgemm_ozaki2(*args) == g.OK
-        else:
-            assert g.sgemm_bf16x(*args, products=6) == g.OK
-    sync()
-    for i, ((dA, dB, dC), h) in enumerate(zip(dev, host)):
-        assert np.array_equal(grouped[i], from_dev(dC, h[2].shape[0]), equal_nan=True), \
-            (i, probs[i]["precision"], probs[i]["m"], probs[i]["n"], probs[i]["k"])
+    # per FP64 problem: exponents, residues, reconstruction; per FP32 problem: split
+    assert gemms + 3 * n_d + n_s <= kernels <= gemms + 3 * n_d + n_s + n_calls
+    for rnd in range(2):
+        if rnd:   # new operand values (other magnitudes) in the same buffers, C reset
+            for (A, B, C), (dA, dB, dC), C0 in zip(host, dev, C_init):
+                dA.copy_(to_dev((A * -0.37).astype(A.dtype, order="F")))
+                dC.copy_(to_dev(C0))
+        assert graph.launch() == g.OK
+        sync()
+        grouped = [from_dev(d[2], h[2].shape[0]) for d, h in zip(dev, host)]
+        single = per_problem_split_calls(probs, dev, C_init)
+        for i in range(len(probs)):
+            assert np.array_equal(grouped[i], single[i], equal_nan=True), \
+                (rnd, i, probs[i]["precision"], probs[i]["m"], probs[i]["n"], probs[i]["k"])
     graph.destroy()
     assert g.device_error() == 0
 
 
 def test_grouped_split_graph_long_k(orc):
     """FP64 problems with k > 1024 (the CRT epilogue's multi-chunk path) and
-    FP32 ones with several chunk runs, in the grouped launches, against the
-    per-problem calls bit for bit."""
+    FP32 ones with several chunk runs, one with an Inf and one with a NaN
+    operand, in the grouped launches, against the per-problem calls bit for
+    bit (NaN where they have NaN)."""
     rng = np.random.default_rng(8)
     probs, host, dev = [], [], []
     shapes = [("d", 300, 200, 1500), ("d", 129, 257, 2100), ("s", 260, 140, 1800),
@@ -189,6 +201,10 @@ def test_grouped_split_graph_long_k(orc):
         dt = np.float64 if prec == "d" else np.float32
         A = orc.storage(m, k, m, dt, 800 + i, 0)
         B = orc.storage(n, k, n, dt, 800 + i, 1)
+        if i == 0:
+            A[3, 5] = np.inf     # a non-finite row of op(A): its row of C is NaN
+        if i == 2:
+            B[7, 2] = np.nan     # a non-finite column of op(B)
         C = orc.storage(m, n, m, dt, 800 + i, 2)
         dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
         probs.append(dict(precision=prec, transa="N", transb="T", m=m, n=n, k=k,
@@ -201,14 +217,9 @@ def test_grouped_split_graph_long_k(orc):
     assert graph.launch() == g.OK
     sync()
     grouped = [from_dev(d[2], h[2].shape[0]) for d, h in zip(dev, host)]
-    for p, (dA, dB, dC), h in zip(probs, dev, host):
-        dC.copy_(to_dev(h[2]))
-        args = (p["transa"], p["transb"], p["m"], p["n"], p["k"], p["alpha"], dA.data_ptr(),
-                p["lda"], dB.data_ptr(), p["ldb"], p["beta"], dC.data_ptr(), p["ldc"])
-        rc = g.dgemm_ozaki2(*args) if p["precision"] == "d" else g.sgemm_bf16x(*args, products=6)
-        assert rc == g.OK
-    sync()
-    for i, ((dA, dB, dC), h) in enumerate(zip(dev, host)):
-        assert np.array_equal(grouped[i], from_dev(dC, h[2].shape[0])), i
+    single = per_problem_split_calls(probs, dev, [h[2] for h in host])
+    for i in range(len(probs)):
+        assert np.array_equal(grouped[i], single[i], equal_nan=True), i
+    assert np.isnan(grouped[0][3, :]).all() and np.isnan(grouped[2][:, 7]).all()
     graph.destroy()
     assert g.device_error() == 0
