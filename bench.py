@@ -822,10 +822,16 @@ FP64_PEAK_TFLOPS = 1.05   # DFMA / DMMA m16n8k8, measured on GB300 by microbench
 FP32_PEAK_TFLOPS = 73.0   # FFMA, measured on GB300 by microbenchmark
 
 
+# name -> (problems, largest dimension); grouped_256 is a reduced batch for
+# multi-pass profiler captures (about 1 GB of workspaces against 13 GB)
+GROUPED_WORKLOADS = {"grouped_1024": (1024, 2048), "grouped_256": (256, 1024)}
+
+
 def run_grouped(args, torch, rank, world):
     """1024 independent GEMMs: m, n, k = round(exp(U[ln 16, ln 2048])), transa/transb
     N or T with p = 0.5, 60% FP64 / 40% FP32, alpha ~ U[0.5, 2], beta in {0, 1},
-    entries U[-1,1), ld = rows of the stored matrix (seed 4).  A step replays a
+    entries U[-1,1), ld = rows of the stored matrix (seed 4); grouped_256: 256
+    problems with dimensions up to 1024.  A step replays a
     captured CUDA graph: the split forms (per-problem operand preparation, one
     grouped GEMM launch per precision, per-problem FP64 reconstruction) for the
     headline, the plain forms (one persistent launch) for the comparison."""
@@ -836,11 +842,12 @@ def run_grouped(args, torch, rank, world):
     rng = np.random.default_rng(4)
     gen = torch.Generator(device="cuda")
     gen.manual_seed(4)
-    count = 1024
+    count, max_dim = GROUPED_WORKLOADS[args.workload]
     probs, bufs, flops = [], [], 0.0
     fl_d = fl_s = 0.0
     for i in range(count):
-        m, n, k = (int(round(math.exp(x))) for x in rng.uniform(math.log(16), math.log(2048), 3))
+        m, n, k = (int(round(math.exp(x)))
+                   for x in rng.uniform(math.log(16), math.log(max_dim), 3))
         ta = "N" if rng.random() < 0.5 else "T"
         tb = "N" if rng.random() < 0.5 else "T"
         prec = "d" if rng.random() < 0.6 else "s"
@@ -930,7 +937,8 @@ def run_grouped(args, torch, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(max_ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic (seeded uniform[-1,1), generated on the device)",
-        "config": {"workload": "grouped_1024", "problems": count, "fp64_share_of_flops":
+        "config": {"workload": args.workload, "problems": count, "max_dim": max_dim,
+                   "fp64_share_of_flops":
                    round(fl_d / flops, 4), "total_gflop": round(flops / 1e9, 3),
                    "form": "split (FP32: bf16x6, FP64: CRT with 16 moduli), CUDA graph: "
                            "operand preparation in branches, one grouped GEMM launch per "
@@ -1187,7 +1195,7 @@ def cpu_baseline(w, cplx=False):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    if args.workload == "grouped_1024":
+    if args.workload in GROUPED_WORKLOADS:
         print(json.dumps({"impl": "reference", "metric": METRIC,
                           "unavailable": "the reference has no grouped interface"}))
         return
@@ -1244,7 +1252,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(CWORKLOADS) +
-                    sorted(TRSM_WORKLOADS) + ["grouped_1024"],
+                    sorted(TRSM_WORKLOADS) + sorted(GROUPED_WORKLOADS),
                     default="sgemm_tn_8192")
     ap.add_argument("--phi", type=float, default=None,
                     help="exponent spread of A and B: (u-0.5)*exp(phi*g) (DGEMM NT 16384 sweep)")
@@ -1269,7 +1277,7 @@ def main():
     if world > 1:
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
-    if args.workload == "grouped_1024":
+    if args.workload in GROUPED_WORKLOADS:
         run_grouped(args, torch, rank, world)
     elif args.workload in TRSM_WORKLOADS:
         run_trsm(args, torch, rank, world)
