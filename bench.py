@@ -925,6 +925,21 @@ def run_grouped(args, torch, rank, world):
     barrier(torch, world)
     ms_split = timed(gs, args.steps, args.warmup)
     ms_plain = timed(gp, max(3, args.steps // 2), args.warmup)
+    # per form: each precision's problems alone as a split-form graph
+    # (tensor pipe work: 16 residue GEMMs per FP64 product, 6 BF16 products per FP32 one)
+    per_form = {}
+    pk = peaks()
+    for tag, prec, fl, P in (("fp64_crt16", "d", fl_d, 16), ("fp32_bf16x6", "s", fl_s, 6)):
+        sub = [p for p in probs if p["precision"] == prec]
+        if not sub or fl == 0.0:
+            continue
+        gf = g.GroupedGraph(sub, form=1)
+        ms = timed(gf, max(3, args.steps // 2), args.warmup)
+        gf.destroy()
+        per_form[tag] = {"problems": len(sub), "ms": round(ms, 4),
+                         "tflops": round(fl / (ms / 1e3) / 1e12, 3),
+                         "tensor_pipe_frac": round(P * fl / (ms / 1e3) / 1e12 / pk["bf16_tflops"], 4),
+                         "peak": pk["bf16_tflops"], "peak_source": "%s bf16 burst" % pk["source"]}
     barrier(torch, world)
     clocks = sampler.stop() if sampler else None
     max_ms = allreduce_max(torch, world, ms_split)
@@ -954,6 +969,7 @@ def run_grouped(args, torch, rank, world):
                      "unit": "TFLOP/s", "frac": round(t_lb / (ms_plain / 1e3), 4),
                      "traffic": None,
                      "peak_source": "FP64 1.05 and FP32 73 TFLOP/s measured by microbenchmark"},
+        "per_form": per_form,
         "accuracy": {"plain": err_plain, "split": err_split, "samples": "8 entries x 48 problems"},
         "clocks": clocks,
         "gpu_launches": args.steps * kernels_split,
