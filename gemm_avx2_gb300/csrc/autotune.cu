@@ -367,38 +367,40 @@ int autotune(int kind, char ta, char tb, int m, int n, int k, const void *A, int
     }
     if (!found) best.param = 12;
   }
-  // the output tile width: the results are the same bit for bit, so only
-  // the time decides (the caller's own override is restored afterwards)
-  {
-    const int user_tile = split_tile_override();
-    double t128 = 0, t256 = 0;
-    set_split_tile_n(128);
-    rc = timed(best.param, best.chunk, &t128);
-    if (rc == GB300_OK) {
-      set_split_tile_n(256);
-      rc = timed(best.param, best.chunk, &t256);
+  // The output tile width, then the tensor-core GEMM's cluster mode at that
+  // width: the results are the same bit for bit, so only the time decides.
+  // The two candidates are timed alternately over kLayoutRounds rounds and
+  // compared by their fastest round, so that a clock or power-cap transient
+  // during one timing does not decide (the caller's own overrides are
+  // restored afterwards).
+  constexpr int kLayoutRounds = 3;
+  auto faster_of = [&](auto set, int a, int b, int *pick, double *ms) -> int {
+    double ta = 1e30, tb = 1e30;
+    for (int r = 0; r < kLayoutRounds; ++r) {
+      double t = 0;
+      set(a);
+      int e = timed(best.param, best.chunk, &t);
+      if (e != GB300_OK) return e;
+      ta = t < ta ? t : ta;
+      set(b);
+      e = timed(best.param, best.chunk, &t);
+      if (e != GB300_OK) return e;
+      tb = t < tb ? t : tb;
     }
-    set_split_tile_n(user_tile);
-    if (rc != GB300_OK) return rc;
-    best.tile = t128 < t256 ? 128 : 256;
-    best.ms = t128 < t256 ? t128 : t256;
-  }
-  // the tensor-core GEMM's cluster mode at that width (same results bit for bit)
+    *pick = ta <= tb ? a : b;
+    *ms = ta <= tb ? ta : tb;
+    return GB300_OK;
+  };
   {
     const int user_tile = split_tile_override(), user_pair = pair_mma_override();
-    double tp = 0, tm = 0;
-    set_split_tile_n(best.tile);
-    set_pair_mma(1);
-    rc = timed(best.param, best.chunk, &tp);
+    rc = faster_of([](int v) { set_split_tile_n(v); }, 256, 128, &best.tile, &best.ms);
     if (rc == GB300_OK) {
-      set_pair_mma(2);
-      rc = timed(best.param, best.chunk, &tm);
+      set_split_tile_n(best.tile);
+      rc = faster_of([](int v) { set_pair_mma(v); }, 1, 2, &best.pair, &best.ms);
     }
     set_pair_mma(user_pair);
     set_split_tile_n(user_tile);
     if (rc != GB300_OK) return rc;
-    best.pair = tp < tm ? 1 : 2;
-    best.ms = tp < tm ? tp : tm;
   }
   best.plain_max = plain.max_rel;
   best.plain_fro = plain.fro;
