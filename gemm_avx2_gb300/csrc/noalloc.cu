@@ -23,8 +23,9 @@
 
 namespace gb300 {
 
-// 32 MiB: enough for the 3xBF16 form up to about m = n = k = 1400 and the
-// 6xBF16 form up to about 1000 (see gb300_split_workspace_bytes).
+// 32 MiB: enough for the 3xBF16 and scaled FP16 forms up to about
+// m = n = k = 1980 and the 6xBF16 form up to about 1600 (see
+// gb300_split_workspace_bytes).
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];

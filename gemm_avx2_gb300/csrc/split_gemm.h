@@ -20,7 +20,10 @@ constexpr int kCrtMaxModuli = 24;  // moduli of the CRT (modular-integer) FP64 f
 // hi + lo terms, products hi*hi + (hi*lo + lo*hi) * 2^-11.
 constexpr int kFp16x3 = 0x103;
 inline bool split_products_ok(int p) { return p == 3 || p == 6 || p == kFp16x3; }
+// Segments of the product stream (6xBF16: 6; 3xBF16 and the scaled FP16 form:
+// 3) and distinct terms stored per operand (3 and 2).
 inline int split_segments(int p) { return p == 6 ? 6 : 3; }
+inline int split_terms(int p) { return p == 6 ? 3 : 2; }
 
 size_t split_workspace_bytes(int kind, int m, int n, int k, int param);
 

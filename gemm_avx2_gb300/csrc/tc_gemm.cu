@@ -65,7 +65,8 @@ __device__ __forceinline__ void bf16_terms(float x, int nterms, __nv_bfloat16 (&
   }
 }
 
-// Segment s of the concatenated operand holds term seg_term[s] of x.
+// The product stream of the split GEMM: segment s multiplies term term[s] of
+// op(A) with term term[s] of op(B) (each operand's map), over K.
 struct SegMap {
   int nseg;
   int term[6];
@@ -89,7 +90,6 @@ __device__ __forceinline__ void f16_terms(float x, int s, unsigned short &hi, un
 struct SplitArgs {
   const float *X0, *X1;
   int ld0, ld1, R0, R1, kc0, kc1, Rp0, Rp1;
-  SegMap seg0, seg1;
   const int *ex0, *ex1;
   __nv_bfloat16 *out0, *out1;
   int K, Kp, nterms;
@@ -97,7 +97,8 @@ struct SplitArgs {
   int zbase;  // operand of blockIdx.z = 0 (1: a launch over op(B) alone)
 };
 
-// out: Rp x (nseg * Kp) row-major 16-bit terms (row stride ldo = nseg*Kp
+// out: Rp x (nterms * Kp) row-major 16-bit terms, term t in columns
+// [t Kp, (t + 1) Kp) (row stride ldo = nterms * Kp
 // elements); grid.y strides over the Rp / 32 row blocks (CTAs past the
 // smaller operand's rows do nothing).  Each thread writes 8 consecutive k of
 // one row (16 bytes) per segment.
@@ -110,7 +111,6 @@ __global__ void __launch_bounds__(256) split_bf16_kernel(const __grid_constant__
   const float *__restrict__ X = z ? p.X1 : p.X0;
   const int ld = z ? p.ld1 : p.ld0, R = z ? p.R1 : p.R0, kcontig = z ? p.kc1 : p.kc0;
   const int Rp = z ? p.Rp1 : p.Rp0, K = p.K, Kp = p.Kp, nterms = p.nterms;
-  const SegMap &seg = z ? p.seg1 : p.seg0;
   const int *__restrict__ ex = z ? p.ex1 : p.ex0;
   __nv_bfloat16 *__restrict__ out = z ? p.out1 : p.out0;
   const int64_t ldo = p.ldo;
@@ -153,13 +153,11 @@ __global__ void __launch_bounds__(256) split_bf16_kernel(const __grid_constant__
       }
     }
     __nv_bfloat16 *row = out + (int64_t)(r0 + r) * ldo + k0 + kq;
-    for (int sg = 0; sg < seg.nseg; ++sg) {
-      const int ti = seg.term[sg];
-      const uint4 v = ti == 0   ? make_uint4(w[0][0], w[0][1], w[0][2], w[0][3])
-                      : ti == 1 ? make_uint4(w[1][0], w[1][1], w[1][2], w[1][3])
-                                : make_uint4(w[2][0], w[2][1], w[2][2], w[2][3]);
-      *reinterpret_cast<uint4 *>(row + (int64_t)sg * Kp) = v;
-    }
+#pragma unroll
+    for (int t = 0; t < 3; ++t)
+      if (t < nterms)
+        *reinterpret_cast<uint4 *>(row + (int64_t)t * Kp) =
+            make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
     __syncthreads();  // the tile is refilled for the next row block
   }
 }
@@ -168,12 +166,11 @@ __global__ void __launch_bounds__(256) split_bf16_kernel(const __grid_constant__
 // when A is transposed, columns of op(B) when B is not): one CTA per row, the
 // row held in registers (VPT values a thread, Kp <= 256 VPT) between the
 // block-wide max and the split, so it is read from memory once.  Writes the
-// row's exponent and its segments exactly as row_absmax_kernel followed by
+// row's exponent and its terms exactly as row_absmax_kernel followed by
 // split_bf16_kernel<true> do (columns [K, Kp) and rows [R, Rp) as zeros).
 struct RowSplitArgs {
   const float *X0, *X1;  // first row of each operand (part)
   int ld0, ld1, R0, R1, Rp0, Rp1;
-  SegMap seg0, seg1;
   int *ex0, *ex1;
   __nv_bfloat16 *out0, *out1;
   int K, Kp;
@@ -209,7 +206,6 @@ __global__ void __launch_bounds__(256) f16_row_split_kernel(const __grid_constan
   const float *__restrict__ X0 = z ? p.X1 : p.X0;
   int *__restrict__ exo = z ? p.ex1 : p.ex0;
   __nv_bfloat16 *__restrict__ out0 = z ? p.out1 : p.out0;
-  const SegMap &seg = z ? p.seg1 : p.seg0;
   const int K = p.K, Kp = p.Kp, t = threadIdx.x;
   const bool vec = p.vec != 0;
   __shared__ unsigned wmax[2][8];  // by row parity: a fast warp may start the next row
@@ -242,9 +238,9 @@ __global__ void __launch_bounds__(256) f16_row_split_kernel(const __grid_constan
     for (int j = 0; j < VPT / 4; ++j) {
       const int e0 = 1024 * j + 4 * t;
       if (e0 >= Kp) continue;  // Kp is a multiple of 64: e0 < Kp covers e0 + 3
-      uint2 w0, w1, w2;  // hi, lo and the zero term of the 4 values
+      uint2 w0, w1;  // hi and lo of the 4 values
       if (bad) {
-        w0 = w1 = w2 = make_uint2(0x7e007e00u, 0x7e007e00u);
+        w0 = w1 = make_uint2(0x7e007e00u, 0x7e007e00u);
       } else {
         unsigned short h[4], l[4];
 #pragma unroll
@@ -253,13 +249,9 @@ __global__ void __launch_bounds__(256) f16_row_split_kernel(const __grid_constan
                         (unsigned)h[2] | ((unsigned)h[3] << 16));
         w1 = make_uint2((unsigned)l[0] | ((unsigned)l[1] << 16),
                         (unsigned)l[2] | ((unsigned)l[3] << 16));
-        w2 = make_uint2(0u, 0u);
       }
-#pragma unroll
-      for (int sg = 0; sg < 3; ++sg) {  // the scaled FP16 form has 3 segments
-        const int ti = seg.term[sg];
-        *reinterpret_cast<uint2 *>(out + (int64_t)sg * Kp + e0) = ti == 0 ? w0 : ti == 1 ? w1 : w2;
-      }
+      *reinterpret_cast<uint2 *>(out + e0) = w0;                   // term 0: hi
+      *reinterpret_cast<uint2 *>(out + (int64_t)Kp + e0) = w1;     // term 1: lo
     }
 #pragma unroll
     for (int i = 0; i < VPT; ++i) v[i] = nv[i];
@@ -471,6 +463,11 @@ __global__ void __launch_bounds__(256) ozaki_slice_kernel(const __grid_constant_
 // ===========================================================================
 struct Bf16xParams {
   int m, n, tiles_m, tiles_n, kblocks;
+  // K' = nseg segments of skb 64-wide blocks; segment s reads the term block
+  // (segA >> 4 s) & 15 of A' and (segB >> 4 s) & 15 of B' (each term stored
+  // once, term t at columns [t Kp, (t + 1) Kp))
+  int skb;
+  unsigned segA, segB;
   // K' is cut into runs of consecutive segments whose products have the same
   // order (i + j): run r ends at block run_end<r> and is accumulated in TMEM
   // chunks of run_chunk<r> blocks (0 = the whole run).  Scalars, not arrays,
@@ -656,9 +653,16 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const int pi = prob_of(u);
         const int kblocks = prm(pi)->kblocks;
         const void *mA = map_a(pi), *mB = map_b(pi);
+        const Bf16xParams &q = *prm(pi);
+        const int skb = q.skb;
+        const unsigned segA = q.segA, segB = q.segB;
         int tm, tn;
         unit_tile(u, pi, tm, tn);
-        for (int kb = 0; kb < kblocks; ++kb, ++L) {
+        int sg = 0, kk = 0;  // segment of block kb and the block within it
+        for (int kb = 0; kb < kblocks; ++kb, ++L, ++kk) {
+          if (kk == skb) { ++sg; kk = 0; }
+          const int xa = (int)(((segA >> (4 * sg)) & 15u) * skb + kk) * kSplitBK;
+          const int xb = (int)(((segB >> (4 * sg)) & 15u) * skb + kk) * kSplitBK;
           const int s = L % kBxStages;
           const uint32_t r = L / kBxStages;
           if (!mbar_wait(&empty[s], (r & 1) ^ 1, p.err, kErrTimeoutEmpty, abort_flag)) break;
@@ -667,14 +671,13 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             // both CTAs' A rows and B halves land on the even CTA's full barrier
             if (rank == 0) mbar_arrive_expect_tx(&full[s], 2 * kBxStage);
             const uint32_t fb = cluster_addr(&full[s], 0);
-            tma_load_2d_pair(sa, mA, kb * kSplitBK, tm * kSplitBM, fb);
-            tma_load_2d_pair(sa + kBxABytes, mB, kb * kSplitBK, tn * BN + (int)rank * (BN / 2),
-                             fb);
+            tma_load_2d_pair(sa, mA, xa, tm * kSplitBM, fb);
+            tma_load_2d_pair(sa + kBxABytes, mB, xb, tn * BN + (int)rank * (BN / 2), fb);
             continue;
           }
           mbar_arrive_expect_tx(&full[s], kBxStage);  // own A and B tiles
-          tma_load_2d(sa, mA, kb * kSplitBK, tm * kSplitBM, &full[s]);
-          tma_load_2d(sa + kBxABytes, mB, kb * kSplitBK, tn * BN, &full[s]);
+          tma_load_2d(sa, mA, xa, tm * kSplitBM, &full[s]);
+          tma_load_2d(sa + kBxABytes, mB, xb, tn * BN, &full[s]);
         }
       }
     }
@@ -1370,7 +1373,7 @@ size_t split_workspace_bytes(int kind, int m, int n, int k, int param) {
     const int64_t Mp = round_up(m, kSplitBM), Np = round_up(n, kBf16xBN);
     // scaled FP16 form: + the max |.| bit patterns and exponents of rows / columns
     const int64_t scales = param == kFp16x3 ? (Mp + Np) * 8 + 512 : 0;
-    return (size_t)((Mp + Np) * split_segments(param) * Kp * 2 + 1024 + scales);
+    return (size_t)((Mp + Np) * split_terms(param) * Kp * 2 + 1024 + scales);
   }
   int S = param > 0 ? param : ozaki_default_slices(m, n, k);
   if (S < 2 || S > kOzakiMaxSlices) return 0;
@@ -1489,7 +1492,7 @@ struct Bf16xLayout {
 static Bf16xLayout bf16x_layout(int m, int n, int k, int products, void *ws) {
   Bf16xLayout L;
   L.Kp = round_up(k, kSplitBK);
-  L.Kld = L.Kp * split_segments(products);
+  L.Kld = L.Kp * split_terms(products);  // each term once
   L.Mp = round_up(m, kSplitBM);
   L.Np = round_up(n, kBf16xBN);
   L.Ap = reinterpret_cast<__nv_bfloat16 *>((reinterpret_cast<uintptr_t>(ws) + 1023) &
@@ -1521,8 +1524,6 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
   SplitArgs sa;
   sa.X0 = A; sa.ld0 = lda; sa.R0 = m; sa.kc0 = an ? 0 : 1; sa.Rp0 = (int)L.Mp;
   sa.X1 = B; sa.ld1 = ldb; sa.R1 = n; sa.kc1 = bn ? 1 : 0; sa.Rp1 = (int)L.Np;
-  sa.seg0 = seg_map(f16 ? 3 : products, true);
-  sa.seg1 = seg_map(f16 ? 3 : products, false);
   sa.ex0 = f16 ? L.ex : nullptr;
   sa.ex1 = f16 ? L.ex + L.Mp : nullptr;
   sa.out0 = L.Ap; sa.out1 = L.Bp;
@@ -1537,7 +1538,6 @@ int split_sgemm_prepare(char ta, char tb, int m, int n, int k, const float *A, i
     RowSplitArgs ra;
     ra.X0 = A; ra.X1 = B; ra.ld0 = lda; ra.ld1 = ldb; ra.R0 = m; ra.R1 = n;
     ra.Rp0 = (int)L.Mp; ra.Rp1 = (int)L.Np;
-    ra.seg0 = sa.seg0; ra.seg1 = sa.seg1;
     ra.ex0 = L.ex; ra.ex1 = L.ex + L.Mp; ra.out0 = L.Ap; ra.out1 = L.Bp;
     ra.K = k; ra.Kp = (int)L.Kp; ra.ldo = L.Kld;
     ra.vec = (reinterpret_cast<uintptr_t>(A) % 16 == 0 && lda % 4 == 0 || !fz[0]) &&
@@ -1590,8 +1590,6 @@ int split_sgemm_prepare_part(int z, char t, int m, int n, int k, const float *X,
   SplitArgs sa;
   sa.X0 = sa.X1 = Xp; sa.ld0 = sa.ld1 = ldx; sa.R0 = sa.R1 = rows;
   sa.kc0 = sa.kc1 = kc ? 1 : 0; sa.Rp0 = sa.Rp1 = Rpart;
-  sa.seg0 = seg_map(f16 ? 3 : products, true);
-  sa.seg1 = seg_map(f16 ? 3 : products, false);
   int *ex = f16 ? L.ex + (z ? L.Mp : 0) + r0 : nullptr;
   sa.ex0 = sa.ex1 = ex;
   __nv_bfloat16 *out = (z ? L.Bp : L.Ap) + (int64_t)r0 * L.Kld;
@@ -1604,7 +1602,6 @@ int split_sgemm_prepare_part(int z, char t, int m, int n, int k, const float *X,
   if (vpt) {  // k-contiguous rows: the fused max pass and split
     RowSplitArgs ra;
     ra.X0 = ra.X1 = Xp; ra.ld0 = ra.ld1 = ldx; ra.R0 = ra.R1 = rows; ra.Rp0 = ra.Rp1 = Rpart;
-    ra.seg0 = sa.seg0; ra.seg1 = sa.seg1;
     ra.ex0 = ra.ex1 = ex; ra.out0 = ra.out1 = out;
     ra.K = k; ra.Kp = (int)L.Kp; ra.ldo = L.Kld; ra.zbase = z;
     ra.vec = reinterpret_cast<uintptr_t>(Xp) % 16 == 0 && ldx % 4 == 0;
@@ -1740,8 +1737,18 @@ static int bf16x_block_setup(int m, int n, int k, int i0, int h, int j0, int w, 
   p.m = h; p.n = w;
   p.tiles_m = (int)(L.Mp / kSplitBM);
   p.tiles_n = 0;  // set by the launch for its tile width
-  p.kblocks = (int)(L.Kld / kSplitBK);
   const int skb = (int)(L.Kp / kSplitBK);  // K blocks of one segment
+  p.kblocks = split_segments(products) * skb;
+  p.skb = skb;
+  {
+    const SegMap sa = seg_map(products == kFp16x3 ? 3 : products, true),
+                 sb = seg_map(products == kFp16x3 ? 3 : products, false);
+    p.segA = p.segB = 0u;
+    for (int sg = 0; sg < sa.nseg; ++sg) {
+      p.segA |= (unsigned)sa.term[sg] << (4 * sg);
+      p.segB |= (unsigned)sb.term[sg] << (4 * sg);
+    }
+  }
   {
     // segments by order (i + j) of their cross product, see seg_map():
     // P = 6: 2 2 2 1 1 0; P = 3 and the scaled FP16 form: 1 1 0.  Segments

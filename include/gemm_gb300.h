@@ -138,7 +138,7 @@ int gb300_dgemm_ozaki_ws(char transa, char transb, int m, int n, int k, double a
  * the library holds it until exit); the call allocates and frees nothing.
  *   - Problems whose scratch (gb300_split_workspace_bytes(0, m, n, k,
  *     products)) exceeds 32 MiB are rejected with GB300_ERR_NOALLOC_LIMIT
- *     (3xBF16: up to about m = n = k = 1400; 6xBF16: about 1000).
+ *     (3xBF16 and FP16X3: up to about m = n = k = 1980; 6xBF16: about 1600).
  *   - The first call on a device looks up the array's device address (set-up,
  *     once per device); make that first call before any stream capture.
  *   - Every call uses the same array: calls whose execution overlaps on the

@@ -52,7 +52,8 @@ def bf16_terms(x: np.ndarray, nterms: int):
     return terms
 
 
-# segment -> term index, for the A and B operands (smallest products first)
+# The GEMM's product stream: segment s multiplies term SEGMENTS[P][0][s] of A'
+# with term SEGMENTS[P][1][s] of B' (smallest products first).
 SEGMENTS = {
     3: ([1, 0, 0], [0, 1, 0]),
     6: ([2, 1, 0, 1, 0, 0], [0, 1, 2, 0, 1, 0]),
@@ -60,12 +61,13 @@ SEGMENTS = {
 
 
 def bf16x_operand(X: np.ndarray, products: int, is_a: bool) -> np.ndarray:
-    """The concatenated K-major operand (R x P*K, float32 holding BF16) of an
-    R x K op(X) view."""
+    """The K-major split operand of an R x K op(X) view (R x T*K, float32
+    holding BF16): its T terms once each, [hi | lo] for P = 3 and
+    [hi | mid | lo] for P = 6, the same for A and B (is_a: kept for the
+    callers; the GEMM pairs the terms by SEGMENTS)."""
     nterms = 2 if products == 3 else 3
     terms = bf16_terms(np.asarray(X, np.float32), nterms)
-    seg = SEGMENTS[products][0 if is_a else 1]
-    return np.concatenate([terms[t] for t in seg], axis=1)
+    return np.concatenate(terms[:nterms], axis=1)
 
 
 def row_exponents(X: np.ndarray) -> np.ndarray:
@@ -140,14 +142,13 @@ def fp16x3_terms(X: np.ndarray):
 
 
 def fp16x3_operand(X: np.ndarray, is_a: bool) -> np.ndarray:
-    """The concatenated K-major operand (R x 3K, FP16 bit patterns as uint16):
-    A = [lo | hi | hi], B = [hi | lo | hi] (products lo*hi, hi*lo, hi*hi)."""
+    """The K-major split operand (R x 2K, FP16 bit patterns as uint16):
+    [hi | lo] for A and B alike (the GEMM's segments pair them as lo*hi,
+    hi*lo, hi*hi by SEGMENTS[3])."""
     hi, lo, _ = fp16x3_terms(X)
-    t = [hi, lo]
-    seg = SEGMENTS[3][0 if is_a else 1]
-    out = np.concatenate([t[i] for i in seg], axis=1).astype(np.float16).view(np.uint16)
-    out = out.copy()
-    out[np.isnan(np.concatenate([t[i] for i in seg], axis=1))] = 0x7E00
+    t = np.concatenate([hi, lo], axis=1)
+    out = t.astype(np.float16).view(np.uint16).copy()
+    out[np.isnan(t)] = 0x7E00
     return out
 
 

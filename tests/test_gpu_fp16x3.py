@@ -35,12 +35,13 @@ def run(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc=None):
 
 
 def workspace_parts(ws, m, n, k):
-    """A' (Mp x 3Kp), B' (Np x 3Kp) as uint16, then the exponents (Mp + Np)."""
+    """A' (Mp x 2Kp), B' (Np x 2Kp) as uint16 (terms hi, lo), then the
+    exponents (Mp + Np)."""
     Kp, Mp, Np = ru(k, 64), ru(m, 128), ru(n, 256)
     raw = ws.cpu().numpy()
     base = ws.data_ptr()
     off = (-base) % 1024
-    kld = 3 * Kp
+    kld = 2 * Kp
     h = raw[off:off + 2 * (Mp + Np) * kld].view(np.uint16)
     Ap, Bp = h[:Mp * kld].reshape(Mp, kld), h[Mp * kld:].reshape(Np, kld)
     end = base + off + 2 * (Mp + Np) * kld

@@ -50,12 +50,13 @@ def test_bf16x_split_bitexact_and_result(orc, products, ta, tb, tile_n):
                        workspace_bytes=need)
     assert rc == g.OK
     sync()
-    # workspace: A' (Mp x P*Kp) then B' (Np x P*Kp), BF16, from the first 1024-aligned byte
+    # workspace: A' (Mp x T*Kp) then B' (Np x T*Kp), BF16 terms (T = 2 for P = 3,
+    # 3 for P = 6), from the first 1024-aligned byte
     Kp = ru(k, 64)
     Mp, Np = ru(m, 128), ru(n, 256)
     off = aligned_view(ws, need)
     raw = ws.cpu().numpy()[off:]
-    kld = products * Kp
+    kld = (2 if products == 3 else 3) * Kp
     bf = raw[:2 * (Mp + Np) * kld].view(np.uint16).astype(np.uint32) << 16
     vals = bf.view(np.float32)
     Ap = vals[:Mp * kld].reshape(Mp, kld)
