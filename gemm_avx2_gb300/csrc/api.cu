@@ -59,6 +59,24 @@ bool encode_2d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t ro
   return r == CUDA_SUCCESS;
 }
 
+bool encode_3d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t d0, int64_t d1,
+               int64_t d2, int64_t ld1, int64_t ld2, int box0, int box1) {
+  EncodeTiledFn fn = get_encode();
+  if (!fn || d0 <= 0 || d1 <= 0 || d2 <= 0) return false;
+  CUtensorMapDataType dt = elem_bytes == 8   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                           : elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                             : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
+  cuuint64_t strides[2] = {(cuuint64_t)(ld1 * (int64_t)elem_bytes),
+                           (cuuint64_t)(ld2 * (int64_t)elem_bytes)};
+  cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, dt, 3, const_cast<void *>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 // ---------------------------------------------------------------- per-device state
 struct DeviceState {
   unsigned *err = nullptr;  // device error word

@@ -141,6 +141,24 @@ __device__ __forceinline__ void tma_load_2d_pair(void *smem_dst, const void *tma
       "l"(tmap), "r"(x), "r"(y), "r"(bar_cluster)
       : "memory");
 }
+// 3-D tiled load: box at (x, y, z) -> smem.  Coordinates past the tensor's
+// extents read as zeros (no memory is touched there).
+__device__ __forceinline__ void tma_load_3d(void *smem_dst, const void *tmap, int32_t x, int32_t y,
+                                            int32_t z, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, "
+      "{%2, %3, %4}], [%5];" ::"r"(smem_u32(smem_dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d_pair(void *smem_dst, const void *tmap, int32_t x,
+                                                 int32_t y, int32_t z, uint32_t bar_cluster) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(smem_dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(bar_cluster)
+      : "memory");
+}
 // Shared::cluster address of `p` (this CTA's shared memory) as seen in CTA `rank`.
 __device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
   uint32_t a;

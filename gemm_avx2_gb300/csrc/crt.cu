@@ -123,7 +123,9 @@ __global__ void __launch_bounds__(256, 3)
   const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
   const int64_t plane = z ? op.plane1 : op.plane0;
   const int64_t step = (plane ? plane : (int64_t)Rp * Kp) / 8;  // one residue block, in uint4
-  for (int r0 = blockIdx.y * 32; r0 < Rp; r0 += gridDim.y * 32) {
+  // rows past R are never read (the GEMM's maps end at the problem's rows),
+  // so only row blocks holding data are written
+  for (int r0 = blockIdx.y * 32; r0 < R; r0 += gridDim.y * 32) {
     load_tile_32x64<double>(X, ld, R, K, kcontig != 0, r0, k0, tile);
     __syncthreads();
     const int gr = r0 + r;
@@ -618,6 +620,7 @@ int crt_block_args(int m, int n, int k, int i0, int h, int j0, int w, double alp
   // the block's residues: plane g, column j0 + j, row i0 + i in the word
   // g Mp Np / 4 + ((j0 + j) / 4) Mp + i0 + i (j0 is a multiple of 256)
   a.m = h; a.n = w; a.k = k; a.S = N; a.mode = 1;
+  a.m_all = m; a.n_all = n;
   a.Mp = L.Mp; a.Np = L.Np; a.Kp = L.Kp;
   a.As = L.As; a.Bs = L.Bs;
   a.row0 = i0; a.col0 = j0;

@@ -52,6 +52,10 @@ struct OzakiGemmArgs {
   // column of op(B) in the operand blocks (Mp, Np: the whole problem's; m, n:
   // the block's; rres, expA, expB point at the block's first entries)
   int row0 = 0, col0 = 0;
+  // the whole problem's m and n: the operand blocks' rows that hold data (the
+  // GEMM reads them through 3-D maps of k x m_all (n_all) x S, so rows past
+  // them and K past k read as zeros whatever the workspace holds there)
+  int m_all = 0, n_all = 0;
 };
 int ozaki_gemm_launch(const OzakiGemmArgs &a, cudaStream_t st, unsigned *err);
 // Per-row max |.| of op(A) and per-column max of op(B) and their scale

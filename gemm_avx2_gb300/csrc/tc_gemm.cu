@@ -1047,20 +1047,20 @@ ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               break;
             }
             uint8_t *sa_ptr = smem + s * kOzStage;
-            const int arow = (sa - 1) * q.Mp + q.row0 + tm * kSplitBM;
+            const int arow = q.row0 + tm * kSplitBM;  // in block sa - 1 of A
             if (PAIR) {
               // both CTAs' A rows and B halves land on the even CTA's full barrier
               if (rank == 0) mbar_arrive_expect_tx(&full[s], 2 * kOzStage);
               const uint32_t fb = cluster_addr(&full[s], 0);
-              tma_load_2d_pair(sa_ptr, mA, kb * kSplitBK, arow, fb);
-              tma_load_2d_pair(sa_ptr + kOzABytes, mB, kb * kSplitBK,
-                               (sb - 1) * q.Np + q.col0 + tn * BN + (int)rank * (BN / 2), fb);
+              tma_load_3d_pair(sa_ptr, mA, kb * kSplitBK, arow, sa - 1, fb);
+              tma_load_3d_pair(sa_ptr + kOzABytes, mB, kb * kSplitBK,
+                               q.col0 + tn * BN + (int)rank * (BN / 2), sb - 1, fb);
               continue;
             }
             mbar_arrive_expect_tx(&full[s], kOzStage);
-            tma_load_2d(sa_ptr, mA, kb * kSplitBK, arow, &full[s]);
-            tma_load_2d(sa_ptr + kOzABytes, mB, kb * kSplitBK,
-                        (sb - 1) * q.Np + q.col0 + tn * BN, &full[s]);
+            tma_load_3d(sa_ptr, mA, kb * kSplitBK, arow, sa - 1, &full[s]);
+            tma_load_3d(sa_ptr + kOzABytes, mB, kb * kSplitBK, q.col0 + tn * BN, sb - 1,
+                        &full[s]);
           }
         }
       }
@@ -1956,6 +1956,7 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
   const OzakiLayout L = ozaki_layout(m, n, k, S, const_cast<void *>(ws));
   OzakiGemmArgs a;
   a.m = m; a.n = n; a.k = k; a.S = S; a.mode = 0;
+  a.m_all = m; a.n_all = n;
   a.Mp = L.Mp; a.Np = L.Np; a.Kp = L.Kp;
   a.As = L.As; a.Bs = L.Bs;
   a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc;
@@ -1963,14 +1964,21 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
   return ozaki_gemm_launch(a, st, err);
 }
 
+// The slice / residue GEMM's operand maps: S blocks of Mp (Np) rows x Kp, of
+// which rows [0, m_all) ([0, n_all)) and K [0, k) hold data; everything past
+// them reads as zeros, so the padding is never read from memory.
+static bool ozaki_maps(const OzakiGemmArgs &a, CUtensorMap *tA, CUtensorMap *tB, int box_b) {
+  const int64_t ma = a.m_all > 0 ? a.m_all : a.Mp, na = a.n_all > 0 ? a.n_all : a.Np;
+  return encode_3d(tA, a.As, 2, a.k, ma, a.S, a.Kp, a.Mp * a.Kp, kSplitBK, kSplitBM) &&
+         encode_3d(tB, a.Bs, 2, a.k, na, a.S, a.Kp, a.Np * a.Kp, kSplitBK, box_b);
+}
+
 template <int BN>
 static int ozaki_launch_bn(const OzakiGemmArgs &a, OzakiParams p, cudaStream_t st) {
   // pair MMAs on row-tile pairs (2-CTA clusters) when there are two or more row tiles
   const bool pair = p.tiles_m >= 2 && use_pair_mma(a.mode ? 2 : 1, a.m, a.n, a.k);
   CUtensorMap tA{}, tB{};
-  if (!encode_2d(&tA, a.As, 2, a.Kp, a.S * a.Mp, a.Kp, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&tB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, pair ? BN / 2 : BN, true))
-    return GB300_ERR_CUDA;
+  if (!ozaki_maps(a, &tA, &tB, pair ? BN / 2 : BN)) return GB300_ERR_CUDA;
   p.tiles_n = (p.n + BN - 1) / BN;
   // CRT form: one modulus per work unit when the tiles alone fill fewer than
   // four waves (a 2048^2 output has 128 tiles for 152 SMs)
@@ -2023,9 +2031,7 @@ int ozaki_group_entry(const OzakiGemmArgs &a, unsigned *err, int unit0, void *en
   GOzProblem e;
   std::memset(&e, 0, sizeof(e));
   ozaki_params(a, err, e.prm);
-  if (!encode_2d(&e.tmA, a.As, 2, a.Kp, a.S * a.Mp, a.Kp, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&e.tmB, a.Bs, 2, a.Kp, a.S * a.Np, a.Kp, kSplitBK, kGroupBN, true))
-    return GB300_ERR_CUDA;
+  if (!ozaki_maps(a, &e.tmA, &e.tmB, kGroupBN)) return GB300_ERR_CUDA;
   e.prm.tiles_n = (a.n + kGroupBN - 1) / kGroupBN;
   e.prm.gsplit = 1;
   e.unit0 = unit0;

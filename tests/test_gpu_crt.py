@@ -18,9 +18,12 @@ def ru(x, a):
 
 
 def run_crt(ta, tb, m, n, k, A, lda, B, ldb, C, N, alpha=1.0, beta=0.0):
+    """The CRT call on a workspace filled with 0xFF bytes (BF16 NaN): the
+    padding rows and K columns of the residue blocks are never written, and
+    the GEMM must never read them."""
     torch = torch_cuda()
     need = g.split_workspace_bytes(2, m, n, k, N)
-    ws = torch.zeros(need, dtype=torch.uint8, device="cuda")
+    ws = torch.full((need,), 255, dtype=torch.uint8, device="cuda")
     dA, dB, dC = to_dev(A), to_dev(B), to_dev(C)
     rc = g.dgemm_ozaki2(ta, tb, m, n, k, alpha, dA.data_ptr(), lda, dB.data_ptr(), ldb, beta,
                         dC.data_ptr(), C.shape[0], moduli=N, workspace=ws.data_ptr(),
@@ -55,7 +58,6 @@ def test_residues_and_result_bitexact(orc, N, ta, tb, tile_n):
     for i in range(N):
         assert np.array_equal(As[i, :m, :k], ra[i]), i
         assert np.array_equal(Bs[i, :n, :k], rb[i]), i
-        assert not As[i, m:, :].any() and not As[i, :, k:].any()
     model = crt.crt_gemm_model(Aop, Bop, N, alpha=1.0, beta=0.5, C=C)
     assert np.array_equal(got, model), np.abs(got - model).max()
     assert g.device_error() == 0
