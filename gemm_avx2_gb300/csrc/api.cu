@@ -60,7 +60,7 @@ bool encode_2d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t ro
 }
 
 bool encode_3d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t d0, int64_t d1,
-               int64_t d2, int64_t ld1, int64_t ld2, int box0, int box1) {
+               int64_t d2, int64_t ld1, int64_t ld2, int box0, int box1, int box2) {
   EncodeTiledFn fn = get_encode();
   if (!fn || d0 <= 0 || d1 <= 0 || d2 <= 0) return false;
   CUtensorMapDataType dt = elem_bytes == 8   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
@@ -69,7 +69,7 @@ bool encode_3d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t d0
   cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
   cuuint64_t strides[2] = {(cuuint64_t)(ld1 * (int64_t)elem_bytes),
                            (cuuint64_t)(ld2 * (int64_t)elem_bytes)};
-  cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, 1};
+  cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, (cuuint32_t)box2};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(map, dt, 3, const_cast<void *>(base), dims, strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,

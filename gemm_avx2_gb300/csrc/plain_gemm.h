@@ -33,11 +33,11 @@ inline bool tma_ok(const void *p, int ld, size_t elem) {
   return (reinterpret_cast<uintptr_t>(p) % 16 == 0) && ((size_t)ld * elem) % 16 == 0;
 }
 
-// 3-D map of d2 blocks of d1 rows x d0 elements (row stride ld1, block
-// stride ld2, in elements), box box0 x box1 x 1, 128-byte swizzle; reads past
-// an extent return zeros.
+// 3-D map of d0 x d1 x d2 elements (d0 contiguous; strides ld1 and ld2 of
+// dimensions 1 and 2, in elements), box box0 x box1 x box2, 128-byte swizzle;
+// reads past an extent return zeros.
 bool encode_3d(CUtensorMap *map, const void *base, size_t elem_bytes, int64_t d0, int64_t d1,
-               int64_t d2, int64_t ld1, int64_t ld2, int box0, int box1);
+               int64_t d2, int64_t ld1, int64_t ld2, int box0, int box1, int box2);
 // Encode a 2-D tiled tensor map over a column-major matrix of rows x cols
 // (rows contiguous, leading dimension ld elements).  box = (box_rows, box_cols).
 // elem_bytes 2 -> BF16, 4 -> FP32, 8 -> FP64.  Returns false if the driver

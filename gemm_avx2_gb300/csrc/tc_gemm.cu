@@ -98,10 +98,10 @@ struct SplitArgs {
 };
 
 // out: Rp x (nterms * Kp) row-major 16-bit terms, term t in columns
-// [t Kp, (t + 1) Kp) (row stride ldo = nterms * Kp
-// elements); grid.y strides over the Rp / 32 row blocks (CTAs past the
-// smaller operand's rows do nothing).  Each thread writes 8 consecutive k of
-// one row (16 bytes) per segment.
+// [t Kp, (t + 1) Kp) (row stride ldo = nterms * Kp elements); grid.y strides
+// over the 32-row blocks that hold rows of op(X) (rows past R are left
+// unwritten: the GEMM's maps end there; columns [K, Kp) are written as
+// zeros).  Each thread writes 8 consecutive k of one row (16 bytes) per term.
 //   F16 = false: BF16 terms t0 = bf16(x), t1 = bf16(x - t0), t2 (nterms of them).
 //   F16 = true : the scaled FP16 (hi, lo) of f16_terms with the row exponents
 //                ex[] (Rp entries); a row whose max is not finite is all NaN.
@@ -110,14 +110,16 @@ __global__ void __launch_bounds__(256) split_bf16_kernel(const __grid_constant__
   const int z = blockIdx.z + p.zbase;
   const float *__restrict__ X = z ? p.X1 : p.X0;
   const int ld = z ? p.ld1 : p.ld0, R = z ? p.R1 : p.R0, kcontig = z ? p.kc1 : p.kc0;
-  const int Rp = z ? p.Rp1 : p.Rp0, K = p.K, Kp = p.Kp, nterms = p.nterms;
+  const int K = p.K, Kp = p.Kp, nterms = p.nterms;
   const int *__restrict__ ex = z ? p.ex1 : p.ex0;
   __nv_bfloat16 *__restrict__ out = z ? p.out1 : p.out0;
   const int64_t ldo = p.ldo;
   __shared__ float tile[32][65];
   const int k0 = blockIdx.x * 64;
   const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
-  for (int r0 = blockIdx.y * 32; r0 < Rp; r0 += gridDim.y * 32) {
+  // rows past R are never read (the GEMM's maps end at the problem's rows),
+  // so only row blocks holding data are written
+  for (int r0 = blockIdx.y * 32; r0 < R; r0 += gridDim.y * 32) {
     load_tile_32x64<float>(X, ld, R, K, kcontig != 0, r0, k0, tile);
     __syncthreads();
     unsigned w[3][4];  // term t of the 8 values, packed in pairs
@@ -167,7 +169,8 @@ __global__ void __launch_bounds__(256) split_bf16_kernel(const __grid_constant__
 // row held in registers (VPT values a thread, Kp <= 256 VPT) between the
 // block-wide max and the split, so it is read from memory once.  Writes the
 // row's exponent and its terms exactly as row_absmax_kernel followed by
-// split_bf16_kernel<true> do (columns [K, Kp) and rows [R, Rp) as zeros).
+// split_bf16_kernel<true> do (columns [K, Kp) as zeros; rows past R left
+// unwritten).
 struct RowSplitArgs {
   const float *X0, *X1;  // first row of each operand (part)
   int ld0, ld1, R0, R1, Rp0, Rp1;
@@ -201,7 +204,7 @@ __device__ __forceinline__ void row_load(const float *__restrict__ X, int K, boo
 template <int VPT>
 __global__ void __launch_bounds__(256) f16_row_split_kernel(const __grid_constant__ RowSplitArgs p) {
   const int z = blockIdx.z + p.zbase;
-  const int R = z ? p.R1 : p.R0, Rp = z ? p.Rp1 : p.Rp0;
+  const int R = z ? p.R1 : p.R0;
   const int ld = z ? p.ld1 : p.ld0;
   const float *__restrict__ X0 = z ? p.X1 : p.X0;
   int *__restrict__ exo = z ? p.ex1 : p.ex0;
@@ -210,14 +213,15 @@ __global__ void __launch_bounds__(256) f16_row_split_kernel(const __grid_constan
   const bool vec = p.vec != 0;
   __shared__ unsigned wmax[2][8];  // by row parity: a fast warp may start the next row
   int row = blockIdx.x;
-  if (row >= Rp) return;  // the other operand has more rows (uniform per CTA)
+  // rows past R are never read (the GEMM's maps end at the problem's rows)
+  if (row >= R) return;  // the other operand has more rows (uniform per CTA)
   // value 4 j + q of this thread is element 1024 j + 4 t + q: a warp reads and
   // writes contiguous runs
   float v[VPT], nv[VPT];
   row_load<VPT>(X0 + (int64_t)row * ld, K, row < R, vec, t, v);
-  for (int it = 0; row < Rp; row += gridDim.x, ++it) {
+  for (int it = 0; row < R; row += gridDim.x, ++it) {
     const int next = row + gridDim.x;
-    if (next < Rp) row_load<VPT>(X0 + (int64_t)next * ld, K, next < R, vec, t, nv);
+    if (next < R) row_load<VPT>(X0 + (int64_t)next * ld, K, true, vec, t, nv);
     const bool live = row < R;
     // max |x| as a bit pattern (NaN and Inf above every finite value)
     unsigned mx = 0;
@@ -414,8 +418,9 @@ __device__ __forceinline__ void slice_digits(const double *x, int e, int S, uint
 // d_s = floor(M * 2^(b - E + 7s)) mod 128, a shift and a mask (the GPU's FP64
 // rate would make the recurrence itself the bottleneck of this pass).
 // out: S blocks of Rp rows x Kp (row-major BF16), slice s at rows (s-1)*Rp;
-// each thread writes 8 consecutive k of one row (16 bytes) per slice.  Both
-// operands in one launch (blockIdx.z).
+// each thread writes 8 consecutive k of one row (16 bytes) per slice; rows
+// past R are left unwritten (the GEMM's maps end there).  Both operands in
+// one launch (blockIdx.z).
 __global__ void __launch_bounds__(256) ozaki_slice_kernel(const __grid_constant__ OperandPair p,
                                                           int S) {
   const int z = blockIdx.z;
@@ -428,7 +433,7 @@ __global__ void __launch_bounds__(256) ozaki_slice_kernel(const __grid_constant_
   const int k0 = blockIdx.x * 64;
   const int r = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
   const int64_t step = (int64_t)Rp * Kp / 8;  // one slice block, in uint4
-  for (int r0 = blockIdx.y * 32; r0 < Rp; r0 += gridDim.y * 32) {
+  for (int r0 = blockIdx.y * 32; r0 < R; r0 += gridDim.y * 32) {
     load_tile_32x64<double>(X, ld, R, K, kcontig != 0, r0, k0, tile);
     __syncthreads();
     const int gr = r0 + r;
@@ -661,8 +666,9 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         int sg = 0, kk = 0;  // segment of block kb and the block within it
         for (int kb = 0; kb < kblocks; ++kb, ++L, ++kk) {
           if (kk == skb) { ++sg; kk = 0; }
-          const int xa = (int)(((segA >> (4 * sg)) & 15u) * skb + kk) * kSplitBK;
-          const int xb = (int)(((segB >> (4 * sg)) & 15u) * skb + kk) * kSplitBK;
+          // 3-D maps of k x terms x rows: (K in the term block, term, row)
+          const int xk = kk * kSplitBK;
+          const int za = (int)((segA >> (4 * sg)) & 15u), zb = (int)((segB >> (4 * sg)) & 15u);
           const int s = L % kBxStages;
           const uint32_t r = L / kBxStages;
           if (!mbar_wait(&empty[s], (r & 1) ^ 1, p.err, kErrTimeoutEmpty, abort_flag)) break;
@@ -671,13 +677,13 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             // both CTAs' A rows and B halves land on the even CTA's full barrier
             if (rank == 0) mbar_arrive_expect_tx(&full[s], 2 * kBxStage);
             const uint32_t fb = cluster_addr(&full[s], 0);
-            tma_load_2d_pair(sa, mA, xa, tm * kSplitBM, fb);
-            tma_load_2d_pair(sa + kBxABytes, mB, xb, tn * BN + (int)rank * (BN / 2), fb);
+            tma_load_3d_pair(sa, mA, xk, za, tm * kSplitBM, fb);
+            tma_load_3d_pair(sa + kBxABytes, mB, xk, zb, tn * BN + (int)rank * (BN / 2), fb);
             continue;
           }
           mbar_arrive_expect_tx(&full[s], kBxStage);  // own A and B tiles
-          tma_load_2d(sa, mA, xa, tm * kSplitBM, &full[s]);
-          tma_load_2d(sa + kBxABytes, mB, xb, tn * BN, &full[s]);
+          tma_load_3d(sa, mA, xk, za, tm * kSplitBM, &full[s]);
+          tma_load_3d(sa + kBxABytes, mB, xk, zb, tn * BN, &full[s]);
         }
       }
     }
@@ -1693,6 +1699,16 @@ static bool use_pair_mma(int kind, int m, int n, int k) {
   return v != 2;
 }
 
+// The split GEMM's operand maps over the rows / columns of L: k x T x rows
+// (K within a term block, the term, the row; T = Kld / Kp terms), so rows
+// past h (w) and K past k read as zeros and the padding is never read.
+static bool bf16x_maps(const Bf16xLayout &L, int h, int w, int k, CUtensorMap *tA,
+                       CUtensorMap *tB, int box_b) {
+  const int64_t T = L.Kld / L.Kp;
+  return encode_3d(tA, L.Ap, 2, k, T, h, L.Kp, L.Kld, kSplitBK, 1, kSplitBM) &&
+         encode_3d(tB, L.Bp, 2, k, T, w, L.Kp, L.Kld, kSplitBK, 1, box_b);
+}
+
 // L: the layout of the rows / columns this launch covers; (tm, tn, k): the
 // problem whose shape class picks the cluster mode.
 template <bool F16, int BN>
@@ -1701,9 +1717,7 @@ static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, int tm, int tn, int
   // pair MMAs on row-tile pairs (2-CTA clusters) when there are two or more row tiles
   const bool pair = L.Mp / kSplitBM >= 2 && use_pair_mma(0, tm, tn, k);
   CUtensorMap tA{}, tB{};
-  if (!encode_2d(&tA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&tB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, pair ? BN / 2 : BN, true))
-    return GB300_ERR_CUDA;
+  if (!bf16x_maps(L, p.m, p.n, k, &tA, &tB, pair ? BN / 2 : BN)) return GB300_ERR_CUDA;
   p.tiles_n = (p.n + BN - 1) / BN;
   return persistent_launch<Bf16xParams>(
       bf16x_gemm_kernel<0, F16, BN>, bf16x_gemm_kernel<2, F16, BN>, kBxThreads,
@@ -1839,9 +1853,7 @@ int bf16x_group_entry(int m, int n, int k, float alpha, float beta, float *C, in
   const int rc = bf16x_block_setup(m, n, k, 0, m, 0, n, alpha, beta, C, ldc, products, 0, ws,
                                    ws_bytes, err, L, e.prm);
   if (rc != GB300_OK) return rc;
-  if (!encode_2d(&e.tmA, L.Ap, 2, L.Kld, L.Mp, L.Kld, kSplitBK, kSplitBM, true) ||
-      !encode_2d(&e.tmB, L.Bp, 2, L.Kld, L.Np, L.Kld, kSplitBK, kGroupBN, true))
-    return GB300_ERR_CUDA;
+  if (!bf16x_maps(L, m, n, k, &e.tmA, &e.tmB, kGroupBN)) return GB300_ERR_CUDA;
   e.prm.tiles_n = (n + kGroupBN - 1) / kGroupBN;
   e.unit0 = unit0;
   *units = e.prm.tiles_m * e.prm.tiles_n;
@@ -1969,8 +1981,8 @@ int ozaki_run(int m, int n, int k, double alpha, double beta, double *C, int ldc
 // them reads as zeros, so the padding is never read from memory.
 static bool ozaki_maps(const OzakiGemmArgs &a, CUtensorMap *tA, CUtensorMap *tB, int box_b) {
   const int64_t ma = a.m_all > 0 ? a.m_all : a.Mp, na = a.n_all > 0 ? a.n_all : a.Np;
-  return encode_3d(tA, a.As, 2, a.k, ma, a.S, a.Kp, a.Mp * a.Kp, kSplitBK, kSplitBM) &&
-         encode_3d(tB, a.Bs, 2, a.k, na, a.S, a.Kp, a.Np * a.Kp, kSplitBK, box_b);
+  return encode_3d(tA, a.As, 2, a.k, ma, a.S, a.Kp, a.Mp * a.Kp, kSplitBK, kSplitBM, 1) &&
+         encode_3d(tB, a.Bs, 2, a.k, na, a.S, a.Kp, a.Np * a.Kp, kSplitBK, box_b, 1);
 }
 
 template <int BN>

@@ -16,8 +16,10 @@ def ru(x, a):
 
 
 def ws_tensor(nbytes):
+    """A workspace filled with 0xFF bytes (BF16 NaN): padding rows of the split
+    operands are never written, and the GEMMs must never read them."""
     torch = torch_cuda()
-    return torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+    return torch.full((nbytes,), 255, dtype=torch.uint8, device="cuda")
 
 
 def aligned_view(ws, nbytes_needed_from):
@@ -65,8 +67,11 @@ def test_bf16x_split_bitexact_and_result(orc, products, ta, tb, tile_n):
     Aop[:m, :k] = op(A, ta, m, k)
     Bop = np.zeros((Np, Kp), np.float32)
     Bop[:n, :k] = op(B, tb, k, n).T
-    assert np.array_equal(Ap.view(np.uint32), osp.bf16x_operand(Aop, products, True).view(np.uint32))
-    assert np.array_equal(Bp.view(np.uint32), osp.bf16x_operand(Bop, products, False).view(np.uint32))
+    # the rows holding op(A) / op(B) (rows past them are left unwritten)
+    assert np.array_equal(Ap[:m].view(np.uint32),
+                          osp.bf16x_operand(Aop, products, True)[:m].view(np.uint32))
+    assert np.array_equal(Bp[:n].view(np.uint32),
+                          osp.bf16x_operand(Bop, products, False)[:n].view(np.uint32))
     # result vs Dot2 truth
     got = from_dev(dC, m)
     truth = orc.dot2gemm(ta, tb, m, n, k, 1.0, A, ar + 1, B, br + 3, 0.5, C, m)
@@ -131,7 +136,9 @@ def test_ozaki_slices_bitexact_and_result(orc, S, ta, tb, tile_n):
     for s in range(S):
         assert np.array_equal(As[s, :m, :k], sa[s])
         assert np.array_equal(Bs[s, :n, :k], sb[s])
-        assert not As[s, m:, :].any() and not As[s, :, k:].any()
+        # K columns past k of the rows holding data are zeros; rows past m are
+        # left unwritten (the GEMM's maps end at m)
+        assert not As[s, :m, k:].any() and not Bs[s, :n, k:].any()
     got = from_dev(dC, m)
     model = osp.ozaki_gemm_model(Aop, Bop, S)
     # the kernel's integer sums are exact, so it matches the model up to the
