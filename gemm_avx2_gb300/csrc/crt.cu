@@ -335,17 +335,22 @@ __device__ __forceinline__ double crt_compose(unsigned long long top, int e2, bo
 // words of 4 columns (word (col / 4) Mp + row), so one 32-bit load per
 // modulus brings the thread's residues, and a warp's 32 rows load 128
 // contiguous bytes and update 32 contiguous elements of each column of C.
+// (m n / 4 threads in a 1-D grid: below 2^39 for every valid C.)
 template <int L>
 __global__ void __launch_bounds__(256)
     crt_reconstruct_kernel(const uint8_t *__restrict__ rres, const int *__restrict__ expA,
                            const int *__restrict__ expB, const __grid_constant__ CrtRecParams rp) {
   const int64_t plane_w = (int64_t)rp.Mp * rp.Np / 4;  // words per residue plane
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= rp.m) return;
-  const int ea = expA[i];
+  // thread t: row t % m of column group t / m, so a warp covers 32 rows of
+  // one group (or, for m < 32, several groups) and small outputs fill whole
+  // warps
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int ngroups = (rp.n + 3) / 4;
+  if (t >= (int64_t)rp.m * ngroups) return;
+  const int i = (int)(t % rp.m), jg = (int)(t / rp.m);
+  const int ea = expA[i];
   const unsigned *base = reinterpret_cast<const unsigned *>(rres);
-  for (int jg = blockIdx.y; jg < ngroups; jg += gridDim.y) {
+  {
     const unsigned *src = base + (int64_t)jg * rp.Mp + i;
     unsigned word[kCrtMaxModuli];
 #pragma unroll
@@ -665,8 +670,8 @@ int crt_reconstruct_launch(const OzakiGemmArgs &a, int b, cudaStream_t st) {
   rp.alpha = a.alpha; rp.beta = a.beta; rp.C = a.C; rp.ldc = a.ldc;
   const uint8_t *rres = a.rres;
   const int *expA = a.expA, *expB = a.expB;
-  const int ngroups = (w + 3) / 4;
-  const dim3 grid((unsigned)((h + 255) / 256), (unsigned)(ngroups < 65535 ? ngroups : 65535));
+  const int64_t threads = (int64_t)h * ((w + 3) / 4);
+  const dim3 grid((unsigned)((threads + 255) / 256));
   // limbs of M: 4 up to 16 moduli, 5 up to 20, 6 up to 24
   const int limbs = (bl + 31) / 32 < 2 ? 2 : (bl + 31) / 32;
   switch (limbs) {
