@@ -462,18 +462,28 @@ def run_ours(args, torch, rank, world):
         hA.copy_(prob.A)
         hB.copy_(prob.B)
         hC.copy_(prob.C0)
+        hC0 = hC.clone()   # the workload's C, restored before every step (C is in / out)
         ah, bh, ch = hA.numpy(), hB.numpy(), hC.numpy()
         for _ in range(2):
+            hC.copy_(hC0)
             assert g.host_split_gemm(form, w["ta"], w["tb"], m, n, k, w["alpha"], ah, w["lda"],
                                      bh, w["ldb"], w["beta"], ch, w["ldc"], param) == g.OK
         steps_e2e = max(3, min(args.steps, 10))
-        t = time.perf_counter()
+        dt = 0.0
         for _ in range(steps_e2e):
+            hC.copy_(hC0)   # outside the timed call
+            t = time.perf_counter()
             assert g.host_split_gemm(form, w["ta"], w["tb"], m, n, k, w["alpha"], ah, w["lda"],
                                      bh, w["ldb"], w["beta"], ch, w["ldc"], param) == g.OK
-        dt = (time.perf_counter() - t) / steps_e2e
+            dt += time.perf_counter() - t
+        dt /= steps_e2e
         esz = 8 if is_d else 4
-        h2d = (prob.ar * prob.ac + prob.br * prob.bc + m * n) * esz
+        # the pipelined host path (page-locked buffers, k >= 1024, m or n >= 4096)
+        # leaves C in host memory when beta = 0 and every entry of C is finite and
+        # non-negative (0 * C = +0): then only A and B cross the link
+        c_moved = not (w["beta"] == 0.0 and k >= 1024 and max(m, n) >= 4096 and
+                       bool(torch.isfinite(hC0).all()) and not bool(torch.signbit(hC0).any()))
+        h2d = (prob.ar * prob.ac + prob.br * prob.bc + (m * n if c_moved else 0)) * esz
         e2e = {"value": round(prob.flops / dt / 1e12, 3), "unit": "TFLOP/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": m * n * esz,
                "ms_per_step": round(dt * 1e3, 3), "api": "gb300_host_%s" %
@@ -735,16 +745,21 @@ def run_complex(args, torch, rank, world):
             hA.copy_(A)
             hB.copy_(B)
             hC.copy_(C0)
+            hC0 = hC.clone()   # the workload's C, restored before every step (C is in / out)
             ah, bh, ch = hA.numpy(), hB.numpy(), hC.numpy()
             for _ in range(2):
+                hC.copy_(hC0)
                 assert g.host_complex(p, w["ta"], w["tb"], m, n, k, w["alpha"], ah, m, bh, k,
                                       w["beta"], ch, m, method=method, param=param) == g.OK
             steps_e2e = max(3, min(args.steps, 10))
-            t = time.perf_counter()
+            dts = 0.0
             for _ in range(steps_e2e):
+                hC.copy_(hC0)   # outside the timed call
+                t = time.perf_counter()
                 assert g.host_complex(p, w["ta"], w["tb"], m, n, k, w["alpha"], ah, m, bh, k,
                                       w["beta"], ch, m, method=method, param=param) == g.OK
-            dts = (time.perf_counter() - t) / steps_e2e
+                dts += time.perf_counter() - t
+            dts /= steps_e2e
             esz = 16 if p == "z" else 8
             e2e = {"value": round(flops / dts / 1e12, 3), "unit": "TFLOP/s",
                    "h2d_bytes_per_step": (m * k + k * n + m * n) * esz,
@@ -1090,7 +1105,10 @@ def transfer_note(form):
     if form == "bf16x":
         return ("pinned host buffers; A, B and C are copied to HBM in row / column parts by the "
                 "copy engines while earlier parts are split and their C blocks multiplied, and "
-                "each C block is copied back as it finishes (bytes above cross the link once)")
+                "each C block is copied back as it finishes; with beta = 0 and C finite and "
+                "non-negative (C = 0 here) C is zero-filled in HBM instead of copied (0 * C = +0); "
+                "the workload's C is restored in host memory before every step, outside the "
+                "timed call (bytes above cross the link once)")
     return ("pinned host buffers; A and B are copied to HBM, C is read and written in host memory "
             "by the epilogue or staged in HBM beside the prepare (bytes above cross the link once)")
 

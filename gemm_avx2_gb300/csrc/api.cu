@@ -11,6 +11,11 @@
 #include <unordered_map>
 #include <utility>
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -174,6 +179,113 @@ static bool host_direct_ok(const void *a, const void *b, const void *c) {
   return host_pinned(a, b, c);
 }
 
+// A small persistent pool of host threads for scans of host buffers (started
+// on first use; the pipelined host path's C scan).  start(n, f) has the
+// workers call f(0) .. f(n - 1) and returns at once; wait() joins in and
+// returns when all are done (one job at a time: start blocks while another
+// caller's job runs).
+class HostPool {
+ public:
+  static HostPool &get() {
+    static HostPool p;
+    return p;
+  }
+  int size() const { return (int)workers_.size() + 1; }
+  void start(int n, std::function<void(int)> f) {
+    run_mu_.lock();  // one job at a time (calls from several devices); wait() unlocks
+    std::lock_guard<std::mutex> lk(mu_);
+    fn_ = std::move(f);
+    job_ = &fn_;
+    njobs_ = n;
+    next_ = 0;
+    done_ = 0;
+    ++gen_;
+    cv_.notify_all();
+  }
+  void wait() {
+    work();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return done_ == njobs_; });
+    job_ = nullptr;
+    lk.unlock();
+    run_mu_.unlock();
+  }
+
+ private:
+  HostPool() {
+    unsigned hw = std::thread::hardware_concurrency();
+    const int nt = hw > 16 ? 15 : hw > 1 ? (int)hw - 1 : 0;
+    for (int i = 0; i < nt; ++i) workers_.emplace_back([this] { loop(); });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto &t : workers_) t.join();
+  }
+  void work() {
+    for (;;) {
+      int i;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!job_ || next_ >= njobs_) return;
+        i = next_++;
+      }
+      (*job_)(i);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (++done_ == njobs_) done_cv_.notify_all();
+    }
+  }
+  void loop() {
+    unsigned long seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+      }
+      work();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  std::function<void(int)> fn_;
+  const std::function<void(int)> *job_ = nullptr;
+  int njobs_ = 0, next_ = 0, done_ = 0;
+  unsigned long gen_ = 0;
+  bool stop_ = false;
+};
+
+// True when every entry of the m x n window of C is finite with its sign bit
+// clear: then beta = 0 makes 0 * C = +0 everywhere, exactly what a zero-filled
+// copy gives, so C need not cross the CPU-GPU link.  The bit patterns are
+// compared as unsigned integers: negative values (sign bit) and Inf / NaN lie
+// at or above the +Inf pattern.
+// The scan starts on the pool and runs while the caller queues other work;
+// *bad is final after HostPool::get().wait().
+template <typename T>
+static void host_c_scan_start(const T *c, int m, int n, int ldc, std::atomic<bool> *bad) {
+  using U = typename std::conditional<sizeof(T) == 8, uint64_t, uint32_t>::type;
+  const U lim = sizeof(T) == 8 ? (U)0x7ff0000000000000ull : (U)0x7f800000u;
+  bad->store(false);
+  HostPool &pool = HostPool::get();
+  const int chunks = pool.size() * 4 < n ? pool.size() * 4 : n;
+  pool.start(chunks, [=](int t) {
+    const int j0 = (int)((int64_t)n * t / chunks), j1 = (int)((int64_t)n * (t + 1) / chunks);
+    for (int j = j0; j < j1 && !bad->load(std::memory_order_relaxed); ++j) {
+      const U *col = reinterpret_cast<const U *>(c + (int64_t)j * ldc);
+      U mx = 0;
+      for (int i = 0; i < m; ++i) mx = col[i] > mx ? col[i] : mx;
+      if (mx >= lim) bad->store(true, std::memory_order_relaxed);
+    }
+  });
+}
+
 // Operand parts of the pipelined host path (GB300_TUNE_HOST_PARTS): 0 =
 // by shape, 1 = no pipeline, P = P row parts of op(A) and P column parts of
 // op(B).
@@ -205,7 +317,12 @@ static std::vector<int> part_bounds(int R, int parts, int align) {
 // runs every C block (i, j) into HBM as soon as both of its parts are
 // prepared; an output stream copies each finished block back.  So the link
 // transfers (about 210 GB/s one way, 320 GB/s both ways together: the bound
-// of this path) overlap the GEMMs of other blocks.  The splits run on a
+// of this path) overlap the GEMMs of other blocks.  With beta = 0 the C
+// parts are copied only when some entry of C is negative, Inf or NaN (a scan
+// of C on host threads while the first two shards of A and B copy):
+// otherwise 0 * C is +0 everywhere and the device copy of C is zero-filled
+// instead, with the same result bits and a third fewer bytes over the link
+// (A, B and C of equal size).  The splits run on a
 // stream of their own and the blocks alternate between two streams, so one
 // block's partial last wave of tiles overlaps the next block.  The epilogues stay in
 // HBM: writing C over the link from the epilogue slowed the blocks 1.5-3x
@@ -234,7 +351,7 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
   for (cudaStream_t *q : {&s->copy_stream, &s->out_stream, &s->prep_stream, &s->block_stream})
     if (!*q && cudaStreamCreateWithFlags(q, cudaStreamNonBlocking) != cudaSuccess)
       return GB300_ERR_CUDA;
-  while ((int)s->part_ev.size() < 1 + 2 * (P + Q) + P * Q) {
+  while ((int)s->part_ev.size() < 1 + 2 * (P + Q) + P * Q + Q) {
     cudaEvent_t e;
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return GB300_ERR_CUDA;
     s->part_ev.push_back(e);
@@ -274,12 +391,35 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
   const cudaMemcpyKind h2d = cudaMemcpyHostToDevice, d2h = cudaMemcpyDeviceToHost;
   // arrival of the parts in HBM, their splits done, the blocks done
   cudaEvent_t *evA = s->part_ev.data() + 1, *evB = evA + P, *evPA = evB + Q, *evPB = evPA + P;
-  cudaEvent_t *evC = evPB + Q;
+  cudaEvent_t *evC = evPB + Q, *evCin = evC + P * Q;  // blocks done, C parts in HBM
   // the side streams start after the work already queued on st (buffer reuse)
   bool ok = cudaEventRecord(s->part_ev[0], st) == cudaSuccess;
   for (cudaStream_t q : {cs, os, ps, bs[1]})
     ok = ok && cudaStreamWaitEvent(q, s->part_ev[0], 0) == cudaSuccess;
-  for (int sh = 0; ok && sh < (P > Q ? P : Q); ++sh) {
+  // beta = 0: is C needed at all?  The scan runs on host threads while the
+  // first `early` shards of A and B are queued; their C parts follow once it
+  // is done.
+  int c_mode = beta == T(0) ? -1 : 1;  // -1 undecided, 0 zero-fill, 1 copy
+  std::atomic<bool> c_bad{false};
+  if (c_mode < 0) host_c_scan_start(c, m, n, ldc, &c_bad);
+  const int nsh = P > Q ? P : Q, early = c_mode < 0 ? (nsh < 2 ? nsh : 2) : 0;
+  auto c_part = [&](int j) {  // C columns of part j: copied or zero-filled, then evCin[j]
+    const int c0 = cb[j], w = cb[j + 1] - c0;
+    return (c_mode == 1
+                ? copy(dC + (int64_t)c0 * uldc, uldc, c + (int64_t)c0 * ldc, ldc, m, w, h2d, cs)
+                : cudaMemset2DAsync(dC + (int64_t)c0 * uldc, (size_t)uldc * sizeof(T), 0,
+                                    (size_t)m * sizeof(T), w, cs) == cudaSuccess) &&
+           cudaEventRecord(evCin[j], cs) == cudaSuccess;
+  };
+  auto decide = [&]() {
+    HostPool::get().wait();
+    c_mode = c_bad.load() ? 1 : 0;
+    bool r = true;
+    for (int j = 0; j < early && j < Q; ++j) r = r && c_part(j);
+    return r;
+  };
+  for (int sh = 0; ok && sh < nsh; ++sh) {
+    if (sh == early && c_mode < 0) ok = decide();
     if (sh < P) {  // op(A) rows [r0, r1): rows of A, or columns of A when transposed
       const int r0 = rb[sh], h = rb[sh + 1] - r0;
       ok = (an ? copy(dA + r0, ulda, a + r0, lda, h, k, h2d, cs)
@@ -291,9 +431,14 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
       const int c0 = cb[sh], w = cb[sh + 1] - c0;
       ok = (bn ? copy(dB + (int64_t)c0 * uldb, uldb, b + (int64_t)c0 * ldb, ldb, k, w, h2d, cs)
                : copy(dB + c0, uldb, b + c0, ldb, w, k, h2d, cs)) &&
-           copy(dC + (int64_t)c0 * uldc, uldc, c + (int64_t)c0 * ldc, ldc, m, w, h2d, cs) &&
            cudaEventRecord(evB[sh], cs) == cudaSuccess;
+      if (ok && c_mode >= 0) ok = c_part(sh);
     }
+  }
+  // the scan is always joined here (its threads use this frame's flag)
+  if (c_mode < 0) {
+    if (ok) ok = decide();
+    else HostPool::get().wait();
   }
   int rc = ok ? GB300_OK : GB300_ERR_CUDA;
   // the splits, each once its part has arrived (all enqueued before the
@@ -317,7 +462,8 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
     const int i0 = rb[i], h = rb[i + 1] - i0, j0 = cb[j], w = cb[j + 1] - j0;
     const cudaStream_t q = bs[nblk & 1];
     if (cudaStreamWaitEvent(q, evPA[i], 0) != cudaSuccess ||
-        cudaStreamWaitEvent(q, evPB[j], 0) != cudaSuccess)
+        cudaStreamWaitEvent(q, evPB[j], 0) != cudaSuccess ||
+        cudaStreamWaitEvent(q, evCin[j], 0) != cudaSuccess)
       return (int)GB300_ERR_CUDA;
     int r = run_block(i0, h, j0, w, ws, q);
     // the finished block goes back while the next ones compute

@@ -133,3 +133,33 @@ def test_pipelined_host_crt_pinned_beta0_nan(orc, host_parts):
     got = pc.numpy().reshape((n, m)).T
     assert np.isnan(got[7, 650]) and np.isnan(got[900, 2])
     assert np.array_equal(got, ref, equal_nan=True)
+
+
+@pytest.mark.parametrize("form", ["bf16x", "crt"])
+@pytest.mark.parametrize("sign", [1.0, -1.0])
+def test_pipelined_host_beta0_c_unread_or_copied(orc, host_parts, form, sign):
+    """beta = 0: when every entry of C is finite and non-negative, 0 * C is +0
+    everywhere and the pipelined host path zero-fills its device copy of C
+    instead of moving C over the link; otherwise it copies C.  Both give the
+    device-pointer call's bits, including the sign of zero: with alpha = -1
+    and a zero row of op(A), that row of the result is 0 * C + (-0), +0 for
+    C >= 0 and -0 for C < 0."""
+    torch = torch_cuda()
+    m, n, k = 1100, 800, 1030
+    dt = np.float32 if form == "bf16x" else np.float64
+    A = orc.uniform((k, m), dt, 87, 0)
+    B = orc.uniform((k, n), dt, 87, 1)
+    A[:, 9] = 0.0                                    # row 9 of op(A) = A^T
+    C = (sign * np.abs(orc.uniform((m, n), dt, 87, 2))).astype(dt)
+    C[:, 17] = 0.0 * sign                            # exact zeros (+0, or -0 when negative)
+    param = g.FP16X3 if form == "bf16x" else 16
+    ref = device_result(form, "T", "N", m, n, k, -1.0, A, k, B, k, 0.0, C, param)
+    pa, pb, pc = (torch.from_numpy(x.ravel(order="F").copy()).pin_memory() for x in (A, B, C))
+    assert host_parts(4) == g.OK
+    f = g.core().gb300_host_sgemm_bf16x if form == "bf16x" else g.core().gb300_host_dgemm_ozaki2
+    assert f(b"T", b"N", m, n, k, -1.0, pa.data_ptr(), k, pb.data_ptr(), k, 0.0,
+             pc.data_ptr(), m, param) == g.OK
+    got = pc.numpy().reshape((n, m)).T
+    u = np.uint32 if form == "bf16x" else np.uint64
+    assert np.array_equal(np.ascontiguousarray(got).view(u), np.ascontiguousarray(ref).view(u))
+    assert np.all(np.signbit(got[9]) == (sign < 0)) and not got[9].any()
