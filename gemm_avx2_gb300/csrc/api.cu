@@ -213,8 +213,11 @@ class HostPool {
 
  private:
   HostPool() {
-    unsigned hw = std::thread::hardware_concurrency();
-    const int nt = hw > 16 ? 15 : hw > 1 ? (int)hw - 1 : 0;
+    // at most 12 threads with the caller, and 4 cores left to the caller's
+    // other threads: the caller waits for the slowest chunk, so a scan thread
+    // preempted by another runnable thread would hold up the whole call
+    const int hw = (int)std::thread::hardware_concurrency();
+    const int nt = hw >= 16 ? 11 : hw > 5 ? hw - 5 : 0;
     for (int i = 0; i < nt; ++i) workers_.emplace_back([this] { loop(); });
   }
   ~HostPool() {
@@ -317,12 +320,12 @@ static std::vector<int> part_bounds(int R, int parts, int align) {
 // runs every C block (i, j) into HBM as soon as both of its parts are
 // prepared; an output stream copies each finished block back.  So the link
 // transfers (about 210 GB/s one way, 320 GB/s both ways together: the bound
-// of this path) overlap the GEMMs of other blocks.  With beta = 0 the C
-// parts are copied only when some entry of C is negative, Inf or NaN (a scan
-// of C on host threads while the first two shards of A and B copy):
-// otherwise 0 * C is +0 everywhere and the device copy of C is zero-filled
-// instead, with the same result bits and a third fewer bytes over the link
-// (A, B and C of equal size).  The splits run on a
+// of this path) overlap the GEMMs of other blocks.  With beta = 0 a C part
+// is copied only when one of its entries is negative, Inf or NaN (a scan of
+// the part on host threads while its shard's A and B copy): otherwise 0 * C
+// is +0 there and the device copy of that part is zero-filled instead, with
+// the same result bits and a third fewer bytes over the link (A, B and C of
+// equal size).  The splits run on a
 // stream of their own and the blocks alternate between two streams, so one
 // block's partial last wave of tiles overlaps the next block.  The epilogues stay in
 // HBM: writing C over the link from the epilogue slowed the blocks 1.5-3x
@@ -396,67 +399,21 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
   bool ok = cudaEventRecord(s->part_ev[0], st) == cudaSuccess;
   for (cudaStream_t q : {cs, os, ps, bs[1]})
     ok = ok && cudaStreamWaitEvent(q, s->part_ev[0], 0) == cudaSuccess;
-  // beta = 0: is C needed at all?  The scan runs on host threads while the
-  // first `early` shards of A and B are queued; their C parts follow once it
-  // is done.
-  int c_mode = beta == T(0) ? -1 : 1;  // -1 undecided, 0 zero-fill, 1 copy
+  // One pass over the shards, so the GPU never waits for this thread: each
+  // shard's A and B parts go on the copy stream; with beta = 0 the scan of
+  // its C part (host threads, started first) decides whether that part is
+  // copied or zero-filled, and runs while the shard's A and B copy; then the
+  // shard's splits, and every block whose parts are now all queued.
+  const bool b0 = beta == T(0);
   std::atomic<bool> c_bad{false};
-  if (c_mode < 0) host_c_scan_start(c, m, n, ldc, &c_bad);
-  const int nsh = P > Q ? P : Q, early = c_mode < 0 ? (nsh < 2 ? nsh : 2) : 0;
-  auto c_part = [&](int j) {  // C columns of part j: copied or zero-filled, then evCin[j]
+  bool scanning = false;
+  auto c_part = [&](int j, bool need) {  // C columns of part j, then evCin[j]
     const int c0 = cb[j], w = cb[j + 1] - c0;
-    return (c_mode == 1
-                ? copy(dC + (int64_t)c0 * uldc, uldc, c + (int64_t)c0 * ldc, ldc, m, w, h2d, cs)
-                : cudaMemset2DAsync(dC + (int64_t)c0 * uldc, (size_t)uldc * sizeof(T), 0,
-                                    (size_t)m * sizeof(T), w, cs) == cudaSuccess) &&
+    return (need ? copy(dC + (int64_t)c0 * uldc, uldc, c + (int64_t)c0 * ldc, ldc, m, w, h2d, cs)
+                 : cudaMemset2DAsync(dC + (int64_t)c0 * uldc, (size_t)uldc * sizeof(T), 0,
+                                     (size_t)m * sizeof(T), w, cs) == cudaSuccess) &&
            cudaEventRecord(evCin[j], cs) == cudaSuccess;
   };
-  auto decide = [&]() {
-    HostPool::get().wait();
-    c_mode = c_bad.load() ? 1 : 0;
-    bool r = true;
-    for (int j = 0; j < early && j < Q; ++j) r = r && c_part(j);
-    return r;
-  };
-  for (int sh = 0; ok && sh < nsh; ++sh) {
-    if (sh == early && c_mode < 0) ok = decide();
-    if (sh < P) {  // op(A) rows [r0, r1): rows of A, or columns of A when transposed
-      const int r0 = rb[sh], h = rb[sh + 1] - r0;
-      ok = (an ? copy(dA + r0, ulda, a + r0, lda, h, k, h2d, cs)
-               : copy(dA + (int64_t)r0 * ulda, ulda, a + (int64_t)r0 * lda, lda, k, h, h2d, cs)) &&
-           cudaEventRecord(evA[sh], cs) == cudaSuccess;
-    }
-    if (ok && sh < Q) {  // op(B) columns [c0, c1), and those columns of C (read also when
-                         // beta == 0: C * 0 keeps the NaN / Inf of C, as C_MULT_BETA does)
-      const int c0 = cb[sh], w = cb[sh + 1] - c0;
-      ok = (bn ? copy(dB + (int64_t)c0 * uldb, uldb, b + (int64_t)c0 * ldb, ldb, k, w, h2d, cs)
-               : copy(dB + c0, uldb, b + c0, ldb, w, k, h2d, cs)) &&
-           cudaEventRecord(evB[sh], cs) == cudaSuccess;
-      if (ok && c_mode >= 0) ok = c_part(sh);
-    }
-  }
-  // the scan is always joined here (its threads use this frame's flag)
-  if (c_mode < 0) {
-    if (ok) ok = decide();
-    else HostPool::get().wait();
-  }
-  int rc = ok ? GB300_OK : GB300_ERR_CUDA;
-  // the splits, each once its part has arrived (all enqueued before the
-  // blocks wait on their events)
-  for (int sh = 0; rc == GB300_OK && sh < (P > Q ? P : Q); ++sh) {
-    if (sh < P) {
-      rc = cudaStreamWaitEvent(ps, evA[sh], 0) == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
-      if (rc == GB300_OK)
-        rc = prepare_part(0, ta, dA, ulda, rb[sh], rb[sh + 1] - rb[sh], ws, ps);
-      if (rc == GB300_OK && cudaEventRecord(evPA[sh], ps) != cudaSuccess) rc = GB300_ERR_CUDA;
-    }
-    if (rc == GB300_OK && sh < Q) {
-      rc = cudaStreamWaitEvent(ps, evB[sh], 0) == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
-      if (rc == GB300_OK)
-        rc = prepare_part(1, tb, dB, uldb, cb[sh], cb[sh + 1] - cb[sh], ws, ps);
-      if (rc == GB300_OK && cudaEventRecord(evPB[sh], ps) != cudaSuccess) rc = GB300_ERR_CUDA;
-    }
-  }
   int nblk = 0;
   auto block = [&](int i, int j) {
     const int i0 = rb[i], h = rb[i + 1] - i0, j0 = cb[j], w = cb[j + 1] - j0;
@@ -475,13 +432,54 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
       r = GB300_ERR_CUDA;
     return r;
   };
-  // the blocks in the order their second part arrives
-  for (int sh = 0; rc == GB300_OK && sh < (P > Q ? P : Q); ++sh) {
+  const int nsh = P > Q ? P : Q;
+  int rc = ok ? GB300_OK : GB300_ERR_CUDA;
+  for (int sh = 0; rc == GB300_OK && sh < nsh; ++sh) {
+    if (b0 && sh < Q) {
+      host_c_scan_start(c + (int64_t)cb[sh] * ldc, m, cb[sh + 1] - cb[sh], ldc, &c_bad);
+      scanning = true;
+    }
+    if (sh < P) {  // op(A) rows [r0, r1): rows of A, or columns of A when transposed
+      const int r0 = rb[sh], h = rb[sh + 1] - r0;
+      ok = (an ? copy(dA + r0, ulda, a + r0, lda, h, k, h2d, cs)
+               : copy(dA + (int64_t)r0 * ulda, ulda, a + (int64_t)r0 * lda, lda, k, h, h2d, cs)) &&
+           cudaEventRecord(evA[sh], cs) == cudaSuccess;
+    }
+    if (ok && sh < Q) {  // op(B) columns [c0, c1), and those columns of C (read when beta != 0,
+                         // and with beta = 0 when one is negative, Inf or NaN: C * 0 keeps
+                         // the NaN / Inf and the negative zeros, as C_MULT_BETA does)
+      const int c0 = cb[sh], w = cb[sh + 1] - c0;
+      ok = (bn ? copy(dB + (int64_t)c0 * uldb, uldb, b + (int64_t)c0 * ldb, ldb, k, w, h2d, cs)
+               : copy(dB + c0, uldb, b + c0, ldb, w, k, h2d, cs)) &&
+           cudaEventRecord(evB[sh], cs) == cudaSuccess;
+      if (ok && !b0) ok = c_part(sh, true);
+    }
+    if (scanning) {
+      HostPool::get().wait();
+      scanning = false;
+      if (ok) ok = c_part(sh, c_bad.load());
+    }
+    rc = ok ? GB300_OK : GB300_ERR_CUDA;
+    // the shard's splits, once its parts have arrived
+    if (rc == GB300_OK && sh < P) {
+      rc = cudaStreamWaitEvent(ps, evA[sh], 0) == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+      if (rc == GB300_OK)
+        rc = prepare_part(0, ta, dA, ulda, rb[sh], rb[sh + 1] - rb[sh], ws, ps);
+      if (rc == GB300_OK && cudaEventRecord(evPA[sh], ps) != cudaSuccess) rc = GB300_ERR_CUDA;
+    }
+    if (rc == GB300_OK && sh < Q) {
+      rc = cudaStreamWaitEvent(ps, evB[sh], 0) == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
+      if (rc == GB300_OK)
+        rc = prepare_part(1, tb, dB, uldb, cb[sh], cb[sh + 1] - cb[sh], ws, ps);
+      if (rc == GB300_OK && cudaEventRecord(evPB[sh], ps) != cudaSuccess) rc = GB300_ERR_CUDA;
+    }
+    // the blocks whose second part is this shard's
     if (sh < P)
       for (int j = 0; rc == GB300_OK && j < Q && j <= sh; ++j) rc = block(sh, j);
     if (sh < Q)
       for (int i = 0; rc == GB300_OK && i < P && i < sh; ++i) rc = block(i, sh);
   }
+  if (scanning) HostPool::get().wait();  // its threads use this frame's flag
   cudaError_t e = cudaSuccess;
   for (cudaStream_t q : {cs, ps, bs[0], bs[1], os}) {
     const cudaError_t eq = cudaStreamSynchronize(q);
