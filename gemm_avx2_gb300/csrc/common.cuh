@@ -159,6 +159,13 @@ __device__ __forceinline__ void tma_load_3d_pair(void *smem_dst, const void *tma
       "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(bar_cluster)
       : "memory");
 }
+// Prefetch of the 2-D box at (x, y) into L2 (no shared memory, no barrier;
+// the parts of the box outside the tensor are skipped).
+__device__ __forceinline__ void tma_prefetch_l2_2d(const void *tmap, int32_t x, int32_t y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(tmap),
+               "r"(x), "r"(y)
+               : "memory");
+}
 // Shared::cluster address of `p` (this CTA's shared memory) as seen in CTA `rank`.
 __device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
   uint32_t a;

@@ -467,6 +467,11 @@ __global__ void __launch_bounds__(256) ozaki_slice_kernel(const __grid_constant_
 // 2.7 us, twice the MMA time of a 4-block chunk.)
 // ===========================================================================
 struct Bf16xParams {
+  // C's window (m x n, ldc) as 128 x BN boxes, when c_pf: the producer
+  // prefetches each tile's C into L2 as the tile starts, so the epilogue's
+  // reads of C (latency-bound loads, a few per thread in flight) hit L2
+  CUtensorMap tmC;
+  int c_pf;
   int m, n, tiles_m, tiles_n, kblocks;
   // K' = nseg segments of skb 64-wide blocks; segment s reads the term block
   // (segA >> 4 s) & 15 of A' and (segB >> 4 s) & 15 of B' (each term stored
@@ -583,6 +588,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     if (!GR) {
       tma_prefetch_desc(&tmA);
       tma_prefetch_desc(&tmB);
+      if (p.c_pf) tma_prefetch_desc(&p.tmC);
     }
   }
   if (warp == 1) {
@@ -663,6 +669,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const unsigned segA = q.segA, segB = q.segB;
         int tm, tn;
         unit_tile(u, pi, tm, tn);
+        if (q.c_pf) tma_prefetch_l2_2d(&q.tmC, tm * kSplitBM, tn * BN);  // for its epilogue
         int sg = 0, kk = 0;  // segment of block kb and the block within it
         for (int kb = 0; kb < kblocks; ++kb, ++L, ++kk) {
           if (kk == skb) { ++sg; kk = 0; }
@@ -801,8 +808,8 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         // scaled FP16 form: the row and column scales come off here (a
         // non-finite row or column is NaN already; its marker exponent is capped)
         const int ea = F16 ? min(pq.expA[row], 1024) - 30 : 0;
-        // C in batches of 16 columns: all loads of a batch are issued before its
-        // stores, so the batch pays one memory latency instead of sixteen
+        // C in batches of 8 columns: all loads of a batch are issued before its
+        // stores, so the batch pays one memory latency instead of eight
 #pragma unroll
         for (int jb = 0; jb < kBxColsPerWarp; jb += 8) {
           float cv[8];
@@ -1709,6 +1716,15 @@ static bool bf16x_maps(const Bf16xLayout &L, int h, int w, int k, CUtensorMap *t
          encode_3d(tB, L.Bp, 2, k, T, w, L.Kp, L.Kld, kSplitBK, 1, box_b);
 }
 
+// The L2 prefetch map of C in 128 x bn boxes, where C's base and column
+// stride are 16-byte multiples (a tensor map's rule); else no prefetch.
+static void bf16x_c_prefetch(Bf16xParams &p, int bn) {
+  p.c_pf = ((uintptr_t)p.C % 16 == 0 && p.ldc % 4 == 0 &&
+            encode_2d(&p.tmC, p.C, 4, p.m, p.n, p.ldc, kSplitBM, bn, false))
+               ? 1
+               : 0;
+}
+
 // L: the layout of the rows / columns this launch covers; (tm, tn, k): the
 // problem whose shape class picks the cluster mode.
 template <bool F16, int BN>
@@ -1719,6 +1735,7 @@ static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, int tm, int tn, int
   CUtensorMap tA{}, tB{};
   if (!bf16x_maps(L, p.m, p.n, k, &tA, &tB, pair ? BN / 2 : BN)) return GB300_ERR_CUDA;
   p.tiles_n = (p.n + BN - 1) / BN;
+  bf16x_c_prefetch(p, BN);
   return persistent_launch<Bf16xParams>(
       bf16x_gemm_kernel<0, F16, BN>, bf16x_gemm_kernel<2, F16, BN>, kBxThreads,
       pair ? ClusterTile<2, BN>::kSmem : ClusterTile<0, BN>::kSmem, tA, tB, p, p.tiles_m,
@@ -1855,6 +1872,7 @@ int bf16x_group_entry(int m, int n, int k, float alpha, float beta, float *C, in
   if (rc != GB300_OK) return rc;
   if (!bf16x_maps(L, m, n, k, &e.tmA, &e.tmB, kGroupBN)) return GB300_ERR_CUDA;
   e.prm.tiles_n = (n + kGroupBN - 1) / kGroupBN;
+  bf16x_c_prefetch(e.prm, kGroupBN);
   e.unit0 = unit0;
   *units = e.prm.tiles_m * e.prm.tiles_n;
   std::memcpy(entry, &e, sizeof(e));
