@@ -467,9 +467,9 @@ __global__ void __launch_bounds__(256) ozaki_slice_kernel(const __grid_constant_
 // 2.7 us, twice the MMA time of a 4-block chunk.)
 // ===========================================================================
 struct Bf16xParams {
-  // C's window (m x n, ldc) as 128 x BN boxes, when c_pf: the producer
-  // prefetches each tile's C into L2 as the tile starts, so the epilogue's
-  // reads of C (latency-bound loads, a few per thread in flight) hit L2
+  // C's window (m x n, ldc) in boxes of 128 rows x 64 columns, when c_pf:
+  // the producer prefetches each tile's C into L2 as the tile starts, and the
+  // staged-C kernel (CS) loads the boxes into shared memory for its epilogue
   CUtensorMap tmC;
   int c_pf;
   int m, n, tiles_m, tiles_n, kblocks;
@@ -547,10 +547,28 @@ struct ClusterTile {
   static constexpr int kSmem = kStages * kStage + 1024 + 256;
 };
 
+// Staged C (kernel CS = true; pair MMAs, 256-wide tiles): the epilogue's plain
+// loads of C, a few per thread in flight, took 10.5 us of a rank-256 tile's
+// 14.5 (a timeline of one CTA; 3.3 us without them), longer than the tile's
+// MMAs.  So C comes in by TMA instead: two shared-memory slots of 128 rows x
+// 64 columns (the columns of one group of 4 epilogue warps) in place of one
+// ring stage.  Column blocks 0 and 1 of a tile load theirs as the tile
+// starts, under its MMAs; blocks 2 and 3 reuse the slots after them.
+constexpr int kCsSlotBytes = kSplitBM * 64 * 4;
+template <int CL, int BN, bool CS>
+struct BxSmem {
+  static constexpr int kStages = CS ? ClusterTile<CL, BN>::kStages - 1 : ClusterTile<CL, BN>::kStages;
+  static constexpr int kBytes = kStages * ClusterTile<CL, BN>::kStage + (CS ? 2 * kCsSlotBytes : 0) +
+                                1024 + 256;
+};
+// Staged C for tiles of at most this many K blocks (MMAs shorter than the C
+// update they have to hide; 24 at k = 256 with 6 products).
+constexpr int kBxStagedMaxKBlocks = 48;
+
 // GR: a grouped launch over the problems of p.grp (one CTA per tile; the
 // kernel parameters' maps are unused), each unit a tile of one problem, with
 // that problem's K extent, chunk runs and epilogue parameters.
-template <int CL, bool F16, int BN, bool GR = false>
+template <int CL, bool F16, int BN, bool GR = false, bool CS = false>
 __global__ void __launch_bounds__(kBxThreads, 1)
 bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   const __grid_constant__ Bf16xParams p) {
@@ -558,18 +576,22 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   using CT = ClusterTile<CL, BN>;
   static_assert(CL == 0 || CL == 2, "cluster modes: 0 (one CTA per tile) or 2 (pair MMAs)");
   static_assert(!GR || CL == 0, "grouped launches run one CTA per tile");
+  static_assert(!CS || (CL == 2 && BN == 256 && !GR), "staged C: pair MMAs on 256-wide tiles");
   constexpr bool PAIR = CT::kPair;
-  constexpr int kBxStages = CT::kStages, kBxStage = CT::kStage;
+  constexpr int kBxStages = BxSmem<CL, BN, CS>::kStages, kBxStage = CT::kStage;
   constexpr int kBxColsPerWarp = T::kCols;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem + kBxStages * kBxStage);
+  uint8_t *cslot = smem + kBxStages * kBxStage;  // CS: the two C slots
+  uint64_t *full = reinterpret_cast<uint64_t *>(cslot + (CS ? 2 * kCsSlotBytes : 0));
   uint64_t *empty = full + kBxStages;
   uint64_t *accf = empty + kBxStages;
   uint64_t *acce = accf + 2;
   uint64_t *done = acce + 2;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  // CS: slot c loaded (cfull), read by column block c (crel1) and by block c + 2 (crel2)
+  uint64_t *cfull = done + 1, *crel1 = cfull + 2, *crel2 = crel1 + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(crel2 + 2);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -583,6 +605,13 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       mbar_init(&acce[b], PAIR ? 2 * kBxEpiWarps : kBxEpiWarps);  // pair: both CTAs drain
     }
     mbar_init(done, 1);
+    if (CS) {
+      for (int c = 0; c < 2; ++c) {
+        mbar_init(&cfull[c], 1);  // the loading thread's expect_tx
+        mbar_init(&crel1[c], 4);  // the 4 warps of the column block that read it
+        mbar_init(&crel2[c], 4);
+      }
+    }
     *abort_flag = 0;
     fence_barrier_init();
     if (!GR) {
@@ -669,7 +698,8 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const unsigned segA = q.segA, segB = q.segB;
         int tm, tn;
         unit_tile(u, pi, tm, tn);
-        if (q.c_pf) tma_prefetch_l2_2d(&q.tmC, tm * kSplitBM, tn * BN);  // for its epilogue
+        if (q.c_pf)  // C of the tile, for its epilogue
+          for (int cb = 0; cb < BN / 64; ++cb) tma_prefetch_l2_2d(&q.tmC, tm * kSplitBM, tn * BN + cb * 64);
         int sg = 0, kk = 0;  // segment of block kb and the block within it
         for (int kb = 0; kb < kblocks; ++kb, ++L, ++kk) {
           if (kk == skb) { ++sg; kk = 0; }
@@ -764,6 +794,34 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     const int h = (warp - 2) >> 2;      // column block of the tile
     const int row_in_tile = q * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + h * kBxColsPerWarp;
+    // CS: column block h uses slot h & 1, after block h - 2 of this tile (h >= 2)
+    // or block h + 2 of the previous tile (h < 2) released it.  Each release
+    // barrier has one releasing block and one waiting block, so its phase t is
+    // tile t's and a waiter is never two phases ahead (as it could be on one
+    // barrier released by both blocks, when a warp of a block runs a tile
+    // ahead of another); the slot's loads alternate between the two blocks,
+    // so cfull's phases have fixed parities.
+    const int cs_slot = h & 1;
+    const uint32_t cs_second = (uint32_t)(h >> 1);
+    const float *cs_c = reinterpret_cast<const float *>(cslot + cs_slot * kCsSlotBytes);
+    const bool cs_loader = CS && q == 0 && lane == 0;
+    bool cs_pending = false;  // a load this thread issued whose slot is not yet read
+    uint32_t cs_tile = 0;     // tiles this CTA's epilogue has finished
+    // wait until the slot is free, then (one thread of the block) load the block's C
+    auto cs_load = [&](const Bf16xParams &pq, int tm, int tn) {
+      const bool freed =
+          cs_second ? mbar_wait(&crel1[cs_slot], cs_tile & 1u, p.err, kErrTimeoutAcc, abort_flag)
+                    : mbar_wait(&crel2[cs_slot], (cs_tile & 1u) ^ 1u, p.err, kErrTimeoutAcc,
+                                abort_flag);  // tile 0: the phase before the first, complete
+      if (!freed) return false;
+      if (cs_loader) {
+        mbar_arrive_expect_tx(&cfull[cs_slot], kCsSlotBytes);
+        tma_load_2d(const_cast<float *>(cs_c), &pq.tmC, tm * kSplitBM, tn * BN + h * 64,
+                    &cfull[cs_slot]);
+        cs_pending = true;
+      }
+      return true;
+    };
     uint32_t chunk = 0;
     bool ok = true;
     for (int u = first; u < nunits && ok; u += stride) {
@@ -772,6 +830,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       const int nchunks = GR ? nchunks_of(pq) : nchunks1;
       int tm, tn;
       unit_tile(u, pi, tm, tn);
+      if (CS && !cs_second && !cs_load(pq, tm, tn)) { ok = false; break; }  // under the MMAs
       float run[kBxColsPerWarp];
 #pragma unroll
       for (int j = 0; j < kBxColsPerWarp; ++j) run[j] = 0.f;
@@ -802,6 +861,14 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         }
       }
       if (!ok) break;
+      if (CS) {
+        if (cs_second && !cs_load(pq, tm, tn)) { ok = false; break; }
+        if (!mbar_wait(&cfull[cs_slot], cs_second, p.err, kErrTimeoutAcc, abort_flag)) {
+          ok = false;
+          break;
+        }
+        cs_pending = false;
+      }
       const int row = tm * kSplitBM + row_in_tile;
       if (row < pq.m) {
         const int col0 = tn * BN + h * kBxColsPerWarp;
@@ -816,7 +883,10 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int col = col0 + jb + j;
-            cv[j] = (col < pq.n) ? pq.C[(int64_t)col * pq.ldc + row] : 0.f;
+            if (CS)  // the slot holds the block's 64 columns x 128 rows, column-major
+              cv[j] = cs_c[(jb + j) * kSplitBM + row_in_tile];
+            else
+              cv[j] = (col < pq.n) ? pq.C[(int64_t)col * pq.ldc + row] : 0.f;
           }
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
@@ -832,7 +902,14 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           }
         }
       }
+      if (CS) {  // the block's 4 warps have read the slot
+        __syncwarp();
+        if (lane == 0) mbar_arrive(cs_second ? &crel2[cs_slot] : &crel1[cs_slot]);
+        ++cs_tile;
+      }
     }
+    // a load still in flight after a time-out lands before the CTA exits
+    if (cs_pending) mbar_wait_limit(&cfull[cs_slot], cs_second, GB300_SPIN_LIMIT, nullptr, 0);
   }
   tc_fence_before();
   __syncthreads();
@@ -1716,11 +1793,11 @@ static bool bf16x_maps(const Bf16xLayout &L, int h, int w, int k, CUtensorMap *t
          encode_3d(tB, L.Bp, 2, k, T, w, L.Kp, L.Kld, kSplitBK, 1, box_b);
 }
 
-// The L2 prefetch map of C in 128 x bn boxes, where C's base and column
+// The map of C in 128 x 64 boxes (L2 prefetch, staged C), where C's base and column
 // stride are 16-byte multiples (a tensor map's rule); else no prefetch.
-static void bf16x_c_prefetch(Bf16xParams &p, int bn) {
+static void bf16x_c_prefetch(Bf16xParams &p) {
   p.c_pf = ((uintptr_t)p.C % 16 == 0 && p.ldc % 4 == 0 &&
-            encode_2d(&p.tmC, p.C, 4, p.m, p.n, p.ldc, kSplitBM, bn, false))
+            encode_2d(&p.tmC, p.C, 4, p.m, p.n, p.ldc, kSplitBM, 64, false))
                ? 1
                : 0;
 }
@@ -1735,7 +1812,13 @@ static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, int tm, int tn, int
   CUtensorMap tA{}, tB{};
   if (!bf16x_maps(L, p.m, p.n, k, &tA, &tB, pair ? BN / 2 : BN)) return GB300_ERR_CUDA;
   p.tiles_n = (p.n + BN - 1) / BN;
-  bf16x_c_prefetch(p, BN);
+  bf16x_c_prefetch(p);
+  if constexpr (BN == 256) {
+    if (pair && p.c_pf && p.kblocks <= kBxStagedMaxKBlocks)  // short K: staged C
+      return persistent_launch<Bf16xParams>(
+          bf16x_gemm_kernel<0, F16, BN>, bf16x_gemm_kernel<2, F16, BN, false, true>, kBxThreads,
+          BxSmem<2, BN, true>::kBytes, tA, tB, p, p.tiles_m, p.tiles_n, true, st);
+  }
   return persistent_launch<Bf16xParams>(
       bf16x_gemm_kernel<0, F16, BN>, bf16x_gemm_kernel<2, F16, BN>, kBxThreads,
       pair ? ClusterTile<2, BN>::kSmem : ClusterTile<0, BN>::kSmem, tA, tB, p, p.tiles_m,
@@ -1872,7 +1955,7 @@ int bf16x_group_entry(int m, int n, int k, float alpha, float beta, float *C, in
   if (rc != GB300_OK) return rc;
   if (!bf16x_maps(L, m, n, k, &e.tmA, &e.tmB, kGroupBN)) return GB300_ERR_CUDA;
   e.prm.tiles_n = (n + kGroupBN - 1) / kGroupBN;
-  bf16x_c_prefetch(e.prm, kGroupBN);
+  bf16x_c_prefetch(e.prm);
   e.unit0 = unit0;
   *units = e.prm.tiles_m * e.prm.tiles_n;
   std::memcpy(entry, &e, sizeof(e));

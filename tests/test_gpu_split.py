@@ -291,3 +291,62 @@ def test_host_pointer_split_forms(orc, form):
     d = np.linalg.norm(C[:m].astype(np.float64) - truth) / np.linalg.norm(truth)
     assert d < (1e-6 if form == "bf16x" else 1e-15), d
     assert np.array_equal(C[m:], C0[m:])
+
+
+def staged_c_runs(orc, m, n, k, products, beta, seed):
+    """C = -op(A) op(B) + beta C with pair MMAs / aligned ldc, one CTA per tile /
+    aligned ldc and pair MMAs / odd ldc (256-wide tiles); the m x n results."""
+    A = orc.uniform((m, k), np.float32, seed, 0)
+    B = orc.uniform((n, k), np.float32, seed, 1)
+    C0 = orc.uniform((m, n), np.float32, seed, 2)
+    C0[7, 3], C0[250, 400], C0[0, n - 1] = np.nan, np.inf, -0.0
+    dA, dB = to_dev(A), to_dev(B)
+    ld4 = ru(m, 4) + 4
+    outs = []
+    try:
+        assert g.tune_param(g.TUNE_TILE_N, 256) == g.OK
+        for mode, ldc in ((1, ld4), (2, ld4), (1, ld4 - 1)):
+            assert g.tune_param(g.TUNE_PAIR_MMA, mode) == g.OK
+            C = np.full((ldc, n), 3.25, np.float32, order="F")
+            C[:m] = C0
+            dC = to_dev(C)
+            assert g.sgemm_bf16x("N", "T", m, n, k, -1.0, dA.data_ptr(), m, dB.data_ptr(), n, beta,
+                                 dC.data_ptr(), ldc, products=products) == g.OK
+            sync()
+            got = from_dev(dC, ldc)
+            assert np.all(got[m:] == 3.25)
+            outs.append(got[:m])
+            del dC
+    finally:
+        g.tune_param(g.TUNE_PAIR_MMA, 0)
+        g.tune_param(g.TUNE_TILE_N, 0)
+    return outs
+
+
+@pytest.mark.parametrize("products,k", [(6, 256), (3, 100), (g.FP16X3, 256), (6, 700)])
+@pytest.mark.parametrize("beta", [1.0, 0.0, 0.5])
+def test_bf16x_staged_c_bitexact(orc, products, k, beta):
+    """Short K (at most 48 K blocks a tile) with pair MMAs, 256-wide tiles and a
+    C whose base and column stride are 16-byte multiples: the epilogue reads C
+    from shared memory, loaded by TMA.  Its results equal bit for bit those of
+    the kernels that read C with plain loads (one CTA per tile; or an odd ldc,
+    which no tensor map can describe), NaN and Inf entries of C included, and
+    the rows of C past m stay untouched.  k = 700 with 6 products (66 K blocks)
+    takes the plain-load path in every mode."""
+    outs = staged_c_runs(orc, 300, 520, k, products, beta, 31)
+    for o in outs[1:]:
+        assert np.array_equal(outs[0].view(np.uint32), o.view(np.uint32))
+    assert np.isnan(outs[0][7, 3])   # beta * NaN, whatever beta
+    assert g.device_error() == 0
+
+
+@pytest.mark.parametrize("products", [6, g.FP16X3])
+def test_bf16x_staged_c_many_tiles(orc, products):
+    """The staged-C epilogue over about four tiles per CTA (4100 x 3900, k = 256:
+    272 row-tile pairs x column tiles on 74 clusters), where each C slot is
+    loaded, read and released again tile after tile: bit-identical to the
+    plain-load kernels."""
+    outs = staged_c_runs(orc, 4100, 3900, 256, products, 1.0, 32)
+    for o in outs[1:]:
+        assert np.array_equal(outs[0].view(np.uint32), o.view(np.uint32))
+    assert g.device_error() == 0
