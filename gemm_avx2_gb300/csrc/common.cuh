@@ -166,6 +166,26 @@ __device__ __forceinline__ void tma_prefetch_l2_2d(const void *tmap, int32_t x, 
                "r"(x), "r"(y)
                : "memory");
 }
+// 2-D tiled store of the box at (x, y) from this CTA's shared memory (parts
+// outside the tensor are not written), then the bulk-group bookkeeping: commit
+// the stores issued so far, wait until they have read shared memory, or until
+// they are complete.
+__device__ __forceinline__ void tma_store_2d(const void *tmap, const void *smem_src, int32_t x,
+                                             int32_t y) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   tmap),
+               "r"(x), "r"(y), "r"(smem_u32(smem_src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read0() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait0() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
 // Shared::cluster address of `p` (this CTA's shared memory) as seen in CTA `rank`.
 __device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
   uint32_t a;

@@ -550,10 +550,12 @@ struct ClusterTile {
 // Staged C (kernel CS = true; pair MMAs, 256-wide tiles): the epilogue's plain
 // loads of C, a few per thread in flight, took 10.5 us of a rank-256 tile's
 // 14.5 (a timeline of one CTA; 3.3 us without them), longer than the tile's
-// MMAs.  So C comes in by TMA instead: two shared-memory slots of 128 rows x
-// 64 columns (the columns of one group of 4 epilogue warps) in place of one
-// ring stage.  Column blocks 0 and 1 of a tile load theirs as the tile
-// starts, under its MMAs; blocks 2 and 3 reuse the slots after them.
+// MMAs.  So C moves by TMA instead: two shared-memory slots of 128 rows x 64
+// columns (the columns of one group of 4 epilogue warps) in place of one ring
+// stage.  Column blocks 0 and 1 of a tile load theirs as the tile starts,
+// under its MMAs; the warps write the results back into the slot and one TMA
+// store takes them to C; blocks 2 and 3 reuse the slots once those stores
+// have read them.
 constexpr int kCsSlotBytes = kSplitBM * 64 * 4;
 template <int CL, int BN, bool CS>
 struct BxSmem {
@@ -589,9 +591,10 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   uint64_t *accf = empty + kBxStages;
   uint64_t *acce = accf + 2;
   uint64_t *done = acce + 2;
-  // CS: slot c loaded (cfull), read by column block c (crel1) and by block c + 2 (crel2)
-  uint64_t *cfull = done + 1, *crel1 = cfull + 2, *crel2 = crel1 + 2;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(crel2 + 2);
+  // CS: slot c loaded (cfull), stored from for column block c (crel1) and for
+  // block c + 2 (crel2); column block h's results written into its slot (cwr)
+  uint64_t *cfull = done + 1, *crel1 = cfull + 2, *crel2 = crel1 + 2, *cwr = crel2 + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cwr + 4);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -608,9 +611,10 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     if (CS) {
       for (int c = 0; c < 2; ++c) {
         mbar_init(&cfull[c], 1);  // the loading thread's expect_tx
-        mbar_init(&crel1[c], 4);  // the 4 warps of the column block that read it
-        mbar_init(&crel2[c], 4);
+        mbar_init(&crel1[c], 1);  // the storing thread, once its store has read the slot
+        mbar_init(&crel2[c], 1);
       }
+      for (int c = 0; c < 4; ++c) mbar_init(&cwr[c], 4);  // the block's 4 warps
     }
     *abort_flag = 0;
     fence_barrier_init();
@@ -897,19 +901,38 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
               // beta C + alpha v rounded as written (no contraction: every
               // instantiation and the grouped launch round alike)
               const float cb = (pq.beta == 1.0f) ? cv[j] : __fmul_rn(cv[j], pq.beta);
-              pq.C[(int64_t)col * pq.ldc + row] = __fadd_rn(cb, __fmul_rn(pq.alpha, v));
+              const float r = __fadd_rn(cb, __fmul_rn(pq.alpha, v));
+              if (CS)
+                const_cast<float *>(cs_c)[(jb + j) * kSplitBM + row_in_tile] = r;
+              else
+                pq.C[(int64_t)col * pq.ldc + row] = r;
             }
           }
         }
       }
-      if (CS) {  // the block's 4 warps have read the slot
+      if (CS) {
+        // the block's results are in the slot (visible to the async proxy):
+        // one thread stores them and frees the slot once the store has read it
+        fence_proxy_async();
         __syncwarp();
-        if (lane == 0) mbar_arrive(cs_second ? &crel2[cs_slot] : &crel1[cs_slot]);
+        if (lane == 0) mbar_arrive(&cwr[h]);
+        if (cs_loader) {
+          if (mbar_wait(&cwr[h], cs_tile & 1u, p.err, kErrTimeoutAcc, abort_flag)) {
+            tma_store_2d(&pq.tmC, cs_c, tm * kSplitBM, tn * BN + h * 64);
+            bulk_commit();
+            bulk_wait_read0();
+          } else {
+            ok = false;
+          }
+          mbar_arrive(cs_second ? &crel2[cs_slot] : &crel1[cs_slot]);
+        }
         ++cs_tile;
       }
     }
-    // a load still in flight after a time-out lands before the CTA exits
+    // a load still in flight after a time-out lands before the CTA exits, and
+    // the last stores are complete
     if (cs_pending) mbar_wait_limit(&cfull[cs_slot], cs_second, GB300_SPIN_LIMIT, nullptr, 0);
+    if (CS && cs_loader) bulk_wait0();
   }
   tc_fence_before();
   __syncthreads();
