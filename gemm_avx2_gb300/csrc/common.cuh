@@ -177,6 +177,29 @@ __device__ __forceinline__ void tma_store_2d(const void *tmap, const void *smem_
                "r"(x), "r"(y), "r"(smem_u32(smem_src))
                : "memory");
 }
+// The same, with an L2 policy (l2_evict_first()): for data read or written
+// once, so that it leaves L2 before the operands that other tiles re-read.
+__device__ __forceinline__ void tma_store_2d_hint(const void *tmap, const void *smem_src, int32_t x,
+                                                  int32_t y, uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group.L2::cache_hint [%0, {%1, %2}], [%3], "
+      "%4;" ::"l"(tmap),
+      "r"(x), "r"(y), "r"(smem_u32(smem_src)), "l"(policy)
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_2d_hint(void *smem_dst, const void *tmap, int32_t x,
+                                                 int32_t y, uint64_t *bar, uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_"
+      "hint [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(smem_dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
 __device__ __forceinline__ void bulk_commit() {
   asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }

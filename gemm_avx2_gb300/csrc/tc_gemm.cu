@@ -820,8 +820,8 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       if (!freed) return false;
       if (cs_loader) {
         mbar_arrive_expect_tx(&cfull[cs_slot], kCsSlotBytes);
-        tma_load_2d(const_cast<float *>(cs_c), &pq.tmC, tm * kSplitBM, tn * BN + h * 64,
-                    &cfull[cs_slot]);
+        tma_load_2d_hint(const_cast<float *>(cs_c), &pq.tmC, tm * kSplitBM, tn * BN + h * 64,
+                         &cfull[cs_slot], l2_evict_first());
         cs_pending = true;
       }
       return true;
@@ -918,7 +918,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         if (lane == 0) mbar_arrive(&cwr[h]);
         if (cs_loader) {
           if (mbar_wait(&cwr[h], cs_tile & 1u, p.err, kErrTimeoutAcc, abort_flag)) {
-            tma_store_2d(&pq.tmC, cs_c, tm * kSplitBM, tn * BN + h * 64);
+            tma_store_2d_hint(&pq.tmC, cs_c, tm * kSplitBM, tn * BN + h * 64, l2_evict_first());
             bulk_commit();
             bulk_wait_read0();
           } else {
