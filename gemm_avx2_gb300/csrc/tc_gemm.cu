@@ -566,6 +566,12 @@ struct BxSmem {
 // Staged C for tiles of at most this many K blocks (MMAs shorter than the C
 // update they have to hide; 24 at k = 256 with 6 products).
 constexpr int kBxStagedMaxKBlocks = 48;
+// Row-tile pairs in a group of the staged-C kernel's raster (8 otherwise):
+// short K leaves each A' row panel small enough (1.5 MB a pair at k = 256)
+// for a larger group to stay in L2 while B' is swept once per group
+// (rank-256 SGEMM, one box: 8 -> 221.1, 16 -> 237.3, 32 -> 231.9, 64 -> 232.2
+// TFLOP/s).
+constexpr int kCsGroupM = 16;
 
 // GR: a grouped launch over the problems of p.grp (one CTA per tile; the
 // kernel parameters' maps are unused), each unit a tile of one problem, with
@@ -668,7 +674,8 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       tile_coords(u - grp[i].unit0, q.tiles_m, q.tiles_n, kSplitGroupM, tm, tn);
     } else {
       int um;
-      tile_coords(u, pm, p.tiles_n, PAIR ? kSplitGroupM / 2 : kSplitGroupM, um, tn);
+      tile_coords(u, pm, p.tiles_n, CS ? kCsGroupM : PAIR ? kSplitGroupM / 2 : kSplitGroupM, um,
+                  tn);
       tm = PAIR ? 2 * um + (int)rank : um;  // PAIR: a row tile past the end is zero-filled, not stored
     }
   };
