@@ -564,7 +564,8 @@ struct BxSmem {
                                 1024 + 256;
 };
 // Staged C for tiles of at most this many K blocks (MMAs shorter than the C
-// update they have to hide; 24 at k = 256 with 6 products).
+// update they have to hide; 24 at k = 256 with 6 products), and for C
+// windows whose rows fill whole 16-byte units (m a multiple of 4).
 constexpr int kBxStagedMaxKBlocks = 48;
 // Row-tile pairs in a group of the staged-C kernel's raster (8 otherwise):
 // short K leaves each A' row panel small enough (1.5 MB a pair at k = 256)
@@ -1844,7 +1845,10 @@ static int bf16x_launch(const Bf16xLayout &L, Bf16xParams p, int tm, int tn, int
   p.tiles_n = (p.n + BN - 1) / BN;
   bf16x_c_prefetch(p);
   if constexpr (BN == 256) {
-    if (pair && p.c_pf && p.kblocks <= kBxStagedMaxKBlocks)  // short K: staged C
+    // short K: staged C; m a multiple of 4, because the TMA store of a box
+    // clips the rows at 16 bytes (an m x n map with m = 170 wrote rows 170 and
+    // 171 of the ld padding), while the plain epilogue stores row by row
+    if (pair && p.c_pf && p.m % 4 == 0 && p.kblocks <= kBxStagedMaxKBlocks)
       return persistent_launch<Bf16xParams>(
           bf16x_gemm_kernel<0, F16, BN>, bf16x_gemm_kernel<2, F16, BN, false, true>, kBxThreads,
           BxSmem<2, BN, true>::kBytes, tA, tB, p, p.tiles_m, p.tiles_n, true, st);

@@ -331,9 +331,14 @@ def test_bf16x_staged_c_bitexact(orc, products, k, beta):
     from shared memory, loaded by TMA.  Its results equal bit for bit those of
     the kernels that read C with plain loads (one CTA per tile; or an odd ldc,
     which no tensor map can describe), NaN and Inf entries of C included, and
-    the rows of C past m stay untouched.  k = 700 with 6 products (66 K blocks)
-    takes the plain-load path in every mode."""
+    the rows of C past m stay untouched.  k = 700 with 6 products (66 K blocks),
+    and m = 298, take the plain-load path in every mode."""
     outs = staged_c_runs(orc, 300, 520, k, products, beta, 31)
+    for o in outs[1:]:
+        assert np.array_equal(outs[0].view(np.uint32), o.view(np.uint32))
+    # m = 298: rows not a multiple of 16 bytes take the plain-load epilogue
+    # (a TMA store of the last row tile would write 2 rows of the ld padding)
+    outs = staged_c_runs(orc, 298, 520, k, products, beta, 33)
     for o in outs[1:]:
         assert np.array_equal(outs[0].view(np.uint32), o.view(np.uint32))
     assert np.isnan(outs[0][7, 3])   # beta * NaN, whatever beta
