@@ -710,7 +710,11 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const unsigned segA = q.segA, segB = q.segB;
         int tm, tn;
         unit_tile(u, pi, tm, tn);
-        if (q.c_pf)  // C of the tile, for its epilogue
+        // C of the tile into L2 for its epilogue, where the tile's MMAs are
+        // too short to hide the C reads (a long tile's prefetched C only
+        // displaces operands: SGEMM TN 8192^3 read 5.35-5.58 GB a launch with
+        // it, 4.85-5.39 without)
+        if (q.c_pf && q.kblocks <= kBxStagedMaxKBlocks)
           for (int cb = 0; cb < BN / 64; ++cb) tma_prefetch_l2_2d(&q.tmC, tm * kSplitBM, tn * BN + cb * 64);
         int sg = 0, kk = 0;  // segment of block kb and the block within it
         for (int kb = 0; kb < kblocks; ++kb, ++L, ++kk) {
