@@ -550,17 +550,18 @@ struct ClusterTile {
 // Staged C (kernel CS = true; pair MMAs, 256-wide tiles): the epilogue's plain
 // loads of C, a few per thread in flight, took 10.5 us of a rank-256 tile's
 // 14.5 (a timeline of one CTA; 3.3 us without them), longer than the tile's
-// MMAs.  So C moves by TMA instead: two shared-memory slots of 128 rows x 64
-// columns (the columns of one group of 4 epilogue warps) in place of one ring
-// stage.  Column blocks 0 and 1 of a tile load theirs as the tile starts,
-// under its MMAs; the warps write the results back into the slot and one TMA
-// store takes them to C; blocks 2 and 3 reuse the slots once those stores
-// have read them.
-constexpr int kCsSlotBytes = kSplitBM * 64 * 4;
+// MMAs.  So C moves by TMA instead: in place of one ring stage, a shared-memory
+// slot of 128 rows x 32 columns for each column block (the 4 epilogue warps
+// of 64 columns).  Each block loads the first half of its C as the tile
+// starts, under its MMAs; its warps write the results back into the slot and
+// one TMA store takes them to C; the second half follows in the same slot
+// once that store has read it.  (Two 64-column slots shared by the blocks
+// kept blocks 2 and 3 waiting for blocks 0 and 1: 5.7 us against 1.4 us.)
+constexpr int kCsSlotBytes = kSplitBM * 32 * 4;
 template <int CL, int BN, bool CS>
 struct BxSmem {
   static constexpr int kStages = CS ? ClusterTile<CL, BN>::kStages - 1 : ClusterTile<CL, BN>::kStages;
-  static constexpr int kBytes = kStages * ClusterTile<CL, BN>::kStage + (CS ? 2 * kCsSlotBytes : 0) +
+  static constexpr int kBytes = kStages * ClusterTile<CL, BN>::kStage + (CS ? 4 * kCsSlotBytes : 0) +
                                 1024 + 256;
 };
 // Staged C for tiles of at most this many K blocks (MMAs shorter than the C
@@ -592,16 +593,16 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
-  uint8_t *cslot = smem + kBxStages * kBxStage;  // CS: the two C slots
-  uint64_t *full = reinterpret_cast<uint64_t *>(cslot + (CS ? 2 * kCsSlotBytes : 0));
+  uint8_t *cslot = smem + kBxStages * kBxStage;  // CS: the C slots of the 4 column blocks
+  uint64_t *full = reinterpret_cast<uint64_t *>(cslot + (CS ? 4 * kCsSlotBytes : 0));
   uint64_t *empty = full + kBxStages;
   uint64_t *accf = empty + kBxStages;
   uint64_t *acce = accf + 2;
   uint64_t *done = acce + 2;
-  // CS: slot c loaded (cfull), stored from for column block c (crel1) and for
-  // block c + 2 (crel2); column block h's results written into its slot (cwr)
-  uint64_t *cfull = done + 1, *crel1 = cfull + 2, *crel2 = crel1 + 2, *cwr = crel2 + 2;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cwr + 4);
+  // CS, per column block: its slot loaded (cfull), its results written into
+  // the slot (cwr), the slot read by their store (crel); two phases a tile each
+  uint64_t *cfull = done + 1, *cwr = cfull + (CS ? 4 : 0), *crel = cwr + (CS ? 4 : 0);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(crel + (CS ? 4 : 0));
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -616,12 +617,11 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     }
     mbar_init(done, 1);
     if (CS) {
-      for (int c = 0; c < 2; ++c) {
+      for (int c = 0; c < 4; ++c) {
         mbar_init(&cfull[c], 1);  // the loading thread's expect_tx
-        mbar_init(&crel1[c], 1);  // the storing thread, once its store has read the slot
-        mbar_init(&crel2[c], 1);
+        mbar_init(&cwr[c], 4);    // the block's 4 warps
+        mbar_init(&crel[c], 1);   // the storing thread, once its store has read the slot
       }
-      for (int c = 0; c < 4; ++c) mbar_init(&cwr[c], 4);  // the block's 4 warps
     }
     *abort_flag = 0;
     fence_barrier_init();
@@ -715,7 +715,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         // displaces operands: SGEMM TN 8192^3 read 5.35-5.58 GB a launch with
         // it, 4.85-5.39 without)
         if (q.c_pf && q.kblocks <= kBxStagedMaxKBlocks)
-          for (int cb = 0; cb < BN / 64; ++cb) tma_prefetch_l2_2d(&q.tmC, tm * kSplitBM, tn * BN + cb * 64);
+          for (int cb = 0; cb < BN / 32; ++cb) tma_prefetch_l2_2d(&q.tmC, tm * kSplitBM, tn * BN + cb * 32);
         int sg = 0, kk = 0;  // segment of block kb and the block within it
         for (int kb = 0; kb < kblocks; ++kb, ++L, ++kk) {
           if (kk == skb) { ++sg; kk = 0; }
@@ -810,33 +810,18 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     const int h = (warp - 2) >> 2;      // column block of the tile
     const int row_in_tile = q * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + h * kBxColsPerWarp;
-    // CS: column block h uses slot h & 1, after block h - 2 of this tile (h >= 2)
-    // or block h + 2 of the previous tile (h < 2) released it.  Each release
-    // barrier has one releasing block and one waiting block, so its phase t is
-    // tile t's and a waiter is never two phases ahead (as it could be on one
-    // barrier released by both blocks, when a warp of a block runs a tile
-    // ahead of another); the slot's loads alternate between the two blocks,
-    // so cfull's phases have fixed parities.
-    const int cs_slot = h & 1;
-    const uint32_t cs_second = (uint32_t)(h >> 1);
-    const float *cs_c = reinterpret_cast<const float *>(cslot + cs_slot * kCsSlotBytes);
+    // CS: column block h's slot holds half of its columns at a time.  Its
+    // barriers move two phases a tile (first half, second half), and every
+    // wait comes after the block's own arrival on the phase before, so the
+    // parities are fixed: no waiter can be two phases ahead.
+    float *cs_c = reinterpret_cast<float *>(cslot + h * kCsSlotBytes);
     const bool cs_loader = CS && q == 0 && lane == 0;
-    bool cs_pending = false;  // a load this thread issued whose slot is not yet read
-    uint32_t cs_tile = 0;     // tiles this CTA's epilogue has finished
-    // wait until the slot is free, then (one thread of the block) load the block's C
-    auto cs_load = [&](const Bf16xParams &pq, int tm, int tn) {
-      const bool freed =
-          cs_second ? mbar_wait(&crel1[cs_slot], cs_tile & 1u, p.err, kErrTimeoutAcc, abort_flag)
-                    : mbar_wait(&crel2[cs_slot], (cs_tile & 1u) ^ 1u, p.err, kErrTimeoutAcc,
-                                abort_flag);  // tile 0: the phase before the first, complete
-      if (!freed) return false;
-      if (cs_loader) {
-        mbar_arrive_expect_tx(&cfull[cs_slot], kCsSlotBytes);
-        tma_load_2d_hint(const_cast<float *>(cs_c), &pq.tmC, tm * kSplitBM, tn * BN + h * 64,
-                         &cfull[cs_slot], l2_evict_first());
-        cs_pending = true;
-      }
-      return true;
+    int cs_pending = -1;  // the half whose load this thread issued and the block has not read
+    auto cs_load = [&](const Bf16xParams &pq, int tm, int tn, int half) {
+      mbar_arrive_expect_tx(&cfull[h], kCsSlotBytes);
+      tma_load_2d_hint(cs_c, &pq.tmC, tm * kSplitBM, tn * BN + h * 64 + half * 32, &cfull[h],
+                       l2_evict_first());
+      cs_pending = half;
     };
     uint32_t chunk = 0;
     bool ok = true;
@@ -846,7 +831,10 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       const int nchunks = GR ? nchunks_of(pq) : nchunks1;
       int tm, tn;
       unit_tile(u, pi, tm, tn);
-      if (CS && !cs_second && !cs_load(pq, tm, tn)) { ok = false; break; }  // under the MMAs
+      if (CS) {  // the first half of the block's C, under the MMAs, once the slot is free
+        if (!mbar_wait(&crel[h], 1u, p.err, kErrTimeoutAcc, abort_flag)) { ok = false; break; }
+        if (cs_loader) cs_load(pq, tm, tn, 0);
+      }
       float run[kBxColsPerWarp];
 #pragma unroll
       for (int j = 0; j < kBxColsPerWarp; ++j) run[j] = 0.f;
@@ -877,30 +865,24 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         }
       }
       if (!ok) break;
-      if (CS) {
-        if (cs_second && !cs_load(pq, tm, tn)) { ok = false; break; }
-        if (!mbar_wait(&cfull[cs_slot], cs_second, p.err, kErrTimeoutAcc, abort_flag)) {
-          ok = false;
-          break;
-        }
-        cs_pending = false;
-      }
       const int row = tm * kSplitBM + row_in_tile;
-      if (row < pq.m) {
-        const int col0 = tn * BN + h * kBxColsPerWarp;
-        // scaled FP16 form: the row and column scales come off here (a
-        // non-finite row or column is NaN already; its marker exponent is capped)
-        const int ea = F16 ? min(pq.expA[row], 1024) - 30 : 0;
-        // C in batches of 8 columns: all loads of a batch are issued before its
-        // stores, so the batch pays one memory latency instead of eight
+      const int col0 = tn * BN + h * kBxColsPerWarp;
+      // scaled FP16 form: the row and column scales come off here (a non-finite
+      // row or column is NaN already; its marker exponent is capped)
+      const int ea = (F16 && row < pq.m) ? min(pq.expA[row], 1024) - 30 : 0;
+      // beta C + alpha v for the columns [c0, c1) of the warp, rounded as
+      // written (no contraction: every instantiation and the grouped launch
+      // round alike); C from the slot (CS) or from memory in batches of 8
+      // columns, all loads of a batch before its stores
+      auto update = [&](int c0, int c1) {
 #pragma unroll
-        for (int jb = 0; jb < kBxColsPerWarp; jb += 8) {
+        for (int jb = c0; jb < c1; jb += 8) {
           float cv[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int col = col0 + jb + j;
-            if (CS)  // the slot holds the block's 64 columns x 128 rows, column-major
-              cv[j] = cs_c[(jb + j) * kSplitBM + row_in_tile];
+            if (CS)  // the slot holds 32 columns x 128 rows, column-major
+              cv[j] = cs_c[(jb - c0 + j) * kSplitBM + row_in_tile];
             else
               cv[j] = (col < pq.n) ? pq.C[(int64_t)col * pq.ldc + row] : 0.f;
           }
@@ -910,40 +892,59 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             if (col < pq.n) {
               const float v =
                   F16 ? scale_pow2f(run[jb + j], ea + min(pq.expB[col], 1024)) : run[jb + j];
-              // beta C + alpha v rounded as written (no contraction: every
-              // instantiation and the grouped launch round alike)
               const float cb = (pq.beta == 1.0f) ? cv[j] : __fmul_rn(cv[j], pq.beta);
               const float r = __fadd_rn(cb, __fmul_rn(pq.alpha, v));
               if (CS)
-                const_cast<float *>(cs_c)[(jb + j) * kSplitBM + row_in_tile] = r;
+                cs_c[(jb - c0 + j) * kSplitBM + row_in_tile] = r;
               else
                 pq.C[(int64_t)col * pq.ldc + row] = r;
             }
           }
         }
-      }
-      if (CS) {
-        // the block's results are in the slot (visible to the async proxy):
-        // one thread stores them and frees the slot once the store has read it
-        fence_proxy_async();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&cwr[h]);
-        if (cs_loader) {
-          if (mbar_wait(&cwr[h], cs_tile & 1u, p.err, kErrTimeoutAcc, abort_flag)) {
-            tma_store_2d_hint(&pq.tmC, cs_c, tm * kSplitBM, tn * BN + h * 64, l2_evict_first());
-            bulk_commit();
-            bulk_wait_read0();
-          } else {
+      };
+      if constexpr (CS) {
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          // the second half's load follows the first half's store (crel phase 0)
+          if (half == 1 && !mbar_wait(&crel[h], 0u, p.err, kErrTimeoutAcc, abort_flag)) {
             ok = false;
+            break;
           }
-          mbar_arrive(cs_second ? &crel2[cs_slot] : &crel1[cs_slot]);
+          if (!mbar_wait(&cfull[h], (uint32_t)half, p.err, kErrTimeoutAcc, abort_flag)) {
+            ok = false;
+            break;
+          }
+          cs_pending = -1;
+          if (row < pq.m) update(half * 32, half * 32 + 32);
+          // the results are in the slot (visible to the async proxy): one
+          // thread stores them, frees the slot once the store has read it and
+          // loads the second half
+          fence_proxy_async();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&cwr[h]);
+          if (cs_loader) {
+            if (mbar_wait(&cwr[h], (uint32_t)half, p.err, kErrTimeoutAcc, abort_flag)) {
+              tma_store_2d_hint(&pq.tmC, cs_c, tm * kSplitBM, tn * BN + h * 64 + half * 32,
+                                l2_evict_first());
+              bulk_commit();
+              bulk_wait_read0();
+              mbar_arrive(&crel[h]);
+              if (half == 0) cs_load(pq, tm, tn, 1);
+            } else {
+              ok = false;
+              mbar_arrive(&crel[h]);
+              break;
+            }
+          }
         }
-        ++cs_tile;
+      } else {
+        if (row < pq.m) update(0, kBxColsPerWarp);
       }
     }
     // a load still in flight after a time-out lands before the CTA exits, and
     // the last stores are complete
-    if (cs_pending) mbar_wait_limit(&cfull[cs_slot], cs_second, GB300_SPIN_LIMIT, nullptr, 0);
+    if (cs_pending >= 0)
+      mbar_wait_limit(&cfull[h], (uint32_t)cs_pending, GB300_SPIN_LIMIT, nullptr, 0);
     if (CS && cs_loader) bulk_wait0();
   }
   tc_fence_before();
@@ -1828,11 +1829,11 @@ static bool bf16x_maps(const Bf16xLayout &L, int h, int w, int k, CUtensorMap *t
          encode_3d(tB, L.Bp, 2, k, T, w, L.Kp, L.Kld, kSplitBK, 1, box_b);
 }
 
-// The map of C in 128 x 64 boxes (L2 prefetch, staged C), where C's base and column
+// The map of C in 128 x 32 boxes (L2 prefetch, staged C), where C's base and column
 // stride are 16-byte multiples (a tensor map's rule); else no prefetch.
 static void bf16x_c_prefetch(Bf16xParams &p) {
   p.c_pf = ((uintptr_t)p.C % 16 == 0 && p.ldc % 4 == 0 &&
-            encode_2d(&p.tmC, p.C, 4, p.m, p.n, p.ldc, kSplitBM, 64, false))
+            encode_2d(&p.tmC, p.C, 4, p.m, p.n, p.ldc, kSplitBM, 32, false))
                ? 1
                : 0;
 }
