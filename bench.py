@@ -1054,13 +1054,21 @@ def run_trsm(args, torch, rank, world):
         R = Al @ X - w["alpha"] * Bc
         return float(np.linalg.norm(R) / (np.linalg.norm(Al) * np.linalg.norm(X)))
 
-    res = {"plain": residual(0), "split": residual(1)}
+    # FP64 updates on the Ozaki slices (form 1) and on the CRT form (form 2),
+    # the faster reported; FP32 on 6xBF16
+    split_forms = [1, 2] if p == "d" else [1]
+    form_names = {1: "Ozaki slices" if p == "d" else "6xBF16", 2: "CRT"}
+    res = {"plain": residual(0)}
+    for f in split_forms:
+        res["split" if f == 1 else "crt"] = residual(f)
     sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
     if sampler:
         sampler.start()
         time.sleep(0.3)
     barrier(torch, world)
-    ms_split = timed(1, args.steps, args.warmup)
+    ms_by_form = {f: timed(f, args.steps, args.warmup) for f in split_forms}
+    best = min(ms_by_form, key=ms_by_form.get)
+    ms_split = ms_by_form[best]
     ms_plain = timed(0, max(3, args.steps // 2), args.warmup)
     barrier(torch, world)
     clocks = sampler.stop() if sampler else None
@@ -1075,7 +1083,8 @@ def run_trsm(args, torch, rank, world):
         "config": {"workload": args.workload, "side": "L", "uplo": "L", "transa": "N",
                    "diag": "N", "m": m, "n": n, "alpha": w["alpha"], "flops_per_call": "m^2 n",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "form": {"name": "split updates (%s)" % ("Ozaki slices" if p == "d" else "6xBF16")},
+        "form": {"name": "split updates (%s)" % form_names[best],
+                 "ms_by_form": {form_names[f]: round(v, 3) for f, v in ms_by_form.items()}},
         "plain": {"value": round(flops / (ms_plain / 1e3) / 1e12, 3), "unit": "TFLOP/s",
                   "ms": round(ms_plain, 3)},
         "accuracy": {"backward_residual": res, "columns": 64},

@@ -1444,7 +1444,7 @@ static int tr_api(int solve, char side, char uplo, char ta, char diag, int m, in
                   const T *A, int lda, T *B, int ldb, int form, void *stream) {
   const int ck = tr_check(side, uplo, ta, diag, m, n, lda, ldb);
   if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
-  if (form != 0 && form != 1) return GB300_ERR_ARG;
+  if (form < 0 || form > 2) return GB300_ERR_ARG;
   DeviceState *s = dev_state();
   if (!s) return GB300_ERR_CUDA;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -184,9 +184,12 @@ static int tr_gemm(int form, char t1, char t2, int mm, int nn, int kk, const T *
     if (form == 1)
       return ozaki_dgemm(t1, t2, mm, nn, kk, a, X, ldx, Y, ldy, 1.0, C, ldc, 0, ws, ws_bytes, st,
                          err);
+    if (form == 2)  // the CRT form, its moduli by shape class (16 untuned)
+      return crt_dgemm(t1, t2, mm, nn, kk, a, X, ldx, Y, ldy, 1.0, C, ldc, 0, ws, ws_bytes, st,
+                       err);
     return plain_dgemm(t1, t2, mm, nn, kk, a, X, ldx, Y, ldy, 1.0, C, ldc, st, err);
   } else {
-    if (form == 1)
+    if (form == 1 || form == 2)
       return split_sgemm(t1, t2, mm, nn, kk, a, X, ldx, Y, ldy, 1.0f, C, ldc, 6, ws, ws_bytes, st,
                          err);
     return plain_sgemm(t1, t2, mm, nn, kk, a, X, ldx, Y, ldy, 1.0f, C, ldc, st, err);
@@ -194,14 +197,15 @@ static int tr_gemm(int form, char t1, char t2, int mm, int nn, int kk, const T *
 }
 
 size_t tr_workspace_bytes(int is_double, int form, int m, int n) {
-  if (form != 1 || m <= 0 || n <= 0) return 0;
+  if ((form != 1 && form != 2) || m <= 0 || n <= 0) return 0;
   // The off-diagonal updates are at most (m x n x 64) for TRSM and
   // (64 x n x m) / (m x 64 x n) for TRMM (left / right): size for the largest.
   const int shapes[4][3] = {{m, n, kTrNb}, {kTrNb, n, m}, {m, kTrNb, n}, {m, n, kTrNb}};
   size_t need = 0;
   for (const auto &sh : shapes) {
-    const size_t w = is_double ? split_workspace_bytes(1, sh[0], sh[1], sh[2], 0)
-                               : split_workspace_bytes(0, sh[0], sh[1], sh[2], 6);
+    const size_t w = !is_double  ? split_workspace_bytes(0, sh[0], sh[1], sh[2], 6)
+                     : form == 2 ? crt_workspace_bytes(sh[0], sh[1], sh[2], 0)
+                                 : split_workspace_bytes(1, sh[0], sh[1], sh[2], 0);
     if (w > need) need = w;
   }
   return need;
@@ -223,8 +227,8 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
               cudaStream_t st, unsigned *err) {
   const int ck = tr_check(side, uplo, transa, diag, m, n, lda, ldb);
   if (ck != GB300_OK) return ck < 0 ? GB300_OK : ck;
-  if (form != 0 && form != 1) return GB300_ERR_ARG;
-  if (form == 1 && (!ws || ws_bytes < tr_workspace_bytes(sizeof(T) == 8, form, m, n)))
+  if (form < 0 || form > 2) return GB300_ERR_ARG;
+  if (form != 0 && (!ws || ws_bytes < tr_workspace_bytes(sizeof(T) == 8, form, m, n)))
     return GB300_ERR_WORKSPACE;
   const bool left = side == 'L' || side == 'l';
   const bool trans = !(transa == 'N' || transa == 'n');

@@ -252,7 +252,8 @@ int gb300_grouped_graph_destroy(gb300_grouped_graph graph);
  * A is m x m ('L') or n x n ('R'), triangle uplo 'U'/'L', diag 'U' (unit) or
  * 'N'; op(A) = A for transa 'N', A^T for 'T'/'C'.  alpha == 0 sets B to zero.
  * form 0: off-diagonal updates with the plain GEMM; form 1: with the split
- * forms (Ozaki for FP64, 6xBF16 for FP32; library-owned workspace).  The
+ * forms (Ozaki slices for FP64, 6xBF16 for FP32; library-owned workspace);
+ * form 2: the CRT form for FP64 (as gb300_dgemm_ozaki2; 6xBF16 for FP32).  The
  * diagonal 64x64 blocks are solved / multiplied by a small CUDA kernel.
  * Device pointers, stream-ordered; GB300_ERR_ARG for invalid characters,
  * sizes or leading dimensions.

@@ -59,6 +59,19 @@ def test_split_form_updates(routine, prec):
     assert d < (1e-13 if prec == "d" else 2e-6), d
 
 
+@pytest.mark.parametrize("side,uplo,ta,diag", [("L", "L", "N", "N"), ("R", "U", "T", "U"),
+                                               ("L", "U", "T", "N"), ("R", "L", "N", "U")])
+@pytest.mark.parametrize("routine", ["trsm", "trmm"])
+def test_crt_form_updates_fp64(routine, side, uplo, ta, diag):
+    """form 2: FP64 off-diagonal updates on the CRT form (exact products of the
+    row / column scaled operands), ragged sizes over the 64-wide blocks and a
+    padded ldb that stays untouched; FP32 takes 6xBF16 as form 1."""
+    d = run(routine, "d", side, uplo, ta, diag, 300, 200, -0.75, 2, 11)
+    assert d < 1e-13, d
+    d = run(routine, "s", side, uplo, ta, diag, 170, 260, 0.5, 2, 12)
+    assert d < 2e-6, d
+
+
 def test_alpha_zero_and_args():
     B = np.full((8, 5), np.nan, order="F")
     A = np.eye(8, order="F")
@@ -70,6 +83,8 @@ def test_alpha_zero_and_args():
         g.ERR_ARG
     assert g.trsm("d", "L", "U", "N", "N", 8, 5, 1.0, dA.data_ptr(), 7, dB.data_ptr(), 8) == \
         g.ERR_ARG
+    assert g.trsm("d", "L", "U", "N", "N", 8, 5, 1.0, dA.data_ptr(), 8, dB.data_ptr(), 8,
+                  form=3) == g.ERR_ARG
 
 
 def test_golden_fixtures_from_reference_kernels():
