@@ -25,6 +25,11 @@
 namespace gb300 {
 
 constexpr int kTrNb = 64;     // diagonal block size
+// TRSM outer block: the 64-wide blocks inside it are solved with updates
+// confined to it, then one rank-256 update of everything after it, so the
+// full-size updates (and their C traffic or CRT reconstructions) are a
+// quarter as many as with a rank-64 update per diagonal block
+constexpr int kTrOuter = 256;
 constexpr int kTrCols = 128;  // right-hand sides per CTA of the diagonal kernels
 
 // op(A)(r, c) of the diagonal block starting at (d0, d0).
@@ -198,9 +203,9 @@ static int tr_gemm(int form, char t1, char t2, int mm, int nn, int kk, const T *
 
 size_t tr_workspace_bytes(int is_double, int form, int m, int n) {
   if ((form != 1 && form != 2) || m <= 0 || n <= 0) return 0;
-  // The off-diagonal updates are at most (m x n x 64) for TRSM and
+  // The off-diagonal updates are at most (m x n x 256) for TRSM and
   // (64 x n x m) / (m x 64 x n) for TRMM (left / right): size for the largest.
-  const int shapes[4][3] = {{m, n, kTrNb}, {kTrNb, n, m}, {m, kTrNb, n}, {m, n, kTrNb}};
+  const int shapes[4][3] = {{m, n, kTrOuter}, {kTrNb, n, m}, {m, kTrNb, n}, {m, n, kTrOuter}};
   size_t need = 0;
   for (const auto &sh : shapes) {
     const size_t w = !is_double  ? split_workspace_bytes(0, sh[0], sh[1], sh[2], 6)
@@ -264,33 +269,46 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
   // so that every block still reads unmodified rows / columns of B.
   const bool forward = left ? (solve ? lower : !lower) : (solve ? !lower : lower);
   int rc = GB300_OK;
-  for (int q = 0; q < nblk && rc == GB300_OK; ++q) {
+  // TRSM: the solved block [c0, c1) of X updates the rows (left) / columns
+  // (right) [r0, r1) still to solve: B(r, :) -= op(A)(r, c) X(c, :), or
+  // B(:, r) -= X(:, c) op(A)(c, r)
+  auto solve_update = [&](int r0, int r1, int c0, int c1) -> int {
+    if (r1 <= r0 || c1 <= c0) return GB300_OK;
+    if (left)
+      return tr_gemm<T>(form, tA, 'N', r1 - r0, n, c1 - c0, opA(r0, c0), lda, B + c0, ldb, B + r0,
+                        ldb, ws, ws_bytes, st, err);
+    return tr_gemm<T>(form, 'N', tA, m, r1 - r0, c1 - c0, B + (int64_t)c0 * ldb, ldb, opA(c0, r0),
+                      lda, B + (int64_t)r0 * ldb, ldb, ws, ws_bytes, st, err);
+  };
+  if (solve) {
+    // forward: the rows / columns still to solve follow the block, else precede it
+    const int nouter = (na + kTrOuter - 1) / kTrOuter;
+    for (int qo = 0; qo < nouter && rc == GB300_OK; ++qo) {
+      const int ob = forward ? qo : nouter - 1 - qo;
+      const int D0 = ob * kTrOuter, D1 = (na - D0) < kTrOuter ? na : D0 + kTrOuter;
+      const int ninner = (D1 - D0 + kTrNb - 1) / kTrNb;
+      for (int qi = 0; qi < ninner && rc == GB300_OK; ++qi) {
+        const int ib = forward ? qi : ninner - 1 - qi;
+        const int d0 = D0 + ib * kTrNb, nb = (D1 - d0) < kTrNb ? (D1 - d0) : kTrNb;
+        const int lo = d0 + nb;  // first index after the block
+        if (left)
+          diag_left_kernel<T><<<(n + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
+              A, lda, trans, lower, unit, d0, nb, B, ldb, n, 1);
+        else
+          diag_right_kernel<T><<<(m + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
+              A, lda, trans, lower, unit, d0, nb, B, ldb, m, 1);
+        rc = forward ? solve_update(lo, D1, d0, lo) : solve_update(D0, d0, d0, lo);
+        if (rc == GB300_OK && cudaGetLastError() != cudaSuccess) rc = GB300_ERR_CUDA;
+      }
+      if (rc == GB300_OK)
+        rc = forward ? solve_update(D1, na, D0, D1) : solve_update(0, D0, D0, D1);
+    }
+  }
+  for (int q = 0; !solve && q < nblk && rc == GB300_OK; ++q) {
     const int ib = forward ? q : nblk - 1 - q;
     const int d0 = ib * kTrNb, nb = (na - d0) < kTrNb ? (na - d0) : kTrNb;
     const int lo = d0 + nb;  // first index after the block
-    if (solve) {
-      if (left) {
-        diag_left_kernel<T><<<(n + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
-            A, lda, trans, lower, unit, d0, nb, B, ldb, n, 1);
-        // the rows still to solve: below the block (lower) or above it (upper)
-        if (lower)
-          rc = tr_gemm<T>(form, tA, 'N', m - lo, n, nb, opA(lo, d0), lda, B + d0, ldb, B + lo,
-                          ldb, ws, ws_bytes, st, err);
-        else
-          rc = tr_gemm<T>(form, tA, 'N', d0, n, nb, opA(0, d0), lda, B + d0, ldb, B, ldb, ws,
-                          ws_bytes, st, err);
-      } else {
-        diag_right_kernel<T><<<(m + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
-            A, lda, trans, lower, unit, d0, nb, B, ldb, m, 1);
-        // the columns still to solve: right of the block (upper) or left of it (lower)
-        if (!lower)
-          rc = tr_gemm<T>(form, 'N', tA, m, n - lo, nb, B + (int64_t)d0 * ldb, ldb, opA(d0, lo),
-                          lda, B + (int64_t)lo * ldb, ldb, ws, ws_bytes, st, err);
-        else
-          rc = tr_gemm<T>(form, 'N', tA, m, d0, nb, B + (int64_t)d0 * ldb, ldb, opA(d0, 0), lda,
-                          B, ldb, ws, ws_bytes, st, err);
-      }
-    } else {
+    {
       // multiply: block rows/cols of the result = diagonal part + off-diagonal part,
       // the off-diagonal part reading rows/columns of B not yet overwritten
       if (left) {
