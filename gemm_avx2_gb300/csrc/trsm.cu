@@ -25,11 +25,6 @@
 namespace gb300 {
 
 constexpr int kTrNb = 64;     // diagonal block size
-// TRSM outer block: the 64-wide blocks inside it are solved with updates
-// confined to it, then one rank-256 update of everything after it, so the
-// full-size updates (and their C traffic or CRT reconstructions) are a
-// quarter as many as with a rank-64 update per diagonal block
-constexpr int kTrOuter = 256;
 constexpr int kTrCols = 128;  // right-hand sides per CTA of the diagonal kernels
 
 // op(A)(r, c) of the diagonal block starting at (d0, d0).
@@ -203,9 +198,12 @@ static int tr_gemm(int form, char t1, char t2, int mm, int nn, int kk, const T *
 
 size_t tr_workspace_bytes(int is_double, int form, int m, int n) {
   if ((form != 1 && form != 2) || m <= 0 || n <= 0) return 0;
-  // The off-diagonal updates are at most (m x n x 256) for TRSM and
-  // (64 x n x m) / (m x 64 x n) for TRMM (left / right): size for the largest.
-  const int shapes[4][3] = {{m, n, kTrOuter}, {kTrNb, n, m}, {m, kTrNb, n}, {m, n, kTrOuter}};
+  // The off-diagonal updates are at most (m x n x half) for TRSM (half: the
+  // first half of the triangle, a multiple of 64) and (64 x n x m) / (m x 64 x
+  // n) for TRMM (left / right): size for the largest.
+  const int na = m > n ? m : n;
+  const int half = ((na + 1) / 2 + kTrNb - 1) / kTrNb * kTrNb;
+  const int shapes[4][3] = {{m, n, half}, {kTrNb, n, m}, {m, kTrNb, n}, {m, n, half}};
   size_t need = 0;
   for (const auto &sh : shapes) {
     const size_t w = !is_double  ? split_workspace_bytes(0, sh[0], sh[1], sh[2], 6)
@@ -280,30 +278,32 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
     return tr_gemm<T>(form, 'N', tA, m, r1 - r0, c1 - c0, B + (int64_t)c0 * ldb, ldb, opA(c0, r0),
                       lda, B + (int64_t)r0 * ldb, ldb, ws, ws_bytes, st, err);
   };
-  if (solve) {
-    // forward: the rows / columns still to solve follow the block, else precede it
-    const int nouter = (na + kTrOuter - 1) / kTrOuter;
-    for (int qo = 0; qo < nouter && rc == GB300_OK; ++qo) {
-      const int ob = forward ? qo : nouter - 1 - qo;
-      const int D0 = ob * kTrOuter, D1 = (na - D0) < kTrOuter ? na : D0 + kTrOuter;
-      const int ninner = (D1 - D0 + kTrNb - 1) / kTrNb;
-      for (int qi = 0; qi < ninner && rc == GB300_OK; ++qi) {
-        const int ib = forward ? qi : ninner - 1 - qi;
-        const int d0 = D0 + ib * kTrNb, nb = (D1 - d0) < kTrNb ? (D1 - d0) : kTrNb;
-        const int lo = d0 + nb;  // first index after the block
-        if (left)
-          diag_left_kernel<T><<<(n + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
-              A, lda, trans, lower, unit, d0, nb, B, ldb, n, 1);
-        else
-          diag_right_kernel<T><<<(m + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
-              A, lda, trans, lower, unit, d0, nb, B, ldb, m, 1);
-        rc = forward ? solve_update(lo, D1, d0, lo) : solve_update(D0, d0, d0, lo);
-        if (rc == GB300_OK && cudaGetLastError() != cudaSuccess) rc = GB300_ERR_CUDA;
-      }
-      if (rc == GB300_OK)
-        rc = forward ? solve_update(D1, na, D0, D1) : solve_update(0, D0, D0, D1);
+  // TRSM by recursive halving of the triangle: solve the first half, update
+  // the second half with it (one GEMM with k = the half), solve the second
+  // half; ranges of at most 64 go to the diagonal kernel.  The halves split at
+  // multiples of 64, so the diagonal blocks are those of a 64-blocked walk.
+  // Against a rank-64 update per diagonal block, the updates' C traffic (and
+  // the CRT form's reconstructions) fall from m^2 n / 128 elements to about
+  // n m log2(m / 64) / 2, and most of the flops run at long K.
+  auto solve_range = [&](auto &self, int D0, int D1) -> int {
+    if (D1 - D0 <= kTrNb) {
+      if (left)
+        diag_left_kernel<T><<<(n + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
+            A, lda, trans, lower, unit, D0, D1 - D0, B, ldb, n, 1);
+      else
+        diag_right_kernel<T><<<(m + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
+            A, lda, trans, lower, unit, D0, D1 - D0, B, ldb, m, 1);
+      return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
     }
-  }
+    const int Dm = D0 + ((D1 - D0) / 2 + kTrNb - 1) / kTrNb * kTrNb;  // D0 < Dm < D1
+    // forward: the rows / columns still to solve follow the solved ones
+    int r = self(self, forward ? D0 : Dm, forward ? Dm : D1);
+    if (r == GB300_OK)
+      r = forward ? solve_update(Dm, D1, D0, Dm) : solve_update(D0, Dm, Dm, D1);
+    if (r == GB300_OK) r = self(self, forward ? Dm : D0, forward ? D1 : Dm);
+    return r;
+  };
+  if (solve) rc = solve_range(solve_range, 0, na);
   for (int q = 0; !solve && q < nblk && rc == GB300_OK; ++q) {
     const int ib = forward ? q : nblk - 1 - q;
     const int d0 = ib * kTrNb, nb = (na - d0) < kTrNb ? (na - d0) : kTrNb;
