@@ -1058,9 +1058,16 @@ def run_trsm(args, torch, rank, world):
     # the faster reported; FP32 on 6xBF16
     split_forms = [1, 2] if p == "d" else [1]
     form_names = {1: "Ozaki slices" if p == "d" else "6xBF16", 2: "CRT"}
-    res = {"plain": residual(0)}
+    # --form plain | split | crt: that form alone (profiling runs)
+    only = {"plain": 0, "split": 1, "crt": 2}.get(args.form) if args.form else None
+    if args.form and only is None:
+        raise SystemExit("--form for TRSM workloads: plain, split or crt")
+    if only is not None:
+        split_forms = [only]
+        form_names[0] = "plain"
+    res = {} if only is not None else {"plain": residual(0)}
     for f in split_forms:
-        res["split" if f == 1 else "crt"] = residual(f)
+        res[{0: "plain", 1: "split", 2: "crt"}[f]] = residual(f)
     sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
     if sampler:
         sampler.start()
@@ -1069,7 +1076,7 @@ def run_trsm(args, torch, rank, world):
     ms_by_form = {f: timed(f, args.steps, args.warmup) for f in split_forms}
     best = min(ms_by_form, key=ms_by_form.get)
     ms_split = ms_by_form[best]
-    ms_plain = timed(0, max(3, args.steps // 2), args.warmup)
+    ms_plain = timed(0, max(3, args.steps // 2), args.warmup) if only is None else None
     barrier(torch, world)
     clocks = sampler.stop() if sampler else None
     max_ms = allreduce_max(torch, world, ms_split)
@@ -1083,10 +1090,10 @@ def run_trsm(args, torch, rank, world):
         "config": {"workload": args.workload, "side": "L", "uplo": "L", "transa": "N",
                    "diag": "N", "m": m, "n": n, "alpha": w["alpha"], "flops_per_call": "m^2 n",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "form": {"name": "split updates (%s)" % form_names[best],
+        "form": {"name": ("%s updates" if best == 0 else "split updates (%s)") % form_names[best],
                  "ms_by_form": {form_names[f]: round(v, 3) for f, v in ms_by_form.items()}},
-        "plain": {"value": round(flops / (ms_plain / 1e3) / 1e12, 3), "unit": "TFLOP/s",
-                  "ms": round(ms_plain, 3)},
+        "plain": ({"value": round(flops / (ms_plain / 1e3) / 1e12, 3), "unit": "TFLOP/s",
+                   "ms": round(ms_plain, 3)} if ms_plain is not None else None),
         "accuracy": {"backward_residual": res, "columns": 64},
         "clocks": clocks,
         "e2e": {"value": None, "skipped": "device-pointer TRSM API"},
@@ -1304,7 +1311,8 @@ def main():
     ap.add_argument("--form", default=None,
                     help="use this split form instead of timing the qualifying ones "
                          "(crt_nN, ozaki_sS, bf16xP, fp16x3, optionally with _cN chunk, _tN "
-                         "tile width, _pair / _cta cluster mode; profiling runs)")
+                         "tile width, _pair / _cta cluster mode; TRSM workloads: plain, split or "
+                         "crt; profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

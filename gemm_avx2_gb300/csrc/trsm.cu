@@ -25,7 +25,8 @@
 namespace gb300 {
 
 constexpr int kTrNb = 64;     // diagonal block size
-constexpr int kTrCols = 128;  // right-hand sides per CTA of the diagonal kernels
+// right-hand sides per CTA of the diagonal kernels (4 lanes each: 128 threads)
+constexpr int kTrCols = 32;
 
 // op(A)(r, c) of the diagonal block starting at (d0, d0).
 template <typename T>
@@ -33,125 +34,124 @@ __device__ __forceinline__ T opA_at(const T *A, int lda, bool trans, int d0, int
   return trans ? A[(int64_t)(d0 + r) * lda + d0 + c] : A[(int64_t)(d0 + c) * lda + d0 + r];
 }
 
-// Load the nb x nb diagonal block of op(A) into shared memory as T[r][c] (only
-// the effective triangle is read; the rest is set to zero).
+// The nb x nb diagonal block of op(A) at (d0, d0) into shared memory as
+// Ms[c][r] = M(r, c), column by column: M = op(A)'s block for the left side,
+// its transpose for the right side (X op(A) = B is op(A)^T X^T = B^T).  Only
+// the effective triangle is read; the unit diagonal is written as 1 and
+// everything else, up to 64 x 64, as 0.
 template <typename T>
-__device__ void load_triangle(const T *A, int lda, bool trans, bool lower, bool unit, int d0,
-                              int nb, T *Ts) {
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int r = e / nb, c = e % nb;
-    const bool in = lower ? (c <= r) : (c >= r);
+__device__ void load_block(const T *A, int lda, bool trans, bool lower, bool unit, bool right,
+                           int d0, int nb, T *Ms) {
+  for (int e = threadIdx.x; e < kTrNb * kTrNb; e += blockDim.x) {
+    const int c = e / kTrNb, r = e % kTrNb;     // M(r, c)
+    const int ar = right ? c : r, ac = right ? r : c;  // the entry of op(A)'s block
     T v = T(0);
-    if (r == c && unit) v = T(1);
-    else if (in) v = opA_at(A, lda, trans, d0, r, c);
-    Ts[r * kTrNb + c] = v;
+    if (r < nb && c < nb) {
+      const bool in = lower ? (ac <= ar) : (ac >= ar);
+      if (ar == ac && unit) v = T(1);
+      else if (in) v = opA_at(A, lda, trans, d0, ar, ac);
+    }
+    Ms[e] = v;
   }
 }
 
-// Left side: the rows [d0, d0+nb) of B, all columns; one thread per column.
-//   solve = true : X = T^-1 Bblk (forward if lower, backward if upper)
-//   solve = false: X = T Bblk
-template <typename T>
-__global__ void __launch_bounds__(kTrCols) diag_left_kernel(const T *__restrict__ A, int lda,
-                                                            int trans, int lower, int unit,
-                                                            int d0, int nb, T *B, int ldb, int n,
-                                                            int solve) {
-  extern __shared__ uint8_t sm[];
-  T *Ts = reinterpret_cast<T *>(sm);                 // [kTrNb][kTrNb]
-  T *Xs = Ts + kTrNb * kTrNb;                        // [kTrNb][kTrCols]
-  load_triangle<T>(A, lda, trans != 0, lower != 0, unit != 0, d0, nb, Ts);
-  const int j = blockIdx.x * kTrCols + threadIdx.x;
-  const bool live = j < n;
-  T *col = B + (int64_t)j * ldb + d0;
-  for (int r = 0; r < nb; ++r) Xs[r * kTrCols + threadIdx.x] = live ? col[r] : T(0);
-  __syncthreads();
-  T *x = Xs + threadIdx.x;
-  if (solve) {
-    if (lower) {
-      for (int r = 0; r < nb; ++r) {
-        T s = x[r * kTrCols];
-        for (int c = 0; c < r; ++c) s -= Ts[r * kTrNb + c] * x[c * kTrCols];
-        x[r * kTrCols] = unit ? s : s / Ts[r * kTrNb + r];
-      }
-    } else {
-      for (int r = nb - 1; r >= 0; --r) {
-        T s = x[r * kTrCols];
-        for (int c = r + 1; c < nb; ++c) s -= Ts[r * kTrNb + c] * x[c * kTrCols];
-        x[r * kTrCols] = unit ? s : s / Ts[r * kTrNb + r];
+// x <- M^-1 x (solve) or M x (multiply) for one right-hand side spread over 4
+// lanes of a warp: lane part p holds x[16 p .. 16 p + 15] in registers, M
+// triangular (LOWER: below the diagonal) in Ms[c][r].  A solve takes the
+// columns in order: a shuffle hands x_c to the group, which divides it by
+// M(c, c) (the lane holding x_c keeps it), and each lane updates its rows still to solve
+// (x_r -= M(r, c) x_c); a multiply sums M(r, c) x_c over the shuffled x_c into
+// separate accumulators.  Rows and columns from nb on are zero in Ms and x and
+// stay so.  (One thread per right-hand side, 2016 multiply-adds in a chain
+// through shared memory, took 42.5 us a block for 8192 FP32 columns.)
+constexpr int kTrLanes = 4;                   // lanes per right-hand side
+constexpr int kTrRows = kTrNb / kTrLanes;     // entries per lane
+template <typename T, bool LOWER, bool SOLVE>
+__device__ __forceinline__ void tri_apply(T (&x)[kTrRows], const T *Ms, int nb, bool unit,
+                                          int part) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  auto m_at = [&](int r, int c) { return Ms[c * kTrNb + r]; };
+  if constexpr (SOLVE) {
+#pragma unroll
+    for (int q = 0; q < kTrNb; ++q) {
+      const int c = LOWER ? q : kTrNb - 1 - q;
+      const int owner = c / kTrRows, ic = c % kTrRows;
+      // every lane of the group divides the shuffled x_c (no divergent
+      // division before the next shuffle); its owner keeps the quotient
+      T xc = __shfl_sync(full, x[ic], (lane & ~(kTrLanes - 1)) | owner);
+      if (c < nb && !unit) xc = xc / m_at(c, c);
+      x[ic] = part == owner ? xc : x[ic];
+#pragma unroll
+      for (int j = 0; j < kTrRows; ++j) {
+        const int r = part * kTrRows + j;
+        if (LOWER ? (r > c) : (r < c)) x[j] -= m_at(r, c) * xc;
       }
     }
   } else {
-    // X = T Bblk in place: lower -> bottom row first, upper -> top row first
-    if (lower) {
-      for (int r = nb - 1; r >= 0; --r) {
-        T s = T(0);
-        for (int c = 0; c <= r; ++c) s += Ts[r * kTrNb + c] * x[c * kTrCols];
-        x[r * kTrCols] = s;
-      }
-    } else {
-      for (int r = 0; r < nb; ++r) {
-        T s = T(0);
-        for (int c = r; c < nb; ++c) s += Ts[r * kTrNb + c] * x[c * kTrCols];
-        x[r * kTrCols] = s;
+    T acc[kTrRows];
+#pragma unroll
+    for (int j = 0; j < kTrRows; ++j) acc[j] = T(0);
+#pragma unroll
+    for (int c = 0; c < kTrNb; ++c) {
+      const int owner = c / kTrRows, ic = c % kTrRows;
+      const T xc = __shfl_sync(full, x[ic], (lane & ~(kTrLanes - 1)) | owner);
+#pragma unroll
+      for (int j = 0; j < kTrRows; ++j) {
+        const int r = part * kTrRows + j;
+        if (LOWER ? (c <= r) : (c >= r)) acc[j] += m_at(r, c) * xc;
       }
     }
+#pragma unroll
+    for (int j = 0; j < kTrRows; ++j) x[j] = acc[j];
   }
-  __syncthreads();
-  if (live)
-    for (int r = 0; r < nb; ++r) col[r] = Xs[r * kTrCols + threadIdx.x];
 }
 
-// Right side: the columns [d0, d0+nb) of B, all rows; one thread per row.
-//   solve = true : X = Bblk T^-1 (forward over columns if upper, backward if lower)
-//   solve = false: X = Bblk T
-template <typename T>
-__global__ void __launch_bounds__(kTrCols) diag_right_kernel(const T *__restrict__ A, int lda,
-                                                             int trans, int lower, int unit,
-                                                             int d0, int nb, T *B, int ldb, int m,
-                                                             int solve) {
+// Left side: rows [d0, d0+nb) of B, kTrLanes lanes per column (kTrCols
+// columns a CTA): SOLVE: X = op(A)_blk^-1 B_blk;  else X = op(A)_blk B_blk.
+// LOWER: op(A)'s effective triangle.
+template <typename T, bool LOWER, bool SOLVE>
+__global__ void __launch_bounds__(kTrCols * kTrLanes) diag_left_kernel(
+    const T *__restrict__ A, int lda, int trans, int unit, int d0, int nb, T *B, int ldb, int n) {
   extern __shared__ uint8_t sm[];
-  T *Ts = reinterpret_cast<T *>(sm);
-  T *Xs = Ts + kTrNb * kTrNb;                        // [kTrNb][kTrCols]: column c, row slot
-  load_triangle<T>(A, lda, trans != 0, lower != 0, unit != 0, d0, nb, Ts);
-  const int i = blockIdx.x * kTrCols + threadIdx.x;
+  T *Ms = reinterpret_cast<T *>(sm);  // [kTrNb][kTrNb], column-major
+  load_block<T>(A, lda, trans != 0, LOWER, unit != 0, false, d0, nb, Ms);
+  __syncthreads();
+  const int j = blockIdx.x * kTrCols + (int)threadIdx.x / kTrLanes;
+  const int part = (int)threadIdx.x % kTrLanes;
+  const bool live = j < n;  // a dead column's lanes still take part in the shuffles
+  T *col = B + (int64_t)(live ? j : 0) * ldb + d0 + part * kTrRows;
+  T x[kTrRows];
+#pragma unroll
+  for (int i = 0; i < kTrRows; ++i) x[i] = (live && part * kTrRows + i < nb) ? col[i] : T(0);
+  tri_apply<T, LOWER, SOLVE>(x, Ms, nb, unit != 0, part);
+#pragma unroll
+  for (int i = 0; i < kTrRows; ++i)
+    if (live && part * kTrRows + i < nb) col[i] = x[i];
+}
+
+// Right side: columns [d0, d0+nb) of B, kTrLanes lanes per row:
+//   SOLVE: X = B_blk op(A)_blk^-1;  else X = B_blk op(A)_blk
+// (the row vector times the block is the block's transpose times the column)
+template <typename T, bool LOWER, bool SOLVE>
+__global__ void __launch_bounds__(kTrCols * kTrLanes) diag_right_kernel(
+    const T *__restrict__ A, int lda, int trans, int unit, int d0, int nb, T *B, int ldb, int m) {
+  extern __shared__ uint8_t sm[];
+  T *Ms = reinterpret_cast<T *>(sm);
+  load_block<T>(A, lda, trans != 0, LOWER, unit != 0, true, d0, nb, Ms);
+  __syncthreads();
+  const int i = blockIdx.x * kTrCols + (int)threadIdx.x / kTrLanes;
+  const int part = (int)threadIdx.x % kTrLanes;
   const bool live = i < m;
-  for (int c = 0; c < nb; ++c)
-    Xs[c * kTrCols + threadIdx.x] = live ? B[(int64_t)(d0 + c) * ldb + i] : T(0);
-  __syncthreads();
-  T *x = Xs + threadIdx.x;
-  if (solve) {
-    if (!lower) {
-      for (int c = 0; c < nb; ++c) {
-        T s = x[c * kTrCols];
-        for (int r = 0; r < c; ++r) s -= x[r * kTrCols] * Ts[r * kTrNb + c];
-        x[c * kTrCols] = unit ? s : s / Ts[c * kTrNb + c];
-      }
-    } else {
-      for (int c = nb - 1; c >= 0; --c) {
-        T s = x[c * kTrCols];
-        for (int r = c + 1; r < nb; ++r) s -= x[r * kTrCols] * Ts[r * kTrNb + c];
-        x[c * kTrCols] = unit ? s : s / Ts[c * kTrNb + c];
-      }
-    }
-  } else {
-    // X = Bblk T in place: upper -> last column first, lower -> first column first
-    if (!lower) {
-      for (int c = nb - 1; c >= 0; --c) {
-        T s = T(0);
-        for (int r = 0; r <= c; ++r) s += x[r * kTrCols] * Ts[r * kTrNb + c];
-        x[c * kTrCols] = s;
-      }
-    } else {
-      for (int c = 0; c < nb; ++c) {
-        T s = T(0);
-        for (int r = c; r < nb; ++r) s += x[r * kTrCols] * Ts[r * kTrNb + c];
-        x[c * kTrCols] = s;
-      }
-    }
-  }
-  __syncthreads();
-  if (live)
-    for (int c = 0; c < nb; ++c) B[(int64_t)(d0 + c) * ldb + i] = Xs[c * kTrCols + threadIdx.x];
+  T *row = B + (int64_t)(d0 + part * kTrRows) * ldb + (live ? i : 0);
+  T x[kTrRows];
+#pragma unroll
+  for (int c = 0; c < kTrRows; ++c)
+    x[c] = (live && part * kTrRows + c < nb) ? row[(int64_t)c * ldb] : T(0);
+  tri_apply<T, !LOWER, SOLVE>(x, Ms, nb, unit != 0, part);  // op(A)^T: the other triangle
+#pragma unroll
+  for (int c = 0; c < kTrRows; ++c)
+    if (live && part * kTrRows + c < nb) row[(int64_t)c * ldb] = x[c];
 }
 
 // B(m x n window) *= s, or = 0 exactly when s == 0 (BLAS: alpha = 0 sets B to zero).
@@ -252,12 +252,28 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
   auto opA = [&](int r0, int c0) -> const T * {
     return trans ? A + (int64_t)r0 * lda + c0 : A + (int64_t)c0 * lda + r0;
   };
-  const int smem = (kTrNb * kTrNb + kTrNb * kTrCols) * (int)sizeof(T);
-  if (cudaFuncSetAttribute(diag_left_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess ||
-      cudaFuncSetAttribute(diag_right_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess)
-    return GB300_ERR_CUDA;
+  const int smem = kTrNb * kTrNb * (int)sizeof(T);  // the block: at most 32 KB (FP64)
+  // the diagonal block [d0, d0 + nb): solve (1) or multiply (0) in place
+  auto diag_block = [&](int d0, int nb, bool sv) {
+    const int rhs = left ? n : m;
+    const dim3 grid((rhs + kTrCols - 1) / kTrCols);
+    const int tr = trans ? 1 : 0, un = unit ? 1 : 0;
+    if (left) {
+      if (lower)
+        (sv ? diag_left_kernel<T, true, true> : diag_left_kernel<T, true, false>)
+            <<<grid, kTrCols * kTrLanes, smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, n);
+      else
+        (sv ? diag_left_kernel<T, false, true> : diag_left_kernel<T, false, false>)
+            <<<grid, kTrCols * kTrLanes, smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, n);
+    } else {
+      if (lower)
+        (sv ? diag_right_kernel<T, true, true> : diag_right_kernel<T, true, false>)
+            <<<grid, kTrCols * kTrLanes, smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, m);
+      else
+        (sv ? diag_right_kernel<T, false, true> : diag_right_kernel<T, false, false>)
+            <<<grid, kTrCols * kTrLanes, smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, m);
+    }
+  };
   const int na = left ? m : n;
   const int nblk = (na + kTrNb - 1) / kTrNb;
   // TRSM scales first (X = op(A)^-1 (alpha B)); TRMM scales last.
@@ -287,12 +303,7 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
   // n m log2(m / 64) / 2, and most of the flops run at long K.
   auto solve_range = [&](auto &self, int D0, int D1) -> int {
     if (D1 - D0 <= kTrNb) {
-      if (left)
-        diag_left_kernel<T><<<(n + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
-            A, lda, trans, lower, unit, D0, D1 - D0, B, ldb, n, 1);
-      else
-        diag_right_kernel<T><<<(m + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
-            A, lda, trans, lower, unit, D0, D1 - D0, B, ldb, m, 1);
+      diag_block(D0, D1 - D0, true);
       return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
     }
     const int Dm = D0 + ((D1 - D0) / 2 + kTrNb - 1) / kTrNb * kTrNb;  // D0 < Dm < D1
@@ -312,8 +323,7 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
       // multiply: block rows/cols of the result = diagonal part + off-diagonal part,
       // the off-diagonal part reading rows/columns of B not yet overwritten
       if (left) {
-        diag_left_kernel<T><<<(n + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
-            A, lda, trans, lower, unit, d0, nb, B, ldb, n, 0);
+        diag_block(d0, nb, false);
         if (lower)  // B_i += op(A)(i, <i) B_<i ; rows above are still the input
           rc = tr_gemm<T>(form, tA, 'N', nb, n, d0, opA(d0, 0), lda, B, ldb, B + d0, ldb, ws,
                           ws_bytes, st, err, true);
@@ -321,8 +331,7 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
           rc = tr_gemm<T>(form, tA, 'N', nb, n, m - lo, opA(d0, lo), lda, B + lo, ldb, B + d0,
                           ldb, ws, ws_bytes, st, err, true);
       } else {
-        diag_right_kernel<T><<<(m + kTrCols - 1) / kTrCols, kTrCols, smem, st>>>(
-            A, lda, trans, lower, unit, d0, nb, B, ldb, m, 0);
+        diag_block(d0, nb, false);
         if (!lower)  // B_j += B_<j op(A)(<j, j)
           rc = tr_gemm<T>(form, 'N', tA, m, nb, d0, B, ldb, opA(0, d0), lda,
                           B + (int64_t)d0 * ldb, ldb, ws, ws_bytes, st, err, true);
