@@ -38,10 +38,12 @@ __device__ __forceinline__ T opA_at(const T *A, int lda, bool trans, int d0, int
 // Ms[c][r] = M(r, c), column by column: M = op(A)'s block for the left side,
 // its transpose for the right side (X op(A) = B is op(A)^T X^T = B^T).  Only
 // the effective triangle is read; the unit diagonal is written as 1 and
-// everything else, up to 64 x 64, as 0.
+// everything else, up to 64 x 64, as 0.  Then Inv[c] = 1 / M(c, c) (0 past nb):
+// the solves multiply by it, one division per entry of the block instead of
+// one per step and lane (the FP64 divisions had held much of the FP64 pipe).
 template <typename T>
 __device__ void load_block(const T *A, int lda, bool trans, bool lower, bool unit, bool right,
-                           int d0, int nb, T *Ms) {
+                           int d0, int nb, T *Ms, T *Inv) {
   for (int e = threadIdx.x; e < kTrNb * kTrNb; e += blockDim.x) {
     const int c = e / kTrNb, r = e % kTrNb;     // M(r, c)
     const int ar = right ? c : r, ac = right ? r : c;  // the entry of op(A)'s block
@@ -53,13 +55,16 @@ __device__ void load_block(const T *A, int lda, bool trans, bool lower, bool uni
     }
     Ms[e] = v;
   }
+  __syncthreads();
+  for (int c = threadIdx.x; c < kTrNb; c += blockDim.x)
+    Inv[c] = c < nb ? T(1) / Ms[c * kTrNb + c] : T(0);
 }
 
 // x <- M^-1 x (solve) or M x (multiply) for one right-hand side spread over 4
 // lanes of a warp: lane part p holds x[16 p .. 16 p + 15] in registers, M
 // triangular (LOWER: below the diagonal) in Ms[c][r].  A solve takes the
-// columns in order: a shuffle hands x_c to the group, which divides it by
-// M(c, c) (the lane holding x_c keeps it), and each lane updates its rows still to solve
+// columns in order: a shuffle hands x_c to the group, which multiplies it by
+// 1 / M(c, c) (the lane holding x_c keeps it), and each lane updates its rows still to solve
 // (x_r -= M(r, c) x_c); a multiply sums M(r, c) x_c over the shuffled x_c into
 // separate accumulators.  Rows and columns from nb on are zero in Ms and x and
 // stay so.  (One thread per right-hand side, 2016 multiply-adds in a chain
@@ -67,8 +72,8 @@ __device__ void load_block(const T *A, int lda, bool trans, bool lower, bool uni
 constexpr int kTrLanes = 4;                   // lanes per right-hand side
 constexpr int kTrRows = kTrNb / kTrLanes;     // entries per lane
 template <typename T, bool LOWER, bool SOLVE>
-__device__ __forceinline__ void tri_apply(T (&x)[kTrRows], const T *Ms, int nb, bool unit,
-                                          int part) {
+__device__ __forceinline__ void tri_apply(T (&x)[kTrRows], const T *Ms, const T *Inv, int nb,
+                                          bool unit, int part) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   auto m_at = [&](int r, int c) { return Ms[c * kTrNb + r]; };
@@ -77,10 +82,10 @@ __device__ __forceinline__ void tri_apply(T (&x)[kTrRows], const T *Ms, int nb, 
     for (int q = 0; q < kTrNb; ++q) {
       const int c = LOWER ? q : kTrNb - 1 - q;
       const int owner = c / kTrRows, ic = c % kTrRows;
-      // every lane of the group divides the shuffled x_c (no divergent
-      // division before the next shuffle); its owner keeps the quotient
+      // every lane of the group scales the shuffled x_c (nothing divergent
+      // before the next shuffle); its owner keeps the result
       T xc = __shfl_sync(full, x[ic], (lane & ~(kTrLanes - 1)) | owner);
-      if (c < nb && !unit) xc = xc / m_at(c, c);
+      if (!unit) xc *= Inv[c];
       x[ic] = part == owner ? xc : x[ic];
 #pragma unroll
       for (int j = 0; j < kTrRows; ++j) {
@@ -115,7 +120,8 @@ __global__ void __launch_bounds__(kTrCols * kTrLanes) diag_left_kernel(
     const T *__restrict__ A, int lda, int trans, int unit, int d0, int nb, T *B, int ldb, int n) {
   extern __shared__ uint8_t sm[];
   T *Ms = reinterpret_cast<T *>(sm);  // [kTrNb][kTrNb], column-major
-  load_block<T>(A, lda, trans != 0, LOWER, unit != 0, false, d0, nb, Ms);
+  T *Inv = Ms + kTrNb * kTrNb;        // [kTrNb]
+  load_block<T>(A, lda, trans != 0, LOWER, unit != 0, false, d0, nb, Ms, Inv);
   __syncthreads();
   const int j = blockIdx.x * kTrCols + (int)threadIdx.x / kTrLanes;
   const int part = (int)threadIdx.x % kTrLanes;
@@ -124,7 +130,7 @@ __global__ void __launch_bounds__(kTrCols * kTrLanes) diag_left_kernel(
   T x[kTrRows];
 #pragma unroll
   for (int i = 0; i < kTrRows; ++i) x[i] = (live && part * kTrRows + i < nb) ? col[i] : T(0);
-  tri_apply<T, LOWER, SOLVE>(x, Ms, nb, unit != 0, part);
+  tri_apply<T, LOWER, SOLVE>(x, Ms, Inv, nb, unit != 0, part);
 #pragma unroll
   for (int i = 0; i < kTrRows; ++i)
     if (live && part * kTrRows + i < nb) col[i] = x[i];
@@ -138,7 +144,8 @@ __global__ void __launch_bounds__(kTrCols * kTrLanes) diag_right_kernel(
     const T *__restrict__ A, int lda, int trans, int unit, int d0, int nb, T *B, int ldb, int m) {
   extern __shared__ uint8_t sm[];
   T *Ms = reinterpret_cast<T *>(sm);
-  load_block<T>(A, lda, trans != 0, LOWER, unit != 0, true, d0, nb, Ms);
+  T *Inv = Ms + kTrNb * kTrNb;
+  load_block<T>(A, lda, trans != 0, LOWER, unit != 0, true, d0, nb, Ms, Inv);
   __syncthreads();
   const int i = blockIdx.x * kTrCols + (int)threadIdx.x / kTrLanes;
   const int part = (int)threadIdx.x % kTrLanes;
@@ -148,7 +155,7 @@ __global__ void __launch_bounds__(kTrCols * kTrLanes) diag_right_kernel(
 #pragma unroll
   for (int c = 0; c < kTrRows; ++c)
     x[c] = (live && part * kTrRows + c < nb) ? row[(int64_t)c * ldb] : T(0);
-  tri_apply<T, !LOWER, SOLVE>(x, Ms, nb, unit != 0, part);  // op(A)^T: the other triangle
+  tri_apply<T, !LOWER, SOLVE>(x, Ms, Inv, nb, unit != 0, part);  // op(A)^T: the other triangle
 #pragma unroll
   for (int c = 0; c < kTrRows; ++c)
     if (live && part * kTrRows + c < nb) row[(int64_t)c * ldb] = x[c];
@@ -252,7 +259,7 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
   auto opA = [&](int r0, int c0) -> const T * {
     return trans ? A + (int64_t)r0 * lda + c0 : A + (int64_t)c0 * lda + r0;
   };
-  const int smem = kTrNb * kTrNb * (int)sizeof(T);  // the block: at most 32 KB (FP64)
+  const int smem = (kTrNb * kTrNb + kTrNb) * (int)sizeof(T);  // the block and 1 / diagonal
   // the diagonal block [d0, d0 + nb): solve (1) or multiply (0) in place
   auto diag_block = [&](int d0, int nb, bool sv) {
     const int rhs = left ? n : m;
