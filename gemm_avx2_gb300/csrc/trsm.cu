@@ -25,7 +25,7 @@
 namespace gb300 {
 
 constexpr int kTrNb = 64;     // diagonal block size
-// right-hand sides per CTA of the diagonal kernels (4 lanes each: 128 threads)
+// right-hand sides per CTA of the diagonal kernels (kTrLanes lanes each)
 constexpr int kTrCols = 32;
 
 // op(A)(r, c) of the diagonal block starting at (d0, d0).
@@ -60,16 +60,18 @@ __device__ void load_block(const T *A, int lda, bool trans, bool lower, bool uni
     Inv[c] = c < nb ? T(1) / Ms[c * kTrNb + c] : T(0);
 }
 
-// x <- M^-1 x (solve) or M x (multiply) for one right-hand side spread over 4
-// lanes of a warp: lane part p holds x[16 p .. 16 p + 15] in registers, M
+// x <- M^-1 x (solve) or M x (multiply) for one right-hand side spread over
+// kTrLanes lanes of a warp: lane part p holds x[kTrRows p ..] in registers, M
 // triangular (LOWER: below the diagonal) in Ms[c][r].  A solve takes the
 // columns in order: a shuffle hands x_c to the group, which multiplies it by
-// 1 / M(c, c) (the lane holding x_c keeps it), and each lane updates its rows still to solve
-// (x_r -= M(r, c) x_c); a multiply sums M(r, c) x_c over the shuffled x_c into
-// separate accumulators.  Rows and columns from nb on are zero in Ms and x and
-// stay so.  (One thread per right-hand side, 2016 multiply-adds in a chain
-// through shared memory, took 42.5 us a block for 8192 FP32 columns.)
-constexpr int kTrLanes = 4;                   // lanes per right-hand side
+// 1 / M(c, c) (the lane holding x_c keeps it), and each lane updates its rows
+// still to solve (x_r -= M(r, c) x_c); a multiply sums M(r, c) x_c over the
+// shuffled x_c into separate accumulators.  Rows and columns from nb on are
+// zero in Ms and x and stay so.  (One thread per right-hand side, 2016
+// multiply-adds in a chain through shared memory, took 42.5 us a block for
+// 8192 FP32 columns; 8 lanes ran STRSM 8192^2 at 74.3 TFLOP/s against 64.9
+// with 4, DTRSM unchanged: its block solves are FP64-pipe-bound.)
+constexpr int kTrLanes = 8;                   // lanes per right-hand side
 constexpr int kTrRows = kTrNb / kTrLanes;     // entries per lane
 template <typename T, bool LOWER, bool SOLVE>
 __device__ __forceinline__ void tri_apply(T (&x)[kTrRows], const T *Ms, const T *Inv, int nb,
