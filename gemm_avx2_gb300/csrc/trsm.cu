@@ -25,7 +25,7 @@
 namespace gb300 {
 
 constexpr int kTrNb = 64;     // diagonal block size
-// right-hand sides per CTA of the diagonal kernels (kTrLanes lanes each)
+// right-hand sides per CTA of the diagonal kernels (tr_lanes<T>() lanes each)
 constexpr int kTrCols = 32;
 
 // op(A)(r, c) of the diagonal block starting at (d0, d0).
@@ -61,7 +61,7 @@ __device__ void load_block(const T *A, int lda, bool trans, bool lower, bool uni
 }
 
 // x <- M^-1 x (solve) or M x (multiply) for one right-hand side spread over
-// kTrLanes lanes of a warp: lane part p holds x[kTrRows p ..] in registers, M
+// kLanes lanes of a warp: lane part p holds x[kRows p ..] in registers, M
 // triangular (LOWER: below the diagonal) in Ms[c][r].  A solve takes the
 // columns in order: a shuffle hands x_c to the group, which multiplies it by
 // 1 / M(c, c) (the lane holding x_c keeps it), and each lane updates its rows
@@ -69,12 +69,14 @@ __device__ void load_block(const T *A, int lda, bool trans, bool lower, bool uni
 // shuffled x_c into separate accumulators.  Rows and columns from nb on are
 // zero in Ms and x and stay so.  (One thread per right-hand side, 2016
 // multiply-adds in a chain through shared memory, took 42.5 us a block for
-// 8192 FP32 columns; 8 lanes ran STRSM 8192^2 at 74.3 TFLOP/s against 64.9
-// with 4, DTRSM unchanged: its block solves are FP64-pipe-bound.)
-constexpr int kTrLanes = 8;                   // lanes per right-hand side
-constexpr int kTrRows = kTrNb / kTrLanes;     // entries per lane
-template <typename T, bool LOWER, bool SOLVE>
-__device__ __forceinline__ void tri_apply(T (&x)[kTrRows], const T *Ms, const T *Inv, int nb,
+// 8192 FP32 columns.  Lanes per right-hand side, STRSM / DTRSM 8192^2: 4 ->
+// 64.9 / 18.0 TFLOP/s, 8 -> 74.3 / 17.9, 16 -> 82.4 / 17.4; the FP64 block
+// solves are FP64-pipe-bound.)
+template <typename T>
+__host__ __device__ constexpr int tr_lanes() { return sizeof(T) == 4 ? 16 : 8; }
+template <typename T, bool LOWER, bool SOLVE, int kLanes = tr_lanes<T>(),
+          int kRows = kTrNb / tr_lanes<T>()>
+__device__ __forceinline__ void tri_apply(T (&x)[kRows], const T *Ms, const T *Inv, int nb,
                                           bool unit, int part) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -83,84 +85,86 @@ __device__ __forceinline__ void tri_apply(T (&x)[kTrRows], const T *Ms, const T 
 #pragma unroll
     for (int q = 0; q < kTrNb; ++q) {
       const int c = LOWER ? q : kTrNb - 1 - q;
-      const int owner = c / kTrRows, ic = c % kTrRows;
+      const int owner = c / kRows, ic = c % kRows;
       // every lane of the group scales the shuffled x_c (nothing divergent
       // before the next shuffle); its owner keeps the result
-      T xc = __shfl_sync(full, x[ic], (lane & ~(kTrLanes - 1)) | owner);
+      T xc = __shfl_sync(full, x[ic], (lane & ~(kLanes - 1)) | owner);
       if (!unit) xc *= Inv[c];
       x[ic] = part == owner ? xc : x[ic];
 #pragma unroll
-      for (int j = 0; j < kTrRows; ++j) {
-        const int r = part * kTrRows + j;
+      for (int j = 0; j < kRows; ++j) {
+        const int r = part * kRows + j;
         if (LOWER ? (r > c) : (r < c)) x[j] -= m_at(r, c) * xc;
       }
     }
   } else {
-    T acc[kTrRows];
+    T acc[kRows];
 #pragma unroll
-    for (int j = 0; j < kTrRows; ++j) acc[j] = T(0);
+    for (int j = 0; j < kRows; ++j) acc[j] = T(0);
 #pragma unroll
     for (int c = 0; c < kTrNb; ++c) {
-      const int owner = c / kTrRows, ic = c % kTrRows;
-      const T xc = __shfl_sync(full, x[ic], (lane & ~(kTrLanes - 1)) | owner);
+      const int owner = c / kRows, ic = c % kRows;
+      const T xc = __shfl_sync(full, x[ic], (lane & ~(kLanes - 1)) | owner);
 #pragma unroll
-      for (int j = 0; j < kTrRows; ++j) {
-        const int r = part * kTrRows + j;
+      for (int j = 0; j < kRows; ++j) {
+        const int r = part * kRows + j;
         if (LOWER ? (c <= r) : (c >= r)) acc[j] += m_at(r, c) * xc;
       }
     }
 #pragma unroll
-    for (int j = 0; j < kTrRows; ++j) x[j] = acc[j];
+    for (int j = 0; j < kRows; ++j) x[j] = acc[j];
   }
 }
 
-// Left side: rows [d0, d0+nb) of B, kTrLanes lanes per column (kTrCols
+// Left side: rows [d0, d0+nb) of B, tr_lanes<T>() lanes per column (kTrCols
 // columns a CTA): SOLVE: X = op(A)_blk^-1 B_blk;  else X = op(A)_blk B_blk.
 // LOWER: op(A)'s effective triangle.
 template <typename T, bool LOWER, bool SOLVE>
-__global__ void __launch_bounds__(kTrCols * kTrLanes) diag_left_kernel(
+__global__ void __launch_bounds__(kTrCols * tr_lanes<T>()) diag_left_kernel(
     const T *__restrict__ A, int lda, int trans, int unit, int d0, int nb, T *B, int ldb, int n) {
+  constexpr int kLanes = tr_lanes<T>(), kRows = kTrNb / kLanes;
   extern __shared__ uint8_t sm[];
   T *Ms = reinterpret_cast<T *>(sm);  // [kTrNb][kTrNb], column-major
   T *Inv = Ms + kTrNb * kTrNb;        // [kTrNb]
   load_block<T>(A, lda, trans != 0, LOWER, unit != 0, false, d0, nb, Ms, Inv);
   __syncthreads();
-  const int j = blockIdx.x * kTrCols + (int)threadIdx.x / kTrLanes;
-  const int part = (int)threadIdx.x % kTrLanes;
+  const int j = blockIdx.x * kTrCols + (int)threadIdx.x / kLanes;
+  const int part = (int)threadIdx.x % kLanes;
   const bool live = j < n;  // a dead column's lanes still take part in the shuffles
-  T *col = B + (int64_t)(live ? j : 0) * ldb + d0 + part * kTrRows;
-  T x[kTrRows];
+  T *col = B + (int64_t)(live ? j : 0) * ldb + d0 + part * kRows;
+  T x[kRows];
 #pragma unroll
-  for (int i = 0; i < kTrRows; ++i) x[i] = (live && part * kTrRows + i < nb) ? col[i] : T(0);
+  for (int i = 0; i < kRows; ++i) x[i] = (live && part * kRows + i < nb) ? col[i] : T(0);
   tri_apply<T, LOWER, SOLVE>(x, Ms, Inv, nb, unit != 0, part);
 #pragma unroll
-  for (int i = 0; i < kTrRows; ++i)
-    if (live && part * kTrRows + i < nb) col[i] = x[i];
+  for (int i = 0; i < kRows; ++i)
+    if (live && part * kRows + i < nb) col[i] = x[i];
 }
 
-// Right side: columns [d0, d0+nb) of B, kTrLanes lanes per row:
+// Right side: columns [d0, d0+nb) of B, tr_lanes<T>() lanes per row:
 //   SOLVE: X = B_blk op(A)_blk^-1;  else X = B_blk op(A)_blk
 // (the row vector times the block is the block's transpose times the column)
 template <typename T, bool LOWER, bool SOLVE>
-__global__ void __launch_bounds__(kTrCols * kTrLanes) diag_right_kernel(
+__global__ void __launch_bounds__(kTrCols * tr_lanes<T>()) diag_right_kernel(
     const T *__restrict__ A, int lda, int trans, int unit, int d0, int nb, T *B, int ldb, int m) {
+  constexpr int kLanes = tr_lanes<T>(), kRows = kTrNb / kLanes;
   extern __shared__ uint8_t sm[];
   T *Ms = reinterpret_cast<T *>(sm);
   T *Inv = Ms + kTrNb * kTrNb;
   load_block<T>(A, lda, trans != 0, LOWER, unit != 0, true, d0, nb, Ms, Inv);
   __syncthreads();
-  const int i = blockIdx.x * kTrCols + (int)threadIdx.x / kTrLanes;
-  const int part = (int)threadIdx.x % kTrLanes;
+  const int i = blockIdx.x * kTrCols + (int)threadIdx.x / kLanes;
+  const int part = (int)threadIdx.x % kLanes;
   const bool live = i < m;
-  T *row = B + (int64_t)(d0 + part * kTrRows) * ldb + (live ? i : 0);
-  T x[kTrRows];
+  T *row = B + (int64_t)(d0 + part * kRows) * ldb + (live ? i : 0);
+  T x[kRows];
 #pragma unroll
-  for (int c = 0; c < kTrRows; ++c)
-    x[c] = (live && part * kTrRows + c < nb) ? row[(int64_t)c * ldb] : T(0);
+  for (int c = 0; c < kRows; ++c)
+    x[c] = (live && part * kRows + c < nb) ? row[(int64_t)c * ldb] : T(0);
   tri_apply<T, !LOWER, SOLVE>(x, Ms, Inv, nb, unit != 0, part);  // op(A)^T: the other triangle
 #pragma unroll
-  for (int c = 0; c < kTrRows; ++c)
-    if (live && part * kTrRows + c < nb) row[(int64_t)c * ldb] = x[c];
+  for (int c = 0; c < kRows; ++c)
+    if (live && part * kRows + c < nb) row[(int64_t)c * ldb] = x[c];
 }
 
 // B(m x n window) *= s, or = 0 exactly when s == 0 (BLAS: alpha = 0 sets B to zero).
@@ -270,17 +274,17 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
     if (left) {
       if (lower)
         (sv ? diag_left_kernel<T, true, true> : diag_left_kernel<T, true, false>)
-            <<<grid, kTrCols * kTrLanes, smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, n);
+            <<<grid, kTrCols * tr_lanes<T>(), smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, n);
       else
         (sv ? diag_left_kernel<T, false, true> : diag_left_kernel<T, false, false>)
-            <<<grid, kTrCols * kTrLanes, smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, n);
+            <<<grid, kTrCols * tr_lanes<T>(), smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, n);
     } else {
       if (lower)
         (sv ? diag_right_kernel<T, true, true> : diag_right_kernel<T, true, false>)
-            <<<grid, kTrCols * kTrLanes, smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, m);
+            <<<grid, kTrCols * tr_lanes<T>(), smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, m);
       else
         (sv ? diag_right_kernel<T, false, true> : diag_right_kernel<T, false, false>)
-            <<<grid, kTrCols * kTrLanes, smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, m);
+            <<<grid, kTrCols * tr_lanes<T>(), smem, st>>>(A, lda, tr, un, d0, nb, B, ldb, m);
     }
   };
   const int na = left ? m : n;
