@@ -288,7 +288,6 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
     }
   };
   const int na = left ? m : n;
-  const int nblk = (na + kTrNb - 1) / kTrNb;
   // TRSM scales first (X = op(A)^-1 (alpha B)); TRMM scales last.
   if (solve && alpha != T(1)) scale(alpha);
   // Block order: a solve walks the triangle from its first row (lower-left /
@@ -296,16 +295,16 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
   // so that every block still reads unmodified rows / columns of B.
   const bool forward = left ? (solve ? lower : !lower) : (solve ? !lower : lower);
   int rc = GB300_OK;
-  // TRSM: the solved block [c0, c1) of X updates the rows (left) / columns
-  // (right) [r0, r1) still to solve: B(r, :) -= op(A)(r, c) X(c, :), or
-  // B(:, r) -= X(:, c) op(A)(c, r)
-  auto solve_update = [&](int r0, int r1, int c0, int c1) -> int {
+  // The rows (left) / columns (right) [r0, r1) of B take the contribution of
+  // [c0, c1): B(r, :) -= op(A)(r, c) B(c, :), or B(:, r) -= B(:, c) op(A)(c, r)
+  // (TRSM: the solved block updates the ones still to solve); += for TRMM
+  auto block_update = [&](int r0, int r1, int c0, int c1, bool add) -> int {
     if (r1 <= r0 || c1 <= c0) return GB300_OK;
     if (left)
       return tr_gemm<T>(form, tA, 'N', r1 - r0, n, c1 - c0, opA(r0, c0), lda, B + c0, ldb, B + r0,
-                        ldb, ws, ws_bytes, st, err);
+                        ldb, ws, ws_bytes, st, err, add);
     return tr_gemm<T>(form, 'N', tA, m, r1 - r0, c1 - c0, B + (int64_t)c0 * ldb, ldb, opA(c0, r0),
-                      lda, B + (int64_t)r0 * ldb, ldb, ws, ws_bytes, st, err);
+                      lda, B + (int64_t)r0 * ldb, ldb, ws, ws_bytes, st, err, add);
   };
   // TRSM by recursive halving of the triangle: solve the first half, update
   // the second half with it (one GEMM with k = the half), solve the second
@@ -323,38 +322,29 @@ int tr_driver(int solve, char side, char uplo, char transa, char diag, int m, in
     // forward: the rows / columns still to solve follow the solved ones
     int r = self(self, forward ? D0 : Dm, forward ? Dm : D1);
     if (r == GB300_OK)
-      r = forward ? solve_update(Dm, D1, D0, Dm) : solve_update(D0, Dm, Dm, D1);
+      r = forward ? block_update(Dm, D1, D0, Dm, false) : block_update(D0, Dm, Dm, D1, false);
     if (r == GB300_OK) r = self(self, forward ? Dm : D0, forward ? D1 : Dm);
     return r;
   };
   if (solve) rc = solve_range(solve_range, 0, na);
-  for (int q = 0; !solve && q < nblk && rc == GB300_OK; ++q) {
-    const int ib = forward ? q : nblk - 1 - q;
-    const int d0 = ib * kTrNb, nb = (na - d0) < kTrNb ? (na - d0) : kTrNb;
-    const int lo = d0 + nb;  // first index after the block
-    {
-      // multiply: block rows/cols of the result = diagonal part + off-diagonal part,
-      // the off-diagonal part reading rows/columns of B not yet overwritten
-      if (left) {
-        diag_block(d0, nb, false);
-        if (lower)  // B_i += op(A)(i, <i) B_<i ; rows above are still the input
-          rc = tr_gemm<T>(form, tA, 'N', nb, n, d0, opA(d0, 0), lda, B, ldb, B + d0, ldb, ws,
-                          ws_bytes, st, err, true);
-        else        // B_i += op(A)(i, >i) B_>i
-          rc = tr_gemm<T>(form, tA, 'N', nb, n, m - lo, opA(d0, lo), lda, B + lo, ldb, B + d0,
-                          ldb, ws, ws_bytes, st, err, true);
-      } else {
-        diag_block(d0, nb, false);
-        if (!lower)  // B_j += B_<j op(A)(<j, j)
-          rc = tr_gemm<T>(form, 'N', tA, m, nb, d0, B, ldb, opA(0, d0), lda,
-                          B + (int64_t)d0 * ldb, ldb, ws, ws_bytes, st, err, true);
-        else         // B_j += B_>j op(A)(>j, j)
-          rc = tr_gemm<T>(form, 'N', tA, m, nb, n - lo, B + (int64_t)lo * ldb, ldb, opA(lo, d0),
-                          lda, B + (int64_t)d0 * ldb, ldb, ws, ws_bytes, st, err, true);
-      }
+  // TRMM in place by the same halving: the half whose new value needs the
+  // other half's old one goes first (forward: the first half, as for the
+  // upper triangle on the left), then it takes that half's contribution, then
+  // the other half; ranges of at most 64 go to the diagonal kernel.  (Per
+  // 64-wide block the updates were 64 rows tall: few tiles for the GEMMs.)
+  auto mul_range = [&](auto &self, int D0, int D1) -> int {
+    if (D1 - D0 <= kTrNb) {
+      diag_block(D0, D1 - D0, false);
+      return cudaGetLastError() == cudaSuccess ? GB300_OK : GB300_ERR_CUDA;
     }
-    if (rc == GB300_OK && cudaGetLastError() != cudaSuccess) rc = GB300_ERR_CUDA;
-  }
+    const int Dm = D0 + ((D1 - D0) / 2 + kTrNb - 1) / kTrNb * kTrNb;  // D0 < Dm < D1
+    int r = self(self, forward ? D0 : Dm, forward ? Dm : D1);
+    if (r == GB300_OK)
+      r = forward ? block_update(D0, Dm, Dm, D1, true) : block_update(Dm, D1, D0, Dm, true);
+    if (r == GB300_OK) r = self(self, forward ? Dm : D0, forward ? D1 : Dm);
+    return r;
+  };
+  if (!solve) rc = mul_range(mul_range, 0, na);
   if (rc == GB300_OK && !solve && alpha != T(1)) scale(alpha);
   if (rc == GB300_OK && cudaGetLastError() != cudaSuccess) rc = GB300_ERR_CUDA;
   return rc;
