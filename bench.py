@@ -77,6 +77,9 @@ WORKLOADS = {
 TRSM_WORKLOADS = {
     "dtrsm_lln_8192": dict(prec="d", m=8192, n=8192, alpha=1.0, seed=7),
     "strsm_lln_8192": dict(prec="s", m=8192, n=8192, alpha=1.0, seed=7),
+    # triangular multiply B = op(A) B, the same shape
+    "dtrmm_lln_8192": dict(prec="d", m=8192, n=8192, alpha=1.0, seed=7, routine="trmm"),
+    "strmm_lln_8192": dict(prec="s", m=8192, n=8192, alpha=1.0, seed=7, routine="trmm"),
 }
 # complex GEMM (the reference's OpenBLAS-style c/z kernels): the split form on
 # the embedded real problem, at equal error to the plain 4M method
@@ -999,17 +1002,21 @@ def run_grouped(args, torch, rank, world):
 
 
 def run_trsm(args, torch, rank, world):
-    """TRSM on the GEMM kernels: the diagonal blocks solved by diag_left_kernel,
-    the rest of B updated by GEMMs (plain form, or the split form: Ozaki
-    slices for FP64, 6xBF16 for FP32).  A is lower triangular with a raised
-    diagonal (well conditioned); the accuracy is the sampled backward residual
-    ||op(A) x - alpha b|| / (||A|| ||x||) over 64 columns of the solution."""
+    """TRSM (or TRMM) on the GEMM kernels: the diagonal blocks solved (or
+    multiplied) by diag_left_kernel, the rest of B updated by GEMMs (plain
+    form, or the split forms: Ozaki slices or the CRT form for FP64, 6xBF16 for
+    FP32).  A is lower triangular with a raised diagonal (well conditioned); the
+    accuracy is the sampled backward residual ||op(A) x - alpha b|| / (||A||
+    ||x||) of the solve, or the relative error ||x - alpha op(A) b|| / (||A||
+    ||b||) of the product, over 64 columns."""
     import numpy as np
 
     import gemm_avx2_gb300 as g
 
     w = TRSM_WORKLOADS[args.workload]
     p, m, n = w["prec"], w["m"], w["n"]
+    trmm = w.get("routine") == "trmm"
+    routine = g.trmm if trmm else g.trsm
     dt = torch.float64 if p == "d" else torch.float32
     gen = torch.Generator(device="cuda")
     gen.manual_seed(w["seed"])
@@ -1024,7 +1031,7 @@ def run_trsm(args, torch, rank, world):
     flops = float(m) * m * n
 
     def call(form):
-        return g.trsm(p, "L", "L", "N", "N", m, n, w["alpha"], A.data_ptr(), m, B.data_ptr(), m,
+        return routine(p, "L", "L", "N", "N", m, n, w["alpha"], A.data_ptr(), m, B.data_ptr(), m,
                       form=form, stream=stream)
 
     def timed(form, steps, warmup):
@@ -1051,6 +1058,9 @@ def run_trsm(args, torch, rank, world):
         idx = torch.as_tensor(cols, device="cuda")
         X = B.index_select(0, idx).double().cpu().numpy().T          # m x 64
         Bc = B0.index_select(0, idx).double().cpu().numpy().T
+        if trmm:
+            R = X - w["alpha"] * (Al @ Bc)
+            return float(np.linalg.norm(R) / (np.linalg.norm(Al) * np.linalg.norm(Bc)))
         R = Al @ X - w["alpha"] * Bc
         return float(np.linalg.norm(R) / (np.linalg.norm(Al) * np.linalg.norm(X)))
 
@@ -1087,14 +1097,15 @@ def run_trsm(args, torch, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if p == "d" else "f32",
         "data": "synthetic (seeded uniform[-1,1), diagonal raised by sqrt(m), on the device)",
-        "config": {"workload": args.workload, "side": "L", "uplo": "L", "transa": "N",
+        "config": {"workload": args.workload, "routine": "trmm" if trmm else "trsm",
+                   "side": "L", "uplo": "L", "transa": "N",
                    "diag": "N", "m": m, "n": n, "alpha": w["alpha"], "flops_per_call": "m^2 n",
                    "parallelism": "replicas" if world > 1 else "single"},
         "form": {"name": ("%s updates" if best == 0 else "split updates (%s)") % form_names[best],
                  "ms_by_form": {form_names[f]: round(v, 3) for f, v in ms_by_form.items()}},
         "plain": ({"value": round(flops / (ms_plain / 1e3) / 1e12, 3), "unit": "TFLOP/s",
                    "ms": round(ms_plain, 3)} if ms_plain is not None else None),
-        "accuracy": {"backward_residual": res, "columns": 64},
+        "accuracy": {("relative_error" if trmm else "backward_residual"): res, "columns": 64},
         "clocks": clocks,
         "e2e": {"value": None, "skipped": "device-pointer TRSM API"},
     }
