@@ -481,10 +481,12 @@ def run_ours(args, torch, rank, world):
             dt += time.perf_counter() - t
         dt /= steps_e2e
         esz = 8 if is_d else 4
-        # the pipelined host path (page-locked buffers, k >= 1024, m or n >= 4096)
+        # the pipelined host path (page-locked buffers, k >= 1024, m or n >= 4096;
+        # 2048 for the FP64 CRT form)
         # leaves C in host memory when beta = 0 and every entry of C is finite and
         # non-negative (0 * C = +0): then only A and B cross the link
-        c_moved = not (w["beta"] == 0.0 and k >= 1024 and max(m, n) >= 4096 and
+        c_moved = not (w["beta"] == 0.0 and k >= 1024 and
+                       max(m, n) >= (2048 if form == "crt" else 4096) and
                        bool(torch.isfinite(hC0).all()) and not bool(torch.signbit(hC0).any()))
         h2d = (prob.ar * prob.ac + prob.br * prob.bc + (m * n if c_moved else 0)) * esz
         e2e = {"value": round(prob.flops / dt / 1e12, 3), "unit": "TFLOP/s",

@@ -293,14 +293,19 @@ static void host_c_scan_start(const T *c, int m, int n, int ldc, std::atomic<boo
 // by shape, 1 = no pipeline, P = P row parts of op(A) and P column parts of
 // op(B).
 static int g_host_parts = 0;
-static int host_parts_for(int R, int k, bool pinned) {
+static int host_parts_for(int R, int k, bool pinned, bool fp64) {
   if (g_host_parts) return g_host_parts;
   // four parts of at least 1024 rows / columns once the operands are large
   // enough for the link to matter: measured best of 1-6 parts at SGEMM TN
   // 8192^3 (5.04 ms a call against 5.47 unpipelined) and 16384^3 (23.5 ms
-  // against 30.4).  Pageable memory is moved by SM copies, which compete
-  // with the GEMM for SMs (slower pipelined): no pipeline by default.
-  return pinned && R >= 4096 && k >= 1024 ? 4 : 1;
+  // against 30.4); for the FP64 CRT form two from 2048 (DGEMM NN 2048^3:
+  // 0.787 ms against 1.088 unpipelined, 3 parts 0.788, 4 parts 0.827), not
+  // for the FP32 splits, whose faster blocks leave less to hide (SGEMM TN
+  // 2048^3 / 3072^3: 0.468 / 0.855 ms with two parts against 0.366 / 0.731).
+  // Pageable memory is moved by SM copies, which compete with the GEMM for
+  // SMs (slower pipelined): no pipeline by default.
+  if (!pinned || k < 1024) return 1;
+  return R >= 4096 ? 4 : (fp64 && R >= 2048) ? 2 : 1;
 }
 
 // Boundaries of `parts` parts of [0, R), each starting on a multiple of align.
@@ -339,8 +344,8 @@ static int host_split_pipelined(DeviceState *s, cudaStream_t st, char ta, char t
   const bool an = notrans(ta), bn = notrans(tb);
   const int arows = an ? m : k, acols = an ? k : m;
   const int brows = bn ? k : n, bcols = bn ? n : k;
-  const std::vector<int> rb = part_bounds(m, host_parts_for(m, k, ce), kSplitBM);
-  const std::vector<int> cb = part_bounds(n, host_parts_for(n, k, ce), kBf16xBN);
+  const std::vector<int> rb = part_bounds(m, host_parts_for(m, k, ce, sizeof(T) == 8), kSplitBM);
+  const std::vector<int> cb = part_bounds(n, host_parts_for(n, k, ce, sizeof(T) == 8), kBf16xBN);
   const int P = (int)rb.size() - 1, Q = (int)cb.size() - 1;
   constexpr int epl = 16 / (int)sizeof(T);  // 16-byte aligned columns in HBM
   auto up = [](int r) { return ((r > 1 ? r : 1) + epl - 1) / epl * epl; };
@@ -534,7 +539,8 @@ static int host_gemm(char ta, char tb, int m, int n, int k, T alpha, const T *a,
       // the FP32 split forms and the FP64 CRT form
       const bool pinned = host_pinned(a, b, c);
       if ((form == 1 || form == 3) && need_ab &&
-          (host_parts_for(m, k, pinned) > 1 || host_parts_for(n, k, pinned) > 1))
+          (host_parts_for(m, k, pinned, sizeof(T) == 8) > 1 ||
+           host_parts_for(n, k, pinned, sizeof(T) == 8) > 1))
         return host_split_pipelined<T>(s, st, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c,
                                        ldc, param, pinned);
     }

@@ -433,7 +433,8 @@ void gb300_tune_cache_clear(void);
  *   stream prepares the parts that have arrived and multiplies the C blocks
  *   whose parts are ready, and C blocks go back as they finish.  1 turns
  *   the pipeline off; 0 restores the choice by shape (page-locked buffers: 4
- *   parts per dimension of 4096 or more when k >= 1024; pageable: off).  The
+ *   parts per dimension of 4096 or more, 2 from 2048 for the FP64 CRT form,
+ *   when k >= 1024; pageable: off).  The
  *   results are the same bit for bit.
  *   GB300_TUNE_MODULUS_SPLIT: work units of the CRT form's GEMM
  *   (gb300_dgemm_ozaki2): 1 = whole output tiles, each CTA running all
