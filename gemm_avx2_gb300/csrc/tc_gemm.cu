@@ -574,6 +574,10 @@ constexpr int kBxStagedMaxKBlocks = 48;
 // (rank-256 SGEMM, one box: 8 -> 221.1, 16 -> 237.3, 32 -> 231.9, 64 -> 232.2
 // TFLOP/s).
 constexpr int kCsGroupM = 16;
+// Row-tile pairs in a group of the pair-MMA raster at long K: 16 from 64
+// pairs, else 8 (SGEMM TN 3xFP16, one box, groups of 4 / 8 / 16: 8192^3
+// 505 / 518 / 515 TFLOP/s, 16384^3 493 / 499 / 510).
+__device__ __forceinline__ int pair_group_m(int pairs) { return pairs >= 64 ? 16 : 8; }
 
 // GR: a grouped launch over the problems of p.grp (one CTA per tile; the
 // kernel parameters' maps are unused), each unit a tile of one problem, with
@@ -675,7 +679,7 @@ bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       tile_coords(u - grp[i].unit0, q.tiles_m, q.tiles_n, kSplitGroupM, tm, tn);
     } else {
       int um;
-      tile_coords(u, pm, p.tiles_n, CS ? kCsGroupM : PAIR ? kSplitGroupM / 2 : kSplitGroupM, um,
+      tile_coords(u, pm, p.tiles_n, CS ? kCsGroupM : PAIR ? pair_group_m(pm) : kSplitGroupM, um,
                   tn);
       tm = PAIR ? 2 * um + (int)rank : um;  // PAIR: a row tile past the end is zero-filled, not stored
     }
