@@ -1,4 +1,4 @@
-// trsm.cu -- blocked triangular solve (TRSM) and triangular multiply (TRMM)
+// trsm.cu -- triangular solve (TRSM) and triangular multiply (TRMM)
 // built on this library's GEMM, the BLAS-3 routines that spend most of their
 // time in GEMM updates.  The reference ships TRSM/TRMM only as OpenBLAS-style
 // packed-panel kernels (OpenBLAS-like_implementation/TRSM_KERNEL_*_simplified.c,
@@ -9,11 +9,13 @@
 //   TRMM: side 'L': B = alpha op(A) B,  side 'R': B = alpha B op(A)
 //
 // A is triangular (uplo 'U'/'L', diag 'U' unit / 'N'), op(A) = A or A^T.  Both
-// reduce to passes over 64-wide blocks of the "effective" triangle of op(A)
-// (lower when uplo == 'L' xor op transposes): one small kernel per diagonal
-// block (the triangle in shared memory, one thread per right-hand side) and
-// one GEMM per block for the off-diagonal part -- the plain kernel (form 0) or
-// the tensor-core split form (form 1: Ozaki for FP64, 6xBF16 for FP32).
+// halve the "effective" triangle of op(A) (lower when uplo == 'L' xor op
+// transposes) recursively: one half, one GEMM for the off-diagonal block
+// between the halves, the other half; a range of at most 64 is one small
+// kernel (the 64 x 64 block in shared memory, each right-hand side on a few
+// lanes of a warp).  The GEMMs are the plain kernel (form 0), the tensor-core
+// split form (form 1: Ozaki slices for FP64, 6xBF16 for FP32) or the CRT form
+// (form 2, FP64; FP32 as form 1).
 #include <cuda_runtime.h>
 
 #include <cstdint>
